@@ -1,0 +1,381 @@
+"""ctypes front-end of the CPU oracle (TEST INFRASTRUCTURE ONLY).
+
+Two back-ends with one interface:
+
+* ``PortSystem``: ``oracle/liboracle.so``, the plain-C restatement
+  (``oracle/tsph_oracle.c``), built on any host by ``oracle/Makefile``.
+* ``RefSystem``: ``oracle/_ref/libtsph_ref.so``, the reference's own headers
+  compiled by ``make -C oracle ref`` (only where the reference sources exist).
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import
+this module.  The product never does.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libtsph_ref.so")
+
+F_RX, F_RY, F_VX, F_VY, F_AX, F_AY, F_RHO, F_DRHO, F_P = range(9)
+F_ROX, F_ROY, F_VOX, F_VOY, F_RHO_O = range(9, 14)
+
+_D = C.c_double
+_P = C.c_void_p
+_I = C.c_int
+_DP = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
+_IP = np.ctypeslib.ndpointer(dtype=np.int32, flags="C_CONTIGUOUS")
+
+
+def build_port(force: bool = False) -> str:
+    if force or not os.path.exists(PORT_LIB):
+        subprocess.run(["make", "-s", "-C", HERE, "all"],
+                       check=True)
+    return PORT_LIB
+
+
+def build_ref() -> str | None:
+    """Build the reference harness if the reference sources are present."""
+    ref = os.environ.get("TSPH_REFERENCE", "/root/reference")
+    if not os.path.isdir(os.path.join(ref, "src")):
+        return REF_LIB if os.path.exists(REF_LIB) else None
+    subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref}"], check=True)
+    return REF_LIB
+
+
+def ref_available() -> bool:
+    if not os.path.exists(REF_LIB):
+        return False
+    try:
+        C.CDLL(REF_LIB)
+        return True
+    except OSError:
+        return False
+
+
+_port = None
+_ref = None
+
+
+def _load_port():
+    global _port
+    if _port is None:
+        build_port()
+        L = C.CDLL(PORT_LIB)
+        L.orc_create.restype = _P
+        L.orc_create.argtypes = [_D] * 11
+        L.orc_destroy.argtypes = [_P]
+        L.orc_set_threads.argtypes = [_I]
+        L.orc_get_threads.restype = _I
+        L.orc_add_particle.argtypes = [_P, _I] + [_D] * 8
+        L.orc_add_gnr.argtypes = [_P, _D, _D]
+        L.orc_np.argtypes = [_P]
+        L.orc_np.restype = _I
+        L.orc_grid.argtypes = [_P, C.POINTER(_I), C.POINTER(_I)]
+        L.orc_const.argtypes = [_P, _I]
+        L.orc_const.restype = _D
+        L.orc_get_field.argtypes = [_P, _I, _DP]
+        L.orc_set_field.argtypes = [_P, _I, _DP]
+        L.orc_get_meta.argtypes = [_P, _IP, _IP]
+        L.orc_get_cells.argtypes = [_P, _IP, _IP]
+        L.orc_get_cells.restype = _I
+        for f in ("orc_divide_to_cells", "orc_clear_cells", "orc_particle_to_cell",
+                  "orc_density_to_pressure", "orc_mdbc_density"):
+            getattr(L, f).argtypes = [_P]
+        L.orc_compute_forces.argtypes = [_P, _I]
+        L.orc_predictor.argtypes = [_P, _D]
+        L.orc_corrector.argtypes = [_P, _D]
+        L.orc_remove_out_of_domain.argtypes = [_P]
+        L.orc_remove_out_of_domain.restype = _I
+        L.orc_step.argtypes = [_P, _I, _D, _I]
+        L.orc_wendland.argtypes = [_D, _D, C.POINTER(_D), C.POINTER(_D)]
+        L.orc_pressure.argtypes = [_D, _D, _D]
+        L.orc_pressure.restype = _D
+        L.orc_pressure_to_density.argtypes = [_D, _D, _D]
+        L.orc_pressure_to_density.restype = _D
+        _port = L
+    return _port
+
+
+def _load_ref():
+    global _ref
+    if _ref is None:
+        L = C.CDLL(REF_LIB)
+        L.ref_create.restype = _P
+        L.ref_create.argtypes = [_D] * 11
+        L.ref_destroy.argtypes = [_P]
+        L.ref_set_threads.argtypes = [_I]
+        L.ref_add_particle.argtypes = [_P, _I] + [_D] * 6
+        L.ref_add_gnr.argtypes = [_P, _D, _D]
+        L.ref_create_block_of_fluid.argtypes = [_P] + [_D] * 4
+        L.ref_create_block_of_fluid_wp.argtypes = [_P] + [_D] * 4
+        L.ref_create_wall_x_mdbc.argtypes = [_P, _D, _D, _D, _I, _D]
+        L.ref_create_wall_y_mdbc.argtypes = [_P, _D, _D, _D, _I, _D]
+        L.ref_create_corner_mdbc.argtypes = [_P, _I, _I, _D, _D]
+        L.ref_create_wall_x.argtypes = [_P, _D, _D, _D, _I]
+        L.ref_create_wall_y.argtypes = [_P, _D, _D, _D, _I]
+        L.ref_np.argtypes = [_P]
+        L.ref_np.restype = _I
+        L.ref_grid.argtypes = [_P, C.POINTER(_I), C.POINTER(_I)]
+        L.ref_get_state.argtypes = [_P] + [_P] * 8
+        L.ref_set_state.argtypes = [_P] + [_P] * 6
+        L.ref_get_gnr.argtypes = [_P, _DP]
+        L.ref_ngnr.argtypes = [_P]
+        L.ref_ngnr.restype = _I
+        L.ref_get_cells.argtypes = [_P, _P, _P]
+        L.ref_get_cells.restype = _I
+        for f in ("ref_divide_to_cells", "ref_clear_cells", "ref_particle_to_cell",
+                  "ref_density_to_pressure", "ref_mdbc_density",
+                  "ref_remove_out_of_domain"):
+            getattr(L, f).argtypes = [_P]
+        L.ref_compute_forces.argtypes = [_P, _I]
+        L.ref_predictor.argtypes = [_P, _D]
+        L.ref_corrector.argtypes = [_P, _D]
+        L.ref_step.argtypes = [_P, _I, _D, _I]
+        _ref = L
+    return _ref
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class _Base:
+    """Common state accessors; ``state()`` returns the reference-order fields."""
+
+    def ncells(self):
+        ncx, ncy = self.grid()
+        return ncx * ncy
+
+
+class PortSystem(_Base):
+    """The plain-C oracle."""
+
+    def __init__(self, h, kap, cs, rho0, visco, delta, dp, domain):
+        self.L = _load_port()
+        self.s = self.L.orc_create(h, kap, cs, rho0, visco, delta, dp, *domain)
+
+    @classmethod
+    def from_case(cls, case, divide=True):
+        o = cls(case.h, case.kap, case.cs, case.rho0, case.visco, case.delta, case.dp,
+                case.domain)
+        ps = case.particles
+        for i in range(ps.np):
+            o.L.orc_add_particle(o.s, ps.type[i], ps.p[i], ps.rho[i], ps.rx[i], ps.ry[i],
+                                 ps.vx[i], ps.vy[i], 0.0, 0.0)
+        for g in ps.gnr:
+            o.L.orc_add_gnr(o.s, g[0], g[1])
+        if divide:
+            o.divide_to_cells()
+            o.particle_to_cell()
+        return o
+
+    def __del__(self):
+        try:
+            self.L.orc_destroy(self.s)
+        except Exception:
+            pass
+
+    @staticmethod
+    def set_threads(n):
+        _load_port().orc_set_threads(int(n))
+
+    @staticmethod
+    def get_threads():
+        return _load_port().orc_get_threads()
+
+    def np(self):
+        return self.L.orc_np(self.s)
+
+    def grid(self):
+        a, b = _I(), _I()
+        self.L.orc_grid(self.s, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def const(self, which):
+        return self.L.orc_const(self.s, which)
+
+    def field(self, f):
+        out = np.empty(self.np(), dtype=np.float64)
+        self.L.orc_get_field(self.s, f, out)
+        return out
+
+    def set_field(self, f, arr):
+        a = np.ascontiguousarray(arr, dtype=np.float64)
+        assert a.shape == (self.np(),)
+        self.L.orc_set_field(self.s, f, a)
+
+    def state(self):
+        n = self.np()
+        idx = np.empty(n, dtype=np.int32)
+        typ = np.empty(n, dtype=np.int32)
+        self.L.orc_get_meta(self.s, idx, typ)
+        g = self.field
+        return dict(r=np.stack([g(F_RX), g(F_RY)], 1), v=np.stack([g(F_VX), g(F_VY)], 1),
+                    a=np.stack([g(F_AX), g(F_AY)], 1), rho=g(F_RHO), drho=g(F_DRHO),
+                    p=g(F_P), index=idx, type=typ)
+
+    def set_state(self, r=None, v=None, a=None, rho=None, drho=None, p=None):
+        if r is not None:
+            self.set_field(F_RX, r[:, 0]); self.set_field(F_RY, r[:, 1])
+        if v is not None:
+            self.set_field(F_VX, v[:, 0]); self.set_field(F_VY, v[:, 1])
+        if a is not None:
+            self.set_field(F_AX, a[:, 0]); self.set_field(F_AY, a[:, 1])
+        if rho is not None:
+            self.set_field(F_RHO, rho)
+        if drho is not None:
+            self.set_field(F_DRHO, drho)
+        if p is not None:
+            self.set_field(F_P, p)
+
+    def cells(self):
+        nc = self.ncells()
+        start = np.empty(nc + 1, dtype=np.int32)
+        lst = np.empty(max(self.np(), 1), dtype=np.int32)
+        n = self.L.orc_get_cells(self.s, start, lst)
+        if n < 0:
+            raise RuntimeError("cells not built")
+        return start, lst[:n]
+
+    def divide_to_cells(self):
+        self.L.orc_divide_to_cells(self.s)
+
+    def clear_cells(self):
+        self.L.orc_clear_cells(self.s)
+
+    def particle_to_cell(self):
+        self.L.orc_particle_to_cell(self.s)
+
+    def density_to_pressure(self):
+        self.L.orc_density_to_pressure(self.s)
+
+    def compute_forces(self, model):
+        self.L.orc_compute_forces(self.s, int(model))
+
+    def mdbc_density(self):
+        self.L.orc_mdbc_density(self.s)
+
+    def predictor(self, dt):
+        self.L.orc_predictor(self.s, dt)
+
+    def corrector(self, dt):
+        self.L.orc_corrector(self.s, dt)
+
+    def remove_out_of_domain(self):
+        return self.L.orc_remove_out_of_domain(self.s)
+
+    def step(self, model, dt, n=1):
+        self.L.orc_step(self.s, int(model), dt, int(n))
+
+
+class RefSystem(_Base):
+    """The reference's own code (oracle/_ref/libtsph_ref.so)."""
+
+    def __init__(self, h, kap, cs, rho0, visco, delta, dp, domain):
+        self.L = _load_ref()
+        self.s = self.L.ref_create(h, kap, cs, rho0, visco, delta, dp, *domain)
+
+    @classmethod
+    def from_case(cls, case, divide=True):
+        o = cls(case.h, case.kap, case.cs, case.rho0, case.visco, case.delta, case.dp,
+                case.domain)
+        ps = case.particles
+        for i in range(ps.np):
+            o.L.ref_add_particle(o.s, ps.type[i], ps.p[i], ps.rho[i], ps.rx[i], ps.ry[i],
+                                 ps.vx[i], ps.vy[i])
+        for g in ps.gnr:
+            o.L.ref_add_gnr(o.s, g[0], g[1])
+        if divide:
+            o.divide_to_cells()
+            o.particle_to_cell()
+        return o
+
+    def __del__(self):
+        try:
+            self.L.ref_destroy(self.s)
+        except Exception:
+            pass
+
+    @staticmethod
+    def set_threads(n):
+        _load_ref().ref_set_threads(int(n))
+
+    def np(self):
+        return self.L.ref_np(self.s)
+
+    def grid(self):
+        a, b = _I(), _I()
+        self.L.ref_grid(self.s, C.byref(a), C.byref(b))
+        return a.value, b.value
+
+    def state(self):
+        n = self.np()
+        r = np.empty((n, 2)); v = np.empty((n, 2)); a = np.empty((n, 2))
+        rho = np.empty(n); drho = np.empty(n); p = np.empty(n)
+        idx = np.empty(n, dtype=np.int32); typ = np.empty(n, dtype=np.int32)
+        self.L.ref_get_state(self.s, _ptr(r), _ptr(v), _ptr(a), _ptr(rho), _ptr(drho),
+                             _ptr(p), _ptr(idx), _ptr(typ))
+        return dict(r=r, v=v, a=a, rho=rho, drho=drho, p=p, index=idx, type=typ)
+
+    def set_state(self, r=None, v=None, a=None, rho=None, drho=None, p=None):
+        c = lambda x, shp: None if x is None else np.ascontiguousarray(x, dtype=np.float64)
+        r, v, a = c(r, 2), c(v, 2), c(a, 2)
+        rho, drho, p = c(rho, 1), c(drho, 1), c(p, 1)
+        self.L.ref_set_state(self.s, _ptr(r), _ptr(v), _ptr(a), _ptr(rho), _ptr(drho),
+                             _ptr(p))
+
+    def gnr(self):
+        out = np.empty((self.L.ref_ngnr(self.s), 2))
+        self.L.ref_get_gnr(self.s, out.reshape(-1))
+        return out
+
+    def cells(self):
+        nc = self.ncells()
+        start = np.empty(nc + 1, dtype=np.int32)
+        lst = np.empty(max(self.np(), 1), dtype=np.int32)
+        n = self.L.ref_get_cells(self.s, _ptr(start), _ptr(lst))
+        return start, lst[:n]
+
+    def divide_to_cells(self):
+        self.L.ref_divide_to_cells(self.s)
+
+    def clear_cells(self):
+        self.L.ref_clear_cells(self.s)
+
+    def particle_to_cell(self):
+        self.L.ref_particle_to_cell(self.s)
+
+    def density_to_pressure(self):
+        self.L.ref_density_to_pressure(self.s)
+
+    def compute_forces(self, model):
+        self.L.ref_compute_forces(self.s, int(model))
+
+    def mdbc_density(self):
+        self.L.ref_mdbc_density(self.s)
+
+    def predictor(self, dt):
+        self.L.ref_predictor(self.s, dt)
+
+    def corrector(self, dt):
+        self.L.ref_corrector(self.s, dt)
+
+    def remove_out_of_domain(self):
+        self.L.ref_remove_out_of_domain(self.s)
+
+    def step(self, model, dt, n=1):
+        self.L.ref_step(self.s, int(model), dt, int(n))
+
+
+def wendland(r, h):
+    L = _load_port()
+    w, f = _D(), _D()
+    L.orc_wendland(r, h, C.byref(w), C.byref(f))
+    return w.value, f.value

@@ -1,0 +1,81 @@
+/*
+ * tsph_oracle.h -- CPU oracle for the 2D WCSPH time step (TEST INFRASTRUCTURE).
+ *
+ * This is the checker, not the product: only the tests, the smoke check and
+ * the CPU-baseline leg of bench.py may load it.  It restates, in plain C and
+ * IEEE double precision, the reference (tomashalada/tinySPH_old, header-only
+ * C++) functions on the time-step path, in the same floating-point operation
+ * order, so that with one thread its results are bit-identical to the
+ * reference compiled from its own sources (see oracle/ref_harness.cpp and
+ * tests/golden/).  Each function cites the reference file:line it follows.
+ *
+ * State is kept in the reference's own particle order (array index = the
+ * reference's particle index, erase-preserving), as structure-of-arrays.
+ */
+#ifndef TSPH_ORACLE_H
+#define TSPH_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct orc_sys orc_sys;
+
+/* wall models of Compute_Forces */
+#define ORC_MDBC 0   /* src/SPH_interaction.h     */
+#define ORC_DBC 1    /* src/SPH_interactionDBC.h  */
+
+/* particle types, src/SPH_defs.h:44-48 */
+#define ORC_FLUID 0
+#define ORC_WALL 1
+
+/* state field ids for orc_get_field / orc_set_field */
+enum {
+    ORC_F_RX = 0, ORC_F_RY, ORC_F_VX, ORC_F_VY, ORC_F_AX, ORC_F_AY,
+    ORC_F_RHO, ORC_F_DRHO, ORC_F_P,
+    ORC_F_ROX, ORC_F_ROY, ORC_F_VOX, ORC_F_VOY, ORC_F_RHO_O,
+    ORC_F_NFIELDS
+};
+
+orc_sys *orc_create(double h, double kap, double cs, double rho0, double visco,
+                    double delta, double dp, double x0, double xm, double y0,
+                    double ym);
+void orc_destroy(orc_sys *s);
+void orc_set_threads(int n);
+int orc_get_threads(void);
+
+void orc_add_particle(orc_sys *s, int type, double p, double rho, double rx,
+                      double ry, double vx, double vy, double ax, double ay);
+void orc_add_gnr(orc_sys *s, double gx, double gy);
+
+int orc_np(const orc_sys *s);
+void orc_grid(const orc_sys *s, int *ncx, int *ncy);
+double orc_const(const orc_sys *s, int which); /* 0 h,1 kap,2 dp,3 cs,4 rho0,5 avisc,6 delta,7 m,8 g */
+
+void orc_get_field(const orc_sys *s, int field, double *out);
+void orc_set_field(orc_sys *s, int field, const double *in);
+void orc_get_meta(const orc_sys *s, int *index, int *type);
+int orc_get_cells(const orc_sys *s, int *cell_start, int *cell_list);
+
+/* the reference entry points */
+void orc_divide_to_cells(orc_sys *s);
+void orc_clear_cells(orc_sys *s);
+void orc_particle_to_cell(orc_sys *s);
+void orc_density_to_pressure(orc_sys *s);
+void orc_compute_forces(orc_sys *s, int model);
+void orc_mdbc_density(orc_sys *s);
+void orc_predictor(orc_sys *s, double dt);
+void orc_corrector(orc_sys *s, double dt);
+int orc_remove_out_of_domain(orc_sys *s);
+/* one RUN-loop body per step (mDBC or DBC case driver order) */
+void orc_step(orc_sys *s, int model, double dt, int nsteps);
+
+/* scalar kernels, exported for unit tests */
+void orc_wendland(double r, double h, double *w, double *f);
+double orc_pressure(double rho, double rho0, double c0);
+double orc_pressure_to_density(double p, double rho0, double c0);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,148 @@
+"""Case builders: the dam break with mDBC walls and the still-water tank with
+DBC walls, with the constants of the reference's case drivers.
+
+A case is a :class:`Case`: particles in the reference's order, the SPH
+constants of ``SPH_constants`` (``src/SPH_data.h:124-140``), the padded domain
+of ``Simulation_data`` (``src/SPH_data.h:205-219``, padded as in
+``PREP_SIMULATION_DATA``, e.g. ``cases/damBreakLong_mDBC/
+SPH_simulationSymplectic.h:206-221``), the wall model and the time step.
+"""
+
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import geometry as geo
+
+WALL_MDBC = 0
+WALL_DBC = 1
+
+
+@dataclass
+class Case:
+    name: str
+    particles: geo.ParticleSet
+    h: float
+    kap: float
+    cs: float
+    rho0: float
+    visco: float
+    delta: float
+    dp: float
+    domain: tuple  # padded (x_0, x_m, y_0, y_m)
+    wall_model: int
+    dt: float
+    meta: dict = field(default_factory=dict)
+
+    @property
+    def np(self) -> int:
+        return self.particles.np
+
+    def constants(self):
+        return dict(h=self.h, kap=self.kap, cs=self.cs, rho0=self.rho0,
+                    visco=self.visco, delta=self.delta, dp=self.dp)
+
+
+def _pad(x_0, x_1, y_0, y_1, nvl, dp):
+    # PREP_SIMULATION_DATA: x_0 -= nvl*dp etc.
+    return (x_0 - nvl * dp, x_1 + nvl * dp, y_0 - nvl * dp, y_1 + nvl * dp)
+
+
+def dam_break_mdbc(dp: float = 0.005, cs: float = 34.3, wall_height: float = 1.0,
+                   tank_length: float = 1.61, column=(0.6, 0.3),
+                   dt: float | None = None) -> Case:
+    """Dam break with mDBC walls: ``cases/damBreakLong_mDBC/constants.h`` and
+    ``geometry.h:9-23``.
+
+    Reference values: dp = 0.005, h = sqrt(2 dp^2) (constants.h:17), kap = 2.1,
+    cs = 34.3 (constants.h:26), visco = 0.02, delta = 0.1, dt = 5e-5
+    (constants.h:21), walls up to y = 1.0 m, domain [0, 2] x [0, 1].  The
+    benchmark configuration uses cs = 35, walls to 0.8 m and dt scaled with dp
+    (dt = 5e-5 * dp / 0.005).
+    """
+    x_0, x_1, y_0, y_1 = 0.0, 2.0, 0.0, 1.0
+    kap = 2.1
+    hh = 1.0 * math.sqrt(2 * dp * dp)
+    if dt is None:
+        dt = 0.00005 * (dp / 0.005)
+    nvl = int(math.ceil(kap * hh / dp))
+    ps = geo.ParticleSet(dp, hh, kap, cs)
+    L = tank_length
+    geo.create_wall_x_mdbc(ps, 0.0 + dp, L, 0.0, -1, dp / 2)
+    geo.create_wall_y_mdbc(ps, 0.0, 0 + dp, wall_height, -1, dp / 2)
+    geo.create_wall_y_mdbc(ps, L, 0 + dp, wall_height, +1, L - dp / 2)
+    geo.create_corner_mdbc(ps, -1, -1, (0.0 + dp / 2, 0.0 + dp / 2))
+    geo.create_corner_mdbc(ps, +1, -1, (L - dp / 2, 0.0 + dp / 2))
+    geo.create_block_of_fluid(ps, 0 + dp, 0 + dp, column[0], column[1])
+    return Case(name=f"dam_break_mdbc_dp{dp:g}", particles=ps, h=hh, kap=kap, cs=cs,
+                rho0=1000.0, visco=0.02, delta=0.1, dp=dp,
+                domain=_pad(x_0, x_1, y_0, y_1, nvl, dp), wall_model=WALL_MDBC,
+                dt=dt, meta=dict(nvl=nvl, wall_height=wall_height, tank_length=L,
+                                 column=tuple(column)))
+
+
+def still_water_dbc(dp: float = 0.005, width: float = 0.5, depth: float = 0.3,
+                    tank_height: float = 0.4, cs: float = 20.0, visco: float = 0.02,
+                    delta: float = 0.1, layers: int = 3,
+                    hydrostatic: bool = True) -> Case:
+    """Still water in a tank with dynamic (DBC) walls.
+
+    Water ``width`` x ``depth`` on a regular lattice at (i + 1/2) dp, filling
+    the tank's interior width, ``layers`` layers of wall particles below and on
+    both sides up to ``tank_height``; h = 1.5 dp, kap = 2.1, dt = 0.2 h / cs.
+    Initial fluid state is hydrostatic (``Create_Block_of_FluidWP``,
+    src/SPH_create.h:689-727: p = 9.81 (H - y) 1000, rho from the inverse EOS);
+    wall particles get the hydrostatic value of their depth (rho0 above the
+    free surface).  The pair loop is the DBC flavour
+    (``src/SPH_interactionDBC.h``).
+    """
+    kap = 2.1
+    hh = 1.5 * dp
+    dt = 0.2 * hh / cs
+    ps = geo.ParticleSet(dp, hh, kap, cs)
+    nx = int(round(width / dp))
+    ny = int(round(depth / dp))
+    nyw = int(round(tank_height / dp))
+
+    def hydro(y):
+        if not hydrostatic or y >= depth:
+            return 0.0, 1000.0
+        p = 9.81 * (depth - y) * 1000
+        return p, geo.pressure_to_density(p, 1000.0, cs)
+
+    # walls first (bottom layers incl. corners, then the two sides)
+    for l in range(layers):
+        y = -(l + 0.5) * dp
+        for i in range(-layers, nx + layers):
+            x = (i + 0.5) * dp
+            p, r = hydro(y)
+            ps.add(geo.WALL, p, r, (x, y))
+    for side in (0, 1):
+        for l in range(layers):
+            x = -(l + 0.5) * dp if side == 0 else width + (l + 0.5) * dp
+            for j in range(nyw):
+                y = (j + 0.5) * dp
+                p, r = hydro(y)
+                ps.add(geo.WALL, p, r, (x, y))
+    for i in range(nx):
+        x = (i + 0.5) * dp
+        for j in range(ny):
+            y = (j + 0.5) * dp
+            p, r = hydro(y)
+            ps.add(geo.FLUID, p, r, (x, y))
+    pad = (layers + 2) * dp
+    domain = (0.0 - pad, width + pad, 0.0 - pad, tank_height + pad)
+    return Case(name=f"still_water_dbc_dp{dp:g}", particles=ps, h=hh, kap=kap, cs=cs,
+                rho0=1000.0, visco=visco, delta=delta, dp=dp, domain=domain,
+                wall_model=WALL_DBC, dt=dt,
+                meta=dict(width=width, depth=depth, tank_height=tank_height,
+                          layers=layers, nfluid=nx * ny))
+
+
+def dam_break_benchmark(dp: float = 0.0005) -> Case:
+    """The benchmark dam break: tank 1.61 x 0.8 m, column 0.6 x 0.3 m, mDBC,
+    cs = 35 m/s, delta = 0.1, dt = 5e-5 * dp / 0.005 (about 0.24 h / cs)."""
+    return dam_break_mdbc(dp=dp, cs=35.0, wall_height=0.8)
