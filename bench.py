@@ -1,0 +1,362 @@
+"""Benchmark: particle-steps/s of the plain GPU WCSPH step on the 720k-particle
+mDBC dam break (tank 1.61 x 0.8 m, column 0.6 x 0.3 m, dp = 0.0005 m, c0 = 35,
+delta = 0.1, FP32 pair math with FP64 positions) on one GB300.
+
+One bench step = one SPH time step (one body of the reference's RUN loop:
+mDBC, predictor, rebuild, forces + corrector, rebuild, forces), replayed from
+a CUDA graph through the C ABI.  Prints one JSON line (see README of the
+driver contract): value (state resident in HBM), e2e (host buffers through
+the C ABI: upload, re-bin, step, download per step), roofline of the pair
+kernel, cpu_baseline (the CPU oracle on the host cores) and clocks.
+
+``--impl reference`` times the reference's CPU algorithm on the same workload
+instead (the oracle restatement, all host cores; the reference sources are
+not present on the GPU host).
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+PAIR_BYTES_PER_PARTICLE = 80.0   # mean algorithmic bytes of the two pair launches / particle
+STEP_BYTES_PER_PARTICLE = 344.0  # algorithmic bytes per particle-step (byte model)
+METRIC = "particle-steps/s, 720k dam break, 1 GB300: surrogate/batched vs plain, <=1% front err"
+
+
+def _env_int(k, d):
+    try:
+        return int(os.environ.get(k, d))
+    except ValueError:
+        return d
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """dram bytes per launch of the pair kernel from the committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", "k_fluid_pairs_dam_break_720k.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch_fullsize:"):
+            try:
+                return float(line.split(":", 1)[1].split()[0])
+            except ValueError:
+                return None
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index=0):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, smax, reasons = [], 0.0, set()
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = max(smax, float(parts[2]))
+            except ValueError:
+                continue
+            for name, val in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                  "sw_power_cap"), parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_rate(case, steps, threads):
+    """Particle-steps/s of the CPU oracle (the reference's algorithm in C,
+    OpenMP, FP64) over `steps` full time steps of `case`."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    P = oracle.PortSystem.from_case(case)
+    P.set_threads(threads)
+    P.step(case.wall_model, case.dt, 1)  # warm-up
+    t0 = time.perf_counter()
+    P.step(case.wall_model, case.dt, steps)
+    dt = time.perf_counter() - t0
+    return P.np() * steps / dt, dt
+
+
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def run_reference(args, rank, world):
+    """The reference arm: the CPU restatement of the reference's step on all
+    host cores, on the same workload.  Rank 0 only."""
+    if rank != 0:
+        return
+    from tinysph_old_gb300 import cases
+
+    case = cases.dam_break_benchmark(args.dp)
+    threads = host_threads()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    P = oracle.PortSystem.from_case(case)
+    P.set_threads(threads)
+    for _ in range(args.warmup):
+        P.step(case.wall_model, case.dt, 1)
+    # bounded: at most ~150 s of timed CPU work
+    times = []
+    budget = 150.0
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        P.step(case.wall_model, case.dt, 1)
+        times.append(time.perf_counter() - t0)
+        if sum(times) > budget:
+            break
+    total = sum(times)
+    n = P.np()
+    value = n * len(times) / total
+    line = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": len(times), "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (dam-break lattice built by the reference's generators)",
+        "impl": "reference",
+        "config": {"workload": f"mDBC dam break dp={args.dp}, {n} particles (plain WCSPH step)",
+                   "particles": n, "dp": args.dp, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads,
+                         "kind": "port",
+                         "sample": f"{len(times)} full time steps of the {n}-particle case"},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=300)
+    ap.add_argument("--warmup", type=int, default=20)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--dp", type=float, default=0.0005)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
+    ap.add_argument("--e2e-steps", type=int, default=30)
+    ap.add_argument("--cpu-steps", type=int, default=0,
+                    help="CPU baseline sample (0 = auto, ~10-30 s)")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    rank = _env_int("RANK", 0)
+    world = _env_int("WORLD_SIZE", 1)
+    local = _env_int("LOCAL_RANK", 0)
+
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+
+    import numpy as np
+    import torch
+
+    from tinysph_old_gb300 import cases, sph
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    case = cases.dam_break_benchmark(args.dp)
+    stream = torch.cuda.Stream()
+    s = sph.ParticleSystem(case.h, case.kap, case.cs, case.rho0, case.visco, case.delta,
+                           case.dp, case.domain, args.precision, stream=stream.cuda_stream)
+    a = case.particles.arrays()
+    gnr = np.zeros((case.np, 2))
+    gnr[:len(a["gnr"])] = a["gnr"]
+    s.add_particles(a["type"], a["r"], a["v"], a["rho"], a["p"], gnr)
+    s.divide_to_cells()
+    s.particle_to_cell()
+    n = s.np
+    model = case.wall_model
+    dt = case.dt
+
+    # ---- warm-up (also captures the CUDA graph)
+    for _ in range(args.warmup):
+        s.step(model, dt, 1)
+    s.sync()
+
+    # ---- timed: one step per event pair, L2 flushed (256 MB write) in between
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t_wall0 = time.perf_counter()
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.zero_()
+                starts[k].record(stream)
+                s.step(model, dt, 1)
+                ends[k].record(stream)
+        stream.synchronize()
+        t_wall = time.perf_counter() - t_wall0
+    torch.cuda.synchronize()
+    ms = sum(starts[k].elapsed_time(ends[k]) for k in range(args.steps))
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        if dist:
+            dist.barrier()
+        ms = float(t.item())
+    value = world * n * args.steps / (ms / 1000.0)
+    health = s.health()
+
+    # ---- per-kernel timing for the roofline (eager launches with events)
+    s.set_profiling(True)
+    s.profile(reset=True)
+    prof_steps = 5
+    s.step(model, dt, prof_steps)
+    prof = s.profile(reset=True)
+    s.set_profiling(False)
+    launches_per_step = (prof["pair_launches"] + prof["sort_launches"] + prof["mdbc_launches"]
+                         + prof["other_launches"] - 1) / prof_steps  # minus the trailing EOS
+    pair_avg_us = prof["pair_us"] / max(prof["pair_launches"], 1)
+    nfluid = int(np.sum(a["type"] == 0))
+    peak, peak_kind = measured_peaks()
+    achieved = PAIR_BYTES_PER_PARTICLE * nfluid / (pair_avg_us * 1e-6) / 1e9
+    traffic = profile_traffic()
+
+    # ---- e2e through the C ABI with pinned host buffers
+    hr = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+    hv = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+    hrho = torch.empty((n,), dtype=torch.float64, pin_memory=True)
+    mask = sph.F_R | sph.F_V | sph.F_RHO
+    s.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+    for _ in range(2):  # warm
+        s.upload_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+        s.particle_to_cell()
+        s.step(model, dt, 1)
+        s.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        s.upload_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+        s.particle_to_cell()
+        s.step(model, dt, 1)
+        s.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+    e2e_s = time.perf_counter() - t0
+    e2e_value = world * n * args.e2e_steps / e2e_s
+    xfer = n * (16 + 16 + 8)
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        threads = host_threads()
+        steps = args.cpu_steps
+        if steps <= 0:
+            r1, t1 = cpu_rate(case, 1, threads)
+            steps = max(1, min(30, int(15.0 / max(t1, 1e-3))))
+            rate, tt = cpu_rate(case, steps, threads)
+        else:
+            rate, tt = cpu_rate(case, steps, threads)
+        cpu = {"value": rate, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+               "sample": f"{steps} full time steps of the same {n}-particle case "
+                         f"({tt:.1f} s, FP64 C restatement of the reference, OpenMP)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 pair math, f64 positions" if args.precision == "fp32" else "f64",
+            "data": "synthetic (dam-break lattice built like the reference's generators)",
+            "config": {"workload": f"mDBC dam break dp={args.dp}, {n} particles "
+                                   f"({nfluid} fluid), plain WCSPH step",
+                       "particles": n, "fluid": nfluid, "dp": args.dp,
+                       "l2": "flushed (256 MB write) between timed steps",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": "particle-steps/s",
+                    "h2d_bytes_per_step": xfer, "d2h_bytes_per_step": xfer,
+                    "path": "tsph_upload(r,v,rho) + tsph_particle_to_cell + tsph_step(1) + "
+                            "tsph_download(r,v,rho), pinned host buffers"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_fluid_pairs (forces + corrector / forces)",
+                         "bytes_per_unit": PAIR_BYTES_PER_PARTICLE, "unit_count": nfluid,
+                         "avg_launch_us": pair_avg_us, "peak_kind": peak_kind},
+            "step_roofline": {"bytes_per_particle_step": STEP_BYTES_PER_PARTICLE,
+                              "achieved_gbs": STEP_BYTES_PER_PARTICLE * value / world / 1e9,
+                              "frac": STEP_BYTES_PER_PARTICLE * value / world / 1e9 / peak},
+            "kernel_us_per_step": {k: prof[k] / prof_steps for k in
+                                   ("pair_us", "sort_us", "mdbc_us", "other_us")},
+            "gpu_launches": int(round(launches_per_step * args.steps)),
+            "clocks": clocks.summary(),
+            "health": health,
+            "wall_s_timed": t_wall,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,214 @@
+/*
+ * tsph.h -- C ABI of the GB300 (sm_103a) 2D weakly-compressible SPH step.
+ *
+ * A drop-in for the time-step path of tomashalada/tinySPH_old: the particle
+ * system, the cell-list pair search, the WCSPH continuity/momentum pair loop
+ * with delta-SPH (Fourtakas) diffusion and artificial viscosity, the DBC and
+ * mDBC wall models and the symplectic integrator.  Every entry point below
+ * names the reference function it replaces (file:line within the reference
+ * project).  Plain C types only; the library owns its device memory.
+ *
+ * Conventions
+ *  - Every call returns an int status: TSPH_OK (0) or a TSPH_ERR_* code.
+ *    tsph_last_error() gives a message for the calling thread.
+ *  - Host arrays are in the reference's particle order: ascending particle
+ *    index among live particles (the reference erases removed particles
+ *    without reordering, src/SPH_particle_system.h:110-146).  Vectors are
+ *    interleaved (x0, y0, x1, y1, ...), doubles, like std::vector<tdouble2>.
+ *  - One CUDA stream per system; calls on one handle are not thread-safe.
+ *  - Walls are static: the reference's integrators move a wall particle by
+ *    v*dt with v = 0 (its pair loops never give walls an acceleration), so
+ *    wall particles are binned once and kept out of the per-step sort.
+ */
+#ifndef TSPH_H
+#define TSPH_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TSPH_ABI_VERSION 1
+
+/* ---- status codes ---- */
+enum {
+    TSPH_OK = 0,
+    TSPH_ERR_ARG = 1,           /* bad argument (null, size, type, range)      */
+    TSPH_ERR_CUDA = 2,          /* a CUDA runtime call failed                   */
+    TSPH_ERR_STATE = 3,         /* call out of order (e.g. cells not built)     */
+    TSPH_ERR_NOMEM = 4,         /* device or host allocation failed             */
+    TSPH_ERR_NUMERIC = 5,       /* NaN/Inf found in the state                   */
+    TSPH_ERR_DENSITY = 6,       /* density outside [0, 1500] (the reference's
+                                   warning range, src/SPH_pressure.h:76-80)     */
+    TSPH_ERR_ESCAPED = 7,       /* a particle left the cell grid                */
+    TSPH_ERR_UNSUPPORTED = 8    /* feature outside this build's scope           */
+};
+
+/* health flags accumulated on the device (tsph_health) */
+#define TSPH_HEALTH_NAN 0x1u
+#define TSPH_HEALTH_DENSITY 0x2u
+#define TSPH_HEALTH_ESCAPED 0x4u
+#define TSPH_HEALTH_REMOVED 0x8u
+
+/* particle types, src/SPH_defs.h:44-48 (fluid = 0, wall = 1) */
+enum { TSPH_FLUID = 0, TSPH_WALL = 1 };
+
+/* wall models: Compute_Forces of src/SPH_interaction.h (mDBC: fluid rows only,
+ * wall density from ghost nodes) and src/SPH_interactionDBC.h (DBC: walls get
+ * a density rate from fluid neighbours) */
+enum { TSPH_WALL_MDBC = 0, TSPH_WALL_DBC = 1 };
+
+/* arithmetic of the pair/integration kernels: FP32 pair math with FP64
+ * positions (the production build), or FP64 throughout (the error study) */
+enum { TSPH_PREC_FP32 = 0, TSPH_PREC_FP64 = 1 };
+
+/* fields for tsph_download / tsph_upload (bit mask) */
+enum {
+    TSPH_F_R = 1 << 0,      /* double[2n] position            data.r    */
+    TSPH_F_V = 1 << 1,      /* double[2n] velocity            data.v    */
+    TSPH_F_A = 1 << 2,      /* double[2n] acceleration        data.a    */
+    TSPH_F_RHO = 1 << 3,    /* double[n]  density             data.rho  */
+    TSPH_F_DRHO = 1 << 4,   /* double[n]  density rate        data.drho */
+    TSPH_F_P = 1 << 5,      /* double[n]  pressure            data.p    */
+    TSPH_F_INDEX = 1 << 6,  /* int32[n]   original index      data.index     */
+    TSPH_F_TYPE = 1 << 7    /* int32[n]   particle type       data.part_type */
+};
+
+/* SPH_constants, src/SPH_data.h:124-140; filled like the Particle_system
+ * constructor (src/SPH_particle_system.h:191-212): gravity (0, 9.81) and
+ * m = rho0 / (1/dp * 1/dp) are derived, not passed. */
+typedef struct {
+    double h;      /* smoothing length                       */
+    double kap;    /* kernel support coefficient (kh = kap h) */
+    double cs;     /* numerical speed of sound c0             */
+    double rho0;   /* reference density                       */
+    double visco;  /* artificial-viscosity alpha              */
+    double delta;  /* delta-SPH coefficient                   */
+    double dp;     /* initial particle spacing                */
+} tsph_constants;
+
+/* Simulation_data, src/SPH_data.h:205-219: the (padded) domain box */
+typedef struct {
+    double x_0, x_m, y_0, y_m;
+} tsph_domain;
+
+/* Host view of the particle state; any pointer may be NULL. */
+typedef struct {
+    double *r, *v, *a, *rho, *drho, *p;
+    int32_t *index, *type;
+} tsph_host_state;
+
+typedef struct tsph_system tsph_system;
+
+/* ---- library ---- */
+int tsph_abi_version(void);
+const char *tsph_last_error(void);
+const char *tsph_status_string(int status);
+/* number of visible CUDA devices (0 without a GPU; never fails) */
+int tsph_device_count(int *count);
+
+/* ---- particle system ---- */
+
+/* Particle_system(h, kap, cs, rho0, visco, delta, dp) + Simulation_data
+ * (src/SPH_particle_system.h:191-212, src/SPH_data.h:215-216).  `stream` is a
+ * cudaStream_t or NULL for a stream owned by the system.  Fails with
+ * TSPH_ERR_CUDA when no GPU is present. */
+int tsph_create(const tsph_constants *c, const tsph_domain *d, int precision,
+                void *stream, tsph_system **out);
+int tsph_destroy(tsph_system *s);
+
+/* Add_particle (src/SPH_particle_system.h:25-50) for n particles, plus the
+ * mDBC ghost node of each wall particle (special.gnr, src/SPH_data.h:51,
+ * pushed by the generators e.g. src/SPH_create.h:575-577).  gnr may be NULL
+ * (DBC); for fluid entries it is ignored.  Velocity of a wall must be 0. */
+int tsph_add_particles(tsph_system *s, int n, const int32_t *type,
+                       const double *r, const double *v, const double *rho,
+                       const double *p, const double *gnr);
+
+int tsph_np(tsph_system *s, int *np);          /* live particles (particles.np) */
+int tsph_grid(tsph_system *s, int *ncx, int *ncy);
+int tsph_particle_mass(tsph_system *s, double *m);
+
+/* Divide_To_Cells, src/SPH_find_pairs.h:5-42: grid of ncx x ncy cells of size
+ * kh = kap*h, offset of = 0.273h, cell (x, y) -> id y + x*ncy. */
+int tsph_divide_to_cells(tsph_system *s);
+/* Clear_cells, src/SPH_find_pairs.h:74-92 (marks the cell lists stale) */
+int tsph_clear_cells(tsph_system *s);
+/* Particle_To_Cell, src/SPH_find_pairs.h:45-72: GPU counting sort by cell
+ * (exact FP64 cell index, histogram, scan, stable scatter, SoA reorder). */
+int tsph_particle_to_cell(tsph_system *s);
+/* cells[c].cp as CSR in the reference's numbering: cell c holds
+ * cell_list[cell_start[c] .. cell_start[c+1]), ascending particle index.
+ * cell_start has ncx*ncy+1 entries, cell_list np entries. */
+int tsph_get_cells(tsph_system *s, int32_t *cell_start, int32_t *cell_list);
+/* Per-particle pair-set digest of the in-support pairs (0 < r <= 2h) over the
+ * 3x3 cell block of each particle: count, sum and xor of the neighbours'
+ * particle indices (reference numbering).  Arrays of np entries. */
+int tsph_pair_digest(tsph_system *s, int32_t *count, int64_t *sum, int32_t *xor_);
+
+/* Host-only (no GPU needed): the grid of Divide_To_Cells for (c, d) and the
+ * exact cell-index tables the device uses in place of the FP64 division of
+ * src/SPH_find_pairs.h:64-65.  bx[k] (k = 0..ncx) is the smallest double x,
+ * mapped to a signed 64-bit integer that orders like the doubles (bits for
+ * x >= +0, bits ^ 0x7fffffffffffffff for x < 0), whose cell index
+ * (int)((x - x_0 + of)/kh) is >= k; by likewise.  Pass bx = by = NULL to get
+ * ncx, ncy only. */
+int tsph_grid_tables(const tsph_constants *c, const tsph_domain *d, int *ncx, int *ncy,
+                     int64_t *bx, int64_t *by);
+
+/* Density_to_pressure, src/SPH_pressure.h:65-89 (Tait EOS :7-21) */
+int tsph_density_to_pressure(tsph_system *s);
+/* mDBC_compute_density_mdbcGeo, src/SPH_mDBC.h:9-50 with
+ * Kernel_density_approximation_MATRIX_mDBC, src/SPH_kernel_approx.h:1141-1343 */
+int tsph_mdbc_density(tsph_system *s);
+/* Compute_Forces: src/SPH_interaction.h:8-149 (TSPH_WALL_MDBC) or
+ * src/SPH_interactionDBC.h:8-155 (TSPH_WALL_DBC) */
+int tsph_compute_forces(tsph_system *s, int wall_model);
+/* Integrate_SymplecticPredictor / Corrector, src/SPH_integration.h:266-309 */
+int tsph_symplectic_predictor(tsph_system *s, double dt);
+int tsph_symplectic_corrector(tsph_system *s, double dt);
+/* RemoveParticlesOutOfDomain, src/SPH_btdebug.h:4-31 */
+int tsph_remove_out_of_domain(tsph_system *s, int *removed);
+
+/* nsteps bodies of SPH_simulation::RUN (cases/damBreakLong_mDBC/
+ * SPH_simulationSymplectic.h:59-118 for mDBC, cases/stillWater_DBC/
+ * SPH_simulationSymplectic.h:58-118 for DBC) as fused kernels replayed from a
+ * CUDA graph.  Requires tsph_particle_to_cell to have been called once (INIT,
+ * :41-45).  Leaves the state the reference has after the same steps. */
+int tsph_step(tsph_system *s, int wall_model, double dt, int nsteps);
+
+/* state transfer in the reference's order; `fields` is a TSPH_F_* mask */
+int tsph_download(tsph_system *s, int fields, const tsph_host_state *out);
+int tsph_upload(tsph_system *s, int fields, const tsph_host_state *in);
+/* wait for the system's stream */
+int tsph_sync(tsph_system *s);
+/* device health word (TSPH_HEALTH_*), optionally cleared */
+int tsph_health(tsph_system *s, uint32_t *flags, int clear);
+
+/* Global reductions in FP64 over fluid particles: total mass, kinetic energy
+ * sum(0.5 m |v|^2) (the harness-side Total_kinetic_energy the still-water
+ * driver calls), and momentum. out[0..3] = mass, ekin, px, py. */
+int tsph_fluid_totals(tsph_system *s, double out[4]);
+
+/* Kernel timing of the system's calls, for the roofline report.  With
+ * profiling on, tsph_step runs its kernels eagerly (no graph) with CUDA events
+ * around every launch on the system's stream; tsph_profile returns the sums
+ * since the last reset.  Off by default (graph replay, no events). */
+typedef struct {
+    double pair_us;      /* pair-loop + fused integrator kernels          */
+    int pair_launches;
+    double sort_us;      /* cell keys, scan, stable scatter                */
+    int sort_launches;
+    double mdbc_us;      /* ghost-node density                            */
+    int mdbc_launches;
+    double other_us;     /* everything else (EOS, predictor, ...)         */
+    int other_launches;
+} tsph_profile_t;
+int tsph_set_profiling(tsph_system *s, int on);
+int tsph_get_profile(tsph_system *s, tsph_profile_t *out, int reset);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TSPH_H */

@@ -94,6 +94,7 @@ def _load_port():
         L.orc_remove_out_of_domain.argtypes = [_P]
         L.orc_remove_out_of_domain.restype = _I
         L.orc_step.argtypes = [_P, _I, _D, _I]
+        L.orc_pair_digest.argtypes = [_P, _IP, np.ctypeslib.ndpointer(dtype=np.int64, flags='C_CONTIGUOUS'), _IP]
         L.orc_wendland.argtypes = [_D, _D, C.POINTER(_D), C.POINTER(_D)]
         L.orc_pressure.argtypes = [_D, _D, _D]
         L.orc_pressure.restype = _D
@@ -138,6 +139,7 @@ def _load_ref():
         L.ref_predictor.argtypes = [_P, _D]
         L.ref_corrector.argtypes = [_P, _D]
         L.ref_step.argtypes = [_P, _I, _D, _I]
+        L.ref_wendland.argtypes = [_D, _D, C.POINTER(_D), C.POINTER(_D)]
         _ref = L
     return _ref
 
@@ -243,6 +245,14 @@ class PortSystem(_Base):
         if n < 0:
             raise RuntimeError("cells not built")
         return start, lst[:n]
+
+    def pair_digest(self):
+        n = self.np()
+        c = np.empty(n, dtype=np.int32)
+        s = np.empty(n, dtype=np.int64)
+        x = np.empty(n, dtype=np.int32)
+        self.L.orc_pair_digest(self.s, c, s, x)
+        return c, s, x
 
     def divide_to_cells(self):
         self.L.orc_divide_to_cells(self.s)
@@ -372,6 +382,13 @@ class RefSystem(_Base):
 
     def step(self, model, dt, n=1):
         self.L.ref_step(self.s, int(model), dt, int(n))
+
+
+def ref_wendland(r, h):
+    L = _load_ref()
+    w, f = _D(), _D()
+    L.ref_wendland(r, h, C.byref(w), C.byref(f))
+    return w.value, f.value
 
 
 def wendland(r, h):

@@ -106,6 +106,13 @@ void ref_create_wall_y(void *c, double x, double y0, double y1, int o) {
     Create_Wall_y(static_cast<RefCase *>(c)->particles, x, y0, y1, o);
 }
 
+// Wendland_kernel, src/SPH_kernel.h:52-77 (returns through its static buffer)
+void ref_wendland(double r, double h, double *w, double *f) {
+    double *k = Wendland_kernel(r, h);
+    *w = k[0];
+    *f = k[1];
+}
+
 int ref_np(void *c) { return (int)static_cast<RefCase *>(c)->particles.np; }
 
 void ref_grid(void *c, int *ncx, int *ncy) {

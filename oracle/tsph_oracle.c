@@ -616,3 +616,44 @@ void orc_step(orc_sys *s, int model, double dt, int nsteps) {
         orc_compute_forces(s, model);
     }
 }
+
+/* Pair-set digest over the reference's 3x3 cell block of every particle
+ * (src/SPH_interaction.h:26-36, neighbour loop :71-82): for each row, the
+ * count, sum and xor of the original indices of neighbours j != i with
+ * r/h <= 2 (the support of the Wendland kernel, src/SPH_kernel.h:63).  Fluid
+ * rows see every neighbour; wall rows see fluid only (the DBC flavour skips
+ * wall-wall pairs, src/SPH_interactionDBC.h:84).  Outputs in particle order. */
+void orc_pair_digest(const orc_sys *s, int *count, long long *sum, int *xr) {
+    const int ncy = s->ncy, nc = s->ncells;
+    const int *cs = s->cell_start, *cl = s->cell_list;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int c = 0; c < nc; c++) {
+        const int ac[9] = {c,           c + 1,       c + 1 + ncy,
+                           c + ncy,     c - 1 + ncy, c - 1,
+                           c - 1 - ncy, c - ncy,     c + 1 - ncy};
+        for (int i = cs[c]; i < cs[c + 1]; i++) {
+            const int ai = cl[i];
+            int cnt = 0, x = 0;
+            long long sm = 0;
+            for (int k = 0; k < 9; k++) {
+                const int cc = ac[k];
+                if (cc < 0 || cc >= nc) continue;
+                for (int n = cs[cc]; n < cs[cc + 1]; n++) {
+                    const int ni = cl[n];
+                    if (ni == ai) continue;
+                    if (s->type[ai] == ORC_WALL && s->type[ni] == ORC_WALL) continue;
+                    const double drx = s->rx[ai] - s->rx[ni], dry = s->ry[ai] - s->ry[ni];
+                    const double drs = sqrt((drx * drx) + (dry * dry));
+                    if (drs / s->h <= 2.0) {
+                        cnt++;
+                        sm += s->index[ni];
+                        x ^= s->index[ni];
+                    }
+                }
+            }
+            count[ai] = cnt;
+            sum[ai] = sm;
+            xr[ai] = x;
+        }
+    }
+}

@@ -70,6 +70,9 @@ int orc_remove_out_of_domain(orc_sys *s);
 /* one RUN-loop body per step (mDBC or DBC case driver order) */
 void orc_step(orc_sys *s, int model, double dt, int nsteps);
 
+/* in-support pair-set digest (count, sum and xor of neighbour indices) */
+void orc_pair_digest(const orc_sys *s, int *count, long long *sum, int *xr);
+
 /* scalar kernels, exported for unit tests */
 void orc_wendland(double r, double h, double *w, double *f);
 double orc_pressure(double rho, double rho0, double c0);

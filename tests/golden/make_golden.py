@@ -1,0 +1,151 @@
+"""Generate the golden vectors in this directory from the reference itself.
+
+Runs the reference's own code (oracle/_ref/libtsph_ref.so, compiled from the
+reference headers by ``make -C oracle ref``) on small seeded cases and stores
+its outputs.  Needs the reference sources; the committed .npz files are what
+the tests read.  Usage: python tests/golden/make_golden.py
+"""
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle as O  # noqa: E402
+from tinysph_old_gb300 import cases  # noqa: E402
+
+SEED = 20261203
+
+
+def perturb(state, rng, dv=0.05, drho=1e-3):
+    """Seeded perturbation of fluid velocity and density (walls untouched)."""
+    fl = state["type"] == 0
+    v = state["v"].copy()
+    rho = state["rho"].copy()
+    v[fl] += rng.normal(0.0, dv, size=(fl.sum(), 2))
+    rho[fl] *= 1.0 + drho * rng.standard_normal(fl.sum())
+    return v, rho
+
+
+def geometry(ref_case_fn, name, out):
+    case = ref_case_fn()
+    R = O.RefSystem(case.h, case.kap, case.cs, case.rho0, case.visco, case.delta, case.dp,
+                    case.domain)
+    return case, R
+
+
+def dam_break_geometry(dp):
+    """The reference's own generators for cases/damBreakLong_mDBC/geometry.h."""
+    case = cases.dam_break_mdbc(dp=dp)
+    R = O.RefSystem(case.h, case.kap, case.cs, case.rho0, case.visco, case.delta, case.dp,
+                    case.domain)
+    L, s = R.L, R.s
+    L.ref_create_wall_x_mdbc(s, 0.0 + dp, 1.61, 0.0, -1, dp / 2)
+    L.ref_create_wall_y_mdbc(s, 0.0, 0 + dp, 1.0, -1, dp / 2)
+    L.ref_create_wall_y_mdbc(s, 1.61, 0 + dp, 1.0, +1, 1.61 - dp / 2)
+    L.ref_create_corner_mdbc(s, -1, -1, 0.0 + dp / 2, 0.0 + dp / 2)
+    L.ref_create_corner_mdbc(s, +1, -1, 1.61 - dp / 2, 0.0 + dp / 2)
+    L.ref_create_block_of_fluid(s, 0 + dp, 0 + dp, 0.6, 0.3)
+    st = R.state()
+    return dict(r=st["r"], type=st["type"], rho=st["rho"], p=st["p"], gnr=R.gnr())
+
+
+def wp_geometry(dp=0.02):
+    """Create_Block_of_FluidWP + DBC walls of the reference (src/SPH_create.h)."""
+    case = cases.still_water_dbc(dp=dp)
+    R = O.RefSystem(case.h, case.kap, case.cs, case.rho0, case.visco, case.delta, case.dp,
+                    case.domain)
+    L, s = R.L, R.s
+    L.ref_create_wall_x(s, 0.0, 0.5, 0.0, -1)
+    L.ref_create_wall_y(s, 0.0, 0.0 + dp, 0.4, -1)
+    L.ref_create_block_of_fluid_wp(s, 0 + dp, 0 + dp, 0.5 - dp, 0.3)
+    st = R.state()
+    return dict(r=st["r"], type=st["type"], rho=st["rho"], p=st["p"])
+
+
+def run_case(case, model, nsteps, rng, snap_every):
+    R = O.RefSystem.from_case(case)
+    R.set_threads(1)
+    st0 = R.state()
+    v, rho = perturb(st0, rng)
+    R.set_state(v=v, rho=rho)
+    init = R.state()
+    # per-function outputs at the perturbed initial state
+    R.density_to_pressure()
+    p0 = R.state()["p"]
+    out = dict(init_r=init["r"], init_v=init["v"], init_rho=init["rho"], init_type=init["type"],
+               init_p=p0)
+    start, lst = R.cells()
+    out["cell_start"] = start
+    out["cell_list"] = lst
+    if model == 0:
+        R.mdbc_density()
+        out["mdbc_rho"] = R.state()["rho"]
+        R.set_state(rho=init["rho"])
+        R.density_to_pressure()
+    R.compute_forces(model)
+    f = R.state()
+    out["forces_a"] = f["a"]
+    out["forces_drho"] = f["drho"]
+    # back to the perturbed initial state (a = drho = 0) and run the RUN loop
+    R2 = O.RefSystem.from_case(case)
+    R2.set_state(v=v, rho=rho)
+    done = 0
+    k = 0
+    while done < nsteps:
+        R2.step(model, case.dt, snap_every)
+        done += snap_every
+        st = R2.state()
+        for key in ("r", "v", "a", "rho", "drho", "p", "index"):
+            out[f"step{done}_{key}"] = st[key]
+        k += 1
+    out["dt"] = np.float64(case.dt)
+    out["nsteps"] = np.int64(nsteps)
+    out["snap_every"] = np.int64(snap_every)
+    return out
+
+
+def wendland_samples():
+    rng = np.random.default_rng(SEED)
+    h = np.array([0.001, np.sqrt(2) * 0.005, 0.0075, 0.04])
+    rows = []
+    for hh in h:
+        r = np.concatenate([[0.0, 2 * hh, 2 * hh * (1 + 1e-12)], rng.uniform(0, 2.2 * hh, 60)])
+        for rr in r:
+            w, f = O.ref_wendland(float(rr), float(hh))
+            rows.append((rr, hh, w, f))
+    return np.array(rows)
+
+
+def main():
+    if O.build_ref() is None or not O.ref_available():
+        raise SystemExit("reference harness not available (needs the reference sources)")
+    rng = np.random.default_rng(SEED)
+    # 1. geometry from the reference generators
+    g = {}
+    for dp in (0.02, 0.01):
+        for k, v in dam_break_geometry(dp).items():
+            g[f"dam_dp{dp:g}_{k}"] = v
+    for k, v in wp_geometry(0.02).items():
+        g[f"wp_dp0.02_{k}"] = v
+    np.savez_compressed(os.path.join(HERE, "geometry.npz"), **g)
+    # 2. dam break, mDBC flavour, 6 steps
+    dam = run_case(cases.dam_break_mdbc(dp=0.02), 0, 6, rng, 2)
+    np.savez_compressed(os.path.join(HERE, "dam_break_mdbc_dp0.02.npz"), **dam)
+    # 3. still water, DBC flavour, 6 steps
+    sw = run_case(cases.still_water_dbc(dp=0.02), 1, 6, rng, 2)
+    np.savez_compressed(os.path.join(HERE, "still_water_dbc_dp0.02.npz"), **sw)
+    # 4. Wendland kernel samples
+    np.savez_compressed(os.path.join(HERE, "wendland.npz"), samples=wendland_samples())
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,204 @@
+"""GPU parity through the C ABI against the oracle and the reference's golden
+vectors.
+
+Bars (stated per field, relative to the natural scale of the field):
+* cell lists and in-support pair sets: bit-exact (both precisions);
+* FP64 build: within 1e-9 of the reference (the only differences are the
+  last-bit differences of CUDA's pow against glibc's, propagated);
+* FP32 build (FP32 pair math, FP64 positions): field tolerances below,
+  derived from FP32 rounding of ~25-term pair sums.
+"""
+
+import os
+
+import numpy as np
+import pytest
+
+from tinysph_old_gb300 import cases
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+G = 9.81
+
+CASES = [
+    ("dam_break_mdbc_dp0.02.npz", lambda: cases.dam_break_mdbc(dp=0.02), 0),
+    ("still_water_dbc_dp0.02.npz", lambda: cases.still_water_dbc(dp=0.02), 1),
+]
+
+
+def _gold(name):
+    return np.load(os.path.join(GOLD, name))
+
+
+def _gpu(tsph, case, g, precision):
+    s = tsph.ParticleSystem.from_case(case, precision)
+    s.upload(v=g["init_v"], rho=g["init_rho"])
+    return s
+
+
+def _err(a, b):
+    return float(np.max(np.abs(np.asarray(a, dtype=np.float64) - np.asarray(b, dtype=np.float64))))
+
+
+# tolerances of the FP32 build, per field (absolute, in SI units), for the
+# dp = 0.02 golden cases; `scale` multiplies with the field's max magnitude
+def _tol32(field, ref):
+    mag = float(np.max(np.abs(ref))) if np.size(ref) else 0.0
+    return {
+        "r": 1e-9,                       # m
+        "v": 2e-6 + 1e-5 * mag,          # m/s
+        "a": 2e-3 + 2e-5 * mag,          # m/s^2 (pair sums of ~100 g terms)
+        "rho": 2e-4,                     # kg/m^3
+        "drho": 2e-2 + 2e-5 * mag,       # kg/m^3/s
+        "p": 5e-2 + 1e-6 * mag,          # Pa
+    }[field]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("fname,builder,model", CASES)
+def test_cells_bit_exact(gpu_tsph, fname, builder, model, precision):
+    g = _gold(fname)
+    s = _gpu(gpu_tsph, builder(), g, precision)
+    start, lst = s.get_cells()
+    assert np.array_equal(start, g["cell_start"])
+    assert np.array_equal(lst, g["cell_list"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("fname,builder,model", CASES)
+def test_pair_digest_bit_exact(gpu_tsph, oracle_mod, fname, builder, model):
+    g = _gold(fname)
+    case = builder()
+    s = _gpu(gpu_tsph, case, g, "fp32")
+    P = oracle_mod.PortSystem.from_case(case)
+    c0, s0, x0 = P.pair_digest()
+    c1, s1, x1 = s.pair_digest()
+    assert np.array_equal(c0, c1)
+    assert np.array_equal(s0, s1)
+    assert np.array_equal(x0, x1)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("fname,builder,model", CASES)
+def test_per_function_parity(gpu_tsph, fname, builder, model, precision):
+    """Density_to_pressure, mDBC and Compute_Forces at the golden input."""
+    g = _gold(fname)
+    s = _gpu(gpu_tsph, builder(), g, precision)
+    s.density_to_pressure()
+    st = s.download()
+    tol = (lambda f, r: 1e-9 * max(1.0, float(np.max(np.abs(r))))) if precision == "fp64" else _tol32
+    assert _err(st["p"], g["init_p"]) <= tol("p", g["init_p"])
+    if model == 0:
+        s.mdbc_density()
+        st = s.download()
+        wall = g["init_type"] == 1
+        e = _err(st["rho"][wall], g["mdbc_rho"][wall])
+        assert e <= (1e-9 if precision == "fp64" else 5e-3), e
+        s.upload(rho=g["init_rho"])
+        s.density_to_pressure()
+    s.compute_forces(model)
+    st = s.download()
+    ea = _err(st["a"], g["forces_a"])
+    ed = _err(st["drho"], g["forces_drho"])
+    assert ea <= tol("a", g["forces_a"]), ea
+    assert ed <= tol("drho", g["forces_drho"]), ed
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("fname,builder,model", CASES)
+def test_fused_step_matches_reference(gpu_tsph, fname, builder, model, precision):
+    """tsph_step (fused kernels, CUDA graph) against the reference's RUN loop."""
+    g = _gold(fname)
+    s = _gpu(gpu_tsph, builder(), g, precision)
+    every = int(g["snap_every"])
+    for k in range(every, int(g["nsteps"]) + 1, every):
+        s.step(model, float(g["dt"]), every)
+        st = s.download()
+        assert np.array_equal(st["index"], g[f"step{k}_index"])
+        for f in ("r", "v", "a", "rho", "drho", "p"):
+            ref = g[f"step{k}_{f}"]
+            e = _err(st[f], ref)
+            if precision == "fp64":
+                lim = 1e-9 * max(1.0, float(np.max(np.abs(ref))))
+            else:
+                lim = _tol32(f, ref) * (1 + k)
+            assert e <= lim, (k, f, e, lim)
+    assert s.health() & ~gpu_tsph.HEALTH_REMOVED == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_fused_equals_per_function_sequence(gpu_tsph, precision):
+    """The fused step and the per-function calls in the reference's RUN order
+    compute the same thing (FP64: bit-identical)."""
+    g = _gold("dam_break_mdbc_dp0.02.npz")
+    case = cases.dam_break_mdbc(dp=0.02)
+    dt = float(g["dt"])
+    a = _gpu(gpu_tsph, case, g, precision)
+    b = _gpu(gpu_tsph, case, g, precision)
+    a.step(0, dt, 3)
+    for _ in range(3):
+        b.mdbc_density()
+        b.density_to_pressure()
+        b.predictor(dt)
+        b.clear_cells()
+        b.particle_to_cell()
+        b.density_to_pressure()
+        b.compute_forces(0)
+        b.corrector(dt)
+        b.remove_out_of_domain()
+        b.clear_cells()
+        b.particle_to_cell()
+        b.density_to_pressure()
+        b.compute_forces(0)
+    sa, sb = a.download(), b.download()
+    for f in ("r", "v", "a", "rho", "drho", "p"):
+        if precision == "fp64":
+            assert np.array_equal(sa[f], sb[f]), f
+        else:
+            assert _err(sa[f], sb[f]) <= 1e-5 * max(1.0, float(np.max(np.abs(sa[f])))), f
+
+
+@pytest.mark.gpu
+def test_stale_cells_are_an_error(gpu_tsph):
+    case = cases.dam_break_mdbc(dp=0.02)
+    s = gpu_tsph.ParticleSystem.from_case(case)
+    s.predictor(case.dt)
+    with pytest.raises(gpu_tsph.TsphError) as e:
+        s.compute_forces(0)
+    assert e.value.status == gpu_tsph.ERR_STATE
+    s.particle_to_cell()
+    s.compute_forces(0)
+
+
+@pytest.mark.gpu
+def test_remove_out_of_domain(gpu_tsph, oracle_mod):
+    """Fluid outside the padded box is removed; the remaining particles keep
+    the reference's numbering (ascending original index)."""
+    case = cases.dam_break_mdbc(dp=0.02)
+    s = gpu_tsph.ParticleSystem.from_case(case, "fp64")
+    st = s.download()
+    r = st["r"].copy()
+    fl = np.where(st["type"] == 0)[0]
+    x0, xm, y0, ym = case.domain
+    r[fl[5]] = (1.0, ym + 0.02)    # above y_m + eps: removed
+    r[fl[7]] = (xm - 0.005, 0.5)   # x > x_m - eps: removed (src/SPH_btdebug.h:22)
+    r[fl[100]] = (1.0, 0.9)        # moved, stays
+    s.upload(r=r)
+    assert s.remove_out_of_domain() == 2
+    assert s.np == case.np - 2
+    s.particle_to_cell()
+    st2 = s.download()
+    assert len(st2["index"]) == case.np - 2
+    assert fl[5] not in set(st2["index"].tolist())
+    assert fl[7] not in set(st2["index"].tolist())
+    assert np.array_equal(np.sort(st2["index"]), st2["index"])
+    P = oracle_mod.PortSystem.from_case(case)
+    P.set_state(r=r)
+    P.remove_out_of_domain()
+    P.particle_to_cell()
+    start, lst = s.get_cells()
+    s0, l0 = P.cells()
+    assert np.array_equal(start, s0) and np.array_equal(lst, l0)

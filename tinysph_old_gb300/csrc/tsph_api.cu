@@ -1,0 +1,482 @@
+// tsph_api.cu -- the extern "C" boundary (include/tsph.h): argument checks,
+// the reference's grid arithmetic (Divide_To_Cells) and its exact cell-index
+// tables, and dispatch to the FP32 or FP64 engine.
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/tsph.h"
+#include "tsph_engine.h"
+#include "tsph_internal.cuh"
+
+using tsph::EngineBase;
+using tsph::HostSetup;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string &msg) {
+    g_err = msg;
+    return code;
+}
+
+// (int)((x - x_0 + of)/kh) exactly as src/SPH_find_pairs.h:64-65 evaluates it,
+// saturated outside the int range (the reference would overflow there)
+int ref_cell(double x, double x0, double of, double kh) {
+    const double q = (x - x0 + of) / kh;
+    if (!(q > -1e9)) return INT_MIN;
+    if (!(q < 1e9)) return INT_MAX;
+    return (int)q;
+}
+
+double from_ordered(long long o) {
+    const long long b = o >= 0 ? o : (o ^ 0x7fffffffffffffffLL);
+    double d;
+    std::memcpy(&d, &b, 8);
+    return d;
+}
+
+// smallest double (as ordered bits) whose cell index is >= k
+long long cell_lower_bound(int k, double x0, double of, double kh) {
+    double span = 3.0;
+    long long lo, hi;
+    for (;;) {
+        lo = tsph::ordered_bits(x0 - of + ((double)k - span) * kh);
+        hi = tsph::ordered_bits(x0 - of + ((double)k + span) * kh);
+        if (ref_cell(from_ordered(lo), x0, of, kh) < k && ref_cell(from_ordered(hi), x0, of, kh) >= k)
+            break;
+        span *= 2;
+    }
+    while ((unsigned long long)hi - (unsigned long long)lo > 1ull) {
+        const long long mid = lo + (long long)(((unsigned long long)hi - (unsigned long long)lo) / 2ull);
+        if (ref_cell(from_ordered(mid), x0, of, kh) >= k) hi = mid; else lo = mid;
+    }
+    return hi;
+}
+
+}  // namespace
+
+struct tsph_system {
+    HostSetup hs;
+    int precision = TSPH_PREC_FP32;
+    void *stream = nullptr;
+    std::unique_ptr<EngineBase> eng;
+    bool divided = false;
+    bool stale_engine = true;  // host particle list changed since the engine was built
+    bool profiling = false;
+};
+
+static int ensure_engine(tsph_system *s) {
+    if (!s->divided) return fail(TSPH_ERR_STATE, "call tsph_divide_to_cells first");
+    if (s->eng && !s->stale_engine) return TSPH_OK;
+    std::unique_ptr<EngineBase> e(s->precision == TSPH_PREC_FP64 ? tsph::make_engine_f64()
+                                                                  : tsph::make_engine_f32());
+    std::string err;
+    s->eng.reset();
+    int rc = e->init(s->hs, s->stream, err);
+    if (rc) return fail(rc, err);
+    e->set_profiling(s->profiling);
+    s->eng = std::move(e);
+    s->stale_engine = false;
+    return TSPH_OK;
+}
+
+#define NEED(s)                                                        \
+    do {                                                               \
+        if (!(s)) return fail(TSPH_ERR_ARG, "null system handle");     \
+    } while (0)
+
+#define ENGINE(s)                                                      \
+    do {                                                               \
+        int rc_ = ensure_engine(s);                                    \
+        if (rc_) return rc_;                                           \
+    } while (0)
+
+#define RUN(expr)                                                      \
+    do {                                                               \
+        std::string err_;                                              \
+        int rc_ = (expr);                                              \
+        if (rc_) return fail(rc_, err_);                               \
+    } while (0)
+
+extern "C" {
+
+int tsph_abi_version(void) { return TSPH_ABI_VERSION; }
+
+const char *tsph_last_error(void) { return g_err.c_str(); }
+
+const char *tsph_status_string(int status) {
+    switch (status) {
+    case TSPH_OK: return "ok";
+    case TSPH_ERR_ARG: return "invalid argument";
+    case TSPH_ERR_CUDA: return "CUDA error";
+    case TSPH_ERR_STATE: return "call out of order";
+    case TSPH_ERR_NOMEM: return "out of memory";
+    case TSPH_ERR_NUMERIC: return "NaN or Inf in the state";
+    case TSPH_ERR_DENSITY: return "density out of range";
+    case TSPH_ERR_ESCAPED: return "particle left the grid";
+    case TSPH_ERR_UNSUPPORTED: return "unsupported";
+    default: return "unknown status";
+    }
+}
+
+int tsph_device_count(int *count) {
+    if (!count) return fail(TSPH_ERR_ARG, "null count");
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        n = 0;
+    }
+    *count = n;
+    return TSPH_OK;
+}
+
+int tsph_create(const tsph_constants *c, const tsph_domain *d, int precision, void *stream,
+                tsph_system **out) {
+    if (!c || !d || !out) return fail(TSPH_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (precision != TSPH_PREC_FP32 && precision != TSPH_PREC_FP64)
+        return fail(TSPH_ERR_ARG, "precision must be TSPH_PREC_FP32 or TSPH_PREC_FP64");
+    if (!(c->h > 0) || !(c->kap > 0) || !(c->dp > 0) || !(c->cs > 0) || !(c->rho0 > 0))
+        return fail(TSPH_ERR_ARG, "h, kap, dp, cs and rho0 must be positive");
+    if (!(d->x_m > d->x_0) || !(d->y_m > d->y_0)) return fail(TSPH_ERR_ARG, "empty domain");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(TSPH_ERR_CUDA, "no CUDA device available");
+    }
+    tsph_system *s = new tsph_system();
+    HostSetup &hs = s->hs;
+    // Particle_system constructor, src/SPH_particle_system.h:191-212
+    hs.h = c->h;
+    hs.kap = c->kap;
+    hs.cs = c->cs;
+    hs.rho0 = c->rho0;
+    hs.dp = c->dp;
+    hs.g = 9.81;
+    hs.m = c->rho0 / (1 / c->dp * 1 / c->dp);
+    hs.visco = c->visco;
+    hs.delta = c->delta;
+    hs.x0 = d->x_0;
+    hs.xm = d->x_m;
+    hs.y0 = d->y_0;
+    hs.ym = d->y_m;
+    s->precision = precision;
+    s->stream = stream;
+    *out = s;
+    return TSPH_OK;
+}
+
+int tsph_destroy(tsph_system *s) {
+    delete s;
+    return TSPH_OK;
+}
+
+int tsph_add_particles(tsph_system *s, int n, const int32_t *type, const double *r,
+                       const double *v, const double *rho, const double *p, const double *gnr) {
+    NEED(s);
+    if (n < 0) return fail(TSPH_ERR_ARG, "negative count");
+    if (n == 0) return TSPH_OK;
+    if (!type || !r || !rho) return fail(TSPH_ERR_ARG, "type, r and rho are required");
+    for (int i = 0; i < n; i++) {
+        if (type[i] != TSPH_FLUID && type[i] != TSPH_WALL)
+            return fail(TSPH_ERR_UNSUPPORTED,
+                        "particle type " + std::to_string(type[i]) +
+                            " (only fluid = 0 and wall = 1 are on this path)");
+        if (type[i] == TSPH_WALL && v && (v[2 * i] != 0.0 || v[2 * i + 1] != 0.0))
+            return fail(TSPH_ERR_UNSUPPORTED, "moving walls are not on this path (wall v must be 0)");
+        if (!std::isfinite(r[2 * i]) || !std::isfinite(r[2 * i + 1]) || !std::isfinite(rho[i]))
+            return fail(TSPH_ERR_ARG, "non-finite position or density");
+    }
+    HostSetup &hs = s->hs;
+    // keep the evolved state when particles are appended to a running system
+    if (s->eng && !s->stale_engine) {
+        int np = 0;
+        std::string err;
+        int rc = s->eng->np_live(&np, err);
+        if (rc) return fail(rc, err);
+        if (np != (int)hs.type.size())
+            return fail(TSPH_ERR_STATE, "cannot append particles after removals");
+        std::vector<double> R(2 * np), V(2 * np), A(2 * np), RHO(np), DRHO(np), P(np);
+        rc = s->eng->download(63, R.data(), V.data(), A.data(), RHO.data(), DRHO.data(), P.data(),
+                              nullptr, nullptr, err);
+        if (rc) return fail(rc, err);
+        hs.r = R;
+        hs.v = V;
+        hs.a = A;
+        hs.rho = RHO;
+        hs.drho = DRHO;
+        hs.p = P;
+    }
+    for (int i = 0; i < n; i++) {
+        hs.type.push_back(type[i]);
+        hs.r.push_back(r[2 * i]);
+        hs.r.push_back(r[2 * i + 1]);
+        hs.v.push_back(v ? v[2 * i] : 0.0);
+        hs.v.push_back(v ? v[2 * i + 1] : 0.0);
+        hs.a.push_back(0.0);
+        hs.a.push_back(0.0);
+        hs.rho.push_back(rho[i]);
+        hs.drho.push_back(0.0);
+        hs.p.push_back(p ? p[i] : 0.0);
+        const bool g = gnr && type[i] == TSPH_WALL;
+        hs.gnr.push_back(g ? gnr[2 * i] : 0.0);
+        hs.gnr.push_back(g ? gnr[2 * i + 1] : 0.0);
+        hs.has_gnr.push_back(g ? 1 : 0);
+    }
+    s->stale_engine = true;
+    return TSPH_OK;
+}
+
+int tsph_np(tsph_system *s, int *np) {
+    NEED(s);
+    if (!np) return fail(TSPH_ERR_ARG, "null np");
+    if (!s->eng || s->stale_engine) {
+        *np = (int)s->hs.type.size();
+        return TSPH_OK;
+    }
+    RUN(s->eng->np_live(np, err_));
+    return TSPH_OK;
+}
+
+int tsph_grid(tsph_system *s, int *ncx, int *ncy) {
+    NEED(s);
+    if (!s->divided) return fail(TSPH_ERR_STATE, "call tsph_divide_to_cells first");
+    if (ncx) *ncx = s->hs.ncx;
+    if (ncy) *ncy = s->hs.ncy;
+    return TSPH_OK;
+}
+
+int tsph_particle_mass(tsph_system *s, double *m) {
+    NEED(s);
+    if (!m) return fail(TSPH_ERR_ARG, "null m");
+    *m = s->hs.m;
+    return TSPH_OK;
+}
+
+// grid dimensions and exact cell-index tables (Divide_To_Cells,
+// src/SPH_find_pairs.h:5-42, and the index of :64-65)
+static int make_grid(HostSetup &hs) {
+    const double kh = hs.kap * hs.h;
+    const double of = hs.h * 0.273;
+    const double qx = (hs.xm - hs.x0 + of) / kh, qy = (hs.ym - hs.y0 + of) / kh;
+    if (!(qx < 1e7) || !(qy < 1e7)) return fail(TSPH_ERR_ARG, "grid too large");
+    const int ncx = (int)qx + 1;
+    const int ncy = (int)qy + 1;
+    if (ncy < 4 || ncx < 1) return fail(TSPH_ERR_UNSUPPORTED, "grid needs at least 4 cells in y");
+    if ((long long)ncx * ncy > 200000000LL) return fail(TSPH_ERR_ARG, "grid too large");
+    hs.kh = kh;
+    hs.of = of;
+    hs.ncx = ncx;
+    hs.ncy = ncy;
+    hs.bx.resize(ncx + 1);
+    hs.by.resize(ncy + 1);
+    for (int k = 0; k <= ncx; k++) hs.bx[k] = cell_lower_bound(k, hs.x0, of, kh);
+    for (int k = 0; k <= ncy; k++) hs.by[k] = cell_lower_bound(k, hs.y0, of, kh);
+    hs.ox.resize(ncx);
+    hs.oy.resize(ncy);
+    for (int k = 0; k < ncx; k++) hs.ox[k] = (hs.x0 - of) + k * kh;
+    for (int k = 0; k < ncy; k++) hs.oy[k] = (hs.y0 - of) + k * kh;
+    return TSPH_OK;
+}
+
+int tsph_grid_tables(const tsph_constants *c, const tsph_domain *d, int *ncx, int *ncy,
+                     int64_t *bx, int64_t *by) {
+    if (!c || !d || !ncx || !ncy) return fail(TSPH_ERR_ARG, "null argument");
+    if (!(c->h > 0) || !(c->kap > 0)) return fail(TSPH_ERR_ARG, "h and kap must be positive");
+    HostSetup hs;
+    hs.h = c->h;
+    hs.kap = c->kap;
+    hs.x0 = d->x_0;
+    hs.xm = d->x_m;
+    hs.y0 = d->y_0;
+    hs.ym = d->y_m;
+    int rc = make_grid(hs);
+    if (rc) return rc;
+    *ncx = hs.ncx;
+    *ncy = hs.ncy;
+    if (bx) std::memcpy(bx, hs.bx.data(), 8 * hs.bx.size());
+    if (by) std::memcpy(by, hs.by.data(), 8 * hs.by.size());
+    return TSPH_OK;
+}
+
+// Divide_To_Cells, src/SPH_find_pairs.h:5-42
+int tsph_divide_to_cells(tsph_system *s) {
+    NEED(s);
+    int rc = make_grid(s->hs);
+    if (rc) return rc;
+    s->divided = true;
+    s->stale_engine = true;
+    return TSPH_OK;
+}
+
+int tsph_clear_cells(tsph_system *s) {
+    NEED(s);
+    if (s->eng && !s->stale_engine) s->eng->invalidate_cells();
+    return TSPH_OK;
+}
+
+int tsph_particle_to_cell(tsph_system *s) {
+    NEED(s);
+    ENGINE(s);
+    RUN(s->eng->particle_to_cell(err_));
+    return TSPH_OK;
+}
+
+int tsph_get_cells(tsph_system *s, int32_t *cell_start, int32_t *cell_list) {
+    NEED(s);
+    if (!cell_start || !cell_list) return fail(TSPH_ERR_ARG, "null output");
+    ENGINE(s);
+    RUN(s->eng->get_cells(cell_start, cell_list, err_));
+    return TSPH_OK;
+}
+
+int tsph_pair_digest(tsph_system *s, int32_t *count, int64_t *sum, int32_t *xor_) {
+    NEED(s);
+    if (!count || !sum || !xor_) return fail(TSPH_ERR_ARG, "null output");
+    ENGINE(s);
+    RUN(s->eng->pair_digest(count, sum, xor_, err_));
+    return TSPH_OK;
+}
+
+int tsph_density_to_pressure(tsph_system *s) {
+    NEED(s);
+    ENGINE(s);
+    RUN(s->eng->density_to_pressure(err_));
+    return TSPH_OK;
+}
+
+int tsph_mdbc_density(tsph_system *s) {
+    NEED(s);
+    ENGINE(s);
+    RUN(s->eng->mdbc_density(err_));
+    return TSPH_OK;
+}
+
+int tsph_compute_forces(tsph_system *s, int wall_model) {
+    NEED(s);
+    if (wall_model != TSPH_WALL_MDBC && wall_model != TSPH_WALL_DBC)
+        return fail(TSPH_ERR_ARG, "wall_model must be TSPH_WALL_MDBC or TSPH_WALL_DBC");
+    ENGINE(s);
+    RUN(s->eng->compute_forces(wall_model, err_));
+    return TSPH_OK;
+}
+
+int tsph_symplectic_predictor(tsph_system *s, double dt) {
+    NEED(s);
+    if (!std::isfinite(dt)) return fail(TSPH_ERR_ARG, "dt must be finite");
+    ENGINE(s);
+    RUN(s->eng->predictor(dt, err_));
+    return TSPH_OK;
+}
+
+int tsph_symplectic_corrector(tsph_system *s, double dt) {
+    NEED(s);
+    if (!std::isfinite(dt)) return fail(TSPH_ERR_ARG, "dt must be finite");
+    ENGINE(s);
+    RUN(s->eng->corrector(dt, err_));
+    return TSPH_OK;
+}
+
+int tsph_remove_out_of_domain(tsph_system *s, int *removed) {
+    NEED(s);
+    ENGINE(s);
+    RUN(s->eng->remove_out_of_domain(removed, err_));
+    return TSPH_OK;
+}
+
+int tsph_step(tsph_system *s, int wall_model, double dt, int nsteps) {
+    NEED(s);
+    if (wall_model != TSPH_WALL_MDBC && wall_model != TSPH_WALL_DBC)
+        return fail(TSPH_ERR_ARG, "wall_model must be TSPH_WALL_MDBC or TSPH_WALL_DBC");
+    if (!std::isfinite(dt) || nsteps < 0) return fail(TSPH_ERR_ARG, "bad dt or nsteps");
+    ENGINE(s);
+    if (nsteps == 0) return TSPH_OK;
+    RUN(s->eng->step(wall_model, dt, nsteps, err_));
+    return TSPH_OK;
+}
+
+int tsph_download(tsph_system *s, int fields, const tsph_host_state *out) {
+    NEED(s);
+    if (!out) return fail(TSPH_ERR_ARG, "null output");
+    ENGINE(s);
+    RUN(s->eng->download(fields, out->r, out->v, out->a, out->rho, out->drho, out->p, out->index,
+                         out->type, err_));
+    if ((fields & TSPH_F_TYPE) && out->type) {
+        // types from the host list, in the reference's order of live particles
+        std::vector<int32_t> idx;
+        int np = 0;
+        RUN(s->eng->np_live(&np, err_));
+        idx.resize(np);
+        RUN(s->eng->download(TSPH_F_INDEX, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                             idx.data(), nullptr, err_));
+        for (int k = 0; k < np; k++) out->type[k] = s->hs.type[idx[k]];
+    }
+    return TSPH_OK;
+}
+
+int tsph_upload(tsph_system *s, int fields, const tsph_host_state *in) {
+    NEED(s);
+    if (!in) return fail(TSPH_ERR_ARG, "null input");
+    if (fields & (TSPH_F_INDEX | TSPH_F_TYPE))
+        return fail(TSPH_ERR_ARG, "index and type are not uploadable");
+    ENGINE(s);
+    RUN(s->eng->upload(fields, in->r, in->v, in->a, in->rho, in->drho, in->p, err_));
+    return TSPH_OK;
+}
+
+int tsph_sync(tsph_system *s) {
+    NEED(s);
+    if (!s->eng) return TSPH_OK;
+    RUN(s->eng->sync(err_));
+    return TSPH_OK;
+}
+
+int tsph_health(tsph_system *s, uint32_t *flags, int clear) {
+    NEED(s);
+    if (!flags) return fail(TSPH_ERR_ARG, "null flags");
+    if (!s->eng || s->stale_engine) {
+        *flags = 0;
+        return TSPH_OK;
+    }
+    RUN(s->eng->health(flags, clear, err_));
+    return TSPH_OK;
+}
+
+int tsph_fluid_totals(tsph_system *s, double out[4]) {
+    NEED(s);
+    if (!out) return fail(TSPH_ERR_ARG, "null output");
+    ENGINE(s);
+    RUN(s->eng->totals(out, err_));
+    return TSPH_OK;
+}
+
+int tsph_set_profiling(tsph_system *s, int on) {
+    NEED(s);
+    s->profiling = on != 0;
+    if (s->eng) s->eng->set_profiling(s->profiling);
+    return TSPH_OK;
+}
+
+int tsph_get_profile(tsph_system *s, tsph_profile_t *out, int reset) {
+    NEED(s);
+    if (!out) return fail(TSPH_ERR_ARG, "null output");
+    std::memset(out, 0, sizeof(*out));
+    if (!s->eng) return TSPH_OK;
+    tsph::Profile p = s->eng->profile(reset != 0);
+    out->pair_us = p.us[tsph::CAT_PAIR];
+    out->pair_launches = p.launches[tsph::CAT_PAIR];
+    out->sort_us = p.us[tsph::CAT_SORT];
+    out->sort_launches = p.launches[tsph::CAT_SORT];
+    out->mdbc_us = p.us[tsph::CAT_MDBC];
+    out->mdbc_launches = p.launches[tsph::CAT_MDBC];
+    out->other_us = p.us[tsph::CAT_OTHER];
+    out->other_launches = p.launches[tsph::CAT_OTHER];
+    return TSPH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,831 @@
+// tsph_engine.cuh -- Engine<T>: device buffers, kernel sequencing, CUDA-graph
+// replay of the fused step.  Included once per precision.
+#pragma once
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <utility>
+#include <vector>
+
+#include "tsph_engine.h"
+#include "tsph_kernels.cuh"
+
+namespace tsph {
+
+#define TSPH_CK(call)                                                              \
+    do {                                                                           \
+        cudaError_t e_ = (call);                                                   \
+        if (e_ != cudaSuccess) {                                                   \
+            err = std::string(#call) + ": " + cudaGetErrorString(e_);              \
+            return 2; /* TSPH_ERR_CUDA */                                          \
+        }                                                                          \
+    } while (0)
+
+static inline int blocks_for(long long n, int b = kBlock) {
+    return (int)std::max<long long>(1, (n + b - 1) / b);
+}
+
+template <typename T> class Engine final : public EngineBase {
+    typedef typename V2<T>::t T2;
+
+    // ---- sizes
+    int nf_ = 0, nw_ = 0, ntot_ = 0;  // fluid capacity, walls, all indices
+    int ncells_ = 0;
+    Grid grid_{};
+    Phys<T> P_{};
+    Box box_{};
+    cudaStream_t st_ = nullptr;
+    bool own_stream_ = false;
+    bool cells_ = false;
+    double m64_ = 0;
+
+    // ---- device memory (one arena per kind; freed in the destructor)
+    std::vector<void *> allocs_;
+    FluidState<T> F_{}, Fs_{};  // current sorted state, predicted sorted state
+    OldState<T> O_{};
+    double2 *Br_ = nullptr;
+    T2 *Bv_ = nullptr;
+    T *Brho_ = nullptr;
+    uint32_t *keyB_ = nullptr, *slotB_ = nullptr, *tmp_id_ = nullptr, *tmp_src_ = nullptr,
+             *perm_ = nullptr;
+    uint32_t *counts_ = nullptr, *fstart_ = nullptr, *wstart_ = nullptr, *tile_sums_ = nullptr;
+    uint32_t *health_ = nullptr, *removed_ = nullptr;
+    WallState<T> W_{};
+    Staging S_{};
+    double *dtot_ = nullptr;
+    long long *bx_ = nullptr, *by_ = nullptr;
+    double *ox_ = nullptr, *oy_ = nullptr;
+    int32_t *dig_count_ = nullptr, *dig_xor_ = nullptr;
+    long long *dig_sum_ = nullptr;
+
+    // ---- graphs keyed by (model, dt bits)
+    std::map<std::pair<int, long long>, cudaGraphExec_t> graphs_;
+
+    // ---- profiling
+    bool prof_ = false;
+    struct Mark {
+        int cat;
+        cudaEvent_t a, b;
+    };
+    std::vector<Mark> marks_;
+    std::vector<cudaEvent_t> ev_pool_;
+    Profile acc_{};
+
+    template <typename P> int alloc(P **p, size_t count, std::string &err) {
+        void *q = nullptr;
+        cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(P));
+        if (e != cudaSuccess) {
+            err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+            return 4;
+        }
+        allocs_.push_back(q);
+        *p = static_cast<P *>(q);
+        return 0;
+    }
+
+    cudaEvent_t ev() {
+        if (ev_pool_.empty()) {
+            cudaEvent_t e;
+            cudaEventCreate(&e);
+            return e;
+        }
+        cudaEvent_t e = ev_pool_.back();
+        ev_pool_.pop_back();
+        return e;
+    }
+
+    // launch with optional event bracketing for the profile
+    template <typename K, typename... A>
+    int launch(int cat, K kern, int grid, int block, std::string &err, A... args) {
+        cudaEvent_t a = nullptr, b = nullptr;
+        if (prof_) {
+            a = ev();
+            b = ev();
+            cudaEventRecord(a, st_);
+        }
+        kern<<<grid, block, 0, st_>>>(args...);
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            err = std::string("kernel launch: ") + cudaGetErrorString(e);
+            return 2;
+        }
+        if (prof_) {
+            cudaEventRecord(b, st_);
+            marks_.push_back({cat, a, b});
+        }
+        return 0;
+    }
+
+    int collect_profile(std::string &err) {
+        if (!prof_ || marks_.empty()) return 0;
+        TSPH_CK(cudaStreamSynchronize(st_));
+        for (auto &m : marks_) {
+            float ms = 0;
+            cudaEventElapsedTime(&ms, m.a, m.b);
+            acc_.us[m.cat] += 1000.0 * ms;
+            acc_.launches[m.cat] += 1;
+            ev_pool_.push_back(m.a);
+            ev_pool_.push_back(m.b);
+        }
+        marks_.clear();
+        return 0;
+    }
+
+    Nbr<T> nbr_fluid(const FluidState<T> &X, bool stored_p) const {
+        return Nbr<T>{X.r, X.loc, X.v, X.rho, stored_p ? X.p : nullptr};
+    }
+    // walls have v = 0: the pair loop reads a zero velocity array
+    T2 *wall_zero_v_ = nullptr;
+
+    Nbr<T> nbr_walls(bool stored_p) const {
+        return Nbr<T>{W_.r, W_.loc, wall_zero_v_, W_.rho, stored_p ? W_.p : nullptr};
+    }
+
+    // scan counts[0..ncells] -> fstart[0..ncells+1]
+    int scan(std::string &err) {
+        const int n = ncells_ + 1;
+        const int ntiles = (n + kScanTile - 1) / kScanTile;
+        int rc;
+        if ((rc = launch(CAT_SORT, k_scan_tiles, ntiles, kScanThreads, err, (const uint32_t *)counts_,
+                         fstart_, tile_sums_, n)))
+            return rc;
+        if ((rc = launch(CAT_SORT, k_scan_sums, 1, kScanThreads, err, tile_sums_, ntiles, fstart_, n)))
+            return rc;
+        return launch(CAT_SORT, k_scan_add, blocks_for(n), kBlock, err, fstart_,
+                      (const uint32_t *)tile_sums_, n);
+    }
+
+    // after keys/slots are in keyB_/slotB_ and counts_ is filled:
+    // scan, stable placement, gather of the source arrays into D (+ old state)
+    int sort_finish(const double2 *sr, const T2 *sv, const T *srho, const uint32_t *sid,
+                    const T2 *sa, const T *sdrho, const T *sp, FluidState<T> D,
+                    const double2 *or2, const T2 *ov2, const T *orho2, OldState<T> Od,
+                    std::string &err) {
+        int rc;
+        if ((rc = scan(err))) return rc;
+        const int *ntot = reinterpret_cast<const int *>(fstart_ + ncells_ + 1);
+        const int nb = blocks_for(nf_);
+        if ((rc = launch(CAT_SORT, k_place, nb, kBlock, err, (const uint32_t *)keyB_,
+                         (const uint32_t *)slotB_, sid, ntot, (const uint32_t *)fstart_, tmp_id_,
+                         tmp_src_)))
+            return rc;
+        if ((rc = launch(CAT_SORT, k_rank, nb, kBlock, err, (const uint32_t *)keyB_, ntot,
+                         (const uint32_t *)fstart_, (const uint32_t *)tmp_id_,
+                         (const uint32_t *)tmp_src_, perm_, ncells_)))
+            return rc;
+        return launch(CAT_SORT, k_gather<T>, nb, kBlock, err, (const uint32_t *)perm_, ntot, grid_,
+                      sr, sv, srho, sid, (const uint32_t *)keyB_, sa, sdrho, sp, D, or2, ov2, orho2,
+                      Od);
+    }
+
+    int zero_counts(std::string &err) {
+        TSPH_CK(cudaMemsetAsync(counts_, 0, sizeof(uint32_t) * (ncells_ + 1), st_));
+        return 0;
+    }
+
+    int do_mdbc(std::string &err) {
+        if (nw_ == 0) return 0;
+        return launch(CAT_MDBC, k_mdbc<T>, blocks_for((long long)nw_ * 32), kBlock, err, W_, nw_,
+                      (const uint32_t *)fstart_, nbr_fluid(F_, false), grid_, P_);
+    }
+
+    // one fused step (enqueue only)
+    int enqueue_step(int model, T dt, std::string &err) {
+        int rc;
+        const bool dbc = model == 1;
+        if (!dbc && (rc = do_mdbc(err))) return rc;
+        // predictor + bin
+        if ((rc = zero_counts(err))) return rc;
+        if ((rc = launch(CAT_OTHER, k_predict_bin<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, W_, nw_, grid_, dt, Br_, Bv_, Brho_, keyB_,
+                         slotB_, counts_, health_)))
+            return rc;
+        if ((rc = sort_finish(Br_, Bv_, Brho_, F_.id, nullptr, nullptr, nullptr, Fs_, F_.r, F_.v,
+                              F_.rho, O_, err)))
+            return rc;
+        // forces at the predicted state + corrector + bin
+        if ((rc = zero_counts(err))) return rc;
+        PairOut po{Br_, (void *)Bv_, (void *)Brho_, keyB_, slotB_, counts_, box_};
+        if ((rc = launch(CAT_PAIR, k_fluid_pairs<T, MODE_CORRECT>, blocks_for(nf_), kBlock, err, Fs_,
+                         (const uint32_t *)fstart_, (const uint32_t *)wstart_,
+                         nbr_fluid(Fs_, false), nbr_walls(false), grid_, P_, O_, dt, po, health_,
+                         (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
+                         (const uint32_t *)nullptr)))
+            return rc;
+        if (nw_ > 0 &&
+            (rc = launch(CAT_PAIR, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
+                         (const uint32_t *)fstart_, nbr_fluid(Fs_, false), grid_, P_, dbc, true, dt,
+                         (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
+                         (const uint32_t *)nullptr, false)))
+            return rc;
+        if ((rc = sort_finish(Br_, Bv_, Brho_, Fs_.id, nullptr, nullptr, nullptr, F_, nullptr,
+                              nullptr, nullptr, O_, err)))
+            return rc;
+        // forces at the new state (a, drho for the next predictor)
+        if ((rc = launch(CAT_PAIR, k_fluid_pairs<T, MODE_FORCES>, blocks_for(nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, (const uint32_t *)wstart_,
+                         nbr_fluid(F_, false), nbr_walls(false), grid_, P_, O_, dt,
+                         PairOut{}, health_, (int32_t *)nullptr, (long long *)nullptr,
+                         (int32_t *)nullptr, (const uint32_t *)nullptr)))
+            return rc;
+        if (dbc && nw_ > 0 &&
+            (rc = launch(CAT_PAIR, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
+                         (const uint32_t *)fstart_, nbr_fluid(F_, false), grid_, P_, true, false, dt,
+                         (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
+                         (const uint32_t *)nullptr, false)))
+            return rc;
+        return 0;
+    }
+
+  public:
+    ~Engine() override {
+        for (auto &g : graphs_) cudaGraphExecDestroy(g.second);
+        for (auto &m : marks_) {
+            cudaEventDestroy(m.a);
+            cudaEventDestroy(m.b);
+        }
+        for (auto e : ev_pool_) cudaEventDestroy(e);
+        for (void *p : allocs_) cudaFree(p);
+        if (own_stream_ && st_) cudaStreamDestroy(st_);
+    }
+
+    int init(const HostSetup &hs, void *stream, std::string &err) override {
+        if (stream) {
+            st_ = static_cast<cudaStream_t>(stream);
+        } else {
+            TSPH_CK(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+            own_stream_ = true;
+        }
+        const int n = (int)hs.type.size();
+        ntot_ = n;
+        ncells_ = hs.ncx * hs.ncy;
+        // split fluid / walls
+        std::vector<int> fl, wl;
+        for (int i = 0; i < n; i++) (hs.type[i] == 1 ? wl : fl).push_back(i);
+        nf_ = (int)fl.size();
+        nw_ = (int)wl.size();
+        // constants
+        m64_ = hs.m;
+        P_.hd = hs.h;
+        P_.h = (T)hs.h;
+        P_.inv_h = (T)(1.0 / hs.h);
+        P_.kh = (T)hs.kh;
+        P_.m = (T)hs.m;
+        P_.c0 = (T)hs.cs;
+        P_.alpha = (T)hs.visco;
+        P_.delta = (T)hs.delta;
+        P_.rho0 = (T)hs.rho0;
+        P_.g = (T)hs.g;
+        P_.awen = (T)(double)(float)(0.557 / (hs.h * hs.h));
+        P_.bwen = (T)(double)(float)(-2.7852 / (hs.h * hs.h * hs.h));
+        P_.four_h2 = (T)(4.0 * hs.h * hs.h);
+        P_.eps_h2 = (T)(0.01 * hs.h * hs.h);
+        P_.bwen_h = (T)((double)(float)(-2.7852 / (hs.h * hs.h * hs.h)) / hs.h);
+        P_.b_eos = (T)(hs.cs * hs.cs * hs.rho0 / 7.0);
+        P_.k_av = (T)(-2.0 * hs.visco * hs.cs * hs.h);
+        P_.k_psi = (T)(2.0 * hs.cs * hs.h * hs.delta);
+        P_.xg = (T)(hs.rho0 * hs.g / (hs.cs * hs.cs * hs.rho0 / 7.0));
+        box_ = Box{hs.x0, hs.xm, hs.y0, hs.ym};
+        // grid tables
+        int rc;
+        if ((rc = alloc(&bx_, hs.bx.size(), err)) || (rc = alloc(&by_, hs.by.size(), err)) ||
+            (rc = alloc(&ox_, hs.ox.size(), err)) || (rc = alloc(&oy_, hs.oy.size(), err)))
+            return rc;
+        TSPH_CK(cudaMemcpy(bx_, hs.bx.data(), 8 * hs.bx.size(), cudaMemcpyHostToDevice));
+        TSPH_CK(cudaMemcpy(by_, hs.by.data(), 8 * hs.by.size(), cudaMemcpyHostToDevice));
+        TSPH_CK(cudaMemcpy(ox_, hs.ox.data(), 8 * hs.ox.size(), cudaMemcpyHostToDevice));
+        TSPH_CK(cudaMemcpy(oy_, hs.oy.data(), 8 * hs.oy.size(), cudaMemcpyHostToDevice));
+        grid_.ax = Axis{bx_, ox_, hs.ncx};
+        grid_.ay = Axis{by_, oy_, hs.ncy};
+        grid_.ncx = hs.ncx;
+        grid_.ncy = hs.ncy;
+        grid_.ncells = ncells_;
+        grid_.khf = (float)hs.kh;
+        // fluid buffers
+        auto alloc_state = [&](FluidState<T> &X) -> int {
+            int r;
+            if ((r = alloc(&X.r, nf_, err)) || (r = alloc(&X.v, nf_, err)) ||
+                (r = alloc(&X.a, nf_, err)) || (r = alloc(&X.rho, nf_, err)) ||
+                (r = alloc(&X.drho, nf_, err)) || (r = alloc(&X.p, nf_, err)) ||
+                (r = alloc(&X.id, nf_, err)) || (r = alloc(&X.key, nf_, err)) ||
+                (r = alloc(&X.loc, nf_, err)))
+                return r;
+            return 0;
+        };
+        if ((rc = alloc_state(F_)) || (rc = alloc_state(Fs_))) return rc;
+        if ((rc = alloc(&O_.r, nf_, err)) || (rc = alloc(&O_.v, nf_, err)) ||
+            (rc = alloc(&O_.rho, nf_, err)) || (rc = alloc(&Br_, nf_, err)) ||
+            (rc = alloc(&Bv_, nf_, err)) || (rc = alloc(&Brho_, nf_, err)) ||
+            (rc = alloc(&keyB_, nf_, err)) || (rc = alloc(&slotB_, nf_, err)) ||
+            (rc = alloc(&tmp_id_, nf_, err)) || (rc = alloc(&tmp_src_, nf_, err)) ||
+            (rc = alloc(&perm_, nf_, err)))
+            return rc;
+        const int ntiles = (ncells_ + 1 + kScanTile - 1) / kScanTile;
+        if (ntiles > kScanTile) {
+            err = "grid too large for the scan";
+            return 1;
+        }
+        if ((rc = alloc(&counts_, ncells_ + 1, err)) || (rc = alloc(&fstart_, ncells_ + 2, err)) ||
+            (rc = alloc(&wstart_, ncells_ + 1, err)) || (rc = alloc(&tile_sums_, ntiles, err)) ||
+            (rc = alloc(&health_, 1, err)) || (rc = alloc(&removed_, 1, err)) ||
+            (rc = alloc(&dtot_, 4 * (size_t)blocks_for(nf_), err)))
+            return rc;
+        TSPH_CK(cudaMemset(health_, 0, 4));
+        TSPH_CK(cudaMemset(removed_, 0, 4));
+        // staging
+        if ((rc = alloc(&S_.r, ntot_, err)) || (rc = alloc(&S_.v, ntot_, err)) ||
+            (rc = alloc(&S_.a, ntot_, err)) || (rc = alloc(&S_.rho, ntot_, err)) ||
+            (rc = alloc(&S_.drho, ntot_, err)) || (rc = alloc(&S_.p, ntot_, err)) ||
+            (rc = alloc(&S_.alive, ntot_, err)))
+            return rc;
+        // ---- fluid initial state in index order
+        {
+            std::vector<double2> r(nf_);
+            std::vector<T2> v(nf_), a(nf_);
+            std::vector<T> rho(nf_), zero(nf_, T(0)), p(nf_);
+            std::vector<uint32_t> id(nf_), key(nf_, 0u);
+            std::vector<float2> loc(nf_, make_float2(0.f, 0.f));
+            for (int k = 0; k < nf_; k++) {
+                const int i = fl[k];
+                r[k] = make_double2(hs.r[2 * i], hs.r[2 * i + 1]);
+                v[k].x = (T)hs.v[2 * i];
+                v[k].y = (T)hs.v[2 * i + 1];
+                a[k].x = (T)hs.a[2 * i];
+                a[k].y = (T)hs.a[2 * i + 1];
+                rho[k] = rho_stored_from_full<T>(hs.rho[i], hs.rho0);
+                zero[k] = (T)hs.drho[i];
+                p[k] = (T)hs.p[i];
+                id[k] = (uint32_t)i;
+            }
+            TSPH_CK(cudaMemcpy(F_.r, r.data(), 16 * (size_t)nf_, cudaMemcpyHostToDevice));
+            TSPH_CK(cudaMemcpy(F_.v, v.data(), sizeof(T2) * nf_, cudaMemcpyHostToDevice));
+            TSPH_CK(cudaMemcpy(F_.a, a.data(), sizeof(T2) * nf_, cudaMemcpyHostToDevice));
+            TSPH_CK(cudaMemcpy(F_.rho, rho.data(), sizeof(T) * nf_, cudaMemcpyHostToDevice));
+            TSPH_CK(cudaMemcpy(F_.drho, zero.data(), sizeof(T) * nf_, cudaMemcpyHostToDevice));
+            TSPH_CK(cudaMemcpy(F_.p, p.data(), sizeof(T) * nf_, cudaMemcpyHostToDevice));
+            TSPH_CK(cudaMemcpy(F_.id, id.data(), 4 * (size_t)nf_, cudaMemcpyHostToDevice));
+            TSPH_CK(cudaMemcpy(F_.key, key.data(), 4 * (size_t)nf_, cudaMemcpyHostToDevice));
+            TSPH_CK(cudaMemcpy(F_.loc, loc.data(), 8 * (size_t)nf_, cudaMemcpyHostToDevice));
+            // all entries live, none binned yet
+            std::vector<uint32_t> fs(ncells_ + 2, 0u);
+            fs[ncells_] = (uint32_t)nf_;
+            fs[ncells_ + 1] = (uint32_t)nf_;
+            TSPH_CK(cudaMemcpy(fstart_, fs.data(), 4 * fs.size(), cudaMemcpyHostToDevice));
+        }
+        // ---- walls: binned once on the host, sorted by (cell, index)
+        {
+            auto cell_of = [&](double x, const std::vector<long long> &b) -> int {
+                const long long o = ordered_bits(x);
+                if (o < b.front()) return -1;
+                if (o >= b.back()) return (int)b.size() - 1;
+                return (int)(std::upper_bound(b.begin(), b.end(), o) - b.begin()) - 1;
+            };
+            std::vector<std::pair<uint32_t, int>> order;
+            for (int i : wl) {
+                const int cx = cell_of(hs.r[2 * i], hs.bx), cy = cell_of(hs.r[2 * i + 1], hs.by);
+                if (cx < 0 || cy < 0 || cx >= hs.ncx || cy >= hs.ncy) {
+                    err = "wall particle " + std::to_string(i) + " lies outside the cell grid";
+                    return 1;
+                }
+                order.push_back({(uint32_t)(cy + cx * hs.ncy), i});
+            }
+            std::sort(order.begin(), order.end());
+            if ((rc = alloc(&W_.r, nw_, err)) || (rc = alloc(&W_.loc, nw_, err)) ||
+                (rc = alloc(&W_.key, nw_, err)) || (rc = alloc(&W_.id, nw_, err)) ||
+                (rc = alloc(&W_.rho, nw_, err)) || (rc = alloc(&W_.drho, nw_, err)) ||
+                (rc = alloc(&W_.p, nw_, err)) || (rc = alloc(&W_.rho_o, nw_, err)) ||
+                (rc = alloc(&W_.gnr, nw_, err)) || (rc = alloc(&W_.gkey, nw_, err)) ||
+                (rc = alloc(&W_.gloc, nw_, err)) || (rc = alloc(&W_.gnd, nw_, err)) ||
+                (rc = alloc(&wall_zero_v_, nw_, err)))
+                return rc;
+            TSPH_CK(cudaMemset(wall_zero_v_, 0, sizeof(T2) * std::max(nw_, 1)));
+            std::vector<double2> r(nw_), g(nw_);
+            std::vector<float2> loc(nw_), gloc(nw_);
+            std::vector<uint32_t> key(nw_), id(nw_), gkey(nw_);
+            std::vector<T> rho(nw_), zero(nw_, T(0)), p(nw_);
+            std::vector<T2> gnd(nw_);
+            std::vector<uint32_t> ws(ncells_ + 1, 0u);
+            for (int k = 0; k < nw_; k++) {
+                const int i = order[k].second;
+                const uint32_t c = order[k].first;
+                const int cx = (int)(c / hs.ncy), cy = (int)(c % hs.ncy);
+                const double x = hs.r[2 * i], y = hs.r[2 * i + 1];
+                r[k] = make_double2(x, y);
+                key[k] = c;
+                id[k] = (uint32_t)i;
+                loc[k] = make_float2((float)(x - hs.ox[cx]), (float)(y - hs.oy[cy]));
+                rho[k] = rho_stored_from_full<T>(hs.rho[i], hs.rho0);
+                zero[k] = (T)hs.drho[i];
+                p[k] = (T)hs.p[i];
+                ws[c + 1]++;
+                const double gx = hs.has_gnr[i] ? hs.gnr[2 * i] : x;
+                const double gy = hs.has_gnr[i] ? hs.gnr[2 * i + 1] : y;
+                g[k] = make_double2(gx, gy);
+                const int gcx = cell_of(gx, hs.bx), gcy = cell_of(gy, hs.by);
+                if (gcx < 0 || gcy < 0 || gcx >= hs.ncx || gcy >= hs.ncy || !hs.has_gnr[i]) {
+                    gkey[k] = (uint32_t)ncells_;
+                    gloc[k] = make_float2(0.f, 0.f);
+                } else {
+                    gkey[k] = (uint32_t)(gcy + gcx * hs.ncy);
+                    gloc[k] = make_float2((float)(gx - hs.ox[gcx]), (float)(gy - hs.oy[gcy]));
+                }
+                gnd[k].x = (T)(x - gx);
+                gnd[k].y = (T)(y - gy);
+            }
+            for (int c = 0; c < ncells_; c++) ws[c + 1] += ws[c];
+            if (nw_ > 0) {
+                TSPH_CK(cudaMemcpy(W_.r, r.data(), 16 * (size_t)nw_, cudaMemcpyHostToDevice));
+                TSPH_CK(cudaMemcpy(W_.loc, loc.data(), 8 * (size_t)nw_, cudaMemcpyHostToDevice));
+                TSPH_CK(cudaMemcpy(W_.key, key.data(), 4 * (size_t)nw_, cudaMemcpyHostToDevice));
+                TSPH_CK(cudaMemcpy(W_.id, id.data(), 4 * (size_t)nw_, cudaMemcpyHostToDevice));
+                TSPH_CK(cudaMemcpy(W_.rho, rho.data(), sizeof(T) * nw_, cudaMemcpyHostToDevice));
+                TSPH_CK(cudaMemcpy(W_.rho_o, rho.data(), sizeof(T) * nw_, cudaMemcpyHostToDevice));
+                TSPH_CK(cudaMemcpy(W_.drho, zero.data(), sizeof(T) * nw_, cudaMemcpyHostToDevice));
+                TSPH_CK(cudaMemcpy(W_.p, p.data(), sizeof(T) * nw_, cudaMemcpyHostToDevice));
+                TSPH_CK(cudaMemcpy(W_.gnr, g.data(), 16 * (size_t)nw_, cudaMemcpyHostToDevice));
+                TSPH_CK(cudaMemcpy(W_.gkey, gkey.data(), 4 * (size_t)nw_, cudaMemcpyHostToDevice));
+                TSPH_CK(cudaMemcpy(W_.gloc, gloc.data(), 8 * (size_t)nw_, cudaMemcpyHostToDevice));
+                TSPH_CK(cudaMemcpy(W_.gnd, gnd.data(), sizeof(T2) * nw_, cudaMemcpyHostToDevice));
+            }
+            TSPH_CK(cudaMemcpy(wstart_, ws.data(), 4 * ws.size(), cudaMemcpyHostToDevice));
+        }
+        TSPH_CK(cudaDeviceSynchronize());
+        cells_ = false;
+        return 0;
+    }
+
+    bool cells_valid() const override { return cells_; }
+    void invalidate_cells() override { cells_ = false; }
+
+    int particle_to_cell(std::string &err) override {
+        int rc;
+        if ((rc = zero_counts(err))) return rc;
+        const int *nptr = reinterpret_cast<const int *>(fstart_ + ncells_);
+        if ((rc = launch(CAT_SORT, k_bin_keep_dead, blocks_for(nf_), kBlock, err,
+                         (const double2 *)F_.r, (const uint32_t *)F_.key, nptr, grid_, keyB_, slotB_,
+                         counts_, health_)))
+            return rc;
+        // gather everything into Fs_ (+ old state into B), then copy back
+        if ((rc = sort_finish(F_.r, F_.v, F_.rho, F_.id, F_.a, F_.drho, F_.p, Fs_, O_.r, O_.v,
+                              O_.rho, OldState<T>{Br_, Bv_, Brho_}, err)))
+            return rc;
+        const size_t n = (size_t)nf_;
+        TSPH_CK(cudaMemcpyAsync(F_.r, Fs_.r, 16 * n, cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(F_.v, Fs_.v, sizeof(T2) * n, cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(F_.a, Fs_.a, sizeof(T2) * n, cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(F_.rho, Fs_.rho, sizeof(T) * n, cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(F_.drho, Fs_.drho, sizeof(T) * n, cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(F_.p, Fs_.p, sizeof(T) * n, cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(F_.id, Fs_.id, 4 * n, cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(F_.key, Fs_.key, 4 * n, cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(F_.loc, Fs_.loc, 8 * n, cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(O_.r, Br_, 16 * n, cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(O_.v, Bv_, sizeof(T2) * n, cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(O_.rho, Brho_, sizeof(T) * n, cudaMemcpyDeviceToDevice, st_));
+        cells_ = true;
+        return collect_profile(err);
+    }
+
+    int density_to_pressure(std::string &err) override {
+        int rc = launch(CAT_OTHER, k_eos<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                        (const uint32_t *)fstart_, ncells_, W_, nw_, P_, health_);
+        if (rc) return rc;
+        return collect_profile(err);
+    }
+
+    int mdbc_density(std::string &err) override {
+        if (!cells_) {
+            err = "cell lists are stale: call tsph_particle_to_cell first";
+            return 3;
+        }
+        int rc = do_mdbc(err);
+        if (rc) return rc;
+        return collect_profile(err);
+    }
+
+    int compute_forces(int model, std::string &err) override {
+        if (!cells_) {
+            err = "cell lists are stale: call tsph_particle_to_cell first";
+            return 3;
+        }
+        int rc;
+        if ((rc = launch(CAT_PAIR, k_fluid_pairs<T, MODE_FORCES>, blocks_for(nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, (const uint32_t *)wstart_,
+                         nbr_fluid(F_, true), nbr_walls(true), grid_, P_, O_, T(0), PairOut{},
+                         health_, (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
+                         (const uint32_t *)nullptr)))
+            return rc;
+        if (model == 1 && nw_ > 0 &&
+            (rc = launch(CAT_PAIR, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
+                         (const uint32_t *)fstart_, nbr_fluid(F_, true), grid_, P_, true, false, T(0),
+                         (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
+                         (const uint32_t *)nullptr, false)))
+            return rc;
+        return collect_profile(err);
+    }
+
+    int predictor(double dt, std::string &err) override {
+        int rc = launch(CAT_OTHER, k_predict_inplace<T>, blocks_for(nw_ + nf_), kBlock, err, F_, O_,
+                        (const uint32_t *)fstart_, ncells_, W_, nw_, (T)dt);
+        if (rc) return rc;
+        cells_ = false;
+        return collect_profile(err);
+    }
+
+    int corrector(double dt, std::string &err) override {
+        int rc = launch(CAT_OTHER, k_correct_inplace<T>, blocks_for(nw_ + nf_), kBlock, err, F_, O_,
+                        (const uint32_t *)fstart_, ncells_, W_, nw_, (T)dt, P_.rho0);
+        if (rc) return rc;
+        cells_ = false;
+        return collect_profile(err);
+    }
+
+    int remove_out_of_domain(int *removed, std::string &err) override {
+        TSPH_CK(cudaMemsetAsync(removed_, 0, 4, st_));
+        int rc = launch(CAT_OTHER, k_remove<T>, blocks_for(nf_), kBlock, err, F_,
+                        (const uint32_t *)fstart_, ncells_, box_, removed_, health_);
+        if (rc) return rc;
+        uint32_t h = 0;
+        TSPH_CK(cudaMemcpyAsync(&h, removed_, 4, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        if (removed) *removed = (int)h;
+        if (h) cells_ = false;
+        return collect_profile(err);
+    }
+
+    int step(int model, double dt, int nsteps, std::string &err) override {
+        if (!cells_) {
+            err = "cell lists are stale: call tsph_particle_to_cell first";
+            return 3;
+        }
+        int rc;
+        if (prof_) {
+            for (int s = 0; s < nsteps; s++)
+                if ((rc = enqueue_step(model, (T)dt, err))) return rc;
+        } else {
+            long long bits;
+            std::memcpy(&bits, &dt, 8);
+            auto key = std::make_pair(model, bits);
+            auto it = graphs_.find(key);
+            if (it == graphs_.end()) {
+                cudaGraph_t g;
+                TSPH_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+                rc = enqueue_step(model, (T)dt, err);
+                cudaGraph_t g2 = nullptr;
+                cudaError_t e = cudaStreamEndCapture(st_, &g2);
+                if (rc) {
+                    if (g2) cudaGraphDestroy(g2);
+                    return rc;
+                }
+                if (e != cudaSuccess) {
+                    err = std::string("cudaStreamEndCapture: ") + cudaGetErrorString(e);
+                    return 2;
+                }
+                g = g2;
+                cudaGraphExec_t ex;
+                e = cudaGraphInstantiate(&ex, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    err = std::string("cudaGraphInstantiate: ") + cudaGetErrorString(e);
+                    return 2;
+                }
+                it = graphs_.emplace(key, ex).first;
+            }
+            for (int s = 0; s < nsteps; s++) TSPH_CK(cudaGraphLaunch(it->second, st_));
+        }
+        // the reference's state after a step holds p = EOS(rho) (step body :110-111)
+        if ((rc = launch(CAT_OTHER, k_eos<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, ncells_, W_, nw_, P_, health_)))
+            return rc;
+        cells_ = true;
+        return collect_profile(err);
+    }
+
+    int np_live(int *np, std::string &err) override {
+        uint32_t nl = 0, rm = 0;
+        TSPH_CK(cudaMemcpyAsync(&nl, fstart_ + ncells_, 4, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        // particles marked by tsph_remove_out_of_domain but not yet re-binned
+        if (!cells_) {
+            std::vector<uint32_t> key(nl);
+            if (nl) TSPH_CK(cudaMemcpy(key.data(), F_.key, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
+            for (uint32_t k : key) rm += (k == (uint32_t)ncells_);
+        }
+        *np = (int)(nl - rm) + nw_;
+        return 0;
+    }
+
+    int download(int mask, double *r, double *v, double *a, double *rho, double *drho, double *p,
+                 int32_t *index, int32_t *type, std::string &err) override {
+        TSPH_CK(cudaMemsetAsync(S_.alive, 0, ntot_, st_));
+        int rc = launch(CAT_OTHER, k_export<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                        (const uint32_t *)fstart_, ncells_, W_, nw_, P_.rho0, S_, mask & 63);
+        if (rc) return rc;
+        std::vector<uint8_t> alive(ntot_);
+        TSPH_CK(cudaMemcpyAsync(alive.data(), S_.alive, ntot_, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        int nlive = 0;
+        for (int i = 0; i < ntot_; i++) nlive += alive[i];
+        const bool dense = nlive == ntot_;
+        std::vector<double> tmp;
+        auto fetch = [&](int bit, const void *src, double *dst, int width) -> int {
+            if (!(mask & bit) || !dst) return 0;
+            if (dense) {
+                TSPH_CK(cudaMemcpyAsync(dst, src, 8 * (size_t)width * ntot_, cudaMemcpyDeviceToHost, st_));
+                return 0;
+            }
+            tmp.resize((size_t)width * ntot_);
+            TSPH_CK(cudaMemcpyAsync(tmp.data(), src, 8 * (size_t)width * ntot_, cudaMemcpyDeviceToHost, st_));
+            TSPH_CK(cudaStreamSynchronize(st_));
+            size_t o = 0;
+            for (int i = 0; i < ntot_; i++)
+                if (alive[i]) {
+                    for (int w = 0; w < width; w++) dst[o * width + w] = tmp[(size_t)i * width + w];
+                    o++;
+                }
+            return 0;
+        };
+        if ((rc = fetch(1, S_.r, r, 2)) || (rc = fetch(2, S_.v, v, 2)) || (rc = fetch(4, S_.a, a, 2)) ||
+            (rc = fetch(8, S_.rho, rho, 1)) || (rc = fetch(16, S_.drho, drho, 1)) ||
+            (rc = fetch(32, S_.p, p, 1)))
+            return rc;
+        TSPH_CK(cudaStreamSynchronize(st_));
+        if ((mask & 64) && index) {
+            int o = 0;
+            for (int i = 0; i < ntot_; i++)
+                if (alive[i]) index[o++] = i;
+        }
+        (void)type;  // filled by the caller from its host copy
+        return collect_profile(err);
+    }
+
+    int upload(int mask, const double *r, const double *v, const double *a, const double *rho,
+               const double *drho, const double *p, std::string &err) override {
+        // alive map from the device
+        TSPH_CK(cudaMemsetAsync(S_.alive, 0, ntot_, st_));
+        int rc = launch(CAT_OTHER, k_export<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                        (const uint32_t *)fstart_, ncells_, W_, nw_, P_.rho0, S_, 0);
+        if (rc) return rc;
+        std::vector<uint8_t> alive(ntot_);
+        TSPH_CK(cudaMemcpyAsync(alive.data(), S_.alive, ntot_, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        int nlive = 0;
+        for (int i = 0; i < ntot_; i++) nlive += alive[i];
+        const bool dense = nlive == ntot_;
+        std::vector<double> tmp;
+        auto put = [&](int bit, void *dst, const double *src, int width) -> int {
+            if (!(mask & bit) || !src) return 0;
+            if (dense) {
+                TSPH_CK(cudaMemcpyAsync(dst, src, 8 * (size_t)width * ntot_, cudaMemcpyHostToDevice, st_));
+                return 0;
+            }
+            tmp.assign((size_t)width * ntot_, 0.0);
+            size_t o = 0;
+            for (int i = 0; i < ntot_; i++)
+                if (alive[i]) {
+                    for (int w = 0; w < width; w++) tmp[(size_t)i * width + w] = src[o * width + w];
+                    o++;
+                }
+            TSPH_CK(cudaMemcpyAsync(dst, tmp.data(), 8 * (size_t)width * ntot_, cudaMemcpyHostToDevice, st_));
+            TSPH_CK(cudaStreamSynchronize(st_));
+            return 0;
+        };
+        if ((rc = put(1, S_.r, r, 2)) || (rc = put(2, S_.v, v, 2)) || (rc = put(4, S_.a, a, 2)) ||
+            (rc = put(8, S_.rho, rho, 1)) || (rc = put(16, S_.drho, drho, 1)) ||
+            (rc = put(32, S_.p, p, 1)))
+            return rc;
+        // walls keep r and v (static); only fluid rows take them
+        if ((rc = launch(CAT_OTHER, k_import<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, ncells_, W_, nw_, P_.rho0, S_, mask & 63)))
+            return rc;
+        TSPH_CK(cudaStreamSynchronize(st_));
+        if (mask & 1) cells_ = false;
+        return collect_profile(err);
+    }
+
+    int get_cells(int32_t *cell_start, int32_t *cell_list, std::string &err) override {
+        if (!cells_) {
+            err = "cell lists are stale: call tsph_particle_to_cell first";
+            return 3;
+        }
+        TSPH_CK(cudaStreamSynchronize(st_));
+        std::vector<uint32_t> fs(ncells_ + 2), ws(ncells_ + 1), fid(nf_), wid(nw_);
+        TSPH_CK(cudaMemcpy(fs.data(), fstart_, 4 * fs.size(), cudaMemcpyDeviceToHost));
+        TSPH_CK(cudaMemcpy(ws.data(), wstart_, 4 * ws.size(), cudaMemcpyDeviceToHost));
+        if (nf_) TSPH_CK(cudaMemcpy(fid.data(), F_.id, 4 * (size_t)nf_, cudaMemcpyDeviceToHost));
+        if (nw_) TSPH_CK(cudaMemcpy(wid.data(), W_.id, 4 * (size_t)nw_, cudaMemcpyDeviceToHost));
+        // reference numbering: rank of the original index among live particles
+        std::vector<int> alive(ntot_, 0);
+        for (int c = 0; c < ncells_; c++)
+            for (uint32_t j = fs[c]; j < fs[c + 1]; j++) alive[fid[j]] = 1;
+        for (int w = 0; w < nw_; w++) alive[wid[w]] = 1;
+        std::vector<int> rank(ntot_, -1);
+        int o = 0;
+        for (int i = 0; i < ntot_; i++)
+            if (alive[i]) rank[i] = o++;
+        int acc = 0;
+        std::vector<int> tmp;
+        for (int c = 0; c < ncells_; c++) {
+            cell_start[c] = acc;
+            tmp.clear();
+            for (uint32_t j = ws[c]; j < ws[c + 1]; j++) tmp.push_back(rank[wid[j]]);
+            for (uint32_t j = fs[c]; j < fs[c + 1]; j++) tmp.push_back(rank[fid[j]]);
+            // walls and fluid are each ascending; merge
+            std::inplace_merge(tmp.begin(), tmp.begin() + (ws[c + 1] - ws[c]), tmp.end());
+            for (int x : tmp) cell_list[acc++] = x;
+        }
+        cell_start[ncells_] = acc;
+        return 0;
+    }
+
+    int pair_digest(int32_t *count, int64_t *sum, int32_t *xr, std::string &err) override {
+        if (!cells_) {
+            err = "cell lists are stale: call tsph_particle_to_cell first";
+            return 3;
+        }
+        int rc;
+        if (!dig_count_) {
+            if ((rc = alloc(&dig_count_, ntot_, err)) || (rc = alloc(&dig_sum_, ntot_, err)) ||
+                (rc = alloc(&dig_xor_, ntot_, err)))
+                return rc;
+        }
+        // fluid rows into [0, nf), wall rows into [nf, nf + nw)
+        if ((rc = launch(CAT_OTHER, k_fluid_pairs<T, MODE_DIGEST>, blocks_for(nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, (const uint32_t *)wstart_, nbr_fluid(F_, true),
+                         nbr_walls(true), grid_, P_, O_, T(0), PairOut{}, health_, dig_count_,
+                         dig_sum_, dig_xor_, (const uint32_t *)W_.id)))
+            return rc;
+        if (nw_ &&
+            (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
+                         (const uint32_t *)fstart_, nbr_fluid(F_, true), grid_, P_, true, false, T(0),
+                         dig_count_ + nf_, dig_sum_ + nf_, dig_xor_ + nf_, (const uint32_t *)F_.id,
+                         true)))
+            return rc;
+        TSPH_CK(cudaStreamSynchronize(st_));
+        uint32_t nl = 0;
+        TSPH_CK(cudaMemcpy(&nl, fstart_ + ncells_, 4, cudaMemcpyDeviceToHost));
+        std::vector<int32_t> c(nl + nw_), x(nl + nw_);
+        std::vector<long long> s(nl + nw_);
+        std::vector<uint32_t> fid(nl), wid(nw_);
+        if (nl) {
+            TSPH_CK(cudaMemcpy(c.data(), dig_count_, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
+            TSPH_CK(cudaMemcpy(s.data(), dig_sum_, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
+            TSPH_CK(cudaMemcpy(x.data(), dig_xor_, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
+            TSPH_CK(cudaMemcpy(fid.data(), F_.id, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
+        }
+        if (nw_) {
+            TSPH_CK(cudaMemcpy(c.data() + nl, dig_count_ + nf_, 4 * (size_t)nw_, cudaMemcpyDeviceToHost));
+            TSPH_CK(cudaMemcpy(s.data() + nl, dig_sum_ + nf_, 8 * (size_t)nw_, cudaMemcpyDeviceToHost));
+            TSPH_CK(cudaMemcpy(x.data() + nl, dig_xor_ + nf_, 4 * (size_t)nw_, cudaMemcpyDeviceToHost));
+            TSPH_CK(cudaMemcpy(wid.data(), W_.id, 4 * (size_t)nw_, cudaMemcpyDeviceToHost));
+        }
+        // rows in ascending original index
+        std::vector<std::pair<uint32_t, int>> rows;
+        for (uint32_t j = 0; j < nl; j++) rows.push_back({fid[j], (int)j});
+        for (int w = 0; w < nw_; w++) rows.push_back({wid[w], (int)nl + w});
+        std::sort(rows.begin(), rows.end());
+        for (size_t k = 0; k < rows.size(); k++) {
+            count[k] = c[rows[k].second];
+            sum[k] = s[rows[k].second];
+            xr[k] = x[rows[k].second];
+        }
+        return 0;
+    }
+
+    int health(uint32_t *flags, int clear, std::string &err) override {
+        TSPH_CK(cudaMemcpyAsync(flags, health_, 4, cudaMemcpyDeviceToHost, st_));
+        if (clear) TSPH_CK(cudaMemsetAsync(health_, 0, 4, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        return 0;
+    }
+
+    int totals(double out[4], std::string &err) override {
+        const int nb = blocks_for(nf_);
+        int rc = launch(CAT_OTHER, k_totals<T>, nb, kBlock, err, F_, (const uint32_t *)fstart_,
+                        ncells_, m64_, dtot_);
+        if (rc) return rc;
+        std::vector<double> h(4 * (size_t)nb);
+        TSPH_CK(cudaMemcpyAsync(h.data(), dtot_, 8 * h.size(), cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        for (int q = 0; q < 4; q++) out[q] = 0;
+        for (int b = 0; b < nb; b++)
+            for (int q = 0; q < 4; q++) out[q] += h[(size_t)b * 4 + q];
+        return collect_profile(err);
+    }
+
+    int sync(std::string &err) override {
+        TSPH_CK(cudaStreamSynchronize(st_));
+        return collect_profile(err);
+    }
+
+    void set_profiling(bool on) override { prof_ = on; }
+    Profile profile(bool reset) override {
+        Profile p = acc_;
+        if (reset) acc_ = Profile{};
+        return p;
+    }
+};
+
+}  // namespace tsph

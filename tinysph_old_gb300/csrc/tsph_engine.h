@@ -1,0 +1,71 @@
+// tsph_engine.h -- host-side interface between the C ABI (tsph_api.cpp) and
+// the precision-specific engines (tsph_engine_f32.cu / tsph_engine_f64.cu).
+#pragma once
+
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace tsph {
+
+// Everything the device side needs, prepared on the host.
+struct HostSetup {
+    // SPH_constants (src/SPH_data.h:124-140)
+    double h, kap, cs, rho0, visco, delta, dp, m, g;
+    // Simulation_data (padded domain)
+    double x0, xm, y0, ym;
+    // grid (Divide_To_Cells, src/SPH_find_pairs.h:5-42)
+    double kh, of;
+    int ncx, ncy;
+    std::vector<long long> bx, by;  // ordered-int64 lower bounds of each cell index, n+1
+    std::vector<double> ox, oy;     // cell origins
+    // particles in the reference's order
+    std::vector<int> type;
+    std::vector<double> r, v, a, rho, drho, p, gnr;  // r, v, a, gnr interleaved (x, y)
+    std::vector<uint8_t> has_gnr;
+};
+
+struct Profile {
+    double us[4] = {0, 0, 0, 0};
+    int launches[4] = {0, 0, 0, 0};
+};
+
+enum { CAT_PAIR = 0, CAT_SORT = 1, CAT_MDBC = 2, CAT_OTHER = 3 };
+
+class EngineBase {
+  public:
+    virtual ~EngineBase() {}
+    // all calls return a TSPH_* status and set `err` on failure
+    virtual int init(const HostSetup &hs, void *stream, std::string &err) = 0;
+    virtual int particle_to_cell(std::string &err) = 0;
+    virtual int density_to_pressure(std::string &err) = 0;
+    virtual int mdbc_density(std::string &err) = 0;
+    virtual int compute_forces(int model, std::string &err) = 0;
+    virtual int predictor(double dt, std::string &err) = 0;
+    virtual int corrector(double dt, std::string &err) = 0;
+    virtual int remove_out_of_domain(int *removed, std::string &err) = 0;
+    virtual int step(int model, double dt, int nsteps, std::string &err) = 0;
+    // state in the reference's order: the engine fills per-index staging and
+    // reports which indices are alive (removed particles are not)
+    virtual int download(int mask, double *r, double *v, double *a, double *rho, double *drho,
+                         double *p, int32_t *index, int32_t *type, std::string &err) = 0;
+    virtual int upload(int mask, const double *r, const double *v, const double *a,
+                       const double *rho, const double *drho, const double *p,
+                       std::string &err) = 0;
+    virtual int get_cells(int32_t *cell_start, int32_t *cell_list, std::string &err) = 0;
+    virtual int pair_digest(int32_t *count, int64_t *sum, int32_t *xr, std::string &err) = 0;
+    virtual int np_live(int *np, std::string &err) = 0;
+    virtual int health(uint32_t *flags, int clear, std::string &err) = 0;
+    virtual int totals(double out[4], std::string &err) = 0;
+    virtual int sync(std::string &err) = 0;
+    virtual void set_profiling(bool on) = 0;
+    virtual Profile profile(bool reset) = 0;
+    virtual bool cells_valid() const = 0;
+    virtual void invalidate_cells() = 0;
+};
+
+EngineBase *make_engine_f32();
+EngineBase *make_engine_f64();
+
+}  // namespace tsph

@@ -1,0 +1,381 @@
+"""Python front-end of the C ABI (``include/tsph.h``), shaped like the
+reference's interface: a particle system object plus free functions named
+after the reference functions they replace (``Divide_To_Cells``,
+``Particle_To_Cell``, ``Compute_Forces``, ...).
+
+There is no fallback: if ``libtsph.so`` cannot be loaded (or built) every
+call raises, and every non-zero status of the library raises
+:class:`TsphError`.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+# status codes (tsph.h)
+OK, ERR_ARG, ERR_CUDA, ERR_STATE, ERR_NOMEM, ERR_NUMERIC, ERR_DENSITY, ERR_ESCAPED, \
+    ERR_UNSUPPORTED = range(9)
+FLUID, WALL = 0, 1
+WALL_MDBC, WALL_DBC = 0, 1
+PREC_FP32, PREC_FP64 = 0, 1
+F_R, F_V, F_A, F_RHO, F_DRHO, F_P, F_INDEX, F_TYPE = (1 << k for k in range(8))
+F_ALL = F_R | F_V | F_A | F_RHO | F_DRHO | F_P | F_INDEX | F_TYPE
+HEALTH_NAN, HEALTH_DENSITY, HEALTH_ESCAPED, HEALTH_REMOVED = 1, 2, 4, 8
+
+# the C entry points declared in include/tsph.h
+ABI_SYMBOLS = (
+    "tsph_abi_version", "tsph_last_error", "tsph_status_string", "tsph_device_count",
+    "tsph_create", "tsph_destroy", "tsph_add_particles", "tsph_np", "tsph_grid",
+    "tsph_particle_mass", "tsph_divide_to_cells", "tsph_clear_cells", "tsph_particle_to_cell",
+    "tsph_get_cells", "tsph_pair_digest", "tsph_grid_tables", "tsph_density_to_pressure", "tsph_mdbc_density",
+    "tsph_compute_forces", "tsph_symplectic_predictor", "tsph_symplectic_corrector",
+    "tsph_remove_out_of_domain", "tsph_step", "tsph_download", "tsph_upload", "tsph_sync",
+    "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
+)
+
+
+class TsphError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"tsph status {status}: {message}")
+        self.status = status
+
+
+class _Constants(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("h", "kap", "cs", "rho0", "visco", "delta", "dp")]
+
+
+class _Domain(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("x_0", "x_m", "y_0", "y_m")]
+
+
+class _HostState(C.Structure):
+    _fields_ = [("r", C.c_void_p), ("v", C.c_void_p), ("a", C.c_void_p), ("rho", C.c_void_p),
+                ("drho", C.c_void_p), ("p", C.c_void_p), ("index", C.c_void_p),
+                ("type", C.c_void_p)]
+
+
+class _Profile(C.Structure):
+    _fields_ = [("pair_us", C.c_double), ("pair_launches", C.c_int),
+                ("sort_us", C.c_double), ("sort_launches", C.c_int),
+                ("mdbc_us", C.c_double), ("mdbc_launches", C.c_int),
+                ("other_us", C.c_double), ("other_launches", C.c_int)]
+
+
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Load ``libtsph.so`` (building it with nvcc if it is missing or stale)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        _build.build()
+    if not os.path.exists(_build.LIB):
+        raise RuntimeError(f"{_build.LIB} is missing: run tinysph_old_gb300/build.py")
+    L = C.CDLL(_build.LIB)
+    P, I, D = C.c_void_p, C.c_int, C.c_double
+    L.tsph_abi_version.restype = I
+    L.tsph_last_error.restype = C.c_char_p
+    L.tsph_status_string.restype = C.c_char_p
+    L.tsph_status_string.argtypes = [I]
+    L.tsph_device_count.argtypes = [C.POINTER(I)]
+    L.tsph_create.argtypes = [C.POINTER(_Constants), C.POINTER(_Domain), I, P, C.POINTER(P)]
+    L.tsph_destroy.argtypes = [P]
+    L.tsph_add_particles.argtypes = [P, I, P, P, P, P, P, P]
+    L.tsph_np.argtypes = [P, C.POINTER(I)]
+    L.tsph_grid.argtypes = [P, C.POINTER(I), C.POINTER(I)]
+    L.tsph_particle_mass.argtypes = [P, C.POINTER(D)]
+    for f in ("tsph_divide_to_cells", "tsph_clear_cells", "tsph_particle_to_cell",
+              "tsph_density_to_pressure", "tsph_mdbc_density", "tsph_sync"):
+        getattr(L, f).argtypes = [P]
+    L.tsph_get_cells.argtypes = [P, P, P]
+    L.tsph_pair_digest.argtypes = [P, P, P, P]
+    L.tsph_grid_tables.argtypes = [C.POINTER(_Constants), C.POINTER(_Domain), C.POINTER(I),
+                                   C.POINTER(I), P, P]
+    L.tsph_compute_forces.argtypes = [P, I]
+    L.tsph_symplectic_predictor.argtypes = [P, D]
+    L.tsph_symplectic_corrector.argtypes = [P, D]
+    L.tsph_remove_out_of_domain.argtypes = [P, C.POINTER(I)]
+    L.tsph_step.argtypes = [P, I, D, I]
+    L.tsph_download.argtypes = [P, I, C.POINTER(_HostState)]
+    L.tsph_upload.argtypes = [P, I, C.POINTER(_HostState)]
+    L.tsph_health.argtypes = [P, C.POINTER(C.c_uint32), I]
+    L.tsph_fluid_totals.argtypes = [P, P]
+    L.tsph_set_profiling.argtypes = [P, I]
+    L.tsph_get_profile.argtypes = [P, C.POINTER(_Profile), I]
+    _lib = L
+    return L
+
+
+def device_count() -> int:
+    n = C.c_int(0)
+    load().tsph_device_count(C.byref(n))
+    return n.value
+
+
+def grid_tables(h, kap, domain):
+    """Host-only: (ncx, ncy, bx, by) of ``tsph_grid_tables`` (no GPU needed)."""
+    L = load()
+    c = _Constants(h, kap, 1.0, 1000.0, 0.0, 0.0, h)
+    d = _Domain(*domain)
+    ncx, ncy = C.c_int(), C.c_int()
+    _check(L.tsph_grid_tables(C.byref(c), C.byref(d), C.byref(ncx), C.byref(ncy), None, None))
+    bx = np.empty(ncx.value + 1, dtype=np.int64)
+    by = np.empty(ncy.value + 1, dtype=np.int64)
+    _check(L.tsph_grid_tables(C.byref(c), C.byref(d), C.byref(ncx), C.byref(ncy), _p(bx), _p(by)))
+    return ncx.value, ncy.value, bx, by
+
+
+def _check(rc: int):
+    if rc != OK:
+        msg = load().tsph_last_error().decode(errors="replace")
+        raise TsphError(rc, msg)
+
+
+def _p(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)
+
+
+class ParticleSystem:
+    """``Particle_system`` + ``Simulation_data`` on the GPU (src/SPH_particle_system.h,
+    src/SPH_data.h).  ``precision`` is ``"fp32"`` (FP32 pair math, FP64
+    positions) or ``"fp64"``."""
+
+    def __init__(self, h, kap, cs, rho0, visco, delta, dp, domain, precision="fp32",
+                 stream=None):
+        L = load()
+        self._L = L
+        c = _Constants(h, kap, cs, rho0, visco, delta, dp)
+        d = _Domain(*domain)
+        prec = {"fp32": PREC_FP32, "fp64": PREC_FP64}[precision]
+        h_ = C.c_void_p()
+        _check(L.tsph_create(C.byref(c), C.byref(d), prec, stream, C.byref(h_)))
+        self._h = h_
+        self.precision = precision
+        self.domain = tuple(domain)
+
+    @classmethod
+    def from_case(cls, case, precision="fp32", divide=True, bin_particles=True):
+        """Build a system from a :class:`tinysph_old_gb300.cases.Case` (INIT of the
+        reference drivers: add particles, Divide_To_Cells, Particle_To_Cell)."""
+        s = cls(case.h, case.kap, case.cs, case.rho0, case.visco, case.delta, case.dp,
+                case.domain, precision)
+        a = case.particles.arrays()
+        gnr = np.zeros((case.np, 2))
+        gn = a["gnr"]
+        if len(gn):
+            # the reference indexes gnr by particle index (walls first)
+            gnr[:len(gn)] = gn
+        s.add_particles(a["type"], a["r"], a["v"], a["rho"], a["p"], gnr if len(gn) else None)
+        if divide:
+            s.divide_to_cells()
+            if bin_particles:
+                s.particle_to_cell()
+        return s
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.tsph_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    # ---- particles
+    def add_particles(self, ptype, r, v=None, rho=None, p=None, gnr=None):
+        n = len(ptype)
+        t = np.ascontiguousarray(ptype, dtype=np.int32)
+        r = np.ascontiguousarray(r, dtype=np.float64).reshape(n, 2)
+        v = None if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(n, 2)
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        p = None if p is None else np.ascontiguousarray(p, dtype=np.float64)
+        g = None if gnr is None else np.ascontiguousarray(gnr, dtype=np.float64).reshape(n, 2)
+        _check(self._L.tsph_add_particles(self._h, n, _p(t), _p(r), _p(v), _p(rho), _p(p), _p(g)))
+
+    @property
+    def np(self) -> int:
+        n = C.c_int()
+        _check(self._L.tsph_np(self._h, C.byref(n)))
+        return n.value
+
+    def grid(self):
+        a, b = C.c_int(), C.c_int()
+        _check(self._L.tsph_grid(self._h, C.byref(a), C.byref(b)))
+        return a.value, b.value
+
+    @property
+    def mass(self) -> float:
+        m = C.c_double()
+        _check(self._L.tsph_particle_mass(self._h, C.byref(m)))
+        return m.value
+
+    # ---- find pairs
+    def divide_to_cells(self):
+        _check(self._L.tsph_divide_to_cells(self._h))
+
+    def clear_cells(self):
+        _check(self._L.tsph_clear_cells(self._h))
+
+    def particle_to_cell(self):
+        _check(self._L.tsph_particle_to_cell(self._h))
+
+    def get_cells(self):
+        ncx, ncy = self.grid()
+        start = np.empty(ncx * ncy + 1, dtype=np.int32)
+        lst = np.empty(max(self.np, 1), dtype=np.int32)
+        _check(self._L.tsph_get_cells(self._h, _p(start), _p(lst)))
+        return start, lst[:start[-1]]
+
+    def pair_digest(self):
+        n = self.np
+        cnt = np.empty(n, dtype=np.int32)
+        sm = np.empty(n, dtype=np.int64)
+        xr = np.empty(n, dtype=np.int32)
+        _check(self._L.tsph_pair_digest(self._h, _p(cnt), _p(sm), _p(xr)))
+        return cnt, sm, xr
+
+    # ---- physics
+    def density_to_pressure(self):
+        _check(self._L.tsph_density_to_pressure(self._h))
+
+    def mdbc_density(self):
+        _check(self._L.tsph_mdbc_density(self._h))
+
+    def compute_forces(self, wall_model=WALL_MDBC):
+        _check(self._L.tsph_compute_forces(self._h, int(wall_model)))
+
+    def predictor(self, dt):
+        _check(self._L.tsph_symplectic_predictor(self._h, float(dt)))
+
+    def corrector(self, dt):
+        _check(self._L.tsph_symplectic_corrector(self._h, float(dt)))
+
+    def remove_out_of_domain(self) -> int:
+        n = C.c_int()
+        _check(self._L.tsph_remove_out_of_domain(self._h, C.byref(n)))
+        return n.value
+
+    def step(self, wall_model, dt, nsteps=1):
+        _check(self._L.tsph_step(self._h, int(wall_model), float(dt), int(nsteps)))
+
+    # ---- state
+    def download(self, fields=F_ALL, out=None):
+        """State in the reference's order as a dict of numpy arrays."""
+        n = self.np
+        res = {} if out is None else out
+        spec = [(F_R, "r", (n, 2), np.float64), (F_V, "v", (n, 2), np.float64),
+                (F_A, "a", (n, 2), np.float64), (F_RHO, "rho", (n,), np.float64),
+                (F_DRHO, "drho", (n,), np.float64), (F_P, "p", (n,), np.float64),
+                (F_INDEX, "index", (n,), np.int32), (F_TYPE, "type", (n,), np.int32)]
+        hs = _HostState()
+        for bit, name, shape, dt in spec:
+            if fields & bit:
+                if name not in res:
+                    res[name] = np.empty(shape, dtype=dt)
+                setattr(hs, name, res[name].ctypes.data)
+        _check(self._L.tsph_download(self._h, int(fields), C.byref(hs)))
+        return res
+
+    def upload(self, **fields):
+        hs = _HostState()
+        mask = 0
+        keep = []
+        bits = dict(r=F_R, v=F_V, a=F_A, rho=F_RHO, drho=F_DRHO, p=F_P)
+        for name, arr in fields.items():
+            if arr is None:
+                continue
+            a = np.ascontiguousarray(arr, dtype=np.float64)
+            keep.append(a)
+            setattr(hs, name, a.ctypes.data)
+            mask |= bits[name]
+        _check(self._L.tsph_upload(self._h, mask, C.byref(hs)))
+
+    def upload_ptrs(self, mask, **ptrs):
+        """Upload from raw host pointers (e.g. pinned buffers)."""
+        hs = _HostState()
+        for k, v in ptrs.items():
+            setattr(hs, k, v)
+        _check(self._L.tsph_upload(self._h, int(mask), C.byref(hs)))
+
+    def download_ptrs(self, mask, **ptrs):
+        hs = _HostState()
+        for k, v in ptrs.items():
+            setattr(hs, k, v)
+        _check(self._L.tsph_download(self._h, int(mask), C.byref(hs)))
+
+    def sync(self):
+        _check(self._L.tsph_sync(self._h))
+
+    def health(self, clear=False) -> int:
+        f = C.c_uint32()
+        _check(self._L.tsph_health(self._h, C.byref(f), 1 if clear else 0))
+        return f.value
+
+    def fluid_totals(self):
+        out = np.zeros(4)
+        _check(self._L.tsph_fluid_totals(self._h, _p(out)))
+        return dict(mass=out[0], ekin=out[1], px=out[2], py=out[3])
+
+    def set_profiling(self, on: bool):
+        _check(self._L.tsph_set_profiling(self._h, 1 if on else 0))
+
+    def profile(self, reset=True):
+        p = _Profile()
+        _check(self._L.tsph_get_profile(self._h, C.byref(p), 1 if reset else 0))
+        return {k: getattr(p, k) for k, _ in _Profile._fields_}
+
+
+# ---- free functions under the reference's names (src/*.h)
+def Divide_To_Cells(particles: ParticleSystem, simulation_data=None):
+    particles.divide_to_cells()
+
+
+def Clear_cells(particles: ParticleSystem):
+    particles.clear_cells()
+
+
+def Particle_To_Cell(particles: ParticleSystem, simulation_data=None):
+    particles.particle_to_cell()
+
+
+def Density_to_pressure(particles: ParticleSystem):
+    particles.density_to_pressure()
+
+
+def mDBC_compute_density_mdbcGeo(particles: ParticleSystem, simulation_data=None):
+    particles.mdbc_density()
+
+
+def Compute_Forces(particles: ParticleSystem, wall_model=WALL_MDBC):
+    particles.compute_forces(wall_model)
+
+
+def Integrate_SymplecticPredictor(particles: ParticleSystem, dt):
+    particles.predictor(dt)
+
+
+def Integrate_SymplecticCorrector(particles: ParticleSystem, dt):
+    particles.corrector(dt)
+
+
+def RemoveParticlesOutOfDomain(particles: ParticleSystem, simulation_data=None) -> int:
+    return particles.remove_out_of_domain()
