@@ -11,6 +11,7 @@
 
 #include "tsph_engine.h"
 #include "tsph_kernels.cuh"
+#include "tsph_pairs_tiled.cuh"
 
 namespace tsph {
 
@@ -187,8 +188,35 @@ template <typename T> class Engine final : public EngineBase {
 
     int do_mdbc(std::string &err) {
         if (nw_ == 0) return 0;
-        return launch(CAT_MDBC, k_mdbc<T>, blocks_for((long long)nw_ * 32), kBlock, err, W_, nw_,
-                      (const uint32_t *)fstart_, nbr_fluid(F_, false), grid_, P_);
+        if constexpr (std::is_same<T, float>::value)
+            return launch(CAT_MDBC, k_mdbc8, blocks_for((long long)nw_ * 8), kBlock, err, W_, nw_,
+                          (const uint32_t *)fstart_, F_, grid_, P_);
+        else
+            return launch(CAT_MDBC, k_mdbc<T>, blocks_for((long long)nw_ * 32), kBlock, err, W_,
+                          nw_, (const uint32_t *)fstart_, nbr_fluid(F_, false), grid_, P_);
+    }
+
+    TileConst K_{};
+
+    // the fluid-row pair pass: tiled FP32 kernel, or the plain FP64 kernel
+    template <int MODE>
+    int fluid_pairs(const FluidState<T> &X, bool stored_p, T dt, PairOut po, std::string &err) {
+        if constexpr (std::is_same<T, float>::value) {
+            const int nb = blocks_for(nf_, kTileT);
+            if (stored_p)
+                return launch(CAT_PAIR, k_pairs_tiled<MODE, true>, nb, kTileT, err, X,
+                              (const uint32_t *)fstart_, (const uint32_t *)wstart_, W_, grid_, P_,
+                              K_, O_, dt, po, health_);
+            return launch(CAT_PAIR, k_pairs_tiled<MODE, false>, nb, kTileT, err, X,
+                          (const uint32_t *)fstart_, (const uint32_t *)wstart_, W_, grid_, P_, K_,
+                          O_, dt, po, health_);
+        } else {
+            return launch(CAT_PAIR, k_fluid_pairs<T, MODE>, blocks_for(nf_), kBlock, err, X,
+                          (const uint32_t *)fstart_, (const uint32_t *)wstart_,
+                          nbr_fluid(X, stored_p), nbr_walls(stored_p), grid_, P_, O_, dt, po,
+                          health_, (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
+                          (const uint32_t *)nullptr);
+        }
     }
 
     // one fused step (enqueue only)
@@ -208,12 +236,7 @@ template <typename T> class Engine final : public EngineBase {
         // forces at the predicted state + corrector + bin
         if ((rc = zero_counts(err))) return rc;
         PairOut po{Br_, (void *)Bv_, (void *)Brho_, keyB_, slotB_, counts_, box_};
-        if ((rc = launch(CAT_PAIR, k_fluid_pairs<T, MODE_CORRECT>, blocks_for(nf_), kBlock, err, Fs_,
-                         (const uint32_t *)fstart_, (const uint32_t *)wstart_,
-                         nbr_fluid(Fs_, false), nbr_walls(false), grid_, P_, O_, dt, po, health_,
-                         (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
-                         (const uint32_t *)nullptr)))
-            return rc;
+        if ((rc = fluid_pairs<MODE_CORRECT>(Fs_, false, dt, po, err))) return rc;
         if (nw_ > 0 &&
             (rc = launch(CAT_PAIR, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
                          (const uint32_t *)fstart_, nbr_fluid(Fs_, false), grid_, P_, dbc, true, dt,
@@ -224,12 +247,7 @@ template <typename T> class Engine final : public EngineBase {
                               nullptr, nullptr, O_, err)))
             return rc;
         // forces at the new state (a, drho for the next predictor)
-        if ((rc = launch(CAT_PAIR, k_fluid_pairs<T, MODE_FORCES>, blocks_for(nf_), kBlock, err, F_,
-                         (const uint32_t *)fstart_, (const uint32_t *)wstart_,
-                         nbr_fluid(F_, false), nbr_walls(false), grid_, P_, O_, dt,
-                         PairOut{}, health_, (int32_t *)nullptr, (long long *)nullptr,
-                         (int32_t *)nullptr, (const uint32_t *)nullptr)))
-            return rc;
+        if ((rc = fluid_pairs<MODE_FORCES>(F_, false, dt, PairOut{}, err))) return rc;
         if (dbc && nw_ > 0 &&
             (rc = launch(CAT_PAIR, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
                          (const uint32_t *)fstart_, nbr_fluid(F_, false), grid_, P_, true, false, dt,
@@ -288,6 +306,7 @@ template <typename T> class Engine final : public EngineBase {
         P_.k_psi = (T)(2.0 * hs.cs * hs.h * hs.delta);
         P_.xg = (T)(hs.rho0 * hs.g / (hs.cs * hs.cs * hs.rho0 / 7.0));
         box_ = Box{hs.x0, hs.xm, hs.y0, hs.ym};
+        if constexpr (std::is_same<T, float>::value) K_ = make_tile_const(P_, hs.h, hs.rho0, hs.g, hs.cs);
         // grid tables
         int rc;
         if ((rc = alloc(&bx_, hs.bx.size(), err)) || (rc = alloc(&by_, hs.by.size(), err)) ||
@@ -511,12 +530,7 @@ template <typename T> class Engine final : public EngineBase {
             return 3;
         }
         int rc;
-        if ((rc = launch(CAT_PAIR, k_fluid_pairs<T, MODE_FORCES>, blocks_for(nf_), kBlock, err, F_,
-                         (const uint32_t *)fstart_, (const uint32_t *)wstart_,
-                         nbr_fluid(F_, true), nbr_walls(true), grid_, P_, O_, T(0), PairOut{},
-                         health_, (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
-                         (const uint32_t *)nullptr)))
-            return rc;
+        if ((rc = fluid_pairs<MODE_FORCES>(F_, true, T(0), PairOut{}, err))) return rc;
         if (model == 1 && nw_ > 0 &&
             (rc = launch(CAT_PAIR, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
                          (const uint32_t *)fstart_, nbr_fluid(F_, true), grid_, P_, true, false, T(0),

@@ -1,0 +1,427 @@
+// tsph_pairs_tiled.cuh -- the FP32 pair loop as a shared-memory tiled gather
+// kernel (the production path of Compute_Forces, src/SPH_interaction.h:8-149,
+// fused with the symplectic corrector of src/SPH_integration.h:289-309).
+//
+// Work decomposition: a CTA takes 128 consecutive fluid particles of the
+// cell-sorted state (their cells are consecutive rows of one or two grid
+// columns).  For each window of at most kTileRows target rows of one column it
+//   1. stages the 3 x (rows + 2) neighbour cells (fluid and walls) into shared
+//      memory: FP32 position relative to the particle's own cell (so r_a - r_b
+//      keeps ~1e-7 relative precision without FP64), velocity, rho - rho0,
+//      p/rho and 1/rho (the EOS and the reciprocal done once per staged
+//      particle instead of once per pair);
+//   2. phase 1: every thread walks its own 3 x 3 cells in shared memory and
+//      appends the in-support neighbours (0 < r <= 2h) to a private list;
+//   3. phase 2: every thread evaluates the WCSPH pair terms over its list, so
+//      the expensive arithmetic runs with nearly all lanes active (a plain
+//      candidate loop would execute it for ~80 candidates with ~30% of the
+//      lanes useful).
+// A window whose neighbour block exceeds the shared-memory capacity falls
+// back to reading the neighbours from global memory (same arithmetic).
+#pragma once
+
+#include "tsph_kernels.cuh"
+
+namespace tsph {
+
+constexpr int kTileT = 128;     // targets per CTA
+constexpr int kTileRows = 24;   // max target rows per window
+constexpr int kTileCap = 1024;  // staged neighbours per window
+constexpr int kList = 48;       // list entries per target (overflow is evaluated in place)
+
+struct TileSmem {
+    float2 loc[kTileCap];
+    float2 vel[kTileCap];
+    float4 rp[kTileCap];  // {rho - rho0, p/rho, 1/rho, 0}
+    int foff[3][kTileRows + 3];
+    int woff[3][kTileRows + 3];
+    float2 off[9];
+    uint16_t list[kList * kTileT];
+};
+
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// Pair terms with the constant factors (m, bwen/h, k_psi) applied once per
+// target by the caller: a = -m bwen_h sum dr w^3 (P_a I_b + P_b I_a + Pi),
+// drho = m bwen_h (sum w^3 dr.dv - k_psi sum psi r^2 w^3 I_b).
+struct Acc4 {
+    float ax, ay, cont, diff;
+};
+
+struct TileConst {
+    float neg_half_inv_h;  // -0.5 / h
+    float eps_h2, four_h2;
+    float k_av_over_2rho0;  // -2 alpha c0 h / (2 rho0)
+    float inv_2rho0;
+    float c1, c2;           // rho0((1 + x)^(1/7) - 1) ~ dy (c1 + c2 dy), x = xg dy
+};
+
+__device__ __forceinline__ void pair_terms(float dx, float dy, float dvx, float dvy, float sa,
+                                           float Pa, float Ia, float sb, float Pb, float Ib,
+                                           const TileConst &K, Acc4 &acc) {
+    const float r2 = fmaf(dx, dx, dy * dy);
+    const float r = r2 * rsqrtf(r2);
+    const float w1 = fmaf(r, K.neg_half_inv_h, 1.f);
+    const float w3 = w1 * w1 * w1;
+    const float drdv = fmaf(dx, dvx, dy * dvy);
+    const float inv_den = rcp_approx(r2 + K.eps_h2);
+    float pterm = fmaf(Pa, Ib, Pb * Ia);
+    if (drdv < 0.f) {
+        // 1/(rho_a + rho_b) = 1/(2 rho0) (1 - e + e^2 - e^3), e = (sa + sb)/(2 rho0)
+        const float e = (sa + sb) * K.inv_2rho0;
+        const float ser = fmaf(e, fmaf(e, fmaf(-e, 1.f, 1.f), -1.f), 1.f);
+        pterm = fmaf(K.k_av_over_2rho0 * drdv, inv_den * ser, pterm);
+    }
+    const float coef = w3 * pterm;
+    acc.ax = fmaf(-dx, coef, acc.ax);
+    acc.ay = fmaf(-dy, coef, acc.ay);
+    acc.cont = fmaf(w3, drdv, acc.cont);
+    const float drhoH = dy * fmaf(K.c2, dy, K.c1);
+    const float psi = ((sb - sa) - drhoH) * inv_den;
+    acc.diff = fmaf(psi * r2, w3 * Ib, acc.diff);
+}
+
+// per-particle derived quantities of a neighbour: {s, p/rho, 1/rho}
+__device__ __forceinline__ float4 staged_rp(float s, float p, const Phys<float> &P) {
+    const float inv = rcp_approx(P.rho0 + s);
+    return make_float4(s, p * inv, inv, 0.f);
+}
+
+template <int MODE, bool STORED_P>
+__global__ void __launch_bounds__(kTileT, 4)
+k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
+              const uint32_t *__restrict__ wstart, WallState<float> Wl, Grid g, Phys<float> P,
+              TileConst K, OldState<float> O, float dt, PairOut out,
+              uint32_t *__restrict__ health) {
+    __shared__ TileSmem sm;
+    const int tid = threadIdx.x;
+    const int ncy = g.ncy;
+    const int nl = n_live(fstart, g.ncells);
+    const int t0 = blockIdx.x * kTileT;
+    if (t0 >= nl) return;
+    const int t1 = min(t0 + kTileT, nl);
+    if (tid < 9) sm.off[tid] = make_float2((float)(1 - tid / 3) * g.khf, (float)(1 - tid % 3) * g.khf);
+    int cur = t0;
+    while (cur < t1) {  // block-uniform loop over row windows
+        const uint32_t kc = __ldg(F.key + cur);
+        const int cx = (int)(kc / (uint32_t)ncy);
+        const int cy0 = (int)kc - cx * ncy;
+        const int rowlim = min(cy0 + kTileRows, ncy);
+        const int we = min(t1, (int)__ldg(fstart + cx * ncy + rowlim));
+        const int cyl = (int)__ldg(F.key + we - 1) - cx * ncy;
+        const int rlo = max(cy0 - 1, 0), rhi = min(cyl + 1, ncy - 1);
+        const int nr = rhi - rlo + 1;
+        __syncthreads();  // previous window finished with shared memory
+        for (int e = tid; e < 3 * (nr + 1); e += kTileT) {
+            const int dxi = e / (nr + 1), q = e - dxi * (nr + 1);
+            const int col = cx + dxi - 1;
+            int fo = 0, wo = 0;
+            if (col >= 0 && col < g.ncx) {
+                const int c = col * ncy + rlo + q;
+                fo = (int)__ldg(fstart + c);
+                wo = (int)__ldg(wstart + c);
+            }
+            sm.foff[dxi][q] = fo;
+            sm.woff[dxi][q] = wo;
+        }
+        __syncthreads();
+        int fb[3], wb[3], f0[3], w0[3];
+        int tot = 0;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            w0[d] = sm.woff[d][0];
+            f0[d] = sm.foff[d][0];
+            wb[d] = tot;
+            tot += sm.woff[d][nr] - w0[d];
+            fb[d] = tot;
+            tot += sm.foff[d][nr] - f0[d];
+        }
+        const int i = cur + tid;
+        const bool active = i < we;
+        Acc4 acc = {0.f, 0.f, 0.f, 0.f};
+        float2 la = make_float2(0.f, 0.f), va = make_float2(0.f, 0.f);
+        float sa = 0.f, Pa = 0.f, Ia = 0.f;
+        int cy = 0;
+        if (tot <= kTileCap) {
+            // ---- stage the neighbour block
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                const int nwd = sm.woff[d][nr] - w0[d];
+                for (int k = tid; k < nwd; k += kTileT) {
+                    const int j = w0[d] + k;
+                    const float s = __ldg(Wl.rho + j);
+                    const float p = STORED_P ? __ldg(Wl.p + j) : eos(s, P);
+                    sm.loc[wb[d] + k] = __ldg(Wl.loc + j);
+                    sm.vel[wb[d] + k] = make_float2(0.f, 0.f);
+                    sm.rp[wb[d] + k] = staged_rp(s, p, P);
+                }
+                const int nfd = sm.foff[d][nr] - f0[d];
+                for (int k = tid; k < nfd; k += kTileT) {
+                    const int j = f0[d] + k;
+                    const float s = __ldg(F.rho + j);
+                    const float p = STORED_P ? __ldg(F.p + j) : eos(s, P);
+                    sm.loc[fb[d] + k] = __ldg(F.loc + j);
+                    sm.vel[fb[d] + k] = __ldg(F.v + j);
+                    sm.rp[fb[d] + k] = staged_rp(s, p, P);
+                }
+            }
+            __syncthreads();
+            if (active) {
+                cy = (int)__ldg(F.key + i) - cx * ncy;
+                const int own = fb[1] + (i - f0[1]);
+                la = sm.loc[own];
+                va = sm.vel[own];
+                const float4 rpa = sm.rp[own];
+                sa = rpa.x;
+                Pa = rpa.y;
+                Ia = rpa.z;
+                // ---- phase 1: in-support neighbours into the list
+                int cnt = 0;
+#pragma unroll
+                for (int dxi = 0; dxi < 3; dxi++) {
+                    const int col = cx + dxi - 1;
+                    if (col < 0 || col >= g.ncx) continue;
+#pragma unroll
+                    for (int dyi = 0; dyi < 3; dyi++) {
+                        const int row = cy + dyi - 1;
+                        if (row < 0 || row >= ncy) continue;
+                        const int q = row - rlo;
+                        const int code = dxi * 3 + dyi;
+                        const float2 o = sm.off[code];
+                        const float bx = la.x + o.x, by = la.y + o.y;
+#pragma unroll
+                        for (int kind = 0; kind < 2; kind++) {
+                            const int j0 = kind == 0 ? wb[dxi] + sm.woff[dxi][q] - w0[dxi]
+                                                     : fb[dxi] + sm.foff[dxi][q] - f0[dxi];
+                            const int j1 = kind == 0 ? wb[dxi] + sm.woff[dxi][q + 1] - w0[dxi]
+                                                     : fb[dxi] + sm.foff[dxi][q + 1] - f0[dxi];
+                            for (int j = j0; j < j1; j++) {
+                                const float2 lb = sm.loc[j];
+                                const float dx = bx - lb.x, dy = by - lb.y;
+                                const float r2 = fmaf(dx, dx, dy * dy);
+                                if (r2 <= K.four_h2 && r2 > 0.f) {
+                                    if (cnt < kList) {
+                                        sm.list[cnt * kTileT + tid] = (uint16_t)((j << 4) | code);
+                                        cnt++;
+                                    } else {
+                                        const float2 vb = sm.vel[j];
+                                        const float4 rb = sm.rp[j];
+                                        pair_terms(dx, dy, va.x - vb.x, va.y - vb.y, sa, Pa, Ia, rb.x,
+                                                   rb.y, rb.z, K, acc);
+                                    }
+                                }
+                            }
+                        }
+                    }
+                }
+                // ---- phase 2: the pair terms over the list
+                for (int k = 0; k < cnt; k++) {
+                    const uint32_t e = sm.list[k * kTileT + tid];
+                    const int j = (int)(e >> 4);
+                    const float2 o = sm.off[e & 15u];
+                    const float2 lb = sm.loc[j];
+                    const float2 vb = sm.vel[j];
+                    const float4 rb = sm.rp[j];
+                    pair_terms((la.x + o.x) - lb.x, (la.y + o.y) - lb.y, va.x - vb.x, va.y - vb.y, sa,
+                               Pa, Ia, rb.x, rb.y, rb.z, K, acc);
+                }
+            }
+        } else if (active) {
+            // ---- fallback: neighbours straight from global memory
+            cy = (int)__ldg(F.key + i) - cx * ncy;
+            la = __ldg(F.loc + i);
+            va = __ldg(F.v + i);
+            sa = __ldg(F.rho + i);
+            {
+                const float p = STORED_P ? __ldg(F.p + i) : eos(sa, P);
+                const float4 rpa = staged_rp(sa, p, P);
+                Pa = rpa.y;
+                Ia = rpa.z;
+            }
+            for (int dxi = 0; dxi < 3; dxi++) {
+                const int col = cx + dxi - 1;
+                if (col < 0 || col >= g.ncx) continue;
+                for (int dyi = 0; dyi < 3; dyi++) {
+                    const int row = cy + dyi - 1;
+                    if (row < 0 || row >= ncy) continue;
+                    const int c = col * ncy + row;
+                    const float ox = (float)(1 - dxi) * g.khf, oy = (float)(1 - dyi) * g.khf;
+                    for (int kind = 0; kind < 2; kind++) {
+                        const int j0 = (int)__ldg((kind == 0 ? wstart : fstart) + c);
+                        const int j1 = (int)__ldg((kind == 0 ? wstart : fstart) + c + 1);
+                        for (int j = j0; j < j1; j++) {
+                            if (kind == 1 && j == i) continue;
+                            const float2 lb = __ldg((kind == 0 ? Wl.loc : F.loc) + j);
+                            const float dx = (la.x + ox) - lb.x, dy = (la.y + oy) - lb.y;
+                            const float r2 = fmaf(dx, dx, dy * dy);
+                            if (!(r2 <= K.four_h2 && r2 > 0.f)) continue;
+                            const float s = __ldg((kind == 0 ? Wl.rho : F.rho) + j);
+                            const float p = STORED_P ? __ldg((kind == 0 ? Wl.p : F.p) + j) : eos(s, P);
+                            const float4 rb = staged_rp(s, p, P);
+                            const float2 vb = kind == 0 ? make_float2(0.f, 0.f) : __ldg(F.v + j);
+                            pair_terms(dx, dy, va.x - vb.x, va.y - vb.y, sa, Pa, Ia, rb.x, rb.y, rb.z,
+                                       K, acc);
+                        }
+                    }
+                }
+            }
+        }
+        if (active) {
+            const float mb = P.m * P.bwen_h;
+            const float ax = acc.ax * mb;
+            const float ay = fmaf(acc.ay, mb, -P.g);
+            const float drho = mb * fmaf(-P.k_psi, acc.diff, acc.cont);
+            if constexpr (MODE == MODE_FORCES) {
+                F.a[i] = make_float2(ax, ay);
+                F.drho[i] = drho;
+            } else {
+                const float so = O.rho[i];
+                const float s_new = corrector_rho(so, sa, drho, dt, P.rho0);
+                const float2 vo = O.v[i];
+                const float2 nv = make_float2(vo.x + ax * dt, vo.y + ay * dt);
+                const double2 ro = O.r[i];
+                const double2 rn =
+                    make_double2(ro.x + ((double)nv.x + (double)vo.x) * (double)dt * 0.5,
+                                 ro.y + ((double)nv.y + (double)vo.y) * (double)dt * 0.5);
+                out.r[i] = rn;
+                reinterpret_cast<float2 *>(out.v)[i] = nv;
+                reinterpret_cast<float *>(out.rho)[i] = s_new;
+                uint32_t nk;
+                if (out_of_domain(rn, out.box)) {
+                    nk = (uint32_t)g.ncells;
+                    atomicOr(health, kHealthRemoved);
+                } else {
+                    int ncx_, ncy_;
+                    nk = cell_key(g, rn, (uint32_t)(cx * ncy + cy), &ncx_, &ncy_);
+                    if (nk == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
+                }
+                if (!(nv.x == nv.x) || !(nv.y == nv.y) || !(s_new == s_new))
+                    atomicOr(health, kHealthNan);
+                out.key[i] = nk;
+                out.slot[i] = atomicAdd(out.counts + nk, 1u);
+            }
+        }
+        cur = we;
+    }
+}
+
+inline TileConst make_tile_const(const Phys<float> &P, double h, double rho0, double g, double cs) {
+    TileConst K;
+    K.neg_half_inv_h = (float)(-0.5 / h);
+    K.eps_h2 = P.eps_h2;
+    K.four_h2 = P.four_h2;
+    K.k_av_over_2rho0 = (float)((double)P.k_av / (2.0 * rho0));
+    K.inv_2rho0 = (float)(1.0 / (2.0 * rho0));
+    const double xg = 7.0 * g / (cs * cs);
+    K.c1 = (float)(rho0 * xg / 7.0);
+    K.c2 = (float)(-rho0 * 3.0 / 49.0 * xg * xg);
+    return K;
+}
+
+}  // namespace tsph
+
+namespace tsph {
+
+// mDBC ghost-node density, FP32 build: 8 lanes per wall particle, the 12
+// moment sums (src/SPH_kernel_approx.h:1237-1287) in FP32, reduced with
+// shuffles; the 3x3 solve in FP64 with one reciprocal of the determinant
+// (threshold 0.001 and the Shepard / 1000 fall-backs of :1290-1333), the
+// clamp at 1000 of src/SPH_mDBC.h:43-44.
+static __global__ void __launch_bounds__(kBlock)
+k_mdbc8(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidState<float> F,
+        Grid g, Phys<float> P) {
+    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+    const int w = gid >> 3, sub = gid & 7;
+    const bool valid = w < nw;
+    float s[12];
+#pragma unroll
+    for (int q = 0; q < 12; q++) s[q] = 0.f;
+    const uint32_t gk = valid ? Wl.gkey[w] : (uint32_t)g.ncells;
+    if (gk < (uint32_t)g.ncells) {
+        const int cx = (int)(gk / (uint32_t)g.ncy);
+        const int cy = (int)gk - cx * g.ncy;
+        const float2 gl = Wl.gloc[w];
+#pragma unroll
+        for (int dxi = 0; dxi < 3; dxi++) {
+            const int col = cx + dxi - 1;
+            if (col < 0 || col >= g.ncx) continue;
+            const float ox = gl.x + (float)(1 - dxi) * g.khf;
+            // three rows of one column are contiguous in the sorted state
+            const int ylo = max(cy - 1, 0), yhi = min(cy + 1, g.ncy - 1);
+            const int c0 = col * g.ncy;
+            const int jlo = (int)__ldg(fstart + c0 + ylo), jhi = (int)__ldg(fstart + c0 + yhi + 1);
+            for (int j = jlo + sub; j < jhi; j += 8) {
+                const uint32_t kb = __ldg(F.key + j);
+                const int rowb = (int)kb - c0;
+                const float2 lb = __ldg(F.loc + j);
+                const float drx = ox - lb.x;
+                const float dry = (gl.y + (float)(cy - rowb) * g.khf) - lb.y;
+                const float r2 = fmaf(drx, drx, dry * dry);
+                if (!(r2 <= P.four_h2)) continue;
+                float W, Fk;
+                if (r2 == 0.f) {
+                    W = P.awen;
+                    Fk = 0.f;
+                } else {
+                    wendland32(r2, P, W, Fk, true);
+                }
+                const float V = P.m * rcp_approx(P.rho0 + __ldg(F.rho + j));
+                s[0] += W;
+                s[1] = fmaf(drx, Fk, s[1]);
+                s[2] = fmaf(dry, Fk, s[2]);
+                const float WV = W * V, FV = Fk * V;
+                s[3] += WV;
+                s[4] = fmaf(drx, WV, s[4]);
+                s[5] = fmaf(dry, WV, s[5]);
+                s[6] = fmaf(drx, FV, s[6]);
+                s[7] = fmaf(drx * drx, FV, s[7]);
+                s[8] = fmaf(drx * dry, FV, s[8]);
+                s[9] = fmaf(dry, FV, s[9]);
+                s[10] = fmaf(dry * drx, FV, s[10]);
+                s[11] = fmaf(dry * dry, FV, s[11]);
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < 12; q++) {
+        s[q] += __shfl_xor_sync(0xffffffffu, s[q], 4);
+        s[q] += __shfl_xor_sync(0xffffffffu, s[q], 2);
+        s[q] += __shfl_xor_sync(0xffffffffu, s[q], 1);
+    }
+    if (!valid || sub != 0) return;
+    const double m = (double)P.m;
+    const double rhoWsum = (double)s[0] * m, drhodx = (double)s[1] * m, drhody = (double)s[2] * m;
+    const double a11 = s[3], a12 = s[4], a13 = s[5], a21 = s[6], a22 = s[7], a23 = s[8],
+                 a31 = s[9], a32 = s[10], a33 = s[11];
+    const double det = det3(a11, a12, a13, a21, a22, a23, a31, a32, a33);
+    double dens;
+    if (det > 0.001) {
+        const double id = 1.0 / det;
+        const double i11 = (a22 * a33 - a23 * a32) * id;
+        const double i12 = -(a12 * a33 - a13 * a32) * id;
+        const double i13 = (a12 * a23 - a13 * a22) * id;
+        const double i21 = -(a21 * a33 - a23 * a31) * id;
+        const double i22 = (a11 * a33 - a13 * a31) * id;
+        const double i23 = -(a11 * a23 - a13 * a21) * id;
+        const double i31 = (a21 * a32 - a22 * a31) * id;
+        const double i32 = -(a11 * a32 - a12 * a31) * id;
+        const double i33 = (a11 * a22 - a12 * a21) * id;
+        const double dens_temp = rhoWsum * i11 + drhodx * i12 + drhody * i13;
+        const double grx = -(rhoWsum * i21 + drhodx * i22 + drhody * i23);
+        const double gry = -(rhoWsum * i31 + drhodx * i32 + drhody * i33);
+        const float2 gnd = Wl.gnd[w];
+        dens = dens_temp + grx * (double)gnd.x + gry * (double)gnd.y;
+    } else if (a11 > 0) {
+        dens = rhoWsum / a11;
+    } else {
+        dens = 1000.;
+    }
+    if (dens < 1000.) dens = 1000.;
+    Wl.rho[w] = (float)(dens - (double)P.rho0);
+}
+
+}  // namespace tsph
