@@ -52,6 +52,7 @@ template <typename T> class Engine final : public EngineBase {
     uint32_t *keyB_ = nullptr, *slotB_ = nullptr, *tmp_id_ = nullptr, *tmp_src_ = nullptr,
              *perm_ = nullptr;
     uint32_t *counts_ = nullptr, *fstart_ = nullptr, *wstart_ = nullptr, *tile_sums_ = nullptr;
+    long long *tmp_y_ = nullptr;
     uint32_t *health_ = nullptr, *removed_ = nullptr;
     WallState<T> W_{};
     Staging S_{};
@@ -168,13 +169,16 @@ template <typename T> class Engine final : public EngineBase {
         if ((rc = scan(err))) return rc;
         const int *ntot = reinterpret_cast<const int *>(fstart_ + ncells_ + 1);
         const int nb = blocks_for(nf_);
+        // FP32 build: cells ordered by (y, index); FP64 build: by index
+        constexpr bool by_y = std::is_same<T, float>::value;
         if ((rc = launch(CAT_SORT, k_place, nb, kBlock, err, (const uint32_t *)keyB_,
                          (const uint32_t *)slotB_, sid, ntot, (const uint32_t *)fstart_, tmp_id_,
-                         tmp_src_)))
+                         tmp_src_, by_y ? sr : (const double2 *)nullptr, tmp_y_)))
             return rc;
         if ((rc = launch(CAT_SORT, k_rank, nb, kBlock, err, (const uint32_t *)keyB_, ntot,
                          (const uint32_t *)fstart_, (const uint32_t *)tmp_id_,
-                         (const uint32_t *)tmp_src_, perm_, ncells_)))
+                         (const uint32_t *)tmp_src_, perm_, ncells_,
+                         by_y ? (const long long *)tmp_y_ : (const long long *)nullptr)))
             return rc;
         return launch(CAT_SORT, k_gather<T>, nb, kBlock, err, (const uint32_t *)perm_, ntot, grid_,
                       sr, sv, srho, sid, (const uint32_t *)keyB_, sa, sdrho, sp, D, or2, ov2, orho2,
@@ -238,7 +242,7 @@ template <typename T> class Engine final : public EngineBase {
         PairOut po{Br_, (void *)Bv_, (void *)Brho_, keyB_, slotB_, counts_, box_};
         if ((rc = fluid_pairs<MODE_CORRECT>(Fs_, false, dt, po, err))) return rc;
         if (nw_ > 0 &&
-            (rc = launch(CAT_PAIR, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
+            (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
                          (const uint32_t *)fstart_, nbr_fluid(Fs_, false), grid_, P_, dbc, true, dt,
                          (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
                          (const uint32_t *)nullptr, false)))
@@ -249,7 +253,7 @@ template <typename T> class Engine final : public EngineBase {
         // forces at the new state (a, drho for the next predictor)
         if ((rc = fluid_pairs<MODE_FORCES>(F_, false, dt, PairOut{}, err))) return rc;
         if (dbc && nw_ > 0 &&
-            (rc = launch(CAT_PAIR, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
+            (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
                          (const uint32_t *)fstart_, nbr_fluid(F_, false), grid_, P_, true, false, dt,
                          (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
                          (const uint32_t *)nullptr, false)))
@@ -339,7 +343,7 @@ template <typename T> class Engine final : public EngineBase {
             (rc = alloc(&Bv_, nf_, err)) || (rc = alloc(&Brho_, nf_, err)) ||
             (rc = alloc(&keyB_, nf_, err)) || (rc = alloc(&slotB_, nf_, err)) ||
             (rc = alloc(&tmp_id_, nf_, err)) || (rc = alloc(&tmp_src_, nf_, err)) ||
-            (rc = alloc(&perm_, nf_, err)))
+            (rc = alloc(&perm_, nf_, err)) || (rc = alloc(&tmp_y_, nf_, err)))
             return rc;
         const int ntiles = (ncells_ + 1 + kScanTile - 1) / kScanTile;
         if (ntiles > kScanTile) {
@@ -410,7 +414,17 @@ template <typename T> class Engine final : public EngineBase {
                 }
                 order.push_back({(uint32_t)(cy + cx * hs.ncy), i});
             }
-            std::sort(order.begin(), order.end());
+            if constexpr (std::is_same<T, float>::value) {
+                std::sort(order.begin(), order.end(), [&](const std::pair<uint32_t, int> &a,
+                                                          const std::pair<uint32_t, int> &b) {
+                    if (a.first != b.first) return a.first < b.first;
+                    const double ya = hs.r[2 * a.second + 1], yb = hs.r[2 * b.second + 1];
+                    if (ya != yb) return ya < yb;
+                    return a.second < b.second;
+                });
+            } else {
+                std::sort(order.begin(), order.end());
+            }
             if ((rc = alloc(&W_.r, nw_, err)) || (rc = alloc(&W_.loc, nw_, err)) ||
                 (rc = alloc(&W_.key, nw_, err)) || (rc = alloc(&W_.id, nw_, err)) ||
                 (rc = alloc(&W_.rho, nw_, err)) || (rc = alloc(&W_.drho, nw_, err)) ||
@@ -532,7 +546,7 @@ template <typename T> class Engine final : public EngineBase {
         int rc;
         if ((rc = fluid_pairs<MODE_FORCES>(F_, true, T(0), PairOut{}, err))) return rc;
         if (model == 1 && nw_ > 0 &&
-            (rc = launch(CAT_PAIR, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
+            (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
                          (const uint32_t *)fstart_, nbr_fluid(F_, true), grid_, P_, true, false, T(0),
                          (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
                          (const uint32_t *)nullptr, false)))
@@ -746,8 +760,7 @@ template <typename T> class Engine final : public EngineBase {
             tmp.clear();
             for (uint32_t j = ws[c]; j < ws[c + 1]; j++) tmp.push_back(rank[wid[j]]);
             for (uint32_t j = fs[c]; j < fs[c + 1]; j++) tmp.push_back(rank[fid[j]]);
-            // walls and fluid are each ascending; merge
-            std::inplace_merge(tmp.begin(), tmp.begin() + (ws[c + 1] - ws[c]), tmp.end());
+            std::sort(tmp.begin(), tmp.end());
             for (int x : tmp) cell_list[acc++] = x;
         }
         cell_start[ncells_] = acc;

@@ -272,24 +272,29 @@ static __global__ void k_scan_add(uint32_t *__restrict__ out, const uint32_t *__
 }
 
 // ------------------------------------------------------ stable scatter
-// place: provisional slot from the atomic histogram
+// place: provisional slot from the atomic histogram.  The order key inside a
+// cell is the particle index (FP64 build: the reference's list order) or, when
+// `r` is given, (y, index) (FP32 build: cells sorted by height, which lets the
+// pair kernel stop early in the rows above and below).
 static __global__ void k_place(const uint32_t *__restrict__ key, const uint32_t *__restrict__ slot,
                         const uint32_t *__restrict__ id, const int *__restrict__ n_ptr,
                         const uint32_t *__restrict__ start, uint32_t *__restrict__ tmp_id,
-                        uint32_t *__restrict__ tmp_src) {
+                        uint32_t *__restrict__ tmp_src, const double2 *__restrict__ r,
+                        long long *__restrict__ tmp_y) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *n_ptr) return;
     const uint32_t d = start[key[i]] + slot[i];
     tmp_id[d] = id[i];
     tmp_src[d] = (uint32_t)i;
+    if (r) tmp_y[d] = ordered_bits(r[i].y);
 }
 
-// rank: final position = cell start + number of cell members with a smaller
-// particle index (the reference's cell lists are ascending by index)
+// rank: final position = cell start + number of cell members that order
+// before this one
 static __global__ void k_rank(const uint32_t *__restrict__ key, const int *__restrict__ n_ptr,
                        const uint32_t *__restrict__ start, const uint32_t *__restrict__ tmp_id,
                        const uint32_t *__restrict__ tmp_src, uint32_t *__restrict__ perm,
-                       int ncells) {
+                       int ncells, const long long *__restrict__ tmp_y) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= *n_ptr) return;
     const uint32_t src = tmp_src[j];
@@ -301,7 +306,15 @@ static __global__ void k_rank(const uint32_t *__restrict__ key, const int *__res
     const uint32_t lo = start[k], hi = start[k + 1];
     const uint32_t me = tmp_id[j];
     uint32_t rank = 0;
-    for (uint32_t m = lo; m < hi; m++) rank += (tmp_id[m] < me) ? 1u : 0u;
+    if (tmp_y) {
+        const long long my = tmp_y[j];
+        for (uint32_t m = lo; m < hi; m++) {
+            const long long ym = tmp_y[m];
+            rank += (ym < my || (ym == my && tmp_id[m] < me)) ? 1u : 0u;
+        }
+    } else {
+        for (uint32_t m = lo; m < hi; m++) rank += (tmp_id[m] < me) ? 1u : 0u;
+    }
     perm[lo + rank] = src;
 }
 

@@ -25,9 +25,9 @@
 namespace tsph {
 
 constexpr int kTileT = 128;     // targets per CTA
-constexpr int kTileRows = 24;   // max target rows per window
-constexpr int kTileCap = 1024;  // staged neighbours per window
-constexpr int kList = 48;       // list entries per target (overflow is evaluated in place)
+constexpr int kTileRows = 16;   // max target rows per window (halved while the block is too big)
+constexpr int kTileCap = 768;   // staged neighbours per window
+constexpr int kList = 40;       // list entries per target (overflow: global-memory path)
 
 struct TileSmem {
     float2 loc[kTileCap];
@@ -91,8 +91,51 @@ __device__ __forceinline__ float4 staged_rp(float s, float p, const Phys<float> 
     return make_float4(s, p * inv, inv, 0.f);
 }
 
+// all in-support neighbours of one target straight from global memory (the
+// path for windows whose neighbour block does not fit in shared memory, and
+// for targets whose list overflows)
+template <bool STORED_P>
+__device__ __forceinline__ void target_global(const FluidState<float> &F, const uint32_t *fstart,
+                                           const uint32_t *wstart, const WallState<float> &Wl,
+                                           const Grid &g, const Phys<float> &P, const TileConst &K,
+                                           int i, int cx, int cy, float2 la, float2 va, float sa,
+                                           float Pa, float Ia, Acc4 &acc) {
+    for (int dxi = 0; dxi < 3; dxi++) {
+        const int col = cx + dxi - 1;
+        if (col < 0 || col >= g.ncx) continue;
+        for (int dyi = 0; dyi < 3; dyi++) {
+            const int row = cy + dyi - 1;
+            if (row < 0 || row >= g.ncy) continue;
+            const int c = col * g.ncy + row;
+            const float ox = (float)(1 - dxi) * g.khf, oy = (float)(1 - dyi) * g.khf;
+            for (int kind = 0; kind < 2; kind++) {
+                const int j0 = (int)__ldg((kind == 0 ? wstart : fstart) + c);
+                const int j1 = (int)__ldg((kind == 0 ? wstart : fstart) + c + 1);
+                for (int j = j0; j < j1; j++) {
+                    if (kind == 1 && j == i) continue;
+                    const float2 lb = __ldg((kind == 0 ? Wl.loc : F.loc) + j);
+                    const float dx = (la.x + ox) - lb.x, dy = (la.y + oy) - lb.y;
+                    const float r2 = fmaf(dx, dx, dy * dy);
+                    if (!(r2 <= K.four_h2 && r2 > 0.f)) continue;
+                    const float s = __ldg((kind == 0 ? Wl.rho : F.rho) + j);
+                    const float p = STORED_P ? __ldg((kind == 0 ? Wl.p : F.p) + j) : eos(s, P);
+                    const float4 rb = staged_rp(s, p, P);
+                    const float2 vb = kind == 0 ? make_float2(0.f, 0.f) : __ldg(F.v + j);
+                    pair_terms(dx, dy, va.x - vb.x, va.y - vb.y, sa, Pa, Ia, rb.x, rb.y, rb.z, K,
+                               acc);
+                }
+            }
+        }
+    }
+}
+
+// in-support test: 0 < r2 <= (2h)^2 as one unsigned compare of the bits
+__device__ __forceinline__ uint32_t in_support(float r2, uint32_t four_h2_bits) {
+    return (uint32_t)(__float_as_uint(r2) - 1u) < four_h2_bits ? 1u : 0u;
+}
+
 template <int MODE, bool STORED_P>
-__global__ void __launch_bounds__(kTileT, 4)
+__global__ void __launch_bounds__(kTileT, 6)
 k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
               const uint32_t *__restrict__ wstart, WallState<float> Wl, Grid g, Phys<float> P,
               TileConst K, OldState<float> O, float dt, PairOut out,
@@ -105,12 +148,16 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
     if (t0 >= nl) return;
     const int t1 = min(t0 + kTileT, nl);
     if (tid < 9) sm.off[tid] = make_float2((float)(1 - tid / 3) * g.khf, (float)(1 - tid % 3) * g.khf);
+    const uint32_t h2bits = __float_as_uint(K.four_h2);
+    // rows above / below are sorted by y: stop once |dy| > 2h (margin for rounding)
+    const float reach = 2.f * P.h * 1.0001f;
     int cur = t0;
+    int rows = kTileRows;
     while (cur < t1) {  // block-uniform loop over row windows
         const uint32_t kc = __ldg(F.key + cur);
         const int cx = (int)(kc / (uint32_t)ncy);
         const int cy0 = (int)kc - cx * ncy;
-        const int rowlim = min(cy0 + kTileRows, ncy);
+        const int rowlim = min(cy0 + rows, ncy);
         const int we = min(t1, (int)__ldg(fstart + cx * ncy + rowlim));
         const int cyl = (int)__ldg(F.key + we - 1) - cx * ncy;
         const int rlo = max(cy0 - 1, 0), rhi = min(cyl + 1, ncy - 1);
@@ -130,15 +177,20 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
         }
         __syncthreads();
         int fb[3], wb[3], f0[3], w0[3];
-        int tot = 0;
+        int tot = 0, totw = 0;
 #pragma unroll
         for (int d = 0; d < 3; d++) {
             w0[d] = sm.woff[d][0];
             f0[d] = sm.foff[d][0];
             wb[d] = tot;
             tot += sm.woff[d][nr] - w0[d];
+            totw += sm.woff[d][nr] - w0[d];
             fb[d] = tot;
             tot += sm.foff[d][nr] - f0[d];
+        }
+        if (tot > kTileCap && rows > 1) {  // too dense: fewer target rows per window
+            rows = (rows + 1) >> 1;
+            continue;
         }
         const int i = cur + tid;
         const bool active = i < we;
@@ -179,8 +231,9 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 sa = rpa.x;
                 Pa = rpa.y;
                 Ia = rpa.z;
-                // ---- phase 1: in-support neighbours into the list
+                // ---- phase 1: in-support neighbours into the list (branch-free append)
                 int cnt = 0;
+                uint16_t *lst = sm.list + tid;
 #pragma unroll
                 for (int dxi = 0; dxi < 3; dxi++) {
                     const int col = cx + dxi - 1;
@@ -191,84 +244,74 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                         if (row < 0 || row >= ncy) continue;
                         const int q = row - rlo;
                         const int code = dxi * 3 + dyi;
-                        const float2 o = sm.off[code];
-                        const float bx = la.x + o.x, by = la.y + o.y;
+                        const float bx = la.x + sm.off[code].x, by = la.y + sm.off[code].y;
 #pragma unroll
                         for (int kind = 0; kind < 2; kind++) {
+                            if (kind == 0 && totw == 0) continue;  // block-uniform: no walls here
                             const int j0 = kind == 0 ? wb[dxi] + sm.woff[dxi][q] - w0[dxi]
                                                      : fb[dxi] + sm.foff[dxi][q] - f0[dxi];
                             const int j1 = kind == 0 ? wb[dxi] + sm.woff[dxi][q + 1] - w0[dxi]
                                                      : fb[dxi] + sm.foff[dxi][q + 1] - f0[dxi];
-                            for (int j = j0; j < j1; j++) {
-                                const float2 lb = sm.loc[j];
-                                const float dx = bx - lb.x, dy = by - lb.y;
-                                const float r2 = fmaf(dx, dx, dy * dy);
-                                if (r2 <= K.four_h2 && r2 > 0.f) {
-                                    if (cnt < kList) {
-                                        sm.list[cnt * kTileT + tid] = (uint16_t)((j << 4) | code);
-                                        cnt++;
-                                    } else {
-                                        const float2 vb = sm.vel[j];
-                                        const float4 rb = sm.rp[j];
-                                        pair_terms(dx, dy, va.x - vb.x, va.y - vb.y, sa, Pa, Ia, rb.x,
-                                                   rb.y, rb.z, K, acc);
-                                    }
+                            if (dyi == 1) {
+                                for (int j = j0; j < j1; j++) {
+                                    const float2 lb = sm.loc[j];
+                                    const float dx = bx - lb.x, dy = by - lb.y;
+                                    const uint32_t in = in_support(fmaf(dx, dx, dy * dy), h2bits);
+                                    lst[min(cnt, kList - 1) * kTileT] = (uint16_t)((j << 4) | code);
+                                    cnt += in;
+                                }
+                            } else if (dyi == 2) {
+                                // row above, ascending y: dy = by - lb.y decreases
+                                for (int j = j0; j < j1; j++) {
+                                    const float2 lb = sm.loc[j];
+                                    const float dx = bx - lb.x, dy = by - lb.y;
+                                    if (dy < -reach) break;
+                                    const uint32_t in = in_support(fmaf(dx, dx, dy * dy), h2bits);
+                                    lst[min(cnt, kList - 1) * kTileT] = (uint16_t)((j << 4) | code);
+                                    cnt += in;
+                                }
+                            } else {
+                                // row below, descending y: dy = by - lb.y increases
+                                for (int j = j1 - 1; j >= j0; j--) {
+                                    const float2 lb = sm.loc[j];
+                                    const float dx = bx - lb.x, dy = by - lb.y;
+                                    if (dy > reach) break;
+                                    const uint32_t in = in_support(fmaf(dx, dx, dy * dy), h2bits);
+                                    lst[min(cnt, kList - 1) * kTileT] = (uint16_t)((j << 4) | code);
+                                    cnt += in;
                                 }
                             }
                         }
                     }
                 }
-                // ---- phase 2: the pair terms over the list
-                for (int k = 0; k < cnt; k++) {
-                    const uint32_t e = sm.list[k * kTileT + tid];
-                    const int j = (int)(e >> 4);
-                    const float2 o = sm.off[e & 15u];
-                    const float2 lb = sm.loc[j];
-                    const float2 vb = sm.vel[j];
-                    const float4 rb = sm.rp[j];
-                    pair_terms((la.x + o.x) - lb.x, (la.y + o.y) - lb.y, va.x - vb.x, va.y - vb.y, sa,
-                               Pa, Ia, rb.x, rb.y, rb.z, K, acc);
+                if (cnt <= kList) {
+                    // ---- phase 2: the pair terms over the list
+                    for (int k = 0; k < cnt; k++) {
+                        const uint32_t e = lst[k * kTileT];
+                        const int j = (int)(e >> 4);
+                        const float2 o = sm.off[e & 15u];
+                        const float2 lb = sm.loc[j];
+                        const float2 vb = sm.vel[j];
+                        const float4 rb = sm.rp[j];
+                        pair_terms((la.x + o.x) - lb.x, (la.y + o.y) - lb.y, va.x - vb.x,
+                                   va.y - vb.y, sa, Pa, Ia, rb.x, rb.y, rb.z, K, acc);
+                    }
+                } else {
+                    target_global<STORED_P>(F, fstart, wstart, Wl, g, P, K, i, cx, cy, la, va, sa,
+                                            Pa, Ia, acc);
                 }
             }
         } else if (active) {
-            // ---- fallback: neighbours straight from global memory
             cy = (int)__ldg(F.key + i) - cx * ncy;
             la = __ldg(F.loc + i);
             va = __ldg(F.v + i);
             sa = __ldg(F.rho + i);
-            {
-                const float p = STORED_P ? __ldg(F.p + i) : eos(sa, P);
-                const float4 rpa = staged_rp(sa, p, P);
-                Pa = rpa.y;
-                Ia = rpa.z;
-            }
-            for (int dxi = 0; dxi < 3; dxi++) {
-                const int col = cx + dxi - 1;
-                if (col < 0 || col >= g.ncx) continue;
-                for (int dyi = 0; dyi < 3; dyi++) {
-                    const int row = cy + dyi - 1;
-                    if (row < 0 || row >= ncy) continue;
-                    const int c = col * ncy + row;
-                    const float ox = (float)(1 - dxi) * g.khf, oy = (float)(1 - dyi) * g.khf;
-                    for (int kind = 0; kind < 2; kind++) {
-                        const int j0 = (int)__ldg((kind == 0 ? wstart : fstart) + c);
-                        const int j1 = (int)__ldg((kind == 0 ? wstart : fstart) + c + 1);
-                        for (int j = j0; j < j1; j++) {
-                            if (kind == 1 && j == i) continue;
-                            const float2 lb = __ldg((kind == 0 ? Wl.loc : F.loc) + j);
-                            const float dx = (la.x + ox) - lb.x, dy = (la.y + oy) - lb.y;
-                            const float r2 = fmaf(dx, dx, dy * dy);
-                            if (!(r2 <= K.four_h2 && r2 > 0.f)) continue;
-                            const float s = __ldg((kind == 0 ? Wl.rho : F.rho) + j);
-                            const float p = STORED_P ? __ldg((kind == 0 ? Wl.p : F.p) + j) : eos(s, P);
-                            const float4 rb = staged_rp(s, p, P);
-                            const float2 vb = kind == 0 ? make_float2(0.f, 0.f) : __ldg(F.v + j);
-                            pair_terms(dx, dy, va.x - vb.x, va.y - vb.y, sa, Pa, Ia, rb.x, rb.y, rb.z,
-                                       K, acc);
-                        }
-                    }
-                }
-            }
+            const float p = STORED_P ? __ldg(F.p + i) : eos(sa, P);
+            const float4 rpa = staged_rp(sa, p, P);
+            Pa = rpa.y;
+            Ia = rpa.z;
+            target_global<STORED_P>(F, fstart, wstart, Wl, g, P, K, i, cx, cy, la, va, sa, Pa, Ia,
+                                    acc);
         }
         if (active) {
             const float mb = P.m * P.bwen_h;
@@ -306,6 +349,7 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
             }
         }
         cur = we;
+        rows = kTileRows;
     }
 }
 
