@@ -28,6 +28,7 @@ UNITS = [
     ("tsph_api.cu", []),
     ("tsph_engine_f32.cu", []),
     ("tsph_engine_f64.cu", ["-fmad=false"]),
+    ("tsph_noalloc.cu", []),
 ]
 
 

@@ -10,6 +10,7 @@
 
 #include "../../include/tsph.h"
 #include "tsph_engine.h"
+#include "tsph_grid_host.h"
 #include "tsph_internal.cuh"
 
 using tsph::EngineBase;
@@ -24,41 +25,13 @@ int fail(int code, const std::string &msg) {
     return code;
 }
 
-// (int)((x - x_0 + of)/kh) exactly as src/SPH_find_pairs.h:64-65 evaluates it,
-// saturated outside the int range (the reference would overflow there)
-int ref_cell(double x, double x0, double of, double kh) {
-    const double q = (x - x0 + of) / kh;
-    if (!(q > -1e9)) return INT_MIN;
-    if (!(q < 1e9)) return INT_MAX;
-    return (int)q;
-}
-
-double from_ordered(long long o) {
-    const long long b = o >= 0 ? o : (o ^ 0x7fffffffffffffffLL);
-    double d;
-    std::memcpy(&d, &b, 8);
-    return d;
-}
-
-// smallest double (as ordered bits) whose cell index is >= k
-long long cell_lower_bound(int k, double x0, double of, double kh) {
-    double span = 3.0;
-    long long lo, hi;
-    for (;;) {
-        lo = tsph::ordered_bits(x0 - of + ((double)k - span) * kh);
-        hi = tsph::ordered_bits(x0 - of + ((double)k + span) * kh);
-        if (ref_cell(from_ordered(lo), x0, of, kh) < k && ref_cell(from_ordered(hi), x0, of, kh) >= k)
-            break;
-        span *= 2;
-    }
-    while ((unsigned long long)hi - (unsigned long long)lo > 1ull) {
-        const long long mid = lo + (long long)(((unsigned long long)hi - (unsigned long long)lo) / 2ull);
-        if (ref_cell(from_ordered(mid), x0, of, kh) >= k) hi = mid; else lo = mid;
-    }
-    return hi;
-}
+using tsph::cell_lower_bound;
 
 }  // namespace
+
+namespace tsph {
+void set_last_error(const std::string &msg) { g_err = msg; }
+}  // namespace tsph
 
 struct tsph_system {
     HostSetup hs;

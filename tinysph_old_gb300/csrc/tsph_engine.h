@@ -65,6 +65,9 @@ class EngineBase {
     virtual void invalidate_cells() = 0;
 };
 
+// message returned by tsph_last_error() for the calling thread
+void set_last_error(const std::string &msg);
+
 EngineBase *make_engine_f32();
 EngineBase *make_engine_f64();
 

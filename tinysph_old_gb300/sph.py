@@ -32,7 +32,7 @@ ABI_SYMBOLS = (
     "tsph_abi_version", "tsph_last_error", "tsph_status_string", "tsph_device_count",
     "tsph_create", "tsph_destroy", "tsph_add_particles", "tsph_np", "tsph_grid",
     "tsph_particle_mass", "tsph_divide_to_cells", "tsph_clear_cells", "tsph_particle_to_cell",
-    "tsph_get_cells", "tsph_pair_digest", "tsph_grid_tables", "tsph_density_to_pressure", "tsph_mdbc_density",
+    "tsph_get_cells", "tsph_pair_digest", "tsph_grid_tables", "tsph_particle_to_cell_noalloc", "tsph_density_to_pressure", "tsph_mdbc_density",
     "tsph_compute_forces", "tsph_symplectic_predictor", "tsph_symplectic_corrector",
     "tsph_remove_out_of_domain", "tsph_step", "tsph_download", "tsph_upload", "tsph_sync",
     "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
@@ -102,6 +102,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_pair_digest.argtypes = [P, P, P, P]
     L.tsph_grid_tables.argtypes = [C.POINTER(_Constants), C.POINTER(_Domain), C.POINTER(I),
                                    C.POINTER(I), P, P]
+    L.tsph_particle_to_cell_noalloc.argtypes = [C.POINTER(_Constants), C.POINTER(_Domain), I, P,
+                                                P, P, P, C.POINTER(I)]
     L.tsph_compute_forces.argtypes = [P, I]
     L.tsph_symplectic_predictor.argtypes = [P, D]
     L.tsph_symplectic_corrector.argtypes = [P, D]
