@@ -1,0 +1,105 @@
+"""Full-size checks on the benchmark workload (720k-particle mDBC dam break,
+dp = 0.0005) through the C ABI: size-independent properties and the oracle at
+full size where it finishes in seconds.
+
+* cell lists and the in-support pair-set digest: bit-exact against the oracle;
+* one fused time step against the oracle's time step (FP32 tolerances);
+* determinism: two identical runs give bit-identical states;
+* mass conservation (no particle leaves the domain in the first steps) and a
+  clean health word.
+"""
+
+import numpy as np
+import pytest
+
+from tinysph_old_gb300 import cases
+
+
+@pytest.fixture(scope="module")
+def big_case():
+    return cases.dam_break_benchmark(0.0005)
+
+
+@pytest.fixture(scope="module")
+def big_oracle(oracle_mod, big_case):
+    import os
+    P = oracle_mod.PortSystem.from_case(big_case)
+    P.set_threads(os.cpu_count() or 1)
+    return P
+
+
+@pytest.mark.gpu
+def test_fullsize_cells_and_pair_sets(gpu_tsph, big_case, big_oracle):
+    s = gpu_tsph.ParticleSystem.from_case(big_case, "fp32")
+    start, lst = s.get_cells()
+    s0, l0 = big_oracle.cells()
+    assert np.array_equal(start, s0)
+    assert np.array_equal(lst, l0)
+    c0, sm0, x0 = big_oracle.pair_digest()
+    c1, sm1, x1 = s.pair_digest()
+    assert np.array_equal(c0, c1)
+    assert np.array_equal(sm0, sm1)
+    assert np.array_equal(x0, x1)
+    # every particle is in exactly one cell, lists ascending
+    assert start[-1] == s.np
+    assert np.array_equal(np.sort(lst), np.arange(s.np))
+
+
+@pytest.mark.gpu
+def test_fullsize_step_matches_oracle(gpu_tsph, oracle_mod, big_case):
+    import os
+    steps = 3
+    s = gpu_tsph.ParticleSystem.from_case(big_case, "fp32")
+    s.step(big_case.wall_model, big_case.dt, steps)
+    got = s.download()
+    P = oracle_mod.PortSystem.from_case(big_case)
+    P.set_threads(os.cpu_count() or 1)
+    P.step(big_case.wall_model, big_case.dt, steps)
+    want = P.state()
+    assert np.array_equal(got["index"], want["index"])
+    fl = want["type"] == 0
+    assert np.max(np.abs(got["r"] - want["r"])) < 1e-9
+    assert np.max(np.abs(got["v"][fl] - want["v"][fl])) < 1e-4
+    assert np.max(np.abs(got["rho"][fl] - want["rho"][fl])) < 2e-3
+    assert np.max(np.abs(got["rho"][~fl] - want["rho"][~fl])) < 2e-2
+    assert np.max(np.abs(got["a"][fl] - want["a"][fl])) < 0.05 + 1e-3 * np.max(np.abs(want["a"][fl]))
+    assert s.health() == 0
+
+
+@pytest.mark.gpu
+def test_fullsize_deterministic_and_conservative(gpu_tsph, big_case):
+    res = []
+    for _ in range(2):
+        s = gpu_tsph.ParticleSystem.from_case(big_case, "fp32")
+        s.step(big_case.wall_model, big_case.dt, 20)
+        res.append(s.download())
+        tot = s.fluid_totals()
+        assert s.np == big_case.np
+        assert np.isclose(tot["mass"], s.mass * int(np.sum(res[-1]["type"] == 0)), rtol=1e-12)
+        assert s.health() == 0
+        s.close()
+    for f in ("r", "v", "rho", "a", "drho", "p"):
+        assert np.array_equal(res[0][f], res[1][f]), f
+
+
+@pytest.mark.gpu
+def test_health_flags_report_bad_states(gpu_tsph):
+    """Failure detection without a GPU fault: a NaN velocity and a particle
+    placed outside the grid are made on the host and uploaded; the device
+    health word reports them and the step keeps running."""
+    case = cases.dam_break_mdbc(dp=0.02)
+    s = gpu_tsph.ParticleSystem.from_case(case, "fp32")
+    st = s.download()
+    fl = np.where(st["type"] == 0)[0]
+    v = st["v"].copy()
+    v[fl[3]] = (np.nan, 0.0)
+    s.upload(v=v)
+    s.step(case.wall_model, case.dt, 1)
+    assert s.health(clear=True) & gpu_tsph.HEALTH_NAN
+    s2 = gpu_tsph.ParticleSystem.from_case(case, "fp32")
+    r = s2.download()["r"].copy()
+    r[fl[4]] = (case.domain[0] - 1.0, 0.1)
+    s2.upload(r=r)
+    s2.particle_to_cell()
+    assert s2.health() & gpu_tsph.HEALTH_ESCAPED
+    assert s2.np == case.np - 1

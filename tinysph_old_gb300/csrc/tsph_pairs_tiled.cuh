@@ -32,7 +32,7 @@ constexpr int kList = 40;       // list entries per target (overflow: global-mem
 struct TileSmem {
     float2 loc[kTileCap];
     float2 vel[kTileCap];
-    float4 rp[kTileCap];  // {rho - rho0, p/rho, 1/rho, 0}
+    float4 rp[kTileCap];  // {rho - rho0, p/rho, 1/rho, rho}
     int foff[3][kTileRows + 3];
     int woff[3][kTileRows + 3];
     float2 off[9];
@@ -55,40 +55,45 @@ struct Acc4 {
 struct TileConst {
     float neg_half_inv_h;  // -0.5 / h
     float eps_h2, four_h2;
-    float k_av_over_2rho0;  // -2 alpha c0 h / (2 rho0)
-    float inv_2rho0;
+    float k_av;             // -2 alpha c0 h: Pi = k_av dr.dv / ((r^2 + eps h^2)(rho_a + rho_b))
     float c1, c2;           // rho0((1 + x)^(1/7) - 1) ~ dy (c1 + c2 dy), x = xg dy
 };
 
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// rb_full = rho_b (full density of the neighbour), ra_full likewise
 __device__ __forceinline__ void pair_terms(float dx, float dy, float dvx, float dvy, float sa,
-                                           float Pa, float Ia, float sb, float Pb, float Ib,
-                                           const TileConst &K, Acc4 &acc) {
-    const float r2 = fmaf(dx, dx, dy * dy);
-    const float r = r2 * rsqrtf(r2);
-    const float w1 = fmaf(r, K.neg_half_inv_h, 1.f);
+                                           float Pa, float Ia, float ra_full, float sb, float Pb,
+                                           float Ib, float rb_full, const TileConst &K, Acc4 &acc) {
+    const float dy2 = dy * dy;
+    const float r2 = fmaf(dx, dx, dy2);
+    const float w1 = fmaf(sqrt_approx(r2), K.neg_half_inv_h, 1.f);
     const float w3 = w1 * w1 * w1;
     const float drdv = fmaf(dx, dvx, dy * dvy);
     const float inv_den = rcp_approx(r2 + K.eps_h2);
     float pterm = fmaf(Pa, Ib, Pb * Ia);
     if (drdv < 0.f) {
-        // 1/(rho_a + rho_b) = 1/(2 rho0) (1 - e + e^2 - e^3), e = (sa + sb)/(2 rho0)
-        const float e = (sa + sb) * K.inv_2rho0;
-        const float ser = fmaf(e, fmaf(e, fmaf(-e, 1.f, 1.f), -1.f), 1.f);
-        pterm = fmaf(K.k_av_over_2rho0 * drdv, inv_den * ser, pterm);
+        // artificial viscosity with the mean density 0.5 (rho_a + rho_b)
+        pterm = fmaf(K.k_av * drdv, inv_den * rcp_approx(ra_full + rb_full), pterm);
     }
     const float coef = w3 * pterm;
     acc.ax = fmaf(-dx, coef, acc.ax);
     acc.ay = fmaf(-dy, coef, acc.ay);
     acc.cont = fmaf(w3, drdv, acc.cont);
-    const float drhoH = dy * fmaf(K.c2, dy, K.c1);
-    const float psi = ((sb - sa) - drhoH) * inv_den;
+    // (rho_b - rho_a) - rho0((1 + x)^(1/7) - 1) with x = 7 g dy / c0^2
+    const float psi = fmaf(-K.c2, dy2, fmaf(-K.c1, dy, sb - sa)) * inv_den;
     acc.diff = fmaf(psi * r2, w3 * Ib, acc.diff);
 }
 
 // per-particle derived quantities of a neighbour: {s, p/rho, 1/rho}
 __device__ __forceinline__ float4 staged_rp(float s, float p, const Phys<float> &P) {
-    const float inv = rcp_approx(P.rho0 + s);
-    return make_float4(s, p * inv, inv, 0.f);
+    const float rho = P.rho0 + s;
+    const float inv = rcp_approx(rho);
+    return make_float4(s, p * inv, inv, rho);
 }
 
 // all in-support neighbours of one target straight from global memory (the
@@ -96,10 +101,11 @@ __device__ __forceinline__ float4 staged_rp(float s, float p, const Phys<float> 
 // for targets whose list overflows)
 template <bool STORED_P>
 __device__ __forceinline__ void target_global(const FluidState<float> &F, const uint32_t *fstart,
-                                           const uint32_t *wstart, const WallState<float> &Wl,
-                                           const Grid &g, const Phys<float> &P, const TileConst &K,
-                                           int i, int cx, int cy, float2 la, float2 va, float sa,
-                                           float Pa, float Ia, Acc4 &acc) {
+                                              const uint32_t *wstart, const WallState<float> &Wl,
+                                              const Grid &g, const Phys<float> &P,
+                                              const TileConst &K, int i, int cx, int cy, float2 la,
+                                              float2 va, float sa, float Pa, float Ia, float Ra,
+                                              Acc4 &acc) {
     for (int dxi = 0; dxi < 3; dxi++) {
         const int col = cx + dxi - 1;
         if (col < 0 || col >= g.ncx) continue;
@@ -121,8 +127,8 @@ __device__ __forceinline__ void target_global(const FluidState<float> &F, const 
                     const float p = STORED_P ? __ldg((kind == 0 ? Wl.p : F.p) + j) : eos(s, P);
                     const float4 rb = staged_rp(s, p, P);
                     const float2 vb = kind == 0 ? make_float2(0.f, 0.f) : __ldg(F.v + j);
-                    pair_terms(dx, dy, va.x - vb.x, va.y - vb.y, sa, Pa, Ia, rb.x, rb.y, rb.z, K,
-                               acc);
+                    pair_terms(dx, dy, va.x - vb.x, va.y - vb.y, sa, Pa, Ia, Ra, rb.x, rb.y, rb.z,
+                               rb.w, K, acc);
                 }
             }
         }
@@ -196,7 +202,7 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
         const bool active = i < we;
         Acc4 acc = {0.f, 0.f, 0.f, 0.f};
         float2 la = make_float2(0.f, 0.f), va = make_float2(0.f, 0.f);
-        float sa = 0.f, Pa = 0.f, Ia = 0.f;
+        float sa = 0.f, Pa = 0.f, Ia = 0.f, Ra = 0.f;
         int cy = 0;
         if (tot <= kTileCap) {
             // ---- stage the neighbour block
@@ -231,8 +237,12 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 sa = rpa.x;
                 Pa = rpa.y;
                 Ia = rpa.z;
-                // ---- phase 1: in-support neighbours into the list (branch-free append)
+                Ra = rpa.w;
+                // ---- phase 1: in-support neighbours into the list.  The list
+                // write is unconditional (the slot is only kept when the pair
+                // is in support); overflow is checked once per cell.
                 int cnt = 0;
+                bool overflow = false;
                 uint16_t *lst = sm.list + tid;
 #pragma unroll
                 for (int dxi = 0; dxi < 3; dxi++) {
@@ -252,41 +262,63 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                                                      : fb[dxi] + sm.foff[dxi][q] - f0[dxi];
                             const int j1 = kind == 0 ? wb[dxi] + sm.woff[dxi][q + 1] - w0[dxi]
                                                      : fb[dxi] + sm.foff[dxi][q + 1] - f0[dxi];
+                            if (cnt + (j1 - j0) > kList) {
+                                overflow = true;
+                                continue;
+                            }
+                            uint16_t *w = lst + cnt * kTileT;
                             if (dyi == 1) {
-                                for (int j = j0; j < j1; j++) {
+                                uint32_t ent = ((uint32_t)j0 << 4) | (uint32_t)code;
+                                for (int j = j0; j < j1; j++, ent += 16u) {
                                     const float2 lb = sm.loc[j];
                                     const float dx = bx - lb.x, dy = by - lb.y;
                                     const uint32_t in = in_support(fmaf(dx, dx, dy * dy), h2bits);
-                                    lst[min(cnt, kList - 1) * kTileT] = (uint16_t)((j << 4) | code);
-                                    cnt += in;
+                                    *w = (uint16_t)ent;
+                                    w += in * kTileT;
                                 }
                             } else if (dyi == 2) {
                                 // row above, ascending y: dy = by - lb.y decreases
-                                for (int j = j0; j < j1; j++) {
+                                uint32_t ent = ((uint32_t)j0 << 4) | (uint32_t)code;
+                                for (int j = j0; j < j1; j++, ent += 16u) {
                                     const float2 lb = sm.loc[j];
                                     const float dx = bx - lb.x, dy = by - lb.y;
                                     if (dy < -reach) break;
                                     const uint32_t in = in_support(fmaf(dx, dx, dy * dy), h2bits);
-                                    lst[min(cnt, kList - 1) * kTileT] = (uint16_t)((j << 4) | code);
-                                    cnt += in;
+                                    *w = (uint16_t)ent;
+                                    w += in * kTileT;
                                 }
                             } else {
                                 // row below, descending y: dy = by - lb.y increases
-                                for (int j = j1 - 1; j >= j0; j--) {
+                                uint32_t ent = ((uint32_t)(j1 - 1) << 4) | (uint32_t)code;
+                                for (int j = j1 - 1; j >= j0; j--, ent -= 16u) {
                                     const float2 lb = sm.loc[j];
                                     const float dx = bx - lb.x, dy = by - lb.y;
                                     if (dy > reach) break;
                                     const uint32_t in = in_support(fmaf(dx, dx, dy * dy), h2bits);
-                                    lst[min(cnt, kList - 1) * kTileT] = (uint16_t)((j << 4) | code);
-                                    cnt += in;
+                                    *w = (uint16_t)ent;
+                                    w += in * kTileT;
                                 }
                             }
+                            cnt = (int)((w - lst) / kTileT);
                         }
                     }
                 }
-                if (cnt <= kList) {
-                    // ---- phase 2: the pair terms over the list
-                    for (int k = 0; k < cnt; k++) {
+                if (!overflow) {
+                    // ---- phase 2: the pair terms over the list, two at a time
+                    int k = 0;
+                    for (; k + 1 < cnt; k += 2) {
+                        const uint32_t e0 = lst[k * kTileT], e1 = lst[(k + 1) * kTileT];
+                        const float2 o0 = sm.off[e0 & 15u], o1 = sm.off[e1 & 15u];
+                        const int j0 = (int)(e0 >> 4), j1 = (int)(e1 >> 4);
+                        const float2 lb0 = sm.loc[j0], lb1 = sm.loc[j1];
+                        const float2 vb0 = sm.vel[j0], vb1 = sm.vel[j1];
+                        const float4 rb0 = sm.rp[j0], rb1 = sm.rp[j1];
+                        pair_terms((la.x + o0.x) - lb0.x, (la.y + o0.y) - lb0.y, va.x - vb0.x,
+                                   va.y - vb0.y, sa, Pa, Ia, Ra, rb0.x, rb0.y, rb0.z, rb0.w, K, acc);
+                        pair_terms((la.x + o1.x) - lb1.x, (la.y + o1.y) - lb1.y, va.x - vb1.x,
+                                   va.y - vb1.y, sa, Pa, Ia, Ra, rb1.x, rb1.y, rb1.z, rb1.w, K, acc);
+                    }
+                    if (k < cnt) {
                         const uint32_t e = lst[k * kTileT];
                         const int j = (int)(e >> 4);
                         const float2 o = sm.off[e & 15u];
@@ -294,11 +326,11 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                         const float2 vb = sm.vel[j];
                         const float4 rb = sm.rp[j];
                         pair_terms((la.x + o.x) - lb.x, (la.y + o.y) - lb.y, va.x - vb.x,
-                                   va.y - vb.y, sa, Pa, Ia, rb.x, rb.y, rb.z, K, acc);
+                                   va.y - vb.y, sa, Pa, Ia, Ra, rb.x, rb.y, rb.z, rb.w, K, acc);
                     }
                 } else {
                     target_global<STORED_P>(F, fstart, wstart, Wl, g, P, K, i, cx, cy, la, va, sa,
-                                            Pa, Ia, acc);
+                                            Pa, Ia, Ra, acc);
                 }
             }
         } else if (active) {
@@ -310,8 +342,9 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
             const float4 rpa = staged_rp(sa, p, P);
             Pa = rpa.y;
             Ia = rpa.z;
+            Ra = rpa.w;
             target_global<STORED_P>(F, fstart, wstart, Wl, g, P, K, i, cx, cy, la, va, sa, Pa, Ia,
-                                    acc);
+                                    Ra, acc);
         }
         if (active) {
             const float mb = P.m * P.bwen_h;
@@ -358,8 +391,7 @@ inline TileConst make_tile_const(const Phys<float> &P, double h, double rho0, do
     K.neg_half_inv_h = (float)(-0.5 / h);
     K.eps_h2 = P.eps_h2;
     K.four_h2 = P.four_h2;
-    K.k_av_over_2rho0 = (float)((double)P.k_av / (2.0 * rho0));
-    K.inv_2rho0 = (float)(1.0 / (2.0 * rho0));
+    K.k_av = P.k_av;
     const double xg = 7.0 * g / (cs * cs);
     K.c1 = (float)(rho0 * xg / 7.0);
     K.c2 = (float)(-rho0 * 3.0 / 49.0 * xg * xg);
