@@ -145,22 +145,20 @@ template <typename T> class Engine final : public EngineBase {
         return Nbr<T>{W_.r, W_.loc, wall_zero_v_, W_.rho, stored_p ? W_.p : nullptr};
     }
 
-    // scan counts[0..ncells] -> fstart[0..ncells+1]
+    // scan counts[0..ncells] -> fstart[0..ncells+1]; leaves counts zeroed
     int scan(std::string &err) {
         const int n = ncells_ + 1;
         const int ntiles = (n + kScanTile - 1) / kScanTile;
         int rc;
-        if ((rc = launch(CAT_SORT, k_scan_tiles, ntiles, kScanThreads, err, (const uint32_t *)counts_,
-                         fstart_, tile_sums_, n)))
+        if ((rc = launch(CAT_SORT, k_scan_tiles_clear, ntiles, kScanThreads, err, counts_, fstart_,
+                         tile_sums_, n)))
             return rc;
-        if ((rc = launch(CAT_SORT, k_scan_sums, 1, kScanThreads, err, tile_sums_, ntiles, fstart_, n)))
-            return rc;
-        return launch(CAT_SORT, k_scan_add, blocks_for(n), kBlock, err, fstart_,
-                      (const uint32_t *)tile_sums_, n);
+        return launch(CAT_SORT, k_scan_add_tiles, blocks_for(n), kBlock, err, fstart_,
+                      (const uint32_t *)tile_sums_, ntiles, n);
     }
 
     // after keys/slots are in keyB_/slotB_ and counts_ is filled:
-    // scan, stable placement, gather of the source arrays into D (+ old state)
+    // scan, stable placement, rank + scatter of the source arrays into D (+ old state)
     int sort_finish(const double2 *sr, const T2 *sv, const T *srho, const uint32_t *sid,
                     const T2 *sa, const T *sdrho, const T *sp, FluidState<T> D,
                     const double2 *or2, const T2 *ov2, const T *orho2, OldState<T> Od,
@@ -175,18 +173,16 @@ template <typename T> class Engine final : public EngineBase {
                          (const uint32_t *)slotB_, sid, ntot, (const uint32_t *)fstart_, tmp_id_,
                          tmp_src_, by_y ? sr : (const double2 *)nullptr, tmp_y_)))
             return rc;
-        if ((rc = launch(CAT_SORT, k_rank, nb, kBlock, err, (const uint32_t *)keyB_, ntot,
-                         (const uint32_t *)fstart_, (const uint32_t *)tmp_id_,
-                         (const uint32_t *)tmp_src_, perm_, ncells_,
-                         by_y ? (const long long *)tmp_y_ : (const long long *)nullptr)))
-            return rc;
-        return launch(CAT_SORT, k_gather<T>, nb, kBlock, err, (const uint32_t *)perm_, ntot, grid_,
-                      sr, sv, srho, sid, (const uint32_t *)keyB_, sa, sdrho, sp, D, or2, ov2, orho2,
-                      Od);
+        return launch(CAT_SORT, k_rank_scatter<T>, nb, kBlock, err, (const uint32_t *)keyB_, ntot,
+                      (const uint32_t *)fstart_, (const uint32_t *)tmp_id_,
+                      (const uint32_t *)tmp_src_,
+                      by_y ? (const long long *)tmp_y_ : (const long long *)nullptr, grid_, sr, sv,
+                      srho, sid, sa, sdrho, sp, D, or2, ov2, orho2, Od);
     }
 
+    // the histogram is zero between sorts (the scan clears it)
     int zero_counts(std::string &err) {
-        TSPH_CK(cudaMemsetAsync(counts_, 0, sizeof(uint32_t) * (ncells_ + 1), st_));
+        (void)err;
         return 0;
     }
 
@@ -357,6 +353,7 @@ template <typename T> class Engine final : public EngineBase {
             return rc;
         TSPH_CK(cudaMemset(health_, 0, 4));
         TSPH_CK(cudaMemset(removed_, 0, 4));
+        TSPH_CK(cudaMemset(counts_, 0, sizeof(uint32_t) * (ncells_ + 1)));
         // staging
         if ((rc = alloc(&S_.r, ntot_, err)) || (rc = alloc(&S_.v, ntot_, err)) ||
             (rc = alloc(&S_.a, ntot_, err)) || (rc = alloc(&S_.rho, ntot_, err)) ||

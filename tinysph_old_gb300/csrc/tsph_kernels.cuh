@@ -245,6 +245,60 @@ static __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32
     if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
 }
 
+// the same, and the histogram is left zeroed for its next use
+static __global__ void __launch_bounds__(kScanThreads) k_scan_tiles_clear(uint32_t *__restrict__ in,
+                                                                         uint32_t *__restrict__ out,
+                                                                         uint32_t *__restrict__ tile_sums,
+                                                                         int n) {
+    const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        v[k] = (base + k < n) ? in[base + k] : 0u;
+        if (base + k < n) in[base + k] = 0u;
+        s += v[k];
+    }
+    uint32_t total;
+    uint32_t off = block_exclusive_scan(s, &total);
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        if (base + k < n) out[base + k] = off;
+        off += v[k];
+    }
+    if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
+}
+
+// add the tile offsets; each block sums the tile totals before its own tile
+// (at most a few hundred), the last block writes the grand total to out[n]
+static __global__ void k_scan_add_tiles(uint32_t *__restrict__ out,
+                                        const uint32_t *__restrict__ tile_sums, int ntiles, int n) {
+    __shared__ uint32_t red[kBlock / 32];
+    const int i0 = blockIdx.x * blockDim.x;
+    const int t = i0 / kScanTile;
+    const bool last = blockIdx.x == gridDim.x - 1;
+    const int upto = last ? ntiles : t;
+    uint32_t acc = 0;
+    for (int u = threadIdx.x; u < upto; u += blockDim.x) acc += tile_sums[u];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    uint32_t tot = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += red[w];
+    uint32_t off = tot;
+    if (last) {
+        // total of all tiles; the offset of this block's own tile excludes it
+        if (threadIdx.x == 0) out[n] = tot;
+        uint32_t mine = 0;
+        if (t < ntiles) mine = tile_sums[t];
+        uint32_t after = 0;
+        for (int u = t + 1; u < ntiles; u++) after += tile_sums[u];
+        off = tot - mine - after;
+    }
+    const int i = i0 + threadIdx.x;
+    if (i < n) out[i] += off;
+}
+
 static __global__ void __launch_bounds__(kScanThreads) k_scan_sums(uint32_t *__restrict__ tile_sums, int ntiles,
                                                            uint32_t *__restrict__ out, int n) {
     // one block; ntiles <= kScanTile
@@ -316,6 +370,63 @@ static __global__ void k_rank(const uint32_t *__restrict__ key, const int *__res
         for (uint32_t m = lo; m < hi; m++) rank += (tmp_id[m] < me) ? 1u : 0u;
     }
     perm[lo + rank] = src;
+}
+
+// rank (as k_rank) and move the particle's record straight to its final
+// slot: D[final] = src[s], recomputing loc; optional acceleration, density
+// rate, pressure and old state travel along
+template <typename T>
+__global__ void k_rank_scatter(const uint32_t *__restrict__ key, const int *__restrict__ n_ptr,
+                               const uint32_t *__restrict__ start, const uint32_t *__restrict__ tmp_id,
+                               const uint32_t *__restrict__ tmp_src, const long long *__restrict__ tmp_y,
+                               Grid g, const double2 *__restrict__ sr,
+                               const typename V2<T>::t *__restrict__ sv, const T *__restrict__ srho,
+                               const uint32_t *__restrict__ sid,
+                               const typename V2<T>::t *__restrict__ sa, const T *__restrict__ sdrho,
+                               const T *__restrict__ sp, FluidState<T> D,
+                               const double2 *__restrict__ or2, const typename V2<T>::t *__restrict__ ov2,
+                               const T *__restrict__ orho2, OldState<T> O) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *n_ptr) return;
+    const uint32_t src = tmp_src[j];
+    const uint32_t k = key[src];
+    uint32_t f = (uint32_t)j;
+    if (k != (uint32_t)g.ncells) {
+        const uint32_t lo = start[k], hi = start[k + 1];
+        const uint32_t me = tmp_id[j];
+        uint32_t rank = 0;
+        if (tmp_y) {
+            const long long my = tmp_y[j];
+            for (uint32_t m = lo; m < hi; m++) {
+                const long long ym = tmp_y[m];
+                rank += (ym < my || (ym == my && tmp_id[m] < me)) ? 1u : 0u;
+            }
+        } else {
+            for (uint32_t m = lo; m < hi; m++) rank += (tmp_id[m] < me) ? 1u : 0u;
+        }
+        f = lo + rank;
+    }
+    const double2 r = sr[src];
+    D.r[f] = r;
+    D.v[f] = sv[src];
+    D.rho[f] = srho[src];
+    D.id[f] = sid[src];
+    D.key[f] = k;
+    if (k < (uint32_t)g.ncells) {
+        const int cx = (int)(k / (uint32_t)g.ncy);
+        const int cy = (int)k - cx * g.ncy;
+        D.loc[f] = cell_local(g, r, cx, cy);
+    } else {
+        D.loc[f] = make_float2(0.f, 0.f);
+    }
+    if (sa) D.a[f] = sa[src];
+    if (sdrho) D.drho[f] = sdrho[src];
+    if (sp) D.p[f] = sp[src];
+    if (or2) {
+        O.r[f] = or2[src];
+        O.v[f] = ov2[src];
+        O.rho[f] = orho2[src];
+    }
 }
 
 // ------------------------------------------------------------- EOS
@@ -496,10 +607,12 @@ k_fluid_pairs(FluidState<T> F, const uint32_t *__restrict__ fstart,
             for (int j = j0; j < j1; j++) {
                 if (part == 1 && j == i) continue;
                 if constexpr (MODE == MODE_DIGEST) {
+                    // the reference's support test in FP64 with no FMA
+                    // contraction: r/h <= 2, r = sqrt(dx*dx + dy*dy)
                     const double2 rb = __ldg(N.r + j);
-                    const double drx = ra.x - rb.x, dry = ra.y - rb.y;
-                    const double drs = sqrt((drx * drx) + (dry * dry));
-                    if ((drs / P.hd) <= 2.0) {
+                    const double drx = __dsub_rn(ra.x, rb.x), dry = __dsub_rn(ra.y, rb.y);
+                    const double drs = __dsqrt_rn(__dadd_rn(__dmul_rn(drx, drx), __dmul_rn(dry, dry)));
+                    if (__ddiv_rn(drs, P.hd) <= 2.0) {
                         const int nid = part == 0 ? (int)wid[j] : (int)F.id[j];
                         dcount++;
                         dsum += nid;
@@ -620,9 +733,9 @@ k_wall_rows(WallState<T> Wl, int nw, const uint32_t *__restrict__ fstart, Nbr<T>
             for (int j = j0; j < j1; j++) {
                 if (digest) {
                     const double2 rb = __ldg(NF.r + j);
-                    const double drx = ra.x - rb.x, dry = ra.y - rb.y;
-                    const double drs = sqrt((drx * drx) + (dry * dry));
-                    if ((drs / P.hd) <= 2.0) {
+                    const double drx = __dsub_rn(ra.x, rb.x), dry = __dsub_rn(ra.y, rb.y);
+                    const double drs = __dsqrt_rn(__dadd_rn(__dmul_rn(drx, drx), __dmul_rn(dry, dry)));
+                    if (__ddiv_rn(drs, P.hd) <= 2.0) {
                         const int nid = (int)fid[j];
                         dcount++;
                         dsum += nid;
@@ -846,6 +959,8 @@ __global__ void k_predict_bin(FluidState<T> F, const uint32_t *__restrict__ fsta
     nv.x = v.x + a.x * dt * T(0.5);
     nv.y = v.y + a.y * dt * T(0.5);
     Bv[f] = nv;
+    if (!(nv.x == nv.x) || !(nv.y == nv.y) || !is_finite_d(rn.x) || !is_finite_d(rn.y))
+        atomicOr(health, kHealthNan);
     int cx, cy;
     const uint32_t k = cell_key(g, rn, F.key[f], &cx, &cy);
     if (k == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);

@@ -445,11 +445,13 @@ k_mdbc8(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidS
                 } else {
                     wendland32(r2, P, W, Fk, true);
                 }
-                const float V = P.m * rcp_approx(P.rho0 + __ldg(F.rho + j));
-                s[0] += W;
-                s[1] = fmaf(drx, Fk, s[1]);
-                s[2] = fmaf(dry, Fk, s[2]);
+                const float sb = __ldg(F.rho + j);  // rho_b - rho0
+                const float V = P.m * rcp_approx(P.rho0 + sb);
                 const float WV = W * V, FV = Fk * V;
+                // right-hand side of the density field shifted by rho0
+                s[0] = fmaf(WV, sb, s[0]);
+                s[1] = fmaf(drx * FV, sb, s[1]);
+                s[2] = fmaf(dry * FV, sb, s[2]);
                 s[3] += WV;
                 s[4] = fmaf(drx, WV, s[4]);
                 s[5] = fmaf(dry, WV, s[5]);
@@ -469,8 +471,13 @@ k_mdbc8(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidS
         s[q] += __shfl_xor_sync(0xffffffffu, s[q], 1);
     }
     if (!valid || sub != 0) return;
-    const double m = (double)P.m;
-    const double rhoWsum = (double)s[0] * m, drhodx = (double)s[1] * m, drhody = (double)s[2] * m;
+    // The reference solves A x = (sum m W, sum m dr_x F, sum m dr_y F) for
+    // x = (rho, grad rho).  With m = V_b rho_b and A's first column
+    // (sum V W, sum V dr_x F, sum V dr_y F), the same system with the
+    // right-hand side sum V (rho_b - rho0) (W, dr_x F, dr_y F) has the
+    // solution (rho - rho0, grad rho): identical in exact arithmetic, ~1000x
+    // smaller numbers (and rounding errors) in FP32.
+    const double rhoWsum = s[0], drhodx = s[1], drhody = s[2];
     const double a11 = s[3], a12 = s[4], a13 = s[5], a21 = s[6], a22 = s[7], a23 = s[8],
                  a31 = s[9], a32 = s[10], a33 = s[11];
     const double det = det3(a11, a12, a13, a21, a22, a23, a31, a32, a33);
@@ -490,14 +497,14 @@ k_mdbc8(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidS
         const double grx = -(rhoWsum * i21 + drhodx * i22 + drhody * i23);
         const double gry = -(rhoWsum * i31 + drhodx * i32 + drhody * i33);
         const float2 gnd = Wl.gnd[w];
-        dens = dens_temp + grx * (double)gnd.x + gry * (double)gnd.y;
+        dens = dens_temp + grx * (double)gnd.x + gry * (double)gnd.y;  // rho - rho0
     } else if (a11 > 0) {
-        dens = rhoWsum / a11;
+        dens = rhoWsum / a11;  // Shepard, shifted
     } else {
-        dens = 1000.;
+        dens = 1000. - (double)P.rho0;
     }
-    if (dens < 1000.) dens = 1000.;
-    Wl.rho[w] = (float)(dens - (double)P.rho0);
+    if (dens + (double)P.rho0 < 1000.) dens = 1000. - (double)P.rho0;  // clamp of src/SPH_mDBC.h:44
+    Wl.rho[w] = (float)dens;
 }
 
 }  // namespace tsph
