@@ -230,6 +230,72 @@ typedef struct {
 int tsph_set_profiling(tsph_system *s, int on);
 int tsph_get_profile(tsph_system *s, tsph_profile_t *out, int reset);
 
+/* ==================================================================
+ * Riemann / ALE-SPH (cases/ALESPH_dambreakLong/MUSCL.h path): leap-frog in
+ * omega (volume), omega*rho and omega*v (src/RALESPH_integration.h), the
+ * one-sided MUSCL gradients (src/_testMUSCL_gradientApprox.h) and the flux
+ * loop with the linearised Riemann solver (src/_testMUSCL_interaction.h,
+ * src/ALESPH_riemann_solver.h).  BT walls carry a normal each (special.n).
+ * FP32 fluxes, FP64 integration of the conserved variables.
+ * ================================================================== */
+typedef struct tsph_ale_system tsph_ale_system;
+
+/* interface states of the flux loop: as the reference computes them
+ * (MUSCL_final adds 0.5 dt/dx (F(W_L) - F(W_L)) = 0 and the neighbour state
+ * carries the active particle's velocity, src/_testMUSCL_interaction.h:185,
+ * src/_testMUSCL_schemes.h:78-88), or the superbee-limited MUSCL states of
+ * both particles (no counterpart in the reference) */
+enum { TSPH_ALE_AS_WRITTEN = 0, TSPH_ALE_MUSCL = 1 };
+
+/* host view; any pointer may be NULL.  grad: 12 per particle (rho, vx, vy
+ * forward x/y, then backward x/y: special.grad*F, grad*B), valid from
+ * tsph_ale_gradient until the particles are next re-binned.  p is the
+ * reference's p: the equation of state of the density that the last flux pass
+ * used (Density_to_pressure runs before the fluxes, not after the leap-frog) */
+typedef struct {
+    double *r, *v, *rho, *p;
+    double *omega, *omegarho, *omegav, *domega, *domegarho, *domegav, *grad;
+    int32_t *index, *type;
+} tsph_ale_host_state;
+
+enum {
+    TSPH_ALE_F_R = 1 << 0, TSPH_ALE_F_V = 1 << 1, TSPH_ALE_F_RHO = 1 << 2, TSPH_ALE_F_P = 1 << 3,
+    TSPH_ALE_F_OMEGA = 1 << 4, TSPH_ALE_F_OMEGARHO = 1 << 5, TSPH_ALE_F_OMEGAV = 1 << 6,
+    TSPH_ALE_F_RATES = 1 << 7, TSPH_ALE_F_GRAD = 1 << 8, TSPH_ALE_F_INDEX = 1 << 9,
+    TSPH_ALE_F_TYPE = 1 << 10
+};
+
+/* Particle_system + Simulation_data for the ALE path */
+int tsph_ale_create(const tsph_constants *c, const tsph_domain *d, void *stream,
+                    tsph_ale_system **out);
+int tsph_ale_destroy(tsph_ale_system *s);
+/* ALESPH_Add_particle (src/SPH_particle_system.h:51-108: omega = dp^2,
+ * omega*v, omega*rho) for n particles; `normal` (2n, may be NULL for fluid)
+ * is special.n of the wall particles (src/ALESPH_create.h:719) */
+int tsph_ale_add_particles(tsph_ale_system *s, int n, const int32_t *type, const double *r,
+                           const double *v, const double *rho, const double *p,
+                           const double *normal);
+int tsph_ale_set_scheme(tsph_ale_system *s, int scheme);
+int tsph_ale_np(tsph_ale_system *s, int *np);
+/* Divide_To_Cells + Particle_To_Cell, src/SPH_find_pairs.h:5-72 */
+int tsph_ale_divide_to_cells(tsph_ale_system *s);
+int tsph_ale_particle_to_cell(tsph_ale_system *s);
+/* Kernel_gradient_approx, src/_testMUSCL_gradientApprox.h:10-231 */
+int tsph_ale_gradient(tsph_ale_system *s);
+/* Compute_Forces(particles, dt), src/_testMUSCL_interaction.h:13-324 */
+int tsph_ale_forces(tsph_ale_system *s, double dt);
+/* Integrate_LeapFrog_partOne / partTwo, src/RALESPH_integration.h:10-107 */
+int tsph_ale_leapfrog_one(tsph_ale_system *s, double dt);
+int tsph_ale_leapfrog_two(tsph_ale_system *s, double dt, int step);
+/* nsteps bodies of SPH_simulation::RUN of cases/ALESPH_dambreakLong/MUSCL.h:82-137
+ * (steps step0+1 .. step0+nsteps); the gradient pass runs only for
+ * TSPH_ALE_MUSCL (the as-written fluxes do not depend on it) */
+int tsph_ale_step(tsph_ale_system *s, double dt, int step0, int nsteps);
+int tsph_ale_download(tsph_ale_system *s, int fields, const tsph_ale_host_state *out);
+int tsph_ale_upload(tsph_ale_system *s, int fields, const tsph_ale_host_state *in);
+int tsph_ale_sync(tsph_ale_system *s);
+int tsph_ale_health(tsph_ale_system *s, uint32_t *flags, int clear);
+
 #ifdef __cplusplus
 }
 #endif

@@ -22,6 +22,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libtsph_ref.so")
+REF_ALE_LIB = os.path.join(HERE, "_ref", "libtsph_ref_ale.so")
 
 F_RX, F_RY, F_VX, F_VY, F_AX, F_AY, F_RHO, F_DRHO, F_P = range(9)
 F_ROX, F_ROY, F_VOX, F_VOY, F_RHO_O = range(9, 14)
@@ -100,6 +101,16 @@ def _load_port():
         L.orc_pressure.restype = _D
         L.orc_pressure_to_density.argtypes = [_D, _D, _D]
         L.orc_pressure_to_density.restype = _D
+        L.orc_ale_add_particle.argtypes = [_P, _I] + [_D] * 6
+        L.orc_ale_add_normal.argtypes = [_P, _D, _D]
+        L.orc_ale_get_field.argtypes = [_P, _I, _DP]
+        L.orc_ale_set_field.argtypes = [_P, _I, _DP]
+        L.orc_ale_set_scheme.argtypes = [_P, _I]
+        L.orc_ale_gradient.argtypes = [_P]
+        L.orc_ale_forces.argtypes = [_P, _D]
+        L.orc_ale_leapfrog_one.argtypes = [_P, _D]
+        L.orc_ale_leapfrog_two.argtypes = [_P, _D, _I]
+        L.orc_ale_step.argtypes = [_P, _D, _I, _I]
         _port = L
     return _port
 
@@ -396,3 +407,199 @@ def wendland(r, h):
     w, f = _D(), _D()
     L.orc_wendland(r, h, C.byref(w), C.byref(f))
     return w.value, f.value
+
+
+# ---------------------------------------------------------------- ALE-SPH
+_ref_ale = None
+
+
+def _load_ref_ale():
+    global _ref_ale
+    if _ref_ale is None:
+        L = C.CDLL(REF_ALE_LIB)
+        L.refale_create.restype = _P
+        L.refale_create.argtypes = [_D] * 11
+        L.refale_destroy.argtypes = [_P]
+        L.refale_set_threads.argtypes = [_I]
+        L.refale_add_particle.argtypes = [_P, _I] + [_D] * 6
+        L.refale_add_normal.argtypes = [_P, _D, _D]
+        L.refale_create_wall_x_bt.argtypes = [_P, _D, _D, _D, _I, _D, _D]
+        L.refale_create_wall_y_bt.argtypes = [_P, _D, _D, _D, _I, _D, _D]
+        L.refale_create_corner_bt.argtypes = [_P, _I, _I, _D, _D, _D, _D]
+        L.refale_create_block_of_fluid.argtypes = [_P] + [_D] * 4
+        L.refale_np.argtypes = [_P]
+        L.refale_np.restype = _I
+        L.refale_nn.argtypes = [_P]
+        L.refale_nn.restype = _I
+        L.refale_get_normals.argtypes = [_P, _DP]
+        L.refale_get_state.argtypes = [_P] + [_P] * 13
+        L.refale_set_velocity_density.argtypes = [_P, _DP, _DP]
+        for f in ("refale_divide_to_cells", "refale_particle_to_cell",
+                  "refale_density_to_pressure", "refale_gradient"):
+            getattr(L, f).argtypes = [_P]
+        L.refale_forces.argtypes = [_P, _D]
+        L.refale_leapfrog_one.argtypes = [_P, _D]
+        L.refale_leapfrog_two.argtypes = [_P, _D, _I]
+        L.refale_step.argtypes = [_P, _D, _I, _I]
+        _ref_ale = L
+    return _ref_ale
+
+
+def ref_ale_available() -> bool:
+    if not os.path.exists(REF_ALE_LIB):
+        return False
+    try:
+        C.CDLL(REF_ALE_LIB)
+        return True
+    except OSError:
+        return False
+
+
+ALE_FIELDS = ("omega", "omegarho", "omegavx", "omegavy", "domega", "domegarho", "domegavx",
+              "domegavy")
+
+
+class PortAle(PortSystem):
+    """The oracle's ALE-SPH functions on a PortSystem."""
+
+    @classmethod
+    def from_case(cls, case, divide=True):
+        o = cls(case.h, case.kap, case.cs, case.rho0, case.visco, case.delta, case.dp,
+                case.domain)
+        ps = case.particles
+        for i in range(ps.np):
+            o.L.orc_ale_add_particle(o.s, ps.type[i], ps.p[i], ps.rho[i], ps.rx[i], ps.ry[i],
+                                     ps.vx[i], ps.vy[i])
+        for n in ps.normals:
+            o.L.orc_ale_add_normal(o.s, n[0], n[1])
+        if divide:
+            o.divide_to_cells()
+            o.particle_to_cell()
+        return o
+
+    def ale_field(self, f):
+        out = np.empty(self.np(), dtype=np.float64)
+        self.L.orc_ale_get_field(self.s, f, out)
+        return out
+
+    def set_ale_field(self, f, arr):
+        self.L.orc_ale_set_field(self.s, f, np.ascontiguousarray(arr, dtype=np.float64))
+
+    def ale_state(self):
+        st = self.state()
+        g = self.ale_field
+        st.update(omega=g(0), omegarho=g(1), omegav=np.stack([g(2), g(3)], 1), domega=g(4),
+                  domegarho=g(5), domegav=np.stack([g(6), g(7)], 1),
+                  grad=np.stack([g(12 + k) for k in range(12)], 1))
+        return st
+
+    def set_velocity_density(self, v, rho):
+        """Fluid v and rho with omega*v, omega*rho kept consistent."""
+        st = self.state()
+        fl = st["type"] == 0
+        om = self.ale_field(0)
+        vv = st["v"].copy(); rr = st["rho"].copy()
+        vv[fl] = v[fl]; rr[fl] = rho[fl]
+        self.set_state(v=vv, rho=rr)
+        omv = np.stack([self.ale_field(2), self.ale_field(3)], 1)
+        omv[fl] = vv[fl] * om[fl, None]
+        omr = self.ale_field(1)
+        omr[fl] = rr[fl] * om[fl]
+        self.set_ale_field(2, omv[:, 0]); self.set_ale_field(3, omv[:, 1])
+        self.set_ale_field(1, omr)
+
+    def set_scheme(self, scheme):
+        self.L.orc_ale_set_scheme(self.s, int(scheme))
+
+    def gradient(self):
+        self.L.orc_ale_gradient(self.s)
+
+    def ale_forces(self, dt):
+        self.L.orc_ale_forces(self.s, dt)
+
+    def leapfrog_one(self, dt):
+        self.L.orc_ale_leapfrog_one(self.s, dt)
+
+    def leapfrog_two(self, dt, step):
+        self.L.orc_ale_leapfrog_two(self.s, dt, int(step))
+
+    def ale_step(self, dt, step0, n):
+        self.L.orc_ale_step(self.s, dt, int(step0), int(n))
+
+
+class RefAle:
+    """The reference's ALE-SPH code (oracle/_ref/libtsph_ref_ale.so)."""
+
+    def __init__(self, case):
+        self.L = _load_ref_ale()
+        self.s = self.L.refale_create(case.h, case.kap, case.cs, case.rho0, case.visco,
+                                      case.delta, case.dp, *case.domain)
+
+    @classmethod
+    def from_case(cls, case, divide=True):
+        o = cls(case)
+        ps = case.particles
+        for i in range(ps.np):
+            o.L.refale_add_particle(o.s, ps.type[i], ps.p[i], ps.rho[i], ps.rx[i], ps.ry[i],
+                                    ps.vx[i], ps.vy[i])
+        for n in ps.normals:
+            o.L.refale_add_normal(o.s, n[0], n[1])
+        if divide:
+            o.L.refale_divide_to_cells(o.s)
+            o.L.refale_particle_to_cell(o.s)
+        return o
+
+    def __del__(self):
+        try:
+            self.L.refale_destroy(self.s)
+        except Exception:
+            pass
+
+    @staticmethod
+    def set_threads(n):
+        _load_ref_ale().refale_set_threads(int(n))
+
+    def np(self):
+        return self.L.refale_np(self.s)
+
+    def ale_state(self):
+        n = self.np()
+        out = dict(r=np.empty((n, 2)), v=np.empty((n, 2)), rho=np.empty(n), p=np.empty(n),
+                   type=np.empty(n, dtype=np.int32), index=np.empty(n, dtype=np.int32),
+                   omega=np.empty(n), omegarho=np.empty(n), omegav=np.empty((n, 2)),
+                   domega=np.empty(n), domegarho=np.empty(n), domegav=np.empty((n, 2)),
+                   grad=np.empty((n, 12)))
+        k = ("r", "v", "rho", "p", "type", "index", "omega", "omegarho", "omegav", "domega",
+             "domegarho", "domegav", "grad")
+        self.L.refale_get_state(self.s, *[_ptr(out[x]) for x in k])
+        return out
+
+    def normals(self):
+        out = np.empty((self.L.refale_nn(self.s), 2))
+        self.L.refale_get_normals(self.s, out.reshape(-1))
+        return out
+
+    def set_velocity_density(self, v, rho):
+        self.L.refale_set_velocity_density(self.s, np.ascontiguousarray(v, dtype=np.float64).reshape(-1),
+                                           np.ascontiguousarray(rho, dtype=np.float64))
+
+    def particle_to_cell(self):
+        self.L.refale_particle_to_cell(self.s)
+
+    def density_to_pressure(self):
+        self.L.refale_density_to_pressure(self.s)
+
+    def gradient(self):
+        self.L.refale_gradient(self.s)
+
+    def ale_forces(self, dt):
+        self.L.refale_forces(self.s, dt)
+
+    def leapfrog_one(self, dt):
+        self.L.refale_leapfrog_one(self.s, dt)
+
+    def leapfrog_two(self, dt, step):
+        self.L.refale_leapfrog_two(self.s, dt, int(step))
+
+    def ale_step(self, dt, step0, n):
+        self.L.refale_step(self.s, dt, int(step0), int(n))

@@ -24,6 +24,7 @@
  * counted as escaped and not binned (the reference indexes out of range).
  */
 #include "tsph_oracle.h"
+#include "tsph_oracle_internal.h"
 
 #include <math.h>
 #include <stdlib.h>
@@ -32,44 +33,24 @@
 #include <omp.h>
 #endif
 
-#define ORC_EPS 0.01 /* src/SPH_defs.h:69 */
-
-struct orc_sys {
-    int np, cap;
-    int *index;
-    int *type;
-    double *p, *rho, *drho;
-    double *rx, *ry, *vx, *vy, *ax, *ay;
-    double *rox, *roy, *vox, *voy, *rho_o;
-    /* mDBC ghost nodes, indexed by particle index (src/SPH_data.h:51) */
-    int ngnr, gcap;
-    double *gx, *gy;
-    /* SPH_constants (src/SPH_data.h:30-46) */
-    double h, kap, dp, cs, rho0, gravy, avisc, delta, m;
-    /* Simulation_data (src/SPH_data.h:111-122): padded domain */
-    double x0, xm, y0, ym;
-    /* cells as CSR: cell c holds cell_list[cell_start[c] .. cell_start[c+1]) */
-    int ncx, ncy, ncells;
-    int *cell_start, *cell_list, *cell_count;
-    int cells_built;
-    int escaped;
-};
-
-static void *xrealloc(void *p, size_t n) {
+void *orc_xrealloc(void *p, size_t n) {
     void *q = realloc(p, n ? n : 1);
     if (!q) abort();
     return q;
 }
 
-static void grow(orc_sys *s, int need) {
+void orc_grow(orc_sys *s, int need) {
     if (need <= s->cap) return;
     int c = s->cap ? s->cap : 256;
     while (c < need) c *= 2;
-    s->index = xrealloc(s->index, sizeof(int) * c);
-    s->type = xrealloc(s->type, sizeof(int) * c);
-#define G(f) s->f = xrealloc(s->f, sizeof(double) * c)
+    s->index = orc_xrealloc(s->index, sizeof(int) * c);
+    s->type = orc_xrealloc(s->type, sizeof(int) * c);
+#define G(f) s->f = orc_xrealloc(s->f, sizeof(double) * c)
     G(p); G(rho); G(drho); G(rx); G(ry); G(vx); G(vy); G(ax); G(ay);
     G(rox); G(roy); G(vox); G(voy); G(rho_o);
+    G(om); G(omr); G(omvx); G(omvy); G(om_o); G(omr_o); G(omvx_o); G(omvy_o);
+    G(dom); G(domr); G(domvx); G(domvy);
+    for (int k = 0; k < 12; k++) s->grad[k] = orc_xrealloc(s->grad[k], sizeof(double) * c);
 #undef G
     s->cap = c;
 }
@@ -105,6 +86,10 @@ void orc_destroy(orc_sys *s) {
     free(s->vx); free(s->vy); free(s->ax); free(s->ay); free(s->rox);
     free(s->roy); free(s->vox); free(s->voy); free(s->rho_o);
     free(s->gx); free(s->gy);
+    free(s->om); free(s->omr); free(s->omvx); free(s->omvy); free(s->om_o); free(s->omr_o);
+    free(s->omvx_o); free(s->omvy_o); free(s->dom); free(s->domr); free(s->domvx);
+    free(s->domvy); free(s->nx); free(s->ny);
+    for (int k = 0; k < 12; k++) free(s->grad[k]);
     free(s->cell_start); free(s->cell_list); free(s->cell_count);
     free(s);
 }
@@ -128,7 +113,7 @@ int orc_get_threads(void) {
 /* Add_particle, src/SPH_particle_system.h:25-50 */
 void orc_add_particle(orc_sys *s, int type, double p, double rho, double rx,
                       double ry, double vx, double vy, double ax, double ay) {
-    grow(s, s->np + 1);
+    orc_grow(s, s->np + 1);
     int i = s->np++;
     s->type[i] = type;
     s->index[i] = i;
@@ -141,6 +126,10 @@ void orc_add_particle(orc_sys *s, int type, double p, double rho, double rx,
     s->rox[i] = rx; s->roy[i] = ry;
     s->vox[i] = vx; s->voy[i] = vy;
     s->rho_o[i] = rho;
+    s->om[i] = s->omr[i] = s->omvx[i] = s->omvy[i] = 0.;
+    s->om_o[i] = s->omr_o[i] = s->omvx_o[i] = s->omvy_o[i] = 0.;
+    s->dom[i] = s->domr[i] = s->domvx[i] = s->domvy[i] = 0.;
+    for (int k = 0; k < 12; k++) s->grad[k][i] = 0.;
     s->cells_built = 0;
 }
 
@@ -148,8 +137,8 @@ void orc_add_particle(orc_sys *s, int type, double p, double rho, double rx,
 void orc_add_gnr(orc_sys *s, double gx, double gy) {
     if (s->ngnr + 1 > s->gcap) {
         int c = s->gcap ? s->gcap * 2 : 256;
-        s->gx = xrealloc(s->gx, sizeof(double) * c);
-        s->gy = xrealloc(s->gy, sizeof(double) * c);
+        s->gx = orc_xrealloc(s->gx, sizeof(double) * c);
+        s->gy = orc_xrealloc(s->gy, sizeof(double) * c);
         s->gcap = c;
     }
     s->gx[s->ngnr] = gx;
@@ -300,8 +289,8 @@ void orc_divide_to_cells(orc_sys *s) {
     s->ncx = (int)((s->xm - s->x0 + of) / kh) + 1;
     s->ncy = (int)((s->ym - s->y0 + of) / kh) + 1;
     s->ncells = s->ncx * s->ncy;
-    s->cell_start = xrealloc(s->cell_start, sizeof(int) * (s->ncells + 1));
-    s->cell_count = xrealloc(s->cell_count, sizeof(int) * (s->ncells + 1));
+    s->cell_start = orc_xrealloc(s->cell_start, sizeof(int) * (s->ncells + 1));
+    s->cell_count = orc_xrealloc(s->cell_count, sizeof(int) * (s->ncells + 1));
     memset(s->cell_start, 0, sizeof(int) * (s->ncells + 1));
     s->cells_built = 0;
 }
@@ -330,7 +319,7 @@ void orc_particle_to_cell(orc_sys *s) {
     const int nc = s->ncells;
     int *cnt = s->cell_count;
     memset(cnt, 0, sizeof(int) * (nc + 1));
-    s->cell_list = xrealloc(s->cell_list, sizeof(int) * (s->np ? s->np : 1));
+    s->cell_list = orc_xrealloc(s->cell_list, sizeof(int) * (s->np ? s->np : 1));
     int *key = malloc(sizeof(int) * (s->np ? s->np : 1));
     if (!key) abort();
     s->escaped = 0;
@@ -565,11 +554,21 @@ void orc_corrector(orc_sys *s, double dt) {
 
 /* Remove_particle, src/SPH_particle_system.h:110-146 (order-preserving
  * erase of every per-particle vector; gnr is not touched, :144) */
-static void erase_particle(orc_sys *s, int p) {
+void orc_erase_particle(orc_sys *s, int p) {
     const int tail = s->np - p - 1;
 #define E(f) memmove(s->f + p, s->f + p + 1, sizeof(s->f[0]) * tail)
     E(index); E(type); E(p); E(rho); E(drho); E(rx); E(ry); E(vx); E(vy);
     E(ax); E(ay); E(rox); E(roy); E(vox); E(voy); E(rho_o);
+    if (s->ale) {
+        E(om); E(omr); E(omvx); E(omvy); E(om_o); E(omr_o); E(omvx_o); E(omvy_o);
+        E(dom); E(domr); E(domvx); E(domvy);
+        for (int k = 0; k < 12; k++) E(grad[k]);
+        if (p < s->nn) {
+            memmove(s->nx + p, s->nx + p + 1, sizeof(double) * (s->nn - p - 1));
+            memmove(s->ny + p, s->ny + p + 1, sizeof(double) * (s->nn - p - 1));
+            s->nn--;
+        }
+    }
 #undef E
     s->np--;
 }
@@ -585,7 +584,7 @@ int orc_remove_out_of_domain(orc_sys *s) {
         const double rx = s->rx[p], ry = s->ry[p];
         if ((ry < (y0 - ORC_EPS)) || (ry > ym + ORC_EPS) || (rx < x0 - ORC_EPS) ||
             (rx > xm - ORC_EPS)) {
-            erase_particle(s, p);
+            orc_erase_particle(s, p);
             removed++;
         }
     }

@@ -73,6 +73,21 @@ void orc_step(orc_sys *s, int model, double dt, int nsteps);
 /* in-support pair-set digest (count, sum and xor of neighbour indices) */
 void orc_pair_digest(const orc_sys *s, int *count, long long *sum, int *xr);
 
+/* ---- ALE-SPH (cases/ALESPH_dambreakLong/MUSCL.h path) ---- */
+void orc_ale_add_particle(orc_sys *s, int type, double p, double rho, double rx, double ry,
+                          double vx, double vy);
+void orc_ale_add_normal(orc_sys *s, double nx, double ny);
+void orc_ale_get_field(const orc_sys *s, int f, double *out);
+void orc_ale_set_field(orc_sys *s, int f, const double *in);
+/* 0: the reference's fluxes (default); 1: superbee MUSCL interface states of
+ * both particles (no counterpart in the reference) */
+void orc_ale_set_scheme(orc_sys *s, int scheme);
+void orc_ale_gradient(orc_sys *s);
+void orc_ale_forces(orc_sys *s, double dt);
+void orc_ale_leapfrog_one(orc_sys *s, double dt);
+void orc_ale_leapfrog_two(orc_sys *s, double dt, int step);
+void orc_ale_step(orc_sys *s, double dt, int step0, int nsteps);
+
 /* scalar kernels, exported for unit tests */
 void orc_wendland(double r, double h, double *w, double *f);
 double orc_pressure(double rho, double rho0, double c0);

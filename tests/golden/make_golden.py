@@ -3,7 +3,8 @@
 Runs the reference's own code (oracle/_ref/libtsph_ref.so, compiled from the
 reference headers by ``make -C oracle ref``) on small seeded cases and stores
 its outputs.  Needs the reference sources; the committed .npz files are what
-the tests read.  Usage: python tests/golden/make_golden.py
+the tests read.  Usage: python tests/golden/make_golden.py [ale]  (``ale``
+regenerates only the ALE-SPH fixture, from oracle/_ref/libtsph_ref_ale.so)
 """
 
 import os
@@ -110,6 +111,60 @@ def run_case(case, model, nsteps, rng, snap_every):
     return out
 
 
+def ale_geometry(dp):
+    """The reference's BT generators for cases/ALESPH_dambreakLong/geometry.h."""
+    case = cases.dam_break_ale(dp=dp)
+    R = O.RefAle(case)
+    L, s = R.L, R.s
+    L.refale_create_wall_x_bt(s, 0.0 + dp, 1.61 - dp, 0.0, -1, 0.0, 1.0)
+    L.refale_create_wall_y_bt(s, 0.0, 0.0 + dp, 1.0, -1, 1.0, 0.0)
+    L.refale_create_wall_y_bt(s, 1.61, 0.0 + dp, 1.0, +1, -1.0, 0.0)
+    L.refale_create_corner_bt(s, -1, -1, 0.0, 0.0, np.sqrt(2), np.sqrt(2))
+    L.refale_create_corner_bt(s, +1, -1, 1.61, 0.0, -np.sqrt(2), np.sqrt(2))
+    L.refale_create_block_of_fluid(s, 0.0 + dp, 0 + dp, 0.6, 0.3)
+    st = R.ale_state()
+    return dict(r=st["r"], type=st["type"], rho=st["rho"], omega=st["omega"],
+                normals=R.normals())
+
+
+def run_ale(case, nsteps, rng, snap_every):
+    """Riemann / ALE-SPH dam break (cases/ALESPH_dambreakLong/MUSCL.h RUN loop)
+    from a seeded perturbation of the fluid velocity and density."""
+    O.RefAle.set_threads(1)
+    R = O.RefAle.from_case(case)
+    st0 = R.ale_state()
+    fl = st0["type"] == 0
+    v = st0["v"].copy()
+    rho = st0["rho"].copy()
+    v[fl] += rng.normal(0.0, 0.05, size=(fl.sum(), 2))
+    rho[fl] *= 1.0 + 1e-3 * rng.standard_normal(fl.sum())
+    R.set_velocity_density(v, rho)
+    init = R.ale_state()
+    out = {f"init_{k}": init[k] for k in ("r", "v", "rho", "type", "omega", "omegarho", "omegav")}
+    out["normals"] = R.normals()
+    # per-function outputs at the perturbed initial state
+    R.density_to_pressure()
+    R.gradient()
+    R.ale_forces(case.dt)
+    f = R.ale_state()
+    for k in ("grad", "domega", "domegarho", "domegav"):
+        out[f"forces_{k}"] = f[k]
+    R2 = O.RefAle.from_case(case)
+    R2.set_velocity_density(v, rho)
+    done = 0
+    while done < nsteps:
+        R2.ale_step(case.dt, done, snap_every)
+        done += snap_every
+        st = R2.ale_state()
+        for k in ("r", "v", "rho", "p", "omega", "omegarho", "omegav", "domega", "domegarho",
+                  "domegav", "index"):
+            out[f"step{done}_{k}"] = st[k]
+    out["dt"] = np.float64(case.dt)
+    out["nsteps"] = np.int64(nsteps)
+    out["snap_every"] = np.int64(snap_every)
+    return out
+
+
 def wendland_samples():
     rng = np.random.default_rng(SEED)
     h = np.array([0.001, np.sqrt(2) * 0.005, 0.0075, 0.04])
@@ -122,7 +177,22 @@ def wendland_samples():
     return np.array(rows)
 
 
+def main_ale():
+    """ALE-SPH fixtures (own seed, so the WCSPH fixtures do not change)."""
+    if not O.ref_ale_available():
+        raise SystemExit("reference ALE harness not available (needs the reference sources)")
+    rng = np.random.default_rng(SEED + 1)
+    out = {}
+    for k, v in ale_geometry(0.02).items():
+        out[f"geom_{k}"] = v
+    out.update(run_ale(cases.dam_break_ale(dp=0.02), 6, rng, 2))
+    np.savez_compressed(os.path.join(HERE, "dam_break_ale_dp0.02.npz"), **out)
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "ale":
+        main_ale()
+        return
     if O.build_ref() is None or not O.ref_available():
         raise SystemExit("reference harness not available (needs the reference sources)")
     rng = np.random.default_rng(SEED)
@@ -142,6 +212,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "still_water_dbc_dp0.02.npz"), **sw)
     # 4. Wendland kernel samples
     np.savez_compressed(os.path.join(HERE, "wendland.npz"), samples=wendland_samples())
+    # 5. Riemann / ALE-SPH dam break, 6 steps
+    main_ale()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

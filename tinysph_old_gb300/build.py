@@ -29,6 +29,7 @@ UNITS = [
     ("tsph_engine_f32.cu", []),
     ("tsph_engine_f64.cu", ["-fmad=false"]),
     ("tsph_noalloc.cu", []),
+    ("tsph_ale.cu", []),
 ]
 
 

@@ -1,0 +1,1168 @@
+// tsph_ale.cu -- the Riemann / ALE-SPH step on the GPU (cases/ALESPH_dambreakLong/
+// MUSCL.h path): FP32 fluxes, FP64 integration of omega, omega*rho, omega*v.
+//
+// State in HBM (fluid, sorted by cell like the WCSPH engine): r FP64, loc
+// FP32 (cell-local position), the conserved omega / omega*rho (FP64) and
+// omega*v (FP64 x2), their leap-frog copies, the rates (FP32), and the
+// derived rho - rho0 and v (FP32) that the flux loop reads.  Walls (one BT
+// layer with normals) are static and binned once.
+//
+// Kernels per step: k_ale_lf1 (leap-frog part one, in place: particles do
+// not move), k_ale_grad (one-sided gradients; only for the MUSCL scheme),
+// k_ale_flux (the pair loop), k_ale_lf2_bin (part two + out-of-domain +
+// cell and histogram slot), then the counting sort (scan, k_place,
+// k_ale_rank_scatter).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/tsph.h"
+#include "tsph_engine.h"
+#include "tsph_grid_host.h"
+#include "tsph_kernels.cuh"
+
+namespace tsph {
+namespace {
+
+struct AleFluid {
+    double2 *r;
+    float2 *loc;
+    uint32_t *key, *id;
+    double *om, *omr;
+    double2 *omv;
+    double *om_o, *omr_o;
+    double2 *omv_o;
+    float *dom, *domr;
+    float2 *domv;
+    float *s;   // rho - rho0
+    float2 *v;
+    float *ps;  // rho - rho0 at the last Density_to_pressure (the reference's p)
+    float *grad;  // 12 per particle, valid until the next re-binning
+};
+
+struct AleWalls {
+    double2 *r;
+    float2 *loc;
+    uint32_t *key, *id;
+    float2 *n;
+    float *s;
+};
+
+struct AleConst {
+    float h, inv_h, m, c0, rho0, g, dp, four_h2, awen, bwen_h, b_eos;
+    float dx_exact;  // below this |dx| the FP32 cell-local difference may carry the wrong sign
+};
+
+__device__ __forceinline__ float ale_eos(float s, const AleConst &K) {
+    const float x = s / K.rho0;
+    return K.b_eos * x * (7.f + x * (21.f + x * (35.f + x * (35.f + x * (21.f + x * (7.f + x))))));
+}
+
+// W and (dW/dr)/r of the Wendland kernel for 0 < r2 <= 4h^2
+__device__ __forceinline__ void ale_wendland(float r2, const AleConst &K, float &W, float &F) {
+    const float r = r2 * rsqrtf(r2);
+    const float w1 = fmaf(-0.5f * K.inv_h, r, 1.f);
+    const float w2 = w1 * w1;
+    F = K.bwen_h * w2 * w1;
+    W = K.awen * fmaf(2.f * K.inv_h, r, 1.f) * w2 * w2;
+}
+
+// MUSCL_superBee slope D, src/_testMUSCL_schemes.h:33-77
+__device__ __forceinline__ float superbee(float gFx, float gFy, float gBx, float gBy, float dx,
+                                          float dy) {
+    const float DF = gFx * dx + gFy * dy, DB = gBx * dx + gBy * dy;
+    if (DF > 0.f) return fmaxf(0.f, fmaxf(fminf(2.f * DB, DF), fminf(DB, DF)));
+    if (DF < 0.f) return fminf(0.f, fminf(fmaxf(2.f * DB, DF), fmaxf(DB, DF)));
+    return 0.f;
+}
+
+__device__ __forceinline__ void derive(double om, double omr, double2 omv, float rho0, float &s,
+                                       float2 &v) {
+    // rho = omega*rho / omega, v = omega*v / (rho omega), src/RALESPH_integration.h:31-32;
+    // rho - rho0 from the FP64 numerator keeps its precision in FP32
+    const double num = fma(-(double)rho0, om, omr);
+    const float omf = (float)om;
+    s = (float)num / omf;
+    const float omrf = (float)omr;
+    v = make_float2((float)omv.x / omrf, (float)omv.y / omrf);
+}
+
+__device__ __forceinline__ int n_live_ale(const uint32_t *fstart, int ncells) {
+    return (int)__ldg(fstart + ncells);
+}
+
+// Integrate_LeapFrog_partOne, src/RALESPH_integration.h:10-36 (in place)
+__global__ void k_ale_lf1(AleFluid F, const uint32_t *__restrict__ fstart, int ncells, double dt,
+                          float rho0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_live_ale(fstart, ncells)) return;
+    const double om = F.om[i], omr = F.omr[i];
+    const double2 omv = F.omv[i];
+    F.om_o[i] = om;
+    F.omr_o[i] = omr;
+    F.omv_o[i] = omv;
+    const double h = dt * 0.5;
+    const double om2 = om + (double)F.dom[i] * h, omr2 = omr + (double)F.domr[i] * h;
+    const float2 dv = F.domv[i];
+    const double2 omv2 = make_double2(omv.x + (double)dv.x * h, omv.y + (double)dv.y * h);
+    F.om[i] = om2;
+    F.omr[i] = omr2;
+    F.omv[i] = omv2;
+    float s;
+    float2 v;
+    derive(om2, omr2, omv2, rho0, s, v);
+    F.s[i] = s;
+    F.v[i] = v;
+}
+
+// Integrate_LeapFrog_partTwo, src/RALESPH_integration.h:38-107, for target i:
+// returns the new position and writes the new conserved state to D[o]
+__device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int o, double dt,
+                                       int step, float rho0) {
+    double2 r = F.r[i];
+    // the reference's p was computed from the density the fluxes used
+    const float s_flux = F.s[i];
+    const float2 dv = F.domv[i];
+    double om, omr;
+    double2 omv;
+    if (step == 1) {
+        const double om0 = F.om[i], omr0 = F.omr[i];
+        const double2 omv0 = F.omv[i];
+        D.om_o[o] = om0;
+        D.omr_o[o] = omr0;
+        D.omv_o[o] = omv0;
+        const double h = dt * 0.5;
+        om = om0 + (double)F.dom[i] * h;
+        omr = omr0 + (double)F.domr[i] * h;
+        omv = make_double2(omv0.x + (double)dv.x * h, omv0.y + (double)dv.y * h);
+        float s;
+        float2 v;
+        derive(om, omr, omv, rho0, s, v);
+        r = make_double2(r.x + (double)v.x * dt * 0.5, r.y + (double)v.y * dt * 0.5);
+        D.s[o] = s;
+        D.v[o] = v;
+    } else {
+        const float2 v0 = F.v[i];
+        r = make_double2(r.x + (double)v0.x * dt, r.y + (double)v0.y * dt);
+        om = F.om_o[i] + (double)F.dom[i] * dt;
+        omr = F.omr_o[i] + (double)F.domr[i] * dt;
+        const double2 o2 = F.omv_o[i];
+        omv = make_double2(o2.x + (double)dv.x * dt, o2.y + (double)dv.y * dt);
+        float s;
+        float2 v;
+        derive(om, omr, omv, rho0, s, v);
+        D.s[o] = s;
+        D.v[o] = v;
+        D.om_o[o] = F.om_o[i];
+        D.omr_o[o] = F.omr_o[i];
+        D.omv_o[o] = o2;
+    }
+    D.om[o] = om;
+    D.omr[o] = omr;
+    D.omv[o] = omv;
+    D.dom[o] = F.dom[i];
+    D.domr[o] = F.domr[i];
+    D.domv[o] = dv;
+    D.id[o] = F.id[i];
+    D.r[o] = r;
+    D.ps[o] = s_flux;
+    return r;
+}
+
+// part two in place (per-function entry point)
+__global__ void k_ale_lf2(AleFluid F, const uint32_t *__restrict__ fstart, int ncells, double dt,
+                          int step, float rho0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_live_ale(fstart, ncells)) return;
+    lf2(F, i, F, i, dt, step, rho0);
+}
+
+// part two out of place + RemoveParticlesOutOfDomain (src/SPH_btdebug.h:4-31)
+// + cell and histogram slot of the new position
+__global__ void k_ale_lf2_bin(AleFluid F, const uint32_t *__restrict__ fstart, Grid g, double dt,
+                              int step, float rho0, Box box, AleFluid D,
+                              uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
+                              uint32_t *__restrict__ counts, uint32_t *__restrict__ health) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_live_ale(fstart, g.ncells)) return;
+    const double2 rn = lf2(F, i, D, i, dt, step, rho0);
+    const float2 v = D.v[i];
+    if (!(v.x == v.x) || !(v.y == v.y) || !(D.s[i] == D.s[i])) atomicOr(health, kHealthNan);
+    uint32_t k;
+    if (out_of_domain(rn, box)) {
+        k = (uint32_t)g.ncells;
+        atomicOr(health, kHealthRemoved);
+    } else {
+        int cx, cy;
+        k = cell_key(g, rn, F.key[i], &cx, &cy);
+        if (k == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
+    }
+    key[i] = k;
+    slot[i] = atomicAdd(counts + k, 1u);
+}
+
+// cell key of the current positions (per-function Particle_To_Cell)
+__global__ void k_ale_bin(AleFluid F, const uint32_t *__restrict__ fstart, Grid g,
+                          uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
+                          uint32_t *__restrict__ counts, uint32_t *__restrict__ health) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_live_ale(fstart, g.ncells)) return;
+    int cx, cy;
+    uint32_t k = F.key[i];
+    if (k != (uint32_t)g.ncells) {
+        k = cell_key(g, F.r[i], k, &cx, &cy);
+        if (k == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
+    }
+    key[i] = k;
+    slot[i] = atomicAdd(counts + k, 1u);
+}
+
+// rank inside the cell by particle index and move the record (+ loc)
+__global__ void k_ale_rank_scatter(const uint32_t *__restrict__ key, const int *__restrict__ n_ptr,
+                                   const uint32_t *__restrict__ start,
+                                   const uint32_t *__restrict__ tmp_id,
+                                   const uint32_t *__restrict__ tmp_src, Grid g, AleFluid S,
+                                   AleFluid D) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= *n_ptr) return;
+    const uint32_t src = tmp_src[j];
+    const uint32_t k = key[src];
+    uint32_t f = (uint32_t)j;
+    if (k != (uint32_t)g.ncells) {
+        const uint32_t lo = start[k], hi = start[k + 1];
+        const uint32_t me = tmp_id[j];
+        uint32_t rank = 0;
+        for (uint32_t m = lo; m < hi; m++) rank += tmp_id[m] < me ? 1u : 0u;
+        f = lo + rank;
+    }
+    const double2 r = S.r[src];
+    D.r[f] = r;
+    D.key[f] = k;
+    D.id[f] = S.id[src];
+    if (k < (uint32_t)g.ncells) {
+        const int cx = (int)(k / (uint32_t)g.ncy), cy = (int)k - cx * g.ncy;
+        D.loc[f] = cell_local(g, r, cx, cy);
+    }
+    D.om[f] = S.om[src];
+    D.omr[f] = S.omr[src];
+    D.omv[f] = S.omv[src];
+    D.om_o[f] = S.om_o[src];
+    D.omr_o[f] = S.omr_o[src];
+    D.omv_o[f] = S.omv_o[src];
+    D.dom[f] = S.dom[src];
+    D.domr[f] = S.domr[src];
+    D.domv[f] = S.domv[src];
+    D.s[f] = S.s[src];
+    D.v[f] = S.v[src];
+    D.ps[f] = S.ps[src];
+}
+
+// neighbour at larger x (dx = x_a - x_b < 0) -> forward sums, smaller x ->
+// backward sums, equal x -> neither (src/_testMUSCL_gradientApprox.h:135-178).
+// The split is discontinuous in x_a - x_b, so its sign is taken from the FP64
+// positions whenever the FP32 difference is within its rounding error
+// (particles of one lattice column stay within ~1e-8 m of each other for
+// many steps).
+__device__ __forceinline__ float exact_side(float dx, double xa, const double2 *rb, int j,
+                                            const AleConst &K) {
+    if (fabsf(dx) >= K.dx_exact) return dx;
+    const double d = xa - __ldg(&rb[j].x);
+    return d < 0.0 ? -1.f : (d > 0.0 ? 1.f : 0.f);
+}
+
+__device__ __forceinline__ void accumulate_side(float gF[6], float gB[6], float dx,
+                                                const float t[6]) {
+    const float wf = dx < 0.f ? 1.f : 0.f, wb = dx > 0.f ? 1.f : 0.f;
+#pragma unroll
+    for (int q = 0; q < 6; q++) {
+        gF[q] = fmaf(wf, t[q], gF[q]);
+        gB[q] = fmaf(wb, t[q], gB[q]);
+    }
+}
+
+// Kernel_gradient_approx, src/_testMUSCL_gradientApprox.h:10-231: forward
+// (neighbour at larger x) / backward one-sided gradients of rho, vx, vy,
+// walls through their normals, x2; zero when no neighbour is in support.
+__global__ void __launch_bounds__(kBlock)
+k_ale_grad(AleFluid F, const uint32_t *__restrict__ fstart, const uint32_t *__restrict__ wstart,
+           AleWalls Wl, Grid g, AleConst K) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_live_ale(fstart, g.ncells)) return;
+    const uint32_t key = F.key[i];
+    const int cx = (int)(key / (uint32_t)g.ncy), cy = (int)key - cx * g.ncy;
+    const float2 la = F.loc[i], va = F.v[i];
+    const float sa = F.s[i];
+    const double xa = F.r[i].x;
+    float gF[6] = {0, 0, 0, 0, 0, 0}, gB[6] = {0, 0, 0, 0, 0, 0};
+    float gamma = 0.f;
+    for (int dxi = 0; dxi < 3; dxi++) {
+        const int col = cx + dxi - 1;
+        if (col < 0 || col >= g.ncx) continue;
+        for (int dyi = 0; dyi < 3; dyi++) {
+            const int row = cy + dyi - 1;
+            if (row < 0 || row >= g.ncy) continue;
+            const int c = col * g.ncy + row;
+            const float bx = la.x + (float)(1 - dxi) * g.khf, by = la.y + (float)(1 - dyi) * g.khf;
+            for (int j = (int)__ldg(wstart + c); j < (int)__ldg(wstart + c + 1); j++) {
+                const float2 lb = __ldg(Wl.loc + j);
+                const float dx = bx - lb.x, dy = by - lb.y;
+                const float r2 = fmaf(dx, dx, dy * dy);
+                if (!(r2 <= K.four_h2)) continue;
+                float W, Fk;
+                if (r2 == 0.f) { W = K.awen; Fk = 0.f; } else ale_wendland(r2, K, W, Fk);
+                const float2 n = __ldg(Wl.n + j);
+                const float nbx = -n.x, nby = -n.y;
+                const float sb = __ldg(Wl.s + j);
+                const float wdp = W * K.dp;
+                const float t[6] = {(sb - sa) * nbx * wdp, (sb - sa) * nby * wdp,
+                                    -va.x * nbx * wdp,     -va.x * nby * wdp,
+                                    -va.y * nbx * wdp,     -va.y * nby * wdp};
+                accumulate_side(gF, gB, exact_side(dx, xa, Wl.r, j, K), t);
+                gamma += W * K.m / (K.rho0 + sb);
+            }
+            for (int j = (int)__ldg(fstart + c); j < (int)__ldg(fstart + c + 1); j++) {
+                if (j == i) continue;
+                const float2 lb = __ldg(F.loc + j);
+                const float dx = bx - lb.x, dy = by - lb.y;
+                const float r2 = fmaf(dx, dx, dy * dy);
+                if (!(r2 <= K.four_h2)) continue;
+                float W, Fk;
+                if (r2 == 0.f) { W = K.awen; Fk = 0.f; } else ale_wendland(r2, K, W, Fk);
+                const float sb = __ldg(F.s + j);
+                const float2 vb = __ldg(F.v + j);
+                const float nom = (float)__ldg(F.om + j);
+                const float dWx = dx * Fk, dWy = dy * Fk;
+                const float ds = (sb - sa) * nom, dvx = (vb.x - va.x) * nom,
+                            dvy = (vb.y - va.y) * nom;
+                const float t[6] = {ds * dWx, ds * dWy, dvx * dWx, dvx * dWy, dvy * dWx, dvy * dWy};
+                accumulate_side(gF, gB, exact_side(dx, xa, F.r, j, K), t);
+                gamma += W * K.m / (K.rho0 + sb);
+            }
+        }
+    }
+    float *o = F.grad + (size_t)12 * i;
+    for (int q = 0; q < 6; q++) {
+        o[q] = gamma == 0.f ? 0.f : gF[q] * 2.f;
+        o[6 + q] = gamma == 0.f ? 0.f : gB[q] * 2.f;
+    }
+}
+
+// does fluid particle j (sorted index) have any neighbour with W > 0?
+__device__ bool ale_has_support(const AleFluid &F, const uint32_t *fstart, const uint32_t *wstart,
+                                const AleWalls &Wl, const Grid &g, const AleConst &K, int j) {
+    const uint32_t key = F.key[j];
+    const int cx = (int)(key / (uint32_t)g.ncy), cy = (int)key - cx * g.ncy;
+    const float2 la = F.loc[j];
+    for (int dxi = 0; dxi < 3; dxi++) {
+        const int col = cx + dxi - 1;
+        if (col < 0 || col >= g.ncx) continue;
+        for (int dyi = 0; dyi < 3; dyi++) {
+            const int row = cy + dyi - 1;
+            if (row < 0 || row >= g.ncy) continue;
+            const int c = col * g.ncy + row;
+            const float bx = la.x + (float)(1 - dxi) * g.khf, by = la.y + (float)(1 - dyi) * g.khf;
+            for (int kind = 0; kind < 2; kind++) {
+                const uint32_t *st = kind ? fstart : wstart;
+                for (int n = (int)st[c]; n < (int)st[c + 1]; n++) {
+                    if (kind && n == j) continue;
+                    const float2 lb = kind ? F.loc[n] : Wl.loc[n];
+                    const float dx = bx - lb.x, dy = by - lb.y;
+                    if (fmaf(dx, dx, dy * dy) < K.four_h2) return true;
+                }
+            }
+        }
+    }
+    return false;
+}
+
+// Compute_Forces(particles, dt), src/_testMUSCL_interaction.h:13-324, FP32.
+// SCHEME 0 (as written): the interface states are the particle states and the
+// neighbour's velocity is the active particle's (:184-200 with MUSCL_final
+// returning its third argument), so vL = vR = v_a . n_ab.  SCHEME 1: the
+// superbee MUSCL states of both particles (left of a, right of b).
+template <int SCHEME>
+__global__ void __launch_bounds__(kBlock)
+k_ale_flux(AleFluid F, const uint32_t *__restrict__ fstart, const uint32_t *__restrict__ wstart,
+           AleWalls Wl, Grid g, AleConst K) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_live_ale(fstart, g.ncells)) return;
+    const uint32_t key = F.key[i];
+    const int cx = (int)(key / (uint32_t)g.ncy), cy = (int)key - cx * g.ncy;
+    const float2 la = F.loc[i], va = F.v[i];
+    const float sa = F.s[i];
+    const float rhoa = K.rho0 + sa;
+    const float ao = (float)F.om[i];
+    float gA[12];
+    if (SCHEME == 1)
+        for (int q = 0; q < 12; q++) gA[q] = F.grad[(size_t)12 * i + q];
+    float dom = 0.f, domr = 0.f, dvx_s = 0.f, dvy_s = 0.f, gamma = 0.f;
+    for (int dxi = 0; dxi < 3; dxi++) {
+        const int col = cx + dxi - 1;
+        if (col < 0 || col >= g.ncx) continue;
+        for (int dyi = 0; dyi < 3; dyi++) {
+            const int row = cy + dyi - 1;
+            if (row < 0 || row >= g.ncy) continue;
+            const int c = col * g.ncy + row;
+            const float bx = la.x + (float)(1 - dxi) * g.khf, by = la.y + (float)(1 - dyi) * g.khf;
+            // BT wall neighbours, :253-265, :275-281
+            for (int j = (int)__ldg(wstart + c); j < (int)__ldg(wstart + c + 1); j++) {
+                const float2 lb = __ldg(Wl.loc + j);
+                const float dx = bx - lb.x, dy = by - lb.y;
+                const float r2 = fmaf(dx, dx, dy * dy);
+                if (!(r2 <= K.four_h2) || r2 == 0.f) continue;
+                float W, Fk;
+                ale_wendland(r2, K, W, Fk);
+                const float2 n = __ldg(Wl.n + j);
+                const float nbx = -n.x, nby = -n.y;
+                const float vn = va.x * nbx + va.y * nby;
+                const float ps = ale_eos(sa + rhoa * vn / K.c0, K);
+                const float wdp = W * K.dp;
+                dvx_s -= 2.f * wdp * (ps * nbx);
+                dvy_s -= 2.f * wdp * (ps * nby);
+                dom -= vn * wdp;
+                gamma += W * K.m / (K.rho0 + __ldg(Wl.s + j));
+            }
+            for (int j = (int)__ldg(fstart + c); j < (int)__ldg(fstart + c + 1); j++) {
+                if (j == i) continue;
+                const float2 lb = __ldg(F.loc + j);
+                const float dx = bx - lb.x, dy = by - lb.y;
+                const float r2 = fmaf(dx, dx, dy * dy);
+                if (!(r2 <= K.four_h2) || r2 == 0.f) continue;
+                float W, Fk;
+                ale_wendland(r2, K, W, Fk);
+                const float sb = __ldg(F.s + j);
+                const float2 vb = __ldg(F.v + j);
+                const float no = (float)__ldg(F.om + j);
+                const float dWx = dx * Fk, dWy = dy * Fk;
+                const float inv_r = rsqrtf(r2);
+                const float nx = -dx * inv_r, ny = -dy * inv_r;  // pair normal
+                float vL, vR, sL, sR;
+                if (SCHEME == 0) {
+                    vL = va.x * nx + va.y * ny;
+                    vR = vL;
+                    sL = sa;
+                    sR = sb;
+                } else {
+                    float gB[12];
+                    for (int q = 0; q < 12; q++) gB[q] = __ldg(F.grad + (size_t)12 * j + q);
+                    sL = sa - superbee(gA[0], gA[1], gA[6], gA[7], dx, dy);
+                    const float vLx = va.x - superbee(gA[2], gA[3], gA[8], gA[9], dx, dy);
+                    const float vLy = va.y - superbee(gA[4], gA[5], gA[10], gA[11], dx, dy);
+                    sR = sb + superbee(gB[0], gB[1], gB[6], gB[7], dx, dy);
+                    const float vRx = vb.x + superbee(gB[2], gB[3], gB[8], gB[9], dx, dy);
+                    const float vRy = vb.y + superbee(gB[4], gB[5], gB[10], gB[11], dx, dy);
+                    vL = vLx * nx + vLy * ny;
+                    vR = vRx * nx + vRy * ny;
+                }
+                const float rbar = K.rho0 + 0.5f * (sa + sb);
+                // velRiemannLinearized / densRiemannLinearized,
+                // src/ALESPH_riemann_solver.h:6-18,86-96
+                const float vss = 0.5f * (vR + vL) - 0.5f * (sR - sL) * K.c0 / rbar;
+                const float ss = 0.5f * (sL + sR) + 0.5f * (vL - vR) * rbar / K.c0;
+                const float ps = ale_eos(ss, K);
+                const float rhos = K.rho0 + ss;
+                const float h2 = 0.5f * (vL + vR);
+                const float vsx = nx * vss + (0.5f * (va.x + vb.x) - nx * h2);
+                const float vsy = ny * vss + (0.5f * (va.y + vb.y) - ny * h2);
+                const float ex = vsx - va.x, ey = vsy - va.y;
+                const float vsdW = ex * dWx + ey * dWy;
+                dvx_s -= 2.f * no * ((rhos * vsx * ex + ps) * dWx + (rhos * vsx * ey) * dWy);
+                dvy_s -= 2.f * no * ((rhos * vsy * ex) * dWx + (rhos * vsy * ey + ps) * dWy);
+                const float dvdW = (va.x - vb.x) * dWx + (va.y - vb.y) * dWy;
+                dom -= dvdW * no;
+                domr -= 2.f * rhos * no * vsdW;
+                gamma += W * K.m / (K.rho0 + sb);
+            }
+        }
+    }
+    bool zero = gamma == 0.f;
+    if (zero) {
+        // the reference's gamma_sum is not reset between the particles of a
+        // cell (:49, :299): a particle without neighbours still gets the
+        // gravity term when an earlier particle of its cell had some
+        const uint32_t me = F.id[i];
+        const int c = cx * g.ncy + cy;
+        for (int j = (int)fstart[c]; j < (int)fstart[c + 1] && zero; j++)
+            if (j != i && F.id[j] < me && ale_has_support(F, fstart, wstart, Wl, g, K, j)) zero = false;
+    }
+    if (zero) {
+        F.dom[i] = 0.f;
+        F.domr[i] = 0.f;
+        F.domv[i] = make_float2(0.f, 0.f);
+    } else {
+        F.dom[i] = dom * ao;
+        F.domr[i] = domr * ao;
+        F.domv[i] = make_float2(dvx_s * ao, dvy_s * ao - K.g * ao * rhoa);
+    }
+}
+
+#define ACK(call)                                                                 \
+    do {                                                                          \
+        cudaError_t e_ = (call);                                                  \
+        if (e_ != cudaSuccess) {                                                  \
+            err = std::string(#call) + ": " + cudaGetErrorString(e_);             \
+            return TSPH_ERR_CUDA;                                                 \
+        }                                                                         \
+    } while (0)
+
+inline int nblk(long long n) { return (int)std::max<long long>(1, (n + kBlock - 1) / kBlock); }
+
+}  // namespace
+
+// host-side ALE system: particles, grid tables, device buffers
+class AleEngine {
+  public:
+    // host setup
+    double h = 0, kap = 0, cs = 0, rho0 = 0, visco = 0, delta = 0, dp = 0, m = 0;
+    double x0 = 0, xm = 0, y0 = 0, ym = 0, kh = 0, of = 0;
+    int ncx = 0, ncy = 0, ncells = 0;
+    std::vector<long long> bx, by;
+    std::vector<double> ox, oy;
+    std::vector<int> type;
+    std::vector<double> r, v, rho, p, nrm;
+    int scheme = TSPH_ALE_AS_WRITTEN;
+    bool divided = false, built = false, cells = false;
+    cudaStream_t st = nullptr;
+    bool own = false;
+
+    // device
+    int nf = 0, nw = 0, ntot = 0;
+    std::vector<void *> allocs;
+    AleFluid A{}, B{};  // current sorted state, spare
+    AleWalls W{};
+    Grid grid{};
+    AleConst K{};
+    uint32_t *fstart = nullptr, *wstart = nullptr, *counts = nullptr, *tiles = nullptr;
+    uint32_t *keyB = nullptr, *slotB = nullptr, *tmp_id = nullptr, *tmp_src = nullptr;
+    uint32_t *health = nullptr;
+    float *grad = nullptr;
+    long long *dbx = nullptr, *dby = nullptr;
+    double *dox = nullptr, *doy = nullptr;
+
+    ~AleEngine() { release(); if (own && st) cudaStreamDestroy(st); }
+
+    void release() {
+        for (void *q : allocs) cudaFree(q);
+        allocs.clear();
+        built = false;
+    }
+
+    template <typename P> int alloc(P **q, size_t n, std::string &err) {
+        void *x = nullptr;
+        cudaError_t e = cudaMalloc(&x, std::max<size_t>(n, 1) * sizeof(P));
+        if (e != cudaSuccess) {
+            err = std::string("cudaMalloc: ") + cudaGetErrorString(e);
+            return TSPH_ERR_NOMEM;
+        }
+        allocs.push_back(x);
+        *q = static_cast<P *>(x);
+        return 0;
+    }
+
+    int alloc_fluid(AleFluid &X, std::string &err) {
+        int rc;
+        if ((rc = alloc(&X.r, nf, err)) || (rc = alloc(&X.loc, nf, err)) ||
+            (rc = alloc(&X.key, nf, err)) || (rc = alloc(&X.id, nf, err)) ||
+            (rc = alloc(&X.om, nf, err)) || (rc = alloc(&X.omr, nf, err)) ||
+            (rc = alloc(&X.omv, nf, err)) || (rc = alloc(&X.om_o, nf, err)) ||
+            (rc = alloc(&X.omr_o, nf, err)) || (rc = alloc(&X.omv_o, nf, err)) ||
+            (rc = alloc(&X.dom, nf, err)) || (rc = alloc(&X.domr, nf, err)) ||
+            (rc = alloc(&X.domv, nf, err)) || (rc = alloc(&X.s, nf, err)) ||
+            (rc = alloc(&X.v, nf, err)) || (rc = alloc(&X.ps, nf, err)))
+            return rc;
+        X.grad = grad;
+        return 0;
+    }
+
+    int build(std::string &err) {
+        release();
+        const int n = (int)type.size();
+        ntot = n;
+        std::vector<int> fl, wl;
+        for (int i = 0; i < n; i++) (type[i] == 1 ? wl : fl).push_back(i);
+        nf = (int)fl.size();
+        nw = (int)wl.size();
+        if ((ncells + 1 + kScanTile - 1) / kScanTile > kScanTile) {
+            err = "grid too large for the scan";
+            return TSPH_ERR_UNSUPPORTED;
+        }
+        K.h = (float)h;
+        K.inv_h = (float)(1.0 / h);
+        K.m = (float)m;
+        K.c0 = (float)cs;
+        K.rho0 = (float)rho0;
+        K.g = 9.81f;
+        K.dp = (float)dp;
+        K.four_h2 = (float)(4.0 * h * h);
+        K.awen = (float)(0.557 / (h * h));
+        K.bwen_h = (float)((double)(float)(-2.7852 / (h * h * h)) / h);
+        K.b_eos = (float)(cs * cs * rho0 / 7.0);
+        // FP32 x_a - x_b from cell-local positions: a few ulps of kh
+        K.dx_exact = (float)(4e-6 * kh);
+        int rc;
+        if ((rc = alloc(&grad, (size_t)12 * nf, err))) return rc;
+        ACK(cudaMemset(grad, 0, sizeof(float) * 12 * std::max(nf, 1)));
+        if ((rc = alloc_fluid(A, err)) || (rc = alloc_fluid(B, err))) return rc;
+        if ((rc = alloc(&fstart, ncells + 2, err)) || (rc = alloc(&wstart, ncells + 1, err)) ||
+            (rc = alloc(&counts, ncells + 1, err)) ||
+            (rc = alloc(&tiles, (ncells + 1 + kScanTile - 1) / kScanTile, err)) ||
+            (rc = alloc(&keyB, nf, err)) || (rc = alloc(&slotB, nf, err)) ||
+            (rc = alloc(&tmp_id, nf, err)) || (rc = alloc(&tmp_src, nf, err)) ||
+            (rc = alloc(&health, 1, err)) || (rc = alloc(&dbx, bx.size(), err)) ||
+            (rc = alloc(&dby, by.size(), err)) || (rc = alloc(&dox, ox.size(), err)) ||
+            (rc = alloc(&doy, oy.size(), err)))
+            return rc;
+        ACK(cudaMemcpy(dbx, bx.data(), 8 * bx.size(), cudaMemcpyHostToDevice));
+        ACK(cudaMemcpy(dby, by.data(), 8 * by.size(), cudaMemcpyHostToDevice));
+        ACK(cudaMemcpy(dox, ox.data(), 8 * ox.size(), cudaMemcpyHostToDevice));
+        ACK(cudaMemcpy(doy, oy.data(), 8 * oy.size(), cudaMemcpyHostToDevice));
+        ACK(cudaMemset(counts, 0, 4 * (size_t)(ncells + 1)));
+        ACK(cudaMemset(health, 0, 4));
+        grid.ax = Axis{dbx, dox, ncx};
+        grid.ay = Axis{dby, doy, ncy};
+        grid.ncx = ncx;
+        grid.ncy = ncy;
+        grid.ncells = ncells;
+        grid.khf = (float)kh;
+        // fluid in index order (ALESPH_Add_particle values)
+        {
+            std::vector<double2> R(nf), OMV(nf);
+            std::vector<double> OM(nf), OMR(nf);
+            std::vector<float> S(nf), Z(nf, 0.f);
+            std::vector<float2> V(nf), Z2(nf, make_float2(0.f, 0.f));
+            std::vector<uint32_t> ID(nf), KEY(nf, 0u);
+            const double dp2 = dp * dp;
+            for (int k = 0; k < nf; k++) {
+                const int i = fl[k];
+                R[k] = make_double2(r[2 * i], r[2 * i + 1]);
+                OM[k] = dp2;
+                OMV[k] = make_double2(v[2 * i] * dp2, v[2 * i + 1] * dp2);
+                OMR[k] = rho[i] * dp2;
+                S[k] = (float)(rho[i] - rho0);
+                V[k] = make_float2((float)v[2 * i], (float)v[2 * i + 1]);
+                ID[k] = (uint32_t)i;
+            }
+            if (nf) {
+                ACK(cudaMemcpy(A.r, R.data(), 16 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.om, OM.data(), 8 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.om_o, OM.data(), 8 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.omr, OMR.data(), 8 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.omr_o, OMR.data(), 8 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.omv, OMV.data(), 16 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.omv_o, OMV.data(), 16 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.s, S.data(), 4 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.ps, S.data(), 4 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.v, V.data(), 8 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.dom, Z.data(), 4 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.domr, Z.data(), 4 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.domv, Z2.data(), 8 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.id, ID.data(), 4 * (size_t)nf, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(A.key, KEY.data(), 4 * (size_t)nf, cudaMemcpyHostToDevice));
+            }
+            std::vector<uint32_t> fs(ncells + 2, 0u);
+            fs[ncells] = (uint32_t)nf;
+            fs[ncells + 1] = (uint32_t)nf;
+            ACK(cudaMemcpy(fstart, fs.data(), 4 * fs.size(), cudaMemcpyHostToDevice));
+        }
+        // walls, binned once on the host (by cell, then index)
+        {
+            auto cell_of = [](double x, const std::vector<long long> &b) -> int {
+                const long long o = ordered_bits(x);
+                if (o < b.front()) return -1;
+                if (o >= b.back()) return (int)b.size() - 1;
+                return (int)(std::upper_bound(b.begin(), b.end(), o) - b.begin()) - 1;
+            };
+            std::vector<std::pair<uint32_t, int>> ord;
+            for (int i : wl) {
+                const int cx = cell_of(r[2 * i], bx), cy = cell_of(r[2 * i + 1], by);
+                if (cx < 0 || cy < 0 || cx >= ncx || cy >= ncy) {
+                    err = "wall particle " + std::to_string(i) + " lies outside the cell grid";
+                    return TSPH_ERR_ARG;
+                }
+                ord.push_back({(uint32_t)(cy + cx * ncy), i});
+            }
+            std::sort(ord.begin(), ord.end());
+            if ((rc = alloc(&W.r, nw, err)) || (rc = alloc(&W.loc, nw, err)) ||
+                (rc = alloc(&W.key, nw, err)) || (rc = alloc(&W.id, nw, err)) ||
+                (rc = alloc(&W.n, nw, err)) || (rc = alloc(&W.s, nw, err)))
+                return rc;
+            std::vector<double2> R(nw);
+            std::vector<float2> L(nw), N(nw);
+            std::vector<uint32_t> KEY(nw), ID(nw), ws(ncells + 1, 0u);
+            std::vector<float> S(nw);
+            for (int k = 0; k < nw; k++) {
+                const int i = ord[k].second;
+                const uint32_t c = ord[k].first;
+                const int cx = (int)(c / ncy), cy = (int)(c % ncy);
+                R[k] = make_double2(r[2 * i], r[2 * i + 1]);
+                L[k] = make_float2((float)(r[2 * i] - ox[cx]), (float)(r[2 * i + 1] - oy[cy]));
+                KEY[k] = c;
+                ID[k] = (uint32_t)i;
+                N[k] = make_float2((float)nrm[2 * i], (float)nrm[2 * i + 1]);
+                S[k] = (float)(rho[i] - rho0);
+                ws[c + 1]++;
+            }
+            for (int c = 0; c < ncells; c++) ws[c + 1] += ws[c];
+            if (nw) {
+                ACK(cudaMemcpy(W.r, R.data(), 16 * (size_t)nw, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(W.loc, L.data(), 8 * (size_t)nw, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(W.key, KEY.data(), 4 * (size_t)nw, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(W.id, ID.data(), 4 * (size_t)nw, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(W.n, N.data(), 8 * (size_t)nw, cudaMemcpyHostToDevice));
+                ACK(cudaMemcpy(W.s, S.data(), 4 * (size_t)nw, cudaMemcpyHostToDevice));
+            }
+            ACK(cudaMemcpy(wstart, ws.data(), 4 * ws.size(), cudaMemcpyHostToDevice));
+        }
+        ACK(cudaDeviceSynchronize());
+        built = true;
+        cells = false;
+        return 0;
+    }
+
+    // counting sort of X (keys in keyB/slotB, histogram in counts) into Y
+    int sort(AleFluid X, AleFluid Y, std::string &err) {
+        const int n = ncells + 1;
+        const int nt = (n + kScanTile - 1) / kScanTile;
+        k_scan_tiles_clear<<<nt, kScanThreads, 0, st>>>(counts, fstart, tiles, n);
+        k_scan_add_tiles<<<nblk(n), kBlock, 0, st>>>(fstart, tiles, nt, n);
+        const int *ntot_ = reinterpret_cast<const int *>(fstart + ncells + 1);
+        k_place<<<nblk(nf), kBlock, 0, st>>>(keyB, slotB, X.id, ntot_, fstart, tmp_id, tmp_src,
+                                             nullptr, nullptr);
+        k_ale_rank_scatter<<<nblk(nf), kBlock, 0, st>>>(keyB, ntot_, fstart, tmp_id, tmp_src, grid,
+                                                        X, Y);
+        ACK(cudaGetLastError());
+        return 0;
+    }
+
+    int particle_to_cell(std::string &err) {
+        k_ale_bin<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, keyB, slotB, counts, health);
+        int rc = sort(A, B, err);
+        if (rc) return rc;
+        std::swap(A, B);
+        cells = true;
+        return 0;
+    }
+
+    int gradient(std::string &err) {
+        k_ale_grad<<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
+        ACK(cudaGetLastError());
+        return 0;
+    }
+
+    int forces(std::string &err) {
+        if (scheme == TSPH_ALE_MUSCL)
+            k_ale_flux<1><<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
+        else
+            k_ale_flux<0><<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
+        ACK(cudaGetLastError());
+        return 0;
+    }
+
+    int lf1(double dt, std::string &err) {
+        k_ale_lf1<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, dt, (float)rho0);
+        ACK(cudaGetLastError());
+        return 0;
+    }
+
+    int lf2(double dt, int step, std::string &err) {
+        k_ale_lf2<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, dt, step, (float)rho0);
+        ACK(cudaGetLastError());
+        cells = false;
+        return 0;
+    }
+
+    int step(double dt, int step0, int nsteps, std::string &err) {
+        const Box box{x0, xm, y0, ym};
+        for (int k = 1; k <= nsteps; k++) {
+            const int stp = step0 + k;
+            int rc;
+            if (stp > 1 && (rc = lf1(dt, err))) return rc;
+            if (scheme == TSPH_ALE_MUSCL && (rc = gradient(err))) return rc;
+            if ((rc = forces(err))) return rc;
+            k_ale_lf2_bin<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, dt, stp, (float)rho0, box,
+                                                       B, keyB, slotB, counts, health);
+            if ((rc = sort(B, A, err))) return rc;
+        }
+        ACK(cudaGetLastError());
+        cells = true;
+        return 0;
+    }
+
+    int np_live(int *np, std::string &err) {
+        uint32_t nl = 0;
+        ACK(cudaMemcpyAsync(&nl, fstart + ncells, 4, cudaMemcpyDeviceToHost, st));
+        ACK(cudaStreamSynchronize(st));
+        *np = (int)nl + nw;
+        return 0;
+    }
+
+    int download(int mask, const tsph_ale_host_state *o, std::string &err) {
+        ACK(cudaStreamSynchronize(st));
+        uint32_t nl = 0;
+        ACK(cudaMemcpy(&nl, fstart + ncells, 4, cudaMemcpyDeviceToHost));
+        std::vector<double2> R(nl), OMV(nl);
+        std::vector<double> OM(nl), OMR(nl);
+        std::vector<float> S(nl), PS(nl), DOM(nl), DOMR(nl), G((size_t)12 * nl);
+        std::vector<float2> V(nl), DOMV(nl);
+        std::vector<uint32_t> ID(nl), WID(nw);
+        std::vector<double2> WR(nw);
+        std::vector<float> WS(nw);
+        if (nl) {
+            ACK(cudaMemcpy(R.data(), A.r, 16 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(OM.data(), A.om, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(OMR.data(), A.omr, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(OMV.data(), A.omv, 16 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(S.data(), A.s, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(PS.data(), A.ps, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(V.data(), A.v, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(DOM.data(), A.dom, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(DOMR.data(), A.domr, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(DOMV.data(), A.domv, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(ID.data(), A.id, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(G.data(), grad, 48 * (size_t)nl, cudaMemcpyDeviceToHost));
+        }
+        if (nw) {
+            ACK(cudaMemcpy(WID.data(), W.id, 4 * (size_t)nw, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(WR.data(), W.r, 16 * (size_t)nw, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(WS.data(), W.s, 4 * (size_t)nw, cudaMemcpyDeviceToHost));
+        }
+        // rows in ascending original index: (id, fluid row or -1 - wall row)
+        std::vector<std::pair<uint32_t, int>> rows;
+        for (uint32_t j = 0; j < nl; j++) rows.push_back({ID[j], (int)j});
+        for (int w = 0; w < nw; w++) rows.push_back({WID[w], -1 - w});
+        std::sort(rows.begin(), rows.end());
+        const double dp2 = dp * dp;
+        for (size_t k = 0; k < rows.size(); k++) {
+            const int j = rows[k].second;
+            const bool wall = j < 0;
+            const int w = -1 - j;
+            const double rh = wall ? rho0 + (double)WS[w] : rho0 + (double)S[j];
+            if ((mask & TSPH_ALE_F_R) && o->r) {
+                const double2 x = wall ? WR[w] : R[j];
+                o->r[2 * k] = x.x;
+                o->r[2 * k + 1] = x.y;
+            }
+            if ((mask & TSPH_ALE_F_V) && o->v) {
+                o->v[2 * k] = wall ? 0. : (double)V[j].x;
+                o->v[2 * k + 1] = wall ? 0. : (double)V[j].y;
+            }
+            if ((mask & TSPH_ALE_F_RHO) && o->rho) o->rho[k] = rh;
+            if ((mask & TSPH_ALE_F_P) && o->p) {
+                // Density_to_pressure of the density the last fluxes used
+                const double x = (wall ? rh : rho0 + (double)PS[j]) / rho0;
+                o->p[k] = cs * cs * rho0 / 7. * (std::pow(x, 7.) - 1);
+            }
+            if ((mask & TSPH_ALE_F_OMEGA) && o->omega) o->omega[k] = wall ? dp2 : OM[j];
+            if ((mask & TSPH_ALE_F_OMEGARHO) && o->omegarho) o->omegarho[k] = wall ? rh * dp2 : OMR[j];
+            if ((mask & TSPH_ALE_F_OMEGAV) && o->omegav) {
+                o->omegav[2 * k] = wall ? 0. : OMV[j].x;
+                o->omegav[2 * k + 1] = wall ? 0. : OMV[j].y;
+            }
+            if (mask & TSPH_ALE_F_RATES) {
+                if (o->domega) o->domega[k] = wall ? 0. : (double)DOM[j];
+                if (o->domegarho) o->domegarho[k] = wall ? 0. : (double)DOMR[j];
+                if (o->domegav) {
+                    o->domegav[2 * k] = wall ? 0. : (double)DOMV[j].x;
+                    o->domegav[2 * k + 1] = wall ? 0. : (double)DOMV[j].y;
+                }
+            }
+            if ((mask & TSPH_ALE_F_GRAD) && o->grad)
+                for (int q = 0; q < 12; q++)
+                    o->grad[12 * k + q] = wall ? 0. : (double)G[(size_t)12 * j + q];
+            if ((mask & TSPH_ALE_F_INDEX) && o->index) o->index[k] = (int32_t)rows[k].first;
+            if ((mask & TSPH_ALE_F_TYPE) && o->type) o->type[k] = wall ? 1 : 0;
+        }
+        return 0;
+    }
+
+    // upload omega, v, rho and r of fluid particles (omega*v and omega*rho
+    // follow), host arrays in the reference's order
+    int upload(int mask, const tsph_ale_host_state *in, std::string &err) {
+        ACK(cudaStreamSynchronize(st));
+        uint32_t nl = 0;
+        ACK(cudaMemcpy(&nl, fstart + ncells, 4, cudaMemcpyDeviceToHost));
+        if (nl + nw != (uint32_t)ntot) {
+            err = "upload after removals is not supported on the ALE path";
+            return TSPH_ERR_STATE;
+        }
+        std::vector<uint32_t> ID(nl);
+        std::vector<double> OM(nl), OMR(nl);
+        std::vector<double2> OMV(nl), R(nl);
+        std::vector<float> S(nl), PS(nl);
+        std::vector<float2> V(nl);
+        if (nl) {
+            ACK(cudaMemcpy(PS.data(), A.ps, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(ID.data(), A.id, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(OM.data(), A.om, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(OMR.data(), A.omr, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(OMV.data(), A.omv, 16 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(S.data(), A.s, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(V.data(), A.v, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
+            ACK(cudaMemcpy(R.data(), A.r, 16 * (size_t)nl, cudaMemcpyDeviceToHost));
+        }
+        for (uint32_t j = 0; j < nl; j++) {
+            const uint32_t i = ID[j];
+            if ((mask & TSPH_ALE_F_OMEGA) && in->omega) {
+                // new volume, same rho = omega*rho / omega and same
+                // v = omega*v / (rho omega)
+                const double f = in->omega[i] / OM[j];
+                OM[j] = in->omega[i];
+                OMR[j] *= f;
+                OMV[j] = make_double2(OMV[j].x * f, OMV[j].y * f);
+            }
+            if ((mask & TSPH_ALE_F_RHO) && in->rho) {
+                OMR[j] = in->rho[i] * OM[j];
+                S[j] = (float)(in->rho[i] - rho0);
+                PS[j] = S[j];
+            }
+            if ((mask & TSPH_ALE_F_V) && in->v) {
+                OMV[j] = make_double2(in->v[2 * i] * OM[j], in->v[2 * i + 1] * OM[j]);
+                V[j] = make_float2((float)in->v[2 * i], (float)in->v[2 * i + 1]);
+            }
+            if ((mask & TSPH_ALE_F_R) && in->r) R[j] = make_double2(in->r[2 * i], in->r[2 * i + 1]);
+        }
+        if (nl) {
+            ACK(cudaMemcpy(A.om, OM.data(), 8 * (size_t)nl, cudaMemcpyHostToDevice));
+            ACK(cudaMemcpy(A.omr, OMR.data(), 8 * (size_t)nl, cudaMemcpyHostToDevice));
+            ACK(cudaMemcpy(A.omv, OMV.data(), 16 * (size_t)nl, cudaMemcpyHostToDevice));
+            ACK(cudaMemcpy(A.s, S.data(), 4 * (size_t)nl, cudaMemcpyHostToDevice));
+            ACK(cudaMemcpy(A.ps, PS.data(), 4 * (size_t)nl, cudaMemcpyHostToDevice));
+            ACK(cudaMemcpy(A.v, V.data(), 8 * (size_t)nl, cudaMemcpyHostToDevice));
+            ACK(cudaMemcpy(A.r, R.data(), 16 * (size_t)nl, cudaMemcpyHostToDevice));
+        }
+        if (mask & TSPH_ALE_F_R) cells = false;
+        return 0;
+    }
+};
+
+}  // namespace tsph
+
+struct tsph_ale_system {
+    tsph::AleEngine e;
+};
+
+namespace {
+int afail(int code, const std::string &m) {
+    tsph::set_last_error(m);
+    return code;
+}
+int aready(tsph_ale_system *s) {
+    if (!s) return afail(TSPH_ERR_ARG, "null system handle");
+    if (!s->e.divided) return afail(TSPH_ERR_STATE, "call tsph_ale_divide_to_cells first");
+    if (!s->e.built) {
+        std::string err;
+        int rc = s->e.build(err);
+        if (rc) return afail(rc, err);
+    }
+    return TSPH_OK;
+}
+int acells(tsph_ale_system *s) {
+    if (!s->e.cells) return afail(TSPH_ERR_STATE, "cell lists are stale: call tsph_ale_particle_to_cell");
+    return TSPH_OK;
+}
+}  // namespace
+
+#define AREADY(s)                         \
+    do {                                  \
+        int rc_ = aready(s);              \
+        if (rc_) return rc_;              \
+    } while (0)
+#define ARUN(expr)                        \
+    do {                                  \
+        std::string err_;                 \
+        int rc_ = (expr);                 \
+        if (rc_) return afail(rc_, err_); \
+    } while (0)
+
+extern "C" {
+
+int tsph_ale_create(const tsph_constants *c, const tsph_domain *d, void *stream,
+                    tsph_ale_system **out) {
+    if (!c || !d || !out) return afail(TSPH_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (!(c->h > 0) || !(c->kap > 0) || !(c->dp > 0) || !(c->cs > 0) || !(c->rho0 > 0))
+        return afail(TSPH_ERR_ARG, "h, kap, dp, cs and rho0 must be positive");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return afail(TSPH_ERR_CUDA, "no CUDA device available");
+    }
+    tsph_ale_system *s = new tsph_ale_system();
+    tsph::AleEngine &e = s->e;
+    e.h = c->h;
+    e.kap = c->kap;
+    e.cs = c->cs;
+    e.rho0 = c->rho0;
+    e.visco = c->visco;
+    e.delta = c->delta;
+    e.dp = c->dp;
+    e.m = c->rho0 / (1 / c->dp * 1 / c->dp);
+    e.x0 = d->x_0;
+    e.xm = d->x_m;
+    e.y0 = d->y_0;
+    e.ym = d->y_m;
+    if (stream) {
+        e.st = static_cast<cudaStream_t>(stream);
+    } else {
+        if (cudaStreamCreateWithFlags(&e.st, cudaStreamNonBlocking) != cudaSuccess) {
+            delete s;
+            return afail(TSPH_ERR_CUDA, "cudaStreamCreate failed");
+        }
+        e.own = true;
+    }
+    *out = s;
+    return TSPH_OK;
+}
+
+int tsph_ale_destroy(tsph_ale_system *s) {
+    delete s;
+    return TSPH_OK;
+}
+
+int tsph_ale_add_particles(tsph_ale_system *s, int n, const int32_t *type, const double *r,
+                           const double *v, const double *rho, const double *p,
+                           const double *normal) {
+    if (!s) return afail(TSPH_ERR_ARG, "null system handle");
+    if (n < 0 || (n > 0 && (!type || !r || !rho))) return afail(TSPH_ERR_ARG, "bad arguments");
+    if (s->e.built) return afail(TSPH_ERR_STATE, "add all particles before the first step");
+    for (int i = 0; i < n; i++) {
+        if (type[i] != TSPH_FLUID && type[i] != TSPH_WALL)
+            return afail(TSPH_ERR_UNSUPPORTED, "only fluid and wall particles are on this path");
+        if (type[i] == TSPH_WALL && !normal)
+            return afail(TSPH_ERR_ARG, "wall particles of the ALE path need a normal");
+        s->e.type.push_back(type[i]);
+        s->e.r.push_back(r[2 * i]);
+        s->e.r.push_back(r[2 * i + 1]);
+        s->e.v.push_back(v ? v[2 * i] : 0.);
+        s->e.v.push_back(v ? v[2 * i + 1] : 0.);
+        s->e.rho.push_back(rho[i]);
+        s->e.p.push_back(p ? p[i] : 0.);
+        s->e.nrm.push_back(normal ? normal[2 * i] : 0.);
+        s->e.nrm.push_back(normal ? normal[2 * i + 1] : 0.);
+    }
+    return TSPH_OK;
+}
+
+int tsph_ale_set_scheme(tsph_ale_system *s, int scheme) {
+    if (!s) return afail(TSPH_ERR_ARG, "null system handle");
+    if (scheme != TSPH_ALE_AS_WRITTEN && scheme != TSPH_ALE_MUSCL)
+        return afail(TSPH_ERR_ARG, "unknown scheme");
+    s->e.scheme = scheme;
+    return TSPH_OK;
+}
+
+int tsph_ale_np(tsph_ale_system *s, int *np) {
+    if (!s || !np) return afail(TSPH_ERR_ARG, "null argument");
+    if (!s->e.built) {
+        *np = (int)s->e.type.size();
+        return TSPH_OK;
+    }
+    ARUN(s->e.np_live(np, err_));
+    return TSPH_OK;
+}
+
+int tsph_ale_divide_to_cells(tsph_ale_system *s) {
+    if (!s) return afail(TSPH_ERR_ARG, "null system handle");
+    tsph::AleEngine &e = s->e;
+    const double kh = e.kap * e.h, of = e.h * 0.273;
+    const double qx = (e.xm - e.x0 + of) / kh, qy = (e.ym - e.y0 + of) / kh;
+    if (!(qx < 1e7) || !(qy < 1e7)) return afail(TSPH_ERR_ARG, "grid too large");
+    e.ncx = (int)qx + 1;
+    e.ncy = (int)qy + 1;
+    if (e.ncy < 4) return afail(TSPH_ERR_UNSUPPORTED, "grid needs at least 4 cells in y");
+    e.ncells = e.ncx * e.ncy;
+    e.kh = kh;
+    e.of = of;
+    e.bx.resize(e.ncx + 1);
+    e.by.resize(e.ncy + 1);
+    for (int k = 0; k <= e.ncx; k++) e.bx[k] = tsph::cell_lower_bound(k, e.x0, of, kh);
+    for (int k = 0; k <= e.ncy; k++) e.by[k] = tsph::cell_lower_bound(k, e.y0, of, kh);
+    e.ox.resize(e.ncx);
+    e.oy.resize(e.ncy);
+    for (int k = 0; k < e.ncx; k++) e.ox[k] = (e.x0 - of) + k * kh;
+    for (int k = 0; k < e.ncy; k++) e.oy[k] = (e.y0 - of) + k * kh;
+    e.divided = true;
+    e.built = false;
+    return TSPH_OK;
+}
+
+int tsph_ale_particle_to_cell(tsph_ale_system *s) {
+    AREADY(s);
+    ARUN(s->e.particle_to_cell(err_));
+    return TSPH_OK;
+}
+
+int tsph_ale_gradient(tsph_ale_system *s) {
+    AREADY(s);
+    int rc = acells(s);
+    if (rc) return rc;
+    ARUN(s->e.gradient(err_));
+    return TSPH_OK;
+}
+
+int tsph_ale_forces(tsph_ale_system *s, double dt) {
+    AREADY(s);
+    (void)dt;  // only enters the cancelled Hancock term of MUSCL_final
+    int rc = acells(s);
+    if (rc) return rc;
+    ARUN(s->e.forces(err_));
+    return TSPH_OK;
+}
+
+int tsph_ale_leapfrog_one(tsph_ale_system *s, double dt) {
+    AREADY(s);
+    ARUN(s->e.lf1(dt, err_));
+    return TSPH_OK;
+}
+
+int tsph_ale_leapfrog_two(tsph_ale_system *s, double dt, int step) {
+    AREADY(s);
+    ARUN(s->e.lf2(dt, step, err_));
+    return TSPH_OK;
+}
+
+int tsph_ale_step(tsph_ale_system *s, double dt, int step0, int nsteps) {
+    AREADY(s);
+    if (nsteps < 0 || step0 < 0) return afail(TSPH_ERR_ARG, "bad step range");
+    int rc = acells(s);
+    if (rc) return rc;
+    ARUN(s->e.step(dt, step0, nsteps, err_));
+    return TSPH_OK;
+}
+
+int tsph_ale_download(tsph_ale_system *s, int fields, const tsph_ale_host_state *out) {
+    AREADY(s);
+    if (!out) return afail(TSPH_ERR_ARG, "null output");
+    ARUN(s->e.download(fields, out, err_));
+    return TSPH_OK;
+}
+
+int tsph_ale_upload(tsph_ale_system *s, int fields, const tsph_ale_host_state *in) {
+    AREADY(s);
+    if (!in) return afail(TSPH_ERR_ARG, "null input");
+    ARUN(s->e.upload(fields, in, err_));
+    return TSPH_OK;
+}
+
+int tsph_ale_sync(tsph_ale_system *s) {
+    if (!s) return afail(TSPH_ERR_ARG, "null system handle");
+    if (!s->e.st) return TSPH_OK;
+    if (cudaStreamSynchronize(s->e.st) != cudaSuccess) return afail(TSPH_ERR_CUDA, "sync failed");
+    return TSPH_OK;
+}
+
+int tsph_ale_health(tsph_ale_system *s, uint32_t *flags, int clear) {
+    if (!s || !flags) return afail(TSPH_ERR_ARG, "null argument");
+    *flags = 0;
+    if (!s->e.built) return TSPH_OK;
+    if (cudaMemcpyAsync(flags, s->e.health, 4, cudaMemcpyDeviceToHost, s->e.st) != cudaSuccess)
+        return afail(TSPH_ERR_CUDA, "health read failed");
+    if (clear) cudaMemsetAsync(s->e.health, 0, 4, s->e.st);
+    cudaStreamSynchronize(s->e.st);
+    return TSPH_OK;
+}
+
+}  // extern "C"

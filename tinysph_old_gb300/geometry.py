@@ -174,3 +174,46 @@ def create_wall_y(ps: ParticleSet, x, y_0, y_1, orientation):
         rx = x + dp * l * orientation
         for i in range(npart + 1):
             ps.add(WALL, 0.0, ps.rho0, (rx, y_0 + i * dp))
+
+
+class AleParticleSet(ParticleSet):
+    """Particles of the ALE-SPH path: ``ALESPH_Add_particle``
+    (src/SPH_particle_system.h:51-108) plus the BT wall normals
+    (``special.n``, src/SPH_data.h:52), indexed by particle index."""
+
+    def __init__(self, dp, h, kap, cs, rho0=1000.0):
+        super().__init__(dp, h, kap, cs, rho0)
+        self.normals: list[tuple[float, float]] = []
+
+
+def create_wall_x_bt(ps: AleParticleSet, x_0, x_1, y, orientation, n):
+    """``Create_Wall_x_bt`` (one layer, normal n), src/ALESPH_create.h:690-725."""
+    dp = ps.dp
+    npart = int(_len(x_0, y, x_1, y) / dp)
+    for l in range(1):
+        ry = y + dp * l * orientation
+        for i in range(npart + 1):
+            ps.add(WALL, 0.0, ps.rho0, (x_0 + i * dp, ry))
+            ps.normals.append((n[0], n[1]))
+
+
+def create_wall_y_bt(ps: AleParticleSet, x, y_0, y_1, orientation, n):
+    """``Create_Wall_y_bt``, src/ALESPH_create.h:727-761."""
+    dp = ps.dp
+    npart = int(_len(x, y_0, x, y_1) / dp)
+    for l in range(1):
+        rx = x + dp * l * orientation
+        for i in range(npart + 1):
+            ps.add(WALL, 0.0, ps.rho0, (rx, y_0 + i * dp))
+            ps.normals.append((n[0], n[1]))
+
+
+def create_corner_bt(ps: AleParticleSet, orientation_x, orientation_y, xyv, n):
+    """``Create_corner_bt``, src/ALESPH_create.h:763-792."""
+    dp = ps.dp
+    for l in range(1):
+        ry = xyv[1] + dp * l * orientation_y
+        for i in range(1):
+            rx = xyv[0] + dp * i * orientation_x
+            ps.add(WALL, 0.0, ps.rho0, (rx, ry))
+            ps.normals.append((n[0], n[1]))

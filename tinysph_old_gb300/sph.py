@@ -36,7 +36,17 @@ ABI_SYMBOLS = (
     "tsph_compute_forces", "tsph_symplectic_predictor", "tsph_symplectic_corrector",
     "tsph_remove_out_of_domain", "tsph_step", "tsph_download", "tsph_upload", "tsph_sync",
     "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
+    "tsph_ale_create", "tsph_ale_destroy", "tsph_ale_add_particles", "tsph_ale_set_scheme",
+    "tsph_ale_np", "tsph_ale_divide_to_cells", "tsph_ale_particle_to_cell", "tsph_ale_gradient",
+    "tsph_ale_forces", "tsph_ale_leapfrog_one", "tsph_ale_leapfrog_two", "tsph_ale_step",
+    "tsph_ale_download", "tsph_ale_upload", "tsph_ale_sync", "tsph_ale_health",
 )
+
+ALE_AS_WRITTEN = 0
+ALE_MUSCL = 1
+(ALE_F_R, ALE_F_V, ALE_F_RHO, ALE_F_P, ALE_F_OMEGA, ALE_F_OMEGARHO, ALE_F_OMEGAV, ALE_F_RATES,
+ ALE_F_GRAD, ALE_F_INDEX, ALE_F_TYPE) = (1 << k for k in range(11))
+ALE_F_ALL = (1 << 11) - 1
 
 
 class TsphError(RuntimeError):
@@ -57,6 +67,12 @@ class _HostState(C.Structure):
     _fields_ = [("r", C.c_void_p), ("v", C.c_void_p), ("a", C.c_void_p), ("rho", C.c_void_p),
                 ("drho", C.c_void_p), ("p", C.c_void_p), ("index", C.c_void_p),
                 ("type", C.c_void_p)]
+
+
+class _AleHostState(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("r", "v", "rho", "p", "omega", "omegarho", "omegav",
+                                          "domega", "domegarho", "domegav", "grad", "index",
+                                          "type")]
 
 
 class _Profile(C.Structure):
@@ -115,6 +131,20 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_fluid_totals.argtypes = [P, P]
     L.tsph_set_profiling.argtypes = [P, I]
     L.tsph_get_profile.argtypes = [P, C.POINTER(_Profile), I]
+    L.tsph_ale_create.argtypes = [C.POINTER(_Constants), C.POINTER(_Domain), P, C.POINTER(P)]
+    for f in ("tsph_ale_destroy", "tsph_ale_divide_to_cells", "tsph_ale_particle_to_cell",
+              "tsph_ale_gradient", "tsph_ale_sync"):
+        getattr(L, f).argtypes = [P]
+    L.tsph_ale_add_particles.argtypes = [P, I, P, P, P, P, P, P]
+    L.tsph_ale_set_scheme.argtypes = [P, I]
+    L.tsph_ale_np.argtypes = [P, C.POINTER(I)]
+    L.tsph_ale_forces.argtypes = [P, D]
+    L.tsph_ale_leapfrog_one.argtypes = [P, D]
+    L.tsph_ale_leapfrog_two.argtypes = [P, D, I]
+    L.tsph_ale_step.argtypes = [P, D, I, I]
+    L.tsph_ale_download.argtypes = [P, I, C.POINTER(_AleHostState)]
+    L.tsph_ale_upload.argtypes = [P, I, C.POINTER(_AleHostState)]
+    L.tsph_ale_health.argtypes = [P, C.POINTER(C.c_uint32), I]
     _lib = L
     return L
 
@@ -381,3 +411,158 @@ def Integrate_SymplecticCorrector(particles: ParticleSystem, dt):
 
 def RemoveParticlesOutOfDomain(particles: ParticleSystem, simulation_data=None) -> int:
     return particles.remove_out_of_domain()
+
+
+class AleSystem:
+    """Riemann / ALE-SPH ``Particle_system`` on the GPU (the path of
+    cases/ALESPH_dambreakLong/MUSCL.h): leap-frog in omega, omega*rho,
+    omega*v (src/RALESPH_integration.h), one-sided MUSCL gradients and the
+    linearised-Riemann flux loop (src/_testMUSCL_interaction.h); BT walls with
+    a normal each.  ``scheme`` is :data:`ALE_AS_WRITTEN` (the reference's
+    fluxes) or :data:`ALE_MUSCL`."""
+
+    def __init__(self, h, kap, cs, rho0, visco, delta, dp, domain, stream=None):
+        L = load()
+        self._L = L
+        c = _Constants(h, kap, cs, rho0, visco, delta, dp)
+        d = _Domain(*domain)
+        h_ = C.c_void_p()
+        _check(L.tsph_ale_create(C.byref(c), C.byref(d), stream, C.byref(h_)))
+        self._h = h_
+        self.domain = tuple(domain)
+
+    @classmethod
+    def from_case(cls, case, scheme=ALE_AS_WRITTEN, divide=True, bin_particles=True):
+        """INIT of the ALE driver: ALESPH_Add_particle for every particle
+        (normals of the walls from the generators), Divide_To_Cells,
+        Particle_To_Cell."""
+        s = cls(case.h, case.kap, case.cs, case.rho0, case.visco, case.delta, case.dp,
+                case.domain)
+        a = case.particles.arrays()
+        nrm = np.zeros((case.np, 2))
+        nn = np.asarray(case.particles.normals, dtype=np.float64).reshape(-1, 2)
+        # special.n is indexed by particle index: walls come first
+        nrm[:len(nn)] = nn
+        s.add_particles(a["type"], a["r"], a["v"], a["rho"], a["p"], nrm)
+        s.set_scheme(scheme)
+        if divide:
+            s.divide_to_cells()
+            if bin_particles:
+                s.particle_to_cell()
+        return s
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.tsph_ale_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def add_particles(self, ptype, r, v=None, rho=None, p=None, normal=None):
+        n = len(ptype)
+        t = np.ascontiguousarray(ptype, dtype=np.int32)
+        r = np.ascontiguousarray(r, dtype=np.float64).reshape(n, 2)
+        v = None if v is None else np.ascontiguousarray(v, dtype=np.float64).reshape(n, 2)
+        rho = np.ascontiguousarray(rho, dtype=np.float64)
+        p = None if p is None else np.ascontiguousarray(p, dtype=np.float64)
+        nr = None if normal is None else np.ascontiguousarray(normal, dtype=np.float64).reshape(n, 2)
+        _check(self._L.tsph_ale_add_particles(self._h, n, _p(t), _p(r), _p(v), _p(rho), _p(p),
+                                              _p(nr)))
+
+    def set_scheme(self, scheme):
+        _check(self._L.tsph_ale_set_scheme(self._h, int(scheme)))
+
+    @property
+    def np(self) -> int:
+        n = C.c_int()
+        _check(self._L.tsph_ale_np(self._h, C.byref(n)))
+        return n.value
+
+    def divide_to_cells(self):
+        _check(self._L.tsph_ale_divide_to_cells(self._h))
+
+    def particle_to_cell(self):
+        _check(self._L.tsph_ale_particle_to_cell(self._h))
+
+    def gradient(self):
+        _check(self._L.tsph_ale_gradient(self._h))
+
+    def forces(self, dt):
+        _check(self._L.tsph_ale_forces(self._h, float(dt)))
+
+    def leapfrog_one(self, dt):
+        _check(self._L.tsph_ale_leapfrog_one(self._h, float(dt)))
+
+    def leapfrog_two(self, dt, step):
+        _check(self._L.tsph_ale_leapfrog_two(self._h, float(dt), int(step)))
+
+    def step(self, dt, step0, nsteps=1):
+        _check(self._L.tsph_ale_step(self._h, float(dt), int(step0), int(nsteps)))
+
+    def download(self, fields=ALE_F_ALL):
+        """State in the reference's order as a dict of numpy arrays."""
+        n = self.np
+        spec = [(ALE_F_R, "r", (n, 2), np.float64), (ALE_F_V, "v", (n, 2), np.float64),
+                (ALE_F_RHO, "rho", (n,), np.float64), (ALE_F_P, "p", (n,), np.float64),
+                (ALE_F_OMEGA, "omega", (n,), np.float64),
+                (ALE_F_OMEGARHO, "omegarho", (n,), np.float64),
+                (ALE_F_OMEGAV, "omegav", (n, 2), np.float64),
+                (ALE_F_RATES, "domega", (n,), np.float64),
+                (ALE_F_RATES, "domegarho", (n,), np.float64),
+                (ALE_F_RATES, "domegav", (n, 2), np.float64),
+                (ALE_F_GRAD, "grad", (n, 12), np.float64),
+                (ALE_F_INDEX, "index", (n,), np.int32), (ALE_F_TYPE, "type", (n,), np.int32)]
+        hs = _AleHostState()
+        res = {}
+        for bit, name, shape, dt in spec:
+            if fields & bit:
+                res[name] = np.empty(shape, dtype=dt)
+                setattr(hs, name, res[name].ctypes.data)
+        _check(self._L.tsph_ale_download(self._h, int(fields), C.byref(hs)))
+        return res
+
+    def upload(self, r=None, v=None, rho=None, omega=None):
+        """Set fluid positions, velocities, densities and volumes (omega*v and
+        omega*rho follow), arrays in the reference's particle order."""
+        hs = _AleHostState()
+        mask = 0
+        keep = []
+        for name, arr, bit in (("r", r, ALE_F_R), ("v", v, ALE_F_V), ("rho", rho, ALE_F_RHO),
+                               ("omega", omega, ALE_F_OMEGA)):
+            if arr is None:
+                continue
+            a = np.ascontiguousarray(arr, dtype=np.float64)
+            keep.append(a)
+            setattr(hs, name, a.ctypes.data)
+            mask |= bit
+        _check(self._L.tsph_ale_upload(self._h, mask, C.byref(hs)))
+
+    def sync(self):
+        _check(self._L.tsph_ale_sync(self._h))
+
+    def health(self, clear=False) -> int:
+        f = C.c_uint32()
+        _check(self._L.tsph_ale_health(self._h, C.byref(f), 1 if clear else 0))
+        return f.value
+
+
+def Kernel_gradient_approx(particles: AleSystem):
+    particles.gradient()
+
+
+def Integrate_LeapFrog_partOne(particles: AleSystem, dt):
+    particles.leapfrog_one(dt)
+
+
+def Integrate_LeapFrog_partTwo(particles: AleSystem, dt, step):
+    particles.leapfrog_two(dt, step)
