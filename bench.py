@@ -12,6 +12,10 @@ kernel, cpu_baseline (the CPU oracle on the host cores) and clocks.
 ``--impl reference`` times the reference's CPU algorithm on the same workload
 instead (the oracle restatement, all host cores; the reference sources are
 not present on the GPU host).
+
+``--workload ale`` measures the Riemann / ALE-SPH step instead: the BT-wall
+dam break of cases/ALESPH_dambreakLong at dp = 0.0004 m (1,125,000 fluid
+particles), FP32 fluxes with FP64 leap-frog integration.
 """
 
 from __future__ import annotations
@@ -31,6 +35,12 @@ sys.path.insert(0, ROOT)
 PAIR_BYTES_PER_PARTICLE = 80.0   # mean algorithmic bytes of the two pair launches / particle
 STEP_BYTES_PER_PARTICLE = 344.0  # algorithmic bytes per particle-step (byte model)
 METRIC = "particle-steps/s, 720k dam break, 1 GB300: surrogate/batched vs plain, <=1% front err"
+# ALE-SPH byte model per fluid particle: flux pass reads loc, key, v, rho - rho0,
+# omega (32 B) and writes the three rates (16 B); whole step (leap-frog one
+# 124 B, fluxes 48 B, leap-frog two + binning 208 B, counting sort 276 B)
+ALE_FLUX_BYTES_PER_PARTICLE = 48.0
+ALE_STEP_BYTES_PER_PARTICLE = 656.0
+ALE_METRIC = "particle-steps/s, ALE-SPH dam break dp=0.0004 (1.1M fluid), 1 GB300"
 
 
 def _env_int(k, d):
@@ -51,7 +61,7 @@ def measured_peaks():
 
 def profile_traffic():
     """dram bytes per launch of the pair kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "k_fluid_pairs_dam_break_720k.txt")
+    p = os.path.join(ROOT, "profiles", "k_pairs_tiled_dam_break_720k.md")
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -142,10 +152,183 @@ def host_threads():
         return os.cpu_count() or 1
 
 
+def run_reference_ale(args):
+    """Reference arm of the ALE workload: the oracle's restatement of the
+    reference's MUSCL.h RUN loop on all host cores."""
+    from tinysph_old_gb300 import cases
+
+    case = cases.dam_break_ale(dp=args.dp)
+    threads = host_threads()
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    P = oracle.PortAle.from_case(case)
+    P.set_threads(threads)
+    for k in range(args.warmup):
+        P.ale_step(case.dt, k, 1)
+    times = []
+    for k in range(args.steps):
+        t0 = time.perf_counter()
+        P.ale_step(case.dt, args.warmup + k, 1)
+        times.append(time.perf_counter() - t0)
+        if sum(times) > 150.0:
+            break
+    total = sum(times)
+    n = P.np()
+    value = n * len(times) / total
+    print(json.dumps({
+        "metric": ALE_METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": 1,
+        "steps": len(times), "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (BT-wall dam break built like the reference's generators)",
+        "impl": "reference",
+        "config": {"workload": f"ALE-SPH dam break dp={args.dp}, {n} particles", "particles": n,
+                   "dp": args.dp, "l2": "n/a (CPU)"},
+        "cpu_baseline": {"value": value, "unit": "particle-steps/s", "cores": threads,
+                         "kind": "port", "sample": f"{len(times)} time steps of the {n}-particle case"},
+        "e2e": {"value": value, "unit": "particle-steps/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def run_ale(args, rank, world, local):
+    """Our arm of the ALE workload (N = 1; replicas for N > 1)."""
+    import numpy as np
+    import torch
+
+    from tinysph_old_gb300 import cases, sph
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    case = cases.dam_break_ale(dp=args.dp)
+    stream = torch.cuda.Stream()
+    s = sph.AleSystem(case.h, case.kap, case.cs, case.rho0, case.visco, case.delta, case.dp,
+                      case.domain, stream=stream.cuda_stream)
+    a = case.particles.arrays()
+    nrm = np.zeros((case.np, 2))
+    nn = np.asarray(case.particles.normals).reshape(-1, 2)
+    nrm[:len(nn)] = nn
+    s.add_particles(a["type"], a["r"], a["v"], a["rho"], a["p"], nrm)
+    s.set_scheme(sph.ALE_MUSCL if args.scheme == "muscl" else sph.ALE_AS_WRITTEN)
+    s.divide_to_cells()
+    s.particle_to_cell()
+    n = s.np
+    nfluid = int(np.sum(a["type"] == 0))
+    dt = case.dt
+    step = 0
+    for _ in range(args.warmup):
+        s.step(dt, step, 1)
+        step += 1
+    s.sync()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                flush.zero_()
+                starts[k].record(stream)
+                s.step(dt, step, 1)
+                step += 1
+                ends[k].record(stream)
+        stream.synchronize()
+    torch.cuda.synchronize()
+    ms = sum(starts[k].elapsed_time(ends[k]) for k in range(args.steps))
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n * args.steps / (ms / 1000.0)
+    # flux kernel alone (one launch per call), events on the system's stream
+    fl_us = []
+    for _ in range(5):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            flush.zero_()
+            e0.record(stream)
+            s.forces(dt)
+            e1.record(stream)
+        stream.synchronize()
+        fl_us.append(1000.0 * e0.elapsed_time(e1))
+    flux_us = statistics.median(fl_us)
+    peak, peak_kind = measured_peaks()
+    achieved = ALE_FLUX_BYTES_PER_PARTICLE * nfluid / (flux_us * 1e-6) / 1e9
+    # e2e: host state in and out through the C ABI every step
+    hr = np.empty((n, 2)); hv = np.empty((n, 2)); hrho = np.empty(n)
+    st = s.download(sph.ALE_F_R | sph.ALE_F_V | sph.ALE_F_RHO)
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        s.upload(r=st["r"], v=st["v"], rho=st["rho"])
+        s.particle_to_cell()
+        s.step(dt, step, 1)
+        step += 1
+        st = s.download(sph.ALE_F_R | sph.ALE_F_V | sph.ALE_F_RHO)
+    e2e_value = world * n * args.e2e_steps / (time.perf_counter() - t0)
+    xfer = n * 40
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        threads = host_threads()
+        P = oracle.PortAle.from_case(case)
+        P.set_threads(threads)
+        P.ale_step(dt, 0, 1)
+        t0 = time.perf_counter()
+        nst = 3
+        P.ale_step(dt, 1, nst)
+        tt = time.perf_counter() - t0
+        cpu = {"value": P.np() * nst / tt, "unit": "particle-steps/s", "cores": threads,
+               "kind": "port", "sample": f"{nst} time steps of the same {n}-particle case "
+                                         f"({tt:.1f} s, FP64 C restatement, OpenMP)"}
+    if rank == 0:
+        line = {
+            "metric": ALE_METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 fluxes, f64 integration",
+            "data": "synthetic (BT-wall dam break built like the reference's generators)",
+            "config": {"workload": f"ALE-SPH dam break dp={args.dp}, {n} particles "
+                                   f"({nfluid} fluid), scheme {args.scheme}",
+                       "particles": n, "fluid": nfluid, "dp": args.dp,
+                       "l2": "flushed (256 MB write) between timed steps",
+                       "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
+            "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": xfer,
+                    "d2h_bytes_per_step": xfer,
+                    "path": "tsph_ale_upload(r,v,rho) + tsph_ale_particle_to_cell + "
+                            "tsph_ale_step(1) + tsph_ale_download(r,v,rho), pageable buffers"},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None, "kernel": "k_ale_flux",
+                         "bytes_per_unit": ALE_FLUX_BYTES_PER_PARTICLE, "unit_count": nfluid,
+                         "avg_launch_us": flux_us, "peak_kind": peak_kind},
+            "step_roofline": {"bytes_per_particle_step": ALE_STEP_BYTES_PER_PARTICLE,
+                              "achieved_gbs": ALE_STEP_BYTES_PER_PARTICLE * value / world / 1e9,
+                              "frac": ALE_STEP_BYTES_PER_PARTICLE * value / world / 1e9 / peak},
+            "gpu_launches": args.steps * (8 if args.scheme == "muscl" else 7),
+            "clocks": clocks.summary(),
+            "health": s.health(),
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
 def run_reference(args, rank, world):
     """The reference arm: the CPU restatement of the reference's step on all
     host cores, on the same workload.  Rank 0 only."""
     if rank != 0:
+        return
+    if args.workload == "ale":
+        run_reference_ale(args)
         return
     from tinysph_old_gb300 import cases
 
@@ -193,7 +376,11 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--dp", type=float, default=0.0005)
+    ap.add_argument("--workload", default="dam_break", choices=["dam_break", "ale"])
+    ap.add_argument("--scheme", default="as_written", choices=["as_written", "muscl"],
+                    help="ALE interface states (ALE workload only)")
+    ap.add_argument("--dp", type=float, default=None,
+                    help="particle spacing (default 0.0005 dam break, 0.0004 ALE)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])
     ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--cpu-steps", type=int, default=0,
@@ -201,6 +388,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.dp is None:
+        args.dp = 0.0004 if args.workload == "ale" else 0.0005
 
     rank = _env_int("RANK", 0)
     world = _env_int("WORLD_SIZE", 1)
@@ -208,6 +397,9 @@ def main():
 
     if args.impl == "reference":
         run_reference(args, rank, world)
+        return
+    if args.workload == "ale":
+        run_ale(args, rank, world, local)
         return
 
     import numpy as np
@@ -338,7 +530,7 @@ def main():
                             "tsph_download(r,v,rho), pinned host buffers"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_fluid_pairs (forces + corrector / forces)",
+                         "kernel": "k_pairs_tiled (forces + corrector / forces)",
                          "bytes_per_unit": PAIR_BYTES_PER_PARTICLE, "unit_count": nfluid,
                          "avg_launch_us": pair_avg_us, "peak_kind": peak_kind},
             "step_roofline": {"bytes_per_particle_step": STEP_BYTES_PER_PARTICLE,
