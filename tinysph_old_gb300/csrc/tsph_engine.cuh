@@ -235,7 +235,7 @@ template <typename T> class Engine final : public EngineBase {
             return rc;
         // forces at the predicted state + corrector + bin
         if ((rc = zero_counts(err))) return rc;
-        PairOut po{Br_, (void *)Bv_, (void *)Brho_, keyB_, slotB_, counts_, box_};
+        PairOut po{Br_, (void *)Bv_, (void *)Brho_, keyB_, slotB_, counts_, box_, make_box_bits(box_)};
         if ((rc = fluid_pairs<MODE_CORRECT>(Fs_, false, dt, po, err))) return rc;
         if (nw_ > 0 &&
             (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,

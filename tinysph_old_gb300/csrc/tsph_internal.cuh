@@ -122,6 +122,12 @@ struct Box {
     double x0, xm, y0, ym;
 };
 
+// the thresholds of RemoveParticlesOutOfDomain (x0 - eps, xm - eps, y0 - eps,
+// ym + eps with eps = 0.01, src/SPH_btdebug.h:16-19) as ordered bits
+struct BoxBits {
+    long long x_lo, x_hi, y_lo, y_hi;
+};
+
 // physical constants in both precisions
 template <typename T> struct Phys {
     double hd;             // h in FP64 (exact pair-set tests)

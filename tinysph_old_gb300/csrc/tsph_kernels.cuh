@@ -549,7 +549,19 @@ struct PairOut {  // where MODE_CORRECT writes the new (unsorted) state
     void *rho;
     uint32_t *key, *slot, *counts;
     Box box;
+    BoxBits boxb;
 };
+
+// ordered bits with -0.0 folded onto +0.0 (they compare equal in FP64)
+__host__ __device__ inline long long ordered_bits_fold0(double x) {
+    const long long o = ordered_bits(x);
+    return o == -1LL ? 0LL : o;
+}
+
+inline BoxBits make_box_bits(const Box &b) {
+    return BoxBits{ordered_bits_fold0(b.x0 - 0.01), ordered_bits_fold0(b.xm - 0.01),
+                   ordered_bits_fold0(b.y0 - 0.01), ordered_bits_fold0(b.ym + 0.01)};
+}
 
 template <typename T> struct Nbr {  // neighbour fields read by the pair loop
     const double2 *r;
@@ -952,8 +964,14 @@ __global__ void k_predict_bin(FluidState<T> F, const uint32_t *__restrict__ fsta
     const auto v = F.v[f];
     const auto a = F.a[f];
     Brho[f] = F.rho[f] + F.drho[f] * dt * T(0.5);
-    const double2 rn =
-        make_double2(r.x + (double)v.x * (double)dt * 0.5, r.y + (double)v.y * (double)dt * 0.5);
+    double2 rn;
+    if constexpr (std::is_same<T, float>::value) {
+        // FP32 displacement (v is FP32 already), one FP64 add per axis
+        const float hdt = dt * 0.5f;
+        rn = make_double2(r.x + (double)(v.x * hdt), r.y + (double)(v.y * hdt));
+    } else {
+        rn = make_double2(r.x + (double)v.x * (double)dt * 0.5, r.y + (double)v.y * (double)dt * 0.5);
+    }
     Br[f] = rn;
     typename V2<T>::t nv;
     nv.x = v.x + a.x * dt * T(0.5);

@@ -26,13 +26,15 @@ namespace tsph {
 
 constexpr int kTileT = 128;     // targets per CTA
 constexpr int kTileRows = 16;   // max target rows per window (halved while the block is too big)
-constexpr int kTileCap = 768;   // staged neighbours per window
-constexpr int kList = 40;       // list entries per target (overflow: global-memory path)
+constexpr int kTileCap = 608;   // staged neighbours per window
+constexpr int kList = 36;       // list entries per target (overflow: global-memory path)
 
+// 8 CTAs of 128 threads per SM: 28 B per staged neighbour + 72 B of list per
+// target keep a CTA under 27.5 KB of shared memory
 struct TileSmem {
     float2 loc[kTileCap];
-    float2 vel[kTileCap];
-    float4 rp[kTileCap];  // {rho - rho0, p/rho, 1/rho, rho}
+    float4 vs[kTileCap];   // {vx, vy, rho - rho0, p/rho}
+    float inv[kTileCap];   // 1/rho
     int foff[3][kTileRows + 3];
     int woff[3][kTileRows + 3];
     float2 off[9];
@@ -57,6 +59,7 @@ struct TileConst {
     float eps_h2, four_h2;
     float k_av;             // -2 alpha c0 h: Pi = k_av dr.dv / ((r^2 + eps h^2)(rho_a + rho_b))
     float c1, c2;           // rho0((1 + x)^(1/7) - 1) ~ dy (c1 + c2 dy), x = xg dy
+    float two_rho0;
 };
 
 __device__ __forceinline__ float sqrt_approx(float x) {
@@ -65,10 +68,10 @@ __device__ __forceinline__ float sqrt_approx(float x) {
     return r;
 }
 
-// rb_full = rho_b (full density of the neighbour), ra_full likewise
+// Ra2 = 2 rho0 + (rho_a - rho0), so rho_a + rho_b = Ra2 + sb
 __device__ __forceinline__ void pair_terms(float dx, float dy, float dvx, float dvy, float sa,
-                                           float Pa, float Ia, float ra_full, float sb, float Pb,
-                                           float Ib, float rb_full, const TileConst &K, Acc4 &acc) {
+                                           float Pa, float Ia, float Ra2, float sb, float Pb,
+                                           float Ib, const TileConst &K, Acc4 &acc) {
     const float dy2 = dy * dy;
     const float r2 = fmaf(dx, dx, dy2);
     const float w1 = fmaf(sqrt_approx(r2), K.neg_half_inv_h, 1.f);
@@ -78,7 +81,7 @@ __device__ __forceinline__ void pair_terms(float dx, float dy, float dvx, float 
     float pterm = fmaf(Pa, Ib, Pb * Ia);
     if (drdv < 0.f) {
         // artificial viscosity with the mean density 0.5 (rho_a + rho_b)
-        pterm = fmaf(K.k_av * drdv, inv_den * rcp_approx(ra_full + rb_full), pterm);
+        pterm = fmaf(K.k_av * drdv, inv_den * rcp_approx(Ra2 + sb), pterm);
     }
     const float coef = w3 * pterm;
     acc.ax = fmaf(-dx, coef, acc.ax);
@@ -89,11 +92,9 @@ __device__ __forceinline__ void pair_terms(float dx, float dy, float dvx, float 
     acc.diff = fmaf(psi * r2, w3 * Ib, acc.diff);
 }
 
-// per-particle derived quantities of a neighbour: {s, p/rho, 1/rho}
-__device__ __forceinline__ float4 staged_rp(float s, float p, const Phys<float> &P) {
-    const float rho = P.rho0 + s;
-    const float inv = rcp_approx(rho);
-    return make_float4(s, p * inv, inv, rho);
+// per-particle derived quantities of a neighbour: {vx, vy, s, p/rho} and 1/rho
+__device__ __forceinline__ float4 staged_vs(float2 v, float s, float p, float inv) {
+    return make_float4(v.x, v.y, s, p * inv);
 }
 
 // all in-support neighbours of one target straight from global memory (the
@@ -104,7 +105,7 @@ __device__ __forceinline__ void target_global(const FluidState<float> &F, const 
                                               const uint32_t *wstart, const WallState<float> &Wl,
                                               const Grid &g, const Phys<float> &P,
                                               const TileConst &K, int i, int cx, int cy, float2 la,
-                                              float2 va, float sa, float Pa, float Ia, float Ra,
+                                              float2 va, float sa, float Pa, float Ia, float Ra2,
                                               Acc4 &acc) {
     for (int dxi = 0; dxi < 3; dxi++) {
         const int col = cx + dxi - 1;
@@ -125,10 +126,10 @@ __device__ __forceinline__ void target_global(const FluidState<float> &F, const 
                     if (!(r2 <= K.four_h2 && r2 > 0.f)) continue;
                     const float s = __ldg((kind == 0 ? Wl.rho : F.rho) + j);
                     const float p = STORED_P ? __ldg((kind == 0 ? Wl.p : F.p) + j) : eos(s, P);
-                    const float4 rb = staged_rp(s, p, P);
+                    const float ib = rcp_approx(P.rho0 + s);
                     const float2 vb = kind == 0 ? make_float2(0.f, 0.f) : __ldg(F.v + j);
-                    pair_terms(dx, dy, va.x - vb.x, va.y - vb.y, sa, Pa, Ia, Ra, rb.x, rb.y, rb.z,
-                               rb.w, K, acc);
+                    pair_terms(dx, dy, va.x - vb.x, va.y - vb.y, sa, Pa, Ia, Ra2, s, p * ib, ib, K,
+                               acc);
                 }
             }
         }
@@ -140,8 +141,20 @@ __device__ __forceinline__ uint32_t in_support(float r2, uint32_t four_h2_bits) 
     return (uint32_t)(__float_as_uint(r2) - 1u) < four_h2_bits ? 1u : 0u;
 }
 
+// RemoveParticlesOutOfDomain's test (src/SPH_btdebug.h:16-19) on the ordered
+// bits of the coordinates against precomputed ordered thresholds: integer
+// compares instead of FP64 ones (GB300 issues FP64 at a small fraction of the
+// FP32 rate).  NaN coordinates compare false, as in FP64.
+__device__ __forceinline__ bool out_of_domain_bits(double2 r, const BoxBits &b) {
+    const long long ox = ordered_bits_fold0(r.x), oy = ordered_bits_fold0(r.y);
+    const long long ax = __double_as_longlong(r.x) & 0x7fffffffffffffffLL;
+    const long long ay = __double_as_longlong(r.y) & 0x7fffffffffffffffLL;
+    const bool nan = ax > 0x7ff0000000000000LL || ay > 0x7ff0000000000000LL;
+    return !nan && (oy < b.y_lo || oy > b.y_hi || ox < b.x_lo || ox > b.x_hi);
+}
+
 template <int MODE, bool STORED_P>
-__global__ void __launch_bounds__(kTileT, 6)
+__global__ void __launch_bounds__(kTileT, 8)
 k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
               const uint32_t *__restrict__ wstart, WallState<float> Wl, Grid g, Phys<float> P,
               TileConst K, OldState<float> O, float dt, PairOut out,
@@ -202,7 +215,7 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
         const bool active = i < we;
         Acc4 acc = {0.f, 0.f, 0.f, 0.f};
         float2 la = make_float2(0.f, 0.f), va = make_float2(0.f, 0.f);
-        float sa = 0.f, Pa = 0.f, Ia = 0.f, Ra = 0.f;
+        float sa = 0.f, Pa = 0.f, Ia = 0.f, Ra2 = 0.f;
         int cy = 0;
         if (tot <= kTileCap) {
             // ---- stage the neighbour block
@@ -213,18 +226,20 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                     const int j = w0[d] + k;
                     const float s = __ldg(Wl.rho + j);
                     const float p = STORED_P ? __ldg(Wl.p + j) : eos(s, P);
+                    const float ib = rcp_approx(P.rho0 + s);
                     sm.loc[wb[d] + k] = __ldg(Wl.loc + j);
-                    sm.vel[wb[d] + k] = make_float2(0.f, 0.f);
-                    sm.rp[wb[d] + k] = staged_rp(s, p, P);
+                    sm.vs[wb[d] + k] = staged_vs(make_float2(0.f, 0.f), s, p, ib);
+                    sm.inv[wb[d] + k] = ib;
                 }
                 const int nfd = sm.foff[d][nr] - f0[d];
                 for (int k = tid; k < nfd; k += kTileT) {
                     const int j = f0[d] + k;
                     const float s = __ldg(F.rho + j);
                     const float p = STORED_P ? __ldg(F.p + j) : eos(s, P);
+                    const float ib = rcp_approx(P.rho0 + s);
                     sm.loc[fb[d] + k] = __ldg(F.loc + j);
-                    sm.vel[fb[d] + k] = __ldg(F.v + j);
-                    sm.rp[fb[d] + k] = staged_rp(s, p, P);
+                    sm.vs[fb[d] + k] = staged_vs(__ldg(F.v + j), s, p, ib);
+                    sm.inv[fb[d] + k] = ib;
                 }
             }
             __syncthreads();
@@ -232,12 +247,12 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 cy = (int)__ldg(F.key + i) - cx * ncy;
                 const int own = fb[1] + (i - f0[1]);
                 la = sm.loc[own];
-                va = sm.vel[own];
-                const float4 rpa = sm.rp[own];
-                sa = rpa.x;
-                Pa = rpa.y;
-                Ia = rpa.z;
-                Ra = rpa.w;
+                const float4 vsa = sm.vs[own];
+                va = make_float2(vsa.x, vsa.y);
+                sa = vsa.z;
+                Pa = vsa.w;
+                Ia = sm.inv[own];
+                Ra2 = K.two_rho0 + sa;
                 // ---- phase 1: in-support neighbours into the list.  The list
                 // write is unconditional (the slot is only kept when the pair
                 // is in support); overflow is checked once per cell.
@@ -268,8 +283,21 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                             }
                             uint16_t *w = lst + cnt * kTileT;
                             if (dyi == 1) {
+                                // own row: every candidate, two per iteration
                                 uint32_t ent = ((uint32_t)j0 << 4) | (uint32_t)code;
-                                for (int j = j0; j < j1; j++, ent += 16u) {
+                                int j = j0;
+                                for (; j + 1 < j1; j += 2, ent += 32u) {
+                                    const float2 lb0 = sm.loc[j], lb1 = sm.loc[j + 1];
+                                    const float dx0 = bx - lb0.x, dy0 = by - lb0.y;
+                                    const float dx1 = bx - lb1.x, dy1 = by - lb1.y;
+                                    const uint32_t in0 = in_support(fmaf(dx0, dx0, dy0 * dy0), h2bits);
+                                    const uint32_t in1 = in_support(fmaf(dx1, dx1, dy1 * dy1), h2bits);
+                                    *w = (uint16_t)ent;
+                                    w += in0 * kTileT;
+                                    *w = (uint16_t)(ent + 16u);
+                                    w += in1 * kTileT;
+                                }
+                                if (j < j1) {
                                     const float2 lb = sm.loc[j];
                                     const float dx = bx - lb.x, dy = by - lb.y;
                                     const uint32_t in = in_support(fmaf(dx, dx, dy * dy), h2bits);
@@ -311,26 +339,25 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                         const float2 o0 = sm.off[e0 & 15u], o1 = sm.off[e1 & 15u];
                         const int j0 = (int)(e0 >> 4), j1 = (int)(e1 >> 4);
                         const float2 lb0 = sm.loc[j0], lb1 = sm.loc[j1];
-                        const float2 vb0 = sm.vel[j0], vb1 = sm.vel[j1];
-                        const float4 rb0 = sm.rp[j0], rb1 = sm.rp[j1];
-                        pair_terms((la.x + o0.x) - lb0.x, (la.y + o0.y) - lb0.y, va.x - vb0.x,
-                                   va.y - vb0.y, sa, Pa, Ia, Ra, rb0.x, rb0.y, rb0.z, rb0.w, K, acc);
-                        pair_terms((la.x + o1.x) - lb1.x, (la.y + o1.y) - lb1.y, va.x - vb1.x,
-                                   va.y - vb1.y, sa, Pa, Ia, Ra, rb1.x, rb1.y, rb1.z, rb1.w, K, acc);
+                        const float4 b0 = sm.vs[j0], b1 = sm.vs[j1];
+                        const float ib0 = sm.inv[j0], ib1 = sm.inv[j1];
+                        pair_terms((la.x + o0.x) - lb0.x, (la.y + o0.y) - lb0.y, va.x - b0.x,
+                                   va.y - b0.y, sa, Pa, Ia, Ra2, b0.z, b0.w, ib0, K, acc);
+                        pair_terms((la.x + o1.x) - lb1.x, (la.y + o1.y) - lb1.y, va.x - b1.x,
+                                   va.y - b1.y, sa, Pa, Ia, Ra2, b1.z, b1.w, ib1, K, acc);
                     }
                     if (k < cnt) {
                         const uint32_t e = lst[k * kTileT];
                         const int j = (int)(e >> 4);
                         const float2 o = sm.off[e & 15u];
                         const float2 lb = sm.loc[j];
-                        const float2 vb = sm.vel[j];
-                        const float4 rb = sm.rp[j];
-                        pair_terms((la.x + o.x) - lb.x, (la.y + o.y) - lb.y, va.x - vb.x,
-                                   va.y - vb.y, sa, Pa, Ia, Ra, rb.x, rb.y, rb.z, rb.w, K, acc);
+                        const float4 b = sm.vs[j];
+                        pair_terms((la.x + o.x) - lb.x, (la.y + o.y) - lb.y, va.x - b.x,
+                                   va.y - b.y, sa, Pa, Ia, Ra2, b.z, b.w, sm.inv[j], K, acc);
                     }
                 } else {
                     target_global<STORED_P>(F, fstart, wstart, Wl, g, P, K, i, cx, cy, la, va, sa,
-                                            Pa, Ia, Ra, acc);
+                                            Pa, Ia, Ra2, acc);
                 }
             }
         } else if (active) {
@@ -339,12 +366,11 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
             va = __ldg(F.v + i);
             sa = __ldg(F.rho + i);
             const float p = STORED_P ? __ldg(F.p + i) : eos(sa, P);
-            const float4 rpa = staged_rp(sa, p, P);
-            Pa = rpa.y;
-            Ia = rpa.z;
-            Ra = rpa.w;
+            Ia = rcp_approx(P.rho0 + sa);
+            Pa = p * Ia;
+            Ra2 = K.two_rho0 + sa;
             target_global<STORED_P>(F, fstart, wstart, Wl, g, P, K, i, cx, cy, la, va, sa, Pa, Ia,
-                                    Ra, acc);
+                                    Ra2, acc);
         }
         if (active) {
             const float mb = P.m * P.bwen_h;
@@ -355,19 +381,24 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 F.a[i] = make_float2(ax, ay);
                 F.drho[i] = drho;
             } else {
+                // Integrate_SymplecticCorrector (src/SPH_integration.h:289-309):
+                // rho from the epsilon form with 1/rho_a already at hand, the
+                // displacement (v + v_o) dt/2 in FP32, one FP64 add per axis
                 const float so = O.rho[i];
-                const float s_new = corrector_rho(so, sa, drho, dt, P.rho0);
+                const float e = -drho * Ia * dt;
+                const float ie = rcp_approx(2.f + e);
+                const float s_new = so * ((2.f - e) * ie) - P.rho0 * (2.f * e * ie);
                 const float2 vo = O.v[i];
-                const float2 nv = make_float2(vo.x + ax * dt, vo.y + ay * dt);
+                const float2 nv = make_float2(fmaf(ax, dt, vo.x), fmaf(ay, dt, vo.y));
+                const float hdt = 0.5f * dt;
                 const double2 ro = O.r[i];
-                const double2 rn =
-                    make_double2(ro.x + ((double)nv.x + (double)vo.x) * (double)dt * 0.5,
-                                 ro.y + ((double)nv.y + (double)vo.y) * (double)dt * 0.5);
+                const double2 rn = make_double2(ro.x + (double)((nv.x + vo.x) * hdt),
+                                                ro.y + (double)((nv.y + vo.y) * hdt));
                 out.r[i] = rn;
                 reinterpret_cast<float2 *>(out.v)[i] = nv;
                 reinterpret_cast<float *>(out.rho)[i] = s_new;
                 uint32_t nk;
-                if (out_of_domain(rn, out.box)) {
+                if (out_of_domain_bits(rn, out.boxb)) {
                     nk = (uint32_t)g.ncells;
                     atomicOr(health, kHealthRemoved);
                 } else {
@@ -395,6 +426,7 @@ inline TileConst make_tile_const(const Phys<float> &P, double h, double rho0, do
     const double xg = 7.0 * g / (cs * cs);
     K.c1 = (float)(rho0 * xg / 7.0);
     K.c2 = (float)(-rho0 * 3.0 / 49.0 * xg * xg);
+    K.two_rho0 = (float)(2.0 * rho0);
     return K;
 }
 
