@@ -171,6 +171,45 @@ def test_fused_equals_per_function_sequence(gpu_tsph, precision):
 
 
 @pytest.mark.gpu
+def test_fused_step_rebins_when_particles_outrun_the_skin(gpu_tsph):
+    """The fused FP32 step keeps the cells of the last binning through the
+    predictor while every particle moved less than the skin ((kh - 2h)/2 per
+    axis); fluid at 30 m/s moves ~2x the skin in half a step, which must
+    trigger the gated re-binning: the step then matches the per-function
+    sequence (which always re-bins) within FP32 rounding."""
+    g = _gold("dam_break_mdbc_dp0.02.npz")
+    case = cases.dam_break_mdbc(dp=0.02)
+    dt = float(g["dt"])
+    rng = np.random.default_rng(5)
+    v = g["init_v"].copy()
+    fl = g["init_type"] == 0
+    ang = rng.uniform(0, 2 * np.pi, fl.sum())
+    v[fl] = 30.0 * np.stack([np.cos(ang), np.sin(ang)], 1)
+    a = gpu_tsph.ParticleSystem.from_case(case, "fp32")
+    b = gpu_tsph.ParticleSystem.from_case(case, "fp32")
+    for s in (a, b):
+        s.upload(v=v, rho=g["init_rho"])
+        s.density_to_pressure()
+        s.compute_forces(0)
+    a.step(0, dt, 1)
+    b.mdbc_density()
+    b.density_to_pressure()
+    b.predictor(dt)
+    b.particle_to_cell()
+    b.density_to_pressure()
+    b.compute_forces(0)
+    b.corrector(dt)
+    b.remove_out_of_domain()
+    b.particle_to_cell()
+    b.density_to_pressure()
+    b.compute_forces(0)
+    sa, sb = a.download(), b.download()
+    assert np.array_equal(sa["index"], sb["index"])
+    for f in ("r", "v", "a", "rho", "drho"):
+        assert _err(sa[f], sb[f]) <= 1e-5 * max(1.0, float(np.max(np.abs(sa[f])))), f
+
+
+@pytest.mark.gpu
 def test_stale_cells_are_an_error(gpu_tsph):
     case = cases.dam_break_mdbc(dp=0.02)
     s = gpu_tsph.ParticleSystem.from_case(case)

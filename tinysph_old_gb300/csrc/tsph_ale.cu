@@ -726,11 +726,11 @@ class AleEngine {
     int sort(AleFluid X, AleFluid Y, std::string &err) {
         const int n = ncells + 1;
         const int nt = (n + kScanTile - 1) / kScanTile;
-        k_scan_tiles_clear<<<nt, kScanThreads, 0, st>>>(counts, fstart, tiles, n);
-        k_scan_add_tiles<<<nblk(n), kBlock, 0, st>>>(fstart, tiles, nt, n);
+        k_scan_tiles_clear<<<nt, kScanThreads, 0, st>>>(counts, fstart, tiles, n, nullptr);
+        k_scan_add_tiles<<<nblk(n), kBlock, 0, st>>>(fstart, tiles, nt, n, nullptr);
         const int *ntot_ = reinterpret_cast<const int *>(fstart + ncells + 1);
         k_place<<<nblk(nf), kBlock, 0, st>>>(keyB, slotB, X.id, ntot_, fstart, tmp_id, tmp_src,
-                                             nullptr, nullptr);
+                                             nullptr, nullptr, nullptr);
         k_ale_rank_scatter<<<nblk(nf), kBlock, 0, st>>>(keyB, ntot_, fstart, tmp_id, tmp_src, grid,
                                                         X, Y);
         ACK(cudaGetLastError());

@@ -54,6 +54,8 @@ template <typename T> class Engine final : public EngineBase {
     uint32_t *counts_ = nullptr, *fstart_ = nullptr, *wstart_ = nullptr, *tile_sums_ = nullptr;
     long long *tmp_y_ = nullptr;
     uint32_t *health_ = nullptr, *removed_ = nullptr;
+    uint32_t *rebuild_ = nullptr;  // set when the fused step must re-bin after the predictor
+    float skin_ = 0.f;             // per-axis move allowed without re-binning (FP32 fused step)
     WallState<T> W_{};
     Staging S_{};
     double *dtot_ = nullptr;
@@ -146,15 +148,15 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     // scan counts[0..ncells] -> fstart[0..ncells+1]; leaves counts zeroed
-    int scan(std::string &err) {
+    int scan(std::string &err, const uint32_t *gate = nullptr) {
         const int n = ncells_ + 1;
         const int ntiles = (n + kScanTile - 1) / kScanTile;
         int rc;
         if ((rc = launch(CAT_SORT, k_scan_tiles_clear, ntiles, kScanThreads, err, counts_, fstart_,
-                         tile_sums_, n)))
+                         tile_sums_, n, gate)))
             return rc;
         return launch(CAT_SORT, k_scan_add_tiles, blocks_for(n), kBlock, err, fstart_,
-                      (const uint32_t *)tile_sums_, ntiles, n);
+                      (const uint32_t *)tile_sums_, ntiles, n, gate);
     }
 
     // after keys/slots are in keyB_/slotB_ and counts_ is filled:
@@ -162,22 +164,22 @@ template <typename T> class Engine final : public EngineBase {
     int sort_finish(const double2 *sr, const T2 *sv, const T *srho, const uint32_t *sid,
                     const T2 *sa, const T *sdrho, const T *sp, FluidState<T> D,
                     const double2 *or2, const T2 *ov2, const T *orho2, OldState<T> Od,
-                    std::string &err) {
+                    std::string &err, const uint32_t *gate = nullptr) {
         int rc;
-        if ((rc = scan(err))) return rc;
+        if ((rc = scan(err, gate))) return rc;
         const int *ntot = reinterpret_cast<const int *>(fstart_ + ncells_ + 1);
         const int nb = blocks_for(nf_);
         // FP32 build: cells ordered by (y, index); FP64 build: by index
         constexpr bool by_y = std::is_same<T, float>::value;
         if ((rc = launch(CAT_SORT, k_place, nb, kBlock, err, (const uint32_t *)keyB_,
                          (const uint32_t *)slotB_, sid, ntot, (const uint32_t *)fstart_, tmp_id_,
-                         tmp_src_, by_y ? sr : (const double2 *)nullptr, tmp_y_)))
+                         tmp_src_, by_y ? sr : (const double2 *)nullptr, tmp_y_, gate)))
             return rc;
         return launch(CAT_SORT, k_rank_scatter<T>, nb, kBlock, err, (const uint32_t *)keyB_, ntot,
                       (const uint32_t *)fstart_, (const uint32_t *)tmp_id_,
                       (const uint32_t *)tmp_src_,
                       by_y ? (const long long *)tmp_y_ : (const long long *)nullptr, grid_, sr, sv,
-                      srho, sid, sa, sdrho, sp, D, or2, ov2, orho2, Od);
+                      srho, sid, sa, sdrho, sp, D, or2, ov2, orho2, Od, gate);
     }
 
     // the histogram is zero between sorts (the scan clears it)
@@ -196,19 +198,22 @@ template <typename T> class Engine final : public EngineBase {
                           nw_, (const uint32_t *)fstart_, nbr_fluid(F_, false), grid_, P_);
     }
 
-    TileConst K_{};
+    TileConst K_{}, Kskin_{};
 
-    // the fluid-row pair pass: tiled FP32 kernel, or the plain FP64 kernel
+    // the fluid-row pair pass: tiled FP32 kernel, or the plain FP64 kernel.
+    // `skinned`: the cells are those of the binning before the predictor.
     template <int MODE>
-    int fluid_pairs(const FluidState<T> &X, bool stored_p, T dt, PairOut po, std::string &err) {
+    int fluid_pairs(const FluidState<T> &X, bool stored_p, T dt, PairOut po, std::string &err,
+                    bool skinned = false) {
         if constexpr (std::is_same<T, float>::value) {
             const int nb = blocks_for(nf_, kTileT);
+            const TileConst K = skinned ? Kskin_ : K_;
             if (stored_p)
                 return launch(CAT_PAIR, k_pairs_tiled<MODE, true>, nb, kTileT, err, X,
                               (const uint32_t *)fstart_, (const uint32_t *)wstart_, W_, grid_, P_,
-                              K_, O_, dt, po, health_);
+                              K, O_, dt, po, health_);
             return launch(CAT_PAIR, k_pairs_tiled<MODE, false>, nb, kTileT, err, X,
-                          (const uint32_t *)fstart_, (const uint32_t *)wstart_, W_, grid_, P_, K_,
+                          (const uint32_t *)fstart_, (const uint32_t *)wstart_, W_, grid_, P_, K,
                           O_, dt, po, health_);
         } else {
             return launch(CAT_PAIR, k_fluid_pairs<T, MODE>, blocks_for(nf_), kBlock, err, X,
@@ -224,19 +229,43 @@ template <typename T> class Engine final : public EngineBase {
         int rc;
         const bool dbc = model == 1;
         if (!dbc && (rc = do_mdbc(err))) return rc;
-        // predictor + bin
-        if ((rc = zero_counts(err))) return rc;
-        if ((rc = launch(CAT_OTHER, k_predict_bin<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
-                         (const uint32_t *)fstart_, W_, nw_, grid_, dt, Br_, Bv_, Brho_, keyB_,
-                         slotB_, counts_, health_)))
-            return rc;
-        if ((rc = sort_finish(Br_, Bv_, Brho_, F_.id, nullptr, nullptr, nullptr, Fs_, F_.r, F_.v,
-                              F_.rho, O_, err)))
-            return rc;
+        bool skinned = false;
+        if constexpr (std::is_same<T, float>::value) skinned = skin_ > 0.f;
+        if (skinned) {
+            // predictor in the current order; the re-binning runs only when
+            // some particle moved more than the skin (gated on rebuild_)
+            TSPH_CK(cudaMemsetAsync(rebuild_, 0, 4, st_));
+            if ((rc = launch(CAT_OTHER, k_predict_keep<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                             (const uint32_t *)fstart_, W_, nw_, grid_, dt, Fs_, O_, skin_,
+                             rebuild_, health_)))
+                return rc;
+            const uint32_t *gate = rebuild_;
+            if ((rc = launch(CAT_SORT, k_bin_gated<T>, blocks_for(nf_), kBlock, err,
+                             (const FluidState<T>)Fs_, (const uint32_t *)fstart_, grid_, keyB_,
+                             slotB_, counts_, health_, gate)))
+                return rc;
+            if ((rc = sort_finish(Fs_.r, Fs_.v, Fs_.rho, Fs_.id, nullptr, nullptr, nullptr, F_,
+                                  O_.r, O_.v, O_.rho, OldState<T>{Br_, Bv_, Brho_}, err, gate)))
+                return rc;
+            if ((rc = launch(CAT_SORT, k_copy_back<T>, blocks_for(nf_), kBlock, err,
+                             (const FluidState<T>)F_, (const double2 *)Br_, (const T2 *)Bv_,
+                             (const T *)Brho_, (const uint32_t *)fstart_, ncells_, Fs_, O_, gate)))
+                return rc;
+        } else {
+            // predictor + bin
+            if ((rc = zero_counts(err))) return rc;
+            if ((rc = launch(CAT_OTHER, k_predict_bin<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                             (const uint32_t *)fstart_, W_, nw_, grid_, dt, Br_, Bv_, Brho_, keyB_,
+                             slotB_, counts_, health_)))
+                return rc;
+            if ((rc = sort_finish(Br_, Bv_, Brho_, F_.id, nullptr, nullptr, nullptr, Fs_, F_.r,
+                                  F_.v, F_.rho, O_, err)))
+                return rc;
+        }
         // forces at the predicted state + corrector + bin
         if ((rc = zero_counts(err))) return rc;
         PairOut po{Br_, (void *)Bv_, (void *)Brho_, keyB_, slotB_, counts_, box_, make_box_bits(box_)};
-        if ((rc = fluid_pairs<MODE_CORRECT>(Fs_, false, dt, po, err))) return rc;
+        if ((rc = fluid_pairs<MODE_CORRECT>(Fs_, false, dt, po, err, skinned))) return rc;
         if (nw_ > 0 &&
             (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
                          (const uint32_t *)fstart_, nbr_fluid(Fs_, false), grid_, P_, dbc, true, dt,
@@ -306,7 +335,14 @@ template <typename T> class Engine final : public EngineBase {
         P_.k_psi = (T)(2.0 * hs.cs * hs.h * hs.delta);
         P_.xg = (T)(hs.rho0 * hs.g / (hs.cs * hs.cs * hs.rho0 / 7.0));
         box_ = Box{hs.x0, hs.xm, hs.y0, hs.ym};
-        if constexpr (std::is_same<T, float>::value) K_ = make_tile_const(P_, hs.h, hs.rho0, hs.g, hs.cs);
+        if constexpr (std::is_same<T, float>::value) {
+            K_ = make_tile_const(P_, hs.h, hs.rho0, hs.g, hs.cs);
+            // per-axis move allowed between two binnings: kh >= 2h + 2 skin,
+            // with 5 % margin for the FP32 cell-local arithmetic
+            skin_ = (float)(0.95 * 0.5 * (hs.kh - 2.0 * hs.h));
+            Kskin_ = K_;
+            Kskin_.reach = K_.reach + 2.f * skin_;
+        }
         // grid tables
         int rc;
         if ((rc = alloc(&bx_, hs.bx.size(), err)) || (rc = alloc(&by_, hs.by.size(), err)) ||
@@ -349,6 +385,7 @@ template <typename T> class Engine final : public EngineBase {
         if ((rc = alloc(&counts_, ncells_ + 1, err)) || (rc = alloc(&fstart_, ncells_ + 2, err)) ||
             (rc = alloc(&wstart_, ncells_ + 1, err)) || (rc = alloc(&tile_sums_, ntiles, err)) ||
             (rc = alloc(&health_, 1, err)) || (rc = alloc(&removed_, 1, err)) ||
+            (rc = alloc(&rebuild_, 1, err)) ||
             (rc = alloc(&dtot_, 4 * (size_t)blocks_for(nf_), err)))
             return rc;
         TSPH_CK(cudaMemset(health_, 0, 4));

@@ -156,11 +156,19 @@ __device__ __forceinline__ float2 cell_local(const Grid &g, double2 r, int cx, i
     return make_float2((float)(r.x - __ldg(g.ax.org + cx)), (float)(r.y - __ldg(g.ay.org + cy)));
 }
 
+// The sort kernels take an optional gate: when `gate` is given and holds 0
+// the kernel does nothing (a rebuild that a CUDA graph carries but that only
+// runs when a device-side check asked for it).
+__device__ __forceinline__ bool gated_off(const uint32_t *gate) {
+    return gate != nullptr && __ldg(gate) == 0u;
+}
+
 // keys + histogram slot of fluid particles [0, n) (n read from *n_ptr).
 static __global__ void k_bin(const double2 *__restrict__ r, const uint32_t *__restrict__ old_key,
                       const int *__restrict__ n_ptr, Grid g, uint32_t *__restrict__ key,
                       uint32_t *__restrict__ slot, uint32_t *__restrict__ counts,
-                      uint32_t *__restrict__ health) {
+                      uint32_t *__restrict__ health, const uint32_t *__restrict__ gate) {
+    if (gated_off(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *n_ptr) return;
     int cx, cy;
@@ -249,7 +257,9 @@ static __global__ void __launch_bounds__(kScanThreads) k_scan_tiles(const uint32
 static __global__ void __launch_bounds__(kScanThreads) k_scan_tiles_clear(uint32_t *__restrict__ in,
                                                                          uint32_t *__restrict__ out,
                                                                          uint32_t *__restrict__ tile_sums,
-                                                                         int n) {
+                                                                         int n,
+                                                                         const uint32_t *__restrict__ gate) {
+    if (gated_off(gate)) return;
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
     uint32_t s = 0;
@@ -272,7 +282,9 @@ static __global__ void __launch_bounds__(kScanThreads) k_scan_tiles_clear(uint32
 // add the tile offsets; each block sums the tile totals before its own tile
 // (at most a few hundred), the last block writes the grand total to out[n]
 static __global__ void k_scan_add_tiles(uint32_t *__restrict__ out,
-                                        const uint32_t *__restrict__ tile_sums, int ntiles, int n) {
+                                        const uint32_t *__restrict__ tile_sums, int ntiles, int n,
+                                        const uint32_t *__restrict__ gate) {
+    if (gated_off(gate)) return;
     __shared__ uint32_t red[kBlock / 32];
     const int i0 = blockIdx.x * blockDim.x;
     const int t = i0 / kScanTile;
@@ -334,7 +346,8 @@ static __global__ void k_place(const uint32_t *__restrict__ key, const uint32_t 
                         const uint32_t *__restrict__ id, const int *__restrict__ n_ptr,
                         const uint32_t *__restrict__ start, uint32_t *__restrict__ tmp_id,
                         uint32_t *__restrict__ tmp_src, const double2 *__restrict__ r,
-                        long long *__restrict__ tmp_y) {
+                        long long *__restrict__ tmp_y, const uint32_t *__restrict__ gate) {
+    if (gated_off(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *n_ptr) return;
     const uint32_t d = start[key[i]] + slot[i];
@@ -385,7 +398,9 @@ __global__ void k_rank_scatter(const uint32_t *__restrict__ key, const int *__re
                                const typename V2<T>::t *__restrict__ sa, const T *__restrict__ sdrho,
                                const T *__restrict__ sp, FluidState<T> D,
                                const double2 *__restrict__ or2, const typename V2<T>::t *__restrict__ ov2,
-                               const T *__restrict__ orho2, OldState<T> O) {
+                               const T *__restrict__ orho2, OldState<T> O,
+                               const uint32_t *__restrict__ gate) {
+    if (gated_off(gate)) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= *n_ptr) return;
     const uint32_t src = tmp_src[j];
@@ -984,6 +999,87 @@ __global__ void k_predict_bin(FluidState<T> F, const uint32_t *__restrict__ fsta
     if (k == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
     key[f] = k;
     slot[f] = atomicAdd(counts + k, 1u);
+}
+
+// Predictor of the fused FP32 step without re-binning: the predicted state
+// goes to D in the current sorted order (cells, loc origins and fstart stay
+// those of the last binning), the old state to O.  The cells stay exact for
+// the pair set as long as every particle has moved less than `skin` per axis
+// since its binning (a pair within 2h then still lies inside the 3 x 3 cell
+// block, kh >= 2h + 2 skin); a larger move sets *rebuild, which runs the
+// gated re-binning before the pair pass.
+template <typename T>
+__global__ void k_predict_keep(FluidState<T> F, const uint32_t *__restrict__ fstart,
+                               WallState<T> Wl, int nw, Grid g, T dt, FluidState<T> D,
+                               OldState<T> O, float skin, uint32_t *__restrict__ rebuild,
+                               uint32_t *__restrict__ health) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nw) {
+        const T r = Wl.rho[i];
+        Wl.rho_o[i] = r;
+        Wl.rho[i] = r + Wl.drho[i] * dt * T(0.5);
+        return;
+    }
+    const int f = i - nw;
+    if (f >= n_live(fstart, g.ncells)) return;
+    const double2 r = F.r[f];
+    const auto v = F.v[f];
+    const auto a = F.a[f];
+    const T s = F.rho[f];
+    O.r[f] = r;
+    O.v[f] = v;
+    O.rho[f] = s;
+    const float hdt = (float)dt * 0.5f;
+    const float dx = (float)v.x * hdt, dy = (float)v.y * hdt;
+    D.r[f] = make_double2(r.x + (double)dx, r.y + (double)dy);
+    typename V2<T>::t nv;
+    nv.x = v.x + a.x * dt * T(0.5);
+    nv.y = v.y + a.y * dt * T(0.5);
+    D.v[f] = nv;
+    D.rho[f] = s + F.drho[f] * dt * T(0.5);
+    const float2 l = F.loc[f];
+    D.loc[f] = make_float2(l.x + dx, l.y + dy);
+    D.key[f] = F.key[f];
+    D.id[f] = F.id[f];
+    if (!(fabsf(dx) <= skin && fabsf(dy) <= skin)) atomicOr(rebuild, 1u);
+    if (!(nv.x == nv.x) || !(nv.y == nv.y) || !(dx == dx) || !(dy == dy))
+        atomicOr(health, kHealthNan);
+}
+
+// gated re-binning of the predicted state: keys + histogram slots
+template <typename T>
+__global__ void k_bin_gated(const FluidState<T> X, const uint32_t *__restrict__ fstart, Grid g,
+                            uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
+                            uint32_t *__restrict__ counts, uint32_t *__restrict__ health,
+                            const uint32_t *__restrict__ gate) {
+    if (gated_off(gate)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_live(fstart, g.ncells)) return;
+    int cx, cy;
+    const uint32_t k = cell_key(g, X.r[i], X.key[i], &cx, &cy);
+    if (k == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
+    key[i] = k;
+    slot[i] = atomicAdd(counts + k, 1u);
+}
+
+// gated copy of a re-binned state back into the buffers the graph reads
+template <typename T>
+__global__ void k_copy_back(const FluidState<T> S, const double2 *__restrict__ or2,
+                            const typename V2<T>::t *__restrict__ ov2, const T *__restrict__ orho2,
+                            const uint32_t *__restrict__ fstart, int ncells, FluidState<T> D,
+                            OldState<T> O, const uint32_t *__restrict__ gate) {
+    if (gated_off(gate)) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= (int)fstart[ncells + 1]) return;
+    D.r[j] = S.r[j];
+    D.v[j] = S.v[j];
+    D.rho[j] = S.rho[j];
+    D.id[j] = S.id[j];
+    D.key[j] = S.key[j];
+    D.loc[j] = S.loc[j];
+    O.r[j] = or2[j];
+    O.v[j] = ov2[j];
+    O.rho[j] = orho2[j];
 }
 
 // ------------------------------------------------------------ gathers

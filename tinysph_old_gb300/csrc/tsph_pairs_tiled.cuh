@@ -60,6 +60,7 @@ struct TileConst {
     float k_av;             // -2 alpha c0 h: Pi = k_av dr.dv / ((r^2 + eps h^2)(rho_a + rho_b))
     float c1, c2;           // rho0((1 + x)^(1/7) - 1) ~ dy (c1 + c2 dy), x = xg dy
     float two_rho0;
+    float reach;            // |dy| beyond which the y-sorted rows above / below stop
 };
 
 __device__ __forceinline__ float sqrt_approx(float x) {
@@ -168,8 +169,10 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
     const int t1 = min(t0 + kTileT, nl);
     if (tid < 9) sm.off[tid] = make_float2((float)(1 - tid / 3) * g.khf, (float)(1 - tid % 3) * g.khf);
     const uint32_t h2bits = __float_as_uint(K.four_h2);
-    // rows above / below are sorted by y: stop once |dy| > 2h (margin for rounding)
-    const float reach = 2.f * P.h * 1.0001f;
+    // rows above / below are sorted by y (as of the last binning): stop once
+    // |dy| > K.reach = 2h (+ rounding margin, + twice the skin when the cells
+    // were kept through the predictor)
+    const float reach = K.reach;
     int cur = t0;
     int rows = kTileRows;
     while (cur < t1) {  // block-uniform loop over row windows
@@ -427,6 +430,7 @@ inline TileConst make_tile_const(const Phys<float> &P, double h, double rho0, do
     K.c1 = (float)(rho0 * xg / 7.0);
     K.c2 = (float)(-rho0 * 3.0 / 49.0 * xg * xg);
     K.two_rho0 = (float)(2.0 * rho0);
+    K.reach = (float)(2.0 * h * 1.0001);
     return K;
 }
 
