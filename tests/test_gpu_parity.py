@@ -171,12 +171,15 @@ def test_fused_equals_per_function_sequence(gpu_tsph, precision):
 
 
 @pytest.mark.gpu
-def test_fused_step_rebins_when_particles_outrun_the_skin(gpu_tsph):
+@pytest.mark.parametrize("graph", [True, False])
+def test_fused_step_rebins_when_particles_outrun_the_skin(gpu_tsph, graph):
     """The fused FP32 step keeps the cells of the last binning through the
     predictor while every particle moved less than the skin ((kh - 2h)/2 per
     axis); fluid at 30 m/s moves ~2x the skin in half a step, which must
-    trigger the gated re-binning: the step then matches the per-function
-    sequence (which always re-bins) within FP32 rounding."""
+    trigger the re-binning (a conditional node of the step's CUDA graph, or
+    gated kernels when the step runs eagerly under profiling): the step then
+    matches the per-function sequence (which always re-bins) within FP32
+    rounding."""
     g = _gold("dam_break_mdbc_dp0.02.npz")
     case = cases.dam_break_mdbc(dp=0.02)
     dt = float(g["dt"])
@@ -191,6 +194,7 @@ def test_fused_step_rebins_when_particles_outrun_the_skin(gpu_tsph):
         s.upload(v=v, rho=g["init_rho"])
         s.density_to_pressure()
         s.compute_forces(0)
+    a.set_profiling(not graph)
     a.step(0, dt, 1)
     b.mdbc_density()
     b.density_to_pressure()

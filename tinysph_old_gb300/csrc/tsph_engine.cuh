@@ -55,6 +55,8 @@ template <typename T> class Engine final : public EngineBase {
     long long *tmp_y_ = nullptr;
     uint32_t *health_ = nullptr, *removed_ = nullptr;
     uint32_t *rebuild_ = nullptr;  // set when the fused step must re-bin after the predictor
+    bool capturing_ = false;       // enqueue_step is being captured into a graph
+    cudaStream_t st2_ = nullptr;   // side stream: captures the conditional re-binning body
     float skin_ = 0.f;             // per-axis move allowed without re-binning (FP32 fused step)
     WallState<T> W_{};
     Staging S_{};
@@ -224,6 +226,22 @@ template <typename T> class Engine final : public EngineBase {
         }
     }
 
+    // re-binning of the predicted state Fs_ (+ old state O_): sort into F_
+    // and B, copy back (FP32 fused step, when the skin was exceeded)
+    int rebin_predicted(const uint32_t *gate, std::string &err) {
+        int rc;
+        if ((rc = launch(CAT_SORT, k_bin_gated<T>, blocks_for(nf_), kBlock, err,
+                         (const FluidState<T>)Fs_, (const uint32_t *)fstart_, grid_, keyB_, slotB_,
+                         counts_, health_, gate)))
+            return rc;
+        if ((rc = sort_finish(Fs_.r, Fs_.v, Fs_.rho, Fs_.id, nullptr, nullptr, nullptr, F_, O_.r,
+                              O_.v, O_.rho, OldState<T>{Br_, Bv_, Brho_}, err, gate)))
+            return rc;
+        return launch(CAT_SORT, k_copy_back<T>, blocks_for(nf_), kBlock, err,
+                      (const FluidState<T>)F_, (const double2 *)Br_, (const T2 *)Bv_,
+                      (const T *)Brho_, (const uint32_t *)fstart_, ncells_, Fs_, O_, gate);
+    }
+
     // one fused step (enqueue only)
     int enqueue_step(int model, T dt, std::string &err) {
         int rc;
@@ -233,24 +251,52 @@ template <typename T> class Engine final : public EngineBase {
         if constexpr (std::is_same<T, float>::value) skinned = skin_ > 0.f;
         if (skinned) {
             // predictor in the current order; the re-binning runs only when
-            // some particle moved more than the skin (gated on rebuild_)
+            // some particle moved more than the skin: in a graph as the body
+            // of a conditional node the predictor switches on, otherwise as
+            // kernels gated on rebuild_
             TSPH_CK(cudaMemsetAsync(rebuild_, 0, 4, st_));
+            cudaGraphConditionalHandle cond = 0;
+            cudaGraph_t cg = nullptr;
+            cudaStreamCaptureStatus cs;
+            const cudaGraphNode_t *deps = nullptr;
+            size_t nd = 0;
+            if (capturing_) {
+                TSPH_CK(cudaStreamGetCaptureInfo(st_, &cs, nullptr, &cg, &deps, nullptr, &nd));
+                TSPH_CK(cudaGraphConditionalHandleCreate(&cond, cg, 0, cudaGraphCondAssignDefault));
+            }
             if ((rc = launch(CAT_OTHER, k_predict_keep<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
                              (const uint32_t *)fstart_, W_, nw_, grid_, dt, Fs_, O_, skin_,
-                             rebuild_, health_)))
+                             rebuild_, health_, cond, capturing_ ? 1 : 0)))
                 return rc;
-            const uint32_t *gate = rebuild_;
-            if ((rc = launch(CAT_SORT, k_bin_gated<T>, blocks_for(nf_), kBlock, err,
-                             (const FluidState<T>)Fs_, (const uint32_t *)fstart_, grid_, keyB_,
-                             slotB_, counts_, health_, gate)))
+            if (capturing_) {
+                TSPH_CK(cudaStreamGetCaptureInfo(st_, &cs, nullptr, &cg, &deps, nullptr, &nd));
+                cudaGraphNodeParams np = {};
+                np.type = cudaGraphNodeTypeConditional;
+                np.conditional.handle = cond;
+                np.conditional.type = cudaGraphCondTypeIf;
+                np.conditional.size = 1;
+                cudaGraphNode_t cn;
+                TSPH_CK(cudaGraphAddNode(&cn, cg, deps, nullptr, nd, &np));
+                cudaGraph_t body = np.conditional.phGraph_out[0];
+                if (!st2_) TSPH_CK(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
+                TSPH_CK(cudaStreamBeginCaptureToGraph(st2_, body, nullptr, nullptr, 0,
+                                                      cudaStreamCaptureModeThreadLocal));
+                std::swap(st_, st2_);
+                rc = rebin_predicted(nullptr, err);
+                std::swap(st_, st2_);
+                cudaGraph_t bodyc = nullptr;
+                const cudaError_t e = cudaStreamEndCapture(st2_, &bodyc);
+                if (rc) return rc;
+                if (e != cudaSuccess) {
+                    err = std::string("cudaStreamEndCapture (re-binning body): ") +
+                          cudaGetErrorString(e);
+                    return 2;
+                }
+                TSPH_CK(cudaStreamUpdateCaptureDependencies(st_, &cn, nullptr, 1,
+                                                            cudaStreamSetCaptureDependencies));
+            } else if ((rc = rebin_predicted(rebuild_, err))) {
                 return rc;
-            if ((rc = sort_finish(Fs_.r, Fs_.v, Fs_.rho, Fs_.id, nullptr, nullptr, nullptr, F_,
-                                  O_.r, O_.v, O_.rho, OldState<T>{Br_, Bv_, Brho_}, err, gate)))
-                return rc;
-            if ((rc = launch(CAT_SORT, k_copy_back<T>, blocks_for(nf_), kBlock, err,
-                             (const FluidState<T>)F_, (const double2 *)Br_, (const T2 *)Bv_,
-                             (const T *)Brho_, (const uint32_t *)fstart_, ncells_, Fs_, O_, gate)))
-                return rc;
+            }
         } else {
             // predictor + bin
             if ((rc = zero_counts(err))) return rc;
@@ -295,6 +341,7 @@ template <typename T> class Engine final : public EngineBase {
         }
         for (auto e : ev_pool_) cudaEventDestroy(e);
         for (void *p : allocs_) cudaFree(p);
+        if (st2_) cudaStreamDestroy(st2_);
         if (own_stream_ && st_) cudaStreamDestroy(st_);
     }
 
@@ -634,7 +681,9 @@ template <typename T> class Engine final : public EngineBase {
             if (it == graphs_.end()) {
                 cudaGraph_t g;
                 TSPH_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+                capturing_ = true;
                 rc = enqueue_step(model, (T)dt, err);
+                capturing_ = false;
                 cudaGraph_t g2 = nullptr;
                 cudaError_t e = cudaStreamEndCapture(st_, &g2);
                 if (rc) {

@@ -1006,13 +1006,15 @@ __global__ void k_predict_bin(FluidState<T> F, const uint32_t *__restrict__ fsta
 // those of the last binning), the old state to O.  The cells stay exact for
 // the pair set as long as every particle has moved less than `skin` per axis
 // since its binning (a pair within 2h then still lies inside the 3 x 3 cell
-// block, kh >= 2h + 2 skin); a larger move sets *rebuild, which runs the
-// gated re-binning before the pair pass.
+// block, kh >= 2h + 2 skin); a larger move sets *rebuild (and, inside a CUDA
+// graph, the conditional node `cond`), which runs the re-binning before the
+// pair pass.
 template <typename T>
 __global__ void k_predict_keep(FluidState<T> F, const uint32_t *__restrict__ fstart,
                                WallState<T> Wl, int nw, Grid g, T dt, FluidState<T> D,
                                OldState<T> O, float skin, uint32_t *__restrict__ rebuild,
-                               uint32_t *__restrict__ health) {
+                               uint32_t *__restrict__ health, cudaGraphConditionalHandle cond,
+                               int use_cond) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nw) {
         const T r = Wl.rho[i];
@@ -1041,7 +1043,10 @@ __global__ void k_predict_keep(FluidState<T> F, const uint32_t *__restrict__ fst
     D.loc[f] = make_float2(l.x + dx, l.y + dy);
     D.key[f] = F.key[f];
     D.id[f] = F.id[f];
-    if (!(fabsf(dx) <= skin && fabsf(dy) <= skin)) atomicOr(rebuild, 1u);
+    if (!(fabsf(dx) <= skin && fabsf(dy) <= skin)) {
+        atomicOr(rebuild, 1u);
+        if (use_cond) cudaGraphSetConditional(cond, 1u);
+    }
     if (!(nv.x == nv.x) || !(nv.y == nv.y) || !(dx == dx) || !(dy == dy))
         atomicOr(health, kHealthNan);
 }
