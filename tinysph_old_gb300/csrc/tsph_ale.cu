@@ -119,9 +119,13 @@ __global__ void k_ale_lf1(AleFluid F, const uint32_t *__restrict__ fstart, int n
 }
 
 // Integrate_LeapFrog_partTwo, src/RALESPH_integration.h:38-107, for target i:
-// returns the new position and writes the new conserved state to D[o]
+// returns the new position, the new conserved state goes to D[o].  STEP
+// (the fused step, out of place): the leap-frog copies and the derived rho, v
+// are not written (the sort derives rho, v from the conserved state; the
+// copies are dead until the next part one).
+template <bool STEP>
 __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int o, double dt,
-                                       int step, float rho0) {
+                                       int step, float rho0, float &s_out, float2 &v_out) {
     double2 r = F.r[i];
     // the reference's p was computed from the density the fluxes used
     const float s_flux = F.s[i];
@@ -131,19 +135,17 @@ __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int
     if (step == 1) {
         const double om0 = F.om[i], omr0 = F.omr[i];
         const double2 omv0 = F.omv[i];
-        D.om_o[o] = om0;
-        D.omr_o[o] = omr0;
-        D.omv_o[o] = omv0;
+        if (!STEP) {
+            D.om_o[o] = om0;
+            D.omr_o[o] = omr0;
+            D.omv_o[o] = omv0;
+        }
         const double h = dt * 0.5;
         om = om0 + (double)F.dom[i] * h;
         omr = omr0 + (double)F.domr[i] * h;
         omv = make_double2(omv0.x + (double)dv.x * h, omv0.y + (double)dv.y * h);
-        float s;
-        float2 v;
-        derive(om, omr, omv, rho0, s, v);
-        r = make_double2(r.x + (double)v.x * dt * 0.5, r.y + (double)v.y * dt * 0.5);
-        D.s[o] = s;
-        D.v[o] = v;
+        derive(om, omr, omv, rho0, s_out, v_out);
+        r = make_double2(r.x + (double)v_out.x * dt * 0.5, r.y + (double)v_out.y * dt * 0.5);
     } else {
         const float2 v0 = F.v[i];
         r = make_double2(r.x + (double)v0.x * dt, r.y + (double)v0.y * dt);
@@ -151,14 +153,16 @@ __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int
         omr = F.omr_o[i] + (double)F.domr[i] * dt;
         const double2 o2 = F.omv_o[i];
         omv = make_double2(o2.x + (double)dv.x * dt, o2.y + (double)dv.y * dt);
-        float s;
-        float2 v;
-        derive(om, omr, omv, rho0, s, v);
-        D.s[o] = s;
-        D.v[o] = v;
-        D.om_o[o] = F.om_o[i];
-        D.omr_o[o] = F.omr_o[i];
-        D.omv_o[o] = o2;
+        derive(om, omr, omv, rho0, s_out, v_out);
+        if (!STEP) {
+            D.om_o[o] = F.om_o[i];
+            D.omr_o[o] = F.omr_o[i];
+            D.omv_o[o] = o2;
+        }
+    }
+    if (!STEP) {
+        D.s[o] = s_out;
+        D.v[o] = v_out;
     }
     D.om[o] = om;
     D.omr[o] = omr;
@@ -177,7 +181,9 @@ __global__ void k_ale_lf2(AleFluid F, const uint32_t *__restrict__ fstart, int n
                           int step, float rho0) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_live_ale(fstart, ncells)) return;
-    lf2(F, i, F, i, dt, step, rho0);
+    float sn;
+    float2 vn;
+    lf2<false>(F, i, F, i, dt, step, rho0, sn, vn);
 }
 
 // part two out of place + RemoveParticlesOutOfDomain (src/SPH_btdebug.h:4-31)
@@ -188,9 +194,10 @@ __global__ void k_ale_lf2_bin(AleFluid F, const uint32_t *__restrict__ fstart, G
                               uint32_t *__restrict__ counts, uint32_t *__restrict__ health) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_live_ale(fstart, g.ncells)) return;
-    const double2 rn = lf2(F, i, D, i, dt, step, rho0);
-    const float2 v = D.v[i];
-    if (!(v.x == v.x) || !(v.y == v.y) || !(D.s[i] == D.s[i])) atomicOr(health, kHealthNan);
+    float sn;
+    float2 v;
+    const double2 rn = lf2<true>(F, i, D, i, dt, step, rho0, sn, v);
+    if (!(v.x == v.x) || !(v.y == v.y) || !(sn == sn)) atomicOr(health, kHealthNan);
     uint32_t k;
     if (out_of_domain(rn, box)) {
         k = (uint32_t)g.ncells;
@@ -220,12 +227,17 @@ __global__ void k_ale_bin(AleFluid F, const uint32_t *__restrict__ fstart, Grid 
     slot[i] = atomicAdd(counts + k, 1u);
 }
 
-// rank inside the cell by particle index and move the record (+ loc)
+// rank inside the cell by (y, particle index) and move the record (+ loc).
+// STEP: after the fused step's part two — the leap-frog copies stay behind
+// and rho - rho0, v are derived from the conserved state; otherwise (a plain
+// re-binning) every field moves as it is.
+template <bool STEP>
 __global__ void k_ale_rank_scatter(const uint32_t *__restrict__ key, const int *__restrict__ n_ptr,
                                    const uint32_t *__restrict__ start,
                                    const uint32_t *__restrict__ tmp_id,
-                                   const uint32_t *__restrict__ tmp_src, Grid g, AleFluid S,
-                                   AleFluid D) {
+                                   const uint32_t *__restrict__ tmp_src,
+                                   const long long *__restrict__ tmp_y, Grid g, AleFluid S,
+                                   AleFluid D, float rho0) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= *n_ptr) return;
     const uint32_t src = tmp_src[j];
@@ -234,8 +246,12 @@ __global__ void k_ale_rank_scatter(const uint32_t *__restrict__ key, const int *
     if (k != (uint32_t)g.ncells) {
         const uint32_t lo = start[k], hi = start[k + 1];
         const uint32_t me = tmp_id[j];
+        const long long my = tmp_y[j];
         uint32_t rank = 0;
-        for (uint32_t m = lo; m < hi; m++) rank += tmp_id[m] < me ? 1u : 0u;
+        for (uint32_t m = lo; m < hi; m++) {
+            const long long ym = tmp_y[m];
+            rank += (ym < my || (ym == my && tmp_id[m] < me)) ? 1u : 0u;
+        }
         f = lo + rank;
     }
     const double2 r = S.r[src];
@@ -246,18 +262,28 @@ __global__ void k_ale_rank_scatter(const uint32_t *__restrict__ key, const int *
         const int cx = (int)(k / (uint32_t)g.ncy), cy = (int)k - cx * g.ncy;
         D.loc[f] = cell_local(g, r, cx, cy);
     }
-    D.om[f] = S.om[src];
-    D.omr[f] = S.omr[src];
-    D.omv[f] = S.omv[src];
-    D.om_o[f] = S.om_o[src];
-    D.omr_o[f] = S.omr_o[src];
-    D.omv_o[f] = S.omv_o[src];
+    const double om = S.om[src], omr = S.omr[src];
+    const double2 omv = S.omv[src];
+    D.om[f] = om;
+    D.omr[f] = omr;
+    D.omv[f] = omv;
     D.dom[f] = S.dom[src];
     D.domr[f] = S.domr[src];
     D.domv[f] = S.domv[src];
-    D.s[f] = S.s[src];
-    D.v[f] = S.v[src];
     D.ps[f] = S.ps[src];
+    if (STEP) {
+        float sn;
+        float2 vn;
+        derive(om, omr, omv, rho0, sn, vn);
+        D.s[f] = sn;
+        D.v[f] = vn;
+    } else {
+        D.om_o[f] = S.om_o[src];
+        D.omr_o[f] = S.omr_o[src];
+        D.omv_o[f] = S.omv_o[src];
+        D.s[f] = S.s[src];
+        D.v[f] = S.v[src];
+    }
 }
 
 // neighbour at larger x (dx = x_a - x_b < 0) -> forward sums, smaller x ->
@@ -499,6 +525,307 @@ k_ale_flux(AleFluid F, const uint32_t *__restrict__ fstart, const uint32_t *__re
     }
 }
 
+
+// ---- the as-written flux loop as a shared-memory tiled gather (the layout
+// of the WCSPH pair kernel): a CTA takes 128 consecutive sorted fluid
+// particles, stages the 3 x (rows + 2) neighbour cells, builds each target's
+// in-support list, then evaluates the pairs.  Cells are sorted by y, so the
+// rows above and below stop once |dy| > 2h.
+constexpr int kAleT = 128;
+constexpr int kAleRows = 16;
+constexpr int kAleCap = 608;
+constexpr int kAleList = 36;
+
+struct AleTile {
+    float2 loc[kAleCap];
+    float4 q[kAleCap];  // fluid {vx, vy, rho - rho0, omega}; wall {-nx, -ny, rho - rho0, -1}
+    int foff[3][kAleRows + 3];
+    int woff[3][kAleRows + 3];
+    float2 off[9];
+    uint16_t list[kAleList * kAleT];
+};
+
+__device__ __forceinline__ float ale_rcp(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+struct AleAcc {
+    float dom, domr, dvx, dvy;
+    bool any;  // some neighbour with W > 0 (gamma_sum != 0)
+};
+
+// one as-written pair term (src/_testMUSCL_interaction.h:184-296 with
+// MUSCL_final's states: rho_L = rho_a, rho_R = rho_b, v_L = v_R = v_a . n)
+__device__ __forceinline__ void ale_pair(float dx, float dy, float2 va, float sa, float rhoa,
+                                         float4 qb, const AleConst &K, AleAcc &acc) {
+    const float r2 = fmaf(dx, dx, dy * dy);
+    const float inv_r = rsqrtf(r2);
+    const float r = r2 * inv_r;
+    const float w1 = fmaf(-0.5f * K.inv_h, r, 1.f);
+    const float w2 = w1 * w1;
+    const float W = K.awen * fmaf(2.f * K.inv_h, r, 1.f) * w2 * w2;
+    acc.any |= W > 0.f;
+    if (qb.w < 0.f) {
+        // BT wall: rho* = rho_a (1 + v_a . n_b / c0), pressure along n_b
+        const float vn = va.x * qb.x + va.y * qb.y;
+        const float ps = ale_eos(sa + rhoa * vn / K.c0, K);
+        const float wdp = W * K.dp;
+        acc.dvx = fmaf(-2.f * wdp * ps, qb.x, acc.dvx);
+        acc.dvy = fmaf(-2.f * wdp * ps, qb.y, acc.dvy);
+        acc.dom = fmaf(-vn, wdp, acc.dom);
+        return;
+    }
+    const float F = K.bwen_h * w2 * w1;
+    const float dWx = dx * F, dWy = dy * F;
+    const float sb = qb.z;
+    const float ob = qb.w;
+    const float nx = -dx * inv_r, ny = -dy * inv_r;
+    // v* = v_L n - (rho_R - rho_L) c0 / (2 rho_bar) n + mean tangential part;
+    // rho* = mean density (v_L = v_R)
+    const float k = -0.5f * (sb - sa) * K.c0 * ale_rcp(K.rho0 + 0.5f * (sa + sb));
+    const float ss = 0.5f * (sa + sb);
+    const float ps = ale_eos(ss, K);
+    const float rhos = K.rho0 + ss;
+    const float vsx = fmaf(nx, k, 0.5f * (va.x + qb.x));
+    const float vsy = fmaf(ny, k, 0.5f * (va.y + qb.y));
+    const float ex = vsx - va.x, ey = vsy - va.y;
+    const float t2 = 2.f * ob;
+    acc.dvx = fmaf(-t2, fmaf(fmaf(rhos * vsx, ex, ps), dWx, rhos * vsx * ey * dWy), acc.dvx);
+    acc.dvy = fmaf(-t2, fmaf(rhos * vsy * ex, dWx, fmaf(rhos * vsy, ey, ps) * dWy), acc.dvy);
+    acc.dom = fmaf(-ob, (va.x - qb.x) * dWx + (va.y - qb.y) * dWy, acc.dom);
+    acc.domr = fmaf(-t2 * rhos, ex * dWx + ey * dWy, acc.domr);
+}
+
+__global__ void __launch_bounds__(kAleT, 8)
+k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
+                 const uint32_t *__restrict__ wstart, AleWalls Wl, Grid g, AleConst K) {
+    __shared__ AleTile sm;
+    const int tid = threadIdx.x;
+    const int ncy = g.ncy;
+    const int nl = n_live_ale(fstart, g.ncells);
+    const int t0 = blockIdx.x * kAleT;
+    if (t0 >= nl) return;
+    const int t1 = min(t0 + kAleT, nl);
+    if (tid < 9) sm.off[tid] = make_float2((float)(1 - tid / 3) * g.khf, (float)(1 - tid % 3) * g.khf);
+    const uint32_t h2bits = __float_as_uint(K.four_h2);
+    const float reach = 2.f * K.h * 1.0001f;
+    int cur = t0;
+    int rows = kAleRows;
+    while (cur < t1) {
+        const uint32_t kc = __ldg(F.key + cur);
+        const int cx = (int)(kc / (uint32_t)ncy);
+        const int cy0 = (int)kc - cx * ncy;
+        const int rowlim = min(cy0 + rows, ncy);
+        const int we = min(t1, (int)__ldg(fstart + cx * ncy + rowlim));
+        const int cyl = (int)__ldg(F.key + we - 1) - cx * ncy;
+        const int rlo = max(cy0 - 1, 0), rhi = min(cyl + 1, ncy - 1);
+        const int nr = rhi - rlo + 1;
+        __syncthreads();
+        for (int e = tid; e < 3 * (nr + 1); e += kAleT) {
+            const int dxi = e / (nr + 1), q = e - dxi * (nr + 1);
+            const int col = cx + dxi - 1;
+            int fo = 0, wo = 0;
+            if (col >= 0 && col < g.ncx) {
+                const int c = col * ncy + rlo + q;
+                fo = (int)__ldg(fstart + c);
+                wo = (int)__ldg(wstart + c);
+            }
+            sm.foff[dxi][q] = fo;
+            sm.woff[dxi][q] = wo;
+        }
+        __syncthreads();
+        int fb[3], wb[3], f0[3], w0[3];
+        int tot = 0, totw = 0;
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+            w0[d] = sm.woff[d][0];
+            f0[d] = sm.foff[d][0];
+            wb[d] = tot;
+            tot += sm.woff[d][nr] - w0[d];
+            totw += sm.woff[d][nr] - w0[d];
+            fb[d] = tot;
+            tot += sm.foff[d][nr] - f0[d];
+        }
+        if (tot > kAleCap && rows > 1) {
+            rows = (rows + 1) >> 1;
+            continue;
+        }
+        const int i = cur + tid;
+        const bool active = i < we;
+        AleAcc acc = {0.f, 0.f, 0.f, 0.f, false};
+        bool done = false;
+        float2 va = make_float2(0.f, 0.f);
+        float sa = 0.f;
+        if (tot <= kAleCap) {
+#pragma unroll
+            for (int d = 0; d < 3; d++) {
+                const int nwd = sm.woff[d][nr] - w0[d];
+                for (int k = tid; k < nwd; k += kAleT) {
+                    const int j = w0[d] + k;
+                    const float2 n = __ldg(Wl.n + j);
+                    sm.loc[wb[d] + k] = __ldg(Wl.loc + j);
+                    sm.q[wb[d] + k] = make_float4(-n.x, -n.y, __ldg(Wl.s + j), -1.f);
+                }
+                const int nfd = sm.foff[d][nr] - f0[d];
+                for (int k = tid; k < nfd; k += kAleT) {
+                    const int j = f0[d] + k;
+                    const float2 v = __ldg(F.v + j);
+                    sm.loc[fb[d] + k] = __ldg(F.loc + j);
+                    sm.q[fb[d] + k] = make_float4(v.x, v.y, __ldg(F.s + j), (float)__ldg(F.om + j));
+                }
+            }
+            __syncthreads();
+            if (active) {
+                const int cy = (int)__ldg(F.key + i) - cx * ncy;
+                const int own = fb[1] + (i - f0[1]);
+                const float2 la = sm.loc[own];
+                const float4 qa = sm.q[own];
+                va = make_float2(qa.x, qa.y);
+                sa = qa.z;
+                const float rhoa = K.rho0 + sa;
+                int cnt = 0;
+                bool overflow = false;
+                uint16_t *lst = sm.list + tid;
+#pragma unroll
+                for (int dxi = 0; dxi < 3; dxi++) {
+                    const int col = cx + dxi - 1;
+                    if (col < 0 || col >= g.ncx) continue;
+#pragma unroll
+                    for (int dyi = 0; dyi < 3; dyi++) {
+                        const int row = cy + dyi - 1;
+                        if (row < 0 || row >= ncy) continue;
+                        const int q = row - rlo;
+                        const int code = dxi * 3 + dyi;
+                        const float bx = la.x + sm.off[code].x, by = la.y + sm.off[code].y;
+#pragma unroll
+                        for (int kind = 0; kind < 2; kind++) {
+                            if (kind == 0 && totw == 0) continue;
+                            const int j0 = kind == 0 ? wb[dxi] + sm.woff[dxi][q] - w0[dxi]
+                                                     : fb[dxi] + sm.foff[dxi][q] - f0[dxi];
+                            const int j1 = kind == 0 ? wb[dxi] + sm.woff[dxi][q + 1] - w0[dxi]
+                                                     : fb[dxi] + sm.foff[dxi][q + 1] - f0[dxi];
+                            if (cnt + (j1 - j0) > kAleList) {
+                                overflow = true;
+                                continue;
+                            }
+                            uint16_t *w = lst + cnt * kAleT;
+                            if (dyi == 1 || kind == 0) {
+                                uint32_t ent = ((uint32_t)j0 << 4) | (uint32_t)code;
+                                for (int j = j0; j < j1; j++, ent += 16u) {
+                                    const float2 lb = sm.loc[j];
+                                    const float dx = bx - lb.x, dy = by - lb.y;
+                                    const uint32_t in = (uint32_t)(__float_as_uint(fmaf(dx, dx, dy * dy)) - 1u) < h2bits ? 1u : 0u;
+                                    *w = (uint16_t)ent;
+                                    w += in * kAleT;
+                                }
+                            } else if (dyi == 2) {
+                                uint32_t ent = ((uint32_t)j0 << 4) | (uint32_t)code;
+                                for (int j = j0; j < j1; j++, ent += 16u) {
+                                    const float2 lb = sm.loc[j];
+                                    const float dx = bx - lb.x, dy = by - lb.y;
+                                    if (dy < -reach) break;
+                                    const uint32_t in = (uint32_t)(__float_as_uint(fmaf(dx, dx, dy * dy)) - 1u) < h2bits ? 1u : 0u;
+                                    *w = (uint16_t)ent;
+                                    w += in * kAleT;
+                                }
+                            } else {
+                                uint32_t ent = ((uint32_t)(j1 - 1) << 4) | (uint32_t)code;
+                                for (int j = j1 - 1; j >= j0; j--, ent -= 16u) {
+                                    const float2 lb = sm.loc[j];
+                                    const float dx = bx - lb.x, dy = by - lb.y;
+                                    if (dy > reach) break;
+                                    const uint32_t in = (uint32_t)(__float_as_uint(fmaf(dx, dx, dy * dy)) - 1u) < h2bits ? 1u : 0u;
+                                    *w = (uint16_t)ent;
+                                    w += in * kAleT;
+                                }
+                            }
+                            cnt = (int)((w - lst) / kAleT);
+                        }
+                    }
+                }
+                if (!overflow) {
+                    for (int k = 0; k < cnt; k++) {
+                        const uint32_t e = lst[k * kAleT];
+                        const int j = (int)(e >> 4);
+                        const float2 o = sm.off[e & 15u];
+                        const float2 lb = sm.loc[j];
+                        ale_pair((la.x + o.x) - lb.x, (la.y + o.y) - lb.y, va, sa, rhoa, sm.q[j], K,
+                                 acc);
+                    }
+                    done = true;
+                }
+            }
+        }
+        if (active && !done) {
+            // window too dense for shared memory, or list overflow: from global memory
+            const int cy = (int)__ldg(F.key + i) - cx * ncy;
+            const float2 la = __ldg(F.loc + i);
+            va = __ldg(F.v + i);
+            sa = __ldg(F.s + i);
+            const float rhoa = K.rho0 + sa;
+            acc = {0.f, 0.f, 0.f, 0.f, false};
+            for (int dxi = 0; dxi < 3; dxi++) {
+                const int col = cx + dxi - 1;
+                if (col < 0 || col >= g.ncx) continue;
+                for (int dyi = 0; dyi < 3; dyi++) {
+                    const int row = cy + dyi - 1;
+                    if (row < 0 || row >= ncy) continue;
+                    const int c = col * ncy + row;
+                    const float bx = la.x + (float)(1 - dxi) * g.khf,
+                                by = la.y + (float)(1 - dyi) * g.khf;
+                    for (int j = (int)__ldg(wstart + c); j < (int)__ldg(wstart + c + 1); j++) {
+                        const float2 lb = __ldg(Wl.loc + j);
+                        const float dx = bx - lb.x, dy = by - lb.y;
+                        const float r2 = fmaf(dx, dx, dy * dy);
+                        if (!(r2 <= K.four_h2) || r2 == 0.f) continue;
+                        const float2 n = __ldg(Wl.n + j);
+                        ale_pair(dx, dy, va, sa, rhoa, make_float4(-n.x, -n.y, __ldg(Wl.s + j), -1.f),
+                                 K, acc);
+                    }
+                    for (int j = (int)__ldg(fstart + c); j < (int)__ldg(fstart + c + 1); j++) {
+                        if (j == i) continue;
+                        const float2 lb = __ldg(F.loc + j);
+                        const float dx = bx - lb.x, dy = by - lb.y;
+                        const float r2 = fmaf(dx, dx, dy * dy);
+                        if (!(r2 <= K.four_h2) || r2 == 0.f) continue;
+                        const float2 vb = __ldg(F.v + j);
+                        ale_pair(dx, dy, va, sa, rhoa,
+                                 make_float4(vb.x, vb.y, __ldg(F.s + j), (float)__ldg(F.om + j)), K,
+                                 acc);
+                    }
+                }
+            }
+        }
+        if (active) {
+            const int cy = (int)__ldg(F.key + i) - cx * ncy;
+            bool zero = !acc.any;
+            if (zero) {
+                // gamma_sum is not reset between the particles of a cell
+                // (src/_testMUSCL_interaction.h:49, :299)
+                const uint32_t me = F.id[i];
+                const int c = cx * ncy + cy;
+                for (int j = (int)fstart[c]; j < (int)fstart[c + 1] && zero; j++)
+                    if (j != i && F.id[j] < me && ale_has_support(F, fstart, wstart, Wl, g, K, j))
+                        zero = false;
+            }
+            if (zero) {
+                F.dom[i] = 0.f;
+                F.domr[i] = 0.f;
+                F.domv[i] = make_float2(0.f, 0.f);
+            } else {
+                const float ao = (float)F.om[i];
+                F.dom[i] = acc.dom * ao;
+                F.domr[i] = acc.domr * ao;
+                F.domv[i] = make_float2(acc.dvx * ao, acc.dvy * ao - K.g * ao * (K.rho0 + sa));
+            }
+        }
+        cur = we;
+        rows = kAleRows;
+    }
+}
+
 #define ACK(call)                                                                 \
     do {                                                                          \
         cudaError_t e_ = (call);                                                  \
@@ -508,7 +835,7 @@ k_ale_flux(AleFluid F, const uint32_t *__restrict__ fstart, const uint32_t *__re
         }                                                                         \
     } while (0)
 
-inline int nblk(long long n) { return (int)std::max<long long>(1, (n + kBlock - 1) / kBlock); }
+inline int nblk(long long n, int b = kBlock) { return (int)std::max<long long>(1, (n + b - 1) / b); }
 
 }  // namespace
 
@@ -537,7 +864,11 @@ class AleEngine {
     AleConst K{};
     uint32_t *fstart = nullptr, *wstart = nullptr, *counts = nullptr, *tiles = nullptr;
     uint32_t *keyB = nullptr, *slotB = nullptr, *tmp_id = nullptr, *tmp_src = nullptr;
+    long long *tmp_y = nullptr;
     uint32_t *health = nullptr;
+    // the leap-frog copies (omega_o, ...) hold part one's values: false after
+    // a fused step (its re-binning leaves them behind)
+    bool copies_valid = true;
     float *grad = nullptr;
     long long *dbx = nullptr, *dby = nullptr;
     double *dox = nullptr, *doy = nullptr;
@@ -611,6 +942,7 @@ class AleEngine {
             (rc = alloc(&tiles, (ncells + 1 + kScanTile - 1) / kScanTile, err)) ||
             (rc = alloc(&keyB, nf, err)) || (rc = alloc(&slotB, nf, err)) ||
             (rc = alloc(&tmp_id, nf, err)) || (rc = alloc(&tmp_src, nf, err)) ||
+            (rc = alloc(&tmp_y, nf, err)) ||
             (rc = alloc(&health, 1, err)) || (rc = alloc(&dbx, bx.size(), err)) ||
             (rc = alloc(&dby, by.size(), err)) || (rc = alloc(&dox, ox.size(), err)) ||
             (rc = alloc(&doy, oy.size(), err)))
@@ -723,23 +1055,27 @@ class AleEngine {
     }
 
     // counting sort of X (keys in keyB/slotB, histogram in counts) into Y
-    int sort(AleFluid X, AleFluid Y, std::string &err) {
+    int sort(AleFluid X, AleFluid Y, bool step_sort, std::string &err) {
         const int n = ncells + 1;
         const int nt = (n + kScanTile - 1) / kScanTile;
         k_scan_tiles_clear<<<nt, kScanThreads, 0, st>>>(counts, fstart, tiles, n, nullptr);
         k_scan_add_tiles<<<nblk(n), kBlock, 0, st>>>(fstart, tiles, nt, n, nullptr);
         const int *ntot_ = reinterpret_cast<const int *>(fstart + ncells + 1);
         k_place<<<nblk(nf), kBlock, 0, st>>>(keyB, slotB, X.id, ntot_, fstart, tmp_id, tmp_src,
-                                             nullptr, nullptr, nullptr);
-        k_ale_rank_scatter<<<nblk(nf), kBlock, 0, st>>>(keyB, ntot_, fstart, tmp_id, tmp_src, grid,
-                                                        X, Y);
+                                             X.r, tmp_y, nullptr);
+        if (step_sort)
+            k_ale_rank_scatter<true><<<nblk(nf), kBlock, 0, st>>>(keyB, ntot_, fstart, tmp_id, tmp_src,
+                                                                  tmp_y, grid, X, Y, (float)rho0);
+        else
+            k_ale_rank_scatter<false><<<nblk(nf), kBlock, 0, st>>>(
+                keyB, ntot_, fstart, tmp_id, tmp_src, tmp_y, grid, X, Y, (float)rho0);
         ACK(cudaGetLastError());
         return 0;
     }
 
     int particle_to_cell(std::string &err) {
         k_ale_bin<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, keyB, slotB, counts, health);
-        int rc = sort(A, B, err);
+        int rc = sort(A, B, false, err);
         if (rc) return rc;
         std::swap(A, B);
         cells = true;
@@ -756,7 +1092,7 @@ class AleEngine {
         if (scheme == TSPH_ALE_MUSCL)
             k_ale_flux<1><<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
         else
-            k_ale_flux<0><<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
+            k_ale_flux_tiled<<<nblk(nf, kAleT), kAleT, 0, st>>>(A, fstart, wstart, W, grid, K);
         ACK(cudaGetLastError());
         return 0;
     }
@@ -764,10 +1100,15 @@ class AleEngine {
     int lf1(double dt, std::string &err) {
         k_ale_lf1<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, dt, (float)rho0);
         ACK(cudaGetLastError());
+        copies_valid = true;
         return 0;
     }
 
     int lf2(double dt, int step, std::string &err) {
+        if (step != 1 && !copies_valid) {
+            err = "Integrate_LeapFrog_partTwo (step > 1) needs part one of the same step first";
+            return TSPH_ERR_STATE;
+        }
         k_ale_lf2<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, dt, step, (float)rho0);
         ACK(cudaGetLastError());
         cells = false;
@@ -784,10 +1125,11 @@ class AleEngine {
             if ((rc = forces(err))) return rc;
             k_ale_lf2_bin<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, dt, stp, (float)rho0, box,
                                                        B, keyB, slotB, counts, health);
-            if ((rc = sort(B, A, err))) return rc;
+            if ((rc = sort(B, A, true, err))) return rc;
         }
         ACK(cudaGetLastError());
         cells = true;
+        if (nsteps > 0) copies_valid = false;
         return 0;
     }
 
