@@ -37,9 +37,10 @@ STEP_BYTES_PER_PARTICLE = 344.0  # algorithmic bytes per particle-step (byte mod
 METRIC = "particle-steps/s, 720k dam break, 1 GB300: surrogate/batched vs plain, <=1% front err"
 # ALE-SPH byte model per fluid particle: flux pass reads loc, key, v, rho - rho0,
 # omega (32 B) and writes the three rates (16 B); whole step (leap-frog one
-# 124 B, fluxes 48 B, leap-frog two + binning 208 B, counting sort 276 B)
+# 124 B, fluxes 48 B, leap-frog two + binning 164 B, placement 36 B,
+# rank + scatter 188 B, scan 15 B)
 ALE_FLUX_BYTES_PER_PARTICLE = 48.0
-ALE_STEP_BYTES_PER_PARTICLE = 656.0
+ALE_STEP_BYTES_PER_PARTICLE = 575.0
 ALE_METRIC = "particle-steps/s, ALE-SPH dam break dp=0.0004 (1.1M fluid), 1 GB300"
 
 

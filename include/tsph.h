@@ -213,6 +213,24 @@ int tsph_health(tsph_system *s, uint32_t *flags, int clear);
  * driver calls), and momentum. out[0..3] = mass, ekin, px, py. */
 int tsph_fluid_totals(tsph_system *s, double out[4]);
 
+/* ---- probes of the case drivers (cases/damBreakLong_mDBC/
+ * SPH_simulationSymplectic.h:156-199), on the current state and cells.
+ * Water_Elevation / Water_Elevation_inverse (src/SPH_water_level.h:84-150)
+ * at n gauges: from (x[k], y0[k]) upwards (inverse[k] = 0) or downwards
+ * (inverse[k] = 1; inverse may be NULL) with the reference's growing sampling
+ * step dp * 5e-5 * i, to the first height where the kernel volume sum m W /
+ * rho drops to (rises to) 0.5; out[k] = that level, NaN if never reached. */
+int tsph_water_level(tsph_system *s, int n, const double *x, const double *y0,
+                     const int32_t *inverse, double *out);
+/* Kernel_velocity_approximation_TEST (src/testing.h:6-149) at n points
+ * xy[2k], xy[2k+1]: out[4k..4k+3] = Shepard {rho, p, vx, vy} (0 where the
+ * kernel volume is <= 0.5); Pressure_in_point (src/SPH_measure_pressure.h:6-15)
+ * is out[4k+1]. */
+int tsph_point_fields(tsph_system *s, int n, const double *xy, double *out);
+/* water front: the largest x of the live fluid with y <= y_max (NaN if
+ * none).  No counterpart in the reference, which records no front. */
+int tsph_water_front(tsph_system *s, double y_max, double *x_front);
+
 /* Kernel timing of the system's calls, for the roofline report.  With
  * profiling on, tsph_step runs its kernels eagerly (no graph) with CUDA events
  * around every launch on the system's stream; tsph_profile returns the sums

@@ -96,6 +96,9 @@ def _load_port():
         L.orc_remove_out_of_domain.restype = _I
         L.orc_step.argtypes = [_P, _I, _D, _I]
         L.orc_pair_digest.argtypes = [_P, _IP, np.ctypeslib.ndpointer(dtype=np.int64, flags='C_CONTIGUOUS'), _IP]
+        L.orc_water_level.argtypes = [_P, _D, _D, _I]
+        L.orc_water_level.restype = _D
+        L.orc_point_fields.argtypes = [_P, _D, _D, _DP]
         L.orc_wendland.argtypes = [_D, _D, C.POINTER(_D), C.POINTER(_D)]
         L.orc_pressure.argtypes = [_D, _D, _D]
         L.orc_pressure.restype = _D
@@ -150,6 +153,11 @@ def _load_ref():
         L.ref_predictor.argtypes = [_P, _D]
         L.ref_corrector.argtypes = [_P, _D]
         L.ref_step.argtypes = [_P, _I, _D, _I]
+        L.ref_water_level.argtypes = [_P, _D, _D, _I]
+        L.ref_water_level.restype = _D
+        L.ref_point_fields.argtypes = [_P, _D, _D, _DP]
+        L.ref_pressure_in_point.argtypes = [_P, _D, _D]
+        L.ref_pressure_in_point.restype = _D
         L.ref_wendland.argtypes = [_D, _D, C.POINTER(_D), C.POINTER(_D)]
         _ref = L
     return _ref
@@ -256,6 +264,14 @@ class PortSystem(_Base):
         if n < 0:
             raise RuntimeError("cells not built")
         return start, lst[:n]
+
+    def water_level(self, x, y0, inverse=False):
+        return self.L.orc_water_level(self.s, float(x), float(y0), 1 if inverse else 0)
+
+    def point_fields(self, x, y):
+        out = np.zeros(4)
+        self.L.orc_point_fields(self.s, float(x), float(y), out)
+        return out
 
     def pair_digest(self):
         n = self.np()
@@ -393,6 +409,17 @@ class RefSystem(_Base):
 
     def step(self, model, dt, n=1):
         self.L.ref_step(self.s, int(model), dt, int(n))
+
+    def water_level(self, x, y0, inverse=False):
+        return self.L.ref_water_level(self.s, float(x), float(y0), 1 if inverse else 0)
+
+    def point_fields(self, x, y):
+        out = np.zeros(4)
+        self.L.ref_point_fields(self.s, float(x), float(y), out)
+        return out
+
+    def pressure_in_point(self, x, y):
+        return self.L.ref_pressure_in_point(self.s, float(x), float(y))
 
 
 def ref_wendland(r, h):

@@ -26,6 +26,8 @@
 #include "SPH_mDBC.h"
 #include "SPH_btdebug.h"
 #include "SPH_create.h"
+#include "SPH_water_level.h"
+#include "SPH_measure_pressure.h"
 
 #include <iostream>
 #include <sstream>
@@ -243,4 +245,23 @@ void ref_step(void *c, int model, double dt, int nsteps) {
     }
 }
 
+
+// probes of the case drivers (cases/damBreakLong_mDBC/SPH_simulationSymplectic.h:156-199)
+double ref_water_level(void *c, double x, double y0, int inverse) {
+    RefCase *rc = static_cast<RefCase *>(c);
+    Quiet q;
+    return inverse ? Water_Elevation_inverse(rc->particles, rc->sim, x, y0)
+                   : Water_Elevation(rc->particles, rc->sim, x, y0);
+}
+
+void ref_point_fields(void *c, double x, double y, double *out4) {
+    RefCase *rc = static_cast<RefCase *>(c);
+    const std::array<real, 4> f = Kernel_velocity_approximation_TEST(rc->particles, rc->sim, {x, y});
+    for (int k = 0; k < 4; k++) out4[k] = f[k];
+}
+
+double ref_pressure_in_point(void *c, double x, double y) {
+    RefCase *rc = static_cast<RefCase *>(c);
+    return Pressure_in_point(rc->particles, rc->sim, {x, y});
+}
 }  // extern "C"

@@ -74,6 +74,11 @@ void orc_step(orc_sys *s, int model, double dt, int nsteps);
 void orc_pair_digest(const orc_sys *s, int *count, long long *sum, int *xr);
 
 /* ---- ALE-SPH (cases/ALESPH_dambreakLong/MUSCL.h path) ---- */
+/* probes of the case drivers: water level (src/SPH_water_level.h:84-150) and
+ * Shepard point fields {rho, p, vx, vy} (src/testing.h:6-149) */
+double orc_water_level(orc_sys *s, double x, double y0, int inverse);
+void orc_point_fields(orc_sys *s, double x, double y, double out[4]);
+
 void orc_ale_add_particle(orc_sys *s, int type, double p, double rho, double rx, double ry,
                           double vx, double vy);
 void orc_ale_add_normal(orc_sys *s, double nx, double ny);

@@ -3,8 +3,8 @@
 Runs the reference's own code (oracle/_ref/libtsph_ref.so, compiled from the
 reference headers by ``make -C oracle ref``) on small seeded cases and stores
 its outputs.  Needs the reference sources; the committed .npz files are what
-the tests read.  Usage: python tests/golden/make_golden.py [ale]  (``ale``
-regenerates only the ALE-SPH fixture, from oracle/_ref/libtsph_ref_ale.so)
+the tests read.  Usage: python tests/golden/make_golden.py [ale|probes]  (``ale`` /
+``probes`` regenerate only the ALE-SPH or the probe fixture)
 """
 
 import os
@@ -189,9 +189,38 @@ def main_ale():
     np.savez_compressed(os.path.join(HERE, "dam_break_ale_dp0.02.npz"), **out)
 
 
+WL_GAUGES = [(0.3, 0.0, 0), (0.3, 0.45, 1), (0.865, 0.0, 0), (0.865, 0.45, 1),
+             (1.114, 0.0, 0), (1.114, 0.45, 1), (1.3625, 0.0, 0), (1.3625, 0.45, 1)]
+PT_PROBES = [(1.61, 0.003), (1.61, 0.015), (1.61, 0.03), (1.61, 0.08), (0.3, 0.1), (0.2, 0.25),
+             (0.55, 0.05), (0.7, 0.02), (0.05, 0.29), (1.0, 0.5)]
+
+
+def main_probes():
+    """Probes of cases/damBreakLong_mDBC (water levels h1-h4 and their inverse
+    gauges, constants.h:57-80; pressure sensors p1-p4, :84-94, plus interior
+    points) on the reference's state after 20 steps at dp = 0.01."""
+    if O.build_ref() is None or not O.ref_available():
+        raise SystemExit("reference harness not available (needs the reference sources)")
+    case = cases.dam_break_mdbc(dp=0.01)
+    R = O.RefSystem.from_case(case)
+    R.set_threads(1)
+    R.step(0, case.dt, 20)
+    st = R.state()
+    out = {k: st[k] for k in ("r", "v", "rho", "p", "type", "index")}
+    out["gauges"] = np.array(WL_GAUGES, dtype=np.float64)
+    out["water_level"] = np.array([R.water_level(x, y0, bool(inv)) for x, y0, inv in WL_GAUGES])
+    out["points"] = np.array(PT_PROBES, dtype=np.float64)
+    out["point_fields"] = np.array([R.point_fields(x, y) for x, y in PT_PROBES])
+    out["pressure_in_point"] = np.array([R.pressure_in_point(x, y) for x, y in PT_PROBES])
+    np.savez_compressed(os.path.join(HERE, "probes_dam_break_dp0.01.npz"), **out)
+
+
 def main():
     if len(sys.argv) > 1 and sys.argv[1] == "ale":
         main_ale()
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "probes":
+        main_probes()
         return
     if O.build_ref() is None or not O.ref_available():
         raise SystemExit("reference harness not available (needs the reference sources)")
@@ -214,6 +243,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "wendland.npz"), samples=wendland_samples())
     # 5. Riemann / ALE-SPH dam break, 6 steps
     main_ale()
+    # 6. probes (water level, point fields)
+    main_probes()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

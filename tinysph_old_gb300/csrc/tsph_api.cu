@@ -428,6 +428,33 @@ int tsph_fluid_totals(tsph_system *s, double out[4]) {
     return TSPH_OK;
 }
 
+int tsph_water_level(tsph_system *s, int n, const double *x, const double *y0,
+                     const int32_t *inverse, double *out) {
+    NEED(s);
+    if (n < 0 || (n > 0 && (!x || !y0 || !out))) return fail(TSPH_ERR_ARG, "bad arguments");
+    if (n == 0) return TSPH_OK;
+    ENGINE(s);
+    RUN(s->eng->water_level(n, x, y0, inverse, out, err_));
+    return TSPH_OK;
+}
+
+int tsph_point_fields(tsph_system *s, int n, const double *xy, double *out) {
+    NEED(s);
+    if (n < 0 || (n > 0 && (!xy || !out))) return fail(TSPH_ERR_ARG, "bad arguments");
+    if (n == 0) return TSPH_OK;
+    ENGINE(s);
+    RUN(s->eng->point_fields(n, xy, out, err_));
+    return TSPH_OK;
+}
+
+int tsph_water_front(tsph_system *s, double y_max, double *x_front) {
+    NEED(s);
+    if (!x_front) return fail(TSPH_ERR_ARG, "null output");
+    ENGINE(s);
+    RUN(s->eng->water_front(y_max, x_front, err_));
+    return TSPH_OK;
+}
+
 int tsph_set_profiling(tsph_system *s, int on) {
     NEED(s);
     s->profiling = on != 0;

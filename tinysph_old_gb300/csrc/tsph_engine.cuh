@@ -12,6 +12,8 @@
 #include "tsph_engine.h"
 #include "tsph_kernels.cuh"
 #include "tsph_pairs_tiled.cuh"
+#include "tsph_probes.cuh"
+#include "tsph_grid_host.h"
 
 namespace tsph {
 
@@ -40,7 +42,10 @@ template <typename T> class Engine final : public EngineBase {
     cudaStream_t st_ = nullptr;
     bool own_stream_ = false;
     bool cells_ = false;
-    double m64_ = 0;
+    double m64_ = 0, dp64_ = 0;
+    // probe scratch (grown on demand)
+    double *pr_d_ = nullptr;
+    size_t pr_cap_ = 0;
 
     // ---- device memory (one arena per kind; freed in the destructor)
     std::vector<void *> allocs_;
@@ -341,6 +346,7 @@ template <typename T> class Engine final : public EngineBase {
         }
         for (auto e : ev_pool_) cudaEventDestroy(e);
         for (void *p : allocs_) cudaFree(p);
+        if (pr_d_) cudaFree(pr_d_);
         if (st2_) cudaStreamDestroy(st2_);
         if (own_stream_ && st_) cudaStreamDestroy(st_);
     }
@@ -362,6 +368,7 @@ template <typename T> class Engine final : public EngineBase {
         nw_ = (int)wl.size();
         // constants
         m64_ = hs.m;
+        dp64_ = hs.dp;
         P_.hd = hs.h;
         P_.h = (T)hs.h;
         P_.inv_h = (T)(1.0 / hs.h);
@@ -922,6 +929,117 @@ template <typename T> class Engine final : public EngineBase {
         for (int q = 0; q < 4; q++) out[q] = 0;
         for (int b = 0; b < nb; b++)
             for (int q = 0; q < 4; q++) out[q] += h[(size_t)b * 4 + q];
+        return collect_profile(err);
+    }
+
+    ProbeSrc<T> probe_src() const {
+        constexpr bool shifted = std::is_same<T, float>::value;
+        return ProbeSrc<T>{F_.r, F_.v, F_.rho, F_.p, W_.r, W_.rho, W_.p,
+                           (const uint32_t *)fstart_, (const uint32_t *)wstart_, grid_, P_.hd,
+                           (double)P_.awen, (double)P_.bwen, m64_, shifted ? (double)P_.rho0 : 0.0};
+    }
+
+    // device scratch for the probes, `bytes` at least
+    int probe_scratch(size_t bytes, std::string &err) {
+        if (bytes <= pr_cap_) return 0;
+        if (pr_d_) cudaFree(pr_d_);
+        pr_d_ = nullptr;
+        pr_cap_ = 0;
+        TSPH_CK(cudaMalloc(&pr_d_, bytes));
+        pr_cap_ = bytes;
+        return 0;
+    }
+
+    int water_level(int n, const double *x, const double *y0, const int32_t *inverse, double *out,
+                    std::string &err) override {
+        if (!cells_) {
+            err = "cell lists are stale: call tsph_particle_to_cell first";
+            return 3;
+        }
+        // the sample heights of each gauge, accumulated as the reference does
+        // (ar.y += i dp_wl, src/SPH_water_level.h:96-101); past the grid the
+        // kernel volume is 0, so the sequence ends there
+        const double dp_wl = dp64_ * 0.00005;
+        const int nmax = (int)(box_.ym / dp_wl);
+        const double top = box_.ym + 2.0 * (double)P_.kh, bot = box_.y0 - 2.0 * (double)P_.kh;
+        std::vector<double> ys;
+        std::vector<int> off(n + 1, 0), inv(n);
+        for (int g = 0; g < n; g++) {
+            off[g] = (int)ys.size();
+            inv[g] = inverse && inverse[g] ? 1 : 0;
+            double ay = y0[g];
+            for (int i = 0; i < nmax; i++) {
+                if (inv[g]) ay -= i * dp_wl;
+                else ay += i * dp_wl;
+                ys.push_back(ay);
+                if (inv[g] ? ay < bot : ay > top) break;
+            }
+        }
+        off[n] = (int)ys.size();
+        const size_t nb = 8 * ys.size() + 8 * (size_t)n + 4 * (size_t)(n + 1) + 4 * (size_t)n * 2 + 64;
+        int rc;
+        if ((rc = probe_scratch(nb, err))) return rc;
+        double *d_ys = pr_d_;
+        double *d_x = d_ys + ys.size();
+        int *d_off = reinterpret_cast<int *>(d_x + n);
+        int *d_inv = d_off + n + 1;
+        int *d_first = d_inv + n;
+        TSPH_CK(cudaMemcpyAsync(d_ys, ys.data(), 8 * ys.size(), cudaMemcpyHostToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(d_x, x, 8 * (size_t)n, cudaMemcpyHostToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(d_off, off.data(), 4 * (size_t)(n + 1), cudaMemcpyHostToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(d_inv, inv.data(), 4 * (size_t)n, cudaMemcpyHostToDevice, st_));
+        int most = 1;
+        for (int g = 0; g < n; g++) most = std::max(most, off[g + 1] - off[g]);
+        TSPH_CK(cudaMemsetAsync(d_first, 0x7f, 4 * (size_t)n, st_));
+        const dim3 wl_grid((unsigned)n, (unsigned)((most + kWlChunk - 1) / kWlChunk));
+        k_water_level<T><<<wl_grid, 256, 0, st_>>>(probe_src(), (const double *)d_x,
+                                                   (const int *)d_inv, (const double *)d_ys,
+                                                   (const int *)d_off, d_first);
+        TSPH_CK(cudaGetLastError());
+        std::vector<int> first(n);
+        TSPH_CK(cudaMemcpyAsync(first.data(), d_first, 4 * (size_t)n, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        for (int g = 0; g < n; g++) {
+            const int i = first[g];
+            if (i < 0 || i >= off[g + 1] - off[g]) {
+                out[g] = std::nan("");
+                continue;
+            }
+            const double ay = ys[(size_t)off[g] + i];
+            out[g] = inv[g] ? ay + i * dp_wl : ay - i * dp_wl;
+        }
+        return collect_profile(err);
+    }
+
+    int point_fields(int n, const double *xy, double *out, std::string &err) override {
+        if (!cells_) {
+            err = "cell lists are stale: call tsph_particle_to_cell first";
+            return 3;
+        }
+        int rc;
+        if ((rc = probe_scratch(8 * 6 * (size_t)n + 64, err))) return rc;
+        double *d_xy = pr_d_, *d_out = pr_d_ + 2 * (size_t)n;
+        TSPH_CK(cudaMemcpyAsync(d_xy, xy, 16 * (size_t)n, cudaMemcpyHostToDevice, st_));
+        if ((rc = launch(CAT_OTHER, k_point_fields<T>, (int)(((long long)n * 32 + 255) / 256), 256,
+                         err, probe_src(), (const double *)d_xy, n, d_out)))
+            return rc;
+        TSPH_CK(cudaMemcpyAsync(out, d_out, 32 * (size_t)n, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        return collect_profile(err);
+    }
+
+    int water_front(double y_max, double *x, std::string &err) override {
+        int rc;
+        if ((rc = probe_scratch(64, err))) return rc;
+        unsigned long long *d_best = reinterpret_cast<unsigned long long *>(pr_d_);
+        TSPH_CK(cudaMemsetAsync(d_best, 0, 8, st_));
+        if ((rc = launch(CAT_OTHER, k_water_front, blocks_for(nf_), kBlock, err, (const double2 *)F_.r,
+                         (const uint32_t *)fstart_, ncells_, y_max, d_best)))
+            return rc;
+        unsigned long long best = 0;
+        TSPH_CK(cudaMemcpyAsync(&best, d_best, 8, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        *x = best ? from_ordered((long long)(best ^ 0x8000000000000000ULL)) : std::nan("");
         return collect_profile(err);
     }
 

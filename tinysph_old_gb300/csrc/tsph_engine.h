@@ -58,6 +58,10 @@ class EngineBase {
     virtual int np_live(int *np, std::string &err) = 0;
     virtual int health(uint32_t *flags, int clear, std::string &err) = 0;
     virtual int totals(double out[4], std::string &err) = 0;
+    virtual int water_level(int n, const double *x, const double *y0, const int32_t *inverse,
+                            double *out, std::string &err) = 0;
+    virtual int point_fields(int n, const double *xy, double *out, std::string &err) = 0;
+    virtual int water_front(double y_max, double *x, std::string &err) = 0;
     virtual int sync(std::string &err) = 0;
     virtual void set_profiling(bool on) = 0;
     virtual Profile profile(bool reset) = 0;

@@ -36,6 +36,7 @@ ABI_SYMBOLS = (
     "tsph_compute_forces", "tsph_symplectic_predictor", "tsph_symplectic_corrector",
     "tsph_remove_out_of_domain", "tsph_step", "tsph_download", "tsph_upload", "tsph_sync",
     "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
+    "tsph_water_level", "tsph_point_fields", "tsph_water_front",
     "tsph_ale_create", "tsph_ale_destroy", "tsph_ale_add_particles", "tsph_ale_set_scheme",
     "tsph_ale_np", "tsph_ale_divide_to_cells", "tsph_ale_particle_to_cell", "tsph_ale_gradient",
     "tsph_ale_forces", "tsph_ale_leapfrog_one", "tsph_ale_leapfrog_two", "tsph_ale_step",
@@ -131,6 +132,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_fluid_totals.argtypes = [P, P]
     L.tsph_set_profiling.argtypes = [P, I]
     L.tsph_get_profile.argtypes = [P, C.POINTER(_Profile), I]
+    L.tsph_water_level.argtypes = [P, I, P, P, P, P]
+    L.tsph_point_fields.argtypes = [P, I, P, P]
+    L.tsph_water_front.argtypes = [P, D, C.POINTER(D)]
     L.tsph_ale_create.argtypes = [C.POINTER(_Constants), C.POINTER(_Domain), P, C.POINTER(P)]
     for f in ("tsph_ale_destroy", "tsph_ale_divide_to_cells", "tsph_ale_particle_to_cell",
               "tsph_ale_gradient", "tsph_ale_sync"):
@@ -367,6 +371,30 @@ class ParticleSystem:
         _check(self._L.tsph_fluid_totals(self._h, _p(out)))
         return dict(mass=out[0], ekin=out[1], px=out[2], py=out[3])
 
+    # ---- probes (src/SPH_water_level.h, src/testing.h)
+    def water_level(self, x, y0, inverse=None):
+        """Water_Elevation (inverse=False) / Water_Elevation_inverse at gauges."""
+        x = np.ascontiguousarray(np.atleast_1d(x), dtype=np.float64)
+        y0 = np.ascontiguousarray(np.broadcast_to(y0, x.shape), dtype=np.float64)
+        inv = None
+        if inverse is not None:
+            inv = np.ascontiguousarray(np.broadcast_to(inverse, x.shape), dtype=np.int32)
+        out = np.empty(len(x))
+        _check(self._L.tsph_water_level(self._h, len(x), _p(x), _p(y0), _p(inv), _p(out)))
+        return out
+
+    def point_fields(self, xy):
+        """Shepard {rho, p, vx, vy} at points (n, 2); Pressure_in_point = [:, 1]."""
+        xy = np.ascontiguousarray(np.asarray(xy, dtype=np.float64).reshape(-1, 2))
+        out = np.empty((len(xy), 4))
+        _check(self._L.tsph_point_fields(self._h, len(xy), _p(xy), _p(out)))
+        return out
+
+    def water_front(self, y_max):
+        x = C.c_double()
+        _check(self._L.tsph_water_front(self._h, float(y_max), C.byref(x)))
+        return x.value
+
     def set_profiling(self, on: bool):
         _check(self._L.tsph_set_profiling(self._h, 1 if on else 0))
 
@@ -411,6 +439,18 @@ def Integrate_SymplecticCorrector(particles: ParticleSystem, dt):
 
 def RemoveParticlesOutOfDomain(particles: ParticleSystem, simulation_data=None) -> int:
     return particles.remove_out_of_domain()
+
+
+def Water_Elevation(particles: ParticleSystem, simulation_data, x, y0) -> float:
+    return float(particles.water_level(x, y0, 0)[0])
+
+
+def Water_Elevation_inverse(particles: ParticleSystem, simulation_data, x, y0) -> float:
+    return float(particles.water_level(x, y0, 1)[0])
+
+
+def Pressure_in_point(particles: ParticleSystem, simulation_data, ar) -> float:
+    return float(particles.point_fields([ar])[0, 1])
 
 
 class AleSystem:
