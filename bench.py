@@ -323,6 +323,163 @@ def run_ale(args, rank, world, local):
         dist.destroy_process_group()
 
 
+BATCH_METRIC = "particle-steps/s, 512 seeded dam-break/still-water cases (2k-100k particles), 1 GB300"
+
+
+def run_batch(args, rank, world, local):
+    """Batched workload: 512 seeded cases packed into one system per group of
+    equal constants, one step = one time step of every case; next to it the
+    same cases stepped one system at a time (the plain path looped per case)."""
+    import numpy as np
+    import torch
+
+    from tinysph_old_gb300 import batch as B
+    from tinysph_old_gb300 import sph
+
+    torch.cuda.set_device(local)
+    specs = B.sample_specs(args.cases, seed=args.seed)
+    bt = B.Batch(specs)
+    n = bt.np
+    for _ in range(args.warmup):
+        bt.step(1)
+    bt.sync()
+    torch.cuda.synchronize()
+    streams = bt._streams
+    main = torch.cuda.current_stream()
+    t_start = torch.cuda.Event(enable_timing=True)
+    ends = [torch.cuda.Event(enable_timing=True) for _ in streams]
+    with ClockSampler(local) as clocks:
+        t_start.record(main)
+        for st in streams:
+            st.wait_event(t_start)
+        bt.step(args.steps)
+        for st, e in zip(streams, ends):
+            e.record(st)
+        torch.cuda.synchronize()
+    ms = max(t_start.elapsed_time(e) for e in ends)
+    value = n * args.steps / (ms / 1000.0)
+    # per group: step time alone (for the projection to 0.5 s of every case)
+    group_ms = []
+    for g, st in zip(bt.groups, streams):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        g.system.step(g.wall_model, g.dt, 5)
+        e1.record(st)
+        torch.cuda.synchronize()
+        group_ms.append(e0.elapsed_time(e1) / 5)
+    t_half = sum(round(0.5 / g.dt) * m for g, m in zip(bt.groups, group_ms)) / 1000.0
+    # pair-kernel roofline on the largest group (eager launches with events)
+    big = max(bt.groups, key=lambda g: g.np)
+    big.system.set_profiling(True)
+    big.system.profile(reset=True)
+    big.system.step(big.wall_model, big.dt, 3)
+    prof = big.system.profile(reset=True)
+    big.system.set_profiling(False)
+    pair_us = prof["pair_us"] / max(prof["pair_launches"], 1)
+    nfl_big = sum(int(np.sum(c.type == 0)) for c in big.cases)
+    peak, peak_kind = measured_peaks()
+    achieved = PAIR_BYTES_PER_PARTICLE * nfl_big / (pair_us * 1e-6) / 1e9
+    # e2e: every group's state in from pinned host memory and out again per step
+    hostbufs = []
+    for g in bt.groups:
+        m = g.np
+        hostbufs.append([torch.empty((m, 2), dtype=torch.float64, pin_memory=True),
+                         torch.empty((m, 2), dtype=torch.float64, pin_memory=True),
+                         torch.empty((m,), dtype=torch.float64, pin_memory=True)])
+    mask = sph.F_R | sph.F_V | sph.F_RHO
+    for g, (hr, hv, hrho) in zip(bt.groups, hostbufs):
+        g.system.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        for g, (hr, hv, hrho) in zip(bt.groups, hostbufs):
+            g.system.upload_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+            g.system.particle_to_cell()
+            g.system.step(g.wall_model, g.dt, 1)
+        for g, (hr, hv, hrho) in zip(bt.groups, hostbufs):
+            g.system.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+    e2e_value = n * args.e2e_steps / (time.perf_counter() - t0)
+    # the plain path looped over the cases: each case alone, one system at a time
+    loop_ms = 0.0
+    loop_half = 0.0
+    st0 = torch.cuda.Stream()
+    for spec in specs:
+        a = B.case_arrays(spec)
+        s = sph.ParticleSystem(a.h, a.kap, a.cs, 1000.0, 0.02, 0.1, spec.dp, a.domain, "fp32",
+                               stream=st0.cuda_stream)
+        s.add_particles(a.type, a.r, None, a.rho, a.p, a.gnr if a.wall_model == 0 else None)
+        s.divide_to_cells()
+        s.particle_to_cell()
+        s.step(a.wall_model, a.dt, 3)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st0)
+        s.step(a.wall_model, a.dt, args.loop_steps)
+        e1.record(st0)
+        st0.synchronize()
+        case_ms = e0.elapsed_time(e1) / args.loop_steps
+        loop_ms += case_ms
+        loop_half += round(0.5 / a.dt) * case_ms / 1000.0
+        s.close()
+    looped_value = n / (loop_ms / 1000.0)
+    cpu = None
+    if not args.no_cpu:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle
+
+        threads = host_threads()
+        tot, tt = 0, 0.0
+        for spec in specs[:4]:
+            a = B.case_arrays(spec)
+            P = oracle.PortSystem(a.h, a.kap, a.cs, 1000.0, 0.02, 0.1, spec.dp, a.domain)
+            for i in range(a.np):
+                P.L.orc_add_particle(P.s, int(a.type[i]), float(a.p[i]), float(a.rho[i]),
+                                     float(a.r[i, 0]), float(a.r[i, 1]), 0.0, 0.0, 0.0, 0.0)
+            if a.wall_model == 0:  # ghost nodes of the walls (walls come first)
+                for i in np.nonzero(a.type == 1)[0]:
+                    P.L.orc_add_gnr(P.s, float(a.gnr[i, 0]), float(a.gnr[i, 1]))
+            P.set_threads(threads)
+            P.divide_to_cells()
+            P.particle_to_cell()
+            t0 = time.perf_counter()
+            P.step(a.wall_model, a.dt, 3)
+            tt += time.perf_counter() - t0
+            tot += a.np * 3
+        cpu = {"value": tot / tt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+               "sample": f"3 time steps of each of the first 4 cases ({tot // 3} particles, "
+                         f"{tt:.1f} s, FP64 C restatement, OpenMP)"}
+    line = {
+        "metric": BATCH_METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 pair math, f64 positions",
+        "data": "synthetic (seeded tanks built like the reference's generators)",
+        "config": {"workload": f"{len(specs)} cases (seed {args.seed}) in {len(bt.groups)} packed "
+                               f"groups, {n} particles; one step = one time step of every case",
+                   "particles": n, "groups": [[g.key[0], g.key[1], len(g.cases), g.np]
+                                              for g in bt.groups],
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": "single GPU"},
+        "looped": {"value": looped_value, "unit": "particle-steps/s",
+                   "ms_per_step": loop_ms, "speedup_batched": value / looped_value,
+                   "how": "each case alone in its own system, CUDA-graph steps, one after another"},
+        "projected_s_to_0.5s_physical": {"batched": t_half, "looped": loop_half},
+        "group_ms_per_step": group_ms,
+        "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": n * 40,
+                "d2h_bytes_per_step": n * 40,
+                "path": "per group tsph_upload(r,v,rho) + tsph_particle_to_cell + tsph_step(1) + "
+                        "tsph_download(r,v,rho), pinned host buffers"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": f"k_pairs_tiled, largest group {big.key}",
+                     "bytes_per_unit": PAIR_BYTES_PER_PARTICLE, "unit_count": nfl_big,
+                     "avg_launch_us": pair_us, "peak_kind": peak_kind},
+        "gpu_launches": args.steps * 13 * len(bt.groups),
+        "clocks": clocks.summary(),
+        "health": [g.system.health() for g in bt.groups],
+    }
+    if cpu:
+        line["cpu_baseline"] = cpu
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank, world):
     """The reference arm: the CPU restatement of the reference's step on all
     host cores, on the same workload.  Rank 0 only."""
@@ -377,7 +534,11 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dam_break", choices=["dam_break", "ale"])
+    ap.add_argument("--workload", default="dam_break", choices=["dam_break", "ale", "batch"])
+    ap.add_argument("--cases", type=int, default=512, help="batch workload: number of cases")
+    ap.add_argument("--seed", type=int, default=0, help="batch workload: case seed")
+    ap.add_argument("--loop-steps", type=int, default=10,
+                    help="batch workload: timed steps per case of the looped comparison")
     ap.add_argument("--scheme", default="as_written", choices=["as_written", "muscl"],
                     help="ALE interface states (ALE workload only)")
     ap.add_argument("--dp", type=float, default=None,
@@ -401,6 +562,10 @@ def main():
         return
     if args.workload == "ale":
         run_ale(args, rank, world, local)
+        return
+    if args.workload == "batch":
+        if rank == 0:
+            run_batch(args, rank, world, local)
         return
 
     import numpy as np

@@ -245,6 +245,14 @@ typedef struct {
     double other_us;     /* everything else (EOS, predictor, ...)         */
     int other_launches;
 } tsph_profile_t;
+/* Tile shape of the FP32 pair kernel: 0 = 608 staged neighbours and 36 list
+ * entries per target, 1 = 512 and 44 (for h ~ 1.5 dp).  tsph_autotune times
+ * both on the current particles (a forces pass each; the state is left as it
+ * was) and keeps the faster; the first tsph_step does this by itself.
+ * us[2] (may be NULL) receives the two times in microseconds.  No counterpart
+ * in the reference. */
+int tsph_autotune(tsph_system *s, int32_t *shape, double us[2]);
+int tsph_set_tile_shape(tsph_system *s, int shape);
 int tsph_set_profiling(tsph_system *s, int on);
 int tsph_get_profile(tsph_system *s, tsph_profile_t *out, int reset);
 

@@ -254,3 +254,28 @@ def test_remove_out_of_domain(gpu_tsph, oracle_mod):
     start, lst = s.get_cells()
     s0, l0 = P.cells()
     assert np.array_equal(start, s0) and np.array_equal(lst, l0)
+
+
+@pytest.mark.gpu
+def test_autotune_leaves_the_state_and_both_tile_shapes_agree(gpu_tsph):
+    """tsph_autotune times the two tile shapes of the FP32 pair kernel without
+    touching the state; stepping with either shape gives the same result up
+    to FP32 summation order."""
+    g = _gold("dam_break_mdbc_dp0.02.npz")
+    case = cases.dam_break_mdbc(dp=0.02)
+    dt = float(g["dt"])
+    s = _gpu(gpu_tsph, case, g, "fp32")
+    before = s.download()
+    shape, us = s.autotune()
+    assert shape in (0, 1) and np.all(us > 0)
+    after = s.download()
+    for f in ("r", "v", "a", "rho", "drho", "p"):
+        assert np.array_equal(before[f], after[f]), f
+    res = []
+    for shape in (0, 1):
+        t = _gpu(gpu_tsph, case, g, "fp32")
+        t.set_tile_shape(shape)
+        t.step(0, dt, 4)
+        res.append(t.download())
+    for f in ("r", "v", "a", "rho", "drho"):
+        assert _err(res[0][f], res[1][f]) <= 1e-5 * max(1.0, float(np.max(np.abs(res[0][f])))), f

@@ -598,6 +598,26 @@ __device__ __forceinline__ void ale_pair(float dx, float dy, float2 va, float sa
     acc.domr = fmaf(-t2 * rhos, ex * dWx + ey * dWy, acc.domr);
 }
 
+// the bounded append of a cell that could overflow the list (one copy, out
+// of line: the unrolled neighbour loop calls it rarely)
+static __device__ __noinline__ int append_bounded_kAleT(const float2 *loc, uint16_t *lst, int cnt,
+                                                   int j0, int j1, int code, float bx, float by,
+                                                   uint32_t h2bits, bool &overflow) {
+    for (int j = j0; j < j1; j++) {
+        const float2 lb = loc[j];
+        const float dx = bx - lb.x, dy = by - lb.y;
+        if (((uint32_t)(__float_as_uint(fmaf(dx, dx, dy * dy)) - 1u) < h2bits ? 1u : 0u)) {
+            if (cnt < kAleList) {
+                lst[cnt * kAleT] = (uint16_t)(((uint32_t)j << 4) | (uint32_t)code);
+                cnt++;
+            } else {
+                overflow = true;
+            }
+        }
+    }
+    return cnt;
+}
+
 __global__ void __launch_bounds__(kAleT, 8)
 k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                  const uint32_t *__restrict__ wstart, AleWalls Wl, Grid g, AleConst K) {
@@ -707,7 +727,11 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                             const int j1 = kind == 0 ? wb[dxi] + sm.woff[dxi][q + 1] - w0[dxi]
                                                      : fb[dxi] + sm.foff[dxi][q + 1] - f0[dxi];
                             if (cnt + (j1 - j0) > kAleList) {
-                                overflow = true;
+                                // the cell could overflow the list: append one
+                                // at a time, bounded (a target with more than
+                                // kAleList neighbours takes the global-memory path)
+                                cnt = append_bounded_kAleT(sm.loc, lst, cnt, j0, j1, code, bx, by, h2bits,
+                                                         overflow);
                                 continue;
                             }
                             uint16_t *w = lst + cnt * kAleT;

@@ -455,6 +455,22 @@ int tsph_water_front(tsph_system *s, double y_max, double *x_front) {
     return TSPH_OK;
 }
 
+int tsph_autotune(tsph_system *s, int32_t *shape, double us[2]) {
+    NEED(s);
+    ENGINE(s);
+    int c = 0;
+    RUN(s->eng->autotune(&c, us, err_));
+    if (shape) *shape = c;
+    return TSPH_OK;
+}
+
+int tsph_set_tile_shape(tsph_system *s, int shape) {
+    NEED(s);
+    ENGINE(s);
+    RUN(s->eng->set_tile_shape(shape, err_));
+    return TSPH_OK;
+}
+
 int tsph_set_profiling(tsph_system *s, int on) {
     NEED(s);
     s->profiling = on != 0;

@@ -206,6 +206,74 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     TileConst K_{}, Kskin_{};
+    int tile_shape_ = -1;  // 0 TileWide, 1 TileDeep; -1: not tuned yet
+
+  public:
+    // time both tile shapes on the current particles (forces pass, a and drho
+    // saved and restored) and keep the faster; FP32 build only
+    int autotune(int *choice, double us[2], std::string &err) override {
+        if constexpr (!std::is_same<T, float>::value) {
+            tile_shape_ = 0;
+            if (choice) *choice = 0;
+            if (us) us[0] = us[1] = 0;
+            return 0;
+        } else {
+            if (!cells_) {
+                err = "cell lists are stale: call tsph_particle_to_cell first";
+                return 3;
+            }
+            const bool prof = prof_;
+            prof_ = false;
+            TSPH_CK(cudaMemcpyAsync(Bv_, F_.a, sizeof(T2) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
+            TSPH_CK(cudaMemcpyAsync(Brho_, F_.drho, sizeof(T) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
+            cudaEvent_t e0 = ev(), e1 = ev();
+            float best[2] = {0, 0};
+            int rc = 0;
+            for (int shape = 0; shape < 2 && !rc; shape++) {
+                tile_shape_ = shape;
+                rc = fluid_pairs<MODE_FORCES>(F_, false, T(0), PairOut{}, err);  // warm
+                for (int rep = 0; rep < 3 && !rc; rep++) {
+                    cudaEventRecord(e0, st_);
+                    rc = fluid_pairs<MODE_FORCES>(F_, false, T(0), PairOut{}, err);
+                    cudaEventRecord(e1, st_);
+                    cudaEventSynchronize(e1);
+                    float ms = 0;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (rep == 0 || ms < best[shape]) best[shape] = ms;
+                }
+            }
+            ev_pool_.push_back(e0);
+            ev_pool_.push_back(e1);
+            prof_ = prof;
+            if (rc) return rc;
+            TSPH_CK(cudaMemcpyAsync(F_.a, Bv_, sizeof(T2) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
+            TSPH_CK(cudaMemcpyAsync(F_.drho, Brho_, sizeof(T) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
+            TSPH_CK(cudaStreamSynchronize(st_));
+            tile_shape_ = best[1] < best[0] ? 1 : 0;
+            // graphs captured with the other shape are stale
+            for (auto &g : graphs_) cudaGraphExecDestroy(g.second);
+            graphs_.clear();
+            if (choice) *choice = tile_shape_;
+            if (us) {
+                us[0] = 1000.0 * best[0];
+                us[1] = 1000.0 * best[1];
+            }
+            return 0;
+        }
+    }
+
+    int set_tile_shape(int shape, std::string &err) override {
+        if (shape < 0 || shape > 1) {
+            err = "tile shape must be 0 or 1";
+            return 1;
+        }
+        tile_shape_ = shape;
+        for (auto &g : graphs_) cudaGraphExecDestroy(g.second);
+        graphs_.clear();
+        return 0;
+    }
+
+  private:
 
     // the fluid-row pair pass: tiled FP32 kernel, or the plain FP64 kernel.
     // `skinned`: the cells are those of the binning before the predictor.
@@ -215,13 +283,19 @@ template <typename T> class Engine final : public EngineBase {
         if constexpr (std::is_same<T, float>::value) {
             const int nb = blocks_for(nf_, kTileT);
             const TileConst K = skinned ? Kskin_ : K_;
+            const uint32_t *fs = fstart_, *ws = wstart_;
+            if (tile_shape_ == 1) {
+                if (stored_p)
+                    return launch(CAT_PAIR, k_pairs_tiled<MODE, true, TileDeep>, nb, kTileT, err,
+                                  X, fs, ws, W_, grid_, P_, K, O_, dt, po, health_);
+                return launch(CAT_PAIR, k_pairs_tiled<MODE, false, TileDeep>, nb, kTileT, err, X,
+                              fs, ws, W_, grid_, P_, K, O_, dt, po, health_);
+            }
             if (stored_p)
-                return launch(CAT_PAIR, k_pairs_tiled<MODE, true>, nb, kTileT, err, X,
-                              (const uint32_t *)fstart_, (const uint32_t *)wstart_, W_, grid_, P_,
-                              K, O_, dt, po, health_);
-            return launch(CAT_PAIR, k_pairs_tiled<MODE, false>, nb, kTileT, err, X,
-                          (const uint32_t *)fstart_, (const uint32_t *)wstart_, W_, grid_, P_, K,
-                          O_, dt, po, health_);
+                return launch(CAT_PAIR, k_pairs_tiled<MODE, true, TileWide>, nb, kTileT, err, X,
+                              fs, ws, W_, grid_, P_, K, O_, dt, po, health_);
+            return launch(CAT_PAIR, k_pairs_tiled<MODE, false, TileWide>, nb, kTileT, err, X, fs,
+                          ws, W_, grid_, P_, K, O_, dt, po, health_);
         } else {
             return launch(CAT_PAIR, k_fluid_pairs<T, MODE>, blocks_for(nf_), kBlock, err, X,
                           (const uint32_t *)fstart_, (const uint32_t *)wstart_,
@@ -677,6 +751,7 @@ template <typename T> class Engine final : public EngineBase {
             return 3;
         }
         int rc;
+        if (tile_shape_ < 0 && (rc = autotune(nullptr, nullptr, err))) return rc;
         if (prof_) {
             for (int s = 0; s < nsteps; s++)
                 if ((rc = enqueue_step(model, (T)dt, err))) return rc;

@@ -62,6 +62,8 @@ class EngineBase {
                             double *out, std::string &err) = 0;
     virtual int point_fields(int n, const double *xy, double *out, std::string &err) = 0;
     virtual int water_front(double y_max, double *x, std::string &err) = 0;
+    virtual int autotune(int *choice, double us[2], std::string &err) = 0;
+    virtual int set_tile_shape(int shape, std::string &err) = 0;
     virtual int sync(std::string &err) = 0;
     virtual void set_profiling(bool on) = 0;
     virtual Profile profile(bool reset) = 0;

@@ -26,19 +26,27 @@ namespace tsph {
 
 constexpr int kTileT = 128;     // targets per CTA
 constexpr int kTileRows = 16;   // max target rows per window (halved while the block is too big)
-constexpr int kTileCap = 608;   // staged neighbours per window
-constexpr int kList = 36;       // list entries per target (overflow: global-memory path)
+// Two tile shapes, both 8 CTAs/SM (under 27.5 KB of shared memory each):
+// 608 staged neighbours + 36 list entries per target (h ~ 1.4 dp: ~24
+// neighbours), or 512 + 44 (h ~ 1.5 dp: ~28 neighbours); the engine times both
+// on its own particles and keeps the faster (a target whose list would
+// overflow takes the global-memory path).
+template <int CAP, int LIST> struct TileShape {
+    static constexpr int cap = CAP, list = LIST;
+};
+typedef TileShape<608, 36> TileWide;
+typedef TileShape<512, 44> TileDeep;
 
 // 8 CTAs of 128 threads per SM: 28 B per staged neighbour + 72 B of list per
 // target keep a CTA under 27.5 KB of shared memory
-struct TileSmem {
-    float2 loc[kTileCap];
-    float4 vs[kTileCap];   // {vx, vy, rho - rho0, p/rho}
-    float inv[kTileCap];   // 1/rho
+template <class SH> struct TileSmem {
+    float2 loc[SH::cap];
+    float4 vs[SH::cap];   // {vx, vy, rho - rho0, p/rho}
+    float inv[SH::cap];   // 1/rho
     int foff[3][kTileRows + 3];
     int woff[3][kTileRows + 3];
     float2 off[9];
-    uint16_t list[kList * kTileT];
+    uint16_t list[SH::list * kTileT];
 };
 
 __device__ __forceinline__ float rcp_approx(float x) {
@@ -154,13 +162,13 @@ __device__ __forceinline__ bool out_of_domain_bits(double2 r, const BoxBits &b) 
     return !nan && (oy < b.y_lo || oy > b.y_hi || ox < b.x_lo || ox > b.x_hi);
 }
 
-template <int MODE, bool STORED_P>
+template <int MODE, bool STORED_P, class SH>
 __global__ void __launch_bounds__(kTileT, 8)
 k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
               const uint32_t *__restrict__ wstart, WallState<float> Wl, Grid g, Phys<float> P,
               TileConst K, OldState<float> O, float dt, PairOut out,
               uint32_t *__restrict__ health) {
-    __shared__ TileSmem sm;
+    __shared__ TileSmem<SH> sm;
     const int tid = threadIdx.x;
     const int ncy = g.ncy;
     const int nl = n_live(fstart, g.ncells);
@@ -210,7 +218,7 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
             fb[d] = tot;
             tot += sm.foff[d][nr] - f0[d];
         }
-        if (tot > kTileCap && rows > 1) {  // too dense: fewer target rows per window
+        if (tot > SH::cap && rows > 1) {  // too dense: fewer target rows per window
             rows = (rows + 1) >> 1;
             continue;
         }
@@ -220,7 +228,7 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
         float2 la = make_float2(0.f, 0.f), va = make_float2(0.f, 0.f);
         float sa = 0.f, Pa = 0.f, Ia = 0.f, Ra2 = 0.f;
         int cy = 0;
-        if (tot <= kTileCap) {
+        if (tot <= SH::cap) {
             // ---- stage the neighbour block
 #pragma unroll
             for (int d = 0; d < 3; d++) {
@@ -280,7 +288,7 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                                                      : fb[dxi] + sm.foff[dxi][q] - f0[dxi];
                             const int j1 = kind == 0 ? wb[dxi] + sm.woff[dxi][q + 1] - w0[dxi]
                                                      : fb[dxi] + sm.foff[dxi][q + 1] - f0[dxi];
-                            if (cnt + (j1 - j0) > kList) {
+                            if (cnt + (j1 - j0) > SH::list) {
                                 overflow = true;
                                 continue;
                             }

@@ -36,7 +36,8 @@ ABI_SYMBOLS = (
     "tsph_compute_forces", "tsph_symplectic_predictor", "tsph_symplectic_corrector",
     "tsph_remove_out_of_domain", "tsph_step", "tsph_download", "tsph_upload", "tsph_sync",
     "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
-    "tsph_water_level", "tsph_point_fields", "tsph_water_front",
+    "tsph_water_level", "tsph_point_fields", "tsph_water_front", "tsph_autotune",
+    "tsph_set_tile_shape",
     "tsph_ale_create", "tsph_ale_destroy", "tsph_ale_add_particles", "tsph_ale_set_scheme",
     "tsph_ale_np", "tsph_ale_divide_to_cells", "tsph_ale_particle_to_cell", "tsph_ale_gradient",
     "tsph_ale_forces", "tsph_ale_leapfrog_one", "tsph_ale_leapfrog_two", "tsph_ale_step",
@@ -135,6 +136,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_water_level.argtypes = [P, I, P, P, P, P]
     L.tsph_point_fields.argtypes = [P, I, P, P]
     L.tsph_water_front.argtypes = [P, D, C.POINTER(D)]
+    L.tsph_autotune.argtypes = [P, P, P]
+    L.tsph_set_tile_shape.argtypes = [P, I]
     L.tsph_ale_create.argtypes = [C.POINTER(_Constants), C.POINTER(_Domain), P, C.POINTER(P)]
     for f in ("tsph_ale_destroy", "tsph_ale_divide_to_cells", "tsph_ale_particle_to_cell",
               "tsph_ale_gradient", "tsph_ale_sync"):
@@ -394,6 +397,17 @@ class ParticleSystem:
         x = C.c_double()
         _check(self._L.tsph_water_front(self._h, float(y_max), C.byref(x)))
         return x.value
+
+    def autotune(self):
+        """Time both tile shapes of the pair kernel, keep the faster:
+        (shape, [us shape 0, us shape 1])."""
+        c = C.c_int32()
+        us = np.zeros(2)
+        _check(self._L.tsph_autotune(self._h, C.byref(c), _p(us)))
+        return c.value, us
+
+    def set_tile_shape(self, shape: int):
+        _check(self._L.tsph_set_tile_shape(self._h, int(shape)))
 
     def set_profiling(self, on: bool):
         _check(self._L.tsph_set_profiling(self._h, 1 if on else 0))
