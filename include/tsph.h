@@ -254,6 +254,17 @@ typedef struct {
 int tsph_autotune(tsph_system *s, int32_t *shape, double us[2]);
 int tsph_set_tile_shape(tsph_system *s, int shape);
 int tsph_set_profiling(tsph_system *s, int on);
+
+/* ---- output and restart
+ * write_to_ASCII_VTK (src/SPH_data_to_vtk.h:4-51): the same POLYDATA file
+ * (points, type, pressure, density, velocity) in the reference's order. */
+int tsph_write_vtk(tsph_system *s, const char *path);
+/* binary checkpoint of the live particles (state, rates, ghost nodes,
+ * constants, domain, precision, tile shape; no counterpart in the reference)
+ * and a new system restarted from it: stepping it continues the saved run
+ * bit for bit. */
+int tsph_save_checkpoint(tsph_system *s, const char *path);
+int tsph_load_checkpoint(const char *path, void *stream, tsph_system **out);
 int tsph_get_profile(tsph_system *s, tsph_profile_t *out, int reset);
 
 /* ==================================================================

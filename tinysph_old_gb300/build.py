@@ -30,6 +30,7 @@ UNITS = [
     ("tsph_engine_f64.cu", ["-fmad=false"]),
     ("tsph_noalloc.cu", []),
     ("tsph_ale.cu", []),
+    ("tsph_io.cu", []),
 ]
 
 

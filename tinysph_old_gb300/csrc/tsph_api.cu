@@ -33,15 +33,7 @@ namespace tsph {
 void set_last_error(const std::string &msg) { g_err = msg; }
 }  // namespace tsph
 
-struct tsph_system {
-    HostSetup hs;
-    int precision = TSPH_PREC_FP32;
-    void *stream = nullptr;
-    std::unique_ptr<EngineBase> eng;
-    bool divided = false;
-    bool stale_engine = true;  // host particle list changed since the engine was built
-    bool profiling = false;
-};
+#include "tsph_system.h"
 
 static int ensure_engine(tsph_system *s) {
     if (!s->divided) return fail(TSPH_ERR_STATE, "call tsph_divide_to_cells first");

@@ -262,6 +262,8 @@ template <typename T> class Engine final : public EngineBase {
         }
     }
 
+    int tile_shape() const override { return tile_shape_; }
+
     int set_tile_shape(int shape, std::string &err) override {
         if (shape < 0 || shape > 1) {
             err = "tile shape must be 0 or 1";

@@ -64,6 +64,7 @@ class EngineBase {
     virtual int water_front(double y_max, double *x, std::string &err) = 0;
     virtual int autotune(int *choice, double us[2], std::string &err) = 0;
     virtual int set_tile_shape(int shape, std::string &err) = 0;
+    virtual int tile_shape() const = 0;
     virtual int sync(std::string &err) = 0;
     virtual void set_profiling(bool on) = 0;
     virtual Profile profile(bool reset) = 0;

@@ -146,6 +146,12 @@ template <typename T> __device__ __forceinline__ T rho_full(T s, T rho0) {
     if constexpr (std::is_same<T, float>::value) return rho0 + s;
     else return s;
 }
+// the same in FP64 (what the host reads: rho0 + s rounded to float would
+// drop the low bits of s, ~6e-5 kg/m^3 at rho ~ 1000)
+template <typename T> __device__ __forceinline__ double rho_full64(T s, T rho0) {
+    if constexpr (std::is_same<T, float>::value) return (double)rho0 + (double)s;
+    else return s;
+}
 template <typename T> __host__ __device__ __forceinline__ T rho_stored_from_full(double full, double rho0) {
     if constexpr (std::is_same<T, float>::value) return (float)(full - rho0);
     else return full;

@@ -1145,7 +1145,7 @@ __global__ void k_export(FluidState<T> F, const uint32_t *__restrict__ fstart, i
         if (mask & 1) S.r[id] = Wl.r[i];
         if (mask & 2) S.v[id] = make_double2(0., 0.);
         if (mask & 4) S.a[id] = make_double2(0., 0.);
-        if (mask & 8) S.rho[id] = (double)rho_full(Wl.rho[i], rho0);
+        if (mask & 8) S.rho[id] = rho_full64(Wl.rho[i], rho0);
         if (mask & 16) S.drho[id] = (double)Wl.drho[i];
         if (mask & 32) S.p[id] = (double)Wl.p[i];
         S.alive[id] = 1;
@@ -1167,7 +1167,7 @@ __global__ void k_export(FluidState<T> F, const uint32_t *__restrict__ fstart, i
         const auto a = F.a[f];
         S.a[id] = make_double2((double)a.x, (double)a.y);
     }
-    if (mask & 8) S.rho[id] = (double)rho_full(F.rho[f], rho0);
+    if (mask & 8) S.rho[id] = rho_full64(F.rho[f], rho0);
     if (mask & 16) S.drho[id] = (double)F.drho[f];
     if (mask & 32) S.p[id] = (double)F.p[f];
     S.alive[id] = 1;

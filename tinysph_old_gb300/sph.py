@@ -37,7 +37,7 @@ ABI_SYMBOLS = (
     "tsph_remove_out_of_domain", "tsph_step", "tsph_download", "tsph_upload", "tsph_sync",
     "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
     "tsph_water_level", "tsph_point_fields", "tsph_water_front", "tsph_autotune",
-    "tsph_set_tile_shape",
+    "tsph_set_tile_shape", "tsph_write_vtk", "tsph_save_checkpoint", "tsph_load_checkpoint",
     "tsph_ale_create", "tsph_ale_destroy", "tsph_ale_add_particles", "tsph_ale_set_scheme",
     "tsph_ale_np", "tsph_ale_divide_to_cells", "tsph_ale_particle_to_cell", "tsph_ale_gradient",
     "tsph_ale_forces", "tsph_ale_leapfrog_one", "tsph_ale_leapfrog_two", "tsph_ale_step",
@@ -138,6 +138,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_water_front.argtypes = [P, D, C.POINTER(D)]
     L.tsph_autotune.argtypes = [P, P, P]
     L.tsph_set_tile_shape.argtypes = [P, I]
+    L.tsph_write_vtk.argtypes = [P, C.c_char_p]
+    L.tsph_save_checkpoint.argtypes = [P, C.c_char_p]
+    L.tsph_load_checkpoint.argtypes = [C.c_char_p, P, C.POINTER(P)]
     L.tsph_ale_create.argtypes = [C.POINTER(_Constants), C.POINTER(_Domain), P, C.POINTER(P)]
     for f in ("tsph_ale_destroy", "tsph_ale_divide_to_cells", "tsph_ale_particle_to_cell",
               "tsph_ale_gradient", "tsph_ale_sync"):
@@ -397,6 +400,26 @@ class ParticleSystem:
         x = C.c_double()
         _check(self._L.tsph_water_front(self._h, float(y_max), C.byref(x)))
         return x.value
+
+    def write_vtk(self, path):
+        """write_to_ASCII_VTK (src/SPH_data_to_vtk.h)."""
+        _check(self._L.tsph_write_vtk(self._h, os.fsencode(path)))
+
+    def save_checkpoint(self, path):
+        _check(self._L.tsph_save_checkpoint(self._h, os.fsencode(path)))
+
+    @classmethod
+    def load_checkpoint(cls, path, stream=None):
+        """A new system restarted from a checkpoint."""
+        L = load()
+        h_ = C.c_void_p()
+        _check(L.tsph_load_checkpoint(os.fsencode(path), stream, C.byref(h_)))
+        s = cls.__new__(cls)
+        s._L = L
+        s._h = h_
+        s.precision = None
+        s.domain = None
+        return s
 
     def autotune(self):
         """Time both tile shapes of the pair kernel, keep the faster:
