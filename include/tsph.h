@@ -277,12 +277,16 @@ int tsph_get_profile(tsph_system *s, tsph_profile_t *out, int reset);
  * ================================================================== */
 typedef struct tsph_ale_system tsph_ale_system;
 
-/* interface states of the flux loop: as the reference computes them
- * (MUSCL_final adds 0.5 dt/dx (F(W_L) - F(W_L)) = 0 and the neighbour state
- * carries the active particle's velocity, src/_testMUSCL_interaction.h:185,
- * src/_testMUSCL_schemes.h:78-88), or the superbee-limited MUSCL states of
- * both particles (no counterpart in the reference) */
-enum { TSPH_ALE_AS_WRITTEN = 0, TSPH_ALE_MUSCL = 1 };
+/* interface states of the flux loop: as the reference's MUSCL.h driver
+ * computes them (MUSCL_final adds 0.5 dt/dx (F(W_L) - F(W_L)) = 0 and the
+ * neighbour state carries the active particle's velocity,
+ * src/_testMUSCL_interaction.h:185, src/_testMUSCL_schemes.h:78-88); the
+ * superbee-limited MUSCL states of both particles (no counterpart in the
+ * reference); or the first-order fluxes of the SPH_simulationINT.h driver
+ * (Compute_Forces(Particle_system&), src/RALESPH_interaction.h:12-289: both
+ * particles' own states, limited Riemann density, linear wall pressure; no
+ * gradient pass) */
+enum { TSPH_ALE_AS_WRITTEN = 0, TSPH_ALE_MUSCL = 1, TSPH_ALE_FIRST_ORDER = 2 };
 
 /* host view; any pointer may be NULL.  grad: 12 per particle (rho, vx, vy
  * forward x/y, then backward x/y: special.grad*F, grad*B), valid from

@@ -111,6 +111,7 @@ def _load_port():
         L.orc_ale_set_scheme.argtypes = [_P, _I]
         L.orc_ale_gradient.argtypes = [_P]
         L.orc_ale_forces.argtypes = [_P, _D]
+        L.orc_ale_forces_first_order.argtypes = [_P]
         L.orc_ale_leapfrog_one.argtypes = [_P, _D]
         L.orc_ale_leapfrog_two.argtypes = [_P, _D, _I]
         L.orc_ale_step.argtypes = [_P, _D, _I, _I]
@@ -468,6 +469,8 @@ def _load_ref_ale():
         L.refale_leapfrog_one.argtypes = [_P, _D]
         L.refale_leapfrog_two.argtypes = [_P, _D, _I]
         L.refale_step.argtypes = [_P, _D, _I, _I]
+        L.refale_forces_first_order.argtypes = [_P]
+        L.refale_step_first_order.argtypes = [_P, _D, _I, _I]
         _ref_ale = L
     return _ref_ale
 
@@ -543,6 +546,9 @@ class PortAle(PortSystem):
 
     def ale_forces(self, dt):
         self.L.orc_ale_forces(self.s, dt)
+
+    def ale_forces_first_order(self):
+        self.L.orc_ale_forces_first_order(self.s)
 
     def leapfrog_one(self, dt):
         self.L.orc_ale_leapfrog_one(self.s, dt)
@@ -621,6 +627,12 @@ class RefAle:
 
     def ale_forces(self, dt):
         self.L.refale_forces(self.s, dt)
+
+    def ale_forces_first_order(self):
+        self.L.refale_forces_first_order(self.s)
+
+    def ale_step_first_order(self, dt, step0, n):
+        self.L.refale_step_first_order(self.s, dt, int(step0), int(n))
 
     def leapfrog_one(self, dt):
         self.L.refale_leapfrog_one(self.s, dt)

@@ -15,6 +15,7 @@
 #include "ALESPH_create.h"
 #include "_testMUSCL_gradientApprox.h"
 #include "_testMUSCL_interaction.h"
+#include "RALESPH_interaction.h"
 #include "SPH_btdebug.h"
 
 #include <iostream>
@@ -156,6 +157,26 @@ void refale_step(void *c, double dt, int step0, int n) {
         Density_to_pressure(P);
         Kernel_gradient_approx(P);
         Compute_Forces(P, dt);
+        Integrate_LeapFrog_partTwo(P, dt, step);
+        RemoveParticlesOutOfDomain_ALE(P, K(c)->sim);
+    }
+}
+
+// the first-order variant of cases/ALESPH_dambreakLong/SPH_simulationINT.h:84-133
+// (Compute_Forces(Particle_system&), src/RALESPH_interaction.h:12-289; no
+// gradient pass)
+void refale_forces_first_order(void *c) { Compute_Forces(K(c)->particles); }
+
+void refale_step_first_order(void *c, double dt, int step0, int n) {
+    Quiet q;
+    Particle_system &P = K(c)->particles;
+    for (int k = 1; k <= n; k++) {
+        const int step = step0 + k;
+        if (step > 1) Integrate_LeapFrog_partOne(P, dt);
+        Clear_cells(P);
+        Particle_To_Cell(P, K(c)->sim);
+        Density_to_pressure(P);
+        Compute_Forces(P);
         Integrate_LeapFrog_partTwo(P, dt, step);
         RemoveParticlesOutOfDomain_ALE(P, K(c)->sim);
     }

@@ -84,11 +84,15 @@ void orc_ale_add_particle(orc_sys *s, int type, double p, double rho, double rx,
 void orc_ale_add_normal(orc_sys *s, double nx, double ny);
 void orc_ale_get_field(const orc_sys *s, int f, double *out);
 void orc_ale_set_field(orc_sys *s, int f, const double *in);
-/* 0: the reference's fluxes (default); 1: superbee MUSCL interface states of
- * both particles (no counterpart in the reference) */
+/* 0: the reference's MUSCL.h fluxes (default); 1: superbee MUSCL interface
+ * states of both particles (no counterpart in the reference); 2: the
+ * first-order fluxes of SPH_simulationINT.h (src/RALESPH_interaction.h) */
 void orc_ale_set_scheme(orc_sys *s, int scheme);
 void orc_ale_gradient(orc_sys *s);
 void orc_ale_forces(orc_sys *s, double dt);
+/* the first-order variant, src/RALESPH_interaction.h:12-289 (scheme 2 in
+ * orc_ale_step) */
+void orc_ale_forces_first_order(orc_sys *s);
 void orc_ale_leapfrog_one(orc_sys *s, double dt);
 void orc_ale_leapfrog_two(orc_sys *s, double dt, int step);
 void orc_ale_step(orc_sys *s, double dt, int step0, int nsteps);

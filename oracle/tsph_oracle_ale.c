@@ -316,6 +316,95 @@ void orc_ale_forces(orc_sys *s, double dt) {
     }
 }
 
+/* Compute_Forces(Particle_system&), src/RALESPH_interaction.h:12-289: the
+ * first-order variant of cases/ALESPH_dambreakLong/SPH_simulationINT.h (both
+ * particles' own states, velRiemannLinearized and
+ * densRiemannLinearizedWithLimiter, src/ALESPH_riemann_solver.h:20-34,86-96;
+ * BT walls with the linear equation of state Compute_Pressure2,
+ * src/SPH_pressure.h:24-34) */
+void orc_ale_forces_first_order(orc_sys *s) {
+    const int ncy = s->ncy, nc = s->ncells;
+    const double h = s->h, m = s->m, c0 = s->cs, rho0 = s->rho0, dp = s->dp;
+    const double gx = 0., gy = s->gravy;
+    const int *cs = s->cell_start, *cl = s->cell_list;
+#pragma omp parallel for schedule(dynamic, 3)
+    for (int c = 0; c < nc; c++) {
+        const int ac[9] = {c,           c + 1,       c + 1 + ncy,
+                           c + ncy,     c - 1 + ncy, c - 1,
+                           c - 1 - ncy, c - ncy,     c + 1 - ncy};
+        double gamma_sum = 0; /* per cell, never reset per particle */
+        for (int i = cs[c]; i < cs[c + 1]; i++) {
+            const int ai = cl[i];
+            if (s->type[ai] != ORC_FLUID) continue;
+            const double arx = s->rx[ai], ary = s->ry[ai];
+            const double avx = s->vx[ai], avy = s->vy[ai];
+            const double arho = s->rho[ai];
+            const double ao = s->om[ai];
+            double dom_s = 0, domr_s = 0, domvx_s = 0, domvy_s = 0;
+            for (int k = 0; k < 9; k++) {
+                const int cc = ac[k];
+                if (cc < 0 || cc >= nc) continue;
+                for (int n = cs[cc]; n < cs[cc + 1]; n++) {
+                    const int ni = cl[n];
+                    if (ai == ni) continue;
+                    const double nvx = s->vx[ni], nvy = s->vy[ni];
+                    const double nrho = s->rho[ni];
+                    const double no = s->om[ni];
+                    const double drx = arx - s->rx[ni], dry = ary - s->ry[ni];
+                    const double dvx = avx - nvx, dvy = avy - nvy;
+                    const double drs = sqrt((drx * drx) + (dry * dry));
+                    double W, F;
+                    orc_wendland(drs, h, &W, &F);
+                    const double dWx = drx * F, dWy = dry * F;
+                    const double dvdW = dvx * dWx + dvy * dWy;
+                    const double drnx = drx * (1 / drs) * (-1), drny = dry * (1 / drs) * (-1);
+                    const double vL = avx * drnx + avy * drny;
+                    const double vR = nvx * drnx + nvy * drny;
+                    const double avgrho = 0.5 * (arho + nrho);
+                    const double vss = 0.5 * (vR + vL) - 0.5 * (nrho - arho) * c0 / avgrho;
+                    const double d = vL - vR;
+                    const double mx = (d > 0) ? d : 0;
+                    const double beta = ((3. * mx) < c0) ? (3. * mx) : c0;
+                    double rhos = 0.5 * (arho + nrho) + 0.5 * beta * (vL - vR) * avgrho / (c0 * c0);
+                    double ps = orc_pressure(rhos, rho0, c0);
+                    const double vsx = drnx * vss + ((avx + nvx) * 0.5 - drnx * (vL + vR) * 0.5);
+                    const double vsy = drny * vss + ((avy + nvy) * 0.5 - drny * (vL + vR) * 0.5);
+                    const double vzx = avx, vzy = avy;
+                    if (s->type[ni] == ORC_WALL) {
+                        const double nbx = s->nx[ni] * (-1), nby = s->ny[ni] * (-1);
+                        rhos = arho - ((0 - avx) * nbx + (0 - avy) * nby) * arho / c0;
+                        ps = c0 * c0 * (rhos - rho0) * 1;
+                        domvx_s -= 2 * W * dp * (ps * nbx);
+                        domvy_s -= 2 * W * dp * (ps * nby);
+                        const double dvn = dvx * nbx + dvy * nby;
+                        dom_s -= dvn * W * dp;
+                    } else {
+                        domvx_s -= 2 * no *
+                                   ((rhos * vsx * (vsx - vzx) + ps) * dWx + (rhos * vsx * (vsy - vzy)) * dWy);
+                        domvy_s -= 2 * no *
+                                   ((rhos * vsy * (vsx - vzx)) * dWx + (rhos * vsy * (vsy - vzy) + ps) * dWy);
+                        const double vsdW = (vsx - vzx) * dWx + (vsy - vzy) * dWy;
+                        dom_s -= dvdW * no;
+                        domr_s -= 2 * rhos * no * vsdW;
+                    }
+                    gamma_sum += W * m / nrho;
+                }
+            }
+            if (gamma_sum == 0) {
+                s->dom[ai] = 0.;
+                s->domr[ai] = 0.;
+                s->domvx[ai] = 0.;
+                s->domvy[ai] = 0.;
+            } else {
+                s->dom[ai] = dom_s * ao;
+                s->domr[ai] = domr_s * ao;
+                s->domvx[ai] = domvx_s * ao - gx * ao * arho;
+                s->domvy[ai] = domvy_s * ao - gy * ao * arho;
+            }
+        }
+    }
+}
+
 /* Integrate_LeapFrog_partOne, src/RALESPH_integration.h:10-36 */
 void orc_ale_leapfrog_one(orc_sys *s, double dt) {
 #pragma omp parallel for schedule(static)
@@ -385,8 +474,12 @@ void orc_ale_step(orc_sys *s, double dt, int step0, int nsteps) {
         orc_clear_cells(s);
         orc_particle_to_cell(s);
         orc_density_to_pressure(s);
-        orc_ale_gradient(s);
-        orc_ale_forces(s, dt);
+        if (s->ale_scheme == 2) {
+            orc_ale_forces_first_order(s); /* SPH_simulationINT.h: no gradient pass */
+        } else {
+            orc_ale_gradient(s);
+            orc_ale_forces(s, dt);
+        }
         orc_ale_leapfrog_two(s, dt, step);
         orc_remove_out_of_domain(s);
     }

@@ -127,7 +127,7 @@ def ale_geometry(dp):
                 normals=R.normals())
 
 
-def run_ale(case, nsteps, rng, snap_every):
+def run_ale(case, nsteps, rng, snap_every, first_order=False):
     """Riemann / ALE-SPH dam break (cases/ALESPH_dambreakLong/MUSCL.h RUN loop)
     from a seeded perturbation of the fluid velocity and density."""
     O.RefAle.set_threads(1)
@@ -144,8 +144,11 @@ def run_ale(case, nsteps, rng, snap_every):
     out["normals"] = R.normals()
     # per-function outputs at the perturbed initial state
     R.density_to_pressure()
-    R.gradient()
-    R.ale_forces(case.dt)
+    if first_order:
+        R.ale_forces_first_order()
+    else:
+        R.gradient()
+        R.ale_forces(case.dt)
     f = R.ale_state()
     for k in ("grad", "domega", "domegarho", "domegav"):
         out[f"forces_{k}"] = f[k]
@@ -153,7 +156,10 @@ def run_ale(case, nsteps, rng, snap_every):
     R2.set_velocity_density(v, rho)
     done = 0
     while done < nsteps:
-        R2.ale_step(case.dt, done, snap_every)
+        if first_order:
+            R2.ale_step_first_order(case.dt, done, snap_every)
+        else:
+            R2.ale_step(case.dt, done, snap_every)
         done += snap_every
         st = R2.ale_state()
         for k in ("r", "v", "rho", "p", "omega", "omegarho", "omegav", "domega", "domegarho",
@@ -187,6 +193,10 @@ def main_ale():
         out[f"geom_{k}"] = v
     out.update(run_ale(cases.dam_break_ale(dp=0.02), 6, rng, 2))
     np.savez_compressed(os.path.join(HERE, "dam_break_ale_dp0.02.npz"), **out)
+    # the first-order driver (cases/ALESPH_dambreakLong/SPH_simulationINT.h)
+    fo = run_ale(cases.dam_break_ale(dp=0.02), 6, np.random.default_rng(SEED + 2), 2,
+                 first_order=True)
+    np.savez_compressed(os.path.join(HERE, "dam_break_ale_first_order_dp0.02.npz"), **fo)
 
 
 WL_GAUGES = [(0.3, 0.0, 0), (0.3, 0.45, 1), (0.865, 0.0, 0), (0.865, 0.45, 1),

@@ -145,7 +145,33 @@ def test_ale_muscl_scheme_vs_oracle(gpu_tsph, oracle_mod):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("scheme", [0, 1])
+def test_ale_first_order_vs_reference_golden(gpu_tsph):
+    """The first-order driver (SPH_simulationINT.h, src/RALESPH_interaction.h):
+    fluxes at the initial state and 6 fused steps against the reference."""
+    g = np.load(os.path.join(GOLD, "dam_break_ale_first_order_dp0.02.npz"))
+    case = cases.dam_break_ale(dp=0.02)
+    s = _gpu(gpu_tsph, case, g, scheme=gpu_tsph.ALE_FIRST_ORDER)
+    s.forces(float(g["dt"]))
+    st = s.download()
+    fl = st["type"] == 0
+    for k in RATES:
+        e = _err(st[k][fl], g[f"forces_{k}"][fl])
+        assert e <= _rate_tol(g[f"forces_{k}"][fl]), (k, e)
+    s = _gpu(gpu_tsph, case, g, scheme=gpu_tsph.ALE_FIRST_ORDER)
+    every = int(g["snap_every"])
+    dt = float(g["dt"])
+    rates = {f: g[f"forces_{f}"] for f in RATES}
+    for k in range(every, int(g["nsteps"]) + 1, every):
+        s.step(dt, k - every, every)
+        ref = {f: g[f"step{k}_{f}"] for f in ("r", "v", "rho", "p", "omega", "omegarho",
+                                              "omegav", "domega", "domegarho", "domegav",
+                                              "index")}
+        ref["type"] = g["init_type"]
+        _check_state(s.download(), ref, dt, k, rates, case.cs, tag=f"first-order step{k}")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("scheme", [0, 1, 2])
 def test_ale_fused_equals_per_function_sequence(gpu_tsph, scheme):
     """tsph_ale_step and the reference's RUN order through the per-function
     entry points give bit-identical states (same kernels, same order)."""

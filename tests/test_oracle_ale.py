@@ -127,3 +127,25 @@ def test_ale_oracle_matches_live_reference_dp001(oracle_mod):
     x, y = R.ale_state(), P.ale_state()
     for f in FIELDS + ("grad",):
         assert np.array_equal(x[f], y[f]), f
+
+
+def test_first_order_oracle_matches_reference_golden(oracle_mod):
+    """The first-order driver (cases/ALESPH_dambreakLong/SPH_simulationINT.h,
+    src/RALESPH_interaction.h): fluxes and 6 steps, bit for bit."""
+    O = oracle_mod
+    g = np.load(os.path.join(GOLD, "dam_break_ale_first_order_dp0.02.npz"))
+    case = cases.dam_break_ale(dp=0.02)
+    P = _port(O, case, g)
+    P.density_to_pressure()
+    P.ale_forces_first_order()
+    st = P.ale_state()
+    for k in ("domega", "domegarho", "domegav"):
+        assert np.array_equal(st[k], g[f"forces_{k}"]), k
+    P2 = _port(O, case, g)
+    P2.set_scheme(2)
+    every = int(g["snap_every"])
+    for k in range(every, int(g["nsteps"]) + 1, every):
+        P2.ale_step(float(g["dt"]), k - every, every)
+        st = P2.ale_state()
+        for f in FIELDS:
+            assert np.array_equal(st[f], g[f"step{k}_{f}"]), (k, f)

@@ -556,8 +556,13 @@ struct AleAcc {
     bool any;  // some neighbour with W > 0 (gamma_sum != 0)
 };
 
-// one as-written pair term (src/_testMUSCL_interaction.h:184-296 with
-// MUSCL_final's states: rho_L = rho_a, rho_R = rho_b, v_L = v_R = v_a . n)
+// one pair term.  SCHEME 0 (as written, src/_testMUSCL_interaction.h:184-296
+// with MUSCL_final's states): rho_L = rho_a, rho_R = rho_b, v_L = v_R =
+// v_a . n.  SCHEME 2 (first order, src/RALESPH_interaction.h:132-256): v_R =
+// v_b . n, rho* with densRiemannLinearizedWithLimiter
+// (src/ALESPH_riemann_solver.h:20-34), walls with the linear equation of
+// state Compute_Pressure2 (src/SPH_pressure.h:24-34).
+template <int SCHEME>
 __device__ __forceinline__ void ale_pair(float dx, float dy, float2 va, float sa, float rhoa,
                                          float4 qb, const AleConst &K, AleAcc &acc) {
     const float r2 = fmaf(dx, dx, dy * dy);
@@ -570,7 +575,8 @@ __device__ __forceinline__ void ale_pair(float dx, float dy, float2 va, float sa
     if (qb.w < 0.f) {
         // BT wall: rho* = rho_a (1 + v_a . n_b / c0), pressure along n_b
         const float vn = va.x * qb.x + va.y * qb.y;
-        const float ps = ale_eos(sa + rhoa * vn / K.c0, K);
+        const float sw = sa + rhoa * vn / K.c0;
+        const float ps = SCHEME == 2 ? K.c0 * K.c0 * sw : ale_eos(sw, K);
         const float wdp = W * K.dp;
         acc.dvx = fmaf(-2.f * wdp * ps, qb.x, acc.dvx);
         acc.dvy = fmaf(-2.f * wdp * ps, qb.y, acc.dvy);
@@ -582,14 +588,27 @@ __device__ __forceinline__ void ale_pair(float dx, float dy, float2 va, float sa
     const float sb = qb.z;
     const float ob = qb.w;
     const float nx = -dx * inv_r, ny = -dy * inv_r;
-    // v* = v_L n - (rho_R - rho_L) c0 / (2 rho_bar) n + mean tangential part;
-    // rho* = mean density (v_L = v_R)
-    const float k = -0.5f * (sb - sa) * K.c0 * ale_rcp(K.rho0 + 0.5f * (sa + sb));
-    const float ss = 0.5f * (sa + sb);
+    float vsx, vsy, ss;
+    if (SCHEME == 2) {
+        const float vL = va.x * nx + va.y * ny, vR = qb.x * nx + qb.y * ny;
+        const float rbar = K.rho0 + 0.5f * (sa + sb);
+        const float vss = 0.5f * (vR + vL) - 0.5f * (sb - sa) * K.c0 * ale_rcp(rbar);
+        const float d = vL - vR;
+        const float beta = fminf(3.f * fmaxf(d, 0.f), K.c0);
+        ss = 0.5f * (sa + sb) + 0.5f * beta * d * rbar / (K.c0 * K.c0);
+        const float t = vss - 0.5f * (vL + vR);
+        vsx = fmaf(nx, t, 0.5f * (va.x + qb.x));
+        vsy = fmaf(ny, t, 0.5f * (va.y + qb.y));
+    } else {
+        // v* = v_L n - (rho_R - rho_L) c0 / (2 rho_bar) n + mean tangential
+        // part; rho* = mean density (v_L = v_R)
+        const float k = -0.5f * (sb - sa) * K.c0 * ale_rcp(K.rho0 + 0.5f * (sa + sb));
+        ss = 0.5f * (sa + sb);
+        vsx = fmaf(nx, k, 0.5f * (va.x + qb.x));
+        vsy = fmaf(ny, k, 0.5f * (va.y + qb.y));
+    }
     const float ps = ale_eos(ss, K);
     const float rhos = K.rho0 + ss;
-    const float vsx = fmaf(nx, k, 0.5f * (va.x + qb.x));
-    const float vsy = fmaf(ny, k, 0.5f * (va.y + qb.y));
     const float ex = vsx - va.x, ey = vsy - va.y;
     const float t2 = 2.f * ob;
     acc.dvx = fmaf(-t2, fmaf(fmaf(rhos * vsx, ex, ps), dWx, rhos * vsx * ey * dWy), acc.dvx);
@@ -618,6 +637,7 @@ static __device__ __noinline__ int append_bounded_kAleT(const float2 *loc, uint1
     return cnt;
 }
 
+template <int SCHEME>
 __global__ void __launch_bounds__(kAleT, 8)
 k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                  const uint32_t *__restrict__ wstart, AleWalls Wl, Grid g, AleConst K) {
@@ -775,7 +795,7 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                         const int j = (int)(e >> 4);
                         const float2 o = sm.off[e & 15u];
                         const float2 lb = sm.loc[j];
-                        ale_pair((la.x + o.x) - lb.x, (la.y + o.y) - lb.y, va, sa, rhoa, sm.q[j], K,
+                        ale_pair<SCHEME>((la.x + o.x) - lb.x, (la.y + o.y) - lb.y, va, sa, rhoa, sm.q[j], K,
                                  acc);
                     }
                     done = true;
@@ -805,7 +825,7 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                         const float r2 = fmaf(dx, dx, dy * dy);
                         if (!(r2 <= K.four_h2) || r2 == 0.f) continue;
                         const float2 n = __ldg(Wl.n + j);
-                        ale_pair(dx, dy, va, sa, rhoa, make_float4(-n.x, -n.y, __ldg(Wl.s + j), -1.f),
+                        ale_pair<SCHEME>(dx, dy, va, sa, rhoa, make_float4(-n.x, -n.y, __ldg(Wl.s + j), -1.f),
                                  K, acc);
                     }
                     for (int j = (int)__ldg(fstart + c); j < (int)__ldg(fstart + c + 1); j++) {
@@ -815,7 +835,7 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                         const float r2 = fmaf(dx, dx, dy * dy);
                         if (!(r2 <= K.four_h2) || r2 == 0.f) continue;
                         const float2 vb = __ldg(F.v + j);
-                        ale_pair(dx, dy, va, sa, rhoa,
+                        ale_pair<SCHEME>(dx, dy, va, sa, rhoa,
                                  make_float4(vb.x, vb.y, __ldg(F.s + j), (float)__ldg(F.om + j)), K,
                                  acc);
                     }
@@ -1115,8 +1135,10 @@ class AleEngine {
     int forces(std::string &err) {
         if (scheme == TSPH_ALE_MUSCL)
             k_ale_flux<1><<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
+        else if (scheme == TSPH_ALE_FIRST_ORDER)
+            k_ale_flux_tiled<2><<<nblk(nf, kAleT), kAleT, 0, st>>>(A, fstart, wstart, W, grid, K);
         else
-            k_ale_flux_tiled<<<nblk(nf, kAleT), kAleT, 0, st>>>(A, fstart, wstart, W, grid, K);
+            k_ale_flux_tiled<0><<<nblk(nf, kAleT), kAleT, 0, st>>>(A, fstart, wstart, W, grid, K);
         ACK(cudaGetLastError());
         return 0;
     }
@@ -1414,7 +1436,7 @@ int tsph_ale_add_particles(tsph_ale_system *s, int n, const int32_t *type, const
 
 int tsph_ale_set_scheme(tsph_ale_system *s, int scheme) {
     if (!s) return afail(TSPH_ERR_ARG, "null system handle");
-    if (scheme != TSPH_ALE_AS_WRITTEN && scheme != TSPH_ALE_MUSCL)
+    if (scheme != TSPH_ALE_AS_WRITTEN && scheme != TSPH_ALE_MUSCL && scheme != TSPH_ALE_FIRST_ORDER)
         return afail(TSPH_ERR_ARG, "unknown scheme");
     s->e.scheme = scheme;
     return TSPH_OK;

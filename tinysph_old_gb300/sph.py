@@ -46,6 +46,7 @@ ABI_SYMBOLS = (
 
 ALE_AS_WRITTEN = 0
 ALE_MUSCL = 1
+ALE_FIRST_ORDER = 2
 (ALE_F_R, ALE_F_V, ALE_F_RHO, ALE_F_P, ALE_F_OMEGA, ALE_F_OMEGARHO, ALE_F_OMEGAV, ALE_F_RATES,
  ALE_F_GRAD, ALE_F_INDEX, ALE_F_TYPE) = (1 << k for k in range(11))
 ALE_F_ALL = (1 << 11) - 1
@@ -496,7 +497,8 @@ class AleSystem:
     omega*v (src/RALESPH_integration.h), one-sided MUSCL gradients and the
     linearised-Riemann flux loop (src/_testMUSCL_interaction.h); BT walls with
     a normal each.  ``scheme`` is :data:`ALE_AS_WRITTEN` (the reference's
-    fluxes) or :data:`ALE_MUSCL`."""
+    MUSCL.h fluxes), :data:`ALE_MUSCL` or :data:`ALE_FIRST_ORDER` (the
+    SPH_simulationINT.h driver, src/RALESPH_interaction.h)."""
 
     def __init__(self, h, kap, cs, rho0, visco, delta, dp, domain, stream=None):
         L = load()
