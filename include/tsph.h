@@ -255,6 +255,52 @@ int tsph_autotune(tsph_system *s, int32_t *shape, double us[2]);
 int tsph_set_tile_shape(tsph_system *s, int shape);
 int tsph_set_profiling(tsph_system *s, int on);
 
+/* ---- the particle graph of the learned surrogate (no counterpart in the
+ * reference).  Nodes: walls first, then the live fluid in the system's sorted
+ * order; edges: the pairs within the kernel support (0 < r <= 2h).  All
+ * arrays are DEVICE pointers with room for `capacity` nodes: pos (double2),
+ * vel (float2), srho (rho - rho0), wall (1 for walls), id (particle index),
+ * deg, nbr (k_slots per node, unused slots -1).  TSPH_ERR_UNSUPPORTED if a
+ * node has more than k_slots neighbours. */
+int tsph_export_graph(tsph_system *s, int k_slots, int capacity, void *pos, void *vel,
+                      float *srho, float *wall, int32_t *id, int32_t *deg, int32_t *nbr,
+                      int32_t *n_nodes, int32_t *n_wall);
+/* the surrogate's update of the fluid over k steps (k_dt = k dt), per node of
+ * the last export (device arrays indexed by node): v += (du, dv), rho += ds,
+ * r += k_dt (v_old + v_new) / 2; the cell lists are stale afterwards */
+int tsph_apply_update(tsph_system *s, const float *du, const float *dv, const float *ds,
+                      double k_dt);
+
+/* ---- the surrogate's graph network (no counterpart in the reference): a
+ * two-layer message-passing network of hidden width 64 over an exported
+ * particle graph, predicting per node (du, dv, d(rho - rho0)) over a window of
+ * k SPH steps in units of the graph's scales.  Forward, loss gradient and Adam
+ * run on the device; parameters are FP32, in the order of
+ * oracle/gnn_oracle.py (tsph_gnn_n_params of them). */
+typedef struct tsph_gnn tsph_gnn;
+typedef struct {
+    const void *pos;           /* double2 per node (device) */
+    const void *vel;           /* float2 per node (device) */
+    const float *srho, *wall;  /* rho - rho0, wall flag (device) */
+    const int32_t *deg, *nbr;  /* neighbour table, k_slots per node (device) */
+    int32_t n_nodes, k_slots;
+    double h, u_scale, s_scale;  /* edge length, velocity and density scales */
+    double origin[2];            /* reference point of the FP32 node positions */
+} tsph_gnn_graph;
+int tsph_gnn_n_params(void);
+int tsph_gnn_create(int capacity, void *stream, tsph_gnn **out);
+int tsph_gnn_destroy(tsph_gnn *g);
+int tsph_gnn_set_params(tsph_gnn *g, const float *host);  /* also resets Adam */
+int tsph_gnn_get_params(tsph_gnn *g, float *host);
+int tsph_gnn_get_grads(tsph_gnn *g, float *host);
+/* y (device, 3 per node) may be NULL */
+int tsph_gnn_forward(tsph_gnn *g, const tsph_gnn_graph *graph, float *y);
+/* forward, mean squared error against target (device, 3 per node) over the
+ * fluid nodes, gradient into the network's gradient buffer */
+int tsph_gnn_loss_grad(tsph_gnn *g, const tsph_gnn_graph *graph, const float *target,
+                       double *loss);
+int tsph_gnn_adam(tsph_gnn *g, double lr, double beta1, double beta2, double eps);
+
 /* ---- output and restart
  * write_to_ASCII_VTK (src/SPH_data_to_vtk.h:4-51): the same POLYDATA file
  * (points, type, pressure, density, velocity) in the reference's order. */

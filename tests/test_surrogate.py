@@ -1,0 +1,128 @@
+"""The learned surrogate's pieces: the exported particle graph and the graph
+network's device kernels (forward and gradients) against the numpy oracle
+(oracle/gnn_oracle.py), whose own gradients are checked by central
+differences."""
+
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from tinysph_old_gb300 import cases
+
+sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                                "oracle"))
+import gnn_oracle as G  # noqa: E402
+
+
+def _toy_graph(rng, n=30, K=8, radius=0.35):
+    pos = rng.uniform(0, 1, (n, 2))
+    d = np.linalg.norm(pos[:, None] - pos[None], axis=2)
+    nbr = -np.ones((n, K), int)
+    deg = np.zeros(n, int)
+    for i in range(n):
+        js = [j for j in np.argsort(d[i]) if j != i and d[i, j] < radius][:K]
+        nbr[i, :len(js)] = js
+        deg[i] = len(js)
+    return pos, nbr, deg
+
+
+def test_oracle_gradients_match_central_differences():
+    rng = np.random.default_rng(0)
+    pos, nbr, deg = _toy_graph(rng)
+    n = len(deg)
+    vel = rng.normal(0, 0.3, (n, 2))
+    srho = rng.normal(0, 1, n)
+    wall = (rng.random(n) < 0.2).astype(float)
+    x, ii, jj, e, dg = G.graph_inputs(pos, vel, srho, wall, deg, nbr, 0.2, 1.0, 1.0)
+    p = G.init_params(1)
+    for k in p:
+        p[k] = p[k] + rng.normal(0, 0.05, p[k].shape)
+    target = rng.normal(0, 1, (n, 3))
+    mask = 1 - wall
+    _, g, _ = G.loss_and_grad(p, x, ii, jj, e, dg, target, mask)
+    flat, gf = G.flatten(p), G.flatten(g)
+    for k in rng.choice(len(flat), 60, replace=False):
+        f2 = flat.copy()
+        f2[k] += 1e-6
+        lp = G.loss_and_grad(G.unflatten(f2), x, ii, jj, e, dg, target, mask)[0]
+        f2[k] -= 2e-6
+        lm = G.loss_and_grad(G.unflatten(f2), x, ii, jj, e, dg, target, mask)[0]
+        fd = (lp - lm) / 2e-6
+        assert abs(fd - gf[k]) <= 1e-4 * max(1e-6, abs(fd) + abs(gf[k])), (k, fd, gf[k])
+
+
+@pytest.mark.gpu
+def test_exported_graph_is_the_symmetric_pair_set(gpu_tsph):
+    from tinysph_old_gb300 import surrogate as S
+
+    case = cases.dam_break_mdbc(dp=0.02)
+    s = gpu_tsph.ParticleSystem.from_case(case)
+    s.step(0, case.dt, 5)
+    gb = S.GraphBuffers(case.np + 16).export(s)
+    hst = gb.host()
+    st = s.download()
+    n = gb.n
+    assert n == case.np and gb.nw == int(np.sum(st["type"] == 1))
+    # node data against the state (reference order by particle index)
+    order = hst["id"]
+    assert np.array_equal(np.sort(order), np.arange(n))
+    assert np.array_equal(hst["pos"], st["r"][order])
+    assert np.allclose(hst["vel"], st["v"][order], atol=1e-7)
+    assert np.array_equal(hst["wall"], (st["type"][order] == 1).astype(float))
+    # edges: symmetric, within 2h, and every pair within 2h (minus a rounding band)
+    edges = {(i, int(j)) for i in range(n) for j in hst["nbr"][i, :hst["deg"][i]]}
+    assert all((j, i) in edges for i, j in edges)
+    r = hst["pos"]
+    d = np.linalg.norm(r[:, None] - r[None], axis=2)
+    two_h = 2 * case.h
+    inside = {(i, j) for i in range(n) for j in np.nonzero((d[i] < two_h * (1 - 1e-6)) & (d[i] > 0))[0]}
+    assert inside <= edges
+    assert all(d[i, j] <= two_h * (1 + 1e-6) for i, j in edges)
+
+
+@pytest.mark.gpu
+def test_gnn_forward_and_gradients_match_the_oracle(gpu_tsph):
+    import torch
+
+    from tinysph_old_gb300 import surrogate as S
+
+    case = cases.dam_break_mdbc(dp=0.02)
+    s = gpu_tsph.ParticleSystem.from_case(case)
+    rng = np.random.default_rng(4)
+    st = s.download()
+    fl = st["type"] == 0
+    v = st["v"].copy()
+    v[fl] = rng.normal(0, 0.5, (fl.sum(), 2))
+    rho = st["rho"].copy()
+    rho[fl] += rng.normal(0, 2.0, fl.sum())
+    s.upload(v=v, rho=rho)
+    gb = S.GraphBuffers(case.np).export(s)
+    hst = gb.host()
+    U, Sc, h = 1.0, 2.0, case.h
+    origin = hst["pos"].mean(0)
+    p = G.init_params(7)
+    for k in p:
+        p[k] = p[k] + rng.normal(0, 0.05, p[k].shape)
+    net = gpu_tsph.Gnn(gb.n)
+    net.set_params(G.flatten(p).astype(np.float32))
+    p32 = G.unflatten(net.params().astype(np.float64))  # the FP32-rounded weights
+    target = rng.normal(0, 1, (gb.n, 3))
+    tgt = torch.tensor(target, dtype=torch.float32, device="cuda")
+    graph = gb.struct(h, U, Sc, tuple(origin))
+    loss = net.loss_grad(graph, tgt.data_ptr())
+    y_dev = torch.empty((gb.n, 3), dtype=torch.float32, device="cuda")
+    net.forward(graph, y_dev.data_ptr())
+    torch.cuda.synchronize()
+    x, ii, jj, e, dg = G.graph_inputs(hst["pos"], hst["vel"], hst["srho"], hst["wall"],
+                                      hst["deg"], hst["nbr"], h, U, Sc)
+    lref, gref, yref = G.loss_and_grad(p32, x, ii, jj, e, dg, target, 1 - hst["wall"])
+    y = y_dev.cpu().numpy()
+    assert np.max(np.abs(y - yref)) <= 1e-4 * max(1.0, np.max(np.abs(yref)))
+    assert abs(loss - lref) <= 1e-4 * lref
+    gdev = G.unflatten(net.grads().astype(np.float64))
+    for name, _ in G.param_shapes():
+        ref = gref[name]
+        err = np.max(np.abs(gdev[name] - ref))
+        assert err <= 2e-3 * max(1e-6, np.max(np.abs(ref))), (name, err, np.max(np.abs(ref)))

@@ -31,6 +31,7 @@ UNITS = [
     ("tsph_noalloc.cu", []),
     ("tsph_ale.cu", []),
     ("tsph_io.cu", []),
+    ("tsph_gnn.cu", []),
 ]
 
 

@@ -447,6 +447,31 @@ int tsph_water_front(tsph_system *s, double y_max, double *x_front) {
     return TSPH_OK;
 }
 
+int tsph_export_graph(tsph_system *s, int k_slots, int capacity, void *pos, void *vel,
+                      float *srho, float *wall, int32_t *id, int32_t *deg, int32_t *nbr,
+                      int32_t *n_nodes, int32_t *n_wall) {
+    NEED(s);
+    if (k_slots < 1 || capacity < 0 || !pos || !vel || !srho || !wall || !id || !deg || !nbr ||
+        !n_nodes || !n_wall)
+        return fail(TSPH_ERR_ARG, "bad arguments");
+    ENGINE(s);
+    int n = 0, nw = 0;
+    RUN(s->eng->export_graph(k_slots, capacity, static_cast<double2 *>(pos),
+                             static_cast<float2 *>(vel), srho, wall, id, deg, nbr, &n, &nw, err_));
+    *n_nodes = n;
+    *n_wall = nw;
+    return TSPH_OK;
+}
+
+int tsph_apply_update(tsph_system *s, const float *du, const float *dv, const float *ds,
+                      double k_dt) {
+    NEED(s);
+    if (!du || !dv || !ds) return fail(TSPH_ERR_ARG, "null update");
+    ENGINE(s);
+    RUN(s->eng->apply_update(du, dv, ds, k_dt, err_));
+    return TSPH_OK;
+}
+
 int tsph_autotune(tsph_system *s, int32_t *shape, double us[2]) {
     NEED(s);
     ENGINE(s);

@@ -13,6 +13,7 @@
 #include "tsph_kernels.cuh"
 #include "tsph_pairs_tiled.cuh"
 #include "tsph_probes.cuh"
+#include "tsph_graph.cuh"
 #include "tsph_grid_host.h"
 
 namespace tsph {
@@ -60,6 +61,7 @@ template <typename T> class Engine final : public EngineBase {
     long long *tmp_y_ = nullptr;
     uint32_t *health_ = nullptr, *removed_ = nullptr;
     uint32_t *rebuild_ = nullptr;  // set when the fused step must re-bin after the predictor
+    bool exported_ = false;        // the sorted order is that of the last export_graph
     bool capturing_ = false;       // enqueue_step is being captured into a graph
     cudaStream_t st2_ = nullptr;   // side stream: captures the conditional re-binning body
     float skin_ = 0.f;             // per-axis move allowed without re-binning (FP32 fused step)
@@ -263,6 +265,57 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int tile_shape() const override { return tile_shape_; }
+
+    int export_graph(int K, int cap, double2 *pos, float2 *vel, float *srho, float *wall,
+                     int32_t *id, int32_t *deg, int32_t *nbr, int *n_nodes, int *n_wall,
+                     std::string &err) override {
+        if (!cells_) {
+            err = "cell lists are stale: call tsph_particle_to_cell first";
+            return 3;
+        }
+        uint32_t nl = 0;
+        TSPH_CK(cudaMemcpyAsync(&nl, fstart_ + ncells_, 4, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        const int n = nw_ + (int)nl;
+        *n_nodes = n;
+        *n_wall = nw_;
+        if (n > cap) {
+            err = "graph capacity " + std::to_string(cap) + " < " + std::to_string(n) + " nodes";
+            return 1;
+        }
+        int rc;
+        TSPH_CK(cudaMemsetAsync(removed_, 0, 4, st_));
+        if ((rc = launch(CAT_OTHER, k_graph_export<T>, blocks_for(n), kBlock, err, F_,
+                         (const uint32_t *)fstart_, (const uint32_t *)wstart_, W_, nw_, grid_,
+                         P_.rho0, (float)(4.0 * P_.hd * P_.hd), K, pos, vel, srho, wall, id, deg,
+                         nbr, removed_)))
+            return rc;
+        uint32_t ovf = 0;
+        TSPH_CK(cudaMemcpyAsync(&ovf, removed_, 4, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaMemsetAsync(removed_, 0, 4, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        if (ovf) {
+            err = "a node has more than " + std::to_string(K) + " neighbours";
+            return 8;
+        }
+        exported_ = true;
+        return collect_profile(err);
+    }
+
+    int apply_update(const float *du, const float *dv, const float *ds, double kdt,
+                     std::string &err) override {
+        if (!exported_ || !cells_) {
+            err = "apply_update needs the order of the last export_graph (no re-binning since)";
+            return 3;
+        }
+        int rc;
+        if ((rc = launch(CAT_OTHER, k_apply_update<T>, blocks_for(nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, ncells_, nw_, du, dv, ds, kdt, health_)))
+            return rc;
+        cells_ = false;
+        exported_ = false;
+        return collect_profile(err);
+    }
 
     int set_tile_shape(int shape, std::string &err) override {
         if (shape < 0 || shape > 1) {
@@ -682,6 +735,7 @@ template <typename T> class Engine final : public EngineBase {
         TSPH_CK(cudaMemcpyAsync(O_.v, Bv_, sizeof(T2) * n, cudaMemcpyDeviceToDevice, st_));
         TSPH_CK(cudaMemcpyAsync(O_.rho, Brho_, sizeof(T) * n, cudaMemcpyDeviceToDevice, st_));
         cells_ = true;
+        exported_ = false;
         return collect_profile(err);
     }
 
@@ -795,6 +849,7 @@ template <typename T> class Engine final : public EngineBase {
                          (const uint32_t *)fstart_, ncells_, W_, nw_, P_, health_)))
             return rc;
         cells_ = true;
+        exported_ = false;
         return collect_profile(err);
     }
 

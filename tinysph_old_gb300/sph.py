@@ -38,6 +38,9 @@ ABI_SYMBOLS = (
     "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
     "tsph_water_level", "tsph_point_fields", "tsph_water_front", "tsph_autotune",
     "tsph_set_tile_shape", "tsph_write_vtk", "tsph_save_checkpoint", "tsph_load_checkpoint",
+    "tsph_export_graph", "tsph_apply_update", "tsph_gnn_n_params", "tsph_gnn_create",
+    "tsph_gnn_destroy", "tsph_gnn_set_params", "tsph_gnn_get_params", "tsph_gnn_get_grads",
+    "tsph_gnn_forward", "tsph_gnn_loss_grad", "tsph_gnn_adam",
     "tsph_ale_create", "tsph_ale_destroy", "tsph_ale_add_particles", "tsph_ale_set_scheme",
     "tsph_ale_np", "tsph_ale_divide_to_cells", "tsph_ale_particle_to_cell", "tsph_ale_gradient",
     "tsph_ale_forces", "tsph_ale_leapfrog_one", "tsph_ale_leapfrog_two", "tsph_ale_step",
@@ -76,6 +79,14 @@ class _AleHostState(C.Structure):
     _fields_ = [(n, C.c_void_p) for n in ("r", "v", "rho", "p", "omega", "omegarho", "omegav",
                                           "domega", "domegarho", "domegav", "grad", "index",
                                           "type")]
+
+
+class GnnGraph(C.Structure):
+    """tsph_gnn_graph: device pointers of an exported particle graph."""
+    _fields_ = [("pos", C.c_void_p), ("vel", C.c_void_p), ("srho", C.c_void_p),
+                ("wall", C.c_void_p), ("deg", C.c_void_p), ("nbr", C.c_void_p),
+                ("n_nodes", C.c_int32), ("k_slots", C.c_int32), ("h", C.c_double),
+                ("u_scale", C.c_double), ("s_scale", C.c_double), ("origin", C.c_double * 2)]
 
 
 class _Profile(C.Structure):
@@ -140,6 +151,17 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_autotune.argtypes = [P, P, P]
     L.tsph_set_tile_shape.argtypes = [P, I]
     L.tsph_write_vtk.argtypes = [P, C.c_char_p]
+    L.tsph_export_graph.argtypes = [P, I, I] + [P] * 7 + [C.POINTER(C.c_int32)] * 2
+    L.tsph_apply_update.argtypes = [P, P, P, P, D]
+    L.tsph_gnn_n_params.restype = I
+    L.tsph_gnn_create.argtypes = [I, P, C.POINTER(P)]
+    L.tsph_gnn_destroy.argtypes = [P]
+    L.tsph_gnn_set_params.argtypes = [P, P]
+    L.tsph_gnn_get_params.argtypes = [P, P]
+    L.tsph_gnn_get_grads.argtypes = [P, P]
+    L.tsph_gnn_forward.argtypes = [P, C.POINTER(GnnGraph), P]
+    L.tsph_gnn_loss_grad.argtypes = [P, C.POINTER(GnnGraph), P, C.POINTER(D)]
+    L.tsph_gnn_adam.argtypes = [P, D, D, D, D]
     L.tsph_save_checkpoint.argtypes = [P, C.c_char_p]
     L.tsph_load_checkpoint.argtypes = [C.c_char_p, P, C.POINTER(P)]
     L.tsph_ale_create.argtypes = [C.POINTER(_Constants), C.POINTER(_Domain), P, C.POINTER(P)]
@@ -422,6 +444,17 @@ class ParticleSystem:
         s.domain = None
         return s
 
+    def export_graph(self, k_slots, capacity, pos, vel, srho, wall, id_, deg, nbr):
+        """Device pointers (ints) -> (n_nodes, n_wall); see tsph_export_graph."""
+        n, nw = C.c_int32(), C.c_int32()
+        _check(self._L.tsph_export_graph(self._h, int(k_slots), int(capacity), pos, vel, srho,
+                                         wall, id_, deg, nbr, C.byref(n), C.byref(nw)))
+        return n.value, nw.value
+
+    def apply_update(self, du, dv, ds, k_dt):
+        """Device pointers of the per-node update; see tsph_apply_update."""
+        _check(self._L.tsph_apply_update(self._h, du, dv, ds, float(k_dt)))
+
     def autotune(self):
         """Time both tile shapes of the pair kernel, keep the faster:
         (shape, [us shape 0, us shape 1])."""
@@ -645,3 +678,51 @@ def Integrate_LeapFrog_partOne(particles: AleSystem, dt):
 
 def Integrate_LeapFrog_partTwo(particles: AleSystem, dt, step):
     particles.leapfrog_two(dt, step)
+
+
+class Gnn:
+    """The surrogate's graph network on the device (tsph_gnn_*)."""
+
+    def __init__(self, capacity, stream=None):
+        self._L = load()
+        h_ = C.c_void_p()
+        _check(self._L.tsph_gnn_create(int(capacity), stream, C.byref(h_)))
+        self._h = h_
+        self.n_params = self._L.tsph_gnn_n_params()
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.tsph_gnn_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_params(self, flat):
+        a = np.ascontiguousarray(flat, dtype=np.float32)
+        assert a.size == self.n_params
+        _check(self._L.tsph_gnn_set_params(self._h, _p(a)))
+
+    def params(self):
+        out = np.empty(self.n_params, dtype=np.float32)
+        _check(self._L.tsph_gnn_get_params(self._h, _p(out)))
+        return out
+
+    def grads(self):
+        out = np.empty(self.n_params, dtype=np.float32)
+        _check(self._L.tsph_gnn_get_grads(self._h, _p(out)))
+        return out
+
+    def forward(self, graph, y_ptr=None):
+        _check(self._L.tsph_gnn_forward(self._h, C.byref(graph), y_ptr))
+
+    def loss_grad(self, graph, target_ptr):
+        l = C.c_double()
+        _check(self._L.tsph_gnn_loss_grad(self._h, C.byref(graph), target_ptr, C.byref(l)))
+        return l.value
+
+    def adam(self, lr, beta1=0.9, beta2=0.999, eps=1e-8):
+        _check(self._L.tsph_gnn_adam(self._h, float(lr), float(beta1), float(beta2), float(eps)))
