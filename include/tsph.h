@@ -260,16 +260,43 @@ int tsph_set_profiling(tsph_system *s, int on);
  * order; edges: the pairs within the kernel support (0 < r <= 2h).  All
  * arrays are DEVICE pointers with room for `capacity` nodes: pos (double2),
  * vel (float2), srho (rho - rho0), wall (1 for walls), id (particle index),
- * deg, nbr (k_slots per node, unused slots -1).  TSPH_ERR_UNSUPPORTED if a
- * node has more than k_slots neighbours. */
+ * deg, nbr (k_slots per node, unused slots -1); acc (float2) and rate (float)
+ * may be NULL, else they receive the rates of the last forces pass, a and
+ * d(rho)/dt (zero for walls).  TSPH_ERR_UNSUPPORTED if a node has more than
+ * k_slots neighbours. */
 int tsph_export_graph(tsph_system *s, int k_slots, int capacity, void *pos, void *vel,
                       float *srho, float *wall, int32_t *id, int32_t *deg, int32_t *nbr,
-                      int32_t *n_nodes, int32_t *n_wall);
-/* the surrogate's update of the fluid over k steps (k_dt = k dt), per node of
- * the last export (device arrays indexed by node): v += (du, dv), rho += ds,
- * r += k_dt (v_old + v_new) / 2; the cell lists are stale afterwards */
-int tsph_apply_update(tsph_system *s, const float *du, const float *dv, const float *ds,
-                      double k_dt);
+                      void *acc, float *rate, int32_t *n_nodes, int32_t *n_wall);
+/* the surrogate's update of the fluid over a window of k steps (k_dt = k dt),
+ * from y (device, 3 floats per node of the last export), with a, drho/dt
+ * those of the last forces pass:
+ *   phase 0 (explicit):  v_new = v + add_rates k_dt a + u_scale (y0, y1),
+ *                        rho_new = rho + add_rates k_dt drho/dt + s_scale y2,
+ *                        r += k_dt (v + v_new) / 2;
+ *   phase 1 (kick):      v_new as in phase 0; rho and r unchanged (the cell
+ *                        lists stay valid, for a forces pass with v_new);
+ *   phase 2 (drift, after a kick and a forces pass):
+ *                        rho += add_rates k_dt drho/dt + s_scale y2 with the
+ *                        rate of that pass, r += k_dt (v_start + v_new) / 2.
+ * Phases 0 and 1 record, per particle, the start-of-window terms of the
+ * window check (tsph_window_check).  The cell lists are stale after phases 0
+ * and 2. */
+int tsph_apply_update(tsph_system *s, const float *y, double u_scale, double s_scale,
+                      double k_dt, int add_rates, int phase);
+/* the per-window check of a surrogate window, after a forces pass at the
+ * window's end state: against the trapezoidal rule of the SPH rates at both
+ * ends, rho_c = rho_0 + k_dt (drho_0 + drho_1) / 2 and
+ * v_c = v_0 + k_dt (a_0 + a_1) / 2, per fluid particle,
+ *   out[0] = max |rho - rho_c| / rho0,  out[1] = rms |rho - rho_c| / rho0,
+ *   out[2] = |sum m (v - v_c)| / (M g k_dt)  (momentum, against gravity's
+ *            impulse on the fluid mass M over the window),
+ *   out[3] = the number of fluid particles checked,
+ *   out[4] = the particle index of the largest density error. */
+int tsph_window_check(tsph_system *s, double k_dt, double out[5]);
+/* a device-side copy of the whole particle state (the start of a surrogate
+ * window) and its restoration (the plain-step fallback). */
+int tsph_state_save(tsph_system *s);
+int tsph_state_restore(tsph_system *s);
 
 /* ---- the surrogate's graph network (no counterpart in the reference): a
  * two-layer message-passing network of hidden width 64 over an exported
@@ -285,7 +312,6 @@ typedef struct {
     const int32_t *deg, *nbr;  /* neighbour table, k_slots per node (device) */
     int32_t n_nodes, k_slots;
     double h, u_scale, s_scale;  /* edge length, velocity and density scales */
-    double origin[2];            /* reference point of the FP32 node positions */
 } tsph_gnn_graph;
 int tsph_gnn_n_params(void);
 int tsph_gnn_create(int capacity, void *stream, tsph_gnn **out);

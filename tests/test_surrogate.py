@@ -101,7 +101,6 @@ def test_gnn_forward_and_gradients_match_the_oracle(gpu_tsph):
     gb = S.GraphBuffers(case.np).export(s)
     hst = gb.host()
     U, Sc, h = 1.0, 2.0, case.h
-    origin = hst["pos"].mean(0)
     p = G.init_params(7)
     for k in p:
         p[k] = p[k] + rng.normal(0, 0.05, p[k].shape)
@@ -110,7 +109,7 @@ def test_gnn_forward_and_gradients_match_the_oracle(gpu_tsph):
     p32 = G.unflatten(net.params().astype(np.float64))  # the FP32-rounded weights
     target = rng.normal(0, 1, (gb.n, 3))
     tgt = torch.tensor(target, dtype=torch.float32, device="cuda")
-    graph = gb.struct(h, U, Sc, tuple(origin))
+    graph = gb.struct(h, U, Sc)
     loss = net.loss_grad(graph, tgt.data_ptr())
     y_dev = torch.empty((gb.n, 3), dtype=torch.float32, device="cuda")
     net.forward(graph, y_dev.data_ptr())

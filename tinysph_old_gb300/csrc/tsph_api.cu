@@ -449,7 +449,7 @@ int tsph_water_front(tsph_system *s, double y_max, double *x_front) {
 
 int tsph_export_graph(tsph_system *s, int k_slots, int capacity, void *pos, void *vel,
                       float *srho, float *wall, int32_t *id, int32_t *deg, int32_t *nbr,
-                      int32_t *n_nodes, int32_t *n_wall) {
+                      void *acc, float *rate, int32_t *n_nodes, int32_t *n_wall) {
     NEED(s);
     if (k_slots < 1 || capacity < 0 || !pos || !vel || !srho || !wall || !id || !deg || !nbr ||
         !n_nodes || !n_wall)
@@ -457,18 +457,42 @@ int tsph_export_graph(tsph_system *s, int k_slots, int capacity, void *pos, void
     ENGINE(s);
     int n = 0, nw = 0;
     RUN(s->eng->export_graph(k_slots, capacity, static_cast<double2 *>(pos),
-                             static_cast<float2 *>(vel), srho, wall, id, deg, nbr, &n, &nw, err_));
+                             static_cast<float2 *>(vel), srho, wall, id, deg, nbr,
+                             static_cast<float2 *>(acc), rate, &n, &nw, err_));
     *n_nodes = n;
     *n_wall = nw;
     return TSPH_OK;
 }
 
-int tsph_apply_update(tsph_system *s, const float *du, const float *dv, const float *ds,
-                      double k_dt) {
+int tsph_apply_update(tsph_system *s, const float *y, double u_scale, double s_scale,
+                      double k_dt, int add_rates, int phase) {
     NEED(s);
-    if (!du || !dv || !ds) return fail(TSPH_ERR_ARG, "null update");
+    if (!y) return fail(TSPH_ERR_ARG, "null update");
+    if (phase < 0 || phase > 2) return fail(TSPH_ERR_ARG, "phase must be 0, 1 or 2");
     ENGINE(s);
-    RUN(s->eng->apply_update(du, dv, ds, k_dt, err_));
+    RUN(s->eng->apply_update(y, u_scale, s_scale, k_dt, add_rates != 0, phase, err_));
+    return TSPH_OK;
+}
+
+int tsph_window_check(tsph_system *s, double k_dt, double out[5]) {
+    NEED(s);
+    if (!out) return fail(TSPH_ERR_ARG, "null output");
+    ENGINE(s);
+    RUN(s->eng->window_check(k_dt, out, err_));
+    return TSPH_OK;
+}
+
+int tsph_state_save(tsph_system *s) {
+    NEED(s);
+    ENGINE(s);
+    RUN(s->eng->state_save(err_));
+    return TSPH_OK;
+}
+
+int tsph_state_restore(tsph_system *s) {
+    NEED(s);
+    ENGINE(s);
+    RUN(s->eng->state_restore(err_));
     return TSPH_OK;
 }
 

@@ -62,6 +62,13 @@ template <typename T> class Engine final : public EngineBase {
     uint32_t *health_ = nullptr, *removed_ = nullptr;
     uint32_t *rebuild_ = nullptr;  // set when the fused step must re-bin after the predictor
     bool exported_ = false;        // the sorted order is that of the last export_graph
+    WindowRef wref_{};             // start-of-window terms of the surrogate's check
+    double *wout_ = nullptr;       // its reductions
+    FluidState<T> Fsv_{};          // the saved state (tsph_state_save)
+    T *wsv_ = nullptr;             // saved wall rho, drho, p, rho_o (4 nw)
+    uint32_t *fstart_sv_ = nullptr;
+    bool saved_ = false, saved_cells_ = false;
+    bool kicked_ = false;          // a kick (apply_update phase 1) awaits its drift
     bool capturing_ = false;       // enqueue_step is being captured into a graph
     cudaStream_t st2_ = nullptr;   // side stream: captures the conditional re-binning body
     float skin_ = 0.f;             // per-axis move allowed without re-binning (FP32 fused step)
@@ -267,8 +274,8 @@ template <typename T> class Engine final : public EngineBase {
     int tile_shape() const override { return tile_shape_; }
 
     int export_graph(int K, int cap, double2 *pos, float2 *vel, float *srho, float *wall,
-                     int32_t *id, int32_t *deg, int32_t *nbr, int *n_nodes, int *n_wall,
-                     std::string &err) override {
+                     int32_t *id, int32_t *deg, int32_t *nbr, float2 *acc, float *rate,
+                     int *n_nodes, int *n_wall, std::string &err) override {
         if (!cells_) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
@@ -288,7 +295,7 @@ template <typename T> class Engine final : public EngineBase {
         if ((rc = launch(CAT_OTHER, k_graph_export<T>, blocks_for(n), kBlock, err, F_,
                          (const uint32_t *)fstart_, (const uint32_t *)wstart_, W_, nw_, grid_,
                          P_.rho0, (float)(4.0 * P_.hd * P_.hd), K, pos, vel, srho, wall, id, deg,
-                         nbr, removed_)))
+                         nbr, acc, rate, removed_)))
             return rc;
         uint32_t ovf = 0;
         TSPH_CK(cudaMemcpyAsync(&ovf, removed_, 4, cudaMemcpyDeviceToHost, st_));
@@ -299,22 +306,104 @@ template <typename T> class Engine final : public EngineBase {
             return 8;
         }
         exported_ = true;
+        kicked_ = false;
         return collect_profile(err);
     }
 
-    int apply_update(const float *du, const float *dv, const float *ds, double kdt,
+    int apply_update(const float *y, double su, double ss, double kdt, bool add_rates, int phase,
                      std::string &err) override {
         if (!exported_ || !cells_) {
             err = "apply_update needs the order of the last export_graph (no re-binning since)";
             return 3;
         }
+        if (phase == 2 && !kicked_) {
+            err = "the drift phase follows a kick (phase 1) and a forces pass";
+            return 3;
+        }
         int rc;
+        if (!wref_.rho) {
+            const size_t n = (size_t)ntot_;
+            if ((rc = alloc(&wref_.rho, n, err)) || (rc = alloc(&wref_.v, n, err)) ||
+                (rc = alloc(&wref_.drho, n, err)) || (rc = alloc(&wref_.a, n, err)) ||
+                (rc = alloc(&wout_, 7, err)))
+                return rc;
+        }
         if ((rc = launch(CAT_OTHER, k_apply_update<T>, blocks_for(nf_), kBlock, err, F_,
-                         (const uint32_t *)fstart_, ncells_, nw_, du, dv, ds, kdt, health_)))
+                         (const uint32_t *)fstart_, ncells_, nw_, y, (float)su, (float)ss, kdt,
+                         add_rates ? 1 : 0, phase, P_.rho0, wref_, health_)))
             return rc;
-        cells_ = false;
-        exported_ = false;
+        kicked_ = phase == 1;
+        if (phase != 1) {
+            cells_ = false;
+            exported_ = false;
+        }
         return collect_profile(err);
+    }
+
+    int window_check(double kdt, double out[5], std::string &err) override {
+        if (!wref_.rho) {
+            err = "no surrogate window was applied";
+            return 3;
+        }
+        if (!cells_) {
+            err = "cell lists are stale: the check follows a forces pass at the window's end";
+            return 3;
+        }
+        int rc;
+        TSPH_CK(cudaMemsetAsync(wout_, 0, 7 * sizeof(double), st_));
+        if ((rc = launch(CAT_OTHER, k_window_check<T>, blocks_for(nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, ncells_, kdt, P_.rho0, wref_, wout_)))
+            return rc;
+        double h[7];
+        TSPH_CK(cudaMemcpyAsync(h, wout_, sizeof h, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        const double rho0 = (double)P_.rho0, cnt = h[5] > 0 ? h[5] : 1.0;
+        out[0] = h[0] / rho0;
+        out[1] = std::sqrt(h[1] / cnt) / rho0;
+        // momentum error per particle against gravity's impulse over the window
+        const double gk = (double)P_.g * kdt * cnt;
+        out[2] = std::sqrt(h[2] * h[2] + h[3] * h[3]) / (gk > 0 ? gk : 1e-300);
+        out[3] = h[5];
+        unsigned long long w;
+        std::memcpy(&w, &h[6], 8);
+        out[4] = (double)(uint32_t)(w & 0xffffffffull);
+        return collect_profile(err);
+    }
+
+    int state_save(std::string &err) override {
+        int rc;
+        const size_t n = (size_t)nf_, nw = (size_t)nw_;
+        if (!saved_) {
+            if ((rc = alloc(&Fsv_.r, n, err)) || (rc = alloc(&Fsv_.v, n, err)) ||
+                (rc = alloc(&Fsv_.a, n, err)) || (rc = alloc(&Fsv_.rho, n, err)) ||
+                (rc = alloc(&Fsv_.drho, n, err)) || (rc = alloc(&Fsv_.p, n, err)) ||
+                (rc = alloc(&Fsv_.id, n, err)) || (rc = alloc(&Fsv_.key, n, err)) ||
+                (rc = alloc(&Fsv_.loc, n, err)) || (rc = alloc(&wsv_, 4 * nw, err)) ||
+                (rc = alloc(&fstart_sv_, (size_t)ncells_ + 1, err)))
+                return rc;
+        }
+        copy_state(Fsv_, F_, wsv_, false);
+        TSPH_CK(cudaMemcpyAsync(fstart_sv_, fstart_, 4 * ((size_t)ncells_ + 1),
+                                cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaGetLastError());
+        saved_ = true;
+        saved_cells_ = cells_;
+        return 0;
+    }
+
+    int state_restore(std::string &err) override {
+        if (!saved_) {
+            err = "no saved state";
+            return 3;
+        }
+        copy_state(F_, Fsv_, wsv_, true);
+        TSPH_CK(cudaMemcpyAsync(fstart_, fstart_sv_, 4 * ((size_t)ncells_ + 1),
+                                cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaGetLastError());
+        cells_ = saved_cells_;
+        exported_ = false;
+        kicked_ = false;
+        return 0;
     }
 
     int set_tile_shape(int shape, std::string &err) override {
@@ -329,6 +418,27 @@ template <typename T> class Engine final : public EngineBase {
     }
 
   private:
+    // fluid rows and the evolving wall fields, between the live state and the
+    // saved copy (to_live: saved -> live)
+    void copy_state(FluidState<T> &dst, const FluidState<T> &src, T *wsv, bool to_live) {
+        const size_t n = (size_t)nf_, nw = (size_t)nw_;
+        const auto D = cudaMemcpyDeviceToDevice;
+        cudaMemcpyAsync(dst.r, src.r, 16 * n, D, st_);
+        cudaMemcpyAsync(dst.v, src.v, sizeof(T2) * n, D, st_);
+        cudaMemcpyAsync(dst.a, src.a, sizeof(T2) * n, D, st_);
+        cudaMemcpyAsync(dst.rho, src.rho, sizeof(T) * n, D, st_);
+        cudaMemcpyAsync(dst.drho, src.drho, sizeof(T) * n, D, st_);
+        cudaMemcpyAsync(dst.p, src.p, sizeof(T) * n, D, st_);
+        cudaMemcpyAsync(dst.id, src.id, 4 * n, D, st_);
+        cudaMemcpyAsync(dst.key, src.key, 4 * n, D, st_);
+        cudaMemcpyAsync(dst.loc, src.loc, 8 * n, D, st_);
+        T *wl[4] = {W_.rho, W_.drho, W_.p, W_.rho_o};
+        for (int k = 0; k < 4; k++) {
+            if (to_live) cudaMemcpyAsync(wl[k], wsv + k * nw, sizeof(T) * nw, D, st_);
+            else cudaMemcpyAsync(wsv + k * nw, wl[k], sizeof(T) * nw, D, st_);
+        }
+    }
+
 
     // the fluid-row pair pass: tiled FP32 kernel, or the plain FP64 kernel.
     // `skinned`: the cells are those of the binning before the predictor.

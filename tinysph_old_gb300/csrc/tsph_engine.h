@@ -67,10 +67,13 @@ class EngineBase {
     virtual int tile_shape() const = 0;
     // the particle graph and the surrogate's window update (device pointers)
     virtual int export_graph(int K, int cap, double2 *pos, float2 *vel, float *srho, float *wall,
-                             int32_t *id, int32_t *deg, int32_t *nbr, int *n_nodes, int *n_wall,
-                             std::string &err) = 0;
-    virtual int apply_update(const float *du, const float *dv, const float *ds, double kdt,
-                             std::string &err) = 0;
+                             int32_t *id, int32_t *deg, int32_t *nbr, float2 *acc, float *rate,
+                             int *n_nodes, int *n_wall, std::string &err) = 0;
+    virtual int apply_update(const float *y, double su, double ss, double kdt, bool add_rates,
+                             int phase, std::string &err) = 0;
+    virtual int window_check(double kdt, double out[5], std::string &err) = 0;
+    virtual int state_save(std::string &err) = 0;
+    virtual int state_restore(std::string &err) = 0;
     virtual int sync(std::string &err) = 0;
     virtual void set_profiling(bool on) = 0;
     virtual Profile profile(bool reset) = 0;

@@ -19,6 +19,7 @@
 // in a fixed order (deterministic).
 #include <cmath>
 #include <cstdint>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -70,7 +71,7 @@ struct Layout {
 };
 
 struct GraphDev {
-    const float2 *pos;  // relative to a reference point, FP32
+    const double2 *pos;
     const float2 *vel;
     const float *srho, *wall;
     const int32_t *deg, *nbr;
@@ -78,9 +79,12 @@ struct GraphDev {
     float inv_h, inv_U, inv_S;
 };
 
-__device__ __forceinline__ void edge_in(const GraphDev &G, int i, int j, float e[EIN]) {
-    const float2 pi = G.pos[i], pj = G.pos[j], vi = G.vel[i], vj = G.vel[j];
-    const float dx = pi.x - pj.x, dy = pi.y - pj.y;
+// the edge input of (i, j): the position difference in FP64, then FP32
+__device__ __forceinline__ void edge_in(const GraphDev &G, double2 pi, float2 vi, int j,
+                                        float e[EIN]) {
+    const double2 pj = G.pos[j];
+    const float2 vj = G.vel[j];
+    const float dx = (float)(pi.x - pj.x), dy = (float)(pi.y - pj.y);
     e[0] = dx * G.inv_h;
     e[1] = dy * G.inv_h;
     e[2] = sqrtf(fmaf(dx, dx, dy * dy)) * G.inv_h;
@@ -88,11 +92,22 @@ __device__ __forceinline__ void edge_in(const GraphDev &G, int i, int j, float e
     e[4] = (vi.y - vj.y) * G.inv_U;
 }
 
-// FP64 positions -> FP32 positions relative to `o`
-__global__ void k_pos32(const double2 *__restrict__ pos, int n, double ox, double oy,
-                        float2 *__restrict__ out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < n) out[i] = make_float2((float)(pos[i].x - ox), (float)(pos[i].y - oy));
+// a warp's edges are computed one per lane (slots k0 + lane), then broadcast
+struct EdgeLane {
+    int j;
+    float e[EIN];
+};
+__device__ __forceinline__ EdgeLane edge_lane(const GraphDev &G, int i, double2 pi, float2 vi,
+                                              int k) {
+    EdgeLane r;
+    r.j = 0;
+#pragma unroll
+    for (int q = 0; q < EIN; q++) r.e[q] = 0.f;
+    if (k < G.deg[i]) {
+        r.j = G.nbr[(size_t)i * G.K + k];
+        edge_in(G, pi, vi, r.j, r.e);
+    }
+    return r;
 }
 
 // encoder: thread per (node, channel); z0 kept for the backward pass
@@ -134,6 +149,7 @@ struct LinArgs {
 };
 
 constexpr int kLinTN = 16;
+constexpr int kLinBlocks = 152 * 4;  // persistent: W is staged once per block
 
 template <int M>
 __global__ void __launch_bounds__(kGB) k_linear(LinArgs a) {
@@ -141,44 +157,54 @@ __global__ void __launch_bounds__(kGB) k_linear(LinArgs a) {
     __shared__ float Xs[kLinTN * 128];
     const int K = a.K1 + a.K2;
     const int tid = threadIdx.x;
-    for (int e = tid; e < K * M; e += kGB) {
-        const int k = e / M, m = e - k * M;
-        Ws[e] = a.W[m * a.wm + k * a.wk];
+    // stage W transposed (Ws[k][m]), reading it in its own order (coalesced)
+    if (a.wk == 1) {
+        for (int e = tid; e < K * M; e += kGB) {
+            const int m = e / K, k = e - m * K;
+            Ws[k * M + m] = a.W[m * a.wm + k];
+        }
+    } else {
+        for (int e = tid; e < K * M; e += kGB) {
+            const int k = e / M, m = e - k * M;
+            Ws[k * M + m] = a.W[m * a.wm + k * a.wk];
+        }
     }
-    const int n0 = blockIdx.x * kLinTN;
-    for (int e = tid; e < kLinTN * K; e += kGB) {
-        const int r = e / K, k = e - r * K;
-        const int n = n0 + r;
-        float v = 0.f;
-        if (n < a.n) v = k < a.K1 ? a.X1[(size_t)n * a.ld1 + k] : a.X2[(size_t)n * a.ld2 + (k - a.K1)];
-        Xs[e] = v;
-    }
-    __syncthreads();
     constexpr int G = kGB / M;          // node groups
     constexpr int PER = kLinTN / G;     // nodes per thread
     const int m = tid % M, grp = tid / M;
-    float acc[PER];
+    for (int n0 = blockIdx.x * kLinTN; n0 < a.n; n0 += gridDim.x * kLinTN) {
+        __syncthreads();
+        for (int e = tid; e < kLinTN * K; e += kGB) {
+            const int r = e / K, k = e - r * K;
+            const int n = n0 + r;
+            float v = 0.f;
+            if (n < a.n) v = k < a.K1 ? a.X1[(size_t)n * a.ld1 + k] : a.X2[(size_t)n * a.ld2 + (k - a.K1)];
+            Xs[e] = v;
+        }
+        __syncthreads();
+        float acc[PER];
 #pragma unroll
-    for (int q = 0; q < PER; q++) acc[q] = 0.f;
-    for (int k = 0; k < K; k++) {
-        const float w = Ws[k * M + m];
+        for (int q = 0; q < PER; q++) acc[q] = 0.f;
+        for (int k = 0; k < K; k++) {
+            const float w = Ws[k * M + m];
 #pragma unroll
-        for (int q = 0; q < PER; q++) acc[q] = fmaf(Xs[(grp + q * G) * K + k], w, acc[q]);
-    }
+            for (int q = 0; q < PER; q++) acc[q] = fmaf(Xs[(grp + q * G) * K + k], w, acc[q]);
+        }
 #pragma unroll
-    for (int q = 0; q < PER; q++) {
-        const int n = n0 + grp + q * G;
-        if (n >= a.n) continue;
-        float y = acc[q];
-        if (a.b) y += a.b[m];
-        if (a.b2) y = fmaf((float)a.deg[n], a.b2[m], y);
-        const size_t o = (size_t)n * M + m;
-        if (a.pre) a.pre[o] = y;
-        if (a.act) y = silu(y);
-        if (a.aux) y *= dsilu(a.aux[o]);
-        if (a.res) y += a.res[o];
-        if (a.accumulate) y += a.Y[o];
-        a.Y[o] = y;
+        for (int q = 0; q < PER; q++) {
+            const int n = n0 + grp + q * G;
+            if (n >= a.n) continue;
+            float y = acc[q];
+            if (a.b) y += a.b[m];
+            if (a.b2) y = fmaf((float)a.deg[n], a.b2[m], y);
+            const size_t o = (size_t)n * M + m;
+            if (a.pre) a.pre[o] = y;
+            if (a.act) y = silu(y);
+            if (a.aux) y *= dsilu(a.aux[o]);
+            if (a.res) y += a.res[o];
+            if (a.accumulate) y += a.Y[o];
+            a.Y[o] = y;
+        }
     }
 }
 
@@ -215,18 +241,23 @@ __global__ void __launch_bounds__(kGB) k_edge_forward(GraphDev G, const float *_
     const float p1 = P[(size_t)i * H + lane + 32] + be[lane + 32];
     float s0 = 0.f, s1 = 0.f;
     const int d = G.deg[i];
-    for (int k = 0; k < d; k++) {
-        const int j = G.nbr[(size_t)i * G.K + k];
-        float e[EIN];
-        edge_in(G, i, j, e);
-        float z0 = p0 + Q[(size_t)j * H + lane], z1 = p1 + Q[(size_t)j * H + lane + 32];
+    const double2 pi = G.pos[i];
+    const float2 vi = G.vel[i];
+    for (int k0 = 0; k0 < d; k0 += 32) {
+        const EdgeLane mine = edge_lane(G, i, pi, vi, k0 + lane);
+        const int cnt = min(32, d - k0);
+        for (int t = 0; t < cnt; t++) {
+            const int j = __shfl_sync(0xffffffffu, mine.j, t);
+            float z0 = p0 + Q[(size_t)j * H + lane], z1 = p1 + Q[(size_t)j * H + lane + 32];
 #pragma unroll
-        for (int q = 0; q < EIN; q++) {
-            z0 = fmaf(w0[q], e[q], z0);
-            z1 = fmaf(w1[q], e[q], z1);
+            for (int q = 0; q < EIN; q++) {
+                const float eq = __shfl_sync(0xffffffffu, mine.e[q], t);
+                z0 = fmaf(w0[q], eq, z0);
+                z1 = fmaf(w1[q], eq, z1);
+            }
+            s0 += silu(z0);
+            s1 += silu(z1);
         }
-        s0 += silu(z0);
-        s1 += silu(z1);
     }
     S[(size_t)i * H + lane] = s0;
     S[(size_t)i * H + lane + 32] = s1;
@@ -263,32 +294,39 @@ __global__ void __launch_bounds__(kGB) k_edge_backward(GraphDev G, const float *
         const float ds0 = dS[(size_t)n * H + lane], ds1 = dS[(size_t)n * H + lane + 32];
         float dp0 = 0.f, dp1 = 0.f, dq0 = 0.f, dq1 = 0.f;
         const int d = G.deg[n];
-        for (int k = 0; k < d; k++) {
-            const int j = G.nbr[(size_t)n * G.K + k];
-            float e[EIN];
-            edge_in(G, n, j, e);  // e_nj; e_jn = (-e0, -e1, e2, -e3, -e4)
-            float a0 = pn0 + Q[(size_t)j * H + lane] + b0, a1 = pn1 + Q[(size_t)j * H + lane + 32] + b1;
-            float c0 = P[(size_t)j * H + lane] + qn0 + b0, c1 = P[(size_t)j * H + lane + 32] + qn1 + b1;
+        const double2 pn = G.pos[n];
+        const float2 vn = G.vel[n];
+        for (int k0 = 0; k0 < d; k0 += 32) {
+            const EdgeLane mine = edge_lane(G, n, pn, vn, k0 + lane);
+            const int cnt = min(32, d - k0);
+            for (int tt = 0; tt < cnt; tt++) {
+                const int j = __shfl_sync(0xffffffffu, mine.j, tt);
+                float e[EIN];  // e_nj; e_jn = (-e0, -e1, e2, -e3, -e4)
 #pragma unroll
-            for (int q = 0; q < EIN; q++) {
-                const float sgn = (q == 2) ? 1.f : -1.f;
-                a0 = fmaf(w0[q], e[q], a0);
-                a1 = fmaf(w1[q], e[q], a1);
-                c0 = fmaf(w0[q], sgn * e[q], c0);
-                c1 = fmaf(w1[q], sgn * e[q], c1);
-            }
-            const float dz0 = ds0 * dsilu(a0), dz1 = ds1 * dsilu(a1);
-            dp0 += dz0;
-            dp1 += dz1;
+                for (int q = 0; q < EIN; q++) e[q] = __shfl_sync(0xffffffffu, mine.e[q], tt);
+                float a0 = pn0 + Q[(size_t)j * H + lane] + b0, a1 = pn1 + Q[(size_t)j * H + lane + 32] + b1;
+                float c0 = P[(size_t)j * H + lane] + qn0 + b0, c1 = P[(size_t)j * H + lane + 32] + qn1 + b1;
 #pragma unroll
-            for (int q = 0; q < EIN; q++) {
-                gw0[q] = fmaf(dz0, e[q], gw0[q]);
-                gw1[q] = fmaf(dz1, e[q], gw1[q]);
+                for (int q = 0; q < EIN; q++) {
+                    const float sgn = (q == 2) ? 1.f : -1.f;
+                    a0 = fmaf(w0[q], e[q], a0);
+                    a1 = fmaf(w1[q], e[q], a1);
+                    c0 = fmaf(w0[q], sgn * e[q], c0);
+                    c1 = fmaf(w1[q], sgn * e[q], c1);
+                }
+                const float dz0 = ds0 * dsilu(a0), dz1 = ds1 * dsilu(a1);
+                dp0 += dz0;
+                dp1 += dz1;
+#pragma unroll
+                for (int q = 0; q < EIN; q++) {
+                    gw0[q] = fmaf(dz0, e[q], gw0[q]);
+                    gw1[q] = fmaf(dz1, e[q], gw1[q]);
+                }
+                gw0[EIN] += dz0;
+                gw1[EIN] += dz1;
+                dq0 = fmaf(dS[(size_t)j * H + lane], dsilu(c0), dq0);
+                dq1 = fmaf(dS[(size_t)j * H + lane + 32], dsilu(c1), dq1);
             }
-            gw0[EIN] += dz0;
-            gw1[EIN] += dz1;
-            dq0 = fmaf(dS[(size_t)j * H + lane], dsilu(c0), dq0);
-            dq1 = fmaf(dS[(size_t)j * H + lane + 32], dsilu(c1), dq1);
         }
         dP[(size_t)n * H + lane] = dp0;
         dP[(size_t)n * H + lane + 32] = dp1;
@@ -497,7 +535,6 @@ struct tsph_gnn {
     cudaStream_t st = nullptr;
     std::vector<void *> allocs;
     float *p = nullptr, *g = nullptr, *m1 = nullptr, *m2 = nullptr;
-    float *posf = nullptr;  // float2 per node
     float *x = nullptr, *z0 = nullptr, *hs[tsph::NL + 1] = {}, *P[tsph::NL] = {}, *Q[tsph::NL] = {},
           *S[tsph::NL] = {}, *mm[tsph::NL] = {}, *u[tsph::NL] = {}, *t[tsph::NL] = {};
     float *y = nullptr, *dy = nullptr, *dh = nullptr, *dh2 = nullptr, *dhm = nullptr,
@@ -542,7 +579,7 @@ LinArgs lin(const float *X1, int K1, int ld1, const float *W, int wm, int wk, fl
 }
 
 int run_lin(tsph_gnn *N, int M, const LinArgs &a) {
-    const int nb = gblocks(a.n, kLinTN);
+    const int nb = std::min(gblocks(a.n, kLinTN), kLinBlocks);
     if (M == 128) k_linear<128><<<nb, kGB, 0, N->st>>>(a);
     else k_linear<64><<<nb, kGB, 0, N->st>>>(a);
     GCK(cudaGetLastError());
@@ -666,10 +703,7 @@ int set_graph(tsph_gnn *N, const tsph_gnn_graph *gr) {
         return TSPH_ERR_ARG;
     }
     const int n = gr->n_nodes;
-    k_pos32<<<gblocks(n), kGB, 0, N->st>>>(static_cast<const double2 *>(gr->pos), n, gr->origin[0],
-                                           gr->origin[1], reinterpret_cast<float2 *>(N->posf));
-    GCK(cudaGetLastError());
-    N->G = GraphDev{reinterpret_cast<const float2 *>(N->posf), static_cast<const float2 *>(gr->vel),
+    N->G = GraphDev{static_cast<const double2 *>(gr->pos), static_cast<const float2 *>(gr->vel),
                     gr->srho, gr->wall, gr->deg, gr->nbr, n, gr->k_slots,
                     (float)(1.0 / gr->h), (float)(1.0 / gr->u_scale), (float)(1.0 / gr->s_scale)};
     return 0;
@@ -699,7 +733,6 @@ int tsph_gnn_create(int capacity, void *stream, tsph_gnn **out) {
     A(&N->g, P);
     A(&N->m1, P);
     A(&N->m2, P);
-    A(&N->posf, 2 * c);
     A(&N->x, NIN * c);
     A(&N->z0, H * c);
     for (int l = 0; l <= NL; l++) A(&N->hs[l], H * c);

@@ -19,6 +19,7 @@ __global__ void k_graph_export(FluidState<T> F, const uint32_t *__restrict__ fst
                                float2 *__restrict__ vel, float *__restrict__ srho,
                                float *__restrict__ wall, int32_t *__restrict__ id,
                                int32_t *__restrict__ deg, int32_t *__restrict__ nbr,
+                               float2 *__restrict__ acc, float *__restrict__ rate,
                                uint32_t *__restrict__ overflow) {
     const int node = blockIdx.x * blockDim.x + threadIdx.x;
     const int nl = n_live(fstart, g.ncells);
@@ -38,6 +39,9 @@ __global__ void k_graph_export(FluidState<T> F, const uint32_t *__restrict__ fst
     }
     wall[node] = is_wall ? 1.f : 0.f;
     id[node] = (int32_t)(is_wall ? Wl.id[node] : F.id[f]);
+    if (acc) acc[node] = is_wall ? make_float2(0.f, 0.f)
+                                 : make_float2((float)F.a[f].x, (float)F.a[f].y);
+    if (rate) rate[node] = is_wall ? 0.f : (float)F.drho[f];
     int cnt = 0;
     int32_t *row = nbr + (size_t)node * K;
     for (int dxi = -1; dxi <= 1; dxi++) {
@@ -78,26 +82,108 @@ __global__ void k_graph_export(FluidState<T> F, const uint32_t *__restrict__ fst
     for (int k = cnt; k < K; k++) row[k] = -1;
 }
 
+// the start-of-window terms of the window check, by particle index
+struct WindowRef {
+    double *rho;    // rho at the window start
+    double2 *v;     // v at the window start
+    float *drho;    // d(rho)/dt of the forces pass at the window start
+    float2 *a;      // a of that pass
+};
+
 // the surrogate's window update of the fluid (node nw + f is fluid row f of
-// the export): v += dv, rho - rho0 += ds, r += k dt (v_old + v_new) / 2
+// the export), phase 0 (explicit), 1 (kick) or 2 (drift):
+//   0: v_new = v + add_rates kdt a + su (y0, y1),  rho += add_rates kdt drho + ss y2,
+//      r += kdt (v + v_new) / 2
+//   1: v_new as in 0; rho, r unchanged
+//   2: rho += add_rates kdt drho + ss y2 (drho of the pass after the kick),
+//      r += kdt (v_start + v) / 2
 template <typename T>
 __global__ void k_apply_update(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
-                               int nw, const float *__restrict__ du, const float *__restrict__ dv,
-                               const float *__restrict__ ds, double kdt,
+                               int nw, const float *__restrict__ y, float su, float ss, double kdt,
+                               int add_rates, int phase, T rho0, WindowRef ref,
                                uint32_t *__restrict__ health) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_live(fstart, ncells)) return;
     const int node = nw + f;
+    const uint32_t pid = F.id[f];
+    const float y0 = y[3 * (size_t)node], y1 = y[3 * (size_t)node + 1], y2 = y[3 * (size_t)node + 2];
+    const T kr = add_rates ? (T)kdt : T(0);
     const auto v0 = F.v[f];
+    if (phase == 2) {
+        F.rho[f] = F.rho[f] + (kr * F.drho[f] + (T)(ss * y2));
+        const double2 vs = ref.v[pid];
+        const double2 r = F.r[f];
+        F.r[f] = make_double2(r.x + kdt * 0.5 * (vs.x + (double)v0.x),
+                              r.y + kdt * 0.5 * (vs.y + (double)v0.y));
+        if (!(F.rho[f] == F.rho[f])) atomicOr(health, kHealthNan);
+        return;
+    }
+    const auto a0 = F.a[f];
+    const T dr0 = F.drho[f];
+    ref.rho[pid] = rho_full64(F.rho[f], rho0);
+    ref.v[pid] = make_double2((double)v0.x, (double)v0.y);
+    ref.drho[pid] = (float)dr0;
+    ref.a[pid] = make_float2((float)a0.x, (float)a0.y);
     typename V2<T>::t v1;
-    v1.x = v0.x + (T)du[node];
-    v1.y = v0.y + (T)dv[node];
+    v1.x = v0.x + kr * a0.x + (T)(su * y0);
+    v1.y = v0.y + kr * a0.y + (T)(su * y1);
     F.v[f] = v1;
-    F.rho[f] = F.rho[f] + (T)ds[node];  // rho - rho0 in the FP32 build, rho in FP64: the same increment
+    if (!(v1.x == v1.x) || !(v1.y == v1.y)) atomicOr(health, kHealthNan);
+    if (phase == 1) return;
+    F.rho[f] = F.rho[f] + (kr * dr0 + (T)(ss * y2));  // rho - rho0 (FP32) or rho (FP64)
     const double2 r = F.r[f];
     F.r[f] = make_double2(r.x + kdt * 0.5 * ((double)v0.x + (double)v1.x),
                           r.y + kdt * 0.5 * ((double)v0.y + (double)v1.y));
-    if (!(v1.x == v1.x) || !(v1.y == v1.y)) atomicOr(health, kHealthNan);
+    if (!(F.rho[f] == F.rho[f])) atomicOr(health, kHealthNan);
+}
+
+// the check of a window after a forces pass at its end state: per fluid
+// particle e = rho - (rho_0 + kdt (drho_0 + drho_1) / 2) and
+// ev = v - (v_0 + kdt (a_0 + a_1) / 2); out[0] max |e| (as the bits of a
+// non-negative double), out[1] sum e^2, out[2..3] sum ev, out[4] sum
+// |kdt (a_0 + a_1) / 2| (diagnostic), out[5] count, out[6] (float bits of
+// max |e|) << 32 | its particle index
+template <typename T>
+__global__ void k_window_check(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
+                               double kdt, T rho0, WindowRef ref, double *__restrict__ out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    double e = 0, ex = 0, ey = 0, dvc = 0, one = 0;
+    unsigned long long arg = 0ull;
+    if (f < n_live(fstart, ncells) && F.key[f] < (uint32_t)ncells) {
+        const uint32_t pid = F.id[f];
+        const double rc = ref.rho[pid] + 0.5 * kdt * ((double)ref.drho[pid] + (double)F.drho[f]);
+        e = fabs(rho_full64(F.rho[f], rho0) - rc);
+        const double2 v0 = ref.v[pid];
+        const float2 a0 = ref.a[pid];
+        const auto a1 = F.a[f];
+        const double cx = 0.5 * kdt * ((double)a0.x + (double)a1.x);
+        const double cy = 0.5 * kdt * ((double)a0.y + (double)a1.y);
+        ex = (double)F.v[f].x - (v0.x + cx);
+        ey = (double)F.v[f].y - (v0.y + cy);
+        dvc = sqrt(cx * cx + cy * cy);
+        one = 1;
+        arg = ((unsigned long long)__float_as_uint((float)e) << 32) | pid;
+    }
+    double mx = e, sq = e * e;
+    for (int o = 16; o; o >>= 1) {
+        mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        sq += __shfl_xor_sync(0xffffffffu, sq, o);
+        ex += __shfl_xor_sync(0xffffffffu, ex, o);
+        ey += __shfl_xor_sync(0xffffffffu, ey, o);
+        dvc += __shfl_xor_sync(0xffffffffu, dvc, o);
+        one += __shfl_xor_sync(0xffffffffu, one, o);
+        const unsigned long long w = __shfl_xor_sync(0xffffffffu, arg, o);
+        arg = w > arg ? w : arg;
+    }
+    if ((threadIdx.x & 31) == 0 && one > 0) {
+        atomicMax(reinterpret_cast<unsigned long long *>(out), (unsigned long long)__double_as_longlong(mx));
+        atomicAdd(out + 1, sq);
+        atomicAdd(out + 2, ex);
+        atomicAdd(out + 3, ey);
+        atomicAdd(out + 4, dvc);
+        atomicAdd(out + 5, one);
+        atomicMax(reinterpret_cast<unsigned long long *>(out + 6), arg);
+    }
 }
 
 }  // namespace tsph

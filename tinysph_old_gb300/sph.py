@@ -38,7 +38,8 @@ ABI_SYMBOLS = (
     "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
     "tsph_water_level", "tsph_point_fields", "tsph_water_front", "tsph_autotune",
     "tsph_set_tile_shape", "tsph_write_vtk", "tsph_save_checkpoint", "tsph_load_checkpoint",
-    "tsph_export_graph", "tsph_apply_update", "tsph_gnn_n_params", "tsph_gnn_create",
+    "tsph_export_graph", "tsph_apply_update", "tsph_window_check", "tsph_state_save",
+    "tsph_state_restore", "tsph_gnn_n_params", "tsph_gnn_create",
     "tsph_gnn_destroy", "tsph_gnn_set_params", "tsph_gnn_get_params", "tsph_gnn_get_grads",
     "tsph_gnn_forward", "tsph_gnn_loss_grad", "tsph_gnn_adam",
     "tsph_ale_create", "tsph_ale_destroy", "tsph_ale_add_particles", "tsph_ale_set_scheme",
@@ -86,7 +87,7 @@ class GnnGraph(C.Structure):
     _fields_ = [("pos", C.c_void_p), ("vel", C.c_void_p), ("srho", C.c_void_p),
                 ("wall", C.c_void_p), ("deg", C.c_void_p), ("nbr", C.c_void_p),
                 ("n_nodes", C.c_int32), ("k_slots", C.c_int32), ("h", C.c_double),
-                ("u_scale", C.c_double), ("s_scale", C.c_double), ("origin", C.c_double * 2)]
+                ("u_scale", C.c_double), ("s_scale", C.c_double)]
 
 
 class _Profile(C.Structure):
@@ -151,8 +152,11 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_autotune.argtypes = [P, P, P]
     L.tsph_set_tile_shape.argtypes = [P, I]
     L.tsph_write_vtk.argtypes = [P, C.c_char_p]
-    L.tsph_export_graph.argtypes = [P, I, I] + [P] * 7 + [C.POINTER(C.c_int32)] * 2
-    L.tsph_apply_update.argtypes = [P, P, P, P, D]
+    L.tsph_export_graph.argtypes = [P, I, I] + [P] * 9 + [C.POINTER(C.c_int32)] * 2
+    L.tsph_apply_update.argtypes = [P, P, D, D, D, I, I]
+    L.tsph_window_check.argtypes = [P, D, C.POINTER(C.c_double)]
+    L.tsph_state_save.argtypes = [P]
+    L.tsph_state_restore.argtypes = [P]
     L.tsph_gnn_n_params.restype = I
     L.tsph_gnn_create.argtypes = [I, P, C.POINTER(P)]
     L.tsph_gnn_destroy.argtypes = [P]
@@ -444,16 +448,34 @@ class ParticleSystem:
         s.domain = None
         return s
 
-    def export_graph(self, k_slots, capacity, pos, vel, srho, wall, id_, deg, nbr):
+    def export_graph(self, k_slots, capacity, pos, vel, srho, wall, id_, deg, nbr, acc=None,
+                     rate=None):
         """Device pointers (ints) -> (n_nodes, n_wall); see tsph_export_graph."""
         n, nw = C.c_int32(), C.c_int32()
         _check(self._L.tsph_export_graph(self._h, int(k_slots), int(capacity), pos, vel, srho,
-                                         wall, id_, deg, nbr, C.byref(n), C.byref(nw)))
+                                         wall, id_, deg, nbr, acc, rate, C.byref(n),
+                                         C.byref(nw)))
         return n.value, nw.value
 
-    def apply_update(self, du, dv, ds, k_dt):
-        """Device pointers of the per-node update; see tsph_apply_update."""
-        _check(self._L.tsph_apply_update(self._h, du, dv, ds, float(k_dt)))
+    def apply_update(self, y, u_scale, s_scale, k_dt, add_rates=True, phase=0):
+        """The surrogate's window update from the device array y (3 floats per
+        node of the last export); phase 0 explicit, 1 kick, 2 drift; see
+        tsph_apply_update."""
+        _check(self._L.tsph_apply_update(self._h, y, float(u_scale), float(s_scale), float(k_dt),
+                                         1 if add_rates else 0, int(phase)))
+
+    def window_check(self, k_dt):
+        """(max, rms) density error / rho0, the momentum error, the count and
+        the worst particle of the last window; see tsph_window_check."""
+        out = (C.c_double * 5)()
+        _check(self._L.tsph_window_check(self._h, float(k_dt), out))
+        return out[0], out[1], out[2], int(out[3]), int(out[4])
+
+    def state_save(self):
+        _check(self._L.tsph_state_save(self._h))
+
+    def state_restore(self):
+        _check(self._L.tsph_state_restore(self._h))
 
     def autotune(self):
         """Time both tile shapes of the pair kernel, keep the faster:
