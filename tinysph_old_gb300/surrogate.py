@@ -231,11 +231,13 @@ def window_sample(system, ga, gb, wall_model, dt, k=K_STRIDE, scheme="kick_drift
 
 
 def generate(specs, t_end, samples_per_case, cases_per_system=25, k=K_STRIDE, log=None,
-             scheme="kick_drift"):
-    """Run the specs (packed `cases_per_system` to a particle system) with the
-    plain step to `t_end` and take `samples_per_case` windows from each, at
-    evenly spaced times (the first after k steps, when the rates of a forces
-    pass exist)."""
+             scheme="kick_drift", rollout_model=None, h=None):
+    """Run the specs (packed `cases_per_system` to a particle system) to
+    `t_end` and take `samples_per_case` windows from each, at evenly spaced
+    times (the first after k steps, when the rates of a forces pass exist).
+    The trajectory is the plain solver's, or with `rollout_model` the
+    surrogate's own rollout with that model (windows checked, plain
+    fallback), so that the samples hold the states the surrogate visits."""
     from . import batch as B
 
     out = []
@@ -247,19 +249,31 @@ def generate(specs, t_end, samples_per_case, cases_per_system=25, k=K_STRIDE, lo
             times = np.linspace(k, nsteps - k, samples_per_case).astype(int)
             cap = g.np + 64
             ga, gb = GraphBuffers(cap, rates=False), GraphBuffers(cap, rates=False)
-            done = 0
+            ro = None
+            if rollout_model is not None:
+                s.step(g.wall_model, dt, k)
+                ro = Rollout(s, rollout_model, dt, g.wall_model, h or g.cases[0].h,
+                             use_net=bool(np.any(rollout_model.params)), capacity=cap,
+                             scheme=scheme)
+            done = k if ro is not None else 0
             t0 = time.time()
             for st in times:
                 st = int(st)
                 if st > done:
-                    s.step(g.wall_model, dt, st - done)
-                    done = st
+                    if ro is not None:
+                        nw = (st - done) // k
+                        ro.run(nw)
+                        done += nw * k
+                    else:
+                        s.step(g.wall_model, dt, st - done)
+                        done = st
                 graph, tgt, base = window_sample(s, ga, gb, g.wall_model, dt, k, scheme)
                 done += k
                 out.append(Sample(graph, tgt, done * dt, base))
             if log:
+                fb = f", fallback {ro.fallback_rate:.2f}" if ro is not None else ""
                 log(f"cases {c0}..{c0 + len(g.cases) - 1}: {g.np} particles, {done} steps, "
-                    f"{len(times)} windows, {time.time() - t0:.1f} s")
+                    f"{len(times)} windows, {time.time() - t0:.1f} s{fb}")
         del bt
     return out
 
