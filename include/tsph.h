@@ -293,6 +293,11 @@ int tsph_apply_update(tsph_system *s, const float *y, double u_scale, double s_s
  *   out[3] = the number of fluid particles checked,
  *   out[4] = the particle index of the largest density error. */
 int tsph_window_check(tsph_system *s, double k_dt, double out[5]);
+/* the CUDA stream the system's kernels run on (the caller's, or the one the
+ * system created when given NULL): work of other libraries on the same
+ * buffers (the surrogate's network, for one) must be ordered with it.  No
+ * counterpart in the reference. */
+int tsph_get_stream(tsph_system *s, void **stream);
 /* a device-side copy of the whole particle state (the start of a surrogate
  * window) and its restoration (the plain-step fallback). */
 int tsph_state_save(tsph_system *s);

@@ -482,6 +482,14 @@ int tsph_window_check(tsph_system *s, double k_dt, double out[5]) {
     return TSPH_OK;
 }
 
+int tsph_get_stream(tsph_system *s, void **stream) {
+    NEED(s);
+    if (!stream) return fail(TSPH_ERR_ARG, "null output");
+    ENGINE(s);
+    *stream = s->eng->stream();
+    return TSPH_OK;
+}
+
 int tsph_state_save(tsph_system *s) {
     NEED(s);
     ENGINE(s);

@@ -273,6 +273,8 @@ template <typename T> class Engine final : public EngineBase {
 
     int tile_shape() const override { return tile_shape_; }
 
+    void *stream() const override { return st_; }
+
     int export_graph(int K, int cap, double2 *pos, float2 *vel, float *srho, float *wall,
                      int32_t *id, int32_t *deg, int32_t *nbr, float2 *acc, float *rate,
                      int *n_nodes, int *n_wall, std::string &err) override {

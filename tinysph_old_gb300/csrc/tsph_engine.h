@@ -75,6 +75,7 @@ class EngineBase {
     virtual int state_save(std::string &err) = 0;
     virtual int state_restore(std::string &err) = 0;
     virtual int sync(std::string &err) = 0;
+    virtual void *stream() const = 0;
     virtual void set_profiling(bool on) = 0;
     virtual Profile profile(bool reset) = 0;
     virtual bool cells_valid() const = 0;

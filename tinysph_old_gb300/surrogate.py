@@ -215,6 +215,7 @@ def window_sample(system, ga, gb, wall_model, dt, k=K_STRIDE, scheme="kick_drift
     start = _by_id(ga, ntot)
     system.state_save()
     y = torch.zeros((n, 3), dtype=torch.float32, device=ga.vel.device)
+    torch.cuda.synchronize()  # the system's kernels run on their own stream
     window_update(system, y.data_ptr(), zero, kdt, wall_model, scheme)
     end_of_window(system, wall_model)
     base = _by_id(gb.export(system), ntot) - start
@@ -414,9 +415,12 @@ class Rollout:
         cap = int(capacity or system.np + 64)
         self.gb = GraphBuffers(cap, rates=False)
         self.y = torch.zeros((cap, 3), dtype=torch.float32, device="cuda")
+        torch.cuda.synchronize()
         self.net = None
         if use_net:
-            self.net = sph.Gnn(cap)
+            # the network runs on the system's stream: its output feeds the
+            # system's update and its input is the system's export
+            self.net = sph.Gnn(cap, stream=system.stream_ptr())
             self.net.set_params(model.params)
         self.windows = 0
         self.fallbacks = 0
@@ -462,6 +466,7 @@ def plain_check_floor(system, wall_model, dt, n_windows, k=K_STRIDE):
     cap = system.np + 64
     gb = GraphBuffers(cap, rates=False)
     y = torch.zeros((cap, 3), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
     out = []
     for _ in range(n_windows):
         gb.export(system)
