@@ -269,20 +269,22 @@ int tsph_export_graph(tsph_system *s, int k_slots, int capacity, void *pos, void
                       void *acc, float *rate, int32_t *n_nodes, int32_t *n_wall);
 /* the surrogate's update of the fluid over a window of k steps (k_dt = k dt),
  * from y (device, 3 floats per node of the last export), with a, drho/dt
- * those of the last forces pass:
- *   phase 0 (explicit):  v_new = v + add_rates k_dt a + u_scale (y0, y1),
- *                        rho_new = rho + add_rates k_dt drho/dt + s_scale y2,
+ * those of the last forces pass and r = 1 if flags has TSPH_UPDATE_RATES:
+ *   phase 0 (explicit):  v_new = v + r k_dt a + u_scale (y0, y1),
+ *                        rho_new = rho + r k_dt drho/dt + s_scale y2,
  *                        r += k_dt (v + v_new) / 2;
  *   phase 1 (kick):      v_new as in phase 0; rho and r unchanged (the cell
  *                        lists stay valid, for a forces pass with v_new);
  *   phase 2 (drift, after a kick and a forces pass):
- *                        rho += add_rates k_dt drho/dt + s_scale y2 with the
- *                        rate of that pass, r += k_dt (v_start + v_new) / 2.
- * Phases 0 and 1 record, per particle, the start-of-window terms of the
- * window check (tsph_window_check).  The cell lists are stale after phases 0
- * and 2. */
+ *                        rho += r k_dt drho/dt + s_scale y2 with the rate of
+ *                        that pass, r += k_dt (v_start + v_new) / 2.
+ * With TSPH_UPDATE_ZERO_MOMENTUM, (y0, y1) less their mean over the fluid
+ * nodes is used: the correction carries no momentum.  Phases 0 and 1 record,
+ * per particle, the start-of-window terms of the window check
+ * (tsph_window_check).  The cell lists are stale after phases 0 and 2. */
+enum { TSPH_UPDATE_RATES = 1, TSPH_UPDATE_ZERO_MOMENTUM = 2 };
 int tsph_apply_update(tsph_system *s, const float *y, double u_scale, double s_scale,
-                      double k_dt, int add_rates, int phase);
+                      double k_dt, int flags, int phase);
 /* the per-window check of a surrogate window, after a forces pass at the
  * window's end state: against the trapezoidal rule of the SPH rates at both
  * ends, rho_c = rho_0 + k_dt (drho_0 + drho_1) / 2 and

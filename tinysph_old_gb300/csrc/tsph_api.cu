@@ -465,12 +465,13 @@ int tsph_export_graph(tsph_system *s, int k_slots, int capacity, void *pos, void
 }
 
 int tsph_apply_update(tsph_system *s, const float *y, double u_scale, double s_scale,
-                      double k_dt, int add_rates, int phase) {
+                      double k_dt, int flags, int phase) {
     NEED(s);
     if (!y) return fail(TSPH_ERR_ARG, "null update");
     if (phase < 0 || phase > 2) return fail(TSPH_ERR_ARG, "phase must be 0, 1 or 2");
     ENGINE(s);
-    RUN(s->eng->apply_update(y, u_scale, s_scale, k_dt, add_rates != 0, phase, err_));
+    RUN(s->eng->apply_update(y, u_scale, s_scale, k_dt, (flags & TSPH_UPDATE_RATES) != 0,
+                             (flags & TSPH_UPDATE_ZERO_MOMENTUM) != 0, phase, err_));
     return TSPH_OK;
 }
 

@@ -64,6 +64,7 @@ template <typename T> class Engine final : public EngineBase {
     bool exported_ = false;        // the sorted order is that of the last export_graph
     WindowRef wref_{};             // start-of-window terms of the surrogate's check
     double *wout_ = nullptr;       // its reductions
+    double *ymean_ = nullptr;      // sums of the update's (y0, y1) over the fluid, and the count
     FluidState<T> Fsv_{};          // the saved state (tsph_state_save)
     T *wsv_ = nullptr;             // saved wall rho, drho, p, rho_o (4 nw)
     uint32_t *fstart_sv_ = nullptr;
@@ -312,8 +313,8 @@ template <typename T> class Engine final : public EngineBase {
         return collect_profile(err);
     }
 
-    int apply_update(const float *y, double su, double ss, double kdt, bool add_rates, int phase,
-                     std::string &err) override {
+    int apply_update(const float *y, double su, double ss, double kdt, bool add_rates,
+                     bool zero_momentum, int phase, std::string &err) override {
         if (!exported_ || !cells_) {
             err = "apply_update needs the order of the last export_graph (no re-binning since)";
             return 3;
@@ -327,12 +328,20 @@ template <typename T> class Engine final : public EngineBase {
             const size_t n = (size_t)ntot_;
             if ((rc = alloc(&wref_.rho, n, err)) || (rc = alloc(&wref_.v, n, err)) ||
                 (rc = alloc(&wref_.drho, n, err)) || (rc = alloc(&wref_.a, n, err)) ||
-                (rc = alloc(&wout_, 7, err)))
+                (rc = alloc(&wout_, 7, err)) || (rc = alloc(&ymean_, 3, err)))
                 return rc;
+        }
+        const double *ym = nullptr;
+        if (zero_momentum && phase != 2) {
+            TSPH_CK(cudaMemsetAsync(ymean_, 0, 3 * sizeof(double), st_));
+            if ((rc = launch(CAT_OTHER, k_fluid_sum2, blocks_for(nf_), kBlock, err,
+                             (const uint32_t *)fstart_, ncells_, nw_, y, ymean_)))
+                return rc;
+            ym = ymean_;
         }
         if ((rc = launch(CAT_OTHER, k_apply_update<T>, blocks_for(nf_), kBlock, err, F_,
                          (const uint32_t *)fstart_, ncells_, nw_, y, (float)su, (float)ss, kdt,
-                         add_rates ? 1 : 0, phase, P_.rho0, wref_, health_)))
+                         add_rates ? 1 : 0, phase, ym, P_.rho0, wref_, health_)))
             return rc;
         kicked_ = phase == 1;
         if (phase != 1) {

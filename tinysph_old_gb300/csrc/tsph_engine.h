@@ -70,7 +70,7 @@ class EngineBase {
                              int32_t *id, int32_t *deg, int32_t *nbr, float2 *acc, float *rate,
                              int *n_nodes, int *n_wall, std::string &err) = 0;
     virtual int apply_update(const float *y, double su, double ss, double kdt, bool add_rates,
-                             int phase, std::string &err) = 0;
+                             bool zero_momentum, int phase, std::string &err) = 0;
     virtual int window_check(double kdt, double out[5], std::string &err) = 0;
     virtual int state_save(std::string &err) = 0;
     virtual int state_restore(std::string &err) = 0;

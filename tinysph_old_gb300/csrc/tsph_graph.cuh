@@ -82,6 +82,29 @@ __global__ void k_graph_export(FluidState<T> F, const uint32_t *__restrict__ fst
     for (int k = cnt; k < K; k++) row[k] = -1;
 }
 
+// sums over the fluid nodes of (y0, y1) and their count into out[0..2]
+static __global__ void k_fluid_sum2(const uint32_t *__restrict__ fstart, int ncells, int nw,
+                             const float *__restrict__ y, double *__restrict__ out) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    double a = 0, b = 0, c = 0;
+    if (f < n_live(fstart, ncells)) {
+        const size_t node = (size_t)(nw + f);
+        a = y[3 * node];
+        b = y[3 * node + 1];
+        c = 1;
+    }
+    for (int o = 16; o; o >>= 1) {
+        a += __shfl_xor_sync(0xffffffffu, a, o);
+        b += __shfl_xor_sync(0xffffffffu, b, o);
+        c += __shfl_xor_sync(0xffffffffu, c, o);
+    }
+    if ((threadIdx.x & 31) == 0 && c > 0) {
+        atomicAdd(out, a);
+        atomicAdd(out + 1, b);
+        atomicAdd(out + 2, c);
+    }
+}
+
 // the start-of-window terms of the window check, by particle index
 struct WindowRef {
     double *rho;    // rho at the window start
@@ -100,13 +123,18 @@ struct WindowRef {
 template <typename T>
 __global__ void k_apply_update(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
                                int nw, const float *__restrict__ y, float su, float ss, double kdt,
-                               int add_rates, int phase, T rho0, WindowRef ref,
-                               uint32_t *__restrict__ health) {
+                               int add_rates, int phase, const double *__restrict__ ysum,
+                               T rho0, WindowRef ref, uint32_t *__restrict__ health) {
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_live(fstart, ncells)) return;
     const int node = nw + f;
     const uint32_t pid = F.id[f];
-    const float y0 = y[3 * (size_t)node], y1 = y[3 * (size_t)node + 1], y2 = y[3 * (size_t)node + 2];
+    float y0 = y[3 * (size_t)node], y1 = y[3 * (size_t)node + 1];
+    const float y2 = y[3 * (size_t)node + 2];
+    if (ysum && ysum[2] > 0) {  // less the fluid mean (a correction without momentum)
+        y0 -= (float)(ysum[0] / ysum[2]);
+        y1 -= (float)(ysum[1] / ysum[2]);
+    }
     const T kr = add_rates ? (T)kdt : T(0);
     const auto v0 = F.v[f];
     if (phase == 2) {

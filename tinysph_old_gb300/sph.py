@@ -458,12 +458,14 @@ class ParticleSystem:
                                          C.byref(nw)))
         return n.value, nw.value
 
-    def apply_update(self, y, u_scale, s_scale, k_dt, add_rates=True, phase=0):
+    def apply_update(self, y, u_scale, s_scale, k_dt, add_rates=True, phase=0,
+                     zero_momentum=False):
         """The surrogate's window update from the device array y (3 floats per
         node of the last export); phase 0 explicit, 1 kick, 2 drift; see
         tsph_apply_update."""
+        flags = (1 if add_rates else 0) | (2 if zero_momentum else 0)
         _check(self._L.tsph_apply_update(self._h, y, float(u_scale), float(s_scale), float(k_dt),
-                                         1 if add_rates else 0, int(phase)))
+                                         flags, int(phase)))
 
     def window_check(self, k_dt):
         """(max, rms) density error / rho0, the momentum error, the count and

@@ -138,15 +138,18 @@ class Model:
         return cls(np.zeros(sph.load().tsph_gnn_n_params(), np.float32), 1.0, 1.0, 1.0, 1.0, k)
 
 
-def window_update(system, y_ptr, model, kdt, wall_model, scheme="kick_drift"):
-    """The update part of a window (after export and the network): kick,
-    forces pass, drift; or the single explicit update."""
+def window_update(system, y_ptr, model, kdt, wall_model, scheme="explicit", zero_momentum=True):
+    """The update part of a window (after export and the network): the
+    single explicit update, or kick, forces pass, drift.  The network's
+    velocity correction is taken less its fluid mean (no momentum)."""
     if scheme == "kick_drift":
-        system.apply_update(y_ptr, model.u_out, model.s_out, kdt, True, phase=1)
+        system.apply_update(y_ptr, model.u_out, model.s_out, kdt, True, phase=1,
+                            zero_momentum=zero_momentum)
         system.compute_forces(wall_model)  # the continuity rate with the kicked velocities
         system.apply_update(y_ptr, model.u_out, model.s_out, kdt, True, phase=2)
     else:
-        system.apply_update(y_ptr, model.u_out, model.s_out, kdt, True, phase=0)
+        system.apply_update(y_ptr, model.u_out, model.s_out, kdt, True, phase=0,
+                            zero_momentum=zero_momentum)
 
 
 def end_of_window(system, wall_model):
@@ -201,7 +204,7 @@ def _by_id(gb, ntot):
     return out
 
 
-def window_sample(system, ga, gb, wall_model, dt, k=K_STRIDE, scheme="kick_drift"):
+def window_sample(system, ga, gb, wall_model, dt, k=K_STRIDE, scheme="explicit"):
     """From `system`'s state: export, run the window without the network
     (then restore), run k plain steps; the two changes matched by particle
     index."""
@@ -232,7 +235,7 @@ def window_sample(system, ga, gb, wall_model, dt, k=K_STRIDE, scheme="kick_drift
 
 
 def generate(specs, t_end, samples_per_case, cases_per_system=25, k=K_STRIDE, log=None,
-             scheme="kick_drift", rollout_model=None, h=None):
+             scheme="explicit", rollout_model=None, h=None):
     """Run the specs (packed `cases_per_system` to a particle system) to
     `t_end` and take `samples_per_case` windows from each, at evenly spaced
     times (the first after k steps, when the rates of a forces pass exist).
@@ -397,8 +400,8 @@ class Rollout:
     ``use_net=False`` runs the same windows with y = 0 (the method without
     the network)."""
 
-    def __init__(self, system, model, dt, wall_model, h, tol_density=0.01, tol_momentum=0.1,
-                 use_net=True, capacity=None, scheme="kick_drift"):
+    def __init__(self, system, model, dt, wall_model, h, tol_density=0.01, tol_momentum=0.5,
+                 use_net=True, capacity=None, scheme="explicit"):
         import torch
 
         self.s = system
