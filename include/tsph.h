@@ -328,6 +328,11 @@ int tsph_gnn_get_params(tsph_gnn *g, float *host);
 int tsph_gnn_get_grads(tsph_gnn *g, float *host);
 /* y (device, 3 per node) may be NULL */
 int tsph_gnn_forward(tsph_gnn *g, const tsph_gnn_graph *graph, float *y);
+/* the same network's forward pass for the rollout: BF16 weights and
+ * activations on the tensor cores with FP32 accumulation, the edge sums in
+ * FP32 with the hardware tanh in SiLU; y (device, n x 3) is required.  Its
+ * outputs differ from tsph_gnn_forward's by the BF16 rounding (about 1 %). */
+int tsph_gnn_infer(tsph_gnn *g, const tsph_gnn_graph *graph, float *y);
 /* forward, mean squared error against target (device, 3 per node) over the
  * fluid nodes, gradient into the network's gradient buffer */
 int tsph_gnn_loss_grad(tsph_gnn *g, const tsph_gnn_graph *graph, const float *target,

@@ -125,3 +125,81 @@ def test_gnn_forward_and_gradients_match_the_oracle(gpu_tsph):
         ref = gref[name]
         err = np.max(np.abs(gdev[name] - ref))
         assert err <= 2e-3 * max(1e-6, np.max(np.abs(ref))), (name, err, np.max(np.abs(ref)))
+
+
+def _random_graph_setup(gpu_tsph, seed=4):
+    from tinysph_old_gb300 import surrogate as S
+
+    case = cases.dam_break_mdbc(dp=0.02)
+    s = gpu_tsph.ParticleSystem.from_case(case)
+    rng = np.random.default_rng(seed)
+    st = s.download()
+    fl = st["type"] == 0
+    v = st["v"].copy()
+    v[fl] = rng.normal(0, 0.5, (fl.sum(), 2))
+    rho = st["rho"].copy()
+    rho[fl] += rng.normal(0, 2.0, fl.sum())
+    s.upload(v=v, rho=rho)
+    gb = S.GraphBuffers(case.np).export(s)
+    p = G.init_params(seed)
+    for k in p:
+        p[k] = p[k] + rng.normal(0, 0.05, p[k].shape)
+    return case, s, gb, p
+
+
+@pytest.mark.gpu
+def test_bf16_tensor_core_inference_matches_the_fp32_forward(gpu_tsph):
+    """tsph_gnn_infer (BF16 weights and activations on the tensor cores, FP32
+    accumulation, hardware tanh in the edge SiLU) against tsph_gnn_forward
+    (FP32 throughout): within the BF16 rounding, 2 % of the outputs' rms."""
+    import torch
+
+    case, s, gb, p = _random_graph_setup(gpu_tsph)
+    net = gpu_tsph.Gnn(gb.n)
+    net.set_params(G.flatten(p).astype(np.float32))
+    graph = gb.struct(case.h, 1.0, 2.0)
+    y32 = torch.empty((gb.n, 3), dtype=torch.float32, device="cuda")
+    y16 = torch.empty((gb.n, 3), dtype=torch.float32, device="cuda")
+    net.forward(graph, y32.data_ptr())
+    net.infer(graph, y16.data_ptr())
+    torch.cuda.synchronize()
+    a, b = y32.cpu().numpy(), y16.cpu().numpy()
+    rms = np.sqrt(np.mean(a * a, 0))
+    err = np.sqrt(np.mean((a - b) ** 2, 0))
+    assert np.all(err <= 0.02 * rms), (err, rms)
+    assert np.max(np.abs(a - b)) <= 0.05 * np.max(np.abs(a))
+
+
+@pytest.mark.gpu
+def test_fallback_windows_reproduce_plain_stepping(gpu_tsph):
+    """A rollout whose every window fails its check (tolerance below zero)
+    restores the saved state and runs the plain steps: bit-identical to plain
+    stepping."""
+    from tinysph_old_gb300 import surrogate as S
+
+    case = cases.dam_break_mdbc(dp=0.02)
+    a = gpu_tsph.ParticleSystem.from_case(case)
+    b = gpu_tsph.ParticleSystem.from_case(case)
+    a.step(0, case.dt, 8)
+    b.step(0, case.dt, 8)
+    ro = S.Rollout(a, S.Model.zero(), case.dt, 0, case.h, use_net=False, tol_density=-1.0)
+    ro.run(6)
+    b.step(0, case.dt, 6 * S.K_STRIDE)
+    assert ro.fallbacks == 6
+    sa, sb = a.download(), b.download()
+    oa, ob = np.argsort(sa["index"]), np.argsort(sb["index"])
+    for f in ("r", "v", "rho"):
+        assert np.array_equal(sa[f][oa], sb[f][ob]), f
+
+
+@pytest.mark.gpu
+def test_window_check_on_the_plain_trajectory_is_at_its_floor(gpu_tsph):
+    """The window check (trapezoidal SPH rates at both ends) applied to the
+    plain solver's own windows: far below the 1 % fallback threshold."""
+    from tinysph_old_gb300 import surrogate as S
+
+    case = cases.dam_break_mdbc(dp=0.02)
+    s = gpu_tsph.ParticleSystem.from_case(case)
+    s.step(0, case.dt, 200)
+    fl = S.plain_check_floor(s, 0, case.dt, 5)
+    assert np.all(fl[:, 0] < 1e-3), fl

@@ -17,6 +17,8 @@
 // dz_nj = dS_n SiLU'(z_nj) for dP_n and dz_jn = dS_j SiLU'(z_jn) for dQ_n.
 // Weight gradients are reduced per block into partial sums and then summed
 // in a fixed order (deterministic).
+#include <cuda_bf16.h>
+
 #include <cmath>
 #include <cstdint>
 #include <algorithm>
@@ -514,6 +516,325 @@ __global__ void k_adam(float *__restrict__ p, const float *__restrict__ g, float
     p[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
 }
 
+// ------------------------------------------------------------------ inference
+// The rollout's forward pass: the same network with BF16 weights and
+// activations on the tensor cores (mma.sync m16n8k16, FP32 accumulation),
+// fused per layer, and the edge sums in FP32 with SiLU(z) = (z/2)(1 +
+// tanh(z/2)) on the hardware tanh.  Five launches:
+//   node<0>  h0 = SiLU(A0 x + a0), P0 = h0 Wp0^T + be0, Q0 = h0 Wq0^T
+//   edge     S0 = sum_j SiLU(P0_i + Q0_j + We0 e_ij)
+//   node<1>  m = W2 S + deg b2, h1 = h0 + Wn2 SiLU(Wn1 [h0, m] + bn1) + bn2,
+//            P1 = h1 Wp1^T + be1, Q1 = h1 Wq1^T
+//   edge     S1
+//   node<2>  h2 from h1, S1 as in node<1>; y = Wd h2 + bd
+// A warp owns 16 nodes (one m16 tile); the weights are staged per block in
+// shared memory as BF16 [out][in] rows padded to in + 8 (conflict-free B
+// fragment loads); a GEMM's FP32 accumulators are repacked in registers as
+// the next GEMM's A fragments.
+typedef __nv_bfloat16 bf16;
+constexpr int kInfWarps = 4;
+constexpr int kInfBlocks = 152 * 4;
+
+__device__ __forceinline__ uint32_t pack_bf16(float lo, float hi) {
+    __nv_bfloat162 v = __floats2bfloat162_rn(lo, hi);
+    return *reinterpret_cast<uint32_t *>(&v);
+}
+__device__ __forceinline__ float2 unpack_bf16(uint32_t u) {
+    __nv_bfloat162 v = *reinterpret_cast<__nv_bfloat162 *>(&u);
+    return __bfloat1622float2(v);
+}
+__device__ __forceinline__ float tanh_hw(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float silu_hw(float z) {
+    const float hz = 0.5f * z;
+    return fmaf(hz, tanh_hw(hz), hz);
+}
+// D = A B + D, A 16 x 16 (row), B 16 x 8 (col), BF16 in, FP32 accumulate
+__device__ __forceinline__ void mma_bf16(float c[4], const uint32_t a[4], uint32_t b0,
+                                         uint32_t b1) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+        "{%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// acc[j] (n-blocks j0 .. j0 + NB - 1) += A (KB k-blocks) W^T, W in shared
+// memory as [out][ld] BF16, input columns k0 + 16 kb
+template <int NB, int KB>
+__device__ __forceinline__ void warp_gemm(float (&acc)[NB][4], const uint32_t (&A)[KB][4],
+                                          const bf16 *W, int ld, int j0, int k0, int lane) {
+    const int g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int j = 0; j < NB; j++) {
+#pragma unroll
+        for (int kb = 0; kb < KB; kb++) {
+            const bf16 *w = W + (size_t)(8 * (j0 + j) + g) * ld + k0 + 16 * kb + 2 * t;
+            const uint32_t b0 = *reinterpret_cast<const uint32_t *>(w);
+            const uint32_t b1 = *reinterpret_cast<const uint32_t *>(w + 8);
+            mma_bf16(acc[j], A[kb], b0, b1);
+        }
+    }
+}
+
+// 64 accumulator columns (8 n-blocks) -> A fragments of a K = 64 input
+__device__ __forceinline__ void acc_to_a(const float (&acc)[8][4], uint32_t (&A)[4][4]) {
+#pragma unroll
+    for (int kb = 0; kb < 4; kb++) {
+        A[kb][0] = pack_bf16(acc[2 * kb][0], acc[2 * kb][1]);
+        A[kb][1] = pack_bf16(acc[2 * kb][2], acc[2 * kb][3]);
+        A[kb][2] = pack_bf16(acc[2 * kb + 1][0], acc[2 * kb + 1][1]);
+        A[kb][3] = pack_bf16(acc[2 * kb + 1][2], acc[2 * kb + 1][3]);
+    }
+}
+
+// A fragments of rows r0 .. r0 + 15 of a BF16 [n][64] array (0 past n)
+__device__ __forceinline__ void load_a(const bf16 *X, int r0, int n, int lane, uint32_t (&A)[4][4]) {
+    const int g = lane >> 2, t = lane & 3;
+    const int ra = r0 + g, rb = r0 + g + 8;
+#pragma unroll
+    for (int kb = 0; kb < 4; kb++) {
+        const int c = 16 * kb + 2 * t;
+        A[kb][0] = ra < n ? *reinterpret_cast<const uint32_t *>(X + (size_t)ra * H + c) : 0u;
+        A[kb][1] = rb < n ? *reinterpret_cast<const uint32_t *>(X + (size_t)rb * H + c) : 0u;
+        A[kb][2] = ra < n ? *reinterpret_cast<const uint32_t *>(X + (size_t)ra * H + c + 8) : 0u;
+        A[kb][3] = rb < n ? *reinterpret_cast<const uint32_t *>(X + (size_t)rb * H + c + 8) : 0u;
+    }
+}
+
+// accumulator columns of n-blocks 0..7 -> BF16 [n][64] rows r0 .. r0 + 15
+__device__ __forceinline__ void store_acc(const float (&acc)[8][4], bf16 *Y, int r0, int n,
+                                          int lane) {
+    const int g = lane >> 2, t = lane & 3;
+    const int ra = r0 + g, rb = r0 + g + 8;
+#pragma unroll
+    for (int j = 0; j < 8; j++) {
+        const int c = 8 * j + 2 * t;
+        if (ra < n) *reinterpret_cast<uint32_t *>(Y + (size_t)ra * H + c) = pack_bf16(acc[j][0], acc[j][1]);
+        if (rb < n) *reinterpret_cast<uint32_t *>(Y + (size_t)rb * H + c) = pack_bf16(acc[j][2], acc[j][3]);
+    }
+}
+
+struct InfArgs {
+    GraphDev G;
+    const float *p;  // FP32 parameters (Layout order)
+    int A0, a0;                              // encoder (MODE 0)
+    int W2, b2, Wn1, bn1, Wn2, bn2;          // the layer finished here (MODE 1, 2)
+    int Wpq, be;                             // the next layer's [Wp; Wq] and be (MODE 0, 1)
+    int Wd, bd;                              // decoder (MODE 2)
+    bf16 *h, *P, *Q;
+    const bf16 *S;
+    float *y;
+};
+
+// shared memory of node<MODE>: BF16 weights, then FP32 vectors
+constexpr int kLd64 = H + 8, kLd128 = 2 * H + 8;
+template <int MODE> struct InfSmem {
+    static constexpr int w2 = 0;
+    static constexpr int wn1 = w2 + (MODE ? H * kLd64 : 0);
+    static constexpr int wn2 = wn1 + (MODE ? H * kLd128 : 0);
+    static constexpr int wpq = wn2 + (MODE ? H * kLd64 : 0);
+    static constexpr int wd = wpq + (MODE < 2 ? 2 * H * kLd64 : 0);
+    static constexpr int bf16_end = wd + (MODE == 2 ? 8 * kLd64 : 0);
+    static constexpr int bytes_bf16 = ((bf16_end * 2 + 15) / 16) * 16;
+    // FP32: A0 (H*NIN), a0, b2, bn1, bn2, be, bd (8)
+    static constexpr int f_A0 = 0, f_a0 = f_A0 + H * NIN, f_b2 = f_a0 + H, f_bn1 = f_b2 + H,
+                         f_bn2 = f_bn1 + H, f_be = f_bn2 + H, f_bd = f_be + H, f_end = f_bd + 8;
+    static constexpr int bytes = bytes_bf16 + 4 * f_end;
+};
+
+__device__ __forceinline__ void stage_w(bf16 *dst, int ld, const float *src, int rows, int cols,
+                                        int rows_pad) {
+    for (int e = threadIdx.x; e < rows_pad * ld; e += blockDim.x) {
+        const int r = e / ld, c = e - r * ld;
+        dst[e] = __float2bfloat16_rn(r < rows && c < cols ? src[r * cols + c] : 0.f);
+    }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(32 * kInfWarps) k_inf_node(InfArgs a) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    typedef InfSmem<MODE> SM;
+    bf16 *sb = reinterpret_cast<bf16 *>(smem_raw);
+    float *sf = reinterpret_cast<float *>(smem_raw + SM::bytes_bf16);
+    const float *p = a.p;
+    if (MODE) {
+        stage_w(sb + SM::w2, kLd64, p + a.W2, H, H, H);
+        stage_w(sb + SM::wn1, kLd128, p + a.Wn1, H, 2 * H, H);
+        stage_w(sb + SM::wn2, kLd64, p + a.Wn2, H, H, H);
+    }
+    if (MODE < 2) stage_w(sb + SM::wpq, kLd64, p + a.Wpq, 2 * H, H, 2 * H);
+    if (MODE == 2) stage_w(sb + SM::wd, kLd64, p + a.Wd, NOUT, H, 8);
+    for (int e = threadIdx.x; e < H; e += blockDim.x) {
+        if (MODE == 0) {
+            sf[SM::f_a0 + e] = p[a.a0 + e];
+            for (int k = 0; k < NIN; k++) sf[SM::f_A0 + e * NIN + k] = p[a.A0 + e * NIN + k];
+        } else {
+            sf[SM::f_b2 + e] = p[a.b2 + e];
+            sf[SM::f_bn1 + e] = p[a.bn1 + e];
+            sf[SM::f_bn2 + e] = p[a.bn2 + e];
+        }
+        if (MODE < 2) sf[SM::f_be + e] = p[a.be + e];
+        if (MODE == 2 && e < 8) sf[SM::f_bd + e] = e < NOUT ? p[a.bd + e] : 0.f;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int g = lane >> 2, t = lane & 3;
+    const int n = a.G.n;
+    for (int tile = blockIdx.x * kInfWarps + warp; tile * 16 < n; tile += gridDim.x * kInfWarps) {
+        const int r0 = tile * 16, ra = r0 + g, rb = r0 + g + 8;
+        float hc[8][4];  // h of this layer's output, FP32, accumulator layout
+        if (MODE == 0) {
+            float xa[NIN] = {0.f, 0.f, 0.f, 0.f}, xb[NIN] = {0.f, 0.f, 0.f, 0.f};
+            if (ra < n) {
+                const float2 v = a.G.vel[ra];
+                xa[0] = v.x * a.G.inv_U; xa[1] = v.y * a.G.inv_U;
+                xa[2] = a.G.srho[ra] * a.G.inv_S; xa[3] = a.G.wall[ra];
+            }
+            if (rb < n) {
+                const float2 v = a.G.vel[rb];
+                xb[0] = v.x * a.G.inv_U; xb[1] = v.y * a.G.inv_U;
+                xb[2] = a.G.srho[rb] * a.G.inv_S; xb[3] = a.G.wall[rb];
+            }
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+#pragma unroll
+                for (int q = 0; q < 2; q++) {
+                    const int c = 8 * j + 2 * t + q;
+                    float za = sf[SM::f_a0 + c], zb = za;
+#pragma unroll
+                    for (int k = 0; k < NIN; k++) {
+                        const float w = sf[SM::f_A0 + c * NIN + k];
+                        za = fmaf(w, xa[k], za);
+                        zb = fmaf(w, xb[k], zb);
+                    }
+                    hc[j][q] = silu(za);
+                    hc[j][2 + q] = silu(zb);
+                }
+            }
+        } else {
+            uint32_t AS[4][4], Ah[4][4], Am[4][4], At[4][4];
+            load_a(a.S, r0, n, lane, AS);
+            float m[8][4];
+            const float da = ra < n ? (float)a.G.deg[ra] : 0.f, db = rb < n ? (float)a.G.deg[rb] : 0.f;
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int c = 8 * j + 2 * t;
+                m[j][0] = da * sf[SM::f_b2 + c];
+                m[j][1] = da * sf[SM::f_b2 + c + 1];
+                m[j][2] = db * sf[SM::f_b2 + c];
+                m[j][3] = db * sf[SM::f_b2 + c + 1];
+            }
+            warp_gemm<8, 4>(m, AS, sb + SM::w2, kLd64, 0, 0, lane);
+            acc_to_a(m, Am);
+            load_a(a.h, r0, n, lane, Ah);
+            float u[8][4];
+#pragma unroll
+            for (int j = 0; j < 8; j++) {
+                const int c = 8 * j + 2 * t;
+                u[j][0] = u[j][2] = sf[SM::f_bn1 + c];
+                u[j][1] = u[j][3] = sf[SM::f_bn1 + c + 1];
+            }
+            warp_gemm<8, 4>(u, Ah, sb + SM::wn1, kLd128, 0, 0, lane);
+            warp_gemm<8, 4>(u, Am, sb + SM::wn1, kLd128, 0, H, lane);
+#pragma unroll
+            for (int j = 0; j < 8; j++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) u[j][q] = silu(u[j][q]);
+            acc_to_a(u, At);
+            // h + bn2 in the accumulator layout (h from its A fragments)
+#pragma unroll
+            for (int kb = 0; kb < 4; kb++) {
+#pragma unroll
+                for (int half = 0; half < 2; half++) {
+                    const int j = 2 * kb + half, c = 8 * j + 2 * t;
+                    const float2 lo = unpack_bf16(Ah[kb][2 * half]), hi = unpack_bf16(Ah[kb][2 * half + 1]);
+                    hc[j][0] = lo.x + sf[SM::f_bn2 + c];
+                    hc[j][1] = lo.y + sf[SM::f_bn2 + c + 1];
+                    hc[j][2] = hi.x + sf[SM::f_bn2 + c];
+                    hc[j][3] = hi.y + sf[SM::f_bn2 + c + 1];
+                }
+            }
+            warp_gemm<8, 4>(hc, At, sb + SM::wn2, kLd64, 0, 0, lane);
+        }
+        uint32_t Ahn[4][4];
+        acc_to_a(hc, Ahn);
+        if (MODE < 2) {
+            store_acc(hc, a.h, r0, n, lane);
+            float pq[8][4];
+#pragma unroll
+            for (int half = 0; half < 2; half++) {  // P (+ be), then Q
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const int c = 8 * j + 2 * t;
+                    const float b0 = half ? 0.f : sf[SM::f_be + c], b1 = half ? 0.f : sf[SM::f_be + c + 1];
+                    pq[j][0] = pq[j][2] = b0;
+                    pq[j][1] = pq[j][3] = b1;
+                }
+                warp_gemm<8, 4>(pq, Ahn, sb + SM::wpq, kLd64, 8 * half, 0, lane);
+                store_acc(pq, half ? a.Q : a.P, r0, n, lane);
+            }
+        } else {
+            float yd[1][4];
+            yd[0][0] = yd[0][2] = sf[SM::f_bd + 2 * t];
+            yd[0][1] = yd[0][3] = sf[SM::f_bd + 2 * t + 1];
+            warp_gemm<1, 4>(yd, Ahn, sb + SM::wd, kLd64, 0, 0, lane);
+#pragma unroll
+            for (int q = 0; q < 2; q++) {
+                const int c = 2 * t + q;
+                if (c < NOUT) {
+                    if (ra < n) a.y[(size_t)ra * NOUT + c] = yd[0][q];
+                    if (rb < n) a.y[(size_t)rb * NOUT + c] = yd[0][2 + q];
+                }
+            }
+        }
+    }
+}
+
+// S_i = sum_j SiLU(P_i + Q_j + We e_ij) (P holds be), warp per node, lane
+// c holds channels 2c and 2c + 1
+__global__ void __launch_bounds__(kGB) k_inf_edge(GraphDev G, const bf16 *__restrict__ P,
+                                                  const bf16 *__restrict__ Q,
+                                                  const float *__restrict__ We,
+                                                  bf16 *__restrict__ S) {
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (i >= G.n) return;
+    const int c0 = 2 * lane;
+    float w0[EIN], w1[EIN];
+#pragma unroll
+    for (int k = 0; k < EIN; k++) {
+        w0[k] = We[c0 * EIN + k];
+        w1[k] = We[(c0 + 1) * EIN + k];
+    }
+    const float2 pi = unpack_bf16(*reinterpret_cast<const uint32_t *>(P + (size_t)i * H + c0));
+    float s0 = 0.f, s1 = 0.f;
+    const int d = G.deg[i];
+    const double2 ri = G.pos[i];
+    const float2 vi = G.vel[i];
+    for (int k0 = 0; k0 < d; k0 += 32) {
+        const EdgeLane mine = edge_lane(G, i, ri, vi, k0 + lane);
+        const int cnt = min(32, d - k0);
+        for (int tt = 0; tt < cnt; tt++) {
+            const int j = __shfl_sync(0xffffffffu, mine.j, tt);
+            const float2 qj = unpack_bf16(*reinterpret_cast<const uint32_t *>(Q + (size_t)j * H + c0));
+            float z0 = pi.x + qj.x, z1 = pi.y + qj.y;
+#pragma unroll
+            for (int q = 0; q < EIN; q++) {
+                const float eq = __shfl_sync(0xffffffffu, mine.e[q], tt);
+                z0 = fmaf(w0[q], eq, z0);
+                z1 = fmaf(w1[q], eq, z1);
+            }
+            s0 += silu_hw(z0);
+            s1 += silu_hw(z1);
+        }
+    }
+    *reinterpret_cast<uint32_t *>(S + (size_t)i * H + c0) = pack_bf16(s0, s1);
+}
+
 #define GCK(call)                                                                 \
     do {                                                                          \
         cudaError_t e_ = (call);                                                  \
@@ -540,6 +861,7 @@ struct tsph_gnn {
     float *y = nullptr, *dy = nullptr, *dh = nullptr, *dh2 = nullptr, *dhm = nullptr,
           *du = nullptr, *dP = nullptr, *dQ = nullptr, *dS = nullptr;
     float *part = nullptr, *epart = nullptr, *lpart = nullptr;
+    float *ib[4] = {};  // inference activations h, P, Q, S (BF16, cap x 64 each)
     int adam_t = 0;
     tsph::GraphDev G{};
     ~tsph_gnn() {
@@ -709,6 +1031,53 @@ int set_graph(tsph_gnn *N, const tsph_gnn_graph *gr) {
     return 0;
 }
 
+// the BF16 tensor-core forward (the rollout's): y [n][3]
+int infer(tsph_gnn *N, float *y) {
+    const int n = N->G.n;
+    if (n == 0) return 0;
+    const Layout &L = N->L;
+    bf16 *hb = reinterpret_cast<bf16 *>(N->ib[0]), *Pb = reinterpret_cast<bf16 *>(N->ib[1]),
+         *Qb = reinterpret_cast<bf16 *>(N->ib[2]), *Sb = reinterpret_cast<bf16 *>(N->ib[3]);
+    GCK(cudaFuncSetAttribute(k_inf_node<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, InfSmem<0>::bytes));
+    GCK(cudaFuncSetAttribute(k_inf_node<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, InfSmem<1>::bytes));
+    GCK(cudaFuncSetAttribute(k_inf_node<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, InfSmem<2>::bytes));
+    const int nb = std::min(gblocks(n, 16 * kInfWarps), kInfBlocks);
+    const int eb = gblocks((long long)n * 32);
+    InfArgs a{};
+    a.G = N->G;
+    a.p = N->p;
+    a.h = hb;
+    a.P = Pb;
+    a.Q = Qb;
+    a.S = Sb;
+    a.y = y;
+    a.A0 = L.A0;
+    a.a0 = L.a0;
+    a.Wpq = L.Wp[0];
+    a.be = L.be[0];
+    k_inf_node<0><<<nb, 32 * kInfWarps, InfSmem<0>::bytes, N->st>>>(a);
+    for (int l = 0; l < NL; l++) {
+        k_inf_edge<<<eb, kGB, 0, N->st>>>(N->G, Pb, Qb, N->p + L.We[l], Sb);
+        a.W2 = L.W2[l];
+        a.b2 = L.b2[l];
+        a.Wn1 = L.Wn1[l];
+        a.bn1 = L.bn1[l];
+        a.Wn2 = L.Wn2[l];
+        a.bn2 = L.bn2[l];
+        if (l + 1 < NL) {
+            a.Wpq = L.Wp[l + 1];
+            a.be = L.be[l + 1];
+            k_inf_node<1><<<nb, 32 * kInfWarps, InfSmem<1>::bytes, N->st>>>(a);
+        } else {
+            a.Wd = L.Wd;
+            a.bd = L.bd;
+            k_inf_node<2><<<nb, 32 * kInfWarps, InfSmem<2>::bytes, N->st>>>(a);
+        }
+    }
+    GCK(cudaGetLastError());
+    return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -756,6 +1125,7 @@ int tsph_gnn_create(int capacity, void *stream, tsph_gnn **out) {
     A(&N->part, (size_t)kWgBlocks * kWgMaxOut);
     A(&N->epart, (size_t)gblocks((long long)c * 32) * H * (EIN + 1));
     A(&N->lpart, (size_t)gblocks((long long)c));
+    for (int k = 0; k < 4; k++) A(&N->ib[k], (size_t)H / 2 * c);
     if (!rc && (cudaMemset(N->p, 0, 4 * P) != cudaSuccess || cudaMemset(N->m1, 0, 4 * P) != cudaSuccess ||
                 cudaMemset(N->m2, 0, 4 * P) != cudaSuccess)) {
         set_last_error("cudaMemset failed");
@@ -803,6 +1173,13 @@ int tsph_gnn_forward(tsph_gnn *N, const tsph_gnn_graph *graph, float *y) {
     int rc;
     if ((rc = set_graph(N, graph)) || (rc = forward(N))) return rc;
     if (y) GCK(cudaMemcpyAsync(y, N->y, 4 * (size_t)NOUT * graph->n_nodes, cudaMemcpyDeviceToDevice, N->st));
+    return TSPH_OK;
+}
+
+int tsph_gnn_infer(tsph_gnn *N, const tsph_gnn_graph *graph, float *y) {
+    if (!N || !y) return (set_last_error("null argument"), TSPH_ERR_ARG);
+    int rc;
+    if ((rc = set_graph(N, graph)) || (rc = infer(N, y))) return rc;
     return TSPH_OK;
 }
 

@@ -41,7 +41,7 @@ ABI_SYMBOLS = (
     "tsph_export_graph", "tsph_apply_update", "tsph_window_check", "tsph_get_stream", "tsph_state_save",
     "tsph_state_restore", "tsph_gnn_n_params", "tsph_gnn_create",
     "tsph_gnn_destroy", "tsph_gnn_set_params", "tsph_gnn_get_params", "tsph_gnn_get_grads",
-    "tsph_gnn_forward", "tsph_gnn_loss_grad", "tsph_gnn_adam",
+    "tsph_gnn_forward", "tsph_gnn_infer", "tsph_gnn_loss_grad", "tsph_gnn_adam",
     "tsph_ale_create", "tsph_ale_destroy", "tsph_ale_add_particles", "tsph_ale_set_scheme",
     "tsph_ale_np", "tsph_ale_divide_to_cells", "tsph_ale_particle_to_cell", "tsph_ale_gradient",
     "tsph_ale_forces", "tsph_ale_leapfrog_one", "tsph_ale_leapfrog_two", "tsph_ale_step",
@@ -165,6 +165,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_gnn_get_params.argtypes = [P, P]
     L.tsph_gnn_get_grads.argtypes = [P, P]
     L.tsph_gnn_forward.argtypes = [P, C.POINTER(GnnGraph), P]
+    L.tsph_gnn_infer.argtypes = [P, C.POINTER(GnnGraph), P]
     L.tsph_gnn_loss_grad.argtypes = [P, C.POINTER(GnnGraph), P, C.POINTER(D)]
     L.tsph_gnn_adam.argtypes = [P, D, D, D, D]
     L.tsph_save_checkpoint.argtypes = [P, C.c_char_p]
@@ -749,6 +750,10 @@ class Gnn:
 
     def forward(self, graph, y_ptr=None):
         _check(self._L.tsph_gnn_forward(self._h, C.byref(graph), y_ptr))
+
+    def infer(self, graph, y_ptr):
+        """The BF16 tensor-core forward (tsph_gnn_infer)."""
+        _check(self._L.tsph_gnn_infer(self._h, C.byref(graph), y_ptr))
 
     def loss_grad(self, graph, target_ptr):
         l = C.c_double()
