@@ -6,7 +6,7 @@ A window, from a state whose last forces pass gave a_0 and drho_0
 (tsph_step leaves the state so):
 
     graph   tsph_export_graph: nodes = particles, edges = pairs with r <= 2h
-    network y = GNN(graph)                                    (tsph_gnn_forward)
+    network y = GNN(graph)                                    (tsph_gnn_infer)
     update  kick   v += k dt a_0 + U_out (y0, y1)             (tsph_apply_update 1)
             a forces pass with the kicked velocities gives drho*
             drift  rho += k dt drho* + S_out y2,
@@ -436,7 +436,8 @@ class Rollout:
         s.state_save()
         self.gb.export(s)
         if self.use_net:
-            self.net.forward(self.gb.struct(self.h, self.m.u_in, self.m.s_in), self.y.data_ptr())
+            # the BF16 tensor-core forward (trained in FP32 by tsph_gnn_loss_grad)
+            self.net.infer(self.gb.struct(self.h, self.m.u_in, self.m.s_in), self.y.data_ptr())
         window_update(s, self.y.data_ptr(), self.m, self.kdt, self.wall_model, self.scheme)
         lost = end_of_window(s, self.wall_model)
         mx, rms, mom, _, worst = s.window_check(self.kdt)
