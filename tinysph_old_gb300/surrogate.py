@@ -479,3 +479,120 @@ def plain_check_floor(system, wall_model, dt, n_windows, k=K_STRIDE):
         system.step(wall_model, dt, k)
         out.append(system.window_check(k * dt)[:3])
     return np.array(out)
+
+
+# ------------------------------------------------------------------ evaluation
+
+GAUGES_X = (0.3, 0.8, 1.3, 1.5)  # free-surface gauges (Water_Elevation), m
+PROBES = ((1.60, 0.02), (1.60, 0.10), (1.60, 0.20))  # pressure probes at the far wall, m
+
+
+def observe(system, front_y=0.02):
+    """The quantities the surrogate is judged on: water front (largest fluid
+    x with y <= front_y), free-surface elevation at the gauges, pressure at
+    the probes (Shepard, as Pressure_in_point)."""
+    return dict(front=system.water_front(front_y),
+                level=system.water_level(np.array(GAUGES_X), 0.0).tolist(),
+                pressure=system.point_fields(np.array(PROBES))[:, 1].tolist())
+
+
+def compare_runs(case, model, t_end, marks, log=None, use_net=True):
+    """Plain SPH and the surrogate from the same start to `t_end`, observed at
+    `marks`; device times of both and the surrogate's fallback rate."""
+    import torch
+
+    out = dict(marks=list(marks), np=None)
+    for kind in ("plain", "surrogate"):
+        s = sph.ParticleSystem.from_case(case)
+        s.step(0, case.dt, K_STRIDE)  # a forces pass for the first window
+        out["np"] = s.np
+        obs = []
+        done = K_STRIDE
+        ro = None
+        if kind == "surrogate":
+            ro = Rollout(s, model, case.dt, case.wall_model, case.h, use_net=use_net)
+        torch.cuda.synchronize()
+        t0 = time.time()
+        for t in marks:
+            nw = max(0, (int(round(t / case.dt)) - done) // K_STRIDE)
+            if ro is None:
+                s.step(case.wall_model, case.dt, nw * K_STRIDE)
+            else:
+                ro.run(nw)
+            done += nw * K_STRIDE
+            s.sync()
+            t1 = time.time()
+            obs.append(observe(s))
+            t0 += time.time() - t1  # observation time excluded
+        torch.cuda.synchronize()
+        out[kind] = dict(obs=obs, seconds=time.time() - t0, steps=done - K_STRIDE)
+        if ro is not None:
+            out[kind]["fallback_rate"] = ro.fallback_rate
+            out[kind]["windows"] = ro.windows
+        if log:
+            log(f"{kind}: {out[kind]['seconds']:.1f} s" +
+                (f", fallback {ro.fallback_rate:.3f}" if ro is not None else ""))
+    p, q = out["plain"]["obs"], out["surrogate"]["obs"]
+    h0 = 0.3
+    out["errors"] = dict(
+        front=[abs(b["front"] - a["front"]) / a["front"] for a, b in zip(p, q)],
+        level=[max(abs(x - y) for x, y in zip(a["level"], b["level"])) / h0 for a, b in zip(p, q)],
+        pressure=[max(abs(x - y) for x, y in zip(a["pressure"], b["pressure"])) /
+                  (1000.0 * 9.81 * h0) for a, b in zip(p, q)])
+    for kind in ("plain", "surrogate"):
+        out[kind]["particle_steps_per_s"] = out["np"] * out[kind]["steps"] / out[kind]["seconds"]
+    return out
+
+
+def pipeline(out_model, n_train=400, n_held=50, t_train=0.3, samples=8, cases_per_system=25,
+             iters=1500, seed=0, eval_dp=0.0005, t_eval=1.0, log=print):
+    """Config 5 end to end: training windows from the surrogate's own rollouts
+    (y = 0 model, plain fallback) over `n_train` seeded dam breaks at
+    dp = 0.002 m, training on the device, the one-window error on `n_held`
+    held-out seeds against the method without the network, and plain versus
+    surrogate on the benchmark dam break at `eval_dp` for `t_eval` s."""
+    from . import batch as B
+    from . import cases as CS
+
+    res = {}
+    specs = training_specs(n_train, seed)
+    held_specs = training_specs(n_held, seed + 1)
+    h = B.case_arrays(specs[0]).h
+    zero = Model.zero()
+    t0 = time.time()
+    data = generate(specs, t_train, samples, cases_per_system, rollout_model=zero, log=log)
+    held = generate(held_specs, t_train, samples, cases_per_system, rollout_model=zero, log=log)
+    res["generate_s"] = time.time() - t0
+    scales = fit_scales(data)
+    t0 = time.time()
+    model, hist = train(data, scales, h, iters=iters, seed=seed, log=log, log_every=250)
+    res["train_s"] = time.time() - t0
+    model.meta.update(n_train=n_train, t_train=t_train, dp=0.002)
+    model.save(out_model)
+    a, z = evaluate(model, held, h)
+    res["held_out_mse_net"], res["held_out_mse_without"] = a.tolist(), z.tolist()
+    log(f"held-out one-window mse: network {a}, without it {z}")
+    del data, held
+    case = CS.dam_break_benchmark(dp=eval_dp)
+    marks = [round(0.05 * i, 2) for i in range(1, int(round(t_eval / 0.05)) + 1)]
+    res["eval"] = compare_runs(case, model, t_eval, marks, log=log)
+    return model, res
+
+
+if __name__ == "__main__":
+    import argparse
+
+    ap = argparse.ArgumentParser(description="train and evaluate the surrogate")
+    ap.add_argument("--out-model", required=True)
+    ap.add_argument("--out-json", required=True)
+    ap.add_argument("--n-train", type=int, default=400)
+    ap.add_argument("--n-held", type=int, default=50)
+    ap.add_argument("--t-train", type=float, default=0.3)
+    ap.add_argument("--iters", type=int, default=1500)
+    ap.add_argument("--eval-dp", type=float, default=0.0005)
+    ap.add_argument("--t-eval", type=float, default=1.0)
+    a = ap.parse_args()
+    _, r = pipeline(a.out_model, a.n_train, a.n_held, a.t_train, iters=a.iters,
+                    eval_dp=a.eval_dp, t_eval=a.t_eval, log=lambda m: print(m, flush=True))
+    with open(a.out_json, "w") as f:
+        json.dump(r, f, indent=1)
