@@ -13,6 +13,10 @@ kernel, cpu_baseline (the CPU oracle on the host cores) and clocks.
 instead (the oracle restatement, all host cores; the reference sources are
 not present on the GPU host).
 
+``--workload surrogate`` measures the learned surrogate: one step = one
+window of 8 SPH steps (network, checked update, plain fallback), next to the
+plain step on the same case.
+
 ``--workload ale`` measures the Riemann / ALE-SPH step instead: the BT-wall
 dam break of cases/ALESPH_dambreakLong at dp = 0.0004 m (1,125,000 fluid
 particles), FP32 fluxes with FP64 leap-frog integration.
@@ -480,6 +484,113 @@ def run_batch(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
+SURROGATE_MODEL = os.path.join(ROOT, "tinysph_old_gb300", "data", "surrogate_dam_break.npz")
+
+
+def run_surrogate(args, rank, world, local):
+    """The learned surrogate on the 720k benchmark dam break: one bench step =
+    one window of k = 8 SPH steps (graph export, BF16 network, update, forces
+    pass, window check, plain fallback when the check fails), next to 8 plain
+    steps from the same state; the water-front error against plain SPH at the
+    end of the timed region."""
+    import numpy as np
+    import torch
+
+    from tinysph_old_gb300 import cases, sph
+    from tinysph_old_gb300 import surrogate as S
+
+    torch.cuda.set_device(local)
+    if not os.path.exists(SURROGATE_MODEL):
+        raise SystemExit(f"missing trained model {SURROGATE_MODEL}")
+    m = S.Model.load(SURROGATE_MODEL)
+    case = cases.dam_break_benchmark(args.dp)
+    k = m.k
+
+    def make():
+        s = sph.ParticleSystem.from_case(case)
+        s.step(case.wall_model, case.dt, args.warmup * k)
+        s.sync()
+        return s
+
+    def timed(s, body, nsteps):
+        st = torch.cuda.ExternalStream(s.stream_ptr())
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(st)
+        for _ in range(nsteps):
+            body()
+        e1.record(st)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1)
+
+    plain = make()
+    n = plain.np
+    with ClockSampler(local) as clocks:
+        ms_plain = timed(plain, lambda: plain.step(case.wall_model, case.dt, k), args.steps)
+        sur = make()
+        ro = S.Rollout(sur, m, case.dt, case.wall_model, case.h, use_net=True)
+        ro.run(3)  # warm-up windows (the network's first launches)
+        ro.windows = ro.fallbacks = 0
+        ro.checks.clear()
+        plain.step(case.wall_model, case.dt, 3 * k)  # same physical time as the surrogate
+        ms_sur = timed(sur, ro.window, args.steps)
+    value = n * k * args.steps / (ms_sur / 1000.0)
+    plain_value = n * k * args.steps / (ms_plain / 1000.0)
+    fa, fb = plain.water_front(0.02), sur.water_front(0.02)
+    # time of the network's forward alone
+    gb = ro.gb.export(sur)
+    g = gb.struct(case.h, m.u_in, m.s_in)
+    inf_ms = timed(sur, lambda: ro.net.infer(g, ro.y.data_ptr()), 10) / 10
+    # e2e: state in from pinned host memory, one window, state out
+    hr = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+    hv = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+    hrho = torch.empty((n,), dtype=torch.float64, pin_memory=True)
+    mask = sph.F_R | sph.F_V | sph.F_RHO
+    sur.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+    t0 = time.perf_counter()
+    for _ in range(args.e2e_steps):
+        sur.upload_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+        sur.particle_to_cell()
+        sur.mdbc_density()
+        sur.density_to_pressure()
+        sur.compute_forces(case.wall_model)
+        ro.window()
+        sur.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+    e2e_value = n * k * args.e2e_steps / (time.perf_counter() - t0)
+    checks = np.array([c[:3] for c in ro.checks]) if ro.checks else np.zeros((1, 3))
+    peak, peak_kind = measured_peaks()
+    line = {
+        "metric": METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_sur / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 network (tensor cores, f32 accumulate); f32 pair math, f64 positions",
+        "data": "synthetic (dam-break lattice built like the reference's generators)",
+        "config": {"workload": f"learned surrogate, mDBC dam break dp={args.dp}, {n} particles; "
+                               f"one step = one window of {k} SPH steps",
+                   "particles": n, "model": os.path.relpath(SURROGATE_MODEL, ROOT),
+                   "l2": "inputs larger than L2 (no flush)", "parallelism": "single GPU"},
+        "plain": {"value": plain_value, "ms_per_window": ms_plain / args.steps,
+                  "surrogate_over_plain": value / plain_value},
+        "fallback_rate": ro.fallback_rate,
+        "check_median": {"density": float(np.median(checks[:, 0])),
+                         "momentum": float(np.median(checks[:, 2]))},
+        "front_error_end": abs(fb - fa) / fa,
+        "infer_ms": inf_ms,
+        "e2e": {"value": e2e_value, "unit": "particle-steps/s",
+                "h2d_bytes_per_step": n * 40, "d2h_bytes_per_step": n * 40,
+                "path": "tsph_upload(r,v,rho) + binning + forces pass + one surrogate window + "
+                        "tsph_download(r,v,rho), pinned host buffers"},
+        "roofline": {"bound": "hbm", "achieved": None, "peak": peak, "unit": "GB/s",
+                     "frac": None, "traffic": None, "peak_kind": peak_kind,
+                     "note": "the window mixes the network (tensor cores, SFU-bound edge sums) "
+                             "and the plain step; the plain step's pair-kernel roofline is in "
+                             "the dam_break workload's line"},
+        "gpu_launches": int(args.steps * (20 + ro.fallback_rate * k * 13)),
+        "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, rank, world):
     """The reference arm: the CPU restatement of the reference's step on all
     host cores, on the same workload.  Rank 0 only."""
@@ -534,7 +645,8 @@ def main():
     ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=20)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="dam_break", choices=["dam_break", "ale", "batch"])
+    ap.add_argument("--workload", default="dam_break",
+                    choices=["dam_break", "ale", "batch", "surrogate"])
     ap.add_argument("--cases", type=int, default=512, help="batch workload: number of cases")
     ap.add_argument("--seed", type=int, default=0, help="batch workload: case seed")
     ap.add_argument("--loop-steps", type=int, default=10,
@@ -566,6 +678,10 @@ def main():
     if args.workload == "batch":
         if rank == 0:
             run_batch(args, rank, world, local)
+        return
+    if args.workload == "surrogate":
+        if rank == 0:
+            run_surrogate(args, rank, world, local)
         return
 
     import numpy as np
