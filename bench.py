@@ -484,7 +484,7 @@ def run_batch(args, rank, world, local):
     print(json.dumps(line), flush=True)
 
 
-SURROGATE_MODEL = os.path.join(ROOT, "tinysph_old_gb300", "data", "surrogate_dam_break.npz")
+SURROGATE_MODEL = os.path.join(ROOT, "tinysph_old_gb300", "data", "surrogate_dam_break.npz")  # surrogate.MODEL_PATH
 
 
 def run_surrogate(args, rank, world, local):

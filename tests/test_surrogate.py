@@ -203,3 +203,39 @@ def test_window_check_on_the_plain_trajectory_is_at_its_floor(gpu_tsph):
     s.step(0, case.dt, 200)
     fl = S.plain_check_floor(s, 0, case.dt, 5)
     assert np.all(fl[:, 0] < 1e-3), fl
+
+
+def test_training_specs_and_model_file_round_trip(tmp_path):
+    """The seeded training tanks keep the column area (about 45k particles at
+    dp = 0.002 m) with aspect ratios in range; a model file keeps parameters
+    and scales."""
+    from tinysph_old_gb300 import surrogate as S
+
+    specs = S.training_specs(20, 3)
+    for sp in specs:
+        assert abs(sp.col_w * sp.col_h - 0.18) < 1e-12
+        assert 0.25 <= sp.col_h / sp.col_w <= 2.0 and sp.col_h < 0.8 and sp.col_w < 1.61
+    assert S.training_specs(20, 3) == specs and S.training_specs(20, 4) != specs
+    m = S.Model(np.arange(G.n_params(), dtype=np.float32), 0.8, 2.4, 0.027, 1.06, 8, {"a": 1})
+    m.save(tmp_path / "m.npz")
+    r = S.Model.load(tmp_path / "m.npz")
+    assert np.array_equal(r.params, m.params) and r.meta == {"a": 1}
+    assert (r.u_in, r.s_in, r.u_out, r.s_out, r.k) == (0.8, 2.4, 0.027, 1.06, 8)
+
+
+@pytest.mark.gpu
+def test_trained_network_gains_over_the_window_without_it(gpu_tsph):
+    """The committed model against y = 0 (one explicit window of k dt from the
+    rates alone) on windows of held-out tanks (seeds the training never saw),
+    taken from the surrogate's own rollout: the network removes most of the
+    window's error in dv and in rho."""
+    from tinysph_old_gb300 import surrogate as S
+    from tinysph_old_gb300 import batch as B
+
+    model = S.Model.load(S.MODEL_PATH)
+    specs = S.training_specs(2, 777)
+    held = S.generate(specs, 0.15, 3, cases_per_system=2, rollout_model=S.Model.zero())
+    h = B.case_arrays(specs[0]).h
+    net, zero = S.evaluate(model, held, h)
+    ratio = net / zero
+    assert ratio[1] < 0.6 and ratio[2] < 0.6, ratio

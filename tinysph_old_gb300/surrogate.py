@@ -31,6 +31,7 @@ from __future__ import annotations
 
 import json
 import math
+import os
 import time
 from dataclasses import dataclass, field
 
@@ -39,6 +40,9 @@ import numpy as np
 from . import sph
 
 K_SLOTS = 48  # neighbour slots per node (the SPH pair set has ~24-36)
+# the trained model shipped with the package (python -m tinysph_old_gb300.surrogate)
+MODEL_PATH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "data",
+                          "surrogate_dam_break.npz")
 K_STRIDE = 8  # SPH steps per surrogate window
 
 
