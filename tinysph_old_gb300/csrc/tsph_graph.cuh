@@ -98,10 +98,26 @@ static __global__ void k_fluid_sum2(const uint32_t *__restrict__ fstart, int nce
         b += __shfl_xor_sync(0xffffffffu, b, o);
         c += __shfl_xor_sync(0xffffffffu, c, o);
     }
-    if ((threadIdx.x & 31) == 0 && c > 0) {
-        atomicAdd(out, a);
-        atomicAdd(out + 1, b);
-        atomicAdd(out + 2, c);
+    // one atomic per block (blockDim.x = kBlock)
+    __shared__ double red[3][kBlock / 32];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        red[0][w] = a;
+        red[1][w] = b;
+        red[2][w] = c;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < kBlock / 32; k++) {
+            a += red[0][k];
+            b += red[1][k];
+            c += red[2][k];
+        }
+        if (c > 0) {
+            atomicAdd(out, a);
+            atomicAdd(out + 1, b);
+            atomicAdd(out + 2, c);
+        }
     }
 }
 
@@ -203,14 +219,39 @@ __global__ void k_window_check(FluidState<T> F, const uint32_t *__restrict__ fst
         const unsigned long long w = __shfl_xor_sync(0xffffffffu, arg, o);
         arg = w > arg ? w : arg;
     }
-    if ((threadIdx.x & 31) == 0 && one > 0) {
-        atomicMax(reinterpret_cast<unsigned long long *>(out), (unsigned long long)__double_as_longlong(mx));
-        atomicAdd(out + 1, sq);
-        atomicAdd(out + 2, ex);
-        atomicAdd(out + 3, ey);
-        atomicAdd(out + 4, dvc);
-        atomicAdd(out + 5, one);
-        atomicMax(reinterpret_cast<unsigned long long *>(out + 6), arg);
+    // one set of atomics per block (blockDim.x = kBlock)
+    __shared__ double red[6][kBlock / 32];
+    __shared__ unsigned long long rarg[kBlock / 32];
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        red[0][w] = mx;
+        red[1][w] = sq;
+        red[2][w] = ex;
+        red[3][w] = ey;
+        red[4][w] = dvc;
+        red[5][w] = one;
+        rarg[w] = arg;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < kBlock / 32; k++) {
+            mx = fmax(mx, red[0][k]);
+            sq += red[1][k];
+            ex += red[2][k];
+            ey += red[3][k];
+            dvc += red[4][k];
+            one += red[5][k];
+            arg = rarg[k] > arg ? rarg[k] : arg;
+        }
+        if (one > 0) {
+            atomicMax(reinterpret_cast<unsigned long long *>(out), (unsigned long long)__double_as_longlong(mx));
+            atomicAdd(out + 1, sq);
+            atomicAdd(out + 2, ex);
+            atomicAdd(out + 3, ey);
+            atomicAdd(out + 4, dvc);
+            atomicAdd(out + 5, one);
+            atomicMax(reinterpret_cast<unsigned long long *>(out + 6), arg);
+        }
     }
 }
 
