@@ -57,7 +57,7 @@ enum { TSPH_FLUID = 0, TSPH_WALL = 1 };
 /* wall models: Compute_Forces of src/SPH_interaction.h (mDBC: fluid rows only,
  * wall density from ghost nodes) and src/SPH_interactionDBC.h (DBC: walls get
  * a density rate from fluid neighbours) */
-enum { TSPH_WALL_MDBC = 0, TSPH_WALL_DBC = 1 };
+enum { TSPH_WALL_MDBC = 0, TSPH_WALL_DBC = 1, TSPH_WALL_BT = 2 };
 
 /* arithmetic of the pair/integration kernels: FP32 pair math with FP64
  * positions (the production build), or FP64 throughout (the error study) */
@@ -121,7 +121,10 @@ int tsph_destroy(tsph_system *s);
 /* Add_particle (src/SPH_particle_system.h:25-50) for n particles, plus the
  * mDBC ghost node of each wall particle (special.gnr, src/SPH_data.h:51,
  * pushed by the generators e.g. src/SPH_create.h:575-577).  gnr may be NULL
- * (DBC); for fluid entries it is ignored.  Velocity of a wall must be 0. */
+ * (DBC); for fluid entries it is ignored.  For boundary-integral walls
+ * (TSPH_WALL_BT) the same array holds each wall particle's normal
+ * (special.n, pushed by src/ALESPH_create.h:690-792).  Velocity of a wall
+ * must be 0. */
 int tsph_add_particles(tsph_system *s, int n, const int32_t *type,
                        const double *r, const double *v, const double *rho,
                        const double *p, const double *gnr);
@@ -184,8 +187,13 @@ int tsph_density_to_pressure(tsph_system *s);
 /* mDBC_compute_density_mdbcGeo, src/SPH_mDBC.h:9-50 with
  * Kernel_density_approximation_MATRIX_mDBC, src/SPH_kernel_approx.h:1141-1343 */
 int tsph_mdbc_density(tsph_system *s);
-/* Compute_Forces: src/SPH_interaction.h:8-149 (TSPH_WALL_MDBC) or
- * src/SPH_interactionDBC.h:8-155 (TSPH_WALL_DBC) */
+/* BT_compute_density_BTGeo, src/SPH_BT.h:9-50 with
+ * Kernel_density_approximation_BT_update, src/SPH_kernel_approx.h:1838-1953:
+ * the density of boundary-integral wall particles */
+int tsph_bt_density(tsph_system *s);
+/* Compute_Forces: src/SPH_interaction.h:8-149 (TSPH_WALL_MDBC),
+ * src/SPH_interactionDBC.h:8-155 (TSPH_WALL_DBC) or
+ * src/SPH_interactionBT.h:8-194 (TSPH_WALL_BT, walls with normals) */
 int tsph_compute_forces(tsph_system *s, int wall_model);
 /* Integrate_SymplecticPredictor / Corrector, src/SPH_integration.h:266-309 */
 int tsph_symplectic_predictor(tsph_system *s, double dt);
@@ -195,7 +203,8 @@ int tsph_remove_out_of_domain(tsph_system *s, int *removed);
 
 /* nsteps bodies of SPH_simulation::RUN (cases/damBreakLong_mDBC/
  * SPH_simulationSymplectic.h:59-118 for mDBC, cases/stillWater_DBC/
- * SPH_simulationSymplectic.h:58-118 for DBC) as fused kernels replayed from a
+ * SPH_simulationSymplectic.h:58-118 for DBC, cases/damBreakLong_BT/
+ * SPH_simulationSymplectic.h for BT walls) as fused kernels replayed from a
  * CUDA graph.  Requires tsph_particle_to_cell to have been called once (INIT,
  * :41-45).  Leaves the state the reference has after the same steps. */
 int tsph_step(tsph_system *s, int wall_model, double dt, int nsteps);

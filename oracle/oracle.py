@@ -23,6 +23,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_LIB = os.path.join(HERE, "liboracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libtsph_ref.so")
 REF_ALE_LIB = os.path.join(HERE, "_ref", "libtsph_ref_ale.so")
+REF_BT_LIB = os.path.join(HERE, "_ref", "libtsph_ref_bt.so")
 
 F_RX, F_RY, F_VX, F_VY, F_AX, F_AY, F_RHO, F_DRHO, F_P = range(9)
 F_ROX, F_ROY, F_VOX, F_VOY, F_RHO_O = range(9, 14)
@@ -87,7 +88,7 @@ def _load_port():
         L.orc_get_cells.argtypes = [_P, _IP, _IP]
         L.orc_get_cells.restype = _I
         for f in ("orc_divide_to_cells", "orc_clear_cells", "orc_particle_to_cell",
-                  "orc_density_to_pressure", "orc_mdbc_density"):
+                  "orc_density_to_pressure", "orc_mdbc_density", "orc_bt_density"):
             getattr(L, f).argtypes = [_P]
         L.orc_compute_forces.argtypes = [_P, _I]
         L.orc_predictor.argtypes = [_P, _D]
@@ -642,3 +643,156 @@ class RefAle:
 
     def ale_step(self, dt, step0, n):
         self.L.refale_step(self.s, dt, int(step0), int(n))
+
+
+# ---------------------------------------------------------------- BT walls
+ORC_BT = 2  # oracle/tsph_oracle.h
+
+
+class PortBt(PortSystem):
+    """The oracle with boundary-integral walls (src/SPH_interactionBT.h,
+    src/SPH_BT.h): the wall normals of the case are added with
+    orc_ale_add_normal (walls first)."""
+
+    @classmethod
+    def from_case(cls, case, divide=True):
+        o = PortSystem.from_case.__func__(cls, case, divide=False)
+        for n in case.particles.normals:
+            o.L.orc_ale_add_normal(o.s, n[0], n[1])
+        if divide:
+            o.divide_to_cells()
+            o.particle_to_cell()
+        return o
+
+    def bt_density(self):
+        self.L.orc_bt_density(self.s)
+
+
+_ref_bt = None
+
+
+def _load_ref_bt():
+    global _ref_bt
+    if _ref_bt is None:
+        L = C.CDLL(REF_BT_LIB)
+        L.refbt_create.restype = _P
+        L.refbt_create.argtypes = [_D] * 11
+        L.refbt_destroy.argtypes = [_P]
+        L.refbt_set_threads.argtypes = [_I]
+        L.refbt_add_particle.argtypes = [_P, _I] + [_D] * 6
+        L.refbt_add_normal.argtypes = [_P, _D, _D]
+        L.refbt_create_wall_x_bt.argtypes = [_P, _D, _D, _D, _I, _D, _D]
+        L.refbt_create_wall_y_bt.argtypes = [_P, _D, _D, _D, _I, _D, _D]
+        L.refbt_create_corner_bt.argtypes = [_P, _I, _I, _D, _D, _D, _D]
+        L.refbt_create_block_of_fluid_wp.argtypes = [_P] + [_D] * 4
+        L.refbt_np.argtypes = [_P]
+        L.refbt_np.restype = _I
+        L.refbt_nn.argtypes = [_P]
+        L.refbt_nn.restype = _I
+        L.refbt_get_normals.argtypes = [_P, _DP]
+        L.refbt_get_state.argtypes = [_P] + [_P] * 8
+        L.refbt_set_velocity_density.argtypes = [_P, _DP, _DP]
+        for f in ("refbt_divide_to_cells", "refbt_particle_to_cell", "refbt_density_to_pressure",
+                  "refbt_wall_density", "refbt_forces"):
+            getattr(L, f).argtypes = [_P]
+        L.refbt_step.argtypes = [_P, _D, _I]
+        _ref_bt = L
+    return _ref_bt
+
+
+def ref_bt_available() -> bool:
+    if not os.path.exists(REF_BT_LIB):
+        return False
+    try:
+        C.CDLL(REF_BT_LIB)
+        return True
+    except OSError:
+        return False
+
+
+class RefBt:
+    """The reference's BT-wall WCSPH code (oracle/_ref/libtsph_ref_bt.so)."""
+
+    def __init__(self, case):
+        self.L = _load_ref_bt()
+        self.s = self.L.refbt_create(case.h, case.kap, case.cs, case.rho0, case.visco,
+                                     case.delta, case.dp, *case.domain)
+
+    @classmethod
+    def from_case(cls, case, divide=True):
+        o = cls(case)
+        ps = case.particles
+        for i in range(ps.np):
+            o.L.refbt_add_particle(o.s, ps.type[i], ps.p[i], ps.rho[i], ps.rx[i], ps.ry[i],
+                                   ps.vx[i], ps.vy[i])
+        for n in ps.normals:
+            o.L.refbt_add_normal(o.s, n[0], n[1])
+        if divide:
+            o.L.refbt_divide_to_cells(o.s)
+            o.L.refbt_particle_to_cell(o.s)
+        return o
+
+    @classmethod
+    def generated(cls, case, dp, L=1.61, wall_height=1.0, column=(0.6, 0.3)):
+        """The same tank built by the reference's own generators
+        (cases/damBreakLong_BT/geometry.h)."""
+        import math
+
+        o = cls(case)
+        s2 = math.sqrt(2)
+        o.L.refbt_create_wall_x_bt(o.s, 0.0 + dp, L - dp, 0.0, -1, 0.0, 1.0)
+        o.L.refbt_create_wall_y_bt(o.s, 0.0, 0.0 + dp, wall_height, -1, 1.0, 0.0)
+        o.L.refbt_create_wall_y_bt(o.s, L, 0.0 + dp, wall_height, +1, -1.0, 0.0)
+        o.L.refbt_create_corner_bt(o.s, -1, -1, 0.0, 0.0, s2, s2)
+        o.L.refbt_create_corner_bt(o.s, +1, -1, L, 0.0, -s2, s2)
+        o.L.refbt_create_block_of_fluid_wp(o.s, 0.0 + dp, 0 + dp, column[0], column[1])
+        return o
+
+    def __del__(self):
+        try:
+            self.L.refbt_destroy(self.s)
+        except Exception:
+            pass
+
+    @staticmethod
+    def set_threads(n):
+        _load_ref_bt().refbt_set_threads(int(n))
+
+    def np(self):
+        return self.L.refbt_np(self.s)
+
+    def state(self):
+        n = self.np()
+        out = dict(r=np.empty((n, 2)), v=np.empty((n, 2)), a=np.empty((n, 2)), rho=np.empty(n),
+                   drho=np.empty(n), p=np.empty(n), type=np.empty(n, dtype=np.int32),
+                   index=np.empty(n, dtype=np.int32))
+        k = ("r", "v", "a", "rho", "drho", "p", "type", "index")
+        self.L.refbt_get_state(self.s, *[_ptr(out[x]) for x in k])
+        return out
+
+    def normals(self):
+        out = np.empty((self.L.refbt_nn(self.s), 2))
+        self.L.refbt_get_normals(self.s, out.reshape(-1))
+        return out
+
+    def set_velocity_density(self, v, rho):
+        self.L.refbt_set_velocity_density(self.s, np.ascontiguousarray(v, dtype=np.float64).reshape(-1),
+                                          np.ascontiguousarray(rho, dtype=np.float64))
+
+    def divide_to_cells(self):
+        self.L.refbt_divide_to_cells(self.s)
+
+    def particle_to_cell(self):
+        self.L.refbt_particle_to_cell(self.s)
+
+    def density_to_pressure(self):
+        self.L.refbt_density_to_pressure(self.s)
+
+    def bt_density(self):
+        self.L.refbt_wall_density(self.s)
+
+    def compute_forces(self):
+        self.L.refbt_forces(self.s)
+
+    def step(self, dt, n=1):
+        self.L.refbt_step(self.s, dt, int(n))

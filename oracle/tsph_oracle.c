@@ -361,7 +361,130 @@ void orc_density_to_pressure(orc_sys *s) {
  * one thread that owns its cell, and the summation order per row is the
  * reference's (neighbour cells zz,zp,pp,pz,pm,zm,mm,mz,mp, each list
  * ascending), so the result does not depend on the thread count. */
+/* Compute_Forces of the boundary-integral flavour, src/SPH_interactionBT.h:
+ * fluid rows only; a fluid neighbour contributes as in SPH_interaction.h, a
+ * wall neighbour b with normal n_b contributes W (p_temp + visco) dp n_b rho_b
+ * to the momentum sum and -(dv . n_b) W rho_b dp to the continuity sum (no
+ * diffusion term); both sums are divided by the Shepard sum gamma =
+ * sum over fluid neighbours of W m / rho_b when gamma > eps, else a = -g and
+ * drho = 0 (:52-187). */
+static void bt_forces(orc_sys *s) {
+    const int ncy = s->ncy;
+    const int nc = s->ncells;
+    const double h = s->h, m = s->m, c0 = s->cs, delta = s->delta, dp = s->dp;
+    const double rho0 = s->rho0, gy = s->gravy, alpha = s->avisc;
+    const int *cs = s->cell_start, *cl = s->cell_list;
+
+#pragma omp parallel for schedule(dynamic, 3)
+    for (int c = 0; c < nc; c++) {
+        const int ac[9] = {c,           c + 1,       c + 1 + ncy,
+                           c + ncy,     c - 1 + ncy, c - 1,
+                           c - 1 - ncy, c - ncy,     c + 1 - ncy};
+        for (int i = cs[c]; i < cs[c + 1]; i++) {
+            const int ai = cl[i];
+            if (s->type[ai] != ORC_FLUID) continue;
+            const double arx = s->rx[ai], ary = s->ry[ai];
+            const double avx = s->vx[ai], avy = s->vy[ai];
+            const double arho = s->rho[ai], ap = s->p[ai];
+            double acx = 0., acy = 0., drho_sum = 0., diff_sum = 0., gamma = 0.;
+            for (int k = 0; k < 9; k++) {
+                const int cc = ac[k];
+                if (cc < 0 || cc >= nc) continue;
+                for (int n = cs[cc]; n < cs[cc + 1]; n++) {
+                    const int ni = cl[n];
+                    if (ai == ni) continue;
+                    const double nrx = s->rx[ni], nry = s->ry[ni];
+                    const double nvx = s->vx[ni], nvy = s->vy[ni];
+                    const double nrho = s->rho[ni], npr = s->p[ni];
+                    const double drx = arx - nrx, dry = ary - nry;
+                    const double dvx = avx - nvx, dvy = avy - nvy;
+                    const double drs = sqrt((drx * drx) + (dry * dry));
+                    const double drdv = drx * dvx + dry * dvy;
+                    double W, F;
+                    orc_wendland(drs, h, &W, &F);
+                    const double dWx = drx * F, dWy = dry * F;
+                    const double dvdW = dvx * dWx + dvy * dWy;
+                    const double drdW = drx * dWx + dry * dWy;
+                    const double p_temp = (ap + npr) / (arho * nrho);
+                    const double visco =
+                        av_term(h, drs, drdv, 0.5 * (arho + nrho), c0, alpha);
+                    const int wall = s->type[ni] == ORC_WALL;
+                    if (wall) {
+                        const double nbx = ni < s->nn ? s->nx[ni] : 0.;
+                        const double nby = ni < s->nn ? s->ny[ni] : 0.;
+                        acx += W * (p_temp + visco) * dp * nbx * nrho;
+                        acy += W * (p_temp + visco) * dp * nby * nrho;
+                        const double dvnb = dvx * nbx + dvy * nby;
+                        drho_sum -= dvnb * W * nrho * dp;
+                    } else {
+                        acx -= dWx * (p_temp + visco) * m;
+                        acy -= dWy * (p_temp + visco) * m;
+                        const double dt_ = fourtakas(h, drs, dry, drdW, arho, nrho,
+                                                     rho0, c0, delta, m, gy);
+                        drho_sum += dvdW * m;
+                        diff_sum -= dt_;
+                    }
+                    if (s->type[ni] == ORC_FLUID) gamma += W * m / nrho;
+                }
+            }
+            if (gamma > ORC_EPS) {
+                s->ax[ai] = acx / gamma - 0.;
+                s->ay[ai] = acy / gamma - gy;
+                s->drho[ai] = drho_sum / gamma + diff_sum / gamma;
+            } else {
+                s->ax[ai] = 0. - 0.;
+                s->ay[ai] = 0. - gy;
+                s->drho[ai] = 0;
+            }
+        }
+    }
+}
+
+/* BT_compute_density_BTGeo, src/SPH_BT.h:9-50, with
+ * Kernel_density_approximation_BT_update, src/SPH_kernel_approx.h:1838-1953:
+ * each wall particle gets the Shepard density of the fluid around its own
+ * position, sum m W / sum m W / rho over the 3x3 cell block (1000 when the
+ * sum is 0), raised to at least 1000. */
+void orc_bt_density(orc_sys *s) {
+    const double kh = s->kap * s->h, of = s->h * 0.273, h = s->h, m = s->m;
+    const int ncy = s->ncy, nc = s->ncells;
+    const int *cs = s->cell_start, *cl = s->cell_list;
+#pragma omp parallel for schedule(static)
+    for (int p = 0; p < s->np; p++) {
+        if (s->type[p] != ORC_WALL) continue;
+        const double arx = s->rx[p], ary = s->ry[p];
+        const int npx = (int)((arx - s->x0 + of) / kh);
+        const int npy = (int)((ary - s->y0 + of) / kh);
+        const int c = npy + npx * ncy;
+        const int ac[9] = {c,           c + 1,       c + 1 + ncy,
+                           c + ncy,     c - 1 + ncy, c - 1,
+                           c - 1 - ncy, c - ncy,     c + 1 - ncy};
+        double Wsum = 0., rhoWsum = 0.;
+        for (int k = 0; k < 9; k++) {
+            const int cc = ac[k];
+            if (cc < 0 || cc >= nc) continue;
+            for (int n = cs[cc]; n < cs[cc + 1]; n++) {
+                const int ni = cl[n];
+                if (s->type[ni] != ORC_FLUID) continue;
+                const double drx = arx - s->rx[ni], dry = ary - s->ry[ni];
+                const double drs = sqrt(drx * drx + dry * dry);
+                double W, F;
+                orc_wendland(drs, h, &W, &F);
+                Wsum += W * m / s->rho[ni];
+                rhoWsum += m * W;
+            }
+        }
+        double dens = Wsum > 0. ? rhoWsum / Wsum : 1000.;
+        if (dens < 1000.) dens = 1000.;
+        s->rho[p] = dens;
+    }
+}
+
 void orc_compute_forces(orc_sys *s, int model) {
+    if (model == ORC_BT) {
+        bt_forces(s);
+        return;
+    }
     const int ncy = s->ncy;
     const int nc = s->ncells;
     const double h = s->h, m = s->m, c0 = s->cs, delta = s->delta;
@@ -600,6 +723,9 @@ void orc_step(orc_sys *s, int model, double dt, int nsteps) {
     for (int k = 0; k < nsteps; k++) {
         if (model == ORC_MDBC) {
             orc_mdbc_density(s);
+            orc_density_to_pressure(s);
+        } else if (model == ORC_BT) {  /* cases/damBreakLong_BT/SPH_simulationSymplectic.h */
+            orc_bt_density(s);
             orc_density_to_pressure(s);
         }
         orc_predictor(s, dt);

@@ -24,6 +24,8 @@ typedef struct orc_sys orc_sys;
 /* wall models of Compute_Forces */
 #define ORC_MDBC 0   /* src/SPH_interaction.h     */
 #define ORC_DBC 1    /* src/SPH_interactionDBC.h  */
+#define ORC_BT 2     /* src/SPH_interactionBT.h: boundary-integral walls with normals
+                        (added with orc_ale_add_normal, walls first) */
 
 /* particle types, src/SPH_defs.h:44-48 */
 #define ORC_FLUID 0
@@ -64,6 +66,7 @@ void orc_particle_to_cell(orc_sys *s);
 void orc_density_to_pressure(orc_sys *s);
 void orc_compute_forces(orc_sys *s, int model);
 void orc_mdbc_density(orc_sys *s);
+void orc_bt_density(orc_sys *s);
 void orc_predictor(orc_sys *s, double dt);
 void orc_corrector(orc_sys *s, double dt);
 int orc_remove_out_of_domain(orc_sys *s);

@@ -3,8 +3,8 @@
 Runs the reference's own code (oracle/_ref/libtsph_ref.so, compiled from the
 reference headers by ``make -C oracle ref``) on small seeded cases and stores
 its outputs.  Needs the reference sources; the committed .npz files are what
-the tests read.  Usage: python tests/golden/make_golden.py [ale|probes]  (``ale`` /
-``probes`` regenerate only the ALE-SPH or the probe fixture)
+the tests read.  Usage: python tests/golden/make_golden.py [ale|probes|bt]  (``ale`` /
+``probes`` / ``bt`` regenerate only the ALE-SPH, the probe or the BT-wall fixture)
 """
 
 import os
@@ -199,6 +199,42 @@ def main_ale():
     np.savez_compressed(os.path.join(HERE, "dam_break_ale_first_order_dp0.02.npz"), **fo)
 
 
+def main_bt():
+    """WCSPH dam break with boundary-integral walls (cases/damBreakLong_BT,
+    SPH_simulationSymplectic.h RUN loop; own seed): the tank from the
+    reference's generators, the per-function outputs (BT wall density,
+    Compute_Forces of src/SPH_interactionBT.h) at a seeded perturbed state,
+    and the state after 20 steps."""
+    if not O.ref_bt_available():
+        raise SystemExit("reference BT harness not available (needs the reference sources)")
+    O.RefBt.set_threads(1)
+    case = cases.dam_break_bt(dp=0.02)
+    gen = O.RefBt.generated(case, case.dp)
+    g = gen.state()
+    out = {"geom_r": g["r"], "geom_type": g["type"], "geom_rho": g["rho"], "geom_p": g["p"],
+           "geom_normals": gen.normals()}
+    rng = np.random.default_rng(SEED + 3)
+    R = O.RefBt.from_case(case)
+    v, rho = perturb(R.state(), rng, dv=0.1, drho=1e-3)
+    R.set_velocity_density(v, rho)
+    out["init_v"], out["init_rho"] = v, rho
+    R.bt_density()
+    R.density_to_pressure()
+    R.compute_forces()
+    f = R.state()
+    for k in ("rho", "p", "a", "drho"):
+        out[f"forces_{k}"] = f[k]
+    R2 = O.RefBt.from_case(case)
+    R2.set_velocity_density(v, rho)
+    for done in (10, 20):
+        R2.step(case.dt, 10)
+        st = R2.state()
+        for k in ("r", "v", "rho", "p", "a", "drho", "index"):
+            out[f"step{done}_{k}"] = st[k]
+    out["dt"] = np.float64(case.dt)
+    np.savez_compressed(os.path.join(HERE, "dam_break_bt_dp0.02.npz"), **out)
+
+
 WL_GAUGES = [(0.3, 0.0, 0), (0.3, 0.45, 1), (0.865, 0.0, 0), (0.865, 0.45, 1),
              (1.114, 0.0, 0), (1.114, 0.45, 1), (1.3625, 0.0, 0), (1.3625, 0.45, 1)]
 PT_PROBES = [(1.61, 0.003), (1.61, 0.015), (1.61, 0.03), (1.61, 0.08), (0.3, 0.1), (0.2, 0.25),
@@ -232,6 +268,9 @@ def main():
     if len(sys.argv) > 1 and sys.argv[1] == "probes":
         main_probes()
         return
+    if len(sys.argv) > 1 and sys.argv[1] == "bt":
+        main_bt()
+        return
     if O.build_ref() is None or not O.ref_available():
         raise SystemExit("reference harness not available (needs the reference sources)")
     rng = np.random.default_rng(SEED)
@@ -255,6 +294,8 @@ def main():
     main_ale()
     # 6. probes (water level, point fields)
     main_probes()
+    # 7. boundary-integral walls (WCSPH), 20 steps
+    main_bt()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

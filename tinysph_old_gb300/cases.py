@@ -19,6 +19,7 @@ from . import geometry as geo
 
 WALL_MDBC = 0
 WALL_DBC = 1
+WALL_BT = 2
 
 
 @dataclass
@@ -146,6 +147,38 @@ def dam_break_benchmark(dp: float = 0.0005) -> Case:
     """The benchmark dam break: tank 1.61 x 0.8 m, column 0.6 x 0.3 m, mDBC,
     cs = 35 m/s, delta = 0.1, dt = 5e-5 * dp / 0.005 (about 0.24 h / cs)."""
     return dam_break_mdbc(dp=dp, cs=35.0, wall_height=0.8)
+
+
+def dam_break_bt(dp: float = 0.005, cs: float = 34.3, dt: float | None = None,
+                 tank_length: float = 1.61, wall_height: float = 1.0,
+                 column=(0.6, 0.3)) -> Case:
+    """WCSPH dam break with boundary-integral (BT) walls:
+    ``cases/damBreakLong_BT/constants_smallDeltaT.h`` and ``geometry.h``
+    (one wall layer with normals, corners with normals (+-sqrt 2, sqrt 2),
+    hydrostatic column ``Create_Block_of_FluidWP``).  Reference values:
+    dp = 0.005, h = sqrt(2 dp^2), cs = 34.3, dt = 2.5e-5 (scaled with dp
+    here).  The wall normals travel in the per-wall vector of
+    ``tsph_add_particles``."""
+    x_0, x_1, y_0, y_1 = 0.0, 2.0, 0.0, 1.0
+    kap = 2.1
+    hh = 1.0 * math.sqrt(2 * dp * dp)
+    if dt is None:
+        dt = 0.000025 * (dp / 0.005)
+    nvl = int(math.ceil(kap * hh / dp))
+    ps = geo.AleParticleSet(dp, hh, kap, cs)
+    L = tank_length
+    geo.create_wall_x_bt(ps, 0.0 + dp, L - dp, 0.0, -1, (0.0, 1.0))
+    geo.create_wall_y_bt(ps, 0.0, 0.0 + dp, wall_height, -1, (1.0, 0.0))
+    geo.create_wall_y_bt(ps, L, 0.0 + dp, wall_height, +1, (-1.0, 0.0))
+    geo.create_corner_bt(ps, -1, -1, (0.0, 0.0), (math.sqrt(2), math.sqrt(2)))
+    geo.create_corner_bt(ps, +1, -1, (L, 0.0), (-math.sqrt(2), math.sqrt(2)))
+    nw = ps.np
+    geo.create_block_of_fluid_wp(ps, 0.0 + dp, 0 + dp, column[0], column[1])
+    ps.gnr = list(ps.normals)  # walls come first: normal k belongs to particle k
+    return Case(name=f"dam_break_bt_dp{dp:g}", particles=ps, h=hh, kap=kap, cs=cs,
+                rho0=1000.0, visco=0.02, delta=0.1, dp=dp,
+                domain=_pad(x_0, x_1, y_0, y_1, nvl, dp), wall_model=WALL_BT, dt=dt,
+                meta=dict(nvl=nvl, nwalls=nw, wall_height=wall_height))
 
 
 def dam_break_ale(dp: float = 0.005, cs: float = 34.3, dt: float | None = None,

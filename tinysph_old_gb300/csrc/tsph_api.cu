@@ -322,10 +322,17 @@ int tsph_mdbc_density(tsph_system *s) {
     return TSPH_OK;
 }
 
+int tsph_bt_density(tsph_system *s) {
+    NEED(s);
+    ENGINE(s);
+    RUN(s->eng->bt_density(err_));
+    return TSPH_OK;
+}
+
 int tsph_compute_forces(tsph_system *s, int wall_model) {
     NEED(s);
-    if (wall_model != TSPH_WALL_MDBC && wall_model != TSPH_WALL_DBC)
-        return fail(TSPH_ERR_ARG, "wall_model must be TSPH_WALL_MDBC or TSPH_WALL_DBC");
+    if (wall_model != TSPH_WALL_MDBC && wall_model != TSPH_WALL_DBC && wall_model != TSPH_WALL_BT)
+        return fail(TSPH_ERR_ARG, "wall_model must be TSPH_WALL_MDBC, TSPH_WALL_DBC or TSPH_WALL_BT");
     ENGINE(s);
     RUN(s->eng->compute_forces(wall_model, err_));
     return TSPH_OK;
@@ -356,8 +363,8 @@ int tsph_remove_out_of_domain(tsph_system *s, int *removed) {
 
 int tsph_step(tsph_system *s, int wall_model, double dt, int nsteps) {
     NEED(s);
-    if (wall_model != TSPH_WALL_MDBC && wall_model != TSPH_WALL_DBC)
-        return fail(TSPH_ERR_ARG, "wall_model must be TSPH_WALL_MDBC or TSPH_WALL_DBC");
+    if (wall_model != TSPH_WALL_MDBC && wall_model != TSPH_WALL_DBC && wall_model != TSPH_WALL_BT)
+        return fail(TSPH_ERR_ARG, "wall_model must be TSPH_WALL_MDBC, TSPH_WALL_DBC or TSPH_WALL_BT");
     if (!std::isfinite(dt) || nsteps < 0) return fail(TSPH_ERR_ARG, "bad dt or nsteps");
     ENGINE(s);
     if (nsteps == 0) return TSPH_OK;

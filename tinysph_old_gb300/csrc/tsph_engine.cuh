@@ -163,6 +163,17 @@ template <typename T> class Engine final : public EngineBase {
     Nbr<T> nbr_walls(bool stored_p) const {
         return Nbr<T>{W_.r, W_.loc, wall_zero_v_, W_.rho, stored_p ? W_.p : nullptr};
     }
+    // boundary-integral walls: the per-wall vector of tsph_add_particles is the normal
+    Nbr<T> nbr_walls_bt(bool stored_p) const {
+        return Nbr<T>{W_.r, W_.loc, wall_zero_v_, W_.rho, stored_p ? W_.p : nullptr, W_.gnr};
+    }
+    int wall_model_ = 0;  // wall model of the pass being enqueued (2: boundary integral)
+
+    int do_bt_density(std::string &err) {
+        if (nw_ == 0) return 0;
+        return launch(CAT_MDBC, k_bt_density<T>, blocks_for(nw_), kBlock, err, W_, nw_,
+                      (const uint32_t *)fstart_, nbr_fluid(F_, false), grid_, P_);
+    }
 
     // scan counts[0..ncells] -> fstart[0..ncells+1]; leaves counts zeroed
     int scan(std::string &err, const uint32_t *gate = nullptr) {
@@ -456,6 +467,12 @@ template <typename T> class Engine final : public EngineBase {
     template <int MODE>
     int fluid_pairs(const FluidState<T> &X, bool stored_p, T dt, PairOut po, std::string &err,
                     bool skinned = false) {
+        if (wall_model_ == 2)  // boundary-integral walls: the per-particle kernel
+            return launch(CAT_PAIR, k_fluid_pairs<T, MODE, true>, blocks_for(nf_), kBlock, err, X,
+                          (const uint32_t *)fstart_, (const uint32_t *)wstart_,
+                          nbr_fluid(X, stored_p), nbr_walls_bt(stored_p), grid_, P_, O_, dt, po,
+                          health_, (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
+                          (const uint32_t *)nullptr);
         if constexpr (std::is_same<T, float>::value) {
             const int nb = blocks_for(nf_, kTileT);
             const TileConst K = skinned ? Kskin_ : K_;
@@ -501,7 +518,9 @@ template <typename T> class Engine final : public EngineBase {
     int enqueue_step(int model, T dt, std::string &err) {
         int rc;
         const bool dbc = model == 1;
-        if (!dbc && (rc = do_mdbc(err))) return rc;
+        wall_model_ = model;
+        if (model == 0 && (rc = do_mdbc(err))) return rc;
+        if (model == 2 && (rc = do_bt_density(err))) return rc;
         bool skinned = false;
         if constexpr (std::is_same<T, float>::value) skinned = skin_ > 0.f;
         if (skinned) {
@@ -629,6 +648,7 @@ template <typename T> class Engine final : public EngineBase {
         P_.delta = (T)hs.delta;
         P_.rho0 = (T)hs.rho0;
         P_.g = (T)hs.g;
+        P_.dp = (T)hs.dp;
         P_.awen = (T)(double)(float)(0.557 / (hs.h * hs.h));
         P_.bwen = (T)(double)(float)(-2.7852 / (hs.h * hs.h * hs.h));
         P_.four_h2 = (T)(4.0 * hs.h * hs.h);
@@ -867,6 +887,16 @@ template <typename T> class Engine final : public EngineBase {
         return collect_profile(err);
     }
 
+    int bt_density(std::string &err) override {
+        if (!cells_) {
+            err = "cell lists are stale: call tsph_particle_to_cell first";
+            return 3;
+        }
+        int rc = do_bt_density(err);
+        if (rc) return rc;
+        return collect_profile(err);
+    }
+
     int mdbc_density(std::string &err) override {
         if (!cells_) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
@@ -883,6 +913,7 @@ template <typename T> class Engine final : public EngineBase {
             return 3;
         }
         int rc;
+        wall_model_ = model;
         if ((rc = fluid_pairs<MODE_FORCES>(F_, true, T(0), PairOut{}, err))) return rc;
         if (model == 1 && nw_ > 0 &&
             (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,

@@ -41,6 +41,7 @@ class EngineBase {
     virtual int particle_to_cell(std::string &err) = 0;
     virtual int density_to_pressure(std::string &err) = 0;
     virtual int mdbc_density(std::string &err) = 0;
+    virtual int bt_density(std::string &err) = 0;
     virtual int compute_forces(int model, std::string &err) = 0;
     virtual int predictor(double dt, std::string &err) = 0;
     virtual int corrector(double dt, std::string &err) = 0;

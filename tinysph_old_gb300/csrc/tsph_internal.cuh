@@ -139,6 +139,7 @@ template <typename T> struct Phys {
     T k_av;                // -2 alpha c0 h        (AV with mean density 0.5(ra+rb))
     T k_psi;               // 2 c0 h delta         (Fourtakas psi prefactor)
     T xg;                  // rho0 g / cb = 7 g / c0^2 (hydrostatic term argument per metre)
+    T dp;                  // particle spacing (boundary-integral wall terms)
 };
 
 // density as stored -> full density

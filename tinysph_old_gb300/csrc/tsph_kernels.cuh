@@ -583,15 +583,89 @@ template <typename T> struct Nbr {  // neighbour fields read by the pair loop
     const float2 *loc;
     const typename V2<T>::t *v;
     const T *rho;
-    const T *p;  // nullptr: compute EOS from rho
+    const T *p;                   // nullptr: compute EOS from rho
+    const double2 *n = nullptr;   // wall normals (boundary-integral walls)
 };
+
+template <typename T> struct BtAcc {
+    T ax, ay, cont, diff, gamma;
+};
+
+// One pair of the boundary-integral flavour, src/SPH_interactionBT.h:99-172
+// (a = fluid target, b = neighbour): a fluid neighbour adds the WCSPH terms
+// and W m / rho_b to the Shepard sum gamma; a wall neighbour with normal n_b
+// adds W (p_temp + visco) dp n_b rho_b to the momentum sum and
+// -(dv . n_b) W rho_b dp to the continuity sum (its diffusion term is not
+// used).  Arithmetic in the reference's order; out-of-support pairs add
+// exactly zero (W = dW = 0) and are skipped; at r = 0 the kernel value is
+// awen, as in src/SPH_kernel.h:68-75.
+template <typename T>
+__device__ __forceinline__ void bt_pair(T drx, T dry, T dvx, T dvy, T arho, T nrho, T ap, T np_,
+                                        bool wall, T nbx, T nby, const Phys<T> &P,
+                                        BtAcc<T> &acc) {
+    T drs, W, F;
+    if constexpr (std::is_same<T, double>::value) {
+        drs = sqrt((drx * drx) + (dry * dry));
+        if (!(drs / P.h <= 2.0)) return;
+        wendland64(drs, P.h, P.awen, P.bwen, W, F);
+    } else {
+        const float r2 = fmaf(drx, drx, dry * dry);
+        if (!(r2 <= P.four_h2)) return;
+        if (r2 == 0.f) {
+            drs = 0.f;
+            W = P.awen;
+            F = 0.f;
+        } else {
+            drs = sqrtf(r2);
+            wendland32(r2, P, W, F, true);
+        }
+    }
+    const T drdv = drx * dvx + dry * dvy;
+    const T p_temp = (ap + np_) / (arho * nrho);
+    T visco = 0;
+    {
+        const T rbar = T(0.5) * (arho + nrho);
+        const T vmax = drdv > P.alpha ? drdv : P.alpha;
+        if (drdv < 0) {
+            const T mu = P.h * drdv / (drs * drs + T(0.01) * P.h * P.h);
+            visco = -vmax * P.c0 * mu / rbar;
+        }
+    }
+    if (wall) {
+        acc.ax += W * (p_temp + visco) * P.dp * nbx * nrho;
+        acc.ay += W * (p_temp + visco) * P.dp * nby * nrho;
+        const T dvnb = dvx * nbx + dvy * nby;
+        acc.cont -= dvnb * W * nrho * P.dp;
+    } else {
+        const T dWx = drx * F, dWy = dry * F;
+        const T dvdW = dvx * dWx + dvy * dWy;
+        const T drdW = drx * dWx + dry * dWy;
+        acc.ax -= dWx * (p_temp + visco) * P.m;
+        acc.ay -= dWy * (p_temp + visco) * P.m;
+        T drhoH;
+        if constexpr (std::is_same<T, double>::value) {
+            const double cb = P.c0 * P.c0 * P.rho0 / 7.;
+            const double dpH = 1. + dry * P.rho0 * P.g / cb;
+            drhoH = P.rho0 * pow(dpH, 1. / 7) - P.rho0;
+        } else {
+            const float x = dry * P.xg;  // rho0((1+x)^(1/7) - 1) by its series, as pair32
+            drhoH = P.rho0 * x * fmaf(-3.f / 49.f, x, 1.f / 7.f);
+        }
+        const T psi = T(2) * P.c0 * P.h * P.delta * ((nrho - arho) - drhoH) /
+                      (drs * drs + T(0.01) * P.h * P.h);
+        const T DT = psi * drdW * P.m / nrho;
+        acc.cont += dvdW * P.m;
+        acc.diff -= DT;
+        acc.gamma += W * P.m / nrho;
+    }
+}
 
 // Fluid rows: Compute_Forces (src/SPH_interaction.h:57-137 / SPH_interactionDBC.h:57-142)
 // for every live fluid particle of the sorted state F, one thread per particle.
 // MODE_CORRECT then applies the symplectic corrector (src/SPH_integration.h:
 // 289-309) with the old state O and bins the new position (key + histogram
 // slot), marking particles outside the domain as removed (src/SPH_btdebug.h:22).
-template <typename T, int MODE>
+template <typename T, int MODE, bool BT = false>
 __global__ void __launch_bounds__(kBlock)
 k_fluid_pairs(FluidState<T> F, const uint32_t *__restrict__ fstart,
               const uint32_t *__restrict__ wstart, Nbr<T> NF, Nbr<T> NW, Grid g, Phys<T> P,
@@ -610,6 +684,7 @@ k_fluid_pairs(FluidState<T> F, const uint32_t *__restrict__ fstart,
     const T rho_a = rho_full(sa, P.rho0);
     const T pa = NF.p ? NF.p[i] : eos(sa, P);
     Acc<T> acc = {T(0), T(0), T(0), T(0)};
+    BtAcc<T> bacc = {T(0), T(0), T(0), T(0), T(0)};
     int dcount = 0;
     long long dsum = 0;
     int dxor = 0;
@@ -628,6 +703,36 @@ k_fluid_pairs(FluidState<T> F, const uint32_t *__restrict__ fstart,
         const float offy = (float)(-kDY[k]) * g.khf;
 #pragma unroll 1
         for (int part = 0; part < 2; part++) {  // walls first, then fluid
+            if constexpr (BT && MODE != MODE_DIGEST) {
+                const Nbr<T> &N = part == 0 ? NW : NF;
+                const uint32_t *st = part == 0 ? wstart : fstart;
+                const int j0 = (int)__ldg(st + c), j1 = (int)__ldg(st + c + 1);
+                for (int j = j0; j < j1; j++) {
+                    if (part == 1 && j == i) continue;
+                    T drx, dry;
+                    if constexpr (std::is_same<T, float>::value) {
+                        const float2 lb = __ldg(N.loc + j);
+                        drx = (la.x - lb.x) + offx;
+                        dry = (la.y - lb.y) + offy;
+                    } else {
+                        const double2 rb = __ldg(N.r + j);
+                        drx = ra.x - rb.x;
+                        dry = ra.y - rb.y;
+                    }
+                    const auto vb = __ldg(N.v + j);
+                    const T nrho = rho_full(__ldg(N.rho + j), P.rho0);
+                    const T pb = N.p ? __ldg(N.p + j) : eos(__ldg(N.rho + j), P);
+                    T nbx = T(0), nby = T(0);
+                    if (part == 0) {
+                        const double2 nb = __ldg(N.n + j);
+                        nbx = (T)nb.x;
+                        nby = (T)nb.y;
+                    }
+                    bt_pair<T>(drx, dry, va.x - vb.x, va.y - vb.y, rho_a, nrho, pa, pb, part == 0,
+                               nbx, nby, P, bacc);
+                }
+                continue;
+            }
             const Nbr<T> &N = part == 0 ? NW : NF;
             const uint32_t *st = part == 0 ? wstart : fstart;
             const int j0 = (int)__ldg(st + c), j1 = (int)__ldg(st + c + 1);
@@ -673,7 +778,17 @@ k_fluid_pairs(FluidState<T> F, const uint32_t *__restrict__ fstart,
         return;
     } else {
         T ax, ay, drho;
-        if constexpr (std::is_same<T, float>::value) {
+        if constexpr (BT) {  // src/SPH_interactionBT.h:172-187 (eps = 0.01, src/SPH_defs.h:69)
+            if (bacc.gamma > T(0.01)) {
+                ax = bacc.ax / bacc.gamma - T(0);
+                ay = bacc.ay / bacc.gamma - P.g;
+                drho = bacc.cont / bacc.gamma + bacc.diff / bacc.gamma;
+            } else {
+                ax = T(0) - T(0);
+                ay = T(0) - P.g;
+                drho = T(0);
+            }
+        } else if constexpr (std::is_same<T, float>::value) {
             ax = acc.ax * P.m;
             ay = acc.ay * P.m - P.g;
             drho = (acc.cont - acc.diff) * P.m;
@@ -716,6 +831,57 @@ k_fluid_pairs(FluidState<T> F, const uint32_t *__restrict__ fstart,
             out.slot[i] = atomicAdd(out.counts + nk, 1u);
         }
     }
+}
+
+// BT_compute_density_BTGeo, src/SPH_BT.h:9-50, with
+// Kernel_density_approximation_BT_update, src/SPH_kernel_approx.h:1838-1953:
+// a wall particle's density is the Shepard density of the fluid in the 3x3
+// cell block of its own cell, sum m W / sum m W / rho_b (1000 when the sum
+// is 0), raised to at least 1000.  One thread per wall particle.
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+k_bt_density(WallState<T> Wl, int nw, const uint32_t *__restrict__ fstart, Nbr<T> NF, Grid g,
+             Phys<T> P) {
+    const int w = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w >= nw) return;
+    const uint32_t key = Wl.key[w];
+    const int cx = (int)(key / (uint32_t)g.ncy);
+    const int cy = (int)key - cx * g.ncy;
+    const double2 ra = Wl.r[w];
+    float2 la = make_float2(0.f, 0.f);
+    if constexpr (std::is_same<T, float>::value) la = Wl.loc[w];
+    T Wsum = T(0), rhoWsum = T(0);
+    for (int k = 0; k < 9; k++) {
+        const int nx = cx + kDX[k], ny = cy + kDY[k];
+        if (nx < 0 || ny < 0 || nx >= g.ncx || ny >= g.ncy) continue;
+        const int c = ny + nx * g.ncy;
+        const float offx = (float)(-kDX[k]) * g.khf;
+        const float offy = (float)(-kDY[k]) * g.khf;
+        const int j0 = (int)__ldg(fstart + c), j1 = (int)__ldg(fstart + c + 1);
+        for (int j = j0; j < j1; j++) {
+            T W;
+            if constexpr (std::is_same<T, float>::value) {
+                const float2 lb = __ldg(NF.loc + j);
+                const float drx = (la.x - lb.x) + offx, dry = (la.y - lb.y) + offy;
+                const float r2 = fmaf(drx, drx, dry * dry);
+                if (!(r2 <= P.four_h2)) continue;
+                float F;
+                if (r2 == 0.f) W = P.awen;
+                else wendland32(r2, P, W, F, true);
+            } else {
+                const double2 rb = __ldg(NF.r + j);
+                const double dx = ra.x - rb.x, dy = ra.y - rb.y;
+                double F;
+                wendland64(sqrt(dx * dx + dy * dy), P.h, P.awen, P.bwen, W, F);
+            }
+            const T nrho = rho_full(__ldg(NF.rho + j), P.rho0);
+            Wsum += W * P.m / nrho;
+            rhoWsum += P.m * W;
+        }
+    }
+    T dens = Wsum > T(0) ? rhoWsum / Wsum : T(1000);
+    if (dens < T(1000)) dens = T(1000);
+    Wl.rho[w] = rho_stored_from_full<T>((double)dens, (double)P.rho0);
 }
 
 // Wall rows of the DBC flavour (src/SPH_interactionDBC.h:57-142): a = 0, drho

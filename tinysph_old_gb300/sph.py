@@ -21,7 +21,7 @@ from . import build as _build
 OK, ERR_ARG, ERR_CUDA, ERR_STATE, ERR_NOMEM, ERR_NUMERIC, ERR_DENSITY, ERR_ESCAPED, \
     ERR_UNSUPPORTED = range(9)
 FLUID, WALL = 0, 1
-WALL_MDBC, WALL_DBC = 0, 1
+WALL_MDBC, WALL_DBC, WALL_BT = 0, 1, 2
 PREC_FP32, PREC_FP64 = 0, 1
 F_R, F_V, F_A, F_RHO, F_DRHO, F_P, F_INDEX, F_TYPE = (1 << k for k in range(8))
 F_ALL = F_R | F_V | F_A | F_RHO | F_DRHO | F_P | F_INDEX | F_TYPE
@@ -32,7 +32,7 @@ ABI_SYMBOLS = (
     "tsph_abi_version", "tsph_last_error", "tsph_status_string", "tsph_device_count",
     "tsph_create", "tsph_destroy", "tsph_add_particles", "tsph_np", "tsph_grid",
     "tsph_particle_mass", "tsph_divide_to_cells", "tsph_clear_cells", "tsph_particle_to_cell",
-    "tsph_get_cells", "tsph_pair_digest", "tsph_grid_tables", "tsph_particle_to_cell_noalloc", "tsph_density_to_pressure", "tsph_mdbc_density",
+    "tsph_get_cells", "tsph_pair_digest", "tsph_grid_tables", "tsph_particle_to_cell_noalloc", "tsph_density_to_pressure", "tsph_mdbc_density", "tsph_bt_density",
     "tsph_compute_forces", "tsph_symplectic_predictor", "tsph_symplectic_corrector",
     "tsph_remove_out_of_domain", "tsph_step", "tsph_download", "tsph_upload", "tsph_sync",
     "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
@@ -127,7 +127,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_grid.argtypes = [P, C.POINTER(I), C.POINTER(I)]
     L.tsph_particle_mass.argtypes = [P, C.POINTER(D)]
     for f in ("tsph_divide_to_cells", "tsph_clear_cells", "tsph_particle_to_cell",
-              "tsph_density_to_pressure", "tsph_mdbc_density", "tsph_sync"):
+              "tsph_density_to_pressure", "tsph_mdbc_density", "tsph_bt_density", "tsph_sync"):
         getattr(L, f).argtypes = [P]
     L.tsph_get_cells.argtypes = [P, P, P]
     L.tsph_pair_digest.argtypes = [P, P, P, P]
@@ -330,6 +330,10 @@ class ParticleSystem:
 
     def mdbc_density(self):
         _check(self._L.tsph_mdbc_density(self._h))
+
+    def bt_density(self):
+        """BT_compute_density_BTGeo (src/SPH_BT.h)."""
+        _check(self._L.tsph_bt_density(self._h))
 
     def compute_forces(self, wall_model=WALL_MDBC):
         _check(self._L.tsph_compute_forces(self._h, int(wall_model)))
