@@ -32,14 +32,15 @@ ABI_SYMBOLS = (
     "tsph_abi_version", "tsph_last_error", "tsph_status_string", "tsph_device_count",
     "tsph_create", "tsph_destroy", "tsph_add_particles", "tsph_np", "tsph_grid",
     "tsph_particle_mass", "tsph_divide_to_cells", "tsph_clear_cells", "tsph_particle_to_cell",
-    "tsph_get_cells", "tsph_pair_digest", "tsph_grid_tables", "tsph_particle_to_cell_noalloc", "tsph_density_to_pressure", "tsph_mdbc_density", "tsph_bt_density",
+    "tsph_get_cells", "tsph_pair_digest", "tsph_grid_tables", "tsph_particle_to_cell_noalloc",
+    "tsph_density_to_pressure", "tsph_mdbc_density", "tsph_bt_density",
     "tsph_compute_forces", "tsph_symplectic_predictor", "tsph_symplectic_corrector",
     "tsph_remove_out_of_domain", "tsph_step", "tsph_download", "tsph_upload", "tsph_sync",
     "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
     "tsph_water_level", "tsph_point_fields", "tsph_water_front", "tsph_autotune",
     "tsph_set_tile_shape", "tsph_write_vtk", "tsph_save_checkpoint", "tsph_load_checkpoint",
-    "tsph_export_graph", "tsph_apply_update", "tsph_window_check", "tsph_get_stream", "tsph_state_save",
-    "tsph_state_restore", "tsph_gnn_n_params", "tsph_gnn_create",
+    "tsph_export_graph", "tsph_apply_update", "tsph_window_check", "tsph_get_stream",
+    "tsph_state_save", "tsph_state_restore", "tsph_gnn_n_params", "tsph_gnn_create",
     "tsph_gnn_destroy", "tsph_gnn_set_params", "tsph_gnn_get_params", "tsph_gnn_get_grads",
     "tsph_gnn_forward", "tsph_gnn_infer", "tsph_gnn_loss_grad", "tsph_gnn_adam",
     "tsph_ale_create", "tsph_ale_destroy", "tsph_ale_add_particles", "tsph_ale_set_scheme",
