@@ -1019,18 +1019,37 @@ template <typename T> class Engine final : public EngineBase {
         return 0;
     }
 
+    // after k_export: whether every particle is alive (counted on the device),
+    // and the alive map on the host only when some are not
+    uint32_t *alive_count_ = nullptr;
+    int alive_map(std::vector<uint8_t> &alive, bool &dense, std::string &err) {
+        int rc;
+        if (!alive_count_ && (rc = alloc(&alive_count_, 1, err))) return rc;
+        TSPH_CK(cudaMemsetAsync(alive_count_, 0, 4, st_));
+        if ((rc = launch(CAT_OTHER, k_count_alive, blocks_for(ntot_), kBlock, err,
+                         (const uint8_t *)S_.alive, ntot_, alive_count_)))
+            return rc;
+        uint32_t cnt = 0;
+        TSPH_CK(cudaMemcpyAsync(&cnt, alive_count_, 4, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        dense = cnt == (uint32_t)ntot_;
+        if (!dense) {
+            alive.resize(ntot_);
+            TSPH_CK(cudaMemcpyAsync(alive.data(), S_.alive, ntot_, cudaMemcpyDeviceToHost, st_));
+            TSPH_CK(cudaStreamSynchronize(st_));
+        }
+        return 0;
+    }
+
     int download(int mask, double *r, double *v, double *a, double *rho, double *drho, double *p,
                  int32_t *index, int32_t *type, std::string &err) override {
         TSPH_CK(cudaMemsetAsync(S_.alive, 0, ntot_, st_));
         int rc = launch(CAT_OTHER, k_export<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
                         (const uint32_t *)fstart_, ncells_, W_, nw_, P_.rho0, S_, mask & 63);
         if (rc) return rc;
-        std::vector<uint8_t> alive(ntot_);
-        TSPH_CK(cudaMemcpyAsync(alive.data(), S_.alive, ntot_, cudaMemcpyDeviceToHost, st_));
-        TSPH_CK(cudaStreamSynchronize(st_));
-        int nlive = 0;
-        for (int i = 0; i < ntot_; i++) nlive += alive[i];
-        const bool dense = nlive == ntot_;
+        std::vector<uint8_t> alive;
+        bool dense = false;
+        if ((rc = alive_map(alive, dense, err))) return rc;
         std::vector<double> tmp;
         auto fetch = [&](int bit, const void *src, double *dst, int width) -> int {
             if (!(mask & bit) || !dst) return 0;
@@ -1057,7 +1076,7 @@ template <typename T> class Engine final : public EngineBase {
         if ((mask & 64) && index) {
             int o = 0;
             for (int i = 0; i < ntot_; i++)
-                if (alive[i]) index[o++] = i;
+                if (dense || alive[i]) index[o++] = i;
         }
         (void)type;  // filled by the caller from its host copy
         return collect_profile(err);
@@ -1070,12 +1089,9 @@ template <typename T> class Engine final : public EngineBase {
         int rc = launch(CAT_OTHER, k_export<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
                         (const uint32_t *)fstart_, ncells_, W_, nw_, P_.rho0, S_, 0);
         if (rc) return rc;
-        std::vector<uint8_t> alive(ntot_);
-        TSPH_CK(cudaMemcpyAsync(alive.data(), S_.alive, ntot_, cudaMemcpyDeviceToHost, st_));
-        TSPH_CK(cudaStreamSynchronize(st_));
-        int nlive = 0;
-        for (int i = 0; i < ntot_; i++) nlive += alive[i];
-        const bool dense = nlive == ntot_;
+        std::vector<uint8_t> alive;
+        bool dense = false;
+        if ((rc = alive_map(alive, dense, err))) return rc;
         std::vector<double> tmp;
         auto put = [&](int bit, void *dst, const double *src, int width) -> int {
             if (!(mask & bit) || !src) return 0;

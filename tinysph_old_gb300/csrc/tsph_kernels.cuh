@@ -1339,6 +1339,13 @@ __global__ void k_export(FluidState<T> F, const uint32_t *__restrict__ fstart, i
     S.alive[id] = 1;
 }
 
+// number of live particles in the alive map (one atomic per warp)
+__global__ void k_count_alive(const uint8_t *__restrict__ alive, int n, uint32_t *__restrict__ count) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const unsigned b = __ballot_sync(0xffffffffu, i < n && alive[i] != 0);
+    if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (uint32_t)__popc(b));
+}
+
 template <typename T>
 __global__ void k_import(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
                          WallState<T> Wl, int nw, T rho0, Staging S, int mask) {
