@@ -1340,7 +1340,7 @@ __global__ void k_export(FluidState<T> F, const uint32_t *__restrict__ fstart, i
 }
 
 // number of live particles in the alive map (one atomic per warp)
-__global__ void k_count_alive(const uint8_t *__restrict__ alive, int n, uint32_t *__restrict__ count) {
+static __global__ void k_count_alive(const uint8_t *__restrict__ alive, int n, uint32_t *__restrict__ count) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const unsigned b = __ballot_sync(0xffffffffu, i < n && alive[i] != 0);
     if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (uint32_t)__popc(b));
