@@ -309,12 +309,6 @@ int tsph_window_check(tsph_system *s, double k_dt, double out[5]);
  * buffers (the surrogate's network, for one) must be ordered with it.  No
  * counterpart in the reference. */
 int tsph_get_stream(tsph_system *s, void **stream);
-/* a smoothing filter for surrogate windows, on the binned fluid: with
- * `shepard`, the Shepard density rho_i = sum_j m W_ij / sum_j m W_ij / rho_j
- * (fluid j, i included); then XSPH velocity smoothing
- * v_i += xsph_eps sum_{j != i} m / rho_ij (v_j - v_i) W_ij.  No counterpart
- * in the reference. */
-int tsph_window_filter(tsph_system *s, double xsph_eps, int shepard);
 /* a device-side copy of the whole particle state (the start of a surrogate
  * window) and its restoration (the plain-step fallback). */
 int tsph_state_save(tsph_system *s);

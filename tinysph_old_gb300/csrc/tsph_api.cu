@@ -498,14 +498,6 @@ int tsph_get_stream(tsph_system *s, void **stream) {
     return TSPH_OK;
 }
 
-int tsph_window_filter(tsph_system *s, double xsph_eps, int shepard) {
-    NEED(s);
-    if (!std::isfinite(xsph_eps)) return fail(TSPH_ERR_ARG, "xsph_eps must be finite");
-    ENGINE(s);
-    RUN(s->eng->window_filter(xsph_eps, shepard != 0, err_));
-    return TSPH_OK;
-}
-
 int tsph_state_save(tsph_system *s) {
     NEED(s);
     ENGINE(s);

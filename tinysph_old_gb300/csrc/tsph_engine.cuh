@@ -392,21 +392,6 @@ template <typename T> class Engine final : public EngineBase {
         return collect_profile(err);
     }
 
-    int window_filter(double eps, bool shepard, std::string &err) override {
-        if (!cells_) {
-            err = "cell lists are stale: call tsph_particle_to_cell first";
-            return 3;
-        }
-        int rc;
-        if ((rc = launch(CAT_OTHER, k_window_filter<T>, blocks_for(nf_), kBlock, err,
-                         (const FluidState<T>)F_, (const uint32_t *)fstart_, grid_, P_, (T)eps,
-                         shepard ? 1 : 0, Brho_, Bv_)))
-            return rc;
-        TSPH_CK(cudaMemcpyAsync(F_.rho, Brho_, sizeof(T) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(F_.v, Bv_, sizeof(T2) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
-        return collect_profile(err);
-    }
-
     int state_save(std::string &err) override {
         int rc;
         const size_t n = (size_t)nf_, nw = (size_t)nw_;

@@ -73,7 +73,6 @@ class EngineBase {
     virtual int apply_update(const float *y, double su, double ss, double kdt, bool add_rates,
                              bool zero_momentum, int phase, std::string &err) = 0;
     virtual int window_check(double kdt, double out[5], std::string &err) = 0;
-    virtual int window_filter(double eps, bool shepard, std::string &err) = 0;
     virtual int state_save(std::string &err) = 0;
     virtual int state_restore(std::string &err) = 0;
     virtual int sync(std::string &err) = 0;

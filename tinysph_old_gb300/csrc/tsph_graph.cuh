@@ -82,71 +82,6 @@ __global__ void k_graph_export(FluidState<T> F, const uint32_t *__restrict__ fst
     for (int k = cnt; k < K; k++) row[k] = -1;
 }
 
-// the window's smoothing filter over the binned fluid: Shepard density
-// rho_i = sum_j m W_ij / sum_j (m / rho_j) W_ij (j over the fluid, i
-// included) when `shepard`, and XSPH velocity smoothing
-// v_i += eps sum_{j != i} m / rho_ij (v_j - v_i) W_ij, rho_ij the mean
-// density; results into (rho_out, v_out), one thread per fluid row
-template <typename T>
-__global__ void __launch_bounds__(kBlock)
-k_window_filter(FluidState<T> F, const uint32_t *__restrict__ fstart, Grid g, Phys<T> P,
-                T eps, int shepard, T *__restrict__ rho_out,
-                typename V2<T>::t *__restrict__ v_out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_live(fstart, g.ncells)) return;
-    const uint32_t key = F.key[i];
-    const auto va = F.v[i];
-    const T sa = F.rho[i];
-    if (key >= (uint32_t)g.ncells) {
-        rho_out[i] = sa;
-        v_out[i] = va;
-        return;
-    }
-    const int cx = (int)(key / (uint32_t)g.ncy), cy = (int)key - cx * g.ncy;
-    const T rho_a = rho_full(sa, P.rho0);
-    const double2 ra = F.r[i];
-    float2 la = make_float2(0.f, 0.f);
-    if constexpr (std::is_same<T, float>::value) la = F.loc[i];
-    T num = P.m * P.awen, den = P.m / rho_a * P.awen;  // the particle itself (W(0) = awen)
-    T dvx = T(0), dvy = T(0);
-    for (int k = 0; k < 9; k++) {
-        const int nx = cx + kDX[k], ny = cy + kDY[k];
-        if (nx < 0 || ny < 0 || nx >= g.ncx || ny >= g.ncy) continue;
-        const int c = ny + nx * g.ncy;
-        const float offx = (float)(-kDX[k]) * g.khf, offy = (float)(-kDY[k]) * g.khf;
-        for (int j = (int)fstart[c]; j < (int)fstart[c + 1]; j++) {
-            if (j == i) continue;
-            T W;
-            if constexpr (std::is_same<T, float>::value) {
-                const float2 lb = F.loc[j];
-                const float drx = (la.x - lb.x) + offx, dry = (la.y - lb.y) + offy;
-                const float r2 = fmaf(drx, drx, dry * dry);
-                if (!(r2 <= P.four_h2)) continue;
-                float Fk;
-                if (r2 == 0.f) W = P.awen;
-                else wendland32(r2, P, W, Fk, true);
-            } else {
-                const double2 rb = F.r[j];
-                const double dx = ra.x - rb.x, dy = ra.y - rb.y;
-                double Fk;
-                wendland64(sqrt(dx * dx + dy * dy), P.h, P.awen, P.bwen, W, Fk);
-            }
-            const T rho_b = rho_full(F.rho[j], P.rho0);
-            num += P.m * W;
-            den += P.m / rho_b * W;
-            const auto vb = F.v[j];
-            const T c2 = P.m / (T(0.5) * (rho_a + rho_b)) * W;
-            dvx += c2 * (vb.x - va.x);
-            dvy += c2 * (vb.y - va.y);
-        }
-    }
-    rho_out[i] = shepard ? rho_stored_from_full<T>((double)(num / den), (double)P.rho0) : sa;
-    typename V2<T>::t vn;
-    vn.x = va.x + eps * dvx;
-    vn.y = va.y + eps * dvy;
-    v_out[i] = vn;
-}
-
 // sums over the fluid nodes of (y0, y1) and their count into out[0..2]
 static __global__ void k_fluid_sum2(const uint32_t *__restrict__ fstart, int ncells, int nw,
                              const float *__restrict__ y, double *__restrict__ out) {

@@ -39,7 +39,7 @@ ABI_SYMBOLS = (
     "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
     "tsph_water_level", "tsph_point_fields", "tsph_water_front", "tsph_autotune",
     "tsph_set_tile_shape", "tsph_write_vtk", "tsph_save_checkpoint", "tsph_load_checkpoint",
-    "tsph_export_graph", "tsph_apply_update", "tsph_window_check", "tsph_window_filter", "tsph_get_stream",
+    "tsph_export_graph", "tsph_apply_update", "tsph_window_check", "tsph_get_stream",
     "tsph_state_save", "tsph_state_restore", "tsph_gnn_n_params", "tsph_gnn_create",
     "tsph_gnn_destroy", "tsph_gnn_set_params", "tsph_gnn_get_params", "tsph_gnn_get_grads",
     "tsph_gnn_forward", "tsph_gnn_infer", "tsph_gnn_loss_grad", "tsph_gnn_adam",
@@ -157,7 +157,6 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_apply_update.argtypes = [P, P, D, D, D, I, I]
     L.tsph_window_check.argtypes = [P, D, C.POINTER(C.c_double)]
     L.tsph_get_stream.argtypes = [P, C.POINTER(P)]
-    L.tsph_window_filter.argtypes = [P, D, I]
     L.tsph_state_save.argtypes = [P]
     L.tsph_state_restore.argtypes = [P]
     L.tsph_gnn_n_params.restype = I
@@ -480,10 +479,6 @@ class ParticleSystem:
         out = (C.c_double * 5)()
         _check(self._L.tsph_window_check(self._h, float(k_dt), out))
         return out[0], out[1], out[2], int(out[3]), int(out[4])
-
-    def window_filter(self, xsph_eps, shepard=True):
-        """Smoothing filter of a surrogate window (tsph_window_filter)."""
-        _check(self._L.tsph_window_filter(self._h, float(xsph_eps), 1 if shepard else 0))
 
     def stream_ptr(self):
         """The CUDA stream (as an int) the system's kernels run on."""

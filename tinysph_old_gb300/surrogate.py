@@ -156,14 +156,11 @@ def window_update(system, y_ptr, model, kdt, wall_model, scheme="explicit", zero
                             zero_momentum=zero_momentum)
 
 
-def end_of_window(system, wall_model, smoothing=None):
-    """Re-bin, optionally smooth ((xsph_eps, shepard): tsph_window_filter) and
-    run the forces pass at the window's end state; returns the number of
-    particles that left the domain."""
+def end_of_window(system, wall_model):
+    """Re-bin and run the forces pass at the window's end state; returns the
+    number of particles that left the domain."""
     lost = system.remove_out_of_domain()
     system.particle_to_cell()
-    if smoothing is not None:
-        system.window_filter(*smoothing)
     if wall_model == sph.WALL_MDBC:
         system.mdbc_density()
     system.density_to_pressure()
@@ -408,7 +405,7 @@ class Rollout:
     the network)."""
 
     def __init__(self, system, model, dt, wall_model, h, tol_density=0.01, tol_momentum=0.5,
-                 use_net=True, capacity=None, scheme="explicit", smoothing=None):
+                 use_net=True, capacity=None, scheme="explicit"):
         import torch
 
         self.s = system
@@ -422,7 +419,6 @@ class Rollout:
         self.tol_momentum = tol_momentum
         self.use_net = use_net
         self.scheme = scheme
-        self.smoothing = smoothing
         cap = int(capacity or system.np + 64)
         self.gb = GraphBuffers(cap, rates=False)
         self.y = torch.zeros((cap, 3), dtype=torch.float32, device="cuda")
@@ -447,7 +443,7 @@ class Rollout:
             # the BF16 tensor-core forward (trained in FP32 by tsph_gnn_loss_grad)
             self.net.infer(self.gb.struct(self.h, self.m.u_in, self.m.s_in), self.y.data_ptr())
         window_update(s, self.y.data_ptr(), self.m, self.kdt, self.wall_model, self.scheme)
-        lost = end_of_window(s, self.wall_model, self.smoothing)
+        lost = end_of_window(s, self.wall_model)
         mx, rms, mom, _, worst = s.window_check(self.kdt)
         flags = s.health(clear=True)
         ok = (lost == 0 and flags == 0 and mx <= self.tol_density
