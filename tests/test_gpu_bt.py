@@ -81,3 +81,34 @@ def test_bt_fused_step_matches_reference(gpu_tsph, precision):
             lim = _tol(precision, f, ref) * (1 if precision == "fp64" else 1 + k)
             assert e <= lim, (k, f, e, lim)
     assert s.health() & ~gpu_tsph.HEALTH_REMOVED == 0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_bt_still_water_against_oracle(gpu_tsph, oracle_mod, precision):
+    """cases/stillWater_BT (h = 2 dp, ~50 neighbours per particle): 200 and
+    2000 steps (0.4 s) against the oracle (itself equal to the reference bit
+    for bit), and the column stays near hydrostatic: interior pressure within
+    15 % (mean) of rho0 g H of p = rho0 g (0.5 - y) (measured 9 % at 0.4 s,
+    the BT walls' compression wave)."""
+    case = cases.still_water_bt(dp=0.02)
+    s = gpu_tsph.ParticleSystem.from_case(case, precision)
+    o = oracle_mod.PortBt.from_case(case)
+    # the FP64 build drifts from the oracle's last bits (CUDA's pow, the
+    # within-cell summation order), grown over 2000 steps: 1e3 x the bars
+    for n, s64, s32 in ((200, 1.0, 1.0), (1800, 1e3, 10.0)):
+        s.step(BT, case.dt, n)
+        o.step(BT, case.dt, n)
+        a, b = s.download(), o.state()
+        ob = np.argsort(b["index"])
+        assert np.array_equal(a["index"], b["index"][ob])
+        fl = a["type"] == 0
+        for f, l64, l32 in (("r", 1e-9, 2e-6), ("v", 1e-9, 2e-4), ("rho", 1e-7, 5e-3)):
+            e = _err(a[f][fl], b[f][ob][fl])
+            lim = l64 * s64 if precision == "fp64" else l32 * s32
+            assert e <= lim, (n, f, e, lim)
+    fl = a["type"] == 0
+    x, y = a["r"][fl, 0], a["r"][fl, 1]
+    inner = (x > 0.2) & (x < 0.6) & (y > 0.1) & (y < 0.4)
+    err = np.abs(a["p"][fl][inner] - 1000.0 * 9.81 * (0.5 - y[inner])) / (1000.0 * 9.81 * 0.5)
+    assert float(np.mean(err)) < 0.15, float(np.mean(err))

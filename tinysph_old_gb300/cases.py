@@ -181,6 +181,34 @@ def dam_break_bt(dp: float = 0.005, cs: float = 34.3, dt: float | None = None,
                 meta=dict(nvl=nvl, nwalls=nw, wall_height=wall_height))
 
 
+def still_water_bt(dp: float = 0.02) -> Case:
+    """Still water with boundary-integral (BT) walls:
+    ``cases/stillWater_BT/constants.h`` and ``geometry.h`` (tank 0.8 m wide,
+    walls to 1 m, water 0.8 - dp wide and 0.5 m deep with hydrostatic p and
+    rho, h = 2 dp, kap = 2.1, cs = 42.48, visco = 0.01, delta = 0.1,
+    dt = 2e-4 at dp = 0.02, scaled with dp)."""
+    x_0, x_1, y_0, y_1 = 0.0, 1.0, 0.0, 1.0
+    kap = 2.1
+    hh = 2.0 * dp
+    dt = 0.0002 * (dp / 0.02)
+    cs = 42.48
+    nvl = int(math.ceil(kap * hh / dp))
+    ps = geo.AleParticleSet(dp, hh, kap, cs)
+    W = 0.8
+    geo.create_wall_x_bt(ps, 0.0 + dp, W - dp, 0.0, -1, (0.0, 1.0))
+    geo.create_wall_y_bt(ps, 0.0, 0.0 + dp, 1.0, -1, (1.0, 0.0))
+    geo.create_wall_y_bt(ps, W, 0.0 + dp, 1.0, +1, (-1.0, 0.0))
+    geo.create_corner_bt(ps, -1, -1, (0.0, 0.0), (math.sqrt(2), math.sqrt(2)))
+    geo.create_corner_bt(ps, +1, -1, (W, 0.0), (-math.sqrt(2), math.sqrt(2)))
+    nw = ps.np
+    geo.create_block_of_fluid_wp(ps, 0 + dp, 0 + dp, W - dp, 0.5)
+    ps.gnr = list(ps.normals)
+    return Case(name=f"still_water_bt_dp{dp:g}", particles=ps, h=hh, kap=kap, cs=cs,
+                rho0=1000.0, visco=0.01, delta=0.1, dp=dp,
+                domain=_pad(x_0, x_1, y_0, y_1, nvl, dp), wall_model=WALL_BT, dt=dt,
+                meta=dict(nvl=nvl, nwalls=nw, depth=0.5))
+
+
 def dam_break_ale(dp: float = 0.005, cs: float = 34.3, dt: float | None = None,
                   tank_length: float = 1.61, wall_height: float = 1.0,
                   column=(0.6, 0.3)) -> Case:
