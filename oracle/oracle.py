@@ -96,6 +96,11 @@ def _load_port():
         L.orc_remove_out_of_domain.argtypes = [_P]
         L.orc_remove_out_of_domain.restype = _I
         L.orc_step.argtypes = [_P, _I, _D, _I]
+        L.orc_add_zone.argtypes = [_P, _D, _D, _D, _D, _I, _D, _D, _D, _D, _I]
+        L.orc_add_zone.restype = _I
+        L.orc_bz_inlet.argtypes = [_P, _I, _D]
+        L.orc_bz_outlet.argtypes = [_P, _I, _D]
+        L.orc_step_zones.argtypes = [_P, _D, _I]
         L.orc_pair_digest.argtypes = [_P, _IP, np.ctypeslib.ndpointer(dtype=np.int64, flags='C_CONTIGUOUS'), _IP]
         L.orc_water_level.argtypes = [_P, _D, _D, _I]
         L.orc_water_level.restype = _D
@@ -155,6 +160,15 @@ def _load_ref():
         L.ref_predictor.argtypes = [_P, _D]
         L.ref_corrector.argtypes = [_P, _D]
         L.ref_step.argtypes = [_P, _I, _D, _I]
+        L.ref_add_zone.argtypes = [_P, _D, _D, _D, _D, _I, _D, _D, _D, _D, _I]
+        L.ref_create_inlet_y.argtypes = [_P, _D, _D, _D, _I, _I, _D, _D, _I]
+        L.ref_create_outlet_y.argtypes = [_P, _D, _D, _D, _I, _I, _D, _D, _I, _I]
+        L.ref_nzones.argtypes = [_P]
+        L.ref_nzones.restype = _I
+        L.ref_get_zone.argtypes = [_P, _I, _DP]
+        L.ref_bz_inlet.argtypes = [_P, _I, _D]
+        L.ref_bz_outlet.argtypes = [_P, _I, _D]
+        L.ref_step_zones.argtypes = [_P, _D, _I]
         L.ref_water_level.argtypes = [_P, _D, _D, _I]
         L.ref_water_level.restype = _D
         L.ref_point_fields.argtypes = [_P, _D, _D, _DP]
@@ -194,10 +208,18 @@ class PortSystem(_Base):
                                  ps.vx[i], ps.vy[i], 0.0, 0.0)
         for g in ps.gnr:
             o.L.orc_add_gnr(o.s, g[0], g[1])
+        for z in case.meta.get("zones", []):
+            o.L.orc_add_zone(o.s, z["x0"], z["xm"], z["y0"], z["ym"], z["nbl"], z["vx"], z["vy"],
+                             z["ox"], z["oy"], z["btype"])
         if divide:
             o.divide_to_cells()
             o.particle_to_cell()
         return o
+
+    def step_zones(self, dt, n=1):
+        """RUN of cases/inflowSlab_mDBC (mDBC step with the zones' inlet and
+        outlet after the predictor)."""
+        self.L.orc_step_zones(self.s, dt, int(n))
 
     def __del__(self):
         try:
@@ -331,10 +353,24 @@ class RefSystem(_Base):
                                  ps.vx[i], ps.vy[i])
         for g in ps.gnr:
             o.L.ref_add_gnr(o.s, g[0], g[1])
+        for z in case.meta.get("zones", []):
+            o.L.ref_add_zone(o.s, z["x0"], z["xm"], z["y0"], z["ym"], z["nbl"], z["vx"], z["vy"],
+                             z["ox"], z["oy"], z["btype"])
         if divide:
             o.divide_to_cells()
             o.particle_to_cell()
         return o
+
+    def step_zones(self, dt, n=1):
+        self.L.ref_step_zones(self.s, dt, int(n))
+
+    def zones(self):
+        out = []
+        for k in range(self.L.ref_nzones(self.s)):
+            z = np.empty(12)
+            self.L.ref_get_zone(self.s, k, z)
+            out.append(z)
+        return out
 
     def __del__(self):
         try:

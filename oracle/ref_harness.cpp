@@ -28,6 +28,8 @@
 #include "SPH_create.h"
 #include "SPH_water_level.h"
 #include "SPH_measure_pressure.h"
+#include "SPH_inlet_outlet_data.h"
+#include "SPH_buffer_zones.h"
 
 #include <iostream>
 #include <sstream>
@@ -264,4 +266,63 @@ double ref_pressure_in_point(void *c, double x, double y) {
     RefCase *rc = static_cast<RefCase *>(c);
     return Pressure_in_point(rc->particles, rc->sim, {x, y});
 }
+// open boundaries (cases/inflowSlab_mDBC): the zone generators of
+// src/SPH_create.h, BZ_Integrate_inlet / _outlet and the case's RUN loop
+void ref_create_inlet_y(void *c, double x, double y0, double y1, int o, int nbl, double vx,
+                        double vy, int type) {
+    Quiet q;
+    DRAW_CreateInletY(static_cast<RefCase *>(c)->particles, x, y0, y1, o, nbl, TDouble2(vx, vy),
+                      type);
+}
+void ref_create_outlet_y(void *c, double x, double y0, double y1, int o, int nbl, double vx,
+                         double vy, int type, int empty) {
+    Quiet q;
+    DRAW_CreateOutletY(static_cast<RefCase *>(c)->particles, x, y0, y1, o, nbl, TDouble2(vx, vy),
+                       type, empty != 0);
+}
+void ref_add_zone(void *c, double x0, double xm, double y0, double ym, int nbl, double vx, double vy,
+                  double ox, double oy, int btype) {
+    static_cast<RefCase *>(c)->particles.zones.push_back(
+        BufferZone(x0, xm, y0, ym, nbl, TDouble2(vx, vy), TDouble2(ox, oy), btype));
+}
+int ref_nzones(void *c) { return (int)static_cast<RefCase *>(c)->particles.zones.size(); }
+// orientation x, y; x0, y0, xm, ym; nbl; bl, bh; btype; v_b x, y
+void ref_get_zone(void *c, int k, double *out12) {
+    const BufferZone &z = static_cast<RefCase *>(c)->particles.zones[k];
+    const double v[12] = {z.orientation.x, z.orientation.y, z.x0, z.y0, z.xm, z.ym,
+                          (double)z.nbl, z.bl, z.bh, (double)z.btype, z.v_b.x, z.v_b.y};
+    for (int i = 0; i < 12; i++) out12[i] = v[i];
+}
+void ref_bz_inlet(void *c, int zone, double dt) {
+    Quiet q;
+    BZ_Integrate_inlet(static_cast<RefCase *>(c)->particles, zone, dt);
+}
+void ref_bz_outlet(void *c, int zone, double dt) {
+    Quiet q;
+    BZ_Integrate_outlet(static_cast<RefCase *>(c)->particles, zone, dt);
+}
+// the body of SPH_simulation::RUN of cases/inflowSlab_mDBC/SPH_simulationSymplectic.h
+void ref_step_zones(void *c, double dt, int nsteps) {
+    Quiet q;
+    RefCase *K = static_cast<RefCase *>(c);
+    Particle_system &P = K->particles;
+    for (int k = 0; k < nsteps; k++) {
+        mDBC_compute_density_mdbcGeo(P, K->sim);
+        Density_to_pressure(P);
+        Integrate_SymplecticPredictor(P, dt);
+        BZ_Integrate_inlet(P, 0, dt);
+        BZ_Integrate_outlet(P, 1, dt);
+        Clear_cells(P);
+        Particle_To_Cell(P, K->sim);
+        Density_to_pressure(P);
+        Compute_Forces(P);
+        Integrate_SymplecticCorrector(P, dt);
+        RemoveParticlesOutOfDomain(P, K->sim);
+        Clear_cells(P);
+        Particle_To_Cell(P, K->sim);
+        Density_to_pressure(P);
+        Compute_Forces(P);
+    }
+}
+
 }  // extern "C"

@@ -66,6 +66,18 @@ void orc_particle_to_cell(orc_sys *s);
 void orc_density_to_pressure(orc_sys *s);
 void orc_compute_forces(orc_sys *s, int model);
 void orc_mdbc_density(orc_sys *s);
+/* open boundaries: BufferZone(x0, xm, y0, ym, nbl, v0, orientation, btype)
+ * (src/SPH_inlet_outlet_data.h) appended to particles.zones; returns its
+ * index or -1 */
+int orc_add_zone(orc_sys *s, double x0, double xm, double y0, double ym, int nbl, double vx,
+                 double vy, double ox, double oy, int btype);
+/* BZ_Integrate_inlet / BZ_Integrate_outlet, src/SPH_buffer_zones.h:10-206 */
+void orc_bz_inlet(orc_sys *s, int zone, double dt);
+void orc_bz_outlet(orc_sys *s, int zone, double dt);
+/* RUN of cases/inflowSlab_mDBC/SPH_simulationSymplectic.h: the mDBC step
+ * with BZ_Integrate_inlet(zone 0) and BZ_Integrate_outlet(zone 1) after the
+ * predictor */
+void orc_step_zones(orc_sys *s, double dt, int nsteps);
 void orc_bt_density(orc_sys *s);
 void orc_predictor(orc_sys *s, double dt);
 void orc_corrector(orc_sys *s, double dt);

@@ -9,6 +9,18 @@
 
 #define ORC_EPS 0.01 /* src/SPH_defs.h:69 */
 
+/* BufferZone, src/SPH_inlet_outlet_data.h (inlet / outlet buffer zones) */
+typedef struct {
+    double ox, oy;          /* orientation {+-1, 0} or {0, +-1} */
+    double x0, y0, xm, ym;  /* zone region */
+    int nbl;                /* buffer layers */
+    double bl, bh;          /* buffer length, height */
+    int btype;              /* particle type of the zone's buffer particles */
+    double vbx, vby;        /* buffer velocity */
+} orc_zone;
+
+#define ORC_MAX_ZONES 8
+
 struct orc_sys {
     int np, cap;
     int *index;
@@ -39,6 +51,9 @@ struct orc_sys {
     double *grad[12];
     int nn, ncap;
     double *nx, *ny;
+    /* open boundaries (particles.zones, src/SPH_particle_system.h:21) */
+    int nzones;
+    orc_zone zones[ORC_MAX_ZONES];
 };
 
 

@@ -209,6 +209,35 @@ def still_water_bt(dp: float = 0.02) -> Case:
                 meta=dict(nvl=nvl, nwalls=nw, depth=0.5))
 
 
+def inflow_slab_mdbc(dp: float = 0.005, dt: float | None = None) -> Case:
+    """Flow from an inlet over a step, mDBC walls, open boundaries:
+    ``cases/inflowSlab_mDBC/constants.h`` and ``geometry.h`` (inlet buffer
+    of 4 columns at x = 0.1 m, y in (0.1, 0.2], v = 0.75 m/s, zone 0; empty
+    outlet zone at x = 1.0 m, zone 1).  Reference values: dp = 0.005,
+    h = sqrt(2 dp^2), cs = 42.48, visco = 0.1, delta = 0.1, dt = 5e-5 (scaled
+    with dp here).  The zones travel in ``meta["zones"]``."""
+    x_0, x_1, y_0, y_1 = 0.0, 2.0, 0.0, 1.0
+    kap = 2.1
+    hh = 1.0 * math.sqrt(2 * dp * dp)
+    if dt is None:
+        dt = 0.00005 * (dp / 0.005)
+    cs = 42.48
+    nvl = int(math.ceil(kap * hh / dp))
+    ps = geo.ParticleSet(dp, hh, kap, cs)
+    geo.create_wall_x_mdbc(ps, 0.0, 0.4 - 3 * dp, 0.1, -1, 0.1 + dp / 2)
+    geo.create_wall_y_mdbc(ps, 0.4, 0 + dp, 0.1 - 3 * dp, -1, 0.4 + dp / 2)
+    geo.create_wall_x_mdbc(ps, 0.4 + dp, 1.2, 0.0, -1, 0 + dp / 2)
+    geo.create_corner_mdbc(ps, -1, -1, (0.4 + dp / 2, 0.0 + dp / 2))
+    geo.create_corner_mdbc(ps, -1, -1, (0.4 + dp / 2, 0.1 + dp / 2))
+    nw = ps.np
+    zones = [geo.create_inlet_y(ps, 0.1, 0.1 + dp, 0.2, -1, 4, (0.75, 0.0), geo.INLET1),
+             geo.create_outlet_y(ps, 1.0, 0.0 + dp, 0.5, +1, 4, (0.5, 0.0), geo.OUTLET1, True)]
+    return Case(name=f"inflow_slab_mdbc_dp{dp:g}", particles=ps, h=hh, kap=kap, cs=cs,
+                rho0=1000.0, visco=0.1, delta=0.1, dp=dp,
+                domain=_pad(x_0, x_1, y_0, y_1, nvl, dp), wall_model=WALL_MDBC, dt=dt,
+                meta=dict(nvl=nvl, nwalls=nw, zones=zones))
+
+
 def dam_break_ale(dp: float = 0.005, cs: float = 34.3, dt: float | None = None,
                   tank_length: float = 1.61, wall_height: float = 1.0,
                   column=(0.6, 0.3)) -> Case:

@@ -217,3 +217,42 @@ def create_corner_bt(ps: AleParticleSet, orientation_x, orientation_y, xyv, n):
             rx = xyv[0] + dp * i * orientation_x
             ps.add(WALL, 0.0, ps.rho0, (rx, ry))
             ps.normals.append((n[0], n[1]))
+
+
+# ------------------------------------------------------------ open boundaries
+INLET1 = 7    # src/SPH_defs.h:53
+OUTLET1 = 12  # src/SPH_defs.h:59
+
+
+def buffer_zone(x0, xm, y0, ym, nbl, v0, orientation, btype):
+    """``BufferZone`` (src/SPH_inlet_outlet_data.h): region, layers, velocity,
+    orientation and the type of its buffer particles."""
+    return dict(x0=x0, xm=xm, y0=y0, ym=ym, nbl=nbl, vx=v0[0], vy=v0[1], ox=orientation[0],
+                oy=orientation[1], btype=btype)
+
+
+def create_inlet_y(ps: ParticleSet, x, y_0, y_1, orientation, nbl, v0, btype):
+    """``DRAW_CreateInletY``, src/SPH_create.h:439-471: nbl columns of buffer
+    particles of type btype moving with v0, and the zone (returned)."""
+    dp = ps.dp
+    npart = int(math.ceil(_len(x, y_0, x, y_1) / dp)) + 1
+    for l in range(nbl):
+        rx = x + dp * l * orientation
+        for hh in range(npart):
+            ps.add(btype, 0.0, ps.rho0, (rx, y_0 + hh * dp), (v0[0], v0[1]))
+    return buffer_zone(x, x + nbl * dp * orientation, y_0, y_1, nbl, v0, (float(orientation), 0.0),
+                       btype)
+
+
+def create_outlet_y(ps: ParticleSet, x, y_0, y_1, orientation, nbl, v0, btype, empty=True):
+    """``DRAW_CreateOutletY``, src/SPH_create.h:508-540 (with empty = false the
+    reference fills the zone with particles of type `inlet`)."""
+    dp = ps.dp
+    if not empty:
+        npart = int(math.ceil(_len(x, y_0, x, y_1) / dp)) + 1
+        for l in range(nbl):
+            rx = x + dp * l * orientation
+            for hh in range(npart):
+                ps.add(6, 0.0, ps.rho0, (rx, y_0 + hh * dp), (v0[0], v0[1]))
+    return buffer_zone(x, x + nbl * dp * orientation, y_0, y_1, nbl, v0, (float(orientation), 0.0),
+                       btype)
