@@ -3,8 +3,9 @@
 Runs the reference's own code (oracle/_ref/libtsph_ref.so, compiled from the
 reference headers by ``make -C oracle ref``) on small seeded cases and stores
 its outputs.  Needs the reference sources; the committed .npz files are what
-the tests read.  Usage: python tests/golden/make_golden.py [ale|probes|bt]  (``ale`` /
-``probes`` / ``bt`` regenerate only the ALE-SPH, the probe or the BT-wall fixture)
+the tests read.  Usage: python tests/golden/make_golden.py [ale|probes|bt|zones]
+(``ale`` / ``probes`` / ``bt`` / ``zones`` regenerate only the ALE-SPH, the
+probe, the BT-wall or the open-boundary fixtures)
 """
 
 import os
@@ -235,6 +236,30 @@ def main_bt():
     np.savez_compressed(os.path.join(HERE, "dam_break_bt_dp0.02.npz"), **out)
 
 
+def main_zones():
+    """Open boundaries: cases/inflowSlab_mDBC (the case's own RUN loop with
+    BZ_Integrate_inlet / _outlet) and an outlet channel that exercises the
+    outlet's retyping and removal; states at snapshots (particle order of
+    the reference's arrays, types included)."""
+    if O.build_ref() is None or not O.ref_available():
+        raise SystemExit("reference harness not available (needs the reference sources)")
+    O.RefSystem.set_threads(1)
+    for case, snaps, fname in ((cases.inflow_slab_mdbc(dp=0.005), (100, 200, 400),
+                                "inflow_slab_mdbc_dp0.005.npz"),
+                               (cases.outlet_channel_mdbc(dp=0.005), (200, 300, 400, 500, 600),
+                                "outlet_channel_mdbc_dp0.005.npz")):
+        R = O.RefSystem.from_case(case)
+        out = {"dt": np.float64(case.dt), "snaps": np.array(snaps)}
+        done = 0
+        for n in snaps:
+            R.step_zones(case.dt, n - done)
+            done = n
+            st = R.state()
+            for k in ("r", "v", "rho", "p", "type"):
+                out[f"step{n}_{k}"] = st[k]
+        np.savez_compressed(os.path.join(HERE, fname), **out)
+
+
 WL_GAUGES = [(0.3, 0.0, 0), (0.3, 0.45, 1), (0.865, 0.0, 0), (0.865, 0.45, 1),
              (1.114, 0.0, 0), (1.114, 0.45, 1), (1.3625, 0.0, 0), (1.3625, 0.45, 1)]
 PT_PROBES = [(1.61, 0.003), (1.61, 0.015), (1.61, 0.03), (1.61, 0.08), (0.3, 0.1), (0.2, 0.25),
@@ -271,6 +296,9 @@ def main():
     if len(sys.argv) > 1 and sys.argv[1] == "bt":
         main_bt()
         return
+    if len(sys.argv) > 1 and sys.argv[1] == "zones":
+        main_zones()
+        return
     if O.build_ref() is None or not O.ref_available():
         raise SystemExit("reference harness not available (needs the reference sources)")
     rng = np.random.default_rng(SEED)
@@ -296,6 +324,8 @@ def main():
     main_probes()
     # 7. boundary-integral walls (WCSPH), 20 steps
     main_bt()
+    # 8. open boundaries
+    main_zones()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

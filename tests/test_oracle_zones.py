@@ -1,0 +1,36 @@
+"""The oracle's open boundaries (inlet / outlet buffer zones,
+src/SPH_buffer_zones.h) against the reference's own runs
+(tests/golden/inflow_slab_mdbc_dp0.005.npz, outlet_channel_mdbc_dp0.005.npz,
+made by tests/golden/make_golden.py): particle counts, types and state at
+every snapshot, bit for bit (x86 here; 1e-12 relative allowed for libm)."""
+
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from tinysph_old_gb300 import cases
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(os.path.dirname(HERE), "oracle"))
+import oracle as O  # noqa: E402
+
+
+@pytest.mark.parametrize("fname,builder", [
+    ("inflow_slab_mdbc_dp0.005.npz", lambda: cases.inflow_slab_mdbc(dp=0.005)),
+    ("outlet_channel_mdbc_dp0.005.npz", lambda: cases.outlet_channel_mdbc(dp=0.005)),
+])
+def test_zones_match_the_reference(fname, builder):
+    g = np.load(os.path.join(HERE, "golden", fname))
+    case = builder()
+    P = O.PortSystem.from_case(case)
+    done = 0
+    for n in g["snaps"]:
+        P.step_zones(float(g["dt"]), int(n) - done)
+        done = int(n)
+        st = P.state()
+        assert np.array_equal(st["type"], g[f"step{n}_type"]), n
+        for f in ("r", "v", "rho", "p"):
+            ref = g[f"step{n}_{f}"]
+            assert np.max(np.abs(st[f] - ref)) <= 1e-12 * max(1.0, float(np.max(np.abs(ref)))), (n, f)

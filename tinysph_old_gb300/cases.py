@@ -238,6 +238,34 @@ def inflow_slab_mdbc(dp: float = 0.005, dt: float | None = None) -> Case:
                 meta=dict(nvl=nvl, nwalls=nw, zones=zones))
 
 
+def outlet_channel_mdbc(dp: float = 0.005, speed: float = 2.0) -> Case:
+    """A fluid slab driven along a floor into an outlet zone (no counterpart
+    case in the reference; it exercises BZ_Integrate_outlet's retyping and
+    removal, src/SPH_buffer_zones.h:111-206): mDBC floor from x = 0 to 1.2
+    m, fluid x in [0.40, 0.48], y in [dp, 0.05] moving at `speed`, an empty
+    inlet zone (zone 0) far upstream and the outlet zone at x = 0.5 m
+    (zone 1, 4 layers, +x)."""
+    x_0, x_1, y_0, y_1 = 0.0, 2.0, 0.0, 1.0
+    kap = 2.1
+    hh = 1.0 * math.sqrt(2 * dp * dp)
+    dt = 0.00005 * (dp / 0.005)
+    cs = 42.48
+    nvl = int(math.ceil(kap * hh / dp))
+    ps = geo.ParticleSet(dp, hh, kap, cs)
+    geo.create_wall_x_mdbc(ps, 0.0, 1.2, 0.0, -1, 0 + dp / 2)
+    nw = ps.np
+    n0 = ps.np
+    geo.create_block_of_fluid(ps, 0.40, 0.0 + dp, 0.48, 0.05)
+    for k in range(n0, ps.np):
+        ps.vx[k] = speed
+    zones = [geo.buffer_zone(0.05, 0.05 - 4 * dp, dp, 0.05, 4, (speed, 0.0), (-1.0, 0.0), geo.INLET1),
+             geo.create_outlet_y(ps, 0.5, 0.0 + dp, 0.5, +1, 4, (speed, 0.0), geo.OUTLET1, True)]
+    return Case(name=f"outlet_channel_mdbc_dp{dp:g}", particles=ps, h=hh, kap=kap, cs=cs,
+                rho0=1000.0, visco=0.1, delta=0.1, dp=dp,
+                domain=_pad(x_0, x_1, y_0, y_1, nvl, dp), wall_model=WALL_MDBC, dt=dt,
+                meta=dict(nvl=nvl, nwalls=nw, zones=zones))
+
+
 def dam_break_ale(dp: float = 0.005, cs: float = 34.3, dt: float | None = None,
                   tank_length: float = 1.61, wall_height: float = 1.0,
                   column=(0.6, 0.3)) -> Case:
