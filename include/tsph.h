@@ -187,6 +187,22 @@ int tsph_density_to_pressure(tsph_system *s);
 /* mDBC_compute_density_mdbcGeo, src/SPH_mDBC.h:9-50 with
  * Kernel_density_approximation_MATRIX_mDBC, src/SPH_kernel_approx.h:1141-1343 */
 int tsph_mdbc_density(tsph_system *s);
+/* open boundaries (cases/inflowSlab_mDBC): a buffer zone, BufferZone(x0, xm,
+ * y0, ym, nbl, v_b, orientation, btype) of src/SPH_inlet_outlet_data.h
+ * pushed by DRAW_CreateInletY / DRAW_CreateOutletY (src/SPH_create.h:439-540);
+ * its buffer particles are added with type btype (inlets 6-10, outlets
+ * 11-15, src/SPH_defs.h:52-61).  Call before the first step.  A system with
+ * zones runs tsph_step as the case's RUN loop (every zone's inlet or outlet
+ * after the predictor) with per-function kernels. */
+int tsph_add_buffer_zone(tsph_system *s, double x0, double xm, double y0, double ym, int nbl,
+                         double vx, double vy, double ox, double oy, int btype);
+/* room for the particles inlets create: extra fluid rows and extra particle
+ * indices (defaults 65536 and 2^20); an inlet that would exceed them fails
+ * with TSPH_ERR_NOMEM.  No counterpart in the reference. */
+int tsph_set_zone_capacity(tsph_system *s, int extra_rows, int extra_ids);
+/* BZ_Integrate_inlet / BZ_Integrate_outlet, src/SPH_buffer_zones.h:10-206 */
+int tsph_bz_inlet(tsph_system *s, int zone, double dt);
+int tsph_bz_outlet(tsph_system *s, int zone, double dt);
 /* BT_compute_density_BTGeo, src/SPH_BT.h:9-50 with
  * Kernel_density_approximation_BT_update, src/SPH_kernel_approx.h:1838-1953:
  * the density of boundary-integral wall particles */

@@ -38,6 +38,11 @@ void set_last_error(const std::string &msg) { g_err = msg; }
 static int ensure_engine(tsph_system *s) {
     if (!s->divided) return fail(TSPH_ERR_STATE, "call tsph_divide_to_cells first");
     if (s->eng && !s->stale_engine) return TSPH_OK;
+    if (s->hs.zones.empty())
+        for (int t : s->hs.type)
+            if (t != TSPH_FLUID && t != TSPH_WALL)
+                return fail(TSPH_ERR_UNSUPPORTED, "particle type " + std::to_string(t) +
+                                                      " needs a buffer zone (tsph_add_buffer_zone)");
     std::unique_ptr<EngineBase> e(s->precision == TSPH_PREC_FP64 ? tsph::make_engine_f64()
                                                                   : tsph::make_engine_f32());
     std::string err;
@@ -148,10 +153,9 @@ int tsph_add_particles(tsph_system *s, int n, const int32_t *type, const double 
     if (n == 0) return TSPH_OK;
     if (!type || !r || !rho) return fail(TSPH_ERR_ARG, "type, r and rho are required");
     for (int i = 0; i < n; i++) {
-        if (type[i] != TSPH_FLUID && type[i] != TSPH_WALL)
-            return fail(TSPH_ERR_UNSUPPORTED,
-                        "particle type " + std::to_string(type[i]) +
-                            " (only fluid = 0 and wall = 1 are on this path)");
+        if (type[i] < 0 || type[i] > 255)
+            return fail(TSPH_ERR_ARG, "particle type " + std::to_string(type[i]) +
+                                          " (fluid 0, wall 1, buffer types 2-255)");
         if (type[i] == TSPH_WALL && v && (v[2 * i] != 0.0 || v[2 * i + 1] != 0.0))
             return fail(TSPH_ERR_UNSUPPORTED, "moving walls are not on this path (wall v must be 0)");
         if (!std::isfinite(r[2 * i]) || !std::isfinite(r[2 * i + 1]) || !std::isfinite(rho[i]))
@@ -322,6 +326,46 @@ int tsph_mdbc_density(tsph_system *s) {
     return TSPH_OK;
 }
 
+int tsph_add_buffer_zone(tsph_system *s, double x0, double xm, double y0, double ym, int nbl,
+                         double vx, double vy, double ox, double oy, int btype) {
+    NEED(s);
+    if (!((ox != 0) ^ (oy != 0)) || btype < 2 || btype > 255)
+        return fail(TSPH_ERR_ARG, "zone orientation must be along x or y, btype in [2, 255]");
+    // BufferZone constructor, src/SPH_inlet_outlet_data.h
+    double bl = std::fabs(xm - x0), bh = std::fabs(ym - y0);
+    if (oy != 0) {
+        bl = std::fabs(ym - y0);
+        bh = std::fabs(xm - x0);
+    }
+    const double z[12] = {ox, oy, x0, y0, xm, ym, (double)nbl, bl, bh, (double)btype, vx, vy};
+    s->hs.zones.insert(s->hs.zones.end(), z, z + 12);
+    s->stale_engine = true;
+    return TSPH_OK;
+}
+
+int tsph_set_zone_capacity(tsph_system *s, int extra_rows, int extra_ids) {
+    NEED(s);
+    if (extra_rows < 0 || extra_ids < 0) return fail(TSPH_ERR_ARG, "capacities must be >= 0");
+    s->hs.extra_rows = extra_rows;
+    s->hs.extra_ids = extra_ids;
+    s->stale_engine = true;
+    return TSPH_OK;
+}
+
+int tsph_bz_inlet(tsph_system *s, int zone, double dt) {
+    NEED(s);
+    ENGINE(s);
+    RUN(s->eng->bz_inlet(zone, dt, err_));
+    return TSPH_OK;
+}
+
+int tsph_bz_outlet(tsph_system *s, int zone, double dt) {
+    NEED(s);
+    ENGINE(s);
+    RUN(s->eng->bz_outlet(zone, dt, err_));
+    return TSPH_OK;
+}
+
 int tsph_bt_density(tsph_system *s) {
     NEED(s);
     ENGINE(s);
@@ -377,9 +421,10 @@ int tsph_download(tsph_system *s, int fields, const tsph_host_state *out) {
     if (!out) return fail(TSPH_ERR_ARG, "null output");
     ENGINE(s);
     RUN(s->eng->download(fields, out->r, out->v, out->a, out->rho, out->drho, out->p, out->index,
-                         out->type, err_));
-    if ((fields & TSPH_F_TYPE) && out->type) {
+                         (fields & TSPH_F_TYPE) ? out->type : nullptr, err_));
+    if ((fields & TSPH_F_TYPE) && out->type && s->hs.zones.empty()) {
         // types from the host list, in the reference's order of live particles
+        // (systems with buffer zones read them from the device above)
         std::vector<int32_t> idx;
         int np = 0;
         RUN(s->eng->np_live(&np, err_));

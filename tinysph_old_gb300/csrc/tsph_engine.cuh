@@ -14,6 +14,7 @@
 #include "tsph_pairs_tiled.cuh"
 #include "tsph_probes.cuh"
 #include "tsph_graph.cuh"
+#include "tsph_zones.cuh"
 #include "tsph_grid_host.h"
 
 namespace tsph {
@@ -35,7 +36,14 @@ template <typename T> class Engine final : public EngineBase {
     typedef typename V2<T>::t T2;
 
     // ---- sizes
-    int nf_ = 0, nw_ = 0, ntot_ = 0;  // fluid capacity, walls, all indices
+    int nf_ = 0, nw_ = 0, ntot_ = 0;  // fluid rows (capacity), walls, particle indices in use
+    int id_cap_ = 0;                  // capacity of the index space (grows with inlets)
+    // open boundaries (buffer zones)
+    bool zones_on_ = false;
+    std::vector<ZoneDev> zones_;
+    uint32_t *zlist_ = nullptr, *zcount_ = nullptr;
+    int zlist_cap_ = 0;
+    uint8_t *zlive_ = nullptr, *zcand_ = nullptr;
     int ncells_ = 0;
     Grid grid_{};
     Phys<T> P_{};
@@ -155,7 +163,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     Nbr<T> nbr_fluid(const FluidState<T> &X, bool stored_p) const {
-        return Nbr<T>{X.r, X.loc, X.v, X.rho, stored_p ? X.p : nullptr};
+        return Nbr<T>{X.r, X.loc, X.v, X.rho, stored_p ? X.p : nullptr, nullptr, X.type};
     }
     // walls have v = 0: the pair loop reads a zero velocity array
     T2 *wall_zero_v_ = nullptr;
@@ -192,7 +200,8 @@ template <typename T> class Engine final : public EngineBase {
     int sort_finish(const double2 *sr, const T2 *sv, const T *srho, const uint32_t *sid,
                     const T2 *sa, const T *sdrho, const T *sp, FluidState<T> D,
                     const double2 *or2, const T2 *ov2, const T *orho2, OldState<T> Od,
-                    std::string &err, const uint32_t *gate = nullptr) {
+                    std::string &err, const uint32_t *gate = nullptr,
+                    const uint8_t *stype = nullptr) {
         int rc;
         if ((rc = scan(err, gate))) return rc;
         const int *ntot = reinterpret_cast<const int *>(fstart_ + ncells_ + 1);
@@ -207,7 +216,8 @@ template <typename T> class Engine final : public EngineBase {
                       (const uint32_t *)fstart_, (const uint32_t *)tmp_id_,
                       (const uint32_t *)tmp_src_,
                       by_y ? (const long long *)tmp_y_ : (const long long *)nullptr, grid_, sr, sv,
-                      srho, sid, sa, sdrho, sp, D, or2, ov2, orho2, Od, gate);
+                      srho, sid, sa, sdrho, sp, D, or2, ov2, orho2, Od, gate,
+                      D.type ? stype : (const uint8_t *)nullptr);
     }
 
     // the histogram is zero between sorts (the scan clears it)
@@ -336,7 +346,7 @@ template <typename T> class Engine final : public EngineBase {
         }
         int rc;
         if (!wref_.rho) {
-            const size_t n = (size_t)ntot_;
+            const size_t n = (size_t)id_cap_;
             if ((rc = alloc(&wref_.rho, n, err)) || (rc = alloc(&wref_.v, n, err)) ||
                 (rc = alloc(&wref_.drho, n, err)) || (rc = alloc(&wref_.a, n, err)) ||
                 (rc = alloc(&wout_, 7, err)) || (rc = alloc(&ymean_, 3, err)))
@@ -392,6 +402,65 @@ template <typename T> class Engine final : public EngineBase {
         return collect_profile(err);
     }
 
+    // BZ_Integrate_inlet, src/SPH_buffer_zones.h:10-108
+    int bz_inlet(int zone, double dt, std::string &err) override {
+        if (!zones_on_ || zone < 0 || zone >= (int)zones_.size()) {
+            err = "no such buffer zone";
+            return 1;
+        }
+        const ZoneDev Z = zones_[zone];
+        int rc;
+        TSPH_CK(cudaMemsetAsync(zcount_, 0, 4, st_));
+        if ((rc = launch(CAT_OTHER, k_inlet_cross<T>, blocks_for(nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, ncells_, Z, dt, zlist_, zlist_cap_, zcount_)))
+            return rc;
+        uint32_t h[2] = {0, 0};
+        TSPH_CK(cudaMemcpyAsync(&h[0], zcount_, 4, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaMemcpyAsync(&h[1], fstart_ + ncells_, 4, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        const int k = (int)h[0];
+        if (k == 0) return collect_profile(err);
+        if (k > zlist_cap_ || (int)h[1] + k > nf_ || ntot_ + k > id_cap_) {
+            err = "buffer zone: no room for the particles the inlet creates (rows " +
+                  std::to_string(h[1]) + " + " + std::to_string(k) + " of " + std::to_string(nf_) +
+                  ", indices " + std::to_string(ntot_) + " of " + std::to_string(id_cap_) + ")";
+            return 4;
+        }
+        if ((rc = launch(CAT_OTHER, k_inlet_append<T>, blocks_for(k), kBlock, err, F_, O_,
+                         (const uint32_t *)fstart_, ncells_, Z, (const uint32_t *)zlist_, k,
+                         (uint32_t)ntot_, P_.rho0, dt)) ||
+            (rc = launch(CAT_OTHER, k_grow_live, 1, 32, err, fstart_, ncells_, k)))
+            return rc;
+        ntot_ += k;
+        cells_ = false;
+        return collect_profile(err);
+    }
+
+    // BZ_Integrate_outlet, src/SPH_buffer_zones.h:111-206 (x zones; the
+    // reference's y branches are empty)
+    int bz_outlet(int zone, double dt, std::string &err) override {
+        (void)dt;
+        if (!zones_on_ || zone < 0 || zone >= (int)zones_.size()) {
+            err = "no such buffer zone";
+            return 1;
+        }
+        const ZoneDev Z = zones_[zone];
+        if (Z.ox == 0) return 0;
+        int rc;
+        TSPH_CK(cudaMemsetAsync(zlive_, 0, (size_t)ntot_, st_));
+        TSPH_CK(cudaMemsetAsync(zcand_, 0, (size_t)ntot_, st_));
+        TSPH_CK(cudaMemsetAsync(removed_, 0, 4, st_));
+        if ((rc = launch(CAT_OTHER, k_outlet_mark<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, ncells_, (const uint32_t *)W_.id, nw_, Z, zlive_,
+                         zcand_)) ||
+            (rc = launch(CAT_OTHER, k_outlet_apply<T>, blocks_for(nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, ncells_, Z, (const uint8_t *)zlive_,
+                         (const uint8_t *)zcand_, removed_, health_)))
+            return rc;
+        cells_ = false;
+        return collect_profile(err);
+    }
+
     int state_save(std::string &err) override {
         int rc;
         const size_t n = (size_t)nf_, nw = (size_t)nw_;
@@ -401,6 +470,7 @@ template <typename T> class Engine final : public EngineBase {
                 (rc = alloc(&Fsv_.drho, n, err)) || (rc = alloc(&Fsv_.p, n, err)) ||
                 (rc = alloc(&Fsv_.id, n, err)) || (rc = alloc(&Fsv_.key, n, err)) ||
                 (rc = alloc(&Fsv_.loc, n, err)) || (rc = alloc(&wsv_, 4 * nw, err)) ||
+                (F_.type && (rc = alloc(&Fsv_.type, n, err))) ||
                 (rc = alloc(&fstart_sv_, (size_t)ncells_ + 1, err)))
                 return rc;
         }
@@ -454,6 +524,7 @@ template <typename T> class Engine final : public EngineBase {
         cudaMemcpyAsync(dst.id, src.id, 4 * n, D, st_);
         cudaMemcpyAsync(dst.key, src.key, 4 * n, D, st_);
         cudaMemcpyAsync(dst.loc, src.loc, 8 * n, D, st_);
+        if (dst.type && src.type) cudaMemcpyAsync(dst.type, src.type, n, D, st_);
         T *wl[4] = {W_.rho, W_.drho, W_.p, W_.rho_o};
         for (int k = 0; k < 4; k++) {
             if (to_live) cudaMemcpyAsync(wl[k], wsv + k * nw, sizeof(T) * nw, D, st_);
@@ -471,6 +542,12 @@ template <typename T> class Engine final : public EngineBase {
             return launch(CAT_PAIR, k_fluid_pairs<T, MODE, true>, blocks_for(nf_), kBlock, err, X,
                           (const uint32_t *)fstart_, (const uint32_t *)wstart_,
                           nbr_fluid(X, stored_p), nbr_walls_bt(stored_p), grid_, P_, O_, dt, po,
+                          health_, (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
+                          (const uint32_t *)nullptr);
+        if (zones_on_)  // buffer particles: the per-particle kernel skips them as targets
+            return launch(CAT_PAIR, k_fluid_pairs<T, MODE, false>, blocks_for(nf_), kBlock, err, X,
+                          (const uint32_t *)fstart_, (const uint32_t *)wstart_,
+                          nbr_fluid(X, stored_p), nbr_walls(stored_p), grid_, P_, O_, dt, po,
                           health_, (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
                           (const uint32_t *)nullptr);
         if constexpr (std::is_same<T, float>::value) {
@@ -633,8 +710,24 @@ template <typename T> class Engine final : public EngineBase {
         // split fluid / walls
         std::vector<int> fl, wl;
         for (int i = 0; i < n; i++) (hs.type[i] == 1 ? wl : fl).push_back(i);
-        nf_ = (int)fl.size();
+        zones_on_ = !hs.zones.empty();
+        const int nf0 = (int)fl.size();
+        nf_ = nf0 + (zones_on_ ? hs.extra_rows : 0);
         nw_ = (int)wl.size();
+        id_cap_ = ntot_ + (zones_on_ ? hs.extra_ids : 0);
+        for (size_t z = 0; z + 12 <= hs.zones.size(); z += 12) {
+            const double *q = hs.zones.data() + z;
+            ZoneDev d;
+            d.ox = q[0];
+            d.oy = q[1];
+            d.x_b = q[0] != 0 ? q[2] : q[3];
+            d.b_len = q[7];
+            d.btype = (int)q[9];
+            d.vbx = q[10];
+            d.vby = q[11];
+            d.dp = hs.dp;
+            zones_.push_back(d);
+        }
         // constants
         m64_ = hs.m;
         dp64_ = hs.dp;
@@ -694,6 +787,13 @@ template <typename T> class Engine final : public EngineBase {
             return 0;
         };
         if ((rc = alloc_state(F_)) || (rc = alloc_state(Fs_))) return rc;
+        if (zones_on_) {
+            zlist_cap_ = 1 << 16;
+            if ((rc = alloc(&F_.type, nf_, err)) || (rc = alloc(&Fs_.type, nf_, err)) ||
+                (rc = alloc(&zlist_, 2 * (size_t)zlist_cap_, err)) || (rc = alloc(&zcount_, 1, err)) ||
+                (rc = alloc(&zlive_, id_cap_, err)) || (rc = alloc(&zcand_, id_cap_, err)))
+                return rc;
+        }
         if ((rc = alloc(&O_.r, nf_, err)) || (rc = alloc(&O_.v, nf_, err)) ||
             (rc = alloc(&O_.rho, nf_, err)) || (rc = alloc(&Br_, nf_, err)) ||
             (rc = alloc(&Bv_, nf_, err)) || (rc = alloc(&Brho_, nf_, err)) ||
@@ -716,19 +816,21 @@ template <typename T> class Engine final : public EngineBase {
         TSPH_CK(cudaMemset(removed_, 0, 4));
         TSPH_CK(cudaMemset(counts_, 0, sizeof(uint32_t) * (ncells_ + 1)));
         // staging
-        if ((rc = alloc(&S_.r, ntot_, err)) || (rc = alloc(&S_.v, ntot_, err)) ||
-            (rc = alloc(&S_.a, ntot_, err)) || (rc = alloc(&S_.rho, ntot_, err)) ||
-            (rc = alloc(&S_.drho, ntot_, err)) || (rc = alloc(&S_.p, ntot_, err)) ||
-            (rc = alloc(&S_.alive, ntot_, err)))
+        if ((rc = alloc(&S_.r, id_cap_, err)) || (rc = alloc(&S_.v, id_cap_, err)) ||
+            (rc = alloc(&S_.a, id_cap_, err)) || (rc = alloc(&S_.rho, id_cap_, err)) ||
+            (rc = alloc(&S_.drho, id_cap_, err)) || (rc = alloc(&S_.p, id_cap_, err)) ||
+            (rc = alloc(&S_.alive, id_cap_, err)))
             return rc;
+        if (zones_on_ && (rc = alloc(&S_.type, id_cap_, err))) return rc;
         // ---- fluid initial state in index order
         {
-            std::vector<double2> r(nf_);
+            std::vector<double2> r(nf_, make_double2(0., 0.));
             std::vector<T2> v(nf_), a(nf_);
-            std::vector<T> rho(nf_), zero(nf_, T(0)), p(nf_);
-            std::vector<uint32_t> id(nf_), key(nf_, 0u);
+            std::vector<T> rho(nf_, T(0)), zero(nf_, T(0)), p(nf_, T(0));
+            std::vector<uint32_t> id(nf_, 0u), key(nf_, 0u);
             std::vector<float2> loc(nf_, make_float2(0.f, 0.f));
-            for (int k = 0; k < nf_; k++) {
+            std::vector<uint8_t> typ(nf_, 0);
+            for (int k = 0; k < nf0; k++) {
                 const int i = fl[k];
                 r[k] = make_double2(hs.r[2 * i], hs.r[2 * i + 1]);
                 v[k].x = (T)hs.v[2 * i];
@@ -739,7 +841,10 @@ template <typename T> class Engine final : public EngineBase {
                 zero[k] = (T)hs.drho[i];
                 p[k] = (T)hs.p[i];
                 id[k] = (uint32_t)i;
+                typ[k] = (uint8_t)hs.type[i];
             }
+            if (zones_on_)
+                TSPH_CK(cudaMemcpy(F_.type, typ.data(), (size_t)nf_, cudaMemcpyHostToDevice));
             TSPH_CK(cudaMemcpy(F_.r, r.data(), 16 * (size_t)nf_, cudaMemcpyHostToDevice));
             TSPH_CK(cudaMemcpy(F_.v, v.data(), sizeof(T2) * nf_, cudaMemcpyHostToDevice));
             TSPH_CK(cudaMemcpy(F_.a, a.data(), sizeof(T2) * nf_, cudaMemcpyHostToDevice));
@@ -751,8 +856,8 @@ template <typename T> class Engine final : public EngineBase {
             TSPH_CK(cudaMemcpy(F_.loc, loc.data(), 8 * (size_t)nf_, cudaMemcpyHostToDevice));
             // all entries live, none binned yet
             std::vector<uint32_t> fs(ncells_ + 2, 0u);
-            fs[ncells_] = (uint32_t)nf_;
-            fs[ncells_ + 1] = (uint32_t)nf_;
+            fs[ncells_] = (uint32_t)nf0;
+            fs[ncells_ + 1] = (uint32_t)nf0;
             TSPH_CK(cudaMemcpy(fstart_, fs.data(), 4 * fs.size(), cudaMemcpyHostToDevice));
         }
         // ---- walls: binned once on the host, sorted by (cell, index)
@@ -860,9 +965,10 @@ template <typename T> class Engine final : public EngineBase {
             return rc;
         // gather everything into Fs_ (+ old state into B), then copy back
         if ((rc = sort_finish(F_.r, F_.v, F_.rho, F_.id, F_.a, F_.drho, F_.p, Fs_, O_.r, O_.v,
-                              O_.rho, OldState<T>{Br_, Bv_, Brho_}, err)))
+                              O_.rho, OldState<T>{Br_, Bv_, Brho_}, err, nullptr, F_.type)))
             return rc;
         const size_t n = (size_t)nf_;
+        if (F_.type) TSPH_CK(cudaMemcpyAsync(F_.type, Fs_.type, n, cudaMemcpyDeviceToDevice, st_));
         TSPH_CK(cudaMemcpyAsync(F_.r, Fs_.r, 16 * n, cudaMemcpyDeviceToDevice, st_));
         TSPH_CK(cudaMemcpyAsync(F_.v, Fs_.v, sizeof(T2) * n, cudaMemcpyDeviceToDevice, st_));
         TSPH_CK(cudaMemcpyAsync(F_.a, Fs_.a, sizeof(T2) * n, cudaMemcpyDeviceToDevice, st_));
@@ -953,12 +1059,40 @@ template <typename T> class Engine final : public EngineBase {
         return collect_profile(err);
     }
 
+    // the RUN body of a case with buffer zones (cases/inflowSlab_mDBC/
+    // SPH_simulationSymplectic.h): the per-function sequence with every
+    // zone's inlet or outlet after the predictor
+    int step_zones(int model, double dt, std::string &err) {
+        int rc;
+        wall_model_ = model;
+        if (model == 0 && (rc = do_mdbc(err))) return rc;
+        if (model == 2 && (rc = do_bt_density(err))) return rc;
+        if ((rc = density_to_pressure(err)) || (rc = predictor(dt, err))) return rc;
+        for (int z = 0; z < (int)zones_.size(); z++) {
+            const int t = zones_[z].btype;
+            if ((rc = (t >= 11 ? bz_outlet(z, dt, err) : bz_inlet(z, dt, err)))) return rc;
+        }
+        int removed = 0;
+        if ((rc = particle_to_cell(err)) || (rc = density_to_pressure(err)) ||
+            (rc = compute_forces(model, err)) || (rc = corrector(dt, err)) ||
+            (rc = remove_out_of_domain(&removed, err)) || (rc = particle_to_cell(err)) ||
+            (rc = density_to_pressure(err)) || (rc = compute_forces(model, err)))
+            return rc;
+        return 0;
+    }
+
     int step(int model, double dt, int nsteps, std::string &err) override {
         if (!cells_) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
         }
         int rc;
+        if (zones_on_) {
+            for (int s = 0; s < nsteps; s++)
+                if ((rc = step_zones(model, dt, err))) return rc;
+            exported_ = false;
+            return 0;
+        }
         if (tile_shape_ < 0 && (rc = autotune(nullptr, nullptr, err))) return rc;
         if (prof_) {
             for (int s = 0; s < nsteps; s++)
@@ -1078,7 +1212,14 @@ template <typename T> class Engine final : public EngineBase {
             for (int i = 0; i < ntot_; i++)
                 if (dense || alive[i]) index[o++] = i;
         }
-        (void)type;  // filled by the caller from its host copy
+        if (type && S_.type) {  // buffer zones change types: read them from the device
+            std::vector<int32_t> t(ntot_);
+            TSPH_CK(cudaMemcpyAsync(t.data(), S_.type, 4 * (size_t)ntot_, cudaMemcpyDeviceToHost, st_));
+            TSPH_CK(cudaStreamSynchronize(st_));
+            int o = 0;
+            for (int i = 0; i < ntot_; i++)
+                if (dense || alive[i]) type[o++] = t[i];
+        }
         return collect_profile(err);
     }
 
@@ -1164,8 +1305,8 @@ template <typename T> class Engine final : public EngineBase {
         }
         int rc;
         if (!dig_count_) {
-            if ((rc = alloc(&dig_count_, ntot_, err)) || (rc = alloc(&dig_sum_, ntot_, err)) ||
-                (rc = alloc(&dig_xor_, ntot_, err)))
+            if ((rc = alloc(&dig_count_, id_cap_, err)) || (rc = alloc(&dig_sum_, id_cap_, err)) ||
+                (rc = alloc(&dig_xor_, id_cap_, err)))
                 return rc;
         }
         // fluid rows into [0, nf), wall rows into [nf, nf + nw)

@@ -24,6 +24,11 @@ struct HostSetup {
     std::vector<int> type;
     std::vector<double> r, v, a, rho, drho, p, gnr;  // r, v, a, gnr interleaved (x, y)
     std::vector<uint8_t> has_gnr;
+    // open boundaries: per zone orientation x, y; x0, y0, xm, ym; nbl; bl, bh;
+    // btype; v_b x, y (BufferZone, src/SPH_inlet_outlet_data.h), and the
+    // room for particles the inlets create
+    std::vector<double> zones;
+    int extra_rows = 65536, extra_ids = 1 << 20;
 };
 
 struct Profile {
@@ -73,6 +78,8 @@ class EngineBase {
     virtual int apply_update(const float *y, double su, double ss, double kdt, bool add_rates,
                              bool zero_momentum, int phase, std::string &err) = 0;
     virtual int window_check(double kdt, double out[5], std::string &err) = 0;
+    virtual int bz_inlet(int zone, double dt, std::string &err) = 0;
+    virtual int bz_outlet(int zone, double dt, std::string &err) = 0;
     virtual int state_save(std::string &err) = 0;
     virtual int state_restore(std::string &err) = 0;
     virtual int sync(std::string &err) = 0;

@@ -98,6 +98,7 @@ template <typename T> struct FluidState {
     uint32_t *id;   // original particle index
     uint32_t *key;  // cell id (ncells = removed)
     float2 *loc;    // r - cell origin, FP32
+    uint8_t *type = nullptr;  // particle type (systems with buffer zones only; 0 = fluid)
 };
 
 template <typename T> struct OldState {  // r_o, v_o, rho_o of the predictor

@@ -399,7 +399,8 @@ __global__ void k_rank_scatter(const uint32_t *__restrict__ key, const int *__re
                                const T *__restrict__ sp, FluidState<T> D,
                                const double2 *__restrict__ or2, const typename V2<T>::t *__restrict__ ov2,
                                const T *__restrict__ orho2, OldState<T> O,
-                               const uint32_t *__restrict__ gate) {
+                               const uint32_t *__restrict__ gate,
+                               const uint8_t *__restrict__ stype) {
     if (gated_off(gate)) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= *n_ptr) return;
@@ -437,6 +438,7 @@ __global__ void k_rank_scatter(const uint32_t *__restrict__ key, const int *__re
     if (sa) D.a[f] = sa[src];
     if (sdrho) D.drho[f] = sdrho[src];
     if (sp) D.p[f] = sp[src];
+    if (stype) D.type[f] = stype[src];
     if (or2) {
         O.r[f] = or2[src];
         O.v[f] = ov2[src];
@@ -548,6 +550,7 @@ __global__ void k_remove(FluidState<T> F, const uint32_t *__restrict__ fstart, i
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_live(fstart, ncells)) return;
     if (F.key[f] == (uint32_t)ncells) return;
+    if (F.type && F.type[f] != 0) return;  // fluid only (src/SPH_btdebug.h:18)
     if (out_of_domain(F.r[f], box)) {
         F.key[f] = (uint32_t)ncells;
         atomicAdd(removed, 1u);
@@ -585,6 +588,8 @@ template <typename T> struct Nbr {  // neighbour fields read by the pair loop
     const T *rho;
     const T *p;                   // nullptr: compute EOS from rho
     const double2 *n = nullptr;   // wall normals (boundary-integral walls)
+    const uint8_t *type = nullptr;  // row types (buffer zones): non-fluid rows are skipped
+                                    // where the reference takes fluid neighbours only
 };
 
 template <typename T> struct BtAcc {
@@ -675,6 +680,8 @@ k_fluid_pairs(FluidState<T> F, const uint32_t *__restrict__ fstart,
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int ncells = g.ncells;
     if (i >= n_live(fstart, ncells)) return;
+    // buffer particles are neighbours but not targets (src/SPH_interaction.h:64)
+    if (MODE == MODE_FORCES && F.type && F.type[i] != 0) return;
     const uint32_t key = F.key[i];
     const int cx = (int)(key / (uint32_t)g.ncy);
     const int cy = (int)key - cx * g.ncy;
@@ -1024,6 +1031,7 @@ k_mdbc(WallState<T> Wl, int nw, const uint32_t *__restrict__ fstart, Nbr<T> NF, 
                 k++;
             }
             const int j = lo[k] + rem;
+            if (NF.type && __ldg(NF.type + j) != 0) continue;  // fluid only (buffer zones)
             const T sb = __ldg(NF.rho + j);
             const T nrho = rho_full(sb, P.rho0);
             if constexpr (std::is_same<T, float>::value) {
@@ -1300,6 +1308,7 @@ struct Staging {
     double2 *r, *v, *a;
     double *rho, *drho, *p;
     uint8_t *alive;
+    int32_t *type = nullptr;  // systems with buffer zones: the particle type by index
 };
 
 template <typename T>
@@ -1314,6 +1323,7 @@ __global__ void k_export(FluidState<T> F, const uint32_t *__restrict__ fstart, i
         if (mask & 8) S.rho[id] = rho_full64(Wl.rho[i], rho0);
         if (mask & 16) S.drho[id] = (double)Wl.drho[i];
         if (mask & 32) S.p[id] = (double)Wl.p[i];
+        if (S.type) S.type[id] = 1;
         S.alive[id] = 1;
         return;
     }
@@ -1336,6 +1346,7 @@ __global__ void k_export(FluidState<T> F, const uint32_t *__restrict__ fstart, i
     if (mask & 8) S.rho[id] = rho_full64(F.rho[f], rho0);
     if (mask & 16) S.drho[id] = (double)F.drho[f];
     if (mask & 32) S.p[id] = (double)F.p[f];
+    if (S.type) S.type[id] = F.type ? (int32_t)F.type[f] : 0;
     S.alive[id] = 1;
 }
 

@@ -475,6 +475,7 @@ k_mdbc8(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidS
             const int c0 = col * g.ncy;
             const int jlo = (int)__ldg(fstart + c0 + ylo), jhi = (int)__ldg(fstart + c0 + yhi + 1);
             for (int j = jlo + sub; j < jhi; j += 8) {
+                if (F.type && __ldg(F.type + j) != 0) continue;  // fluid only (buffer zones)
                 const uint32_t kb = __ldg(F.key + j);
                 const int rowb = (int)kb - c0;
                 const float2 lb = __ldg(F.loc + j);

@@ -34,6 +34,7 @@ ABI_SYMBOLS = (
     "tsph_particle_mass", "tsph_divide_to_cells", "tsph_clear_cells", "tsph_particle_to_cell",
     "tsph_get_cells", "tsph_pair_digest", "tsph_grid_tables", "tsph_particle_to_cell_noalloc",
     "tsph_density_to_pressure", "tsph_mdbc_density", "tsph_bt_density",
+    "tsph_add_buffer_zone", "tsph_set_zone_capacity", "tsph_bz_inlet", "tsph_bz_outlet",
     "tsph_compute_forces", "tsph_symplectic_predictor", "tsph_symplectic_corrector",
     "tsph_remove_out_of_domain", "tsph_step", "tsph_download", "tsph_upload", "tsph_sync",
     "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
@@ -137,6 +138,10 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_particle_to_cell_noalloc.argtypes = [C.POINTER(_Constants), C.POINTER(_Domain), I, P,
                                                 P, P, P, C.POINTER(I)]
     L.tsph_compute_forces.argtypes = [P, I]
+    L.tsph_add_buffer_zone.argtypes = [P, D, D, D, D, I, D, D, D, D, I]
+    L.tsph_set_zone_capacity.argtypes = [P, I, I]
+    L.tsph_bz_inlet.argtypes = [P, I, D]
+    L.tsph_bz_outlet.argtypes = [P, I, D]
     L.tsph_symplectic_predictor.argtypes = [P, D]
     L.tsph_symplectic_corrector.argtypes = [P, D]
     L.tsph_remove_out_of_domain.argtypes = [P, C.POINTER(I)]
@@ -249,6 +254,8 @@ class ParticleSystem:
             # the reference indexes gnr by particle index (walls first)
             gnr[:len(gn)] = gn
         s.add_particles(a["type"], a["r"], a["v"], a["rho"], a["p"], gnr if len(gn) else None)
+        for z in case.meta.get("zones", []):
+            s.add_buffer_zone(**z)
         if divide:
             s.divide_to_cells()
             if bin_particles:
@@ -331,6 +338,20 @@ class ParticleSystem:
 
     def mdbc_density(self):
         _check(self._L.tsph_mdbc_density(self._h))
+
+    def add_buffer_zone(self, x0, xm, y0, ym, nbl, vx, vy, ox, oy, btype):
+        """A buffer zone (tsph_add_buffer_zone; before the first step)."""
+        _check(self._L.tsph_add_buffer_zone(self._h, x0, xm, y0, ym, int(nbl), vx, vy, ox, oy,
+                                            int(btype)))
+
+    def set_zone_capacity(self, extra_rows, extra_ids):
+        _check(self._L.tsph_set_zone_capacity(self._h, int(extra_rows), int(extra_ids)))
+
+    def bz_inlet(self, zone, dt):
+        _check(self._L.tsph_bz_inlet(self._h, int(zone), float(dt)))
+
+    def bz_outlet(self, zone, dt):
+        _check(self._L.tsph_bz_outlet(self._h, int(zone), float(dt)))
 
     def bt_density(self):
         """BT_compute_density_BTGeo (src/SPH_BT.h)."""
