@@ -127,3 +127,27 @@ def test_particle_thrown_out_inside_the_fused_step(gpu_tsph, oracle_mod, precisi
     o.step(0, case.dt, 4)
     assert g.np == case.np - 1 and o.np() == case.np - 1
     _compare(g, o, precision)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_remove_skips_the_particle_after_an_erased_one(gpu_tsph, oracle_mod, precision):
+    """RemoveParticlesOutOfDomain erases inside a forward loop
+    (src/SPH_btdebug.h:4-31): of three consecutive particles outside the box
+    the first and the third go, the second stays until the next call."""
+    ps = _set()
+    geo.create_block_of_fluid(ps, 0.3, 0.3, 0.4, 0.4)
+    case = _case(ps, 0)
+    g = gpu_tsph.ParticleSystem.from_case(case, precision)
+    o = oracle_mod.PortSystem.from_case(case)
+    st = g.download()
+    r = st["r"].copy()
+    for k in (10, 11, 12, 20):
+        r[k] = (0.5, case.domain[3] + 0.05)
+    g.upload(r=r)
+    o.set_state(r=r)
+    assert g.remove_out_of_domain() == o.remove_out_of_domain() == 3
+    assert g.np == case.np - 3
+    # the skipped one goes in the next call
+    assert g.remove_out_of_domain() == o.remove_out_of_domain() == 1
+    assert g.np == case.np - 4

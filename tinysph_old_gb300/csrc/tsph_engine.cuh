@@ -1046,11 +1046,23 @@ template <typename T> class Engine final : public EngineBase {
         return collect_profile(err);
     }
 
+    // RemoveParticlesOutOfDomain with the reference's skip of the particle
+    // after an erased one (the fused step's corrector removes every particle
+    // outside the box instead)
     int remove_out_of_domain(int *removed, std::string &err) override {
+        int rc;
+        if (!zlive_ && ((rc = alloc(&zlive_, id_cap_, err)) || (rc = alloc(&zcand_, id_cap_, err))))
+            return rc;
         TSPH_CK(cudaMemsetAsync(removed_, 0, 4, st_));
-        int rc = launch(CAT_OTHER, k_remove<T>, blocks_for(nf_), kBlock, err, F_,
-                        (const uint32_t *)fstart_, ncells_, box_, removed_, health_);
-        if (rc) return rc;
+        TSPH_CK(cudaMemsetAsync(zlive_, 0, (size_t)ntot_, st_));
+        TSPH_CK(cudaMemsetAsync(zcand_, 0, (size_t)ntot_, st_));
+        if ((rc = launch(CAT_OTHER, k_remove_mark<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, ncells_, (const uint32_t *)W_.id, nw_, box_,
+                         zlive_, zcand_)) ||
+            (rc = launch(CAT_OTHER, k_remove_apply<T>, blocks_for(nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, ncells_, (const uint8_t *)zlive_,
+                         (const uint8_t *)zcand_, removed_, health_)))
+            return rc;
         uint32_t h = 0;
         TSPH_CK(cudaMemcpyAsync(&h, removed_, 4, cudaMemcpyDeviceToHost, st_));
         TSPH_CK(cudaStreamSynchronize(st_));

@@ -544,20 +544,6 @@ __device__ __forceinline__ bool out_of_domain(double2 r, Box box) {
            (r.x > box.xm - 0.01);
 }
 
-template <typename T>
-__global__ void k_remove(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
-                         Box box, uint32_t *__restrict__ removed, uint32_t *__restrict__ health) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= n_live(fstart, ncells)) return;
-    if (F.key[f] == (uint32_t)ncells) return;
-    if (F.type && F.type[f] != 0) return;  // fluid only (src/SPH_btdebug.h:18)
-    if (out_of_domain(F.r[f], box)) {
-        F.key[f] = (uint32_t)ncells;
-        atomicAdd(removed, 1u);
-        atomicOr(health, kHealthRemoved);
-    }
-}
-
 // ---------------------------------------------------------- pair loop
 enum { MODE_FORCES = 0, MODE_CORRECT = 1, MODE_DIGEST = 2 };
 

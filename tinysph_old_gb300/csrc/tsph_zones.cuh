@@ -132,7 +132,57 @@ __global__ void k_outlet_mark(FluidState<T> F, const uint32_t *__restrict__ fsta
     if (out || r.y < Z.dp / 2) cand[id] = 1;
 }
 
-// second pass.  The reference erases inside its forward loop, so the
+// the reference erases inside forward loops (Remove_particle / erase), so
+// the particle right after an erased one is not examined in that call: with
+// `live` the indices present and `cand` the erase candidates, a particle is
+// skipped when the run of candidates just before it (in index order, over
+// present indices) has odd length
+__device__ __forceinline__ bool skipped_after_erase(const uint8_t *__restrict__ live,
+                                                    const uint8_t *__restrict__ cand, int id) {
+    int c = 0;
+    for (int j = id - 1; j >= 0; j--) {
+        if (!live[j]) continue;
+        if (!cand[j]) break;
+        c++;
+    }
+    return (c & 1) != 0;
+}
+
+// RemoveParticlesOutOfDomain, src/SPH_btdebug.h:4-31, first pass: present
+// indices (walls included) and the fluid outside the padded box
+template <typename T>
+__global__ void k_remove_mark(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
+                              const uint32_t *__restrict__ wid, int nw, Box box,
+                              uint8_t *__restrict__ live, uint8_t *__restrict__ cand) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nw) {
+        live[wid[i]] = 1;
+        return;
+    }
+    const int f = i - nw;
+    if (f >= n_live(fstart, ncells) || F.key[f] == (uint32_t)ncells) return;
+    const uint32_t id = F.id[f];
+    live[id] = 1;
+    if (F.type && F.type[f] != 0) return;  // fluid only (src/SPH_btdebug.h:18)
+    if (out_of_domain(F.r[f], box)) cand[id] = 1;
+}
+
+// second pass: a candidate is erased unless the erase of the particle before
+// it skipped it
+template <typename T>
+__global__ void k_remove_apply(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
+                               const uint8_t *__restrict__ live, const uint8_t *__restrict__ cand,
+                               uint32_t *__restrict__ removed, uint32_t *__restrict__ health) {
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_live(fstart, ncells) || F.key[f] == (uint32_t)ncells) return;
+    const int id = (int)F.id[f];
+    if (!cand[id] || skipped_after_erase(live, cand, id)) return;
+    F.key[f] = (uint32_t)ncells;
+    atomicAdd(removed, 1u);
+    atomicOr(health, kHealthRemoved);
+}
+
+// BZ_Integrate_outlet, second pass.  The reference erases inside its forward loop, so the
 // particle right after an erased one is not examined in that call: a
 // particle is skipped when the run of erase candidates just before it (in
 // index order, over present indices) has odd length; otherwise fluid past
@@ -146,13 +196,7 @@ __global__ void k_outlet_apply(FluidState<T> F, const uint32_t *__restrict__ fst
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_live(fstart, ncells) || F.key[f] == (uint32_t)ncells) return;
     const int id = (int)F.id[f];
-    int c = 0;
-    for (int j = id - 1; j >= 0; j--) {
-        if (!live[j]) continue;
-        if (!cand[j]) break;
-        c++;
-    }
-    if (c & 1) return;  // skipped
+    if (skipped_after_erase(live, cand, id)) return;
     if (F.type[f] == 0) {
         const double2 r = F.r[f];
         if (Z.ox > 0 ? (r.x > Z.x_b) : (r.x < Z.x_b)) {
