@@ -163,6 +163,7 @@ def _load_ref():
         L.ref_add_zone.argtypes = [_P, _D, _D, _D, _D, _I, _D, _D, _D, _D, _I]
         L.ref_create_inlet_y.argtypes = [_P, _D, _D, _D, _I, _I, _D, _D, _I]
         L.ref_create_outlet_y.argtypes = [_P, _D, _D, _D, _I, _I, _D, _D, _I, _I]
+        L.ref_create_inlet_x.argtypes = [_P, _D, _D, _D, _I, _I, _D, _D, _I]
         L.ref_nzones.argtypes = [_P]
         L.ref_nzones.restype = _I
         L.ref_get_zone.argtypes = [_P, _I, _DP]

@@ -274,6 +274,12 @@ void ref_create_inlet_y(void *c, double x, double y0, double y1, int o, int nbl,
     DRAW_CreateInletY(static_cast<RefCase *>(c)->particles, x, y0, y1, o, nbl, TDouble2(vx, vy),
                       type);
 }
+void ref_create_inlet_x(void *c, double y, double x0, double x1, int o, int nbl, double vx,
+                        double vy, int type) {
+    Quiet q;
+    DRAW_CreateInletX(static_cast<RefCase *>(c)->particles, y, x0, x1, o, nbl, TDouble2(vx, vy),
+                      type);
+}
 void ref_create_outlet_y(void *c, double x, double y0, double y1, int o, int nbl, double vx,
                          double vy, int type, int empty) {
     Quiet q;
@@ -301,7 +307,8 @@ void ref_bz_outlet(void *c, int zone, double dt) {
     Quiet q;
     BZ_Integrate_outlet(static_cast<RefCase *>(c)->particles, zone, dt);
 }
-// the body of SPH_simulation::RUN of cases/inflowSlab_mDBC/SPH_simulationSymplectic.h
+// the body of SPH_simulation::RUN of cases/inflowSlab_mDBC and
+// cases/flowDrop_mDBC SPH_simulationSymplectic.h
 void ref_step_zones(void *c, double dt, int nsteps) {
     Quiet q;
     RefCase *K = static_cast<RefCase *>(c);
@@ -310,8 +317,10 @@ void ref_step_zones(void *c, double dt, int nsteps) {
         mDBC_compute_density_mdbcGeo(P, K->sim);
         Density_to_pressure(P);
         Integrate_SymplecticPredictor(P, dt);
-        BZ_Integrate_inlet(P, 0, dt);
-        BZ_Integrate_outlet(P, 1, dt);
+        for (int z = 0; z < (int)P.zones.size(); z++) {  // inlets, then outlets, by zone
+            if (P.zones[z].btype >= outlet) BZ_Integrate_outlet(P, z, dt);
+            else BZ_Integrate_inlet(P, z, dt);
+        }
         Clear_cells(P);
         Particle_To_Cell(P, K->sim);
         Density_to_pressure(P);

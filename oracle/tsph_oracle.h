@@ -74,9 +74,10 @@ int orc_add_zone(orc_sys *s, double x0, double xm, double y0, double ym, int nbl
 /* BZ_Integrate_inlet / BZ_Integrate_outlet, src/SPH_buffer_zones.h:10-206 */
 void orc_bz_inlet(orc_sys *s, int zone, double dt);
 void orc_bz_outlet(orc_sys *s, int zone, double dt);
-/* RUN of cases/inflowSlab_mDBC/SPH_simulationSymplectic.h: the mDBC step
- * with BZ_Integrate_inlet(zone 0) and BZ_Integrate_outlet(zone 1) after the
- * predictor */
+/* RUN of cases/inflowSlab_mDBC and cases/flowDrop_mDBC
+ * SPH_simulationSymplectic.h: the mDBC step with every zone's
+ * BZ_Integrate_inlet (types 6-10) or BZ_Integrate_outlet (11-15), in zone
+ * order, after the predictor */
 void orc_step_zones(orc_sys *s, double dt, int nsteps);
 void orc_bt_density(orc_sys *s);
 void orc_predictor(orc_sys *s, double dt);

@@ -111,8 +111,10 @@ void orc_step_zones(orc_sys *s, double dt, int nsteps) {
         orc_mdbc_density(s);
         orc_density_to_pressure(s);
         orc_predictor(s, dt);
-        orc_bz_inlet(s, 0, dt);
-        orc_bz_outlet(s, 1, dt);
+        for (int z = 0; z < s->nzones; z++) {  /* the cases call inlets, then outlets, by zone */
+            if (s->zones[z].btype >= 11) orc_bz_outlet(s, z, dt);
+            else orc_bz_inlet(s, z, dt);
+        }
         orc_clear_cells(s);
         orc_particle_to_cell(s);
         orc_density_to_pressure(s);

@@ -236,27 +236,57 @@ def main_bt():
     np.savez_compressed(os.path.join(HERE, "dam_break_bt_dp0.02.npz"), **out)
 
 
+def _perturbed_walls(case, u):
+    """The case with every wall particle's x scaled by 1 + k u, k in -6..6
+    (a fixed pattern over the particle index): a perturbation of a few units
+    of roundoff u that enters the flow only where it meets the walls."""
+    ps = case.particles
+    for i in range(ps.np):
+        if ps.type[i] == 1:
+            ps.rx[i] = ps.rx[i] * (1 + u * ((i * 7919) % 13 - 6))
+    return case
+
+
 def main_zones():
     """Open boundaries: cases/inflowSlab_mDBC (the case's own RUN loop with
-    BZ_Integrate_inlet / _outlet) and an outlet channel that exercises the
-    outlet's retyping and removal; states at snapshots (particle order of
-    the reference's arrays, types included)."""
+    BZ_Integrate_inlet / _outlet), an outlet channel that exercises the
+    outlet's retyping and removal, and cases/flowDrop_mDBC (a y-oriented
+    inlet jet falling onto a floor that drains through a +x and a -x
+    outlet); states at snapshots (particle order of the reference's arrays,
+    types included).  For the jet, whose impact on the floor amplifies
+    any difference in the last bits, the fixture also holds the reference's
+    own spread at each snapshot: the largest difference per field between
+    its run and its run with the walls perturbed by a few units of FP64
+    (``spread64``) or FP32 (``spread32``) roundoff."""
     if O.build_ref() is None or not O.ref_available():
         raise SystemExit("reference harness not available (needs the reference sources)")
     O.RefSystem.set_threads(1)
-    for case, snaps, fname in ((cases.inflow_slab_mdbc(dp=0.005), (100, 200, 400),
-                                "inflow_slab_mdbc_dp0.005.npz"),
-                               (cases.outlet_channel_mdbc(dp=0.005), (200, 300, 400, 500, 600),
-                                "outlet_channel_mdbc_dp0.005.npz")):
-        R = O.RefSystem.from_case(case)
+    for builder, snaps, fname, spread in (
+            (lambda: cases.inflow_slab_mdbc(dp=0.005), (100, 200, 400),
+             "inflow_slab_mdbc_dp0.005.npz", False),
+            (lambda: cases.outlet_channel_mdbc(dp=0.005), (200, 300, 400, 500, 600),
+             "outlet_channel_mdbc_dp0.005.npz", False),
+            (lambda: cases.flow_drop_mdbc(dp=0.02), (600, 800, 1000, 1200),
+             "flow_drop_mdbc_dp0.02.npz", True)):
+        case = builder()
+        runs = [O.RefSystem.from_case(case)]
+        if spread:
+            runs += [O.RefSystem.from_case(_perturbed_walls(builder(), u))
+                     for u in (2.0 ** -53, 2.0 ** -24)]
         out = {"dt": np.float64(case.dt), "snaps": np.array(snaps)}
         done = 0
         for n in snaps:
-            R.step_zones(case.dt, n - done)
+            for R in runs:
+                R.step_zones(case.dt, n - done)
             done = n
-            st = R.state()
+            st = runs[0].state()
             for k in ("r", "v", "rho", "p", "type"):
                 out[f"step{n}_{k}"] = st[k]
+            for R, tag in zip(runs[1:], ("spread64", "spread32")):
+                pt = R.state()
+                assert np.array_equal(pt["type"], st["type"]), (fname, n, tag)
+                for k in ("r", "v", "rho", "p"):
+                    out[f"step{n}_{k}_{tag}"] = np.float64(np.max(np.abs(pt[k] - st[k])))
         np.savez_compressed(os.path.join(HERE, fname), **out)
 
 

@@ -2,7 +2,13 @@
 runs (tests/golden/inflow_slab_mdbc_dp0.005.npz: cases/inflowSlab_mDBC, the
 inlet creating particles; outlet_channel_mdbc_dp0.005.npz: the outlet's
 retyping and its erasures, including the reference's skip of the particle
-after an erased one).  Particle count, order and types exact; fields within
+after an erased one; flow_drop_mdbc_dp0.02.npz: cases/flowDrop_mDBC, a
+y-oriented inlet and two outlets facing +x and -x).  The jet's impact on
+the floor amplifies differences in the last bits (the reference itself,
+run with its walls moved by a few units of roundoff, departs from its own
+run by 5e-7 of the pressure scale after 1000 steps); for it the bar is at
+least ten times that spread, recorded in the fixture at each precision's
+roundoff.  Particle count, order and types exact; fields within
 1e-9 of their scale (FP64 build: CUDA's pow against glibc's in the last
 bits, grown quadratically with the step count as the flow through the
 outlet amplifies them: 1.5e-7 relative after 600 steps) or the FP32 bars of
@@ -18,12 +24,19 @@ from tinysph_old_gb300 import cases
 GOLD = os.path.join(os.path.dirname(__file__), "golden")
 
 
-def _tol(precision, field, ref, steps):
+def _tol(precision, field, ref, steps, g):
     mag = float(np.max(np.abs(ref))) if np.size(ref) else 0.0
     if precision == "fp64":
-        return 1e-9 * max(1.0, mag) * (1 + (steps / 50) ** 2)
-    base = {"r": 1e-9, "v": 2e-6 + 1e-5 * mag, "rho": 2e-4, "p": 5e-2 + 1e-6 * mag}[field]
-    return base * (1 + steps / 10)
+        bar = 1e-9 * max(1.0, mag) * (1 + (steps / 50) ** 2)
+    else:
+        base = {"r": 1e-9, "v": 2e-6 + 1e-5 * mag, "rho": 2e-4, "p": 5e-2 + 1e-6 * mag}[field]
+        bar = base * (1 + steps / 10)
+    # a flow that amplifies differences in the last bits: 10x the reference's
+    # own spread under a roundoff-sized perturbation at this precision
+    key = f"step{steps}_{field}_spread{precision[2:]}"
+    if key in g.files:
+        bar = max(bar, 10.0 * float(g[key]))
+    return bar
 
 
 @pytest.mark.gpu
@@ -31,6 +44,7 @@ def _tol(precision, field, ref, steps):
 @pytest.mark.parametrize("fname,builder", [
     ("inflow_slab_mdbc_dp0.005.npz", lambda: cases.inflow_slab_mdbc(dp=0.005)),
     ("outlet_channel_mdbc_dp0.005.npz", lambda: cases.outlet_channel_mdbc(dp=0.005)),
+    ("flow_drop_mdbc_dp0.02.npz", lambda: cases.flow_drop_mdbc(dp=0.02)),
 ])
 def test_zones_match_the_reference(gpu_tsph, fname, builder, precision):
     g = np.load(os.path.join(GOLD, fname))
@@ -47,5 +61,5 @@ def test_zones_match_the_reference(gpu_tsph, fname, builder, precision):
         for f in ("r", "v", "rho", "p"):
             ref = g[f"step{n}_{f}"]
             e = float(np.max(np.abs(st[f] - ref)))
-            lim = _tol(precision, f, ref, int(n))
+            lim = _tol(precision, f, ref, int(n), g)
             assert e <= lim, (n, f, e, lim)

@@ -1,7 +1,7 @@
 """The oracle's open boundaries (inlet / outlet buffer zones,
 src/SPH_buffer_zones.h) against the reference's own runs
 (tests/golden/inflow_slab_mdbc_dp0.005.npz, outlet_channel_mdbc_dp0.005.npz,
-made by tests/golden/make_golden.py): particle counts, types and state at
+flow_drop_mdbc_dp0.02.npz, made by tests/golden/make_golden.py): particle counts, types and state at
 every snapshot, bit for bit (x86 here; 1e-12 relative allowed for libm)."""
 
 import os
@@ -20,6 +20,7 @@ import oracle as O  # noqa: E402
 @pytest.mark.parametrize("fname,builder", [
     ("inflow_slab_mdbc_dp0.005.npz", lambda: cases.inflow_slab_mdbc(dp=0.005)),
     ("outlet_channel_mdbc_dp0.005.npz", lambda: cases.outlet_channel_mdbc(dp=0.005)),
+    ("flow_drop_mdbc_dp0.02.npz", lambda: cases.flow_drop_mdbc(dp=0.02)),
 ])
 def test_zones_match_the_reference(fname, builder):
     g = np.load(os.path.join(HERE, "golden", fname))

@@ -238,6 +238,32 @@ def inflow_slab_mdbc(dp: float = 0.005, dt: float | None = None) -> Case:
                 meta=dict(nvl=nvl, nwalls=nw, zones=zones))
 
 
+def flow_drop_mdbc(dp: float = 0.005, dt: float | None = None) -> Case:
+    """A jet falling from an inlet onto a floor, draining through two outlets:
+    ``cases/flowDrop_mDBC/constants.h`` and ``geometry2.h`` (inlet rows above
+    y = 0.3 + 4 dp, x in (0.8, 1.0], v = (0, -3) m/s, zone 0; outlets at
+    x = 1.3 - 4 dp (+x, zone 1) and x = 0.5 (-x, zone 2)).  Reference
+    values: dp = 0.005, h = sqrt(2 dp^2), cs = 34.3, visco = 0.02,
+    delta = 0.1, dt = 5e-5 (scaled with dp here)."""
+    x_0, x_1, y_0, y_1 = 0.0, 2.0, 0.0, 1.0
+    kap = 2.1
+    hh = 1.0 * math.sqrt(2 * dp * dp)
+    if dt is None:
+        dt = 0.00005 * (dp / 0.005)
+    cs = 34.3
+    nvl = int(math.ceil(kap * hh / dp))
+    ps = geo.ParticleSet(dp, hh, kap, cs)
+    geo.create_wall_x_mdbc(ps, 0.0 + dp, 1.61, 0.0, -1, dp / 2)
+    nw = ps.np
+    zones = [geo.create_inlet_x(ps, 0.3 + 4 * dp, 0.8 + dp, 1.0, +1, 4, (0.0, -3.0), geo.INLET1),
+             geo.create_outlet_y(ps, 1.3 - 4 * dp, 0.0 + dp, 0.2, +1, 4, (2.0, 0.0), geo.OUTLET1),
+             geo.create_outlet_y(ps, 0.5, 0.0 + dp, 0.2, -1, 4, (-2.0, 0.0), geo.OUTLET2)]
+    return Case(name=f"flow_drop_mdbc_dp{dp:g}", particles=ps, h=hh, kap=kap, cs=cs,
+                rho0=1000.0, visco=0.02, delta=0.1, dp=dp,
+                domain=_pad(x_0, x_1, y_0, y_1, nvl, dp), wall_model=WALL_MDBC, dt=dt,
+                meta=dict(nvl=nvl, nwalls=nw, zones=zones))
+
+
 def outlet_channel_mdbc(dp: float = 0.005, speed: float = 2.0) -> Case:
     """A fluid slab driven along a floor into an outlet zone (no counterpart
     case in the reference; it exercises BZ_Integrate_outlet's retyping and

@@ -222,6 +222,7 @@ def create_corner_bt(ps: AleParticleSet, orientation_x, orientation_y, xyv, n):
 # ------------------------------------------------------------ open boundaries
 INLET1 = 7    # src/SPH_defs.h:53
 OUTLET1 = 12  # src/SPH_defs.h:59
+OUTLET2 = 13  # src/SPH_defs.h:60
 
 
 def buffer_zone(x0, xm, y0, ym, nbl, v0, orientation, btype):
@@ -241,6 +242,19 @@ def create_inlet_y(ps: ParticleSet, x, y_0, y_1, orientation, nbl, v0, btype):
         for hh in range(npart):
             ps.add(btype, 0.0, ps.rho0, (rx, y_0 + hh * dp), (v0[0], v0[1]))
     return buffer_zone(x, x + nbl * dp * orientation, y_0, y_1, nbl, v0, (float(orientation), 0.0),
+                       btype)
+
+
+def create_inlet_x(ps: ParticleSet, y, x_0, x_1, orientation, nbl, v0, btype):
+    """``DRAW_CreateInletX``, src/SPH_create.h:472-504: nbl rows of buffer
+    particles above (+1) or below (-1) the line y, and the zone (returned)."""
+    dp = ps.dp
+    npart = int(math.ceil(_len(x_0, y, x_1, y) / dp)) + 1
+    for l in range(nbl):
+        ry = y + dp * l * orientation
+        for hh in range(npart):
+            ps.add(btype, 0.0, ps.rho0, (x_0 + hh * dp, ry), (v0[0], v0[1]))
+    return buffer_zone(x_0, x_1, y, y + nbl * dp * orientation, nbl, v0, (0.0, float(orientation)),
                        btype)
 
 
