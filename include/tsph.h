@@ -368,8 +368,9 @@ int tsph_gnn_adam(tsph_gnn *g, double lr, double beta1, double beta2, double eps
  * write_to_ASCII_VTK (src/SPH_data_to_vtk.h:4-51): the same POLYDATA file
  * (points, type, pressure, density, velocity) in the reference's order. */
 int tsph_write_vtk(tsph_system *s, const char *path);
-/* binary checkpoint of the live particles (state, rates, ghost nodes,
- * constants, domain, precision, tile shape; no counterpart in the reference)
+/* binary checkpoint of the live particles (state, rates, types, ghost nodes,
+ * buffer zones and their capacities, constants, domain, precision, tile
+ * shape; no counterpart in the reference)
  * and a new system restarted from it: stepping it continues the saved run
  * bit for bit. */
 int tsph_save_checkpoint(tsph_system *s, const char *path);

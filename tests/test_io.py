@@ -59,3 +59,26 @@ def test_checkpoint_restart_continues_bit_for_bit(gpu_tsph, tmp_path, precision)
     x, y = a.download(), b.download()
     for f in ("r", "v", "a", "rho", "drho", "p", "type"):
         assert np.array_equal(x[f], y[f]), f
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_checkpoint_of_a_system_with_buffer_zones(gpu_tsph, tmp_path, precision):
+    """The outlet channel saved after its outlet has retyped and erased
+    particles (indices past the initial ones, gaps left by erasures): the
+    restarted system keeps the zones and continues bit for bit, appends and
+    erasures included."""
+    case = cases.outlet_channel_mdbc(dp=0.005)
+    a = gpu_tsph.ParticleSystem.from_case(case, precision)
+    a.step(case.wall_model, case.dt, 450)
+    n_saved = a.np
+    p = tmp_path / "zones.ckp"
+    a.save_checkpoint(str(p))
+    a.step(case.wall_model, case.dt, 150)
+    b = gpu_tsph.ParticleSystem.load_checkpoint(str(p))
+    assert b.np == n_saved
+    b.step(case.wall_model, case.dt, 150)
+    x, y = a.download(), b.download()
+    assert len(x["type"]) == len(y["type"]) and len(x["type"]) < n_saved
+    for f in ("r", "v", "a", "rho", "drho", "p", "type"):
+        assert np.array_equal(x[f], y[f]), f

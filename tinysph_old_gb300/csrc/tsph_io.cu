@@ -92,14 +92,20 @@ int tsph_save_checkpoint(tsph_system *s, const char *path) {
     std::vector<double> gnr(2 * (size_t)n, 0.0);
     std::vector<uint8_t> has(n, 0);
     for (int k = 0; k < n; k++) {
-        const int i = z.index[k];
-        gnr[2 * k] = hs.gnr[2 * (size_t)i];
-        gnr[2 * k + 1] = hs.gnr[2 * (size_t)i + 1];
+        // particles an inlet appended have indices past the ones given at
+        // setup, and no ghost node
+        const size_t i = (size_t)z.index[k];
+        if (i >= hs.has_gnr.size()) continue;
+        gnr[2 * k] = hs.gnr[2 * i];
+        gnr[2 * k + 1] = hs.gnr[2 * i + 1];
         has[k] = hs.has_gnr[i];
     }
     std::ofstream f(path, std::ios::binary);
     if (!f) return io_fail(TSPH_ERR_ARG, std::string("cannot open ") + path);
-    const int32_t head[4] = {1, s->precision, s->eng ? s->eng->tile_shape() : -1, n};
+    // version 2: version 1 followed by the buffer zones and their capacities
+    const int32_t head[4] = {2, s->precision, s->eng ? s->eng->tile_shape() : -1, n};
+    const int32_t nz = (int32_t)(hs.zones.size() / 12);
+    const int32_t zcap[2] = {hs.extra_rows, hs.extra_ids};
     const double cst[11] = {hs.h, hs.kap, hs.cs, hs.rho0, hs.visco, hs.delta, hs.dp,
                             hs.x0, hs.xm, hs.y0, hs.ym};
     f.write(kMagic, 8);
@@ -114,6 +120,9 @@ int tsph_save_checkpoint(tsph_system *s, const char *path) {
     put(f, z.p.data(), n);
     put(f, gnr.data(), 2 * (size_t)n);
     put(f, has.data(), n);
+    put(f, &nz, 1);
+    put(f, hs.zones.data(), hs.zones.size());
+    put(f, zcap, 2);
     if (!f) return io_fail(TSPH_ERR_ARG, std::string("write failed: ") + path);
     return TSPH_OK;
 }
@@ -127,7 +136,7 @@ int tsph_load_checkpoint(const char *path, void *stream, tsph_system **out) {
     int32_t head[4];
     double cst[11];
     if (!get(f, magic, 8) || std::memcmp(magic, kMagic, 8) != 0 || !get(f, head, 4) ||
-        head[0] != 1 || head[3] < 0 || !get(f, cst, 11))
+        (head[0] != 1 && head[0] != 2) || head[3] < 0 || !get(f, cst, 11))
         return io_fail(TSPH_ERR_ARG, std::string("not a checkpoint of this library: ") + path);
     const int n = head[3];
     std::vector<int32_t> type(n);
@@ -139,6 +148,15 @@ int tsph_load_checkpoint(const char *path, void *stream, tsph_system **out) {
         !get(f, rho.data(), n) || !get(f, drho.data(), n) || !get(f, p.data(), n) ||
         !get(f, gnr.data(), 2 * (size_t)n) || !get(f, has.data(), n))
         return io_fail(TSPH_ERR_ARG, std::string("truncated checkpoint: ") + path);
+    int32_t nz = 0, zcap[2] = {0, 0};
+    std::vector<double> zones;
+    if (head[0] >= 2) {
+        if (!get(f, &nz, 1) || nz < 0 || nz > 4096)
+            return io_fail(TSPH_ERR_ARG, std::string("truncated checkpoint: ") + path);
+        zones.resize(12 * (size_t)nz);
+        if (!get(f, zones.data(), zones.size()) || !get(f, zcap, 2))
+            return io_fail(TSPH_ERR_ARG, std::string("truncated checkpoint: ") + path);
+    }
     bool any_gnr = false;
     for (int k = 0; k < n; k++) any_gnr |= has[k] != 0;
     const tsph_constants c = {cst[0], cst[1], cst[2], cst[3], cst[4], cst[5], cst[6]};
@@ -146,6 +164,18 @@ int tsph_load_checkpoint(const char *path, void *stream, tsph_system **out) {
     tsph_system *s = nullptr;
     int rc = tsph_create(&c, &d, head[1], stream, &s);
     if (rc) return rc;
+    // zones as tsph_add_buffer_zone stores them: ox, oy, x0, y0, xm, ym, nbl,
+    // b_len, b_height, btype, vx, vy
+    for (int32_t k = 0; k < nz && !rc; k++) {
+        const double *q = &zones[12 * (size_t)k];
+        rc = tsph_add_buffer_zone(s, q[2], q[4], q[3], q[5], (int)q[6], q[10], q[11], q[0], q[1],
+                                  (int)q[9]);
+    }
+    if (!rc && nz > 0) rc = tsph_set_zone_capacity(s, zcap[0], zcap[1]);
+    if (rc) {
+        tsph_destroy(s);
+        return rc;
+    }
     if ((rc = tsph_add_particles(s, n, type.data(), r.data(), v.data(), rho.data(), p.data(),
                                  any_gnr ? gnr.data() : nullptr)) ||
         (rc = tsph_divide_to_cells(s)) || (rc = tsph_particle_to_cell(s))) {
