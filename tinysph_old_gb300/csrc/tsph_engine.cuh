@@ -596,10 +596,12 @@ template <typename T> class Engine final : public EngineBase {
         int rc;
         const bool dbc = model == 1;
         wall_model_ = model;
-        if (model == 0 && (rc = do_mdbc(err))) return rc;
-        if (model == 2 && (rc = do_bt_density(err))) return rc;
         bool skinned = false;
         if constexpr (std::is_same<T, float>::value) skinned = skin_ > 0.f;
+        // FP32 mDBC step with the skin: mDBC and the predictor share a launch
+        const bool mdbc_fused = model == 0 && nw_ > 0 && skinned;
+        if (model == 0 && !mdbc_fused && (rc = do_mdbc(err))) return rc;
+        if (model == 2 && (rc = do_bt_density(err))) return rc;
         if (skinned) {
             // predictor in the current order; the re-binning runs only when
             // some particle moved more than the skin: in a graph as the body
@@ -615,7 +617,17 @@ template <typename T> class Engine final : public EngineBase {
                 TSPH_CK(cudaStreamGetCaptureInfo(st_, &cs, nullptr, &cg, &deps, nullptr, &nd));
                 TSPH_CK(cudaGraphConditionalHandleCreate(&cond, cg, 0, cudaGraphCondAssignDefault));
             }
-            if ((rc = launch(CAT_OTHER, k_predict_keep<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+            if constexpr (std::is_same<T, float>::value) {
+                if (mdbc_fused) {
+                    const int nbm = blocks_for((long long)nw_ * 8);
+                    rc = launch(CAT_MDBC, k_mdbc8_predict, nbm + blocks_for(nf_), kBlock, err, W_,
+                                nw_, nbm, (const uint32_t *)fstart_, F_, grid_, P_, dt, Fs_, O_,
+                                skin_, rebuild_, health_, cond, capturing_ ? 1 : 0);
+                    if (rc) return rc;
+                }
+            }
+            if (!mdbc_fused &&
+                (rc = launch(CAT_OTHER, k_predict_keep<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
                              (const uint32_t *)fstart_, W_, nw_, grid_, dt, Fs_, O_, skin_,
                              rebuild_, health_, cond, capturing_ ? 1 : 0)))
                 return rc;

@@ -1169,20 +1169,15 @@ __global__ void k_predict_bin(FluidState<T> F, const uint32_t *__restrict__ fsta
 // block, kh >= 2h + 2 skin); a larger move sets *rebuild (and, inside a CUDA
 // graph, the conditional node `cond`), which runs the re-binning before the
 // pair pass.
+// the predictor of one fluid row f (shared with the mDBC-fused launch)
 template <typename T>
-__global__ void k_predict_keep(FluidState<T> F, const uint32_t *__restrict__ fstart,
-                               WallState<T> Wl, int nw, Grid g, T dt, FluidState<T> D,
-                               OldState<T> O, float skin, uint32_t *__restrict__ rebuild,
-                               uint32_t *__restrict__ health, cudaGraphConditionalHandle cond,
-                               int use_cond) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < nw) {
-        const T r = Wl.rho[i];
-        Wl.rho_o[i] = r;
-        Wl.rho[i] = r + Wl.drho[i] * dt * T(0.5);
-        return;
-    }
-    const int f = i - nw;
+__device__ __forceinline__ void predict_keep_fluid(int f, const FluidState<T> &F,
+                                                   const uint32_t *__restrict__ fstart,
+                                                   const Grid &g, T dt, const FluidState<T> &D,
+                                                   const OldState<T> &O, float skin,
+                                                   uint32_t *__restrict__ rebuild,
+                                                   uint32_t *__restrict__ health,
+                                                   cudaGraphConditionalHandle cond, int use_cond) {
     if (f >= n_live(fstart, g.ncells)) return;
     const double2 r = F.r[f];
     const auto v = F.v[f];
@@ -1209,6 +1204,22 @@ __global__ void k_predict_keep(FluidState<T> F, const uint32_t *__restrict__ fst
     }
     if (!(nv.x == nv.x) || !(nv.y == nv.y) || !(dx == dx) || !(dy == dy))
         atomicOr(health, kHealthNan);
+}
+
+template <typename T>
+__global__ void k_predict_keep(FluidState<T> F, const uint32_t *__restrict__ fstart,
+                               WallState<T> Wl, int nw, Grid g, T dt, FluidState<T> D,
+                               OldState<T> O, float skin, uint32_t *__restrict__ rebuild,
+                               uint32_t *__restrict__ health, cudaGraphConditionalHandle cond,
+                               int use_cond) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nw) {
+        const T r = Wl.rho[i];
+        Wl.rho_o[i] = r;
+        Wl.rho[i] = r + Wl.drho[i] * dt * T(0.5);
+        return;
+    }
+    predict_keep_fluid<T>(i - nw, F, fstart, g, dt, D, O, skin, rebuild, health, cond, use_cond);
 }
 
 // gated re-binning of the predicted state: keys + histogram slots

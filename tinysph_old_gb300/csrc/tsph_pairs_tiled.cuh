@@ -451,10 +451,12 @@ namespace tsph {
 // shuffles; the 3x3 solve in FP64 with one reciprocal of the determinant
 // (threshold 0.001 and the Shepard / 1000 fall-backs of :1290-1333), the
 // clamp at 1000 of src/SPH_mDBC.h:43-44.
-static __global__ void __launch_bounds__(kBlock)
-k_mdbc8(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidState<float> F,
-        Grid g, Phys<float> P) {
-    const int gid = blockIdx.x * blockDim.x + threadIdx.x;
+// With `predict` the wall's predictor step follows in the same thread
+// (rho_o = rho, rho += drho dt/2, as k_predict_keep does for walls).
+__device__ __forceinline__ void mdbc8_wall(int gid, const WallState<float> &Wl, int nw,
+                                           const uint32_t *__restrict__ fstart,
+                                           const FluidState<float> &F, const Grid &g,
+                                           const Phys<float> &P, bool predict, float dt) {
     const int w = gid >> 3, sub = gid & 7;
     const bool valid = w < nw;
     float s[12];
@@ -549,7 +551,38 @@ k_mdbc8(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidS
         dens = 1000. - (double)P.rho0;
     }
     if (dens + (double)P.rho0 < 1000.) dens = 1000. - (double)P.rho0;  // clamp of src/SPH_mDBC.h:44
-    Wl.rho[w] = (float)dens;
+    const float rw = (float)dens;
+    if (predict) {
+        Wl.rho_o[w] = rw;
+        Wl.rho[w] = rw + Wl.drho[w] * dt * 0.5f;
+    } else {
+        Wl.rho[w] = rw;
+    }
+}
+
+static __global__ void __launch_bounds__(kBlock)
+k_mdbc8(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidState<float> F,
+        Grid g, Phys<float> P) {
+    mdbc8_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, false, 0.f);
+}
+
+// mDBC and the predictor of a step in one launch: the first nbm blocks
+// compute the walls' densities (each wall then takes its predictor step),
+// the rest run the fluid predictor in the current cell order.  The two halves
+// touch disjoint data (mDBC reads F's type, key, loc and rho and writes the
+// walls; the fluid predictor reads F and writes D and O), so the
+// latency-bound ghost-node sums overlap the bandwidth-bound predictor.
+static __global__ void __launch_bounds__(kBlock)
+k_mdbc8_predict(WallState<float> Wl, int nw, int nbm, const uint32_t *__restrict__ fstart,
+                FluidState<float> F, Grid g, Phys<float> P, float dt, FluidState<float> D,
+                OldState<float> O, float skin, uint32_t *__restrict__ rebuild,
+                uint32_t *__restrict__ health, cudaGraphConditionalHandle cond, int use_cond) {
+    if ((int)blockIdx.x < nbm) {
+        mdbc8_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, true, dt);
+        return;
+    }
+    predict_keep_fluid<float>(((int)blockIdx.x - nbm) * blockDim.x + threadIdx.x, F, fstart, g, dt,
+                              D, O, skin, rebuild, health, cond, use_cond);
 }
 
 }  // namespace tsph
