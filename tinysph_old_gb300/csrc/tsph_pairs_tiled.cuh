@@ -45,7 +45,7 @@ template <class SH> struct TileSmem {
     float inv[SH::cap];   // 1/rho
     int foff[3][kTileRows + 3];
     int woff[3][kTileRows + 3];
-    float2 off[9];
+    float offy[4];  // y offset of a neighbour row: below, own, above (list code 0, 1, 2)
     uint16_t list[SH::list * kTileT];
 };
 
@@ -150,6 +150,99 @@ __device__ __forceinline__ uint32_t in_support(float r2, uint32_t four_h2_bits) 
     return (uint32_t)(__float_as_uint(r2) - 1u) < four_h2_bits ? 1u : 0u;
 }
 
+// Phase-1 scans of one staged row range: every in-support candidate
+// (r^2 <= 4h^2) appends its entry (staged index << 2 | row code).  The entry
+// is written unconditionally and kept by advancing the list pointer.  Only
+// the particle's own cell can hold a coincident particle or the particle
+// itself; there (EXCL) the test is 0 < r^2 <= 4h^2, as one unsigned compare
+// of the bits, elsewhere a plain float compare.  Rows are sorted by y, so
+// the row above is walked upwards and the row below downwards until |dy|
+// passes `reach`, two candidates per iteration (the test of the second ends
+// the walk; a candidate beyond the reach fails the support test anyway).
+template <bool EXCL> __device__ __forceinline__ bool support_test(float r2, float h2) {
+    if constexpr (EXCL) return in_support(r2, __float_as_uint(h2)) != 0u;
+    else return r2 <= h2;
+}
+
+template <bool EXCL>
+__device__ __forceinline__ uint16_t *scan_own(const float2 *__restrict__ loc, int j0, int j1,
+                                              float bx, float by, float h2, uint16_t *w) {
+    uint32_t ent = ((uint32_t)j0 << 2) | 1u;
+    int j = j0;
+    for (; j + 1 < j1; j += 2, ent += 8u) {
+        const float2 l0 = loc[j], l1 = loc[j + 1];
+        const float dx0 = bx - l0.x, dy0 = by - l0.y;
+        const float dx1 = bx - l1.x, dy1 = by - l1.y;
+        const bool in0 = support_test<EXCL>(fmaf(dx0, dx0, dy0 * dy0), h2);
+        const bool in1 = support_test<EXCL>(fmaf(dx1, dx1, dy1 * dy1), h2);
+        *w = (uint16_t)ent;
+        w += in0 ? kTileT : 0;
+        *w = (uint16_t)(ent + 4u);
+        w += in1 ? kTileT : 0;
+    }
+    if (j < j1) {
+        const float2 l = loc[j];
+        const float dx = bx - l.x, dy = by - l.y;
+        *w = (uint16_t)ent;
+        w += support_test<EXCL>(fmaf(dx, dx, dy * dy), h2) ? kTileT : 0;
+    }
+    return w;
+}
+
+__device__ __forceinline__ uint16_t *scan_above(const float2 *__restrict__ loc, int j0, int j1,
+                                                float bx, float by, float h2, float reach,
+                                                uint16_t *w) {
+    uint32_t ent = ((uint32_t)j0 << 2) | 2u;
+    int j = j0;
+    bool go = true;
+    for (; go && j + 1 < j1; j += 2, ent += 8u) {
+        const float2 l0 = loc[j], l1 = loc[j + 1];
+        const float dx0 = bx - l0.x, dy0 = by - l0.y;
+        const float dx1 = bx - l1.x, dy1 = by - l1.y;
+        const bool in0 = fmaf(dx0, dx0, dy0 * dy0) <= h2;
+        const bool in1 = fmaf(dx1, dx1, dy1 * dy1) <= h2;
+        *w = (uint16_t)ent;
+        w += in0 ? kTileT : 0;
+        *w = (uint16_t)(ent + 4u);
+        w += in1 ? kTileT : 0;
+        go = dy1 >= -reach;
+    }
+    if (go && j < j1) {
+        const float2 l = loc[j];
+        const float dx = bx - l.x, dy = by - l.y;
+        *w = (uint16_t)ent;
+        w += fmaf(dx, dx, dy * dy) <= h2 ? kTileT : 0;
+    }
+    return w;
+}
+
+__device__ __forceinline__ uint16_t *scan_below(const float2 *__restrict__ loc, int j0, int j1,
+                                                float bx, float by, float h2, float reach,
+                                                uint16_t *w) {
+    uint32_t ent = ((uint32_t)(j1 - 1) << 2);
+    int j = j1 - 1;
+    bool go = true;
+    for (; go && j - 1 >= j0; j -= 2, ent -= 8u) {
+        const float2 l0 = loc[j], l1 = loc[j - 1];
+        const float dx0 = bx - l0.x, dy0 = by - l0.y;
+        const float dx1 = bx - l1.x, dy1 = by - l1.y;
+        const bool in0 = fmaf(dx0, dx0, dy0 * dy0) <= h2;
+        const bool in1 = fmaf(dx1, dx1, dy1 * dy1) <= h2;
+        *w = (uint16_t)ent;
+        w += in0 ? kTileT : 0;
+        *w = (uint16_t)(ent - 4u);
+        w += in1 ? kTileT : 0;
+        go = dy1 <= reach;
+    }
+    if (go && j >= j0) {
+        const float2 l = loc[j];
+        const float dx = bx - l.x, dy = by - l.y;
+        *w = (uint16_t)ent;
+        w += fmaf(dx, dx, dy * dy) <= h2 ? kTileT : 0;
+    }
+    return w;
+}
+
 // RemoveParticlesOutOfDomain's test (src/SPH_btdebug.h:16-19) on the ordered
 // bits of the coordinates against precomputed ordered thresholds: integer
 // compares instead of FP64 ones (GB300 issues FP64 at a small fraction of the
@@ -175,12 +268,18 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
     const int t0 = blockIdx.x * kTileT;
     if (t0 >= nl) return;
     const int t1 = min(t0 + kTileT, nl);
-    if (tid < 9) sm.off[tid] = make_float2((float)(1 - tid / 3) * g.khf, (float)(1 - tid % 3) * g.khf);
-    const uint32_t h2bits = __float_as_uint(K.four_h2);
+    if (tid < 4) sm.offy[tid] = tid < 3 ? (float)(1 - tid) * g.khf : 0.f;
+    const float khf = g.khf;
     // rows above / below are sorted by y (as of the last binning): stop once
     // |dy| > K.reach = 2h (+ rounding margin, + twice the skin when the cells
     // were kept through the predictor)
     const float reach = K.reach;
+    // the CTA's last target: when it lies in the first window's column and
+    // rows, that window is the whole CTA and its end needs no further lookup
+    // (the usual case; each global round trip here is exposed latency)
+    const uint32_t klast = __ldg(F.key + t1 - 1);
+    const int cxl = (int)(klast / (uint32_t)ncy);
+    const int cyll = (int)klast - cxl * ncy;
     int cur = t0;
     int rows = kTileRows;
     while (cur < t1) {  // block-uniform loop over row windows
@@ -188,10 +287,20 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
         const int cx = (int)(kc / (uint32_t)ncy);
         const int cy0 = (int)kc - cx * ncy;
         const int rowlim = min(cy0 + rows, ncy);
-        const int we = min(t1, (int)__ldg(fstart + cx * ncy + rowlim));
-        const int cyl = (int)__ldg(F.key + we - 1) - cx * ncy;
+        int we, cyl;
+        if (cxl == cx && cyll < rowlim) {
+            we = t1;
+            cyl = cyll;
+        } else {
+            we = min(t1, (int)__ldg(fstart + cx * ncy + rowlim));
+            cyl = (int)__ldg(F.key + we - 1) - cx * ncy;
+        }
         const int rlo = max(cy0 - 1, 0), rhi = min(cyl + 1, ncy - 1);
         const int nr = rhi - rlo + 1;
+        const int i = cur + tid;
+        const bool active = i < we;
+        // the target's own cell row, fetched with the cell offsets below
+        const uint32_t ki = active ? __ldg(F.key + i) : 0u;
         __syncthreads();  // previous window finished with shared memory
         for (int e = tid; e < 3 * (nr + 1); e += kTileT) {
             const int dxi = e / (nr + 1), q = e - dxi * (nr + 1);
@@ -222,148 +331,125 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
             rows = (rows + 1) >> 1;
             continue;
         }
-        const int i = cur + tid;
-        const bool active = i < we;
         Acc4 acc = {0.f, 0.f, 0.f, 0.f};
         float2 la = make_float2(0.f, 0.f), va = make_float2(0.f, 0.f);
         float sa = 0.f, Pa = 0.f, Ia = 0.f, Ra2 = 0.f;
         int cy = 0;
         if (tot <= SH::cap) {
-            // ---- stage the neighbour block
+            // ---- stage the neighbour block: slot e of the block is row
+            // e - base + first of its segment (walls of column 0, fluid of
+            // column 0, walls of column 1, ...); every load of a thread is
+            // issued before the first store, one round trip per window.  x is
+            // staged relative to the centre column (|x| < 2 kh: the rounding
+            // stays at ~1e-7 of a cell), y relative to the particle's own cell
+            constexpr int kStage = (SH::cap + kTileT - 1) / kTileT;
+            float2 st_l[kStage], st_v[kStage];
+            float st_s[kStage], st_p[kStage];
 #pragma unroll
-            for (int d = 0; d < 3; d++) {
-                const int nwd = sm.woff[d][nr] - w0[d];
-                for (int k = tid; k < nwd; k += kTileT) {
-                    const int j = w0[d] + k;
-                    const float s = __ldg(Wl.rho + j);
-                    const float p = STORED_P ? __ldg(Wl.p + j) : eos(s, P);
-                    const float ib = rcp_approx(P.rho0 + s);
-                    sm.loc[wb[d] + k] = __ldg(Wl.loc + j);
-                    sm.vs[wb[d] + k] = staged_vs(make_float2(0.f, 0.f), s, p, ib);
-                    sm.inv[wb[d] + k] = ib;
+            for (int u = 0; u < kStage; u++) {
+                const int e = tid + u * kTileT;
+                int j = e + w0[0];
+                bool wall = true;
+                float xs = -khf;  // x of the cell's origin relative to the centre column's
+                if (e >= fb[0]) { j = e - fb[0] + f0[0]; wall = false; }
+                if (e >= wb[1]) { j = e - wb[1] + w0[1]; wall = true; xs = 0.f; }
+                if (e >= fb[1]) { j = e - fb[1] + f0[1]; wall = false; }
+                if (e >= wb[2]) { j = e - wb[2] + w0[2]; wall = true; xs = khf; }
+                if (e >= fb[2]) { j = e - fb[2] + f0[2]; wall = false; }
+                st_l[u] = make_float2(0.f, 0.f);
+                st_v[u] = make_float2(0.f, 0.f);
+                st_s[u] = 0.f;
+                st_p[u] = 0.f;
+                if (e < tot) {
+                    st_l[u] = __ldg((wall ? Wl.loc : F.loc) + j);
+                    st_l[u].x += xs;
+                    st_s[u] = __ldg((wall ? Wl.rho : F.rho) + j);
+                    if (STORED_P) st_p[u] = __ldg((wall ? Wl.p : F.p) + j);
+                    if (!wall) st_v[u] = __ldg(F.v + j);
                 }
-                const int nfd = sm.foff[d][nr] - f0[d];
-                for (int k = tid; k < nfd; k += kTileT) {
-                    const int j = f0[d] + k;
-                    const float s = __ldg(F.rho + j);
-                    const float p = STORED_P ? __ldg(F.p + j) : eos(s, P);
+            }
+#pragma unroll
+            for (int u = 0; u < kStage; u++) {
+                const int e = tid + u * kTileT;
+                if (e < tot) {
+                    const float s = st_s[u];
+                    const float p = STORED_P ? st_p[u] : eos(s, P);
                     const float ib = rcp_approx(P.rho0 + s);
-                    sm.loc[fb[d] + k] = __ldg(F.loc + j);
-                    sm.vs[fb[d] + k] = staged_vs(__ldg(F.v + j), s, p, ib);
-                    sm.inv[fb[d] + k] = ib;
+                    sm.loc[e] = st_l[u];
+                    sm.vs[e] = staged_vs(st_v[u], s, p, ib);
+                    sm.inv[e] = ib;
                 }
             }
             __syncthreads();
             if (active) {
-                cy = (int)__ldg(F.key + i) - cx * ncy;
+                cy = (int)ki - cx * ncy;
                 const int own = fb[1] + (i - f0[1]);
                 la = sm.loc[own];
+                // ---- phase 1: in-support neighbours into the list (entry:
+                // staged index << 2 | row code).  Per column the rows below,
+                // own and above are staged ranges [R0, R1), [R1, R2), [R2, R3).
+                bool overflow = false;
+                uint16_t *const lst = sm.list + tid;
+                uint16_t *const wend = lst + SH::list * kTileT;
+                uint16_t *w = lst;
+                const float by_b = la.y + khf, by_a = la.y - khf;
+                const int q = cy - rlo;
+                const bool hb = cy >= 1, ha = cy + 1 < ncy;
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    const int col = cx + d - 1;
+                    if (col < 0 || col >= g.ncx) continue;
+#pragma unroll
+                    for (int kind = 0; kind < 2; kind++) {
+                        if (kind == 0 && totw == 0) continue;  // block-uniform: no walls here
+                        const int *offs = kind == 0 ? sm.woff[d] : sm.foff[d];
+                        const int base = kind == 0 ? wb[d] - w0[d] : fb[d] - f0[d];
+                        const int R1 = base + offs[q], R2 = base + offs[q + 1];
+                        const int R0 = hb ? base + offs[q - 1] : R1;
+                        const int R3 = ha ? base + offs[q + 2] : R2;
+                        // a range that could overflow the list is skipped (the
+                        // target then takes the global-memory path)
+                        if (wend - w < (R2 - R1) * kTileT) overflow = true;
+                        else if (d == 1 && kind == 1)
+                            w = scan_own<true>(sm.loc, R1, R2, la.x, la.y, K.four_h2, w);
+                        else
+                            w = scan_own<false>(sm.loc, R1, R2, la.x, la.y, K.four_h2, w);
+                        if (wend - w < (R3 - R2) * kTileT) overflow = true;
+                        else w = scan_above(sm.loc, R2, R3, la.x, by_a, K.four_h2, reach, w);
+                        if (wend - w < (R1 - R0) * kTileT) overflow = true;
+                        else w = scan_below(sm.loc, R0, R1, la.x, by_b, K.four_h2, reach, w);
+                    }
+                }
+                const int cnt = (int)((w - lst) / kTileT);
+                // the target's own terms (read after phase 1: fewer live registers there)
                 const float4 vsa = sm.vs[own];
                 va = make_float2(vsa.x, vsa.y);
                 sa = vsa.z;
                 Pa = vsa.w;
                 Ia = sm.inv[own];
                 Ra2 = K.two_rho0 + sa;
-                // ---- phase 1: in-support neighbours into the list.  The list
-                // write is unconditional (the slot is only kept when the pair
-                // is in support); overflow is checked once per cell.
-                int cnt = 0;
-                bool overflow = false;
-                uint16_t *lst = sm.list + tid;
-#pragma unroll
-                for (int dxi = 0; dxi < 3; dxi++) {
-                    const int col = cx + dxi - 1;
-                    if (col < 0 || col >= g.ncx) continue;
-#pragma unroll
-                    for (int dyi = 0; dyi < 3; dyi++) {
-                        const int row = cy + dyi - 1;
-                        if (row < 0 || row >= ncy) continue;
-                        const int q = row - rlo;
-                        const int code = dxi * 3 + dyi;
-                        const float bx = la.x + sm.off[code].x, by = la.y + sm.off[code].y;
-#pragma unroll
-                        for (int kind = 0; kind < 2; kind++) {
-                            if (kind == 0 && totw == 0) continue;  // block-uniform: no walls here
-                            const int j0 = kind == 0 ? wb[dxi] + sm.woff[dxi][q] - w0[dxi]
-                                                     : fb[dxi] + sm.foff[dxi][q] - f0[dxi];
-                            const int j1 = kind == 0 ? wb[dxi] + sm.woff[dxi][q + 1] - w0[dxi]
-                                                     : fb[dxi] + sm.foff[dxi][q + 1] - f0[dxi];
-                            if (cnt + (j1 - j0) > SH::list) {
-                                overflow = true;
-                                continue;
-                            }
-                            uint16_t *w = lst + cnt * kTileT;
-                            if (dyi == 1) {
-                                // own row: every candidate, two per iteration
-                                uint32_t ent = ((uint32_t)j0 << 4) | (uint32_t)code;
-                                int j = j0;
-                                for (; j + 1 < j1; j += 2, ent += 32u) {
-                                    const float2 lb0 = sm.loc[j], lb1 = sm.loc[j + 1];
-                                    const float dx0 = bx - lb0.x, dy0 = by - lb0.y;
-                                    const float dx1 = bx - lb1.x, dy1 = by - lb1.y;
-                                    const uint32_t in0 = in_support(fmaf(dx0, dx0, dy0 * dy0), h2bits);
-                                    const uint32_t in1 = in_support(fmaf(dx1, dx1, dy1 * dy1), h2bits);
-                                    *w = (uint16_t)ent;
-                                    w += in0 * kTileT;
-                                    *w = (uint16_t)(ent + 16u);
-                                    w += in1 * kTileT;
-                                }
-                                if (j < j1) {
-                                    const float2 lb = sm.loc[j];
-                                    const float dx = bx - lb.x, dy = by - lb.y;
-                                    const uint32_t in = in_support(fmaf(dx, dx, dy * dy), h2bits);
-                                    *w = (uint16_t)ent;
-                                    w += in * kTileT;
-                                }
-                            } else if (dyi == 2) {
-                                // row above, ascending y: dy = by - lb.y decreases
-                                uint32_t ent = ((uint32_t)j0 << 4) | (uint32_t)code;
-                                for (int j = j0; j < j1; j++, ent += 16u) {
-                                    const float2 lb = sm.loc[j];
-                                    const float dx = bx - lb.x, dy = by - lb.y;
-                                    if (dy < -reach) break;
-                                    const uint32_t in = in_support(fmaf(dx, dx, dy * dy), h2bits);
-                                    *w = (uint16_t)ent;
-                                    w += in * kTileT;
-                                }
-                            } else {
-                                // row below, descending y: dy = by - lb.y increases
-                                uint32_t ent = ((uint32_t)(j1 - 1) << 4) | (uint32_t)code;
-                                for (int j = j1 - 1; j >= j0; j--, ent -= 16u) {
-                                    const float2 lb = sm.loc[j];
-                                    const float dx = bx - lb.x, dy = by - lb.y;
-                                    if (dy > reach) break;
-                                    const uint32_t in = in_support(fmaf(dx, dx, dy * dy), h2bits);
-                                    *w = (uint16_t)ent;
-                                    w += in * kTileT;
-                                }
-                            }
-                            cnt = (int)((w - lst) / kTileT);
-                        }
-                    }
-                }
                 if (!overflow) {
                     // ---- phase 2: the pair terms over the list, two at a time
                     int k = 0;
                     for (; k + 1 < cnt; k += 2) {
                         const uint32_t e0 = lst[k * kTileT], e1 = lst[(k + 1) * kTileT];
-                        const float2 o0 = sm.off[e0 & 15u], o1 = sm.off[e1 & 15u];
-                        const int j0 = (int)(e0 >> 4), j1 = (int)(e1 >> 4);
+                        const float oy0 = sm.offy[e0 & 3u], oy1 = sm.offy[e1 & 3u];
+                        const int j0 = (int)(e0 >> 2), j1 = (int)(e1 >> 2);
                         const float2 lb0 = sm.loc[j0], lb1 = sm.loc[j1];
                         const float4 b0 = sm.vs[j0], b1 = sm.vs[j1];
                         const float ib0 = sm.inv[j0], ib1 = sm.inv[j1];
-                        pair_terms((la.x + o0.x) - lb0.x, (la.y + o0.y) - lb0.y, va.x - b0.x,
+                        pair_terms(la.x - lb0.x, (la.y + oy0) - lb0.y, va.x - b0.x,
                                    va.y - b0.y, sa, Pa, Ia, Ra2, b0.z, b0.w, ib0, K, acc);
-                        pair_terms((la.x + o1.x) - lb1.x, (la.y + o1.y) - lb1.y, va.x - b1.x,
+                        pair_terms(la.x - lb1.x, (la.y + oy1) - lb1.y, va.x - b1.x,
                                    va.y - b1.y, sa, Pa, Ia, Ra2, b1.z, b1.w, ib1, K, acc);
                     }
                     if (k < cnt) {
                         const uint32_t e = lst[k * kTileT];
-                        const int j = (int)(e >> 4);
-                        const float2 o = sm.off[e & 15u];
+                        const int j = (int)(e >> 2);
+                        const float oy = sm.offy[e & 3u];
                         const float2 lb = sm.loc[j];
                         const float4 b = sm.vs[j];
-                        pair_terms((la.x + o.x) - lb.x, (la.y + o.y) - lb.y, va.x - b.x,
+                        pair_terms(la.x - lb.x, (la.y + oy) - lb.y, va.x - b.x,
                                    va.y - b.y, sa, Pa, Ia, Ra2, b.z, b.w, sm.inv[j], K, acc);
                     }
                 } else {
@@ -372,7 +458,7 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 }
             }
         } else if (active) {
-            cy = (int)__ldg(F.key + i) - cx * ncy;
+            cy = (int)ki - cx * ncy;
             la = __ldg(F.loc + i);
             va = __ldg(F.v + i);
             sa = __ldg(F.rho + i);
