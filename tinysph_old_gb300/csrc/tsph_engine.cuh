@@ -229,7 +229,8 @@ template <typename T> class Engine final : public EngineBase {
     int do_mdbc(std::string &err) {
         if (nw_ == 0) return 0;
         if constexpr (std::is_same<T, float>::value)
-            return launch(CAT_MDBC, k_mdbc8, blocks_for((long long)nw_ * 8), kBlock, err, W_, nw_,
+            return launch(CAT_MDBC, k_mdbc_f32, blocks_for((long long)nw_ * kMdbcLanes), kBlock, err,
+                          W_, nw_,
                           (const uint32_t *)fstart_, F_, grid_, P_);
         else
             return launch(CAT_MDBC, k_mdbc<T>, blocks_for((long long)nw_ * 32), kBlock, err, W_,
@@ -619,8 +620,8 @@ template <typename T> class Engine final : public EngineBase {
             }
             if constexpr (std::is_same<T, float>::value) {
                 if (mdbc_fused) {
-                    const int nbm = blocks_for((long long)nw_ * 8);
-                    rc = launch(CAT_MDBC, k_mdbc8_predict, nbm + blocks_for(nf_), kBlock, err, W_,
+                    const int nbm = blocks_for((long long)nw_ * kMdbcLanes);
+                    rc = launch(CAT_MDBC, k_mdbc_f32_predict, nbm + blocks_for(nf_), kBlock, err, W_,
                                 nw_, nbm, (const uint32_t *)fstart_, F_, grid_, P_, dt, Fs_, O_,
                                 skin_, rebuild_, health_, cond, capturing_ ? 1 : 0);
                     if (rc) return rc;
@@ -1184,7 +1185,8 @@ template <typename T> class Engine final : public EngineBase {
         int rc;
         if (!alive_count_ && (rc = alloc(&alive_count_, 1, err))) return rc;
         TSPH_CK(cudaMemsetAsync(alive_count_, 0, 4, st_));
-        if ((rc = launch(CAT_OTHER, k_count_alive, blocks_for(ntot_), kBlock, err,
+        if ((rc = launch(CAT_OTHER, k_count_alive,
+                         std::min(blocks_for((long long)(ntot_ >> 2) + 1), 4 * 152), kBlock, err,
                          (const uint8_t *)S_.alive, ntot_, alive_count_)))
             return rc;
         uint32_t cnt = 0;

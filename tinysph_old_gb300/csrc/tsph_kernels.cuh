@@ -1347,11 +1347,28 @@ __global__ void k_export(FluidState<T> F, const uint32_t *__restrict__ fstart, i
     S.alive[id] = 1;
 }
 
-// number of live particles in the alive map (one atomic per warp)
-static __global__ void k_count_alive(const uint8_t *__restrict__ alive, int n, uint32_t *__restrict__ count) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const unsigned b = __ballot_sync(0xffffffffu, i < n && alive[i] != 0);
-    if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (uint32_t)__popc(b));
+// number of live particles in the alive map: four flags per 32-bit word
+// (the map is a cudaMalloc allocation, 256-byte aligned), a grid-stride
+// loop, one atomic per block (one per warp on a single counter serialises
+// in L2)
+static __global__ void __launch_bounds__(kBlock) k_count_alive(const uint8_t *__restrict__ alive, int n,
+                                                              uint32_t *__restrict__ count) {
+    __shared__ uint32_t part[kBlock / 32];
+    const uint32_t *__restrict__ a4 = reinterpret_cast<const uint32_t *>(alive);
+    const int nw = n >> 2;
+    uint32_t c = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nw; i += gridDim.x * blockDim.x)
+        c += (uint32_t)__popc(__vcmpne4(__ldg(a4 + i), 0u)) >> 3;
+    if (blockIdx.x == 0 && threadIdx.x < (n & 3)) c += alive[4 * nw + threadIdx.x] != 0 ? 1u : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t t = 0;
+        for (int w = 0; w < kBlock / 32; w++) t += part[w];
+        if (t) atomicAdd(count, t);
+    }
 }
 
 template <typename T>

@@ -532,43 +532,84 @@ inline TileConst make_tile_const(const Phys<float> &P, double h, double rho0, do
 
 namespace tsph {
 
-// mDBC ghost-node density, FP32 build: 8 lanes per wall particle, the 12
-// moment sums (src/SPH_kernel_approx.h:1237-1287) in FP32, reduced with
-// shuffles; the 3x3 solve in FP64 with one reciprocal of the determinant
+// mDBC ghost-node density, FP32 build: 8 lanes per wall particle (a launch
+// of one wave, which leaves room beside it for the fused predictor's blocks),
+// the 12 moment sums (src/SPH_kernel_approx.h:1237-1287) in FP32, reduced
+// with shuffles; the 3x3 solve in FP64 with one reciprocal of the determinant
 // (threshold 0.001 and the Shepard / 1000 fall-backs of :1290-1333), the
 // clamp at 1000 of src/SPH_mDBC.h:43-44.
 // With `predict` the wall's predictor step follows in the same thread
 // (rho_o = rho, rho += drho dt/2, as k_predict_keep does for walls).
-__device__ __forceinline__ void mdbc8_wall(int gid, const WallState<float> &Wl, int nw,
+constexpr int kMdbcLanes = 8;
+
+__device__ __forceinline__ void mdbc_wall(int gid, const WallState<float> &Wl, int nw,
                                            const uint32_t *__restrict__ fstart,
                                            const FluidState<float> &F, const Grid &g,
                                            const Phys<float> &P, bool predict, float dt) {
-    const int w = gid >> 3, sub = gid & 7;
+    const int w = gid / kMdbcLanes, sub = gid % kMdbcLanes;
     const bool valid = w < nw;
     float s[12];
 #pragma unroll
     for (int q = 0; q < 12; q++) s[q] = 0.f;
-    const uint32_t gk = valid ? Wl.gkey[w] : (uint32_t)g.ncells;
+    const uint32_t gk = valid ? __ldg(Wl.gkey + w) : (uint32_t)g.ncells;
     if (gk < (uint32_t)g.ncells) {
         const int cx = (int)(gk / (uint32_t)g.ncy);
         const int cy = (int)gk - cx * g.ncy;
-        const float2 gl = Wl.gloc[w];
+        const float2 gl = __ldg(Wl.gloc + w);
+        // the three rows of a column are contiguous in the sorted state: one
+        // candidate range per column, the three fetched together and walked
+        // as one list, kUnroll candidates (all their loads) per iteration
+        const int ylo = max(cy - 1, 0), yhi = min(cy + 1, g.ncy - 1);
+        int jlo[3], n[3];
 #pragma unroll
-        for (int dxi = 0; dxi < 3; dxi++) {
-            const int col = cx + dxi - 1;
-            if (col < 0 || col >= g.ncx) continue;
-            const float ox = gl.x + (float)(1 - dxi) * g.khf;
-            // three rows of one column are contiguous in the sorted state
-            const int ylo = max(cy - 1, 0), yhi = min(cy + 1, g.ncy - 1);
-            const int c0 = col * g.ncy;
-            const int jlo = (int)__ldg(fstart + c0 + ylo), jhi = (int)__ldg(fstart + c0 + yhi + 1);
-            for (int j = jlo + sub; j < jhi; j += 8) {
-                if (F.type && __ldg(F.type + j) != 0) continue;  // fluid only (buffer zones)
-                const uint32_t kb = __ldg(F.key + j);
-                const int rowb = (int)kb - c0;
-                const float2 lb = __ldg(F.loc + j);
-                const float drx = ox - lb.x;
-                const float dry = (gl.y + (float)(cy - rowb) * g.khf) - lb.y;
+        for (int d = 0; d < 3; d++) {
+            const int col = cx + d - 1;
+            jlo[d] = 0;
+            n[d] = 0;
+            if (col >= 0 && col < g.ncx) {
+                const int c0 = col * g.ncy;
+                jlo[d] = (int)__ldg(fstart + c0 + ylo);
+                n[d] = (int)__ldg(fstart + c0 + yhi + 1) - jlo[d];
+            }
+        }
+        const int n01 = n[0] + n[1], ntot = n01 + n[2];
+        constexpr int kUnroll = 4;
+        for (int e0 = sub; e0 < ntot; e0 += kUnroll * kMdbcLanes) {
+            uint32_t kb[kUnroll];
+            float2 lb[kUnroll];
+            float sbv[kUnroll];
+            int dd[kUnroll];
+            bool use[kUnroll];
+#pragma unroll
+            for (int u = 0; u < kUnroll; u++) {
+                const int e = e0 + u * kMdbcLanes;
+                int d = 2, j = jlo[2] + e - n01;
+                if (e < n[0]) {
+                    d = 0;
+                    j = jlo[0] + e;
+                } else if (e < n01) {
+                    d = 1;
+                    j = jlo[1] + e - n[0];
+                }
+                dd[u] = d;
+                use[u] = e < ntot;
+                kb[u] = 0u;
+                lb[u] = make_float2(0.f, 0.f);
+                sbv[u] = 0.f;
+                if (use[u]) {
+                    kb[u] = __ldg(F.key + j);
+                    lb[u] = __ldg(F.loc + j);
+                    sbv[u] = __ldg(F.rho + j);
+                    if (F.type && __ldg(F.type + j) != 0) use[u] = false;  // fluid only (buffer zones)
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kUnroll; u++) {
+                if (!use[u]) continue;
+                const int col = cx + dd[u] - 1;
+                const int rowb = (int)kb[u] - col * g.ncy;
+                const float drx = (gl.x + (float)(1 - dd[u]) * g.khf) - lb[u].x;
+                const float dry = (gl.y + (float)(cy - rowb) * g.khf) - lb[u].y;
                 const float r2 = fmaf(drx, drx, dry * dry);
                 if (!(r2 <= P.four_h2)) continue;
                 float W, Fk;
@@ -578,7 +619,7 @@ __device__ __forceinline__ void mdbc8_wall(int gid, const WallState<float> &Wl, 
                 } else {
                     wendland32(r2, P, W, Fk, true);
                 }
-                const float sb = __ldg(F.rho + j);  // rho_b - rho0
+                const float sb = sbv[u];  // rho_b - rho0
                 const float V = P.m * rcp_approx(P.rho0 + sb);
                 const float WV = W * V, FV = Fk * V;
                 // right-hand side of the density field shifted by rho0
@@ -599,9 +640,8 @@ __device__ __forceinline__ void mdbc8_wall(int gid, const WallState<float> &Wl, 
     }
 #pragma unroll
     for (int q = 0; q < 12; q++) {
-        s[q] += __shfl_xor_sync(0xffffffffu, s[q], 4);
-        s[q] += __shfl_xor_sync(0xffffffffu, s[q], 2);
-        s[q] += __shfl_xor_sync(0xffffffffu, s[q], 1);
+#pragma unroll
+        for (int o = kMdbcLanes / 2; o > 0; o >>= 1) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
     }
     if (!valid || sub != 0) return;
     // The reference solves A x = (sum m W, sum m dr_x F, sum m dr_y F) for
@@ -647,9 +687,9 @@ __device__ __forceinline__ void mdbc8_wall(int gid, const WallState<float> &Wl, 
 }
 
 static __global__ void __launch_bounds__(kBlock)
-k_mdbc8(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidState<float> F,
-        Grid g, Phys<float> P) {
-    mdbc8_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, false, 0.f);
+k_mdbc_f32(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidState<float> F,
+            Grid g, Phys<float> P) {
+    mdbc_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, false, 0.f);
 }
 
 // mDBC and the predictor of a step in one launch: the first nbm blocks
@@ -659,12 +699,12 @@ k_mdbc8(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidS
 // walls; the fluid predictor reads F and writes D and O), so the
 // latency-bound ghost-node sums overlap the bandwidth-bound predictor.
 static __global__ void __launch_bounds__(kBlock)
-k_mdbc8_predict(WallState<float> Wl, int nw, int nbm, const uint32_t *__restrict__ fstart,
+k_mdbc_f32_predict(WallState<float> Wl, int nw, int nbm, const uint32_t *__restrict__ fstart,
                 FluidState<float> F, Grid g, Phys<float> P, float dt, FluidState<float> D,
                 OldState<float> O, float skin, uint32_t *__restrict__ rebuild,
                 uint32_t *__restrict__ health, cudaGraphConditionalHandle cond, int use_cond) {
     if ((int)blockIdx.x < nbm) {
-        mdbc8_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, true, dt);
+        mdbc_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, true, dt);
         return;
     }
     predict_keep_fluid<float>(((int)blockIdx.x - nbm) * blockDim.x + threadIdx.x, F, fstart, g, dt,
