@@ -3,6 +3,7 @@
 #pragma once
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <numeric>
@@ -94,6 +95,9 @@ template <typename T> class Engine final : public EngineBase {
 
     // ---- profiling
     bool prof_ = false;
+    // programmatic dependent launch of the engine's kernels (TSPH_PDL=0 turns
+    // it off, e.g. to compare)
+    bool pdl_ = true;
     struct Mark {
         int cat;
         cudaEvent_t a, b;
@@ -125,7 +129,10 @@ template <typename T> class Engine final : public EngineBase {
         return e;
     }
 
-    // launch with optional event bracketing for the profile
+    // launch with optional event bracketing for the profile.  Every kernel
+    // launched here begins with pdl_enter(), so it may be launched with
+    // programmatic stream serialisation: its launch overlaps the previous
+    // kernel's tail, its first instruction waits for that kernel.
     template <typename K, typename... A>
     int launch(int cat, K kern, int grid, int block, std::string &err, A... args) {
         cudaEvent_t a = nullptr, b = nullptr;
@@ -134,8 +141,18 @@ template <typename T> class Engine final : public EngineBase {
             b = ev();
             cudaEventRecord(a, st_);
         }
-        kern<<<grid, block, 0, st_>>>(args...);
-        cudaError_t e = cudaGetLastError();
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3((unsigned)block);
+        cfg.dynamicSmemBytes = 0;
+        cfg.stream = st_;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = pdl_ ? 1 : 0;
+        cudaError_t e = cudaLaunchKernelEx(&cfg, kern, args...);
+        if (e == cudaSuccess) e = cudaGetLastError();
         if (e != cudaSuccess) {
             err = std::string("kernel launch: ") + cudaGetErrorString(e);
             return 2;
@@ -711,6 +728,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int init(const HostSetup &hs, void *stream, std::string &err) override {
+        if (const char *v = std::getenv("TSPH_PDL")) pdl_ = std::atoi(v) != 0;
         if (stream) {
             st_ = static_cast<cudaStream_t>(stream);
         } else {

@@ -21,6 +21,7 @@ __global__ void k_graph_export(FluidState<T> F, const uint32_t *__restrict__ fst
                                int32_t *__restrict__ deg, int32_t *__restrict__ nbr,
                                float2 *__restrict__ acc, float *__restrict__ rate,
                                uint32_t *__restrict__ overflow) {
+    pdl_enter();
     const int node = blockIdx.x * blockDim.x + threadIdx.x;
     const int nl = n_live(fstart, g.ncells);
     if (node >= nw + nl) return;
@@ -85,6 +86,7 @@ __global__ void k_graph_export(FluidState<T> F, const uint32_t *__restrict__ fst
 // sums over the fluid nodes of (y0, y1) and their count into out[0..2]
 static __global__ void k_fluid_sum2(const uint32_t *__restrict__ fstart, int ncells, int nw,
                              const float *__restrict__ y, double *__restrict__ out) {
+    pdl_enter();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     double a = 0, b = 0, c = 0;
     if (f < n_live(fstart, ncells)) {
@@ -141,6 +143,7 @@ __global__ void k_apply_update(FluidState<T> F, const uint32_t *__restrict__ fst
                                int nw, const float *__restrict__ y, float su, float ss, double kdt,
                                int add_rates, int phase, const double *__restrict__ ysum,
                                T rho0, WindowRef ref, uint32_t *__restrict__ health) {
+    pdl_enter();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_live(fstart, ncells)) return;
     const int node = nw + f;
@@ -190,6 +193,7 @@ __global__ void k_apply_update(FluidState<T> F, const uint32_t *__restrict__ fst
 template <typename T>
 __global__ void k_window_check(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
                                double kdt, T rho0, WindowRef ref, double *__restrict__ out) {
+    pdl_enter();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     double e = 0, ex = 0, ey = 0, dvc = 0, one = 0;
     unsigned long long arg = 0ull;

@@ -59,6 +59,18 @@ __host__ __device__ inline long long ordered_bits(double x) {
     return b >= 0 ? b : (b ^ 0x7fffffffffffffffLL);
 }
 
+// Programmatic dependent launch.  Every kernel the engine launches starts
+// here: it waits until the previous kernel of the stream has completed and
+// its writes are visible (a no-op when it was launched without the
+// programmatic-serialisation attribute), then lets the next kernel of the
+// stream begin launching, so that kernel's launch and block scheduling
+// overlap this one's tail instead of following it.  Nothing is read or
+// written before the wait.
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ inline bool is_finite_d(double x) {
     return (__double_as_longlong(x) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
 }

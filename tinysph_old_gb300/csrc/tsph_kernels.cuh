@@ -183,6 +183,7 @@ static __global__ void k_bin_keep_dead(const double2 *__restrict__ r, const uint
                                 const int *__restrict__ n_ptr, Grid g,
                                 uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
                                 uint32_t *__restrict__ counts, uint32_t *__restrict__ health) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *n_ptr) return;
     uint32_t k;
@@ -259,6 +260,7 @@ static __global__ void __launch_bounds__(kScanThreads) k_scan_tiles_clear(uint32
                                                                          uint32_t *__restrict__ tile_sums,
                                                                          int n,
                                                                          const uint32_t *__restrict__ gate) {
+    pdl_enter();
     if (gated_off(gate)) return;
     const int base = blockIdx.x * kScanTile + threadIdx.x * kScanItems;
     uint32_t v[kScanItems];
@@ -284,6 +286,7 @@ static __global__ void __launch_bounds__(kScanThreads) k_scan_tiles_clear(uint32
 static __global__ void k_scan_add_tiles(uint32_t *__restrict__ out,
                                         const uint32_t *__restrict__ tile_sums, int ntiles, int n,
                                         const uint32_t *__restrict__ gate) {
+    pdl_enter();
     if (gated_off(gate)) return;
     __shared__ uint32_t red[kBlock / 32];
     const int i0 = blockIdx.x * blockDim.x;
@@ -347,6 +350,7 @@ static __global__ void k_place(const uint32_t *__restrict__ key, const uint32_t 
                         const uint32_t *__restrict__ start, uint32_t *__restrict__ tmp_id,
                         uint32_t *__restrict__ tmp_src, const double2 *__restrict__ r,
                         long long *__restrict__ tmp_y, const uint32_t *__restrict__ gate) {
+    pdl_enter();
     if (gated_off(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *n_ptr) return;
@@ -401,6 +405,7 @@ __global__ void k_rank_scatter(const uint32_t *__restrict__ key, const int *__re
                                const T *__restrict__ orho2, OldState<T> O,
                                const uint32_t *__restrict__ gate,
                                const uint8_t *__restrict__ stype) {
+    pdl_enter();
     if (gated_off(gate)) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= *n_ptr) return;
@@ -450,6 +455,7 @@ __global__ void k_rank_scatter(const uint32_t *__restrict__ key, const int *__re
 template <typename T>
 __global__ void k_eos(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
                       WallState<T> Wl, int nw, Phys<T> P, uint32_t *__restrict__ health) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     T s;
     T *pout;
@@ -473,6 +479,7 @@ __global__ void k_eos(FluidState<T> F, const uint32_t *__restrict__ fstart, int 
 template <typename T>
 __global__ void k_predict_inplace(FluidState<T> F, OldState<T> O, const uint32_t *__restrict__ fstart,
                                   int ncells, WallState<T> Wl, int nw, T dt) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nw) {
         const T r = Wl.rho[i];
@@ -517,6 +524,7 @@ template <typename T> __device__ __forceinline__ T corrector_rho(T rho_o_s, T rh
 template <typename T>
 __global__ void k_correct_inplace(FluidState<T> F, OldState<T> O, const uint32_t *__restrict__ fstart,
                                   int ncells, WallState<T> Wl, int nw, T dt, T rho0) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nw) {
         Wl.rho[i] = corrector_rho(Wl.rho_o[i], Wl.rho[i], Wl.drho[i], dt, rho0);
@@ -663,6 +671,7 @@ k_fluid_pairs(FluidState<T> F, const uint32_t *__restrict__ fstart,
               OldState<T> O, T dt, PairOut out, uint32_t *__restrict__ health,
               int32_t *__restrict__ dig_count, long long *__restrict__ dig_sum,
               int32_t *__restrict__ dig_xor, const uint32_t *__restrict__ wid) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int ncells = g.ncells;
     if (i >= n_live(fstart, ncells)) return;
@@ -835,6 +844,7 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock)
 k_bt_density(WallState<T> Wl, int nw, const uint32_t *__restrict__ fstart, Nbr<T> NF, Grid g,
              Phys<T> P) {
+    pdl_enter();
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nw) return;
     const uint32_t key = Wl.key[w];
@@ -887,6 +897,7 @@ k_wall_rows(WallState<T> Wl, int nw, const uint32_t *__restrict__ fstart, Nbr<T>
             Phys<T> P, bool dbc, bool correct, T dt, int32_t *__restrict__ dig_count,
             long long *__restrict__ dig_sum, int32_t *__restrict__ dig_xor,
             const uint32_t *__restrict__ fid, bool digest) {
+    pdl_enter();
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nw) return;
     T drho = Wl.drho[w];
@@ -975,6 +986,7 @@ template <typename T>
 __global__ void __launch_bounds__(kBlock)
 k_mdbc(WallState<T> Wl, int nw, const uint32_t *__restrict__ fstart, Nbr<T> NF, Grid g,
        Phys<T> P) {
+    pdl_enter();
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (warp >= nw) return;
@@ -1126,6 +1138,7 @@ __global__ void k_predict_bin(FluidState<T> F, const uint32_t *__restrict__ fsta
                               typename V2<T>::t *__restrict__ Bv, T *__restrict__ Brho,
                               uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
                               uint32_t *__restrict__ counts, uint32_t *__restrict__ health) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nw) {
         const T r = Wl.rho[i];
@@ -1212,6 +1225,7 @@ __global__ void k_predict_keep(FluidState<T> F, const uint32_t *__restrict__ fst
                                OldState<T> O, float skin, uint32_t *__restrict__ rebuild,
                                uint32_t *__restrict__ health, cudaGraphConditionalHandle cond,
                                int use_cond) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nw) {
         const T r = Wl.rho[i];
@@ -1228,6 +1242,7 @@ __global__ void k_bin_gated(const FluidState<T> X, const uint32_t *__restrict__ 
                             uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
                             uint32_t *__restrict__ counts, uint32_t *__restrict__ health,
                             const uint32_t *__restrict__ gate) {
+    pdl_enter();
     if (gated_off(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_live(fstart, g.ncells)) return;
@@ -1244,6 +1259,7 @@ __global__ void k_copy_back(const FluidState<T> S, const double2 *__restrict__ o
                             const typename V2<T>::t *__restrict__ ov2, const T *__restrict__ orho2,
                             const uint32_t *__restrict__ fstart, int ncells, FluidState<T> D,
                             OldState<T> O, const uint32_t *__restrict__ gate) {
+    pdl_enter();
     if (gated_off(gate)) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= (int)fstart[ncells + 1]) return;
@@ -1311,6 +1327,7 @@ struct Staging {
 template <typename T>
 __global__ void k_export(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
                          WallState<T> Wl, int nw, T rho0, Staging S, int mask) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nw) {
         const uint32_t id = Wl.id[i];
@@ -1353,6 +1370,7 @@ __global__ void k_export(FluidState<T> F, const uint32_t *__restrict__ fstart, i
 // in L2)
 static __global__ void __launch_bounds__(kBlock) k_count_alive(const uint8_t *__restrict__ alive, int n,
                                                               uint32_t *__restrict__ count) {
+    pdl_enter();
     __shared__ uint32_t part[kBlock / 32];
     const uint32_t *__restrict__ a4 = reinterpret_cast<const uint32_t *>(alive);
     const int nw = n >> 2;
@@ -1374,6 +1392,7 @@ static __global__ void __launch_bounds__(kBlock) k_count_alive(const uint8_t *__
 template <typename T>
 __global__ void k_import(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
                          WallState<T> Wl, int nw, T rho0, Staging S, int mask) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nw) {
         const uint32_t id = Wl.id[i];
@@ -1409,6 +1428,7 @@ __global__ void k_import(FluidState<T> F, const uint32_t *__restrict__ fstart, i
 template <typename T>
 __global__ void k_totals(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells, double m,
                          double *__restrict__ out) {
+    pdl_enter();
     __shared__ double sh[4][kBlock / 32];
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     double v0 = 0, v1 = 0, v2 = 0, v3 = 0;

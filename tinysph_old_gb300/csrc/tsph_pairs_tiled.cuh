@@ -261,6 +261,7 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
               const uint32_t *__restrict__ wstart, WallState<float> Wl, Grid g, Phys<float> P,
               TileConst K, OldState<float> O, float dt, PairOut out,
               uint32_t *__restrict__ health) {
+    pdl_enter();
     __shared__ TileSmem<SH> sm;
     const int tid = threadIdx.x;
     const int ncy = g.ncy;
@@ -689,6 +690,7 @@ __device__ __forceinline__ void mdbc_wall(int gid, const WallState<float> &Wl, i
 static __global__ void __launch_bounds__(kBlock)
 k_mdbc_f32(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidState<float> F,
             Grid g, Phys<float> P) {
+    pdl_enter();
     mdbc_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, false, 0.f);
 }
 
@@ -703,6 +705,7 @@ k_mdbc_f32_predict(WallState<float> Wl, int nw, int nbm, const uint32_t *__restr
                 FluidState<float> F, Grid g, Phys<float> P, float dt, FluidState<float> D,
                 OldState<float> O, float skin, uint32_t *__restrict__ rebuild,
                 uint32_t *__restrict__ health, cudaGraphConditionalHandle cond, int use_cond) {
+    pdl_enter();
     if ((int)blockIdx.x < nbm) {
         mdbc_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, true, dt);
         return;

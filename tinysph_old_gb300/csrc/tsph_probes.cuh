@@ -103,6 +103,7 @@ k_water_level(ProbeSrc<T> S, const double *__restrict__ gx, const int *__restric
 template <typename T>
 __global__ void k_point_fields(ProbeSrc<T> S, const double *__restrict__ xy, int npts,
                                double *__restrict__ out) {
+    pdl_enter();
     const int pt = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (pt >= npts) return;
@@ -161,6 +162,7 @@ __global__ void k_point_fields(ProbeSrc<T> S, const double *__restrict__ xy, int
 // largest x of the live fluid with y <= y_max (ordered bits, atomicMax)
 static __global__ void k_water_front(const double2 *__restrict__ fr, const uint32_t *__restrict__ fstart,
                               int ncells, double y_max, unsigned long long *__restrict__ best) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     unsigned long long v = 0ull;
     if (i < (int)fstart[ncells]) {

@@ -27,6 +27,7 @@ template <typename T>
 __global__ void k_inlet_cross(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
                               ZoneDev Z, double dt, uint32_t *__restrict__ list, int cap,
                               uint32_t *__restrict__ count) {
+    pdl_enter();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_live(fstart, ncells)) return;
     if (F.key[f] == (uint32_t)ncells || F.type[f] != (uint8_t)Z.btype) return;
@@ -66,6 +67,7 @@ template <typename T>
 __global__ void k_inlet_append(FluidState<T> F, OldState<T> O, const uint32_t *__restrict__ fstart,
                                int ncells, ZoneDev Z, const uint32_t *__restrict__ list, int k,
                                uint32_t next_id, T rho0, double dt) {
+    pdl_enter();
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= k) return;
     const uint32_t pid = list[2 * e];
@@ -103,6 +105,7 @@ __global__ void k_inlet_append(FluidState<T> F, OldState<T> O, const uint32_t *_
 
 // the appended rows join the live range
 static __global__ void k_grow_live(uint32_t *__restrict__ fstart, int ncells, int k) {
+    pdl_enter();
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         fstart[ncells] += (uint32_t)k;
         fstart[ncells + 1] += (uint32_t)k;
@@ -117,6 +120,7 @@ template <typename T>
 __global__ void k_outlet_mark(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
                               const uint32_t *__restrict__ wid, int nw, ZoneDev Z,
                               uint8_t *__restrict__ live, uint8_t *__restrict__ cand) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nw) {
         live[wid[i]] = 1;
@@ -154,6 +158,7 @@ template <typename T>
 __global__ void k_remove_mark(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
                               const uint32_t *__restrict__ wid, int nw, Box box,
                               uint8_t *__restrict__ live, uint8_t *__restrict__ cand) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nw) {
         live[wid[i]] = 1;
@@ -173,6 +178,7 @@ template <typename T>
 __global__ void k_remove_apply(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
                                const uint8_t *__restrict__ live, const uint8_t *__restrict__ cand,
                                uint32_t *__restrict__ removed, uint32_t *__restrict__ health) {
+    pdl_enter();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_live(fstart, ncells) || F.key[f] == (uint32_t)ncells) return;
     const int id = (int)F.id[f];
@@ -193,6 +199,7 @@ __global__ void k_outlet_apply(FluidState<T> F, const uint32_t *__restrict__ fst
                                ZoneDev Z, const uint8_t *__restrict__ live,
                                const uint8_t *__restrict__ cand, uint32_t *__restrict__ removed,
                                uint32_t *__restrict__ health) {
+    pdl_enter();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_live(fstart, ncells) || F.key[f] == (uint32_t)ncells) return;
     const int id = (int)F.id[f];
