@@ -94,8 +94,17 @@ __device__ __forceinline__ int n_live_ale(const uint32_t *fstart, int ncells) {
     return (int)__ldg(fstart + ncells);
 }
 
+// The leap-frog increments (rate x step, position change v x step) are
+// formed in FP32 and added to the FP64 state with one FP64 add: the rates
+// and velocities are FP32 values (FP32 pair math, ~1e-6 relative), so the
+// FP32 product (6e-8 relative) loses nothing they carry, and GB300 issues
+// FP64 at a small fraction of the FP32 rate.  dtf = dt, hf = dt/2 in FP32.
+__device__ __forceinline__ double add_f(double x, float rate, float step) {
+    return x + (double)(rate * step);
+}
+
 // Integrate_LeapFrog_partOne, src/RALESPH_integration.h:10-36 (in place)
-__global__ void k_ale_lf1(AleFluid F, const uint32_t *__restrict__ fstart, int ncells, double dt,
+__global__ void k_ale_lf1(AleFluid F, const uint32_t *__restrict__ fstart, int ncells, float hf,
                           float rho0) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_live_ale(fstart, ncells)) return;
@@ -104,10 +113,9 @@ __global__ void k_ale_lf1(AleFluid F, const uint32_t *__restrict__ fstart, int n
     F.om_o[i] = om;
     F.omr_o[i] = omr;
     F.omv_o[i] = omv;
-    const double h = dt * 0.5;
-    const double om2 = om + (double)F.dom[i] * h, omr2 = omr + (double)F.domr[i] * h;
+    const double om2 = add_f(om, F.dom[i], hf), omr2 = add_f(omr, F.domr[i], hf);
     const float2 dv = F.domv[i];
-    const double2 omv2 = make_double2(omv.x + (double)dv.x * h, omv.y + (double)dv.y * h);
+    const double2 omv2 = make_double2(add_f(omv.x, dv.x, hf), add_f(omv.y, dv.y, hf));
     F.om[i] = om2;
     F.omr[i] = omr2;
     F.omv[i] = omv2;
@@ -124,8 +132,9 @@ __global__ void k_ale_lf1(AleFluid F, const uint32_t *__restrict__ fstart, int n
 // are not written (the sort derives rho, v from the conserved state; the
 // copies are dead until the next part one).
 template <bool STEP>
-__device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int o, double dt,
-                                       int step, float rho0, float &s_out, float2 &v_out) {
+__device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int o, float dtf,
+                                       float hf, int step, float rho0, float &s_out,
+                                       float2 &v_out) {
     double2 r = F.r[i];
     // the reference's p was computed from the density the fluxes used
     const float s_flux = F.s[i];
@@ -140,19 +149,18 @@ __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int
             D.omr_o[o] = omr0;
             D.omv_o[o] = omv0;
         }
-        const double h = dt * 0.5;
-        om = om0 + (double)F.dom[i] * h;
-        omr = omr0 + (double)F.domr[i] * h;
-        omv = make_double2(omv0.x + (double)dv.x * h, omv0.y + (double)dv.y * h);
+        om = add_f(om0, F.dom[i], hf);
+        omr = add_f(omr0, F.domr[i], hf);
+        omv = make_double2(add_f(omv0.x, dv.x, hf), add_f(omv0.y, dv.y, hf));
         derive(om, omr, omv, rho0, s_out, v_out);
-        r = make_double2(r.x + (double)v_out.x * dt * 0.5, r.y + (double)v_out.y * dt * 0.5);
+        r = make_double2(add_f(r.x, v_out.x, hf), add_f(r.y, v_out.y, hf));
     } else {
         const float2 v0 = F.v[i];
-        r = make_double2(r.x + (double)v0.x * dt, r.y + (double)v0.y * dt);
-        om = F.om_o[i] + (double)F.dom[i] * dt;
-        omr = F.omr_o[i] + (double)F.domr[i] * dt;
+        r = make_double2(add_f(r.x, v0.x, dtf), add_f(r.y, v0.y, dtf));
+        om = add_f(F.om_o[i], F.dom[i], dtf);
+        omr = add_f(F.omr_o[i], F.domr[i], dtf);
         const double2 o2 = F.omv_o[i];
-        omv = make_double2(o2.x + (double)dv.x * dt, o2.y + (double)dv.y * dt);
+        omv = make_double2(add_f(o2.x, dv.x, dtf), add_f(o2.y, dv.y, dtf));
         derive(om, omr, omv, rho0, s_out, v_out);
         if (!STEP) {
             D.om_o[o] = F.om_o[i];
@@ -177,29 +185,29 @@ __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int
 }
 
 // part two in place (per-function entry point)
-__global__ void k_ale_lf2(AleFluid F, const uint32_t *__restrict__ fstart, int ncells, double dt,
-                          int step, float rho0) {
+__global__ void k_ale_lf2(AleFluid F, const uint32_t *__restrict__ fstart, int ncells, float dtf,
+                          float hf, int step, float rho0) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_live_ale(fstart, ncells)) return;
     float sn;
     float2 vn;
-    lf2<false>(F, i, F, i, dt, step, rho0, sn, vn);
+    lf2<false>(F, i, F, i, dtf, hf, step, rho0, sn, vn);
 }
 
 // part two out of place + RemoveParticlesOutOfDomain (src/SPH_btdebug.h:4-31)
 // + cell and histogram slot of the new position
-__global__ void k_ale_lf2_bin(AleFluid F, const uint32_t *__restrict__ fstart, Grid g, double dt,
-                              int step, float rho0, Box box, AleFluid D,
+__global__ void k_ale_lf2_bin(AleFluid F, const uint32_t *__restrict__ fstart, Grid g, float dtf,
+                              float hf, int step, float rho0, BoxBits boxb, AleFluid D,
                               uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
                               uint32_t *__restrict__ counts, uint32_t *__restrict__ health) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_live_ale(fstart, g.ncells)) return;
     float sn;
     float2 v;
-    const double2 rn = lf2<true>(F, i, D, i, dt, step, rho0, sn, v);
+    const double2 rn = lf2<true>(F, i, D, i, dtf, hf, step, rho0, sn, v);
     if (!(v.x == v.x) || !(v.y == v.y) || !(sn == sn)) atomicOr(health, kHealthNan);
     uint32_t k;
-    if (out_of_domain(rn, box)) {
+    if (out_of_domain_bits(rn, boxb)) {
         k = (uint32_t)g.ncells;
         atomicOr(health, kHealthRemoved);
     } else {
@@ -1144,7 +1152,7 @@ class AleEngine {
     }
 
     int lf1(double dt, std::string &err) {
-        k_ale_lf1<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, dt, (float)rho0);
+        k_ale_lf1<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, (float)(dt * 0.5), (float)rho0);
         ACK(cudaGetLastError());
         copies_valid = true;
         return 0;
@@ -1155,7 +1163,8 @@ class AleEngine {
             err = "Integrate_LeapFrog_partTwo (step > 1) needs part one of the same step first";
             return TSPH_ERR_STATE;
         }
-        k_ale_lf2<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, dt, step, (float)rho0);
+        k_ale_lf2<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, (float)dt, (float)(dt * 0.5),
+                                               step, (float)rho0);
         ACK(cudaGetLastError());
         cells = false;
         return 0;
@@ -1169,7 +1178,8 @@ class AleEngine {
             if (stp > 1 && (rc = lf1(dt, err))) return rc;
             if (scheme == TSPH_ALE_MUSCL && (rc = gradient(err))) return rc;
             if ((rc = forces(err))) return rc;
-            k_ale_lf2_bin<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, dt, stp, (float)rho0, box,
+            k_ale_lf2_bin<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, (float)dt, (float)(dt * 0.5),
+                                                       stp, (float)rho0, make_box_bits(box),
                                                        B, keyB, slotB, counts, health);
             if ((rc = sort(B, A, true, err))) return rc;
         }

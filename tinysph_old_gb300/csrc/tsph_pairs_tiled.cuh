@@ -243,18 +243,6 @@ __device__ __forceinline__ uint16_t *scan_below(const float2 *__restrict__ loc, 
     return w;
 }
 
-// RemoveParticlesOutOfDomain's test (src/SPH_btdebug.h:16-19) on the ordered
-// bits of the coordinates against precomputed ordered thresholds: integer
-// compares instead of FP64 ones (GB300 issues FP64 at a small fraction of the
-// FP32 rate).  NaN coordinates compare false, as in FP64.
-__device__ __forceinline__ bool out_of_domain_bits(double2 r, const BoxBits &b) {
-    const long long ox = ordered_bits_fold0(r.x), oy = ordered_bits_fold0(r.y);
-    const long long ax = __double_as_longlong(r.x) & 0x7fffffffffffffffLL;
-    const long long ay = __double_as_longlong(r.y) & 0x7fffffffffffffffLL;
-    const bool nan = ax > 0x7ff0000000000000LL || ay > 0x7ff0000000000000LL;
-    return !nan && (oy < b.y_lo || oy > b.y_hi || ox < b.x_lo || ox > b.x_hi);
-}
-
 template <int MODE, bool STORED_P, class SH>
 __global__ void __launch_bounds__(kTileT, 8)
 k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
