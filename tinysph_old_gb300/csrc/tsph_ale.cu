@@ -659,6 +659,11 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
     if (tid < 9) sm.off[tid] = make_float2((float)(1 - tid / 3) * g.khf, (float)(1 - tid % 3) * g.khf);
     const uint32_t h2bits = __float_as_uint(K.four_h2);
     const float reach = 2.f * K.h * 1.0001f;
+    // the CTA's last target: when it lies in the first window's column and
+    // rows, that window is the whole CTA (no further lookups for its end)
+    const uint32_t klast = __ldg(F.key + t1 - 1);
+    const int cxl = (int)(klast / (uint32_t)ncy);
+    const int cyll = (int)klast - cxl * ncy;
     int cur = t0;
     int rows = kAleRows;
     while (cur < t1) {
@@ -666,10 +671,19 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
         const int cx = (int)(kc / (uint32_t)ncy);
         const int cy0 = (int)kc - cx * ncy;
         const int rowlim = min(cy0 + rows, ncy);
-        const int we = min(t1, (int)__ldg(fstart + cx * ncy + rowlim));
-        const int cyl = (int)__ldg(F.key + we - 1) - cx * ncy;
+        int we, cyl;
+        if (cxl == cx && cyll < rowlim) {
+            we = t1;
+            cyl = cyll;
+        } else {
+            we = min(t1, (int)__ldg(fstart + cx * ncy + rowlim));
+            cyl = (int)__ldg(F.key + we - 1) - cx * ncy;
+        }
         const int rlo = max(cy0 - 1, 0), rhi = min(cyl + 1, ncy - 1);
         const int nr = rhi - rlo + 1;
+        const int i = cur + tid;
+        const bool active = i < we;
+        const uint32_t ki = active ? __ldg(F.key + i) : 0u;  // fetched with the offsets
         __syncthreads();
         for (int e = tid; e < 3 * (nr + 1); e += kAleT) {
             const int dxi = e / (nr + 1), q = e - dxi * (nr + 1);
@@ -700,33 +714,53 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
             rows = (rows + 1) >> 1;
             continue;
         }
-        const int i = cur + tid;
-        const bool active = i < we;
         AleAcc acc = {0.f, 0.f, 0.f, 0.f, false};
         bool done = false;
         float2 va = make_float2(0.f, 0.f);
         float sa = 0.f;
         if (tot <= kAleCap) {
+            // slot e of the block: segments walls 0, fluid 0, walls 1, ...;
+            // all of a thread's loads go out before its first store
+            constexpr int kStage = (kAleCap + kAleT - 1) / kAleT;
+            float2 st_l[kStage], st_v[kStage];
+            float st_s[kStage];
+            double st_o[kStage];
+            bool st_w[kStage];
 #pragma unroll
-            for (int d = 0; d < 3; d++) {
-                const int nwd = sm.woff[d][nr] - w0[d];
-                for (int k = tid; k < nwd; k += kAleT) {
-                    const int j = w0[d] + k;
-                    const float2 n = __ldg(Wl.n + j);
-                    sm.loc[wb[d] + k] = __ldg(Wl.loc + j);
-                    sm.q[wb[d] + k] = make_float4(-n.x, -n.y, __ldg(Wl.s + j), -1.f);
+            for (int u = 0; u < kStage; u++) {
+                const int e = tid + u * kAleT;
+                int j = e + w0[0];
+                bool wall = true;
+                if (e >= fb[0]) { j = e - fb[0] + f0[0]; wall = false; }
+                if (e >= wb[1]) { j = e - wb[1] + w0[1]; wall = true; }
+                if (e >= fb[1]) { j = e - fb[1] + f0[1]; wall = false; }
+                if (e >= wb[2]) { j = e - wb[2] + w0[2]; wall = true; }
+                if (e >= fb[2]) { j = e - fb[2] + f0[2]; wall = false; }
+                st_w[u] = wall;
+                st_l[u] = make_float2(0.f, 0.f);
+                st_v[u] = make_float2(0.f, 0.f);
+                st_s[u] = 0.f;
+                st_o[u] = 0.0;
+                if (e < tot) {
+                    st_l[u] = __ldg((wall ? Wl.loc : F.loc) + j);
+                    st_v[u] = __ldg((wall ? Wl.n : F.v) + j);
+                    st_s[u] = __ldg((wall ? Wl.s : F.s) + j);
+                    if (!wall) st_o[u] = __ldg(F.om + j);
                 }
-                const int nfd = sm.foff[d][nr] - f0[d];
-                for (int k = tid; k < nfd; k += kAleT) {
-                    const int j = f0[d] + k;
-                    const float2 v = __ldg(F.v + j);
-                    sm.loc[fb[d] + k] = __ldg(F.loc + j);
-                    sm.q[fb[d] + k] = make_float4(v.x, v.y, __ldg(F.s + j), (float)__ldg(F.om + j));
+            }
+#pragma unroll
+            for (int u = 0; u < kStage; u++) {
+                const int e = tid + u * kAleT;
+                if (e < tot) {
+                    sm.loc[e] = st_l[u];
+                    // walls: {-n, s, -1}; fluid: {v, s, omega}
+                    sm.q[e] = st_w[u] ? make_float4(-st_v[u].x, -st_v[u].y, st_s[u], -1.f)
+                                      : make_float4(st_v[u].x, st_v[u].y, st_s[u], (float)st_o[u]);
                 }
             }
             __syncthreads();
             if (active) {
-                const int cy = (int)__ldg(F.key + i) - cx * ncy;
+                const int cy = (int)ki - cx * ncy;
                 const int own = fb[1] + (i - f0[1]);
                 const float2 la = sm.loc[own];
                 const float4 qa = sm.q[own];
@@ -812,7 +846,7 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
         }
         if (active && !done) {
             // window too dense for shared memory, or list overflow: from global memory
-            const int cy = (int)__ldg(F.key + i) - cx * ncy;
+            const int cy = (int)ki - cx * ncy;
             const float2 la = __ldg(F.loc + i);
             va = __ldg(F.v + i);
             sa = __ldg(F.s + i);
@@ -851,7 +885,7 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
             }
         }
         if (active) {
-            const int cy = (int)__ldg(F.key + i) - cx * ncy;
+            const int cy = (int)ki - cx * ncy;
             bool zero = !acc.any;
             if (zero) {
                 // gamma_sum is not reset between the particles of a cell
