@@ -549,7 +549,7 @@ struct AleTile {
     float4 q[kAleCap];  // fluid {vx, vy, rho - rho0, omega}; wall {-nx, -ny, rho - rho0, -1}
     int foff[3][kAleRows + 3];
     int woff[3][kAleRows + 3];
-    float2 off[9];
+    float offy[4];  // y offset of a neighbour row: below, own, above (list code 0, 1, 2)
     uint16_t list[kAleList * kAleT];
 };
 
@@ -627,22 +627,27 @@ __device__ __forceinline__ void ale_pair(float dx, float dy, float2 va, float sa
 
 // the bounded append of a cell that could overflow the list (one copy, out
 // of line: the unrolled neighbour loop calls it rarely)
-static __device__ __noinline__ int append_bounded_kAleT(const float2 *loc, uint16_t *lst, int cnt,
-                                                   int j0, int j1, int code, float bx, float by,
-                                                   uint32_t h2bits, bool &overflow) {
+// one range appended one candidate at a time, at most up to the list's end
+// (the support test with the particle itself and coincident particles
+// excluded, 0 < r^2 <= 4h^2); a candidate past the end sets `overflow`
+static __device__ __forceinline__ uint16_t *append_bounded_ale(const float2 *loc, uint16_t *lst,
+                                                            uint16_t *w, int j0, int j1,
+                                                            uint32_t code, float bx, float by,
+                                                            float h2, bool &overflow) {
+    uint16_t *const wend = lst + kAleList * kAleT;
     for (int j = j0; j < j1; j++) {
         const float2 lb = loc[j];
         const float dx = bx - lb.x, dy = by - lb.y;
-        if (((uint32_t)(__float_as_uint(fmaf(dx, dx, dy * dy)) - 1u) < h2bits ? 1u : 0u)) {
-            if (cnt < kAleList) {
-                lst[cnt * kAleT] = (uint16_t)(((uint32_t)j << 4) | (uint32_t)code);
-                cnt++;
+        if (in_support(fmaf(dx, dx, dy * dy), __float_as_uint(h2))) {
+            if (w < wend) {
+                *w = (uint16_t)(((uint32_t)j << 2) | code);
+                w += kAleT;
             } else {
                 overflow = true;
             }
         }
     }
-    return cnt;
+    return w;
 }
 
 template <int SCHEME>
@@ -656,8 +661,8 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
     const int t0 = blockIdx.x * kAleT;
     if (t0 >= nl) return;
     const int t1 = min(t0 + kAleT, nl);
-    if (tid < 9) sm.off[tid] = make_float2((float)(1 - tid / 3) * g.khf, (float)(1 - tid % 3) * g.khf);
-    const uint32_t h2bits = __float_as_uint(K.four_h2);
+    if (tid < 4) sm.offy[tid] = tid < 3 ? (float)(1 - tid) * g.khf : 0.f;
+    const float khf = g.khf;
     const float reach = 2.f * K.h * 1.0001f;
     // the CTA's last target: when it lies in the first window's column and
     // rows, that window is the whole CTA (no further lookups for its end)
@@ -720,7 +725,8 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
         float sa = 0.f;
         if (tot <= kAleCap) {
             // slot e of the block: segments walls 0, fluid 0, walls 1, ...;
-            // all of a thread's loads go out before its first store
+            // all of a thread's loads go out before its first store; x is
+            // staged relative to the centre column, y to the particle's cell
             constexpr int kStage = (kAleCap + kAleT - 1) / kAleT;
             float2 st_l[kStage], st_v[kStage];
             float st_s[kStage];
@@ -731,10 +737,11 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                 const int e = tid + u * kAleT;
                 int j = e + w0[0];
                 bool wall = true;
+                float xs = -khf;  // x of the cell's origin relative to the centre column's
                 if (e >= fb[0]) { j = e - fb[0] + f0[0]; wall = false; }
-                if (e >= wb[1]) { j = e - wb[1] + w0[1]; wall = true; }
+                if (e >= wb[1]) { j = e - wb[1] + w0[1]; wall = true; xs = 0.f; }
                 if (e >= fb[1]) { j = e - fb[1] + f0[1]; wall = false; }
-                if (e >= wb[2]) { j = e - wb[2] + w0[2]; wall = true; }
+                if (e >= wb[2]) { j = e - wb[2] + w0[2]; wall = true; xs = khf; }
                 if (e >= fb[2]) { j = e - fb[2] + f0[2]; wall = false; }
                 st_w[u] = wall;
                 st_l[u] = make_float2(0.f, 0.f);
@@ -743,6 +750,7 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                 st_o[u] = 0.0;
                 if (e < tot) {
                     st_l[u] = __ldg((wall ? Wl.loc : F.loc) + j);
+                    st_l[u].x += xs;
                     st_v[u] = __ldg((wall ? Wl.n : F.v) + j);
                     st_s[u] = __ldg((wall ? Wl.s : F.s) + j);
                     if (!wall) st_o[u] = __ldg(F.om + j);
@@ -767,77 +775,58 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                 va = make_float2(qa.x, qa.y);
                 sa = qa.z;
                 const float rhoa = K.rho0 + sa;
-                int cnt = 0;
+                // in-support neighbours into the list (entry: staged index << 2
+                // | row code); per column the rows below, own and above are
+                // staged ranges [R0, R1), [R1, R2), [R2, R3).  A range that
+                // could overflow the list is appended one at a time, bounded
+                // (a target with more than kAleList neighbours takes the
+                // global-memory path)
                 bool overflow = false;
-                uint16_t *lst = sm.list + tid;
+                uint16_t *const lst = sm.list + tid;
+                uint16_t *const wend = lst + kAleList * kAleT;
+                uint16_t *w = lst;
+                const float by_b = la.y + khf, by_a = la.y - khf;
+                const int q = cy - rlo;
+                const bool hb = cy >= 1, ha = cy + 1 < ncy;
 #pragma unroll
-                for (int dxi = 0; dxi < 3; dxi++) {
-                    const int col = cx + dxi - 1;
+                for (int d = 0; d < 3; d++) {
+                    const int col = cx + d - 1;
                     if (col < 0 || col >= g.ncx) continue;
 #pragma unroll
-                    for (int dyi = 0; dyi < 3; dyi++) {
-                        const int row = cy + dyi - 1;
-                        if (row < 0 || row >= ncy) continue;
-                        const int q = row - rlo;
-                        const int code = dxi * 3 + dyi;
-                        const float bx = la.x + sm.off[code].x, by = la.y + sm.off[code].y;
-#pragma unroll
-                        for (int kind = 0; kind < 2; kind++) {
-                            if (kind == 0 && totw == 0) continue;
-                            const int j0 = kind == 0 ? wb[dxi] + sm.woff[dxi][q] - w0[dxi]
-                                                     : fb[dxi] + sm.foff[dxi][q] - f0[dxi];
-                            const int j1 = kind == 0 ? wb[dxi] + sm.woff[dxi][q + 1] - w0[dxi]
-                                                     : fb[dxi] + sm.foff[dxi][q + 1] - f0[dxi];
-                            if (cnt + (j1 - j0) > kAleList) {
-                                // the cell could overflow the list: append one
-                                // at a time, bounded (a target with more than
-                                // kAleList neighbours takes the global-memory path)
-                                cnt = append_bounded_kAleT(sm.loc, lst, cnt, j0, j1, code, bx, by, h2bits,
-                                                         overflow);
-                                continue;
-                            }
-                            uint16_t *w = lst + cnt * kAleT;
-                            if (dyi == 1 || kind == 0) {
-                                uint32_t ent = ((uint32_t)j0 << 4) | (uint32_t)code;
-                                for (int j = j0; j < j1; j++, ent += 16u) {
-                                    const float2 lb = sm.loc[j];
-                                    const float dx = bx - lb.x, dy = by - lb.y;
-                                    const uint32_t in = (uint32_t)(__float_as_uint(fmaf(dx, dx, dy * dy)) - 1u) < h2bits ? 1u : 0u;
-                                    *w = (uint16_t)ent;
-                                    w += in * kAleT;
-                                }
-                            } else if (dyi == 2) {
-                                uint32_t ent = ((uint32_t)j0 << 4) | (uint32_t)code;
-                                for (int j = j0; j < j1; j++, ent += 16u) {
-                                    const float2 lb = sm.loc[j];
-                                    const float dx = bx - lb.x, dy = by - lb.y;
-                                    if (dy < -reach) break;
-                                    const uint32_t in = (uint32_t)(__float_as_uint(fmaf(dx, dx, dy * dy)) - 1u) < h2bits ? 1u : 0u;
-                                    *w = (uint16_t)ent;
-                                    w += in * kAleT;
-                                }
-                            } else {
-                                uint32_t ent = ((uint32_t)(j1 - 1) << 4) | (uint32_t)code;
-                                for (int j = j1 - 1; j >= j0; j--, ent -= 16u) {
-                                    const float2 lb = sm.loc[j];
-                                    const float dx = bx - lb.x, dy = by - lb.y;
-                                    if (dy > reach) break;
-                                    const uint32_t in = (uint32_t)(__float_as_uint(fmaf(dx, dx, dy * dy)) - 1u) < h2bits ? 1u : 0u;
-                                    *w = (uint16_t)ent;
-                                    w += in * kAleT;
-                                }
-                            }
-                            cnt = (int)((w - lst) / kAleT);
-                        }
+                    for (int kind = 0; kind < 2; kind++) {
+                        if (kind == 0 && totw == 0) continue;  // block-uniform: no walls here
+                        const int *offs = kind == 0 ? sm.woff[d] : sm.foff[d];
+                        const int base = kind == 0 ? wb[d] - w0[d] : fb[d] - f0[d];
+                        const int R1 = base + offs[q], R2 = base + offs[q + 1];
+                        const int R0 = hb ? base + offs[q - 1] : R1;
+                        const int R3 = ha ? base + offs[q + 2] : R2;
+                        if (wend - w < (R2 - R1) * kAleT)
+                            w = append_bounded_ale(sm.loc, lst, w, R1, R2, 1u, la.x, la.y,
+                                                   K.four_h2, overflow);
+                        else if (d == 1 && kind == 1)
+                            w = scan_own<kAleT, true>(sm.loc, R1, R2, la.x, la.y, K.four_h2, w);
+                        else
+                            w = scan_own<kAleT, false>(sm.loc, R1, R2, la.x, la.y, K.four_h2, w);
+                        if (wend - w < (R3 - R2) * kAleT)
+                            w = append_bounded_ale(sm.loc, lst, w, R2, R3, 2u, la.x, by_a,
+                                                   K.four_h2, overflow);
+                        else
+                            w = scan_above<kAleT>(sm.loc, R2, R3, la.x, by_a, K.four_h2, reach, w);
+                        if (wend - w < (R1 - R0) * kAleT)
+                            w = append_bounded_ale(sm.loc, lst, w, R0, R1, 0u, la.x, by_b,
+                                                   K.four_h2, overflow);
+                        else
+                            w = scan_below<kAleT>(sm.loc, R0, R1, la.x, by_b, K.four_h2, reach, w);
                     }
                 }
+                const int cnt = (int)((w - lst) / kAleT);
                 if (!overflow) {
                     for (int k = 0; k < cnt; k++) {
                         const uint32_t e = lst[k * kAleT];
-                        const int j = (int)(e >> 4);
-                        const float2 o = sm.off[e & 15u];
+                        const int j = (int)(e >> 2);
+                        const float oy = sm.offy[e & 3u];
                         const float2 lb = sm.loc[j];
-                        ale_pair<SCHEME>((la.x + o.x) - lb.x, (la.y + o.y) - lb.y, va, sa, rhoa, sm.q[j], K,
+                        ale_pair<SCHEME>(la.x - lb.x, (la.y + oy) - lb.y, va, sa, rhoa, sm.q[j], K,
                                  acc);
                     }
                     done = true;

@@ -575,6 +575,107 @@ inline BoxBits make_box_bits(const Box &b) {
                    ordered_bits_fold0(b.y0 - 0.01), ordered_bits_fold0(b.ym + 0.01)};
 }
 
+// in-support test: 0 < r2 <= (2h)^2 as one unsigned compare of the bits
+__device__ __forceinline__ uint32_t in_support(float r2, uint32_t four_h2_bits) {
+    return (uint32_t)(__float_as_uint(r2) - 1u) < four_h2_bits ? 1u : 0u;
+}
+
+// Phase-1 scans of one staged row range (lists of the tiled pair kernels,
+// entries STRIDE apart): every in-support candidate
+// (r^2 <= 4h^2) appends its entry (staged index << 2 | row code).  The entry
+// is written unconditionally and kept by advancing the list pointer.  Only
+// the particle's own cell can hold a coincident particle or the particle
+// itself; there (EXCL) the test is 0 < r^2 <= 4h^2, as one unsigned compare
+// of the bits, elsewhere a plain float compare.  Rows are sorted by y, so
+// the row above is walked upwards and the row below downwards until |dy|
+// passes `reach`, two candidates per iteration (the test of the second ends
+// the walk; a candidate beyond the reach fails the support test anyway).
+template <bool EXCL> __device__ __forceinline__ bool support_test(float r2, float h2) {
+    if constexpr (EXCL) return in_support(r2, __float_as_uint(h2)) != 0u;
+    else return r2 <= h2;
+}
+
+template <int STRIDE, bool EXCL>
+__device__ __forceinline__ uint16_t *scan_own(const float2 *__restrict__ loc, int j0, int j1,
+                                              float bx, float by, float h2, uint16_t *w) {
+    uint32_t ent = ((uint32_t)j0 << 2) | 1u;
+    int j = j0;
+    for (; j + 1 < j1; j += 2, ent += 8u) {
+        const float2 l0 = loc[j], l1 = loc[j + 1];
+        const float dx0 = bx - l0.x, dy0 = by - l0.y;
+        const float dx1 = bx - l1.x, dy1 = by - l1.y;
+        const bool in0 = support_test<EXCL>(fmaf(dx0, dx0, dy0 * dy0), h2);
+        const bool in1 = support_test<EXCL>(fmaf(dx1, dx1, dy1 * dy1), h2);
+        *w = (uint16_t)ent;
+        w += in0 ? STRIDE : 0;
+        *w = (uint16_t)(ent + 4u);
+        w += in1 ? STRIDE : 0;
+    }
+    if (j < j1) {
+        const float2 l = loc[j];
+        const float dx = bx - l.x, dy = by - l.y;
+        *w = (uint16_t)ent;
+        w += support_test<EXCL>(fmaf(dx, dx, dy * dy), h2) ? STRIDE : 0;
+    }
+    return w;
+}
+
+template <int STRIDE>
+__device__ __forceinline__ uint16_t *scan_above(const float2 *__restrict__ loc, int j0, int j1,
+                                                float bx, float by, float h2, float reach,
+                                                uint16_t *w) {
+    uint32_t ent = ((uint32_t)j0 << 2) | 2u;
+    int j = j0;
+    bool go = true;
+    for (; go && j + 1 < j1; j += 2, ent += 8u) {
+        const float2 l0 = loc[j], l1 = loc[j + 1];
+        const float dx0 = bx - l0.x, dy0 = by - l0.y;
+        const float dx1 = bx - l1.x, dy1 = by - l1.y;
+        const bool in0 = fmaf(dx0, dx0, dy0 * dy0) <= h2;
+        const bool in1 = fmaf(dx1, dx1, dy1 * dy1) <= h2;
+        *w = (uint16_t)ent;
+        w += in0 ? STRIDE : 0;
+        *w = (uint16_t)(ent + 4u);
+        w += in1 ? STRIDE : 0;
+        go = dy1 >= -reach;
+    }
+    if (go && j < j1) {
+        const float2 l = loc[j];
+        const float dx = bx - l.x, dy = by - l.y;
+        *w = (uint16_t)ent;
+        w += fmaf(dx, dx, dy * dy) <= h2 ? STRIDE : 0;
+    }
+    return w;
+}
+
+template <int STRIDE>
+__device__ __forceinline__ uint16_t *scan_below(const float2 *__restrict__ loc, int j0, int j1,
+                                                float bx, float by, float h2, float reach,
+                                                uint16_t *w) {
+    uint32_t ent = ((uint32_t)(j1 - 1) << 2);
+    int j = j1 - 1;
+    bool go = true;
+    for (; go && j - 1 >= j0; j -= 2, ent -= 8u) {
+        const float2 l0 = loc[j], l1 = loc[j - 1];
+        const float dx0 = bx - l0.x, dy0 = by - l0.y;
+        const float dx1 = bx - l1.x, dy1 = by - l1.y;
+        const bool in0 = fmaf(dx0, dx0, dy0 * dy0) <= h2;
+        const bool in1 = fmaf(dx1, dx1, dy1 * dy1) <= h2;
+        *w = (uint16_t)ent;
+        w += in0 ? STRIDE : 0;
+        *w = (uint16_t)(ent - 4u);
+        w += in1 ? STRIDE : 0;
+        go = dy1 <= reach;
+    }
+    if (go && j >= j0) {
+        const float2 l = loc[j];
+        const float dx = bx - l.x, dy = by - l.y;
+        *w = (uint16_t)ent;
+        w += fmaf(dx, dx, dy * dy) <= h2 ? STRIDE : 0;
+    }
+    return w;
+}
+
 // RemoveParticlesOutOfDomain's test (src/SPH_btdebug.h:16-19) on the ordered
 // bits of the coordinates against precomputed ordered thresholds: integer
 // compares instead of FP64 ones (GB300 issues FP64 at a small fraction of the
