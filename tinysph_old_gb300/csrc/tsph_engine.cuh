@@ -998,20 +998,10 @@ template <typename T> class Engine final : public EngineBase {
         if ((rc = sort_finish(F_.r, F_.v, F_.rho, F_.id, F_.a, F_.drho, F_.p, Fs_, O_.r, O_.v,
                               O_.rho, OldState<T>{Br_, Bv_, Brho_}, err, nullptr, F_.type)))
             return rc;
-        const size_t n = (size_t)nf_;
-        if (F_.type) TSPH_CK(cudaMemcpyAsync(F_.type, Fs_.type, n, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(F_.r, Fs_.r, 16 * n, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(F_.v, Fs_.v, sizeof(T2) * n, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(F_.a, Fs_.a, sizeof(T2) * n, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(F_.rho, Fs_.rho, sizeof(T) * n, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(F_.drho, Fs_.drho, sizeof(T) * n, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(F_.p, Fs_.p, sizeof(T) * n, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(F_.id, Fs_.id, 4 * n, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(F_.key, Fs_.key, 4 * n, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(F_.loc, Fs_.loc, 8 * n, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(O_.r, Br_, 16 * n, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(O_.v, Bv_, sizeof(T2) * n, cudaMemcpyDeviceToDevice, st_));
-        TSPH_CK(cudaMemcpyAsync(O_.rho, Brho_, sizeof(T) * n, cudaMemcpyDeviceToDevice, st_));
+        if ((rc = launch(CAT_SORT, k_copy_state<T>, blocks_for(nf_), kBlock, err, F_,
+                         (const FluidState<T>)Fs_, O_, OldState<T>{Br_, Bv_, Brho_},
+                         (const uint32_t *)fstart_, ncells_)))
+            return rc;
         cells_ = true;
         exported_ = false;
         return collect_profile(err);
@@ -1199,8 +1189,35 @@ template <typename T> class Engine final : public EngineBase {
     // after k_export: whether every particle is alive (counted on the device),
     // and the alive map on the host only when some are not
     uint32_t *alive_count_ = nullptr;
+    // Without buffer zones the index space is fixed and walls are never
+    // removed, so every index is live exactly when the live fluid count plus
+    // the walls equals the index count: one 4-byte read.  The count is that of
+    // the last binning, so it is used only while the cells are fresh (a
+    // removal marks particles dead and leaves the cells stale until the next
+    // binning); otherwise dense stays false and the alive map decides.
+    int dense_by_count(bool &dense, std::string &err) {
+        (void)err;
+        dense = false;
+        if (zones_on_ || !cells_) return 0;
+        uint32_t nl = 0;
+        TSPH_CK(cudaMemcpyAsync(&nl, fstart_ + ncells_, 4, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        dense = (long long)nl + nw_ == (long long)ntot_;
+        return 0;
+    }
+
+    // after k_export wrote S_.alive: whether every index is live, else the map
     int alive_map(std::vector<uint8_t> &alive, bool &dense, std::string &err) {
         int rc;
+        if (!zones_on_ && cells_) {
+            if ((rc = dense_by_count(dense, err))) return rc;
+            if (!dense) {
+                alive.resize(ntot_);
+                TSPH_CK(cudaMemcpyAsync(alive.data(), S_.alive, ntot_, cudaMemcpyDeviceToHost, st_));
+                TSPH_CK(cudaStreamSynchronize(st_));
+            }
+            return 0;
+        }
         if (!alive_count_ && (rc = alloc(&alive_count_, 1, err))) return rc;
         TSPH_CK(cudaMemsetAsync(alive_count_, 0, 4, st_));
         if ((rc = launch(CAT_OTHER, k_count_alive,
@@ -1269,14 +1286,19 @@ template <typename T> class Engine final : public EngineBase {
 
     int upload(int mask, const double *r, const double *v, const double *a, const double *rho,
                const double *drho, const double *p, std::string &err) override {
-        // alive map from the device
-        TSPH_CK(cudaMemsetAsync(S_.alive, 0, ntot_, st_));
-        int rc = launch(CAT_OTHER, k_export<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
-                        (const uint32_t *)fstart_, ncells_, W_, nw_, P_.rho0, S_, 0);
-        if (rc) return rc;
+        // every index live (the usual case) needs no alive map
+        int rc;
         std::vector<uint8_t> alive;
         bool dense = false;
-        if ((rc = alive_map(alive, dense, err))) return rc;
+        if ((rc = dense_by_count(dense, err))) return rc;
+        if (!dense) {
+            // alive map from the device
+            TSPH_CK(cudaMemsetAsync(S_.alive, 0, ntot_, st_));
+            rc = launch(CAT_OTHER, k_export<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                        (const uint32_t *)fstart_, ncells_, W_, nw_, P_.rho0, S_, 0);
+            if (rc) return rc;
+            if ((rc = alive_map(alive, dense, err))) return rc;
+        }
         std::vector<double> tmp;
         auto put = [&](int bit, void *dst, const double *src, int width) -> int {
             if (!(mask & bit) || !src) return 0;

@@ -1332,6 +1332,31 @@ __device__ __forceinline__ void predict_keep_fluid(int f, const FluidState<T> &F
         atomicOr(health, kHealthNan);
 }
 
+// the copy-back of a re-binning: every field of the sorted state S (and the
+// old state carried in B) into the current buffers D and O, one launch over
+// the rows in use (live and removed, fstart[ncells + 1]) instead of one copy
+// per array over the whole capacity
+template <typename T>
+__global__ void k_copy_state(FluidState<T> D, FluidState<T> S, OldState<T> O, OldState<T> B,
+                             const uint32_t *__restrict__ fstart, int ncells) {
+    pdl_enter();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int)__ldg(fstart + ncells + 1)) return;
+    D.r[i] = S.r[i];
+    D.v[i] = S.v[i];
+    D.a[i] = S.a[i];
+    D.rho[i] = S.rho[i];
+    D.drho[i] = S.drho[i];
+    D.p[i] = S.p[i];
+    D.id[i] = S.id[i];
+    D.key[i] = S.key[i];
+    D.loc[i] = S.loc[i];
+    if (D.type) D.type[i] = S.type[i];
+    O.r[i] = B.r[i];
+    O.v[i] = B.v[i];
+    O.rho[i] = B.rho[i];
+}
+
 template <typename T>
 __global__ void k_predict_keep(FluidState<T> F, const uint32_t *__restrict__ fstart,
                                WallState<T> Wl, int nw, Grid g, T dt, FluidState<T> D,
