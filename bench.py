@@ -265,16 +265,20 @@ def run_ale(args, rank, world, local):
     flux_us = statistics.median(fl_us)
     peak, peak_kind = measured_peaks()
     achieved = ALE_FLUX_BYTES_PER_PARTICLE * nfluid / (flux_us * 1e-6) / 1e9
-    # e2e: host state in and out through the C ABI every step
-    hr = np.empty((n, 2)); hv = np.empty((n, 2)); hrho = np.empty(n)
-    st = s.download(sph.ALE_F_R | sph.ALE_F_V | sph.ALE_F_RHO)
+    # e2e: host state in and out through the C ABI every step, pinned buffers
+    hr = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+    hv = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+    hrho = torch.empty((n,), dtype=torch.float64, pin_memory=True)
+    mask = sph.ALE_F_R | sph.ALE_F_V | sph.ALE_F_RHO
+    ptrs = dict(r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+    s.download_ptrs(mask, **ptrs)
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        s.upload(r=st["r"], v=st["v"], rho=st["rho"])
+        s.upload_ptrs(mask, **ptrs)
         s.particle_to_cell()
         s.step(dt, step, 1)
         step += 1
-        st = s.download(sph.ALE_F_R | sph.ALE_F_V | sph.ALE_F_RHO)
+        s.download_ptrs(mask, **ptrs)
     e2e_value = world * n * args.e2e_steps / (time.perf_counter() - t0)
     xfer = n * 40
     cpu = None
@@ -308,7 +312,7 @@ def run_ale(args, rank, world, local):
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": xfer,
                     "d2h_bytes_per_step": xfer,
                     "path": "tsph_ale_upload(r,v,rho) + tsph_ale_particle_to_cell + "
-                            "tsph_ale_step(1) + tsph_ale_download(r,v,rho), pageable buffers"},
+                            "tsph_ale_step(1) + tsph_ale_download(r,v,rho), pinned host buffers"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": None, "kernel": "k_ale_flux",
                          "bytes_per_unit": ALE_FLUX_BYTES_PER_PARTICLE, "unit_count": nfluid,

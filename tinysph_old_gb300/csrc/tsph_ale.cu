@@ -915,6 +915,99 @@ inline int nblk(long long n, int b = kBlock) { return (int)std::max<long long>(1
 }  // namespace
 
 // host-side ALE system: particles, grid tables, device buffers
+// ---------------------------------------------------------- host staging
+// Download / upload through staging arrays indexed by particle (the
+// reference's order): the device writes (reads) each field at its particle's
+// index, so the host copies whole arrays, with no host-side sort.
+struct AleStage {
+    double *r = nullptr, *v = nullptr, *rho = nullptr, *p = nullptr, *om = nullptr,
+           *omr = nullptr, *omv = nullptr, *dom = nullptr, *domr = nullptr, *domv = nullptr,
+           *grad = nullptr;
+    int32_t *type = nullptr;
+    uint8_t *alive = nullptr;
+};
+
+// every live particle (walls, then live fluid rows) writes the requested
+// fields at its index and marks itself alive; values as the reference holds
+// them (walls: v = 0, omega = dp^2, omega rho = rho dp^2, rates and gradients
+// 0; p the equation of state of the density the last fluxes used)
+__global__ void k_ale_export(AleFluid F, const uint32_t *__restrict__ fstart, int ncells,
+                             AleWalls Wl, int nw, AleStage S, double rho0, double dp2,
+                             double b_eos) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool wall = i < nw;
+    const int j = wall ? i : i - nw;
+    if (!wall && j >= n_live_ale(fstart, ncells)) return;
+    const uint32_t id = wall ? Wl.id[j] : F.id[j];
+    const double rh = rho0 + (double)(wall ? Wl.s[j] : F.s[j]);
+    if (S.r) {
+        const double2 x = wall ? Wl.r[j] : F.r[j];
+        S.r[2 * id] = x.x;
+        S.r[2 * id + 1] = x.y;
+    }
+    if (S.v) {
+        const float2 u = wall ? make_float2(0.f, 0.f) : F.v[j];
+        S.v[2 * id] = (double)u.x;
+        S.v[2 * id + 1] = (double)u.y;
+    }
+    if (S.rho) S.rho[id] = rh;
+    if (S.p) {
+        const double x = (wall ? rh : rho0 + (double)F.ps[j]) / rho0;
+        S.p[id] = b_eos * (pow(x, 7.) - 1);
+    }
+    if (S.om) S.om[id] = wall ? dp2 : F.om[j];
+    if (S.omr) S.omr[id] = wall ? rh * dp2 : F.omr[j];
+    if (S.omv) {
+        const double2 q = wall ? make_double2(0., 0.) : F.omv[j];
+        S.omv[2 * id] = q.x;
+        S.omv[2 * id + 1] = q.y;
+    }
+    if (S.dom) S.dom[id] = wall ? 0. : (double)F.dom[j];
+    if (S.domr) S.domr[id] = wall ? 0. : (double)F.domr[j];
+    if (S.domv) {
+        const float2 q = wall ? make_float2(0.f, 0.f) : F.domv[j];
+        S.domv[2 * id] = (double)q.x;
+        S.domv[2 * id + 1] = (double)q.y;
+    }
+    if (S.grad)
+        for (int q = 0; q < 12; q++) S.grad[12 * (size_t)id + q] = wall ? 0. : (double)F.grad[12 * (size_t)j + q];
+    if (S.type) S.type[id] = wall ? 1 : 0;
+    S.alive[id] = 1;
+}
+
+// new volume, density, velocity, position of every live fluid row from the
+// staged host arrays (the reference's order), with the conserved quantities
+// following: omega first (same rho = omega rho / omega, same v = omega v /
+// (rho omega)), then rho, v, r
+__global__ void k_ale_import(AleFluid F, const uint32_t *__restrict__ fstart, int ncells,
+                             AleStage S, double rho0) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n_live_ale(fstart, ncells)) return;
+    const uint32_t i = F.id[j];
+    double om = F.om[j], omr = F.omr[j];
+    double2 omv = F.omv[j];
+    if (S.om) {
+        const double f = S.om[i] / om;
+        om = S.om[i];
+        omr *= f;
+        omv = make_double2(omv.x * f, omv.y * f);
+    }
+    if (S.rho) {
+        omr = S.rho[i] * om;
+        const float sv = (float)(S.rho[i] - rho0);
+        F.s[j] = sv;
+        F.ps[j] = sv;
+    }
+    if (S.v) {
+        omv = make_double2(S.v[2 * i] * om, S.v[2 * i + 1] * om);
+        F.v[j] = make_float2((float)S.v[2 * i], (float)S.v[2 * i + 1]);
+    }
+    if (S.r) F.r[j] = make_double2(S.r[2 * i], S.r[2 * i + 1]);
+    F.om[j] = om;
+    F.omr[j] = omr;
+    F.omv[j] = omv;
+}
+
 class AleEngine {
   public:
     // host setup
@@ -945,6 +1038,7 @@ class AleEngine {
     // a fused step (its re-binning leaves them behind)
     bool copies_valid = true;
     float *grad = nullptr;
+    AleStage stg{};  // download / upload staging (allocated on first use)
     long long *dbx = nullptr, *dby = nullptr;
     double *dox = nullptr, *doy = nullptr;
 
@@ -953,6 +1047,7 @@ class AleEngine {
     void release() {
         for (void *q : allocs) cudaFree(q);
         allocs.clear();
+        stg = AleStage{};
         built = false;
     }
 
@@ -1220,87 +1315,99 @@ class AleEngine {
         return 0;
     }
 
+    template <typename P> int stage(P **q, size_t per, std::string &err) {
+        return *q ? 0 : alloc(q, per * (size_t)ntot, err);
+    }
+
+    // state in the reference's order: the device writes every requested field
+    // at its particle's index (k_ale_export); with every particle live the
+    // host copies whole arrays, otherwise it keeps the live ones
     int download(int mask, const tsph_ale_host_state *o, std::string &err) {
-        ACK(cudaStreamSynchronize(st));
+        int rc;
+        AleStage S{};
+        struct Want {
+            int bit;
+            double *host;
+            double **dev;
+            int width;
+        };
+        const Want want[] = {{TSPH_ALE_F_R, o->r, &stg.r, 2},
+                             {TSPH_ALE_F_V, o->v, &stg.v, 2},
+                             {TSPH_ALE_F_RHO, o->rho, &stg.rho, 1},
+                             {TSPH_ALE_F_P, o->p, &stg.p, 1},
+                             {TSPH_ALE_F_OMEGA, o->omega, &stg.om, 1},
+                             {TSPH_ALE_F_OMEGARHO, o->omegarho, &stg.omr, 1},
+                             {TSPH_ALE_F_OMEGAV, o->omegav, &stg.omv, 2},
+                             {TSPH_ALE_F_RATES, o->domega, &stg.dom, 1},
+                             {TSPH_ALE_F_RATES, o->domegarho, &stg.domr, 1},
+                             {TSPH_ALE_F_RATES, o->domegav, &stg.domv, 2},
+                             {TSPH_ALE_F_GRAD, o->grad, &stg.grad, 12}};
+        double **sp[] = {&S.r, &S.v, &S.rho, &S.p, &S.om, &S.omr, &S.omv, &S.dom, &S.domr,
+                         &S.domv, &S.grad};
+        for (int k = 0; k < 11; k++) {
+            if (!(mask & want[k].bit) || !want[k].host) continue;
+            if ((rc = stage(want[k].dev, (size_t)want[k].width, err))) return rc;
+            *sp[k] = *want[k].dev;
+        }
+        const bool want_type = (mask & TSPH_ALE_F_TYPE) && o->type;
+        if (want_type) {
+            if ((rc = stage(&stg.type, 1, err))) return rc;
+            S.type = stg.type;
+        }
+        if ((rc = stage(&stg.alive, 1, err))) return rc;
+        S.alive = stg.alive;
+        ACK(cudaMemsetAsync(stg.alive, 0, (size_t)ntot, st));
+        k_ale_export<<<nblk(nw + nf), kBlock, 0, st>>>(A, fstart, ncells, W, nw, S, rho0, dp * dp,
+                                                       cs * cs * rho0 / 7.);
+        ACK(cudaGetLastError());
         uint32_t nl = 0;
-        ACK(cudaMemcpy(&nl, fstart + ncells, 4, cudaMemcpyDeviceToHost));
-        std::vector<double2> R(nl), OMV(nl);
-        std::vector<double> OM(nl), OMR(nl);
-        std::vector<float> S(nl), PS(nl), DOM(nl), DOMR(nl), G((size_t)12 * nl);
-        std::vector<float2> V(nl), DOMV(nl);
-        std::vector<uint32_t> ID(nl), WID(nw);
-        std::vector<double2> WR(nw);
-        std::vector<float> WS(nw);
-        if (nl) {
-            ACK(cudaMemcpy(R.data(), A.r, 16 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(OM.data(), A.om, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(OMR.data(), A.omr, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(OMV.data(), A.omv, 16 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(S.data(), A.s, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(PS.data(), A.ps, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(V.data(), A.v, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(DOM.data(), A.dom, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(DOMR.data(), A.domr, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(DOMV.data(), A.domv, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(ID.data(), A.id, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(G.data(), grad, 48 * (size_t)nl, cudaMemcpyDeviceToHost));
+        ACK(cudaMemcpyAsync(&nl, fstart + ncells, 4, cudaMemcpyDeviceToHost, st));
+        ACK(cudaStreamSynchronize(st));
+        const bool dense = (long long)nl + nw == (long long)ntot;
+        std::vector<uint8_t> alive;
+        if (!dense) {
+            alive.resize(ntot);
+            ACK(cudaMemcpyAsync(alive.data(), stg.alive, (size_t)ntot, cudaMemcpyDeviceToHost, st));
+            ACK(cudaStreamSynchronize(st));
         }
-        if (nw) {
-            ACK(cudaMemcpy(WID.data(), W.id, 4 * (size_t)nw, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(WR.data(), W.r, 16 * (size_t)nw, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(WS.data(), W.s, 4 * (size_t)nw, cudaMemcpyDeviceToHost));
-        }
-        // rows in ascending original index: (id, fluid row or -1 - wall row)
-        std::vector<std::pair<uint32_t, int>> rows;
-        for (uint32_t j = 0; j < nl; j++) rows.push_back({ID[j], (int)j});
-        for (int w = 0; w < nw; w++) rows.push_back({WID[w], -1 - w});
-        std::sort(rows.begin(), rows.end());
-        const double dp2 = dp * dp;
-        for (size_t k = 0; k < rows.size(); k++) {
-            const int j = rows[k].second;
-            const bool wall = j < 0;
-            const int w = -1 - j;
-            const double rh = wall ? rho0 + (double)WS[w] : rho0 + (double)S[j];
-            if ((mask & TSPH_ALE_F_R) && o->r) {
-                const double2 x = wall ? WR[w] : R[j];
-                o->r[2 * k] = x.x;
-                o->r[2 * k + 1] = x.y;
+        std::vector<double> tmp;
+        for (int k = 0; k < 11; k++) {
+            if (!*sp[k]) continue;
+            const size_t wdt = (size_t)want[k].width;
+            if (dense) {
+                ACK(cudaMemcpyAsync(want[k].host, *sp[k], 8 * wdt * ntot, cudaMemcpyDeviceToHost, st));
+                continue;
             }
-            if ((mask & TSPH_ALE_F_V) && o->v) {
-                o->v[2 * k] = wall ? 0. : (double)V[j].x;
-                o->v[2 * k + 1] = wall ? 0. : (double)V[j].y;
-            }
-            if ((mask & TSPH_ALE_F_RHO) && o->rho) o->rho[k] = rh;
-            if ((mask & TSPH_ALE_F_P) && o->p) {
-                // Density_to_pressure of the density the last fluxes used
-                const double x = (wall ? rh : rho0 + (double)PS[j]) / rho0;
-                o->p[k] = cs * cs * rho0 / 7. * (std::pow(x, 7.) - 1);
-            }
-            if ((mask & TSPH_ALE_F_OMEGA) && o->omega) o->omega[k] = wall ? dp2 : OM[j];
-            if ((mask & TSPH_ALE_F_OMEGARHO) && o->omegarho) o->omegarho[k] = wall ? rh * dp2 : OMR[j];
-            if ((mask & TSPH_ALE_F_OMEGAV) && o->omegav) {
-                o->omegav[2 * k] = wall ? 0. : OMV[j].x;
-                o->omegav[2 * k + 1] = wall ? 0. : OMV[j].y;
-            }
-            if (mask & TSPH_ALE_F_RATES) {
-                if (o->domega) o->domega[k] = wall ? 0. : (double)DOM[j];
-                if (o->domegarho) o->domegarho[k] = wall ? 0. : (double)DOMR[j];
-                if (o->domegav) {
-                    o->domegav[2 * k] = wall ? 0. : (double)DOMV[j].x;
-                    o->domegav[2 * k + 1] = wall ? 0. : (double)DOMV[j].y;
+            tmp.resize(wdt * ntot);
+            ACK(cudaMemcpyAsync(tmp.data(), *sp[k], 8 * wdt * ntot, cudaMemcpyDeviceToHost, st));
+            ACK(cudaStreamSynchronize(st));
+            size_t q = 0;
+            for (int i = 0; i < ntot; i++)
+                if (alive[i]) {
+                    for (size_t w = 0; w < wdt; w++) want[k].host[q * wdt + w] = tmp[(size_t)i * wdt + w];
+                    q++;
                 }
-            }
-            if ((mask & TSPH_ALE_F_GRAD) && o->grad)
-                for (int q = 0; q < 12; q++)
-                    o->grad[12 * k + q] = wall ? 0. : (double)G[(size_t)12 * j + q];
-            if ((mask & TSPH_ALE_F_INDEX) && o->index) o->index[k] = (int32_t)rows[k].first;
-            if ((mask & TSPH_ALE_F_TYPE) && o->type) o->type[k] = wall ? 1 : 0;
+        }
+        if (want_type) {
+            std::vector<int32_t> t(ntot);
+            ACK(cudaMemcpyAsync(t.data(), stg.type, 4 * (size_t)ntot, cudaMemcpyDeviceToHost, st));
+            ACK(cudaStreamSynchronize(st));
+            int q = 0;
+            for (int i = 0; i < ntot; i++)
+                if (dense || alive[i]) o->type[q++] = t[i];
+        }
+        ACK(cudaStreamSynchronize(st));
+        if ((mask & TSPH_ALE_F_INDEX) && o->index) {
+            int q = 0;
+            for (int i = 0; i < ntot; i++)
+                if (dense || alive[i]) o->index[q++] = i;
         }
         return 0;
     }
 
     // upload omega, v, rho and r of fluid particles (omega*v and omega*rho
-    // follow), host arrays in the reference's order
+    // follow), host arrays in the reference's order: staged by index, applied
+    // per fluid row on the device (k_ale_import)
     int upload(int mask, const tsph_ale_host_state *in, std::string &err) {
         ACK(cudaStreamSynchronize(st));
         uint32_t nl = 0;
@@ -1309,51 +1416,28 @@ class AleEngine {
             err = "upload after removals is not supported on the ALE path";
             return TSPH_ERR_STATE;
         }
-        std::vector<uint32_t> ID(nl);
-        std::vector<double> OM(nl), OMR(nl);
-        std::vector<double2> OMV(nl), R(nl);
-        std::vector<float> S(nl), PS(nl);
-        std::vector<float2> V(nl);
-        if (nl) {
-            ACK(cudaMemcpy(PS.data(), A.ps, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(ID.data(), A.id, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(OM.data(), A.om, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(OMR.data(), A.omr, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(OMV.data(), A.omv, 16 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(S.data(), A.s, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(V.data(), A.v, 8 * (size_t)nl, cudaMemcpyDeviceToHost));
-            ACK(cudaMemcpy(R.data(), A.r, 16 * (size_t)nl, cudaMemcpyDeviceToHost));
+        int rc;
+        AleStage S{};
+        struct Put {
+            int bit;
+            const double *host;
+            double **dev;
+            double **use;
+            int width;
+        };
+        const Put put[] = {{TSPH_ALE_F_OMEGA, in->omega, &stg.om, &S.om, 1},
+                           {TSPH_ALE_F_RHO, in->rho, &stg.rho, &S.rho, 1},
+                           {TSPH_ALE_F_V, in->v, &stg.v, &S.v, 2},
+                           {TSPH_ALE_F_R, in->r, &stg.r, &S.r, 2}};
+        for (const Put &q : put) {
+            if (!(mask & q.bit) || !q.host) continue;
+            if ((rc = stage(q.dev, (size_t)q.width, err))) return rc;
+            ACK(cudaMemcpyAsync(*q.dev, q.host, 8 * (size_t)q.width * ntot, cudaMemcpyHostToDevice, st));
+            *q.use = *q.dev;
         }
-        for (uint32_t j = 0; j < nl; j++) {
-            const uint32_t i = ID[j];
-            if ((mask & TSPH_ALE_F_OMEGA) && in->omega) {
-                // new volume, same rho = omega*rho / omega and same
-                // v = omega*v / (rho omega)
-                const double f = in->omega[i] / OM[j];
-                OM[j] = in->omega[i];
-                OMR[j] *= f;
-                OMV[j] = make_double2(OMV[j].x * f, OMV[j].y * f);
-            }
-            if ((mask & TSPH_ALE_F_RHO) && in->rho) {
-                OMR[j] = in->rho[i] * OM[j];
-                S[j] = (float)(in->rho[i] - rho0);
-                PS[j] = S[j];
-            }
-            if ((mask & TSPH_ALE_F_V) && in->v) {
-                OMV[j] = make_double2(in->v[2 * i] * OM[j], in->v[2 * i + 1] * OM[j]);
-                V[j] = make_float2((float)in->v[2 * i], (float)in->v[2 * i + 1]);
-            }
-            if ((mask & TSPH_ALE_F_R) && in->r) R[j] = make_double2(in->r[2 * i], in->r[2 * i + 1]);
-        }
-        if (nl) {
-            ACK(cudaMemcpy(A.om, OM.data(), 8 * (size_t)nl, cudaMemcpyHostToDevice));
-            ACK(cudaMemcpy(A.omr, OMR.data(), 8 * (size_t)nl, cudaMemcpyHostToDevice));
-            ACK(cudaMemcpy(A.omv, OMV.data(), 16 * (size_t)nl, cudaMemcpyHostToDevice));
-            ACK(cudaMemcpy(A.s, S.data(), 4 * (size_t)nl, cudaMemcpyHostToDevice));
-            ACK(cudaMemcpy(A.ps, PS.data(), 4 * (size_t)nl, cudaMemcpyHostToDevice));
-            ACK(cudaMemcpy(A.v, V.data(), 8 * (size_t)nl, cudaMemcpyHostToDevice));
-            ACK(cudaMemcpy(A.r, R.data(), 16 * (size_t)nl, cudaMemcpyHostToDevice));
-        }
+        k_ale_import<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, S, rho0);
+        ACK(cudaGetLastError());
+        ACK(cudaStreamSynchronize(st));
         if (mask & TSPH_ALE_F_R) cells = false;
         return 0;
     }

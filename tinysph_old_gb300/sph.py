@@ -717,6 +717,21 @@ class AleSystem:
             mask |= bit
         _check(self._L.tsph_ale_upload(self._h, mask, C.byref(hs)))
 
+    def upload_ptrs(self, mask, **ptrs):
+        """Upload from raw host pointers (e.g. pinned buffers), arrays in the
+        reference's particle order."""
+        hs = _AleHostState()
+        for k, v in ptrs.items():
+            setattr(hs, k, v)
+        _check(self._L.tsph_ale_upload(self._h, int(mask), C.byref(hs)))
+
+    def download_ptrs(self, mask, **ptrs):
+        """Download into raw host pointers (e.g. pinned buffers)."""
+        hs = _AleHostState()
+        for k, v in ptrs.items():
+            setattr(hs, k, v)
+        _check(self._L.tsph_ale_download(self._h, int(mask), C.byref(hs)))
+
     def sync(self):
         _check(self._L.tsph_ale_sync(self._h))
 
