@@ -492,7 +492,7 @@ PROBES = ((1.60, 0.02), (1.60, 0.10), (1.60, 0.20))  # pressure probes at the fa
 
 
 def observe(system, front_y=0.02):
-    """The quantities the surrogate is judged on: water front (largest fluid
+    """The quantities the surrogate is checked on: water front (largest fluid
     x with y <= front_y), free-surface elevation at the gauges, pressure at
     the probes (Shepard, as Pressure_in_point)."""
     return dict(front=system.water_front(front_y),
