@@ -6,12 +6,16 @@
 // cell-sorted state (their cells are consecutive rows of one or two grid
 // columns).  For each window of at most kTileRows target rows of one column it
 //   1. stages the 3 x (rows + 2) neighbour cells (fluid and walls) into shared
-//      memory: FP32 position relative to the particle's own cell (so r_a - r_b
-//      keeps ~1e-7 relative precision without FP64), velocity, rho - rho0,
-//      p/rho and 1/rho (the EOS and the reciprocal done once per staged
-//      particle instead of once per pair);
-//   2. phase 1: every thread walks its own 3 x 3 cells in shared memory and
-//      appends the in-support neighbours (0 < r <= 2h) to a private list;
+//      memory, all of a thread's loads issued before its stores: FP32
+//      position, x relative to the window's centre column and y relative to
+//      the particle's own cell (so r_a - r_b keeps ~1e-7 relative precision
+//      without FP64), velocity, rho - rho0, p/rho and 1/rho (the EOS and the
+//      reciprocal done once per staged particle instead of once per pair);
+//   2. phase 1: every thread walks, per neighbour column, the staged ranges
+//      of the rows below, at and above its own (contiguous and sorted by y,
+//      so the rows above and below stop once |dy| passes the reach) and
+//      appends the in-support neighbours (r <= 2h, the particle itself
+//      excluded) to a private list of (staged index, row code) entries;
 //   3. phase 2: every thread evaluates the WCSPH pair terms over its list, so
 //      the expensive arithmetic runs with nearly all lanes active (a plain
 //      candidate loop would execute it for ~80 candidates with ~30% of the
