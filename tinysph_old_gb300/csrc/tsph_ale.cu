@@ -625,11 +625,11 @@ __device__ __forceinline__ void ale_pair(float dx, float dy, float2 va, float sa
     acc.domr = fmaf(-t2 * rhos, ex * dWx + ey * dWy, acc.domr);
 }
 
-// the bounded append of a cell that could overflow the list (one copy, out
-// of line: the unrolled neighbour loop calls it rarely)
-// one range appended one candidate at a time, at most up to the list's end
-// (the support test with the particle itself and coincident particles
-// excluded, 0 < r^2 <= 4h^2); a candidate past the end sets `overflow`
+// the bounded append of a row range that could overflow the list: one
+// candidate at a time, at most up to the list's end (the support test with
+// the particle itself and coincident particles excluded, 0 < r^2 <= 4h^2); a
+// candidate past the end sets `overflow`.  Inlined: out of line, its calls
+// from the unrolled loops made the kernel spill registers.
 static __device__ __forceinline__ uint16_t *append_bounded_ale(const float2 *loc, uint16_t *lst,
                                                             uint16_t *w, int j0, int j1,
                                                             uint32_t code, float bx, float by,
