@@ -48,6 +48,24 @@ ALE_STEP_BYTES_PER_PARTICLE = 575.0
 ALE_METRIC = "particle-steps/s, ALE-SPH dam break dp=0.0004 (1.1M fluid), 1 GB300"
 
 
+def max_over_ranks(x, dist, device):
+    """The largest of each rank's value (the timed region's length: the job
+    is as slow as its slowest rank); `dist` None for one process."""
+    if dist is None:
+        return float(x)
+    import torch
+
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(world, units_per_rank, steps, ms):
+    """Units all ranks processed per second over the slowest rank's time
+    (weak scaling: every rank runs the same work)."""
+    return world * units_per_rank * steps / (ms / 1000.0)
+
+
 def _env_int(k, d):
     try:
         return int(os.environ.get(k, d))
@@ -245,11 +263,8 @@ def run_ale(args, rank, world, local):
         stream.synchronize()
     torch.cuda.synchronize()
     ms = sum(starts[k].elapsed_time(ends[k]) for k in range(args.steps))
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n * args.steps / (ms / 1000.0)
+    ms = max_over_ranks(ms, dist, "cuda")
+    value = whole_job_rate(world, n, args.steps, ms)
     # flux kernel alone (one launch per call), events on the system's stream
     fl_us = []
     for _ in range(5):
@@ -742,13 +757,10 @@ def main():
         t_wall = time.perf_counter() - t_wall0
     torch.cuda.synchronize()
     ms = sum(starts[k].elapsed_time(ends[k]) for k in range(args.steps))
+    ms = max_over_ranks(ms, dist, "cuda")
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        if dist:
-            dist.barrier()
-        ms = float(t.item())
-    value = world * n * args.steps / (ms / 1000.0)
+        dist.barrier()
+    value = whole_job_rate(world, n, args.steps, ms)
     health = s.health()
 
     # ---- per-kernel timing for the roofline (eager launches with events)
