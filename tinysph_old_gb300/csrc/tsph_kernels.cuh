@@ -163,21 +163,6 @@ __device__ __forceinline__ bool gated_off(const uint32_t *gate) {
     return gate != nullptr && __ldg(gate) == 0u;
 }
 
-// keys + histogram slot of fluid particles [0, n) (n read from *n_ptr).
-static __global__ void k_bin(const double2 *__restrict__ r, const uint32_t *__restrict__ old_key,
-                      const int *__restrict__ n_ptr, Grid g, uint32_t *__restrict__ key,
-                      uint32_t *__restrict__ slot, uint32_t *__restrict__ counts,
-                      uint32_t *__restrict__ health, const uint32_t *__restrict__ gate) {
-    if (gated_off(gate)) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *n_ptr) return;
-    int cx, cy;
-    const uint32_t k = cell_key(g, r[i], old_key ? old_key[i] : 0xffffffffu, &cx, &cy);
-    if (k == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
-    key[i] = k;
-    slot[i] = atomicAdd(counts + k, 1u);
-}
-
 // dead particles (removed) get the last bucket without a range check
 static __global__ void k_bin_keep_dead(const double2 *__restrict__ r, const uint32_t *__restrict__ old_key,
                                 const int *__restrict__ n_ptr, Grid g,
@@ -361,35 +346,8 @@ static __global__ void k_place(const uint32_t *__restrict__ key, const uint32_t 
 }
 
 // rank: final position = cell start + number of cell members that order
-// before this one
-static __global__ void k_rank(const uint32_t *__restrict__ key, const int *__restrict__ n_ptr,
-                       const uint32_t *__restrict__ start, const uint32_t *__restrict__ tmp_id,
-                       const uint32_t *__restrict__ tmp_src, uint32_t *__restrict__ perm,
-                       int ncells, const long long *__restrict__ tmp_y) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= *n_ptr) return;
-    const uint32_t src = tmp_src[j];
-    const uint32_t k = key[src];
-    if (k == (uint32_t)ncells) {  // removed: order irrelevant
-        perm[j] = src;
-        return;
-    }
-    const uint32_t lo = start[k], hi = start[k + 1];
-    const uint32_t me = tmp_id[j];
-    uint32_t rank = 0;
-    if (tmp_y) {
-        const long long my = tmp_y[j];
-        for (uint32_t m = lo; m < hi; m++) {
-            const long long ym = tmp_y[m];
-            rank += (ym < my || (ym == my && tmp_id[m] < me)) ? 1u : 0u;
-        }
-    } else {
-        for (uint32_t m = lo; m < hi; m++) rank += (tmp_id[m] < me) ? 1u : 0u;
-    }
-    perm[lo + rank] = src;
-}
-
-// rank (as k_rank) and move the particle's record straight to its final
+// before this one (the order key inside a cell as in k_place); then move
+// the particle's record straight to its final
 // slot: D[final] = src[s], recomputing loc; optional acceleration, density
 // rate, pressure and old state travel along
 template <typename T>
@@ -1415,43 +1373,6 @@ __global__ void k_copy_back(const FluidState<T> S, const double2 *__restrict__ o
 // ------------------------------------------------------------ gathers
 // dst[f] = src[perm[f]] for the sorted state (+ the old state when O != null);
 // recomputes loc from the FP64 position and the key.
-template <typename T>
-__global__ void k_gather(const uint32_t *__restrict__ perm, const int *__restrict__ n_ptr, Grid g,
-                         const double2 *__restrict__ sr, const typename V2<T>::t *__restrict__ sv,
-                         const T *__restrict__ srho, const uint32_t *__restrict__ sid,
-                         const uint32_t *__restrict__ skey,
-                         const typename V2<T>::t *__restrict__ sa, const T *__restrict__ sdrho,
-                         const T *__restrict__ sp, FluidState<T> D,
-                         // optional old state: copied from (or2, ov2, orho2) into O
-                         const double2 *__restrict__ or2, const typename V2<T>::t *__restrict__ ov2,
-                         const T *__restrict__ orho2, OldState<T> O) {
-    const int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= *n_ptr) return;
-    const uint32_t s = perm[f];
-    const double2 r = sr[s];
-    const uint32_t k = skey[s];
-    D.r[f] = r;
-    D.v[f] = sv[s];
-    D.rho[f] = srho[s];
-    D.id[f] = sid[s];
-    D.key[f] = k;
-    if (k < (uint32_t)g.ncells) {
-        const int cx = (int)(k / (uint32_t)g.ncy);
-        const int cy = (int)k - cx * g.ncy;
-        D.loc[f] = cell_local(g, r, cx, cy);
-    } else {
-        D.loc[f] = make_float2(0.f, 0.f);
-    }
-    if (sa) D.a[f] = sa[s];
-    if (sdrho) D.drho[f] = sdrho[s];
-    if (sp) D.p[f] = sp[s];
-    if (or2) {
-        O.r[f] = or2[s];
-        O.v[f] = ov2[s];
-        O.rho[f] = orho2[s];
-    }
-}
-
 // --------------------------------------------------- host <-> device
 // Per-index staging (SoA, double, indexed by original particle index) used by
 // tsph_download / tsph_upload to present the state in the reference's order.
