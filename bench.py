@@ -44,6 +44,7 @@ METRIC = "particle-steps/s, 720k dam break, 1 GB300: surrogate/batched vs plain,
 # 124 B, fluxes 48 B, leap-frog two + binning 164 B, placement 36 B,
 # rank + scatter 188 B, scan 15 B)
 ALE_FLUX_BYTES_PER_PARTICLE = 48.0
+INFER_KERNELS = 5  # one network forward: node kernel, then edge + node kernel for each of 2 layers
 ALE_STEP_BYTES_PER_PARTICLE = 575.0
 ALE_METRIC = "particle-steps/s, ALE-SPH dam break dp=0.0004 (1.1M fluid), 1 GB300"
 
@@ -371,6 +372,8 @@ def run_batch(args, rank, world, local):
     main = torch.cuda.current_stream()
     t_start = torch.cuda.Event(enable_timing=True)
     ends = [torch.cuda.Event(enable_timing=True) for _ in streams]
+    for g in bt.groups:
+        g.system.kernel_launches(reset=True)
     with ClockSampler(local) as clocks:
         t_start.record(main)
         for st in streams:
@@ -380,6 +383,7 @@ def run_batch(args, rank, world, local):
             e.record(st)
         torch.cuda.synchronize()
     ms = max(t_start.elapsed_time(e) for e in ends)
+    timed_launches = sum(g.system.kernel_launches() for g in bt.groups)
     value = n * args.steps / (ms / 1000.0)
     # per group: step time alone (for the projection to 0.5 s of every case)
     group_ms = []
@@ -494,7 +498,7 @@ def run_batch(args, rank, world, local):
                      "kernel": f"k_pairs_tiled, largest group {big.key}",
                      "bytes_per_unit": PAIR_BYTES_PER_PARTICLE, "unit_count": nfl_big,
                      "avg_launch_us": pair_us, "peak_kind": peak_kind},
-        "gpu_launches": args.steps * 13 * len(bt.groups),
+        "gpu_launches": int(timed_launches),
         "clocks": clocks.summary(),
         "health": [g.system.health() for g in bt.groups],
     }
@@ -552,7 +556,11 @@ def run_surrogate(args, rank, world, local):
         ro.windows = ro.fallbacks = 0
         ro.checks.clear()
         plain.step(case.wall_model, case.dt, 3 * k)  # same physical time as the surrogate
+        sur.kernel_launches(reset=True)
         ms_sur = timed(sur, ro.window, args.steps)
+        # the engine's kernels (graph steps per kernel) + the network's forward
+        # (one node kernel, then an edge and a node kernel per layer) per window
+        sur_launches = sur.kernel_launches() + args.steps * INFER_KERNELS
     value = n * k * args.steps / (ms_sur / 1000.0)
     plain_value = n * k * args.steps / (ms_plain / 1000.0)
     fa, fb = plain.water_front(0.02), sur.water_front(0.02)
@@ -604,7 +612,7 @@ def run_surrogate(args, rank, world, local):
                      "note": "the window mixes the network (tensor cores, SFU-bound edge sums) "
                              "and the plain step; the plain step's pair-kernel roofline is in "
                              "the dam_break workload's line"},
-        "gpu_launches": int(args.steps * (20 + ro.fallback_rate * k * 13)),
+        "gpu_launches": int(sur_launches),
         "clocks": clocks.summary(),
     }
     print(json.dumps(line), flush=True)
@@ -745,6 +753,7 @@ def main():
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    s.kernel_launches(reset=True)
     with ClockSampler(local) as clocks:
         t_wall0 = time.perf_counter()
         with torch.cuda.stream(stream):
@@ -756,6 +765,9 @@ def main():
         stream.synchronize()
         t_wall = time.perf_counter() - t_wall0
     torch.cuda.synchronize()
+    # the library's kernels in the timed region (graph steps per kernel, the
+    # conditional re-binning only when it ran; the L2 flush is torch's)
+    timed_launches = s.kernel_launches()
     ms = sum(starts[k].elapsed_time(ends[k]) for k in range(args.steps))
     ms = max_over_ranks(ms, dist, "cuda")
     if dist:
@@ -770,8 +782,6 @@ def main():
     s.step(model, dt, prof_steps)
     prof = s.profile(reset=True)
     s.set_profiling(False)
-    launches_per_step = (prof["pair_launches"] + prof["sort_launches"] + prof["mdbc_launches"]
-                         + prof["other_launches"] - 1) / prof_steps  # minus the trailing EOS
     pair_avg_us = prof["pair_us"] / max(prof["pair_launches"], 1)
     nfluid = int(np.sum(a["type"] == 0))
     peak, peak_kind = measured_peaks()
@@ -841,7 +851,7 @@ def main():
                               "frac": STEP_BYTES_PER_PARTICLE * value / world / 1e9 / peak},
             "kernel_us_per_step": {k: prof[k] / prof_steps for k in
                                    ("pair_us", "sort_us", "mdbc_us", "other_us")},
-            "gpu_launches": int(round(launches_per_step * args.steps)),
+            "gpu_launches": int(timed_launches),
             "clocks": clocks.summary(),
             "health": health,
             "wall_s_timed": t_wall,

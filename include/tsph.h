@@ -232,6 +232,11 @@ int tsph_upload(tsph_system *s, int fields, const tsph_host_state *in);
 int tsph_sync(tsph_system *s);
 /* device health word (TSPH_HEALTH_*), optionally cleared */
 int tsph_health(tsph_system *s, uint32_t *flags, int clear);
+/* number of kernels the library launched for this system (no counterpart in
+ * the reference): eager launches, the kernels of every CUDA-graph step
+ * launched, and those of the conditional re-binning each time it ran on the
+ * device; optionally reset to zero */
+int tsph_kernel_launches(tsph_system *s, long long *count, int reset);
 
 /* Global reductions in FP64 over fluid particles: total mass, kinetic energy
  * sum(0.5 m |v|^2) (the harness-side Total_kinetic_energy the still-water

@@ -1,0 +1,24 @@
+"""tsph_kernel_launches: the kernels a system launched.  A graph step counts
+its kernels, so the count grows by the same amount per step (the conditional
+re-binning stays off at these speeds); the end-of-call equation of state adds
+one per call; reset clears it."""
+
+import pytest
+
+from tinysph_old_gb300 import cases
+
+
+@pytest.mark.gpu
+def test_kernel_launch_count_per_graph_step(gpu_tsph):
+    case = cases.dam_break_mdbc(dp=0.01)
+    s = gpu_tsph.ParticleSystem.from_case(case)
+    s.step(case.wall_model, case.dt, 2)  # captures the graph
+    s.kernel_launches(reset=True)
+    s.step(case.wall_model, case.dt, 5)
+    c5 = s.kernel_launches(reset=True)
+    s.step(case.wall_model, case.dt, 15)
+    c15 = s.kernel_launches(reset=True)
+    per_step = (c15 - c5) / 10
+    assert per_step == int(per_step) and 6 <= per_step <= 12, (c5, c15)
+    assert c5 == 5 * per_step + 1  # + the equation of state after the call
+    assert s.kernel_launches() == 0

@@ -453,6 +453,17 @@ int tsph_sync(tsph_system *s) {
     return TSPH_OK;
 }
 
+int tsph_kernel_launches(tsph_system *s, long long *count, int reset) {
+    NEED(s);
+    if (!count) return fail(TSPH_ERR_ARG, "null count");
+    if (!s->eng) {
+        *count = 0;
+        return TSPH_OK;
+    }
+    RUN(s->eng->kernel_launches(count, reset, err_));
+    return TSPH_OK;
+}
+
 int tsph_health(tsph_system *s, uint32_t *flags, int clear) {
     NEED(s);
     if (!flags) return fail(TSPH_ERR_ARG, "null flags");

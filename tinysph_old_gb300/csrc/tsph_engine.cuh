@@ -92,6 +92,15 @@ template <typename T> class Engine final : public EngineBase {
 
     // ---- graphs keyed by (model, dt bits)
     std::map<std::pair<int, long long>, cudaGraphExec_t> graphs_;
+    // kernel launches: eager ones counted as they are made; a graph's kernels
+    // counted at capture (outside / inside the conditional re-binning body),
+    // its launches then add the outside ones and the body's executions
+    // (counted on the device in rebins_) add the body's
+    long long launched_ = 0;
+    int cap_main_ = 0, cap_body_ = 0, body_kernels_ = 0;
+    bool in_body_ = false;
+    uint32_t *rebins_ = nullptr;
+    std::map<std::pair<int, long long>, int> graph_kernels_;
 
     // ---- profiling
     bool prof_ = false;
@@ -141,6 +150,9 @@ template <typename T> class Engine final : public EngineBase {
             b = ev();
             cudaEventRecord(a, st_);
         }
+        if (!capturing_) launched_++;
+        else if (in_body_) cap_body_++;
+        else cap_main_++;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)grid);
         cfg.blockDim = dim3((unsigned)block);
@@ -599,7 +611,7 @@ template <typename T> class Engine final : public EngineBase {
         int rc;
         if ((rc = launch(CAT_SORT, k_bin_gated<T>, blocks_for(nf_), kBlock, err,
                          (const FluidState<T>)Fs_, (const uint32_t *)fstart_, grid_, keyB_, slotB_,
-                         counts_, health_, gate)))
+                         counts_, health_, gate, in_body_ ? rebins_ : (uint32_t *)nullptr)))
             return rc;
         if ((rc = sort_finish(Fs_.r, Fs_.v, Fs_.rho, Fs_.id, nullptr, nullptr, nullptr, F_, O_.r,
                               O_.v, O_.rho, OldState<T>{Br_, Bv_, Brho_}, err, gate)))
@@ -663,7 +675,9 @@ template <typename T> class Engine final : public EngineBase {
                 TSPH_CK(cudaStreamBeginCaptureToGraph(st2_, body, nullptr, nullptr, 0,
                                                       cudaStreamCaptureModeThreadLocal));
                 std::swap(st_, st2_);
+                in_body_ = true;
                 rc = rebin_predicted(nullptr, err);
+                in_body_ = false;
                 std::swap(st_, st2_);
                 cudaGraph_t bodyc = nullptr;
                 const cudaError_t e = cudaStreamEndCapture(st2_, &bodyc);
@@ -840,11 +854,12 @@ template <typename T> class Engine final : public EngineBase {
         if ((rc = alloc(&counts_, ncells_ + 1, err)) || (rc = alloc(&fstart_, ncells_ + 2, err)) ||
             (rc = alloc(&wstart_, ncells_ + 1, err)) || (rc = alloc(&tile_sums_, ntiles, err)) ||
             (rc = alloc(&health_, 1, err)) || (rc = alloc(&removed_, 1, err)) ||
-            (rc = alloc(&rebuild_, 1, err)) ||
+            (rc = alloc(&rebuild_, 1, err)) || (rc = alloc(&rebins_, 1, err)) ||
             (rc = alloc(&dtot_, 4 * (size_t)blocks_for(nf_), err)))
             return rc;
         TSPH_CK(cudaMemset(health_, 0, 4));
         TSPH_CK(cudaMemset(removed_, 0, 4));
+        TSPH_CK(cudaMemset(rebins_, 0, 4));
         TSPH_CK(cudaMemset(counts_, 0, sizeof(uint32_t) * (ncells_ + 1)));
         // staging
         if ((rc = alloc(&S_.r, id_cap_, err)) || (rc = alloc(&S_.v, id_cap_, err)) ||
@@ -1139,6 +1154,7 @@ template <typename T> class Engine final : public EngineBase {
                 cudaGraph_t g;
                 TSPH_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
                 capturing_ = true;
+                cap_main_ = cap_body_ = 0;
                 rc = enqueue_step(model, (T)dt, err);
                 capturing_ = false;
                 cudaGraph_t g2 = nullptr;
@@ -1160,8 +1176,11 @@ template <typename T> class Engine final : public EngineBase {
                     return 2;
                 }
                 it = graphs_.emplace(key, ex).first;
+                graph_kernels_[key] = cap_main_;
+                if (cap_body_) body_kernels_ = cap_body_;
             }
             for (int s = 0; s < nsteps; s++) TSPH_CK(cudaGraphLaunch(it->second, st_));
+            launched_ += (long long)nsteps * graph_kernels_[key];
         }
         // the reference's state after a step holds p = EOS(rho) (step body :110-111)
         if ((rc = launch(CAT_OTHER, k_eos<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
@@ -1170,6 +1189,19 @@ template <typename T> class Engine final : public EngineBase {
         cells_ = true;
         exported_ = false;
         return collect_profile(err);
+    }
+
+    int kernel_launches(long long *count, int reset, std::string &err) override {
+        (void)err;
+        uint32_t runs = 0;
+        TSPH_CK(cudaMemcpyAsync(&runs, rebins_, 4, cudaMemcpyDeviceToHost, st_));
+        TSPH_CK(cudaStreamSynchronize(st_));
+        *count = launched_ + (long long)runs * body_kernels_;
+        if (reset) {
+            launched_ = 0;
+            TSPH_CK(cudaMemsetAsync(rebins_, 0, 4, st_));
+        }
+        return 0;
     }
 
     int np_live(int *np, std::string &err) override {

@@ -62,6 +62,7 @@ class EngineBase {
     virtual int get_cells(int32_t *cell_start, int32_t *cell_list, std::string &err) = 0;
     virtual int pair_digest(int32_t *count, int64_t *sum, int32_t *xr, std::string &err) = 0;
     virtual int np_live(int *np, std::string &err) = 0;
+    virtual int kernel_launches(long long *count, int reset, std::string &err) = 0;
     virtual int health(uint32_t *flags, int clear, std::string &err) = 0;
     virtual int totals(double out[4], std::string &err) = 0;
     virtual int water_level(int n, const double *x, const double *y0, const int32_t *inverse,

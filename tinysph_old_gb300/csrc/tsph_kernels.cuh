@@ -1337,9 +1337,11 @@ template <typename T>
 __global__ void k_bin_gated(const FluidState<T> X, const uint32_t *__restrict__ fstart, Grid g,
                             uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
                             uint32_t *__restrict__ counts, uint32_t *__restrict__ health,
-                            const uint32_t *__restrict__ gate) {
+                            const uint32_t *__restrict__ gate, uint32_t *__restrict__ runs) {
     pdl_enter();
     if (gated_off(gate)) return;
+    // `runs` counts the executions of a re-binning that a graph carries
+    if (runs && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(runs, 1u);
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_live(fstart, g.ncells)) return;
     int cx, cy;

@@ -37,7 +37,8 @@ ABI_SYMBOLS = (
     "tsph_add_buffer_zone", "tsph_set_zone_capacity", "tsph_bz_inlet", "tsph_bz_outlet",
     "tsph_compute_forces", "tsph_symplectic_predictor", "tsph_symplectic_corrector",
     "tsph_remove_out_of_domain", "tsph_step", "tsph_download", "tsph_upload", "tsph_sync",
-    "tsph_health", "tsph_fluid_totals", "tsph_set_profiling", "tsph_get_profile",
+    "tsph_health", "tsph_kernel_launches", "tsph_fluid_totals", "tsph_set_profiling",
+    "tsph_get_profile",
     "tsph_water_level", "tsph_point_fields", "tsph_water_front", "tsph_autotune",
     "tsph_set_tile_shape", "tsph_write_vtk", "tsph_save_checkpoint", "tsph_load_checkpoint",
     "tsph_export_graph", "tsph_apply_update", "tsph_window_check", "tsph_get_stream",
@@ -149,6 +150,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_download.argtypes = [P, I, C.POINTER(_HostState)]
     L.tsph_upload.argtypes = [P, I, C.POINTER(_HostState)]
     L.tsph_health.argtypes = [P, C.POINTER(C.c_uint32), I]
+    L.tsph_kernel_launches.argtypes = [P, C.POINTER(C.c_longlong), I]
     L.tsph_fluid_totals.argtypes = [P, P]
     L.tsph_set_profiling.argtypes = [P, I]
     L.tsph_get_profile.argtypes = [P, C.POINTER(_Profile), I]
@@ -421,6 +423,13 @@ class ParticleSystem:
 
     def sync(self):
         _check(self._L.tsph_sync(self._h))
+
+    def kernel_launches(self, reset=False) -> int:
+        """Kernels launched for this system (graph steps counted per kernel,
+        the conditional re-binning only when it ran)."""
+        n = C.c_longlong()
+        _check(self._L.tsph_kernel_launches(self._h, C.byref(n), 1 if reset else 0))
+        return n.value
 
     def health(self, clear=False) -> int:
         f = C.c_uint32()
