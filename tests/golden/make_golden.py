@@ -234,6 +234,19 @@ def main_bt():
             out[f"step{done}_{k}"] = st[k]
     out["dt"] = np.float64(case.dt)
     np.savez_compressed(os.path.join(HERE, "dam_break_bt_dp0.02.npz"), **out)
+    # still water with BT walls (cases/stillWater_BT): the reference's RUN
+    # loop from the case's hydrostatic start, states after 100 and 300 steps
+    case = cases.still_water_bt(dp=0.02)
+    R3 = O.RefBt.from_case(case)
+    out = {"dt": np.float64(case.dt), "snaps": np.array([100, 300])}
+    done = 0
+    for n in (100, 300):
+        R3.step(case.dt, n - done)
+        done = n
+        st = R3.state()
+        for k in ("r", "v", "rho", "p", "a", "drho", "index"):
+            out[f"step{n}_{k}"] = st[k]
+    np.savez_compressed(os.path.join(HERE, "still_water_bt_dp0.02.npz"), **out)
 
 
 def _perturbed_walls(case, u):

@@ -1,5 +1,5 @@
 """The oracle's boundary-integral (BT) walls against the reference's own
-outputs (tests/golden/dam_break_bt_dp0.02.npz, made by
+outputs (tests/golden/dam_break_bt_dp0.02.npz and still_water_bt_dp0.02.npz, made by
 tests/golden/make_golden.py from src/SPH_interactionBT.h, src/SPH_BT.h and
 the RUN loop of cases/damBreakLong_BT/SPH_simulationSymplectic.h), and the
 case generator against the reference's generators."""
@@ -57,3 +57,19 @@ def test_bt_steps_match_the_reference():
         assert np.array_equal(st["index"], GOLD[f"step{k}_index"])
         for f in ("r", "v", "rho", "p", "a", "drho"):
             assert _rel(st[f], GOLD[f"step{k}_{f}"]) <= 1e-10, (k, f)
+
+
+def test_bt_still_water_steps_match_the_reference():
+    """cases/stillWater_BT from its hydrostatic start: the reference's RUN
+    loop (tests/golden/still_water_bt_dp0.02.npz) against the oracle."""
+    g = np.load(os.path.join(HERE, "golden", "still_water_bt_dp0.02.npz"))
+    case = cases.still_water_bt(dp=0.02)
+    o = O.PortBt.from_case(case)
+    done = 0
+    for n in g["snaps"]:
+        o.step(O.ORC_BT, float(g["dt"]), int(n) - done)
+        done = int(n)
+        st = o.state()
+        assert np.array_equal(st["index"], g[f"step{n}_index"])
+        for f in ("r", "v", "rho", "p", "a", "drho"):
+            assert _rel(st[f], g[f"step{n}_{f}"]) <= 1e-10, (int(n), f)
