@@ -260,6 +260,17 @@ def _perturbed_walls(case, u):
     return case
 
 
+def main_dbc():
+    """cases/damBreakLong_DBC: the DBC interaction on the dam break (mDBC
+    walls, hydrostatic column), per-function outputs and 6 steps of the RUN
+    loop from a seeded perturbed state (own seed)."""
+    if O.build_ref() is None or not O.ref_available():
+        raise SystemExit("reference harness not available (needs the reference sources)")
+    rng = np.random.default_rng(SEED + 7)
+    out = run_case(cases.dam_break_dbc(dp=0.02), 1, 6, rng, 2)
+    np.savez_compressed(os.path.join(HERE, "dam_break_dbc_dp0.02.npz"), **out)
+
+
 def main_zones():
     """Open boundaries: cases/inflowSlab_mDBC (the case's own RUN loop with
     BZ_Integrate_inlet / _outlet), an outlet channel that exercises the
@@ -342,6 +353,9 @@ def main():
     if len(sys.argv) > 1 and sys.argv[1] == "zones":
         main_zones()
         return
+    if len(sys.argv) > 1 and sys.argv[1] == "dbc":
+        main_dbc()
+        return
     if O.build_ref() is None or not O.ref_available():
         raise SystemExit("reference harness not available (needs the reference sources)")
     rng = np.random.default_rng(SEED)
@@ -369,6 +383,8 @@ def main():
     main_bt()
     # 8. open boundaries
     main_zones()
+    # 9. dam break, DBC flavour
+    main_dbc()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

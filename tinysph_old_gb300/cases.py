@@ -1,5 +1,6 @@
-"""Case builders: the dam break with mDBC walls and the still-water tank with
-DBC walls, with the constants of the reference's case drivers.
+"""Case builders with the constants of the reference's case drivers: dam
+breaks with mDBC, DBC and boundary-integral walls, still water with DBC and
+boundary-integral walls, the ALE-SPH dam break, and open-boundary cases.
 
 A case is a :class:`Case`: particles in the reference's order, the SPH
 constants of ``SPH_constants`` (``src/SPH_data.h:124-140``), the padded domain
@@ -83,6 +84,28 @@ def dam_break_mdbc(dp: float = 0.005, cs: float = 34.3, wall_height: float = 1.0
                 domain=_pad(x_0, x_1, y_0, y_1, nvl, dp), wall_model=WALL_MDBC,
                 dt=dt, meta=dict(nvl=nvl, wall_height=wall_height, tank_length=L,
                                  column=tuple(column)))
+
+
+def dam_break_dbc(dp: float = 0.005, dt: float | None = None) -> Case:
+    """Dam break with DBC walls: ``cases/damBreakLong_DBC/constants.h`` and
+    ``geometry.h`` (the walls of the mDBC case, whose ghost nodes the DBC
+    interaction of src/SPH_interactionDBC.h does not use; a hydrostatic
+    column, Create_Block_of_FluidWP, 0.6 x 0.3 m).  Reference values: dp =
+    0.005, h = sqrt(2 dp^2), kap = 2.1, cs = 34.3, visco = 0.02, delta = 0.1,
+    dt = 5e-5 (scaled with dp here), walls to y = 1.0 m, domain [0, 2] x [0, 1].
+    """
+    base = dam_break_mdbc(dp=dp, dt=dt)
+    ps = geo.ParticleSet(dp, base.h, base.kap, base.cs)
+    L = 1.61
+    geo.create_wall_x_mdbc(ps, 0.0 + dp, L, 0.0, -1, dp / 2)
+    geo.create_wall_y_mdbc(ps, 0.0, 0 + dp, 1.0, -1, dp / 2)
+    geo.create_wall_y_mdbc(ps, L, 0 + dp, 1.0, +1, L - dp / 2)
+    geo.create_corner_mdbc(ps, -1, -1, (0.0 + dp / 2, 0.0 + dp / 2))
+    geo.create_corner_mdbc(ps, +1, -1, (L - dp / 2, 0.0 + dp / 2))
+    geo.create_block_of_fluid_wp(ps, 0 + dp, 0 + dp, 0.6, 0.3)
+    return Case(name=f"dam_break_dbc_dp{dp:g}", particles=ps, h=base.h, kap=base.kap,
+                cs=base.cs, rho0=1000.0, visco=0.02, delta=0.1, dp=dp, domain=base.domain,
+                wall_model=WALL_DBC, dt=base.dt, meta=dict(base.meta))
 
 
 def still_water_dbc(dp: float = 0.005, width: float = 0.5, depth: float = 0.3,
