@@ -263,12 +263,17 @@ def _perturbed_walls(case, u):
 def main_dbc():
     """cases/damBreakLong_DBC: the DBC interaction on the dam break (mDBC
     walls, hydrostatic column), per-function outputs and 6 steps of the RUN
-    loop from a seeded perturbed state (own seed)."""
+    loop from a seeded perturbed state (own seed); cases/stillWater_mDBC the
+    same way."""
     if O.build_ref() is None or not O.ref_available():
         raise SystemExit("reference harness not available (needs the reference sources)")
     rng = np.random.default_rng(SEED + 7)
     out = run_case(cases.dam_break_dbc(dp=0.02), 1, 6, rng, 2)
     np.savez_compressed(os.path.join(HERE, "dam_break_dbc_dp0.02.npz"), **out)
+    # cases/stillWater_mDBC (h = 2 dp: ~50 neighbours), same recipe, own seed
+    rng = np.random.default_rng(SEED + 8)
+    out = run_case(cases.still_water_mdbc(dp=0.02), 0, 6, rng, 2)
+    np.savez_compressed(os.path.join(HERE, "still_water_mdbc_dp0.02.npz"), **out)
 
 
 def main_zones():

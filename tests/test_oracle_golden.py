@@ -29,6 +29,7 @@ def _port_from_golden(O, case, g):
     ("dam_break_mdbc_dp0.02.npz", lambda: cases.dam_break_mdbc(dp=0.02), 0),
     ("still_water_dbc_dp0.02.npz", lambda: cases.still_water_dbc(dp=0.02), 1),
     ("dam_break_dbc_dp0.02.npz", lambda: cases.dam_break_dbc(dp=0.02), 1),
+    ("still_water_mdbc_dp0.02.npz", lambda: cases.still_water_mdbc(dp=0.02), 0),
 ])
 def test_oracle_matches_reference_golden(oracle_mod, fname, builder, model):
     O = oracle_mod

@@ -1,6 +1,7 @@
 """Case builders with the constants of the reference's case drivers: dam
-breaks with mDBC, DBC and boundary-integral walls, still water with DBC and
-boundary-integral walls, the ALE-SPH dam break, and open-boundary cases.
+breaks with mDBC, DBC and boundary-integral walls, still water with mDBC,
+DBC and boundary-integral walls, the ALE-SPH dam break, and open-boundary
+cases.
 
 A case is a :class:`Case`: particles in the reference's order, the SPH
 constants of ``SPH_constants`` (``src/SPH_data.h:124-140``), the padded domain
@@ -106,6 +107,33 @@ def dam_break_dbc(dp: float = 0.005, dt: float | None = None) -> Case:
     return Case(name=f"dam_break_dbc_dp{dp:g}", particles=ps, h=base.h, kap=base.kap,
                 cs=base.cs, rho0=1000.0, visco=0.02, delta=0.1, dp=dp, domain=base.domain,
                 wall_model=WALL_DBC, dt=base.dt, meta=dict(base.meta))
+
+
+def still_water_mdbc(dp: float = 0.02, dt: float | None = None) -> Case:
+    """Still water with mDBC walls: ``cases/stillWater_mDBC/constants.h`` and
+    ``geometry.h`` (tank 0.8 m wide, walls to 1 m, a hydrostatic block
+    0.8 - 2 dp wide and 0.5 m deep, Create_Block_of_FluidWP).  Reference
+    values: dp = 0.02, h = 2 dp, kap = 2.1, cs = 42.48, visco = 0.01,
+    delta = 0.1, dt = 2e-4 (scaled with dp here), domain [0, 1] x [0, 1]."""
+    x_0, x_1, y_0, y_1 = 0.0, 1.0, 0.0, 1.0
+    kap = 2.1
+    hh = 2.0 * dp
+    if dt is None:
+        dt = 0.0002 * (dp / 0.02)
+    cs = 42.48
+    nvl = int(math.ceil(kap * hh / dp))
+    ps = geo.ParticleSet(dp, hh, kap, cs)
+    W = 0.8
+    geo.create_wall_x_mdbc(ps, 0.0 + dp, W - dp, 0.0, -1, dp / 2)
+    geo.create_wall_y_mdbc(ps, 0.0, 0 + dp, 1.0, -1, dp / 2)
+    geo.create_wall_y_mdbc(ps, W, 0 + dp, 1.0, +1, W - dp / 2)
+    geo.create_corner_mdbc(ps, -1, -1, (0.0 + dp / 2, 0.0 + dp / 2))
+    geo.create_corner_mdbc(ps, +1, -1, (W - dp / 2, 0.0 + dp / 2))
+    geo.create_block_of_fluid_wp(ps, 0 + dp, 0 + dp, W - dp, 0.5)
+    return Case(name=f"still_water_mdbc_dp{dp:g}", particles=ps, h=hh, kap=kap, cs=cs,
+                rho0=1000.0, visco=0.01, delta=0.1, dp=dp,
+                domain=_pad(x_0, x_1, y_0, y_1, nvl, dp), wall_model=WALL_MDBC, dt=dt,
+                meta=dict(nvl=nvl, depth=0.5))
 
 
 def still_water_dbc(dp: float = 0.005, width: float = 0.5, depth: float = 0.3,
