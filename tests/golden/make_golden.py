@@ -198,6 +198,9 @@ def main_ale():
     fo = run_ale(cases.dam_break_ale(dp=0.02), 6, np.random.default_rng(SEED + 2), 2,
                  first_order=True)
     np.savez_compressed(os.path.join(HERE, "dam_break_ale_first_order_dp0.02.npz"), **fo)
+    # cases/ALESPH_stillWater (hydrostatic start, h = 2 dp), the MUSCL.h RUN loop
+    sw = run_ale(cases.still_water_ale(dp=0.02), 6, np.random.default_rng(SEED + 9), 2)
+    np.savez_compressed(os.path.join(HERE, "still_water_ale_dp0.02.npz"), **sw)
 
 
 def main_bt():

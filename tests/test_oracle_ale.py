@@ -149,3 +149,29 @@ def test_first_order_oracle_matches_reference_golden(oracle_mod):
         st = P2.ale_state()
         for f in FIELDS:
             assert np.array_equal(st[f], g[f"step{k}_{f}"]), (k, f)
+
+
+def test_ale_still_water_matches_reference_golden(oracle_mod):
+    """cases/ALESPH_stillWater (the stillWater_BT tank, hydrostatic start,
+    h = 2 dp): per-function outputs and 6 steps of the MUSCL.h RUN loop from a
+    seeded perturbation, bit for bit (tests/golden/still_water_ale_dp0.02.npz)."""
+    O = oracle_mod
+    g = np.load(os.path.join(GOLD, "still_water_ale_dp0.02.npz"))
+    case = cases.still_water_ale(dp=0.02)
+    P = _port(O, case, g)
+    st = P.ale_state()
+    for k in ("r", "v", "rho", "omega", "omegarho", "omegav"):
+        assert np.array_equal(st[k], g[f"init_{k}"]), k
+    P.density_to_pressure()
+    P.gradient()
+    P.ale_forces(float(g["dt"]))
+    st = P.ale_state()
+    for k in ("grad", "domega", "domegarho", "domegav"):
+        assert np.array_equal(st[k], g[f"forces_{k}"]), k
+    P2 = _port(O, case, g)
+    every = int(g["snap_every"])
+    for k in range(every, int(g["nsteps"]) + 1, every):
+        P2.ale_step(float(g["dt"]), k - every, every)
+        st = P2.ale_state()
+        for f in FIELDS:
+            assert np.array_equal(st[f], g[f"step{k}_{f}"]), (k, f)

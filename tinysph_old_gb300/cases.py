@@ -260,6 +260,16 @@ def still_water_bt(dp: float = 0.02) -> Case:
                 meta=dict(nvl=nvl, nwalls=nw, depth=0.5))
 
 
+def still_water_ale(dp: float = 0.02) -> Case:
+    """Riemann / ALE-SPH still water: ``cases/ALESPH_stillWater/constants.h``
+    and ``geometry.h``, the tank, walls, hydrostatic block and constants of
+    ``cases/stillWater_BT`` (h = 2 dp, cs = 42.48, visco = 0.01, dt = 2e-4)
+    run by the ALE driver."""
+    c = still_water_bt(dp)
+    c.name = f"still_water_ale_dp{dp:g}"
+    return c
+
+
 def inflow_slab_mdbc(dp: float = 0.005, dt: float | None = None) -> Case:
     """Flow from an inlet over a step, mDBC walls, open boundaries:
     ``cases/inflowSlab_mDBC/constants.h`` and ``geometry.h`` (inlet buffer
