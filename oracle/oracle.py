@@ -100,7 +100,7 @@ def _load_port():
         L.orc_add_zone.restype = _I
         L.orc_bz_inlet.argtypes = [_P, _I, _D]
         L.orc_bz_outlet.argtypes = [_P, _I, _D]
-        L.orc_step_zones.argtypes = [_P, _D, _I]
+        L.orc_step_zones.argtypes = [_P, _I, _D, _I]
         L.orc_pair_digest.argtypes = [_P, _IP, np.ctypeslib.ndpointer(dtype=np.int64, flags='C_CONTIGUOUS'), _IP]
         L.orc_water_level.argtypes = [_P, _D, _D, _I]
         L.orc_water_level.restype = _D
@@ -217,10 +217,10 @@ class PortSystem(_Base):
             o.particle_to_cell()
         return o
 
-    def step_zones(self, dt, n=1):
+    def step_zones(self, dt, n=1, model=0):
         """RUN of cases/inflowSlab_mDBC (mDBC step with the zones' inlet and
-        outlet after the predictor)."""
-        self.L.orc_step_zones(self.s, dt, int(n))
+        outlet after the predictor); model 2 (BT) is cases/flowDrop_BT."""
+        self.L.orc_step_zones(self.s, int(model), dt, int(n))
 
     def __del__(self):
         try:
@@ -733,6 +733,10 @@ def _load_ref_bt():
                   "refbt_wall_density", "refbt_forces"):
             getattr(L, f).argtypes = [_P]
         L.refbt_step.argtypes = [_P, _D, _I]
+        L.refbt_add_zone.argtypes = [_P, _D, _D, _D, _D, _I, _D, _D, _D, _D, _I]
+        L.refbt_create_inlet_x.argtypes = [_P, _D, _D, _D, _I, _I, _D, _D, _I]
+        L.refbt_create_outlet_y.argtypes = [_P, _D, _D, _D, _I, _I, _D, _D, _I, _I]
+        L.refbt_step_zones.argtypes = [_P, _D, _I]
         _ref_bt = L
     return _ref_bt
 
@@ -764,10 +768,18 @@ class RefBt:
                                    ps.vx[i], ps.vy[i])
         for n in ps.normals:
             o.L.refbt_add_normal(o.s, n[0], n[1])
+        for z in case.meta.get("zones", []):
+            o.L.refbt_add_zone(o.s, z["x0"], z["xm"], z["y0"], z["ym"], z["nbl"], z["vx"],
+                               z["vy"], z["ox"], z["oy"], z["btype"])
         if divide:
             o.L.refbt_divide_to_cells(o.s)
             o.L.refbt_particle_to_cell(o.s)
         return o
+
+    def step_zones(self, dt, n=1):
+        """RUN of cases/flowDrop_BT (the BT step with the zones' inlet and
+        outlet after the predictor)."""
+        self.L.refbt_step_zones(self.s, dt, int(n))
 
     @classmethod
     def generated(cls, case, dp, L=1.61, wall_height=1.0, column=(0.6, 0.3)):

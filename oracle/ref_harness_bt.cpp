@@ -5,7 +5,8 @@
 // oracle/_ref/libtsph_ref_bt.so.  A translation unit of its own because
 // src/SPH_interactionBT.h defines Compute_Forces(Particle_system&) beside the
 // other flavours.  Calls the functions of
-// cases/damBreakLong_BT/SPH_simulationSymplectic.h in its RUN order.
+// cases/damBreakLong_BT/SPH_simulationSymplectic.h in its RUN order, and of
+// cases/flowDrop_BT/SPH_simulationSymplectic.h (the same with buffer zones).
 
 #include "SPH_defs.h"
 #include "SPH_particle_system.h"
@@ -16,6 +17,8 @@
 #include "ALESPH_create.h"
 #include "SPH_BT.h"
 #include "SPH_btdebug.h"
+#include "SPH_inlet_outlet_data.h"
+#include "SPH_buffer_zones.h"
 
 #include <iostream>
 #include <sstream>
@@ -132,6 +135,47 @@ void refbt_step(void *c, double dt, int n) {
         BT_compute_density_BTGeo(P, K(c)->sim);
         Density_to_pressure(P);
         Integrate_SymplecticPredictor(P, dt);
+        Clear_cells(P);
+        Particle_To_Cell(P, K(c)->sim);
+        Density_to_pressure(P);
+        Compute_Forces(P);
+        Integrate_SymplecticCorrector(P, dt);
+        RemoveParticlesOutOfDomain(P, K(c)->sim);
+        Clear_cells(P);
+        Particle_To_Cell(P, K(c)->sim);
+        Density_to_pressure(P);
+        Compute_Forces(P);
+    }
+}
+
+// buffer zones (the BufferZone constructor of src/SPH_inlet_outlet_data.h)
+void refbt_add_zone(void *c, double x0, double xm, double y0, double ym, int nbl, double vx,
+                    double vy, double ox, double oy, int btype) {
+    K(c)->particles.zones.push_back(
+        BufferZone(x0, xm, y0, ym, nbl, TDouble2(vx, vy), TDouble2(ox, oy), btype));
+}
+void refbt_create_inlet_x(void *c, double y, double x0, double x1, int o, int nbl, double vx,
+                          double vy, int type) {
+    Quiet q;
+    DRAW_CreateInletX(K(c)->particles, y, x0, x1, o, nbl, TDouble2(vx, vy), type);
+}
+void refbt_create_outlet_y(void *c, double x, double y0, double y1, int o, int nbl, double vx,
+                           double vy, int type, int empty) {
+    Quiet q;
+    DRAW_CreateOutletY(K(c)->particles, x, y0, y1, o, nbl, TDouble2(vx, vy), type, empty != 0);
+}
+// the body of SPH_simulation::RUN of cases/flowDrop_BT/SPH_simulationSymplectic.h
+void refbt_step_zones(void *c, double dt, int n) {
+    Quiet q;
+    Particle_system &P = K(c)->particles;
+    for (int k = 0; k < n; k++) {
+        BT_compute_density_BTGeo(P, K(c)->sim);
+        Density_to_pressure(P);
+        Integrate_SymplecticPredictor(P, dt);
+        for (int z = 0; z < (int)P.zones.size(); z++) {  // inlets, then outlets, by zone
+            if (P.zones[z].btype >= outlet) BZ_Integrate_outlet(P, z, dt);
+            else BZ_Integrate_inlet(P, z, dt);
+        }
         Clear_cells(P);
         Particle_To_Cell(P, K(c)->sim);
         Density_to_pressure(P);

@@ -78,7 +78,7 @@ void orc_bz_outlet(orc_sys *s, int zone, double dt);
  * SPH_simulationSymplectic.h: the mDBC step with every zone's
  * BZ_Integrate_inlet (types 6-10) or BZ_Integrate_outlet (11-15), in zone
  * order, after the predictor */
-void orc_step_zones(orc_sys *s, double dt, int nsteps);
+void orc_step_zones(orc_sys *s, int model, double dt, int nsteps);
 void orc_bt_density(orc_sys *s);
 void orc_predictor(orc_sys *s, double dt);
 void orc_corrector(orc_sys *s, double dt);

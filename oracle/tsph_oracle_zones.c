@@ -106,9 +106,14 @@ void orc_bz_outlet(orc_sys *s, int zone, double dt) {
     s->cells_built = 0;
 }
 
-void orc_step_zones(orc_sys *s, double dt, int nsteps) {
+/* The RUN body of the cases with buffer zones (cases/inflowSlab_mDBC,
+ * cases/flowDrop_mDBC with mDBC walls, cases/flowDrop_BT with
+ * boundary-integral walls: BT_compute_density_BTGeo and the BT
+ * Compute_Forces), every zone's inlet or outlet after the predictor. */
+void orc_step_zones(orc_sys *s, int model, double dt, int nsteps) {
     for (int k = 0; k < nsteps; k++) {
-        orc_mdbc_density(s);
+        if (model == ORC_BT) orc_bt_density(s);
+        else orc_mdbc_density(s);
         orc_density_to_pressure(s);
         orc_predictor(s, dt);
         for (int z = 0; z < s->nzones; z++) {  /* the cases call inlets, then outlets, by zone */
@@ -118,12 +123,12 @@ void orc_step_zones(orc_sys *s, double dt, int nsteps) {
         orc_clear_cells(s);
         orc_particle_to_cell(s);
         orc_density_to_pressure(s);
-        orc_compute_forces(s, ORC_MDBC);
+        orc_compute_forces(s, model);
         orc_corrector(s, dt);
         orc_remove_out_of_domain(s);
         orc_clear_cells(s);
         orc_particle_to_cell(s);
         orc_density_to_pressure(s);
-        orc_compute_forces(s, ORC_MDBC);
+        orc_compute_forces(s, model);
     }
 }

@@ -325,6 +325,32 @@ def flow_drop_mdbc(dp: float = 0.005, dt: float | None = None) -> Case:
                 meta=dict(nvl=nvl, nwalls=nw, zones=zones))
 
 
+def flow_drop_bt(dp: float = 0.005, dt: float | None = None) -> Case:
+    """The falling jet of ``cases/flowDrop_BT`` (``constantsBT.h``,
+    ``geometry.h``): one boundary-integral floor from x = -2 dp to 2 + 2 dp
+    with normal (0, 1), the inlet and the two outlets of flowDrop_mDBC.
+    Reference values: dp = 0.005, h = sqrt(2 dp^2), kap = 2.1, cs = 34.3,
+    visco = 0.02, delta = 0.1, dt = 4e-5 (scaled with dp here)."""
+    x_0, x_1, y_0, y_1 = 0.0, 2.0, 0.0, 1.0
+    kap = 2.1
+    hh = 1.0 * math.sqrt(2 * dp * dp)
+    if dt is None:
+        dt = 0.00004 * (dp / 0.005)
+    cs = 34.3
+    nvl = int(math.ceil(kap * hh / dp))
+    ps = geo.AleParticleSet(dp, hh, kap, cs)
+    geo.create_wall_x_bt(ps, 0.0 - dp * 2, 2.0 + dp * 2, 0.0, -1, (0.0, 1.0))
+    nw = ps.np
+    zones = [geo.create_inlet_x(ps, 0.3 + 4 * dp, 0.8 + dp, 1.0, +1, 4, (0.0, -3.0), geo.INLET1),
+             geo.create_outlet_y(ps, 1.3 - 4 * dp, 0.0 + dp, 0.2, +1, 4, (2.0, 0.0), geo.OUTLET1),
+             geo.create_outlet_y(ps, 0.5, 0.0 + dp, 0.2, -1, 4, (-2.0, 0.0), geo.OUTLET2)]
+    ps.gnr = list(ps.normals)
+    return Case(name=f"flow_drop_bt_dp{dp:g}", particles=ps, h=hh, kap=kap, cs=cs,
+                rho0=1000.0, visco=0.02, delta=0.1, dp=dp,
+                domain=_pad(x_0, x_1, y_0, y_1, nvl, dp), wall_model=WALL_BT, dt=dt,
+                meta=dict(nvl=nvl, nwalls=nw, zones=zones))
+
+
 def outlet_channel_mdbc(dp: float = 0.005, speed: float = 2.0) -> Case:
     """A fluid slab driven along a floor into an outlet zone (no counterpart
     case in the reference; it exercises BZ_Integrate_outlet's retyping and
