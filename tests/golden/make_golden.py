@@ -305,6 +305,38 @@ def main_dbc():
     np.savez_compressed(os.path.join(HERE, "still_water_mdbc_dp0.02.npz"), **out)
 
 
+def main_inflow_tank_bottom():
+    """cases/inflowTankBottom_mDBC at dp = 0.02: the reference's generators
+    and its RUN loop (the mDBC step with the inlet after the predictor)."""
+    O.RefSystem.set_threads(1)
+    dp = 0.02
+    case = cases.inflow_tank_bottom_mdbc(dp=dp)
+    G = O.RefSystem(case.h, case.kap, case.cs, case.rho0, case.visco, case.delta, case.dp,
+                    case.domain)
+    L, s = G.L, G.s
+    L.ref_create_wall_x_mdbc(s, 0.2 + dp, 1.2 - dp, 0.0, -1, dp / 2)
+    L.ref_create_wall_y_mdbc(s, 0.2, 0 + dp, 0.4, -1, dp / 2)
+    L.ref_create_wall_y_mdbc(s, 1.2, 0 + dp, 0.8, +1, 1.2 - dp / 2)
+    L.ref_create_corner_mdbc(s, -1, -1, 0.2 + dp / 2, 0.0 + dp / 2)
+    L.ref_create_corner_mdbc(s, +1, -1, 1.2 - dp / 2, 0.0 + dp / 2)
+    L.ref_create_wall_x_mdbc(s, 0.0 + dp, 0.4, 0.4 + 3 * dp, -1, dp / 2)
+    L.ref_create_block_of_fluid_wp(s, 0.2 + dp, 0 + dp, 1.2, 0.15)
+    L.ref_create_inlet_y(s, 0.1, 0.4 + 4 * dp, 0.5, -1, 4, 1.5, 0.0, 7)
+    g = G.state()
+    out = {f"geom_{k}": g[k] for k in ("r", "v", "rho", "p", "type")}
+    out["dt"] = np.float64(case.dt)
+    out["snaps"] = np.array([500, 1000, 1500])
+    R = O.RefSystem.from_case(case)
+    done = 0
+    for n in out["snaps"]:
+        R.step_zones(case.dt, int(n) - done)
+        done = int(n)
+        st = R.state()
+        for k in ("r", "v", "rho", "p", "type"):
+            out[f"step{n}_{k}"] = st[k]
+    np.savez_compressed(os.path.join(HERE, "inflow_tank_bottom_mdbc_dp0.02.npz"), **out)
+
+
 def main_zones():
     """Open boundaries: cases/inflowSlab_mDBC (the case's own RUN loop with
     BZ_Integrate_inlet / _outlet), an outlet channel that exercises the
@@ -390,6 +422,9 @@ def main():
     if len(sys.argv) > 1 and sys.argv[1] == "dbc":
         main_dbc()
         return
+    if len(sys.argv) > 1 and sys.argv[1] == "tank_bottom":
+        main_inflow_tank_bottom()
+        return
     if O.build_ref() is None or not O.ref_available():
         raise SystemExit("reference harness not available (needs the reference sources)")
     rng = np.random.default_rng(SEED)
@@ -419,6 +454,8 @@ def main():
     main_zones()
     # 9. dam break, DBC flavour
     main_dbc()
+    # 10. inflow over a ledge into a tank (open boundary, mDBC)
+    main_inflow_tank_bottom()
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -60,3 +60,23 @@ def test_flow_drop_bt_matches_the_reference():
         assert np.array_equal(st["type"], g[f"step{n}_type"]), n
         for f in ("r", "v", "rho", "p", "a", "drho"):
             assert np.array_equal(st[f], g[f"step{n}_{f}"]), (int(n), f)
+
+
+def test_inflow_tank_bottom_matches_the_reference():
+    """cases/inflowTankBottom_mDBC (an inlet feeding a ledge above a tank): the
+    case generator against the reference's generators and the RUN loop bit
+    for bit over 1500 steps (tests/golden/inflow_tank_bottom_mdbc_dp0.02.npz)."""
+    g = np.load(os.path.join(HERE, "golden", "inflow_tank_bottom_mdbc_dp0.02.npz"))
+    case = cases.inflow_tank_bottom_mdbc(dp=0.02)
+    a = case.particles.arrays()
+    for k in ("r", "v", "rho", "p", "type"):
+        assert np.array_equal(a[k], g[f"geom_{k}"]), k
+    P = O.PortSystem.from_case(case)
+    done = 0
+    for n in g["snaps"]:
+        P.step_zones(float(g["dt"]), int(n) - done)
+        done = int(n)
+        st = P.state()
+        assert np.array_equal(st["type"], g[f"step{n}_type"]), n
+        for f in ("r", "v", "rho", "p"):
+            assert np.array_equal(st[f], g[f"step{n}_{f}"]), (int(n), f)

@@ -325,6 +325,37 @@ def flow_drop_mdbc(dp: float = 0.005, dt: float | None = None) -> Case:
                 meta=dict(nvl=nvl, nwalls=nw, zones=zones))
 
 
+def inflow_tank_bottom_mdbc(dp: float = 0.005, dt: float | None = None) -> Case:
+    """Inflow over a ledge into a tank, mDBC walls:
+    ``cases/inflowTankBottom_mDBC/constants.h`` and ``geometry.h`` (tank
+    floor x in (0.2, 1.2), left wall to 0.4 m, right wall to 0.8 m, a ledge
+    at y = 0.4 + 3 dp from x = dp to 0.4, a hydrostatic layer 0.15 m deep in
+    the tank, an inlet at x = 0.1 between y = 0.4 + 4 dp and 0.5 blowing +x
+    at 1.5 m/s).  Reference values: dp = 0.005, h = sqrt(2 dp^2), kap = 2.1,
+    cs = 34.3, visco = 0.02, delta = 0.1, dt = 5e-5 (scaled with dp here)."""
+    x_0, x_1, y_0, y_1 = 0.0, 2.0, 0.0, 1.0
+    kap = 2.1
+    hh = 1.0 * math.sqrt(2 * dp * dp)
+    if dt is None:
+        dt = 0.00005 * (dp / 0.005)
+    cs = 34.3
+    nvl = int(math.ceil(kap * hh / dp))
+    ps = geo.ParticleSet(dp, hh, kap, cs)
+    geo.create_wall_x_mdbc(ps, 0.2 + dp, 1.2 - dp, 0.0, -1, dp / 2)
+    geo.create_wall_y_mdbc(ps, 0.2, 0 + dp, 0.4, -1, dp / 2)
+    geo.create_wall_y_mdbc(ps, 1.2, 0 + dp, 0.8, +1, 1.2 - dp / 2)
+    geo.create_corner_mdbc(ps, -1, -1, (0.2 + dp / 2, 0.0 + dp / 2))
+    geo.create_corner_mdbc(ps, +1, -1, (1.2 - dp / 2, 0.0 + dp / 2))
+    geo.create_wall_x_mdbc(ps, 0.0 + dp, 0.4, 0.4 + 3 * dp, -1, dp / 2)
+    nw = ps.np
+    geo.create_block_of_fluid_wp(ps, 0.2 + dp, 0 + dp, 1.2, 0.15)
+    zones = [geo.create_inlet_y(ps, 0.1, 0.4 + 4 * dp, 0.5, -1, 4, (1.5, 0.0), geo.INLET1)]
+    return Case(name=f"inflow_tank_bottom_mdbc_dp{dp:g}", particles=ps, h=hh, kap=kap, cs=cs,
+                rho0=1000.0, visco=0.02, delta=0.1, dp=dp,
+                domain=_pad(x_0, x_1, y_0, y_1, nvl, dp), wall_model=WALL_MDBC, dt=dt,
+                meta=dict(nvl=nvl, nwalls=nw, zones=zones))
+
+
 def flow_drop_bt(dp: float = 0.005, dt: float | None = None) -> Case:
     """The falling jet of ``cases/flowDrop_BT`` (``constantsBT.h``,
     ``geometry.h``): one boundary-integral floor from x = -2 dp to 2 + 2 dp
