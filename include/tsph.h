@@ -150,17 +150,24 @@ int tsph_get_cells(tsph_system *s, int32_t *cell_start, int32_t *cell_list);
  * device memory comes only from their own pool (e.g. a host framework that
  * binds this library through its FFI) or whose time loop must not call
  * cudaMalloc/cudaFree (they synchronise the device).  The caller passes device
- * buffers: r_dev (double[2n] positions), cell_start_dev (int32[ncx*ncy+1]) and
- * cell_list_dev (int32[n]); the result is the reference's cells[c].cp as CSR
- * (ascending particle index in each cell) for the grid of Divide_To_Cells.
+ * buffers: r_dev (double[2n] positions, x and y of each particle; 8-byte
+ * aligned), cell_start_dev (int32[ncx*ncy+1]) and cell_list_dev (int32[n]),
+ * both 4-byte aligned (misaligned pointers: TSPH_ERR_ARG before any work is
+ * queued); the result is the reference's cells[c].cp as CSR (ascending
+ * particle index in each cell) for the grid of Divide_To_Cells.
  * The counting sort's working memory is one static device array of about
  * 16.1 MB inside the library (held by every GPU that loads it until exit), so
  * n <= 1048576, ncx*ncy <= 1048576 and ncx, ncy <= 8192; larger sizes return
+ * TSPH_ERR_ARG.  A cell may hold at most 4096 particles (a cell's ordering
+ * cost grows with the square of its occupancy); a fuller cell returns
  * TSPH_ERR_ARG.  No allocation of any kind happens on the device.  The first
- * call on a device looks up that array's address; make it before any stream
- * capture.  Calls share the array and keep its last contents (each call clears
+ * call on a device looks up that array's address and caches it for the
+ * process; make it before any stream capture, and do not call this entry
+ * point again after resetting the device (cudaDeviceReset) in the same
+ * process.  Calls share the array and keep its last contents (each call clears
  * what must start at zero); calls that overlap on the GPU race, so the call
- * runs on `stream` (NULL = default stream) and waits for it before returning.
+ * runs on `stream` (NULL = default stream) and waits for it before returning
+ * (also when it fails after queueing work).
  * Particles outside the grid are left out and TSPH_ERR_ESCAPED is returned;
  * n_binned (may be NULL) receives the number of particles in the lists. */
 int tsph_particle_to_cell_noalloc(const tsph_constants *c, const tsph_domain *d, int n,

@@ -53,6 +53,25 @@ def test_oracle_gradients_match_central_differences():
         assert abs(fd - gf[k]) <= 1e-4 * max(1e-6, abs(fd) + abs(gf[k])), (k, fd, gf[k])
 
 
+def test_package_parameter_layout_matches_the_oracle():
+    """The package's own layout and initial weights (gnn_params) agree block by
+    block with the oracle's independent statement of the network."""
+    from tinysph_old_gb300 import gnn_params as GP
+
+    assert [(n, tuple(s)) for n, s in GP.param_shapes()] == \
+        [(n, tuple(s)) for n, s in G.param_shapes()]
+    assert GP.n_params() == G.n_params() == 50819
+    for seed in (0, 3):
+        ours = GP.initial_params(seed)
+        theirs = G.flatten(G.init_params(seed)).astype(np.float32)
+        assert ours.dtype == np.float32
+        np.testing.assert_array_equal(ours, theirs)
+    flat = np.arange(GP.n_params(), dtype=np.float64)
+    back = GP.unflatten(flat)
+    np.testing.assert_array_equal(GP.flatten(back, dtype=np.float64), flat)
+    np.testing.assert_array_equal(G.flatten(G.unflatten(flat)), flat)
+
+
 @pytest.mark.gpu
 def test_exported_graph_is_the_symmetric_pair_set(gpu_tsph):
     from tinysph_old_gb300 import surrogate as S

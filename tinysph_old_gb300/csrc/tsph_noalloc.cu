@@ -11,18 +11,28 @@
 // that working memory in one file-scope device array, g_noalloc_scratch,
 // sized for at most kNoAllocMaxParticles particles, kNoAllocMaxCells cells and
 // kNoAllocMaxAxis cells per axis (about 16.1 MB, held by every GPU that loads
-// the library until the process exits).
+// the library until the process exits).  A cell may hold at most
+// kNoAllocMaxPerCell particles: each particle's place in its cell is its rank
+// among the cell's members, found by one pass over them, so a cell's cost
+// grows with the square of its occupancy (SPH spacing puts about ten
+// particles in a cell); a call with a fuller cell returns TSPH_ERR_ARG.
 //
 // Rules of use:
 //  * The first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress, with that device current) and caches it; make the
-//    first call on each device outside any stream capture.
+//    first call on each device outside any stream capture.  The cached
+//    address belongs to the device's current context: a caller that resets
+//    the device (cudaDeviceReset) must not call this entry point again in
+//    the same process.
 //  * Every call shares the one array.  A call clears what must start at zero,
 //    runs on the caller's stream and waits for it before returning; calls that
 //    overlap on the GPU (e.g. from several host threads, or while another
 //    stream still runs an earlier call's work) race on the array.  Calls made
 //    through this entry point are serialised by a host mutex.
 //  * The array keeps the last call's contents.
+//  * Positions are read as two doubles per particle (8-byte alignment, the
+//    alignment of any double array); misaligned pointers are refused before
+//    anything is queued.
 #include <cuda_runtime.h>
 
 #include <mutex>
@@ -38,6 +48,7 @@ constexpr int kNoAllocMaxParticles = 1 << 20;
 constexpr int kNoAllocMaxCells = 1 << 20;
 constexpr int kNoAllocMaxAxis = 8192;
 constexpr int kNoAllocMaxDevices = 64;
+constexpr int kNoAllocMaxPerCell = 4096;
 
 // layout of the scratch array (byte offsets, each 256-byte aligned)
 constexpr size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -50,7 +61,8 @@ constexpr size_t kMaxTiles = ((size_t)kNoAllocMaxCells + 1 + tsph::kScanTile - 1
 constexpr size_t kOffBx = align256(kOffTiles + 4 * kMaxTiles);                      // i64[axis+1]
 constexpr size_t kOffBy = align256(kOffBx + 8 * ((size_t)kNoAllocMaxAxis + 1));      // i64[axis+1]
 constexpr size_t kOffEscaped = align256(kOffBy + 8 * ((size_t)kNoAllocMaxAxis + 1));  // u32
-constexpr size_t kScratchBytes = align256(kOffEscaped + 4);
+constexpr size_t kOffCrowded = kOffEscaped + 4;                                       // u32
+constexpr size_t kScratchBytes = align256(kOffCrowded + 4);
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 
@@ -82,13 +94,14 @@ int scratch_address(unsigned char **out) {
 }
 
 // cell and histogram slot of particle i; outside the grid: not binned
-__global__ void k_na_bin(const double2 *__restrict__ r, int n, tsph::Grid g,
+__global__ void k_na_bin(const double *__restrict__ r, int n, tsph::Grid g,
                          uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
                          uint32_t *__restrict__ counts, uint32_t *__restrict__ escaped) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     int cx, cy;
-    const uint32_t k = tsph::cell_key(g, r[i], 0xffffffffu, &cx, &cy);
+    const double2 ri = make_double2(r[2 * (size_t)i], r[2 * (size_t)i + 1]);
+    const uint32_t k = tsph::cell_key(g, ri, 0xffffffffu, &cx, &cy);
     key[i] = k;
     if (k == (uint32_t)g.ncells) {
         atomicAdd(escaped, 1u);
@@ -108,15 +121,20 @@ __global__ void k_na_place(const uint32_t *__restrict__ key, const uint32_t *__r
 }
 
 // final position: cell start + number of cell members with a smaller index
-// (the reference appends in index order, so each cell list is ascending)
+// (the reference appends in index order, so each cell list is ascending);
+// cells above the occupancy bound are flagged and left unranked
 __global__ void k_na_rank(const uint32_t *__restrict__ key, int n, int ncells,
                           const int32_t *__restrict__ start, const uint32_t *__restrict__ tmp,
-                          int32_t *__restrict__ list) {
+                          int32_t *__restrict__ list, uint32_t *__restrict__ crowded) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t k = key[i];
     if (k == (uint32_t)ncells) return;
     const int lo = start[k], hi = start[k + 1];
+    if (hi - lo > kNoAllocMaxPerCell) {
+        *crowded = 1u;
+        return;
+    }
     int rank = 0;
     for (int m = lo; m < hi; m++) rank += tmp[m] < (uint32_t)i ? 1 : 0;
     list[lo + rank] = i;
@@ -131,6 +149,10 @@ int tsph_particle_to_cell_noalloc(const tsph_constants *c, const tsph_domain *d,
                                   int32_t *cell_list_dev, void *stream, int *n_binned) {
     if (!c || !d || n < 0 || (n > 0 && (!r_dev || !cell_list_dev)) || !cell_start_dev)
         return fail(TSPH_ERR_ARG, "null or negative argument");
+    if ((reinterpret_cast<uintptr_t>(r_dev) & 7u) ||
+        (reinterpret_cast<uintptr_t>(cell_start_dev) & 3u) ||
+        (reinterpret_cast<uintptr_t>(cell_list_dev) & 3u))
+        return fail(TSPH_ERR_ARG, "misaligned buffer (r_dev needs 8-byte, the cell arrays 4-byte alignment)");
     if (n > kNoAllocMaxParticles)
         return fail(TSPH_ERR_ARG, "too many particles for the allocation-free binning (max 1048576)");
     if (!(c->h > 0) || !(c->kap > 0) || !(d->x_m > d->x_0) || !(d->y_m > d->y_0))
@@ -159,20 +181,26 @@ int tsph_particle_to_cell_noalloc(const tsph_constants *c, const tsph_domain *d,
     long long *bx = reinterpret_cast<long long *>(base + kOffBx);
     long long *by = reinterpret_cast<long long *>(base + kOffBy);
     uint32_t *escaped = reinterpret_cast<uint32_t *>(base + kOffEscaped);
+    uint32_t *crowded = reinterpret_cast<uint32_t *>(base + kOffCrowded);
 
     for (int k = 0; k <= ncx; k++) g_hbx[k] = tsph::cell_lower_bound(k, d->x_0, of, kh);
     for (int k = 0; k <= ncy; k++) g_hby[k] = tsph::cell_lower_bound(k, d->y_0, of, kh);
 
+    // on an error after work was queued, wait for that work before returning
+    // (and releasing the mutex), so the next call cannot overlap it on the array
 #define NA_CK(call)                                                             \
     do {                                                                        \
         cudaError_t e_ = (call);                                                \
-        if (e_ != cudaSuccess) return fail(TSPH_ERR_CUDA, cudaGetErrorString(e_)); \
+        if (e_ != cudaSuccess) {                                                \
+            cudaStreamSynchronize(st);                                          \
+            return fail(TSPH_ERR_CUDA, cudaGetErrorString(e_));                 \
+        }                                                                       \
     } while (0)
     NA_CK(cudaMemcpyAsync(bx, g_hbx, 8 * (size_t)(ncx + 1), cudaMemcpyHostToDevice, st));
     NA_CK(cudaMemcpyAsync(by, g_hby, 8 * (size_t)(ncy + 1), cudaMemcpyHostToDevice, st));
-    // what must start at zero: the histogram and the escape counter
+    // what must start at zero: the histogram and the two flags
     NA_CK(cudaMemsetAsync(counts, 0, 4 * ((size_t)ncells + 1), st));
-    NA_CK(cudaMemsetAsync(escaped, 0, 4, st));
+    NA_CK(cudaMemsetAsync(escaped, 0, 8, st));
 
     tsph::Grid g{};
     g.ax = tsph::Axis{bx, nullptr, ncx};
@@ -183,8 +211,7 @@ int tsph_particle_to_cell_noalloc(const tsph_constants *c, const tsph_domain *d,
     g.khf = (float)kh;
     const int nb = n > 0 ? (n + tsph::kBlock - 1) / tsph::kBlock : 1;
     if (n > 0)
-        k_na_bin<<<nb, tsph::kBlock, 0, st>>>(reinterpret_cast<const double2 *>(r_dev), n, g, key,
-                                              slot, counts, escaped);
+        k_na_bin<<<nb, tsph::kBlock, 0, st>>>(r_dev, n, g, key, slot, counts, escaped);
     const int ntiles = (ncells + 1 + tsph::kScanTile - 1) / tsph::kScanTile;
     uint32_t *start = reinterpret_cast<uint32_t *>(cell_start_dev);
     tsph::k_scan_tiles<<<ntiles, tsph::kScanThreads, 0, st>>>(counts, start, tiles, ncells);
@@ -193,17 +220,20 @@ int tsph_particle_to_cell_noalloc(const tsph_constants *c, const tsph_domain *d,
                                                                                        ncells);
     if (n > 0) {
         k_na_place<<<nb, tsph::kBlock, 0, st>>>(key, slot, n, ncells, cell_start_dev, tmp);
-        k_na_rank<<<nb, tsph::kBlock, 0, st>>>(key, n, ncells, cell_start_dev, tmp, cell_list_dev);
+        k_na_rank<<<nb, tsph::kBlock, 0, st>>>(key, n, ncells, cell_start_dev, tmp, cell_list_dev,
+                                               crowded);
     }
     NA_CK(cudaGetLastError());
-    uint32_t nesc = 0;
+    uint32_t flags[2] = {0u, 0u};  // escaped, crowded
     int32_t total = 0;
-    NA_CK(cudaMemcpyAsync(&nesc, escaped, 4, cudaMemcpyDeviceToHost, st));
+    NA_CK(cudaMemcpyAsync(flags, escaped, 8, cudaMemcpyDeviceToHost, st));
     NA_CK(cudaMemcpyAsync(&total, cell_start_dev + ncells, 4, cudaMemcpyDeviceToHost, st));
     NA_CK(cudaStreamSynchronize(st));
 #undef NA_CK
     if (n_binned) *n_binned = total;
-    if (nesc) return fail(TSPH_ERR_ESCAPED, "particles outside the cell grid were left out of the lists");
+    if (flags[1])
+        return fail(TSPH_ERR_ARG, "a cell holds more than 4096 particles (max for the allocation-free binning)");
+    if (flags[0]) return fail(TSPH_ERR_ESCAPED, "particles outside the cell grid were left out of the lists");
     return TSPH_OK;
 }
 

@@ -23,8 +23,8 @@ So the network predicts the part of the window's change that the rates do
 not: y = 0 is the method without it (one symplectic step of k dt).  Device
 memory comes from torch (allocation and, for building training targets,
 index gathers); every computation of the rollout is a kernel of the
-library.  The network's definition and its CPU oracle are in
-oracle/gnn_oracle.py.
+library.  The network's parameter layout and initial weights are in
+gnn_params.py.
 """
 
 from __future__ import annotations
@@ -37,7 +37,7 @@ from dataclasses import dataclass, field
 
 import numpy as np
 
-from . import sph
+from . import gnn_params, sph
 
 K_SLOTS = 48  # neighbour slots per node (the SPH pair set has ~24-36)
 # the trained model shipped with the package (python -m tinysph_old_gb300.surrogate)
@@ -319,17 +319,6 @@ def fit_scales(samples, local=False, direct=False):
 
 # ------------------------------------------------------------------ training
 
-def sys_path_oracle():
-    """Make oracle/ importable (the network's initial weights and parameter
-    layout live with its CPU oracle)."""
-    import os
-    import sys
-
-    d = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "oracle")
-    if d not in sys.path:
-        sys.path.insert(0, d)
-
-
 def train(samples, scales, h, iters=1000, lr=1e-3, lr_end=1e-5, seed=0, params=None,
           log=None, log_every=100, clip=None, direct=False):
     """Adam on the device over the samples (one window per iteration, in a
@@ -337,13 +326,10 @@ def train(samples, scales, h, iters=1000, lr=1e-3, lr_end=1e-5, seed=0, params=N
     clipped to +-clip (normalised units).  Returns (Model, loss history)."""
     import torch
 
-    sys_path_oracle()
-    import gnn_oracle as G
-
     u_in, s_in, u_out, s_out = scales
     cap = max(smp.graph.n for smp in samples)
     net = sph.Gnn(cap)
-    p0 = params if params is not None else G.flatten(G.init_params(seed)).astype(np.float32)
+    p0 = params if params is not None else gnn_params.initial_params(seed)
     net.set_params(p0)
     inv = torch.tensor([1.0 / u_out, 1.0 / u_out, 1.0 / s_out], device="cuda")
     targets = []
