@@ -687,9 +687,9 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=0,
                     help="CPU baseline sample (0 = auto, ~10-30 s)")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--tile-shape", default="auto", choices=["auto", "wide", "deep"],
-                    help="pair-kernel tile shape: timed on the particles (auto) or fixed, "
-                         "e.g. to profile one shape")
+    ap.add_argument("--tile-shape", default="auto", choices=["auto", "wide", "deep", "rec"],
+                    help="pair-kernel variant: timed on the particles (auto) or fixed, "
+                         "e.g. to profile one variant")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.dp is None:
@@ -736,7 +736,7 @@ def main():
     s.divide_to_cells()
     s.particle_to_cell()
     if args.tile_shape != "auto":
-        s.set_tile_shape(0 if args.tile_shape == "wide" else 1)
+        s.set_tile_shape(sph.TILE_SHAPES[args.tile_shape])
     n = s.np
     model = case.wall_model
     dt = case.dt

@@ -50,6 +50,9 @@ enum {
 #define TSPH_HEALTH_DENSITY 0x2u
 #define TSPH_HEALTH_ESCAPED 0x4u
 #define TSPH_HEALTH_REMOVED 0x8u
+/* a pipelined kernel gave up waiting for its own staging pipeline (a bounded
+ * wait ran out; the step's results are not valid) */
+#define TSPH_HEALTH_STALL 0x10u
 
 /* particle types, src/SPH_defs.h:44-48 (fluid = 0, wall = 1) */
 enum { TSPH_FLUID = 0, TSPH_WALL = 1 };
@@ -282,13 +285,20 @@ typedef struct {
     double other_us;     /* everything else (EOS, predictor, ...)         */
     int other_launches;
 } tsph_profile_t;
-/* Tile shape of the FP32 pair kernel: 0 = 608 staged neighbours and 36 list
- * entries per target, 1 = 512 and 44 (for h ~ 1.5 dp).  tsph_autotune times
- * both on the current particles (a forces pass each; the state is left as it
- * was) and keeps the faster; the first tsph_step does this by itself.
- * us[2] (may be NULL) receives the two times in microseconds.  No counterpart
- * in the reference. */
-int tsph_autotune(tsph_system *s, int32_t *shape, double us[2]);
+/* Variant of the FP32 pair kernel (TSPH_N_TILE_SHAPES of them):
+ * 0 = one CTA per 128 targets staging 608 neighbours with 36 list entries per
+ *     target, 1 = the same with 512 and 44 (for h ~ 1.5 dp),
+ * 2 = pair records: a pass forms every particle's neighbour-side values and
+ *     the table of each chunk's windows once, then one CTA per 128 targets
+ *     stages each window's record ranges with bulk copies (472 staged
+ *     neighbours, 38 list entries per target).
+ * tsph_autotune times every variant on the current particles (a warm-up and
+ * 10 timed forces passes each, the median kept; the state is left as it was)
+ * and keeps the fastest; the first tsph_step does this by itself.
+ * us (may be NULL) receives TSPH_N_TILE_SHAPES median times in microseconds.
+ * No counterpart in the reference. */
+#define TSPH_N_TILE_SHAPES 3
+int tsph_autotune(tsph_system *s, int32_t *shape, double us[TSPH_N_TILE_SHAPES]);
 int tsph_set_tile_shape(tsph_system *s, int shape);
 int tsph_set_profiling(tsph_system *s, int on);
 

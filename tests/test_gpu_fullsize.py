@@ -46,10 +46,13 @@ def test_fullsize_cells_and_pair_sets(gpu_tsph, big_case, big_oracle):
 
 
 @pytest.mark.gpu
-def test_fullsize_step_matches_oracle(gpu_tsph, oracle_mod, big_case):
+@pytest.mark.parametrize("variant", [0, 1, 2])
+def test_fullsize_step_matches_oracle(gpu_tsph, oracle_mod, big_case, variant):
+    """Every pair-kernel variant, fixed in turn, against the oracle."""
     import os
     steps = 3
     s = gpu_tsph.ParticleSystem.from_case(big_case, "fp32")
+    s.set_tile_shape(variant)
     s.step(big_case.wall_model, big_case.dt, steps)
     got = s.download()
     P = oracle_mod.PortSystem.from_case(big_case)
@@ -67,10 +70,12 @@ def test_fullsize_step_matches_oracle(gpu_tsph, oracle_mod, big_case):
 
 
 @pytest.mark.gpu
-def test_fullsize_deterministic_and_conservative(gpu_tsph, big_case):
+@pytest.mark.parametrize("variant", [0, 2])
+def test_fullsize_deterministic_and_conservative(gpu_tsph, big_case, variant):
     res = []
     for _ in range(2):
         s = gpu_tsph.ParticleSystem.from_case(big_case, "fp32")
+        s.set_tile_shape(variant)
         s.step(big_case.wall_model, big_case.dt, 20)
         res.append(s.download())
         tot = s.fluid_totals()

@@ -79,13 +79,19 @@ def test_pair_digest_bit_exact(gpu_tsph, oracle_mod, fname, builder, model):
     assert np.array_equal(x0, x1)
 
 
+# precision and pair-kernel variant (FP32: every variant fixed in turn)
+VARIANTS = [("fp32", 0), ("fp32", 1), ("fp32", 2), ("fp64", None)]
+
+
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("precision,variant", VARIANTS)
 @pytest.mark.parametrize("fname,builder,model", CASES)
-def test_per_function_parity(gpu_tsph, fname, builder, model, precision):
+def test_per_function_parity(gpu_tsph, fname, builder, model, precision, variant):
     """Density_to_pressure, mDBC and Compute_Forces at the golden input."""
     g = _gold(fname)
     s = _gpu(gpu_tsph, builder(), g, precision)
+    if variant is not None:
+        s.set_tile_shape(variant)
     s.density_to_pressure()
     st = s.download()
     tol = (lambda f, r: 1e-9 * max(1.0, float(np.max(np.abs(r))))) if precision == "fp64" else _tol32
@@ -107,12 +113,14 @@ def test_per_function_parity(gpu_tsph, fname, builder, model, precision):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("precision,variant", VARIANTS)
 @pytest.mark.parametrize("fname,builder,model", CASES)
-def test_fused_step_matches_reference(gpu_tsph, fname, builder, model, precision):
+def test_fused_step_matches_reference(gpu_tsph, fname, builder, model, precision, variant):
     """tsph_step (fused kernels, CUDA graph) against the reference's RUN loop."""
     g = _gold(fname)
     s = _gpu(gpu_tsph, builder(), g, precision)
+    if variant is not None:
+        s.set_tile_shape(variant)
     every = int(g["snap_every"])
     for k in range(every, int(g["nsteps"]) + 1, every):
         s.step(model, float(g["dt"]), every)
@@ -258,9 +266,9 @@ def test_remove_out_of_domain(gpu_tsph, oracle_mod):
 
 
 @pytest.mark.gpu
-def test_autotune_leaves_the_state_and_both_tile_shapes_agree(gpu_tsph):
-    """tsph_autotune times the two tile shapes of the FP32 pair kernel without
-    touching the state; stepping with either shape gives the same result up
+def test_autotune_leaves_the_state_and_all_tile_shapes_agree(gpu_tsph):
+    """tsph_autotune times the variants of the FP32 pair kernel without
+    touching the state; stepping with any variant gives the same result up
     to FP32 summation order."""
     g = _gold("dam_break_mdbc_dp0.02.npz")
     case = cases.dam_break_mdbc(dp=0.02)
@@ -268,15 +276,17 @@ def test_autotune_leaves_the_state_and_both_tile_shapes_agree(gpu_tsph):
     s = _gpu(gpu_tsph, case, g, "fp32")
     before = s.download()
     shape, us = s.autotune()
-    assert shape in (0, 1) and np.all(us > 0)
+    assert shape in range(gpu_tsph.N_TILE_SHAPES) and np.all(us > 0)
     after = s.download()
     for f in ("r", "v", "a", "rho", "drho", "p"):
         assert np.array_equal(before[f], after[f]), f
     res = []
-    for shape in (0, 1):
+    for shape in range(gpu_tsph.N_TILE_SHAPES):
         t = _gpu(gpu_tsph, case, g, "fp32")
         t.set_tile_shape(shape)
         t.step(0, dt, 4)
+        assert t.health() == 0
         res.append(t.download())
-    for f in ("r", "v", "a", "rho", "drho"):
-        assert _err(res[0][f], res[1][f]) <= 1e-5 * max(1.0, float(np.max(np.abs(res[0][f])))), f
+    for other in res[1:]:
+        for f in ("r", "v", "a", "rho", "drho"):
+            assert _err(res[0][f], other[f]) <= 1e-5 * max(1.0, float(np.max(np.abs(res[0][f])))), f

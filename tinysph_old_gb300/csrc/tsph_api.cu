@@ -568,7 +568,7 @@ int tsph_state_restore(tsph_system *s) {
     return TSPH_OK;
 }
 
-int tsph_autotune(tsph_system *s, int32_t *shape, double us[2]) {
+int tsph_autotune(tsph_system *s, int32_t *shape, double us[TSPH_N_TILE_SHAPES]) {
     NEED(s);
     ENGINE(s);
     int c = 0;

@@ -13,6 +13,7 @@
 #include "tsph_engine.h"
 #include "tsph_kernels.cuh"
 #include "tsph_pairs_tiled.cuh"
+#include "tsph_pairs_rec.cuh"
 #include "tsph_probes.cuh"
 #include "tsph_graph.cuh"
 #include "tsph_zones.cuh"
@@ -267,16 +268,25 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     TileConst K_{}, Kskin_{};
-    int tile_shape_ = -1;  // 0 TileWide, 1 TileDeep; -1: not tuned yet
+    int tile_shape_ = -1;  // 0 TileWide, 1 TileDeep, 2 pair records; -1: not tuned yet
+    // pair records (tile shape 2): of F_, of Fs_, of the walls
+    PairRec rec_f_{}, rec_s_{}, rec_w_{};
+    WinRec *rec_table_ = nullptr;  // windows of each chunk of 128 targets
+    int *rec_nwin_ = nullptr;
+    TileConst Krec_{}, Krec_skin_{};
+    bool rec_setup_ = false;
 
   public:
-    // time both tile shapes on the current particles (forces pass, a and drho
-    // saved and restored) and keep the faster; FP32 build only
-    int autotune(int *choice, double us[2], std::string &err) override {
+    // time every pair-kernel variant on the current particles (forces pass,
+    // a and drho saved and restored): a warm-up and 10 timed launches each,
+    // the median kept; the fastest wins.  FP32 build only.
+    static constexpr int kShapes = 3;
+    int autotune(int *choice, double *us, std::string &err) override {
         if constexpr (!std::is_same<T, float>::value) {
             tile_shape_ = 0;
             if (choice) *choice = 0;
-            if (us) us[0] = us[1] = 0;
+            if (us)
+                for (int k = 0; k < kShapes; k++) us[k] = 0;
             return 0;
         } else {
             if (!cells_) {
@@ -287,38 +297,43 @@ template <typename T> class Engine final : public EngineBase {
             prof_ = false;
             TSPH_CK(cudaMemcpyAsync(Bv_, F_.a, sizeof(T2) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
             TSPH_CK(cudaMemcpyAsync(Brho_, F_.drho, sizeof(T) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
-            cudaEvent_t e0 = ev(), e1 = ev();
-            float best[2] = {0, 0};
+            constexpr int kReps = 10;
+            std::vector<cudaEvent_t> evs(kReps + 1);
+            for (auto &e : evs) e = ev();
+            double med[kShapes] = {0, 0, 0};
             int rc = 0;
-            for (int shape = 0; shape < 2 && !rc; shape++) {
+            for (int shape = 0; shape < kShapes && !rc; shape++) {
                 tile_shape_ = shape;
                 rc = fluid_pairs<MODE_FORCES>(F_, false, T(0), PairOut{}, err);  // warm
-                for (int rep = 0; rep < 3 && !rc; rep++) {
-                    cudaEventRecord(e0, st_);
+                cudaEventRecord(evs[0], st_);
+                for (int rep = 0; rep < kReps && !rc; rep++) {
                     rc = fluid_pairs<MODE_FORCES>(F_, false, T(0), PairOut{}, err);
-                    cudaEventRecord(e1, st_);
-                    cudaEventSynchronize(e1);
-                    float ms = 0;
-                    cudaEventElapsedTime(&ms, e0, e1);
-                    if (rep == 0 || ms < best[shape]) best[shape] = ms;
+                    cudaEventRecord(evs[rep + 1], st_);
                 }
+                if (rc) break;
+                cudaEventSynchronize(evs[kReps]);
+                std::vector<float> t(kReps);
+                for (int rep = 0; rep < kReps; rep++)
+                    cudaEventElapsedTime(&t[rep], evs[rep], evs[rep + 1]);
+                std::sort(t.begin(), t.end());
+                med[shape] = 0.5 * (t[kReps / 2 - 1] + t[kReps / 2]);
             }
-            ev_pool_.push_back(e0);
-            ev_pool_.push_back(e1);
+            for (auto &e : evs) ev_pool_.push_back(e);
             prof_ = prof;
             if (rc) return rc;
             TSPH_CK(cudaMemcpyAsync(F_.a, Bv_, sizeof(T2) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
             TSPH_CK(cudaMemcpyAsync(F_.drho, Brho_, sizeof(T) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
             TSPH_CK(cudaStreamSynchronize(st_));
-            tile_shape_ = best[1] < best[0] ? 1 : 0;
-            // graphs captured with the other shape are stale
+            int best = 0;
+            for (int k = 1; k < kShapes; k++)
+                if (med[k] < med[best]) best = k;
+            tile_shape_ = best;
+            // graphs captured with another variant are stale
             for (auto &g : graphs_) cudaGraphExecDestroy(g.second);
             graphs_.clear();
             if (choice) *choice = tile_shape_;
-            if (us) {
-                us[0] = 1000.0 * best[0];
-                us[1] = 1000.0 * best[1];
-            }
+            if (us)
+                for (int k = 0; k < kShapes; k++) us[k] = 1000.0 * med[k];
             return 0;
         }
     }
@@ -529,8 +544,8 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int set_tile_shape(int shape, std::string &err) override {
-        if (shape < 0 || shape > 1) {
-            err = "tile shape must be 0 or 1";
+        if (shape < 0 || shape >= kShapes) {
+            err = "tile shape must be 0, 1 or 2";
             return 1;
         }
         tile_shape_ = shape;
@@ -584,6 +599,41 @@ template <typename T> class Engine final : public EngineBase {
             const int nb = blocks_for(nf_, kTileT);
             const TileConst K = skinned ? Kskin_ : K_;
             const uint32_t *fs = fstart_, *ws = wstart_;
+            if (tile_shape_ == 2) {
+                int rc;
+                if (!rec_setup_) {
+                    const void *kr[4] = {(const void *)k_pairs_rec<MODE_FORCES, false, RecStd>,
+                                         (const void *)k_pairs_rec<MODE_FORCES, true, RecStd>,
+                                         (const void *)k_pairs_rec<MODE_CORRECT, false, RecStd>,
+                                         (const void *)k_pairs_rec<MODE_CORRECT, true, RecStd>};
+                    for (const void *k : kr)
+                        TSPH_CK(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                     (int)cudaSharedmemCarveoutMaxShared));
+                    rec_setup_ = true;
+                }
+                const PairRec RX = X.r == Fs_.r ? rec_s_ : rec_f_;
+                const int nchunks = blocks_for(nf_, kRecT);
+                const int rb = blocks_for((long long)nw_ + nf_);
+                const int tb = rb + blocks_for(nchunks);
+                const WinRec *tab = rec_table_;
+                const int *nwin = rec_nwin_;
+                if (stored_p)
+                    rc = launch(CAT_PAIR, k_pair_records<true>, tb, kBlock, err, X, fs, W_, nw_,
+                                grid_, P_, RX, rec_w_, rb, ws, nchunks, RecStd::cap, rec_table_,
+                                rec_nwin_);
+                else
+                    rc = launch(CAT_PAIR, k_pair_records<false>, tb, kBlock, err, X, fs, W_, nw_,
+                                grid_, P_, RX, rec_w_, rb, ws, nchunks, RecStd::cap, rec_table_,
+                                rec_nwin_);
+                if (rc) return rc;
+                const TileConst KR = skinned ? Krec_skin_ : Krec_;
+                if (stored_p)
+                    return launch(CAT_PAIR, k_pairs_rec<MODE, true, RecStd>, nchunks, kRecT, err, X,
+                                  fs, ws, W_, grid_, P_, KR, O_, dt, po, RX, rec_w_, tab, nwin,
+                                  health_);
+                return launch(CAT_PAIR, k_pairs_rec<MODE, false, RecStd>, nchunks, kRecT, err, X,
+                              fs, ws, W_, grid_, P_, KR, O_, dt, po, RX, rec_w_, tab, nwin, health_);
+            }
             if (tile_shape_ == 1) {
                 if (stored_p)
                     return launch(CAT_PAIR, k_pairs_tiled<MODE, true, TileDeep>, nb, kTileT, err,
@@ -804,6 +854,15 @@ template <typename T> class Engine final : public EngineBase {
             skin_ = (float)(0.95 * 0.5 * (hs.kh - 2.0 * hs.h));
             Kskin_ = K_;
             Kskin_.reach = K_.reach + 2.f * skin_;
+            // pair records: the support test and the window search use y in
+            // the grid's frame (rounding up to half an ulp of the grid height
+            // per value, plus the fma that forms it): 8 ulps of margin
+            const double ytop = (double)hs.ncy * hs.kh;
+            const float margin = 8.f * std::ldexp(1.f, std::ilogb((float)ytop) - 23);
+            Krec_ = K_;
+            Krec_.reach = K_.reach + margin;
+            Krec_skin_ = Kskin_;
+            Krec_skin_.reach = Kskin_.reach + margin;
         }
         // grid tables
         int rc;
@@ -832,6 +891,24 @@ template <typename T> class Engine final : public EngineBase {
             return 0;
         };
         if ((rc = alloc_state(F_)) || (rc = alloc_state(Fs_))) return rc;
+        if constexpr (std::is_same<T, float>::value) {
+            // pair records (tile shape 2); four spare records: a window's
+            // copies are widened to 4-record boundaries
+            auto alloc_rec = [&](PairRec &R, int n) -> int {
+                int r;
+                const int cap = n + kRecPad;
+                if ((r = alloc(&R.t, cap, err)) || (r = alloc(&R.y, cap, err)) ||
+                    (r = alloc(&R.v, cap, err)) || (r = alloc(&R.inv, cap, err)))
+                    return r;
+                return 0;
+            };
+            const int nchunks = blocks_for(nf_, kRecT);
+            if ((rc = alloc_rec(rec_f_, nf_)) || (rc = alloc_rec(rec_s_, nf_)) ||
+                (rc = alloc_rec(rec_w_, nw_)) ||
+                (rc = alloc(&rec_table_, (size_t)nchunks * kRecMaxWin, err)) ||
+                (rc = alloc(&rec_nwin_, nchunks, err)))
+                return rc;
+        }
         if (zones_on_) {
             zlist_cap_ = 1 << 16;
             if ((rc = alloc(&F_.type, nf_, err)) || (rc = alloc(&Fs_.type, nf_, err)) ||
@@ -851,8 +928,8 @@ template <typename T> class Engine final : public EngineBase {
             err = "grid too large for the scan";
             return 1;
         }
-        if ((rc = alloc(&counts_, ncells_ + 1, err)) || (rc = alloc(&fstart_, ncells_ + 2, err)) ||
-            (rc = alloc(&wstart_, ncells_ + 1, err)) || (rc = alloc(&tile_sums_, ntiles, err)) ||
+        if ((rc = alloc(&counts_, ncells_ + 1, err)) || (rc = alloc(&fstart_, ncells_ + 32, err)) ||
+            (rc = alloc(&wstart_, ncells_ + 32, err)) || (rc = alloc(&tile_sums_, ntiles, err)) ||
             (rc = alloc(&health_, 1, err)) || (rc = alloc(&removed_, 1, err)) ||
             (rc = alloc(&rebuild_, 1, err)) || (rc = alloc(&rebins_, 1, err)) ||
             (rc = alloc(&dtot_, 4 * (size_t)blocks_for(nf_), err)))

@@ -69,7 +69,7 @@ class EngineBase {
                             double *out, std::string &err) = 0;
     virtual int point_fields(int n, const double *xy, double *out, std::string &err) = 0;
     virtual int water_front(double y_max, double *x, std::string &err) = 0;
-    virtual int autotune(int *choice, double us[2], std::string &err) = 0;
+    virtual int autotune(int *choice, double *us, std::string &err) = 0;
     virtual int set_tile_shape(int shape, std::string &err) = 0;
     virtual int tile_shape() const = 0;
     // the particle graph and the surrogate's window update (device pointers)

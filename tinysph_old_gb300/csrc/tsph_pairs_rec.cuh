@@ -1,0 +1,534 @@
+// tsph_pairs_rec.cuh -- the FP32 pair loop of Compute_Forces
+// (src/SPH_interaction.h:8-149, fused with Integrate_SymplecticCorrector,
+// src/SPH_integration.h:289-309) over pair records staged by bulk copies.
+//
+// Pair records.  Before a pair pass, every particle's neighbour-side values
+// are formed once, in the sorted order, by k_pair_records (four arrays, so a
+// window's record is a few contiguous ranges of each):
+//   rt[i] = {x relative to the particle's own cell, y relative to the grid's
+//            first row (~1e-7 m rounding)}                 support test
+//   ry[i] = {y relative to the particle's own cell, cell row as a float}
+//   rv[i] = {vx, vy, rho - rho0, p/rho}
+//   ri[i] = 1/rho
+// The support test and the window search use the coarse y of rt (its rounding
+// can only move pairs within ~1e-4 h of r = 2h, where W and dW vanish to
+// ~1e-12 of their scale); the pair terms form dy from the cell-relative y and
+// the exact row difference, and dx from the cell-relative x and the column
+// offset, as precisely as k_pairs_tiled.
+//
+// Work decomposition: a CTA takes 128 consecutive fluid targets (one thread
+// each) and walks them in windows of at most kRecRows rows of one column.
+// Per window one thread issues cp.async.bulk copies (1-D TMA) of the
+// 3 x (rows + 2) neighbour cells' record ranges (walls and fluid of the three
+// columns; each range widened to 4-record alignment) into shared memory,
+// completing on an mbarrier: no per-neighbour instructions, one round trip.
+// Phase 1 walks, per neighbour column, one contiguous y-window of the
+// y-sorted column (both ends by binary search on the coarse y), so every lane
+// of a warp runs about the same number of candidates, and keeps the
+// in-support neighbours in a per-thread list of (staged index, column)
+// entries; when a column might not fit in some lane's list, the whole warp
+// sums its lists (phase 2) and empties them first (a warp-uniform step, so
+// no lane waits on another's), and the pairs are still summed in candidate
+// order.  Phase 2 sums the WCSPH pair terms (pair_terms
+// of k_pairs_tiled) over the list.
+//
+// With the cells of the last binning kept through the predictor the columns
+// are y-sorted as of that binning and every particle has moved less than the
+// skin since: K.reach includes twice the skin (and the coarse y's rounding),
+// which keeps the search and the early stop conservative.
+#pragma once
+
+#include "tsph_pairs_tiled.cuh"
+
+namespace tsph {
+
+constexpr int kRecT = 128;    // targets per CTA (one thread each)
+constexpr int kRecRows = 16;  // max target rows per window
+constexpr int kRecPad = 4;    // records per 16 bytes of the narrowest array (ri)
+
+constexpr unsigned long long kWaitNs = 4000000000ull;  // bounded mbarrier waits (4 s)
+constexpr int kRecMaxWin = 4;  // windows per chunk in the window table
+constexpr int kRecOffRun = ((kRecRows + 3 + 3) + 3) & ~3;  // offsets copied per column
+enum { kRecStaged = 0, kRecGlobal = 1 };
+
+// One window of a chunk (written by k_pair_records, read by k_pairs_rec):
+// targets [cur, we) in rows rlo+1.. of column cx, staged rows [rlo, rlo+nr);
+// segment s (walls, fluid of columns cx-1, cx, cx+1) is staged from the
+// 4-aligned global row first[s], n[s] rows (a multiple of 4).
+struct __align__(16) WinRec {
+    int cur, we, cx, rlo, nr, mode, tot, pad;
+    int first[6];
+    int n[6];
+};
+
+template <int CAP, int LIST> struct RecShape {
+    static constexpr int cap = CAP, list = LIST;
+};
+typedef RecShape<472, 38> RecStd;
+
+struct PairRec {  // one set of pair records (fluid rows or walls)
+    float2 *t, *y;
+    float4 *v;
+    float *inv;
+};
+
+template <class SH> struct RecSmem {
+    float4 v[SH::cap];
+    float2 t[SH::cap];
+    float2 y[SH::cap];
+    float inv[SH::cap];
+    uint16_t list[SH::list * kRecT];
+    // fstart / wstart of the staged rows of each column, copied from the
+    // 4-aligned index below (col * ncy + rlo); row q of column d is at
+    // [d][q + oshift[d]]
+    int foff[3][kRecOffRun];
+    int woff[3][kRecOffRun];
+    int oshift[3];
+    int base[6];  // staged index of global row j of segment s = base[s] + j
+    WinRec win;
+    float offx[4];
+    unsigned long long bar;
+};
+
+// ---------------------------------------------------------------- records
+// The windows of chunk c (targets [128 c, 128 c + 128) of the live rows): at
+// most kRecRows target rows of one column each, halved while the staged
+// block exceeds `cap`; a block that does not fit even for one row, and the
+// rest of a chunk that needs more than kRecMaxWin windows, take the
+// global-memory path.
+__device__ __forceinline__ void rec_window_table(int c, int cap, const FluidState<float> &F,
+                                                 const uint32_t *__restrict__ fstart,
+                                                 const uint32_t *__restrict__ wstart,
+                                                 const Grid &g, WinRec *__restrict__ table,
+                                                 int *__restrict__ nwin) {
+    const int nl = n_live(fstart, g.ncells);
+    const int t0 = c * kRecT;
+    if (t0 >= nl) {
+        nwin[c] = 0;
+        return;
+    }
+    const int ncy = g.ncy;
+    const int t1 = min(t0 + kRecT, nl);
+    const uint32_t klast = __ldg(F.key + t1 - 1);
+    const int cxl = (int)(klast / (uint32_t)ncy);
+    const int cyll = (int)klast - cxl * ncy;
+    int cur = t0, nwc = 0;
+    while (cur < t1 && nwc < kRecMaxWin) {
+        const uint32_t kc = __ldg(F.key + cur);
+        const int cx = (int)(kc / (uint32_t)ncy);
+        const int cy0 = (int)kc - cx * ncy;
+        WinRec R;
+        int rows = kRecRows, we, tot;
+        for (;;) {
+            const int rowlim = min(cy0 + rows, ncy);
+            int cyl;
+            if (cxl == cx && cyll < rowlim) {
+                we = t1;
+                cyl = cyll;
+            } else {
+                we = min(t1, (int)__ldg(fstart + cx * ncy + rowlim));
+                cyl = (int)__ldg(F.key + we - 1) - cx * ncy;
+            }
+            R.rlo = max(cy0 - 1, 0);
+            const int rhi = min(cyl + 1, ncy - 1);
+            R.nr = rhi - R.rlo + 1;
+            tot = 0;
+            for (int sgi = 0; sgi < 6; sgi++) {
+                const int col = cx + (sgi >> 1) - 1;
+                const uint32_t *st = (sgi & 1) ? fstart : wstart;
+                int j0 = 0, j1 = 0;
+                if (col >= 0 && col < g.ncx) {
+                    j0 = (int)__ldg(st + col * ncy + R.rlo);
+                    j1 = (int)__ldg(st + col * ncy + rhi + 1);
+                }
+                const int a0 = j0 & ~(kRecPad - 1);
+                const int cnt = j1 > j0 ? ((j1 - a0 + kRecPad - 1) & ~(kRecPad - 1)) : 0;
+                R.first[sgi] = a0;
+                R.n[sgi] = cnt;
+                tot += cnt;
+            }
+            if (tot > cap && rows > 1) {
+                rows = (rows + 1) >> 1;
+                continue;
+            }
+            break;
+        }
+        R.mode = tot <= cap ? kRecStaged : kRecGlobal;
+        if (nwc == kRecMaxWin - 1 && we < t1) {
+            we = t1;
+            R.mode = kRecGlobal;
+        }
+        R.cur = cur;
+        R.we = we;
+        R.cx = cx;
+        R.tot = tot;
+        R.pad = 0;
+        table[(size_t)c * kRecMaxWin + nwc] = R;
+        nwc++;
+        cur = we;
+    }
+    nwin[c] = nwc;
+}
+
+// pair records of the fluid rows [0, n_live) and the walls [0, nw) of a state
+// (p from the EOS of rho, or the stored p); the blocks from `rec_blocks` on
+// build the window table, one thread per chunk of 128 targets
+template <bool STORED_P>
+__global__ void __launch_bounds__(kBlock)
+k_pair_records(FluidState<float> F, const uint32_t *__restrict__ fstart, WallState<float> Wl,
+               int nw, Grid g, Phys<float> P, PairRec RF, PairRec RW, int rec_blocks,
+               const uint32_t *__restrict__ wstart, int nchunks, int cap,
+               WinRec *__restrict__ table, int *__restrict__ nwin) {
+    pdl_enter();
+    if ((int)blockIdx.x >= rec_blocks) {
+        const int c = ((int)blockIdx.x - rec_blocks) * blockDim.x + threadIdx.x;
+        if (c < nchunks) rec_window_table(c, cap, F, fstart, wstart, g, table, nwin);
+        return;
+    }
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int nl = n_live(fstart, g.ncells);
+    const bool wall = i < nw;
+    const int j = wall ? i : i - nw;
+    if (!wall && j >= nl) return;
+    const uint32_t key = __ldg((wall ? Wl.key : F.key) + j);
+    const float2 l = __ldg((wall ? Wl.loc : F.loc) + j);
+    const float s = __ldg((wall ? Wl.rho : F.rho) + j);
+    const float2 v = wall ? make_float2(0.f, 0.f) : __ldg(F.v + j);
+    const float p = STORED_P ? __ldg((wall ? Wl.p : F.p) + j) : eos(s, P);
+    const int cx = (int)(key / (uint32_t)g.ncy);
+    const float row = (float)((int)key - cx * g.ncy);
+    const float ib = rcp_approx(P.rho0 + s);
+    (wall ? RW.t : RF.t)[j] = make_float2(l.x, fmaf(row, g.khf, l.y));
+    (wall ? RW.y : RF.y)[j] = make_float2(l.y, row);
+    (wall ? RW.v : RF.v)[j] = make_float4(v.x, v.y, s, p * ib);
+    (wall ? RW.inv : RF.inv)[j] = ib;
+}
+
+// ---------------------------------------------------------------- plumbing
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *b, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(unsigned long long *b) {
+    asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(
+                     smem_u32(b))
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try(unsigned long long *b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0u;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// wait for the phase with the given parity to complete; false after
+// kWaitNs (the caller then records kHealthStall and leaves)
+__device__ __forceinline__ bool mbar_wait(unsigned long long *b, uint32_t parity) {
+    if (mbar_try(b, parity)) return true;
+    const unsigned long long t0 = global_ns();
+    while (!mbar_try(b, parity))
+        if (global_ns() - t0 > kWaitNs) return false;
+    return true;
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         unsigned long long *b) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(b))
+        : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void fence_mbar_init() {
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// phase 1 over one column's fluid candidates [s, e) (the column's y-window):
+// entry = staged index << 2 | column
+template <bool EXCL>
+__device__ __forceinline__ uint16_t *rec_scan(const float2 *__restrict__ t, int s, int e, float xa,
+                                              float ya, float h2, uint32_t col, uint16_t *w) {
+    int j = s;
+    uint32_t ent = ((uint32_t)s << 2) | col;
+    for (; j + 1 < e; j += 2, ent += 8u) {
+        const float2 l0 = t[j], l1 = t[j + 1];
+        const float dx0 = xa - l0.x, dy0 = ya - l0.y;
+        const float dx1 = xa - l1.x, dy1 = ya - l1.y;
+        const float r0 = fmaf(dx0, dx0, dy0 * dy0), r1 = fmaf(dx1, dx1, dy1 * dy1);
+        *w = (uint16_t)ent;
+        w += support_test<EXCL>(r0, h2) ? kRecT : 0;
+        *w = (uint16_t)(ent + 4u);
+        w += support_test<EXCL>(r1, h2) ? kRecT : 0;
+    }
+    if (j < e) {
+        const float2 l = t[j];
+        const float dx = xa - l.x, dy = ya - l.y;
+        *w = (uint16_t)ent;
+        w += support_test<EXCL>(fmaf(dx, dx, dy * dy), h2) ? kRecT : 0;
+    }
+    return w;
+}
+
+// first index of [lo, hi) whose coarse y is not below y (ABOVE: above y)
+template <bool ABOVE>
+__device__ __forceinline__ int rec_bound(const float2 *__restrict__ t, int lo, int hi, float y) {
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const float ym = t[mid].y;
+        if (ABOVE ? !(ym > y) : (ym < y)) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// phase 2: the pair terms over list entries [0, cnt)
+template <class SH>
+__device__ __forceinline__ void rec_eval(const RecSmem<SH> &sm, const uint16_t *lst, int cnt,
+                                         float xa, float yca, float rowa, float2 va, float sa,
+                                         float Pa, float Ia, float Ra2, float khf,
+                                         const TileConst &K, Acc4 &acc) {
+    int k = 0;
+    for (; k + 1 < cnt; k += 2) {
+        const uint32_t e0 = lst[k * kRecT], e1 = lst[(k + 1) * kRecT];
+        const int j0 = (int)(e0 >> 2), j1 = (int)(e1 >> 2);
+        const float ox0 = sm.offx[e0 & 3u], ox1 = sm.offx[e1 & 3u];
+        const float2 a0 = sm.t[j0], a1 = sm.t[j1];
+        const float2 c0 = sm.y[j0], c1 = sm.y[j1];
+        const float4 v0 = sm.v[j0], v1 = sm.v[j1];
+        const float i0 = sm.inv[j0], i1 = sm.inv[j1];
+        pair_terms((xa + ox0) - a0.x, fmaf(rowa - c0.y, khf, yca - c0.x), va.x - v0.x,
+                   va.y - v0.y, sa, Pa, Ia, Ra2, v0.z, v0.w, i0, K, acc);
+        pair_terms((xa + ox1) - a1.x, fmaf(rowa - c1.y, khf, yca - c1.x), va.x - v1.x,
+                   va.y - v1.y, sa, Pa, Ia, Ra2, v1.z, v1.w, i1, K, acc);
+    }
+    if (k < cnt) {
+        const uint32_t e = lst[k * kRecT];
+        const int j = (int)(e >> 2);
+        const float ox = sm.offx[e & 3u];
+        const float2 a = sm.t[j], c = sm.y[j];
+        const float4 v = sm.v[j];
+        pair_terms((xa + ox) - a.x, fmaf(rowa - c.y, khf, yca - c.x), va.x - v.x, va.y - v.y, sa,
+                   Pa, Ia, Ra2, v.z, v.w, sm.inv[j], K, acc);
+    }
+}
+
+template <int MODE, bool STORED_P, class SH>
+__global__ void __launch_bounds__(kRecT, 8)
+k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
+            const uint32_t *__restrict__ wstart, WallState<float> Wl, Grid g, Phys<float> P,
+            TileConst K, OldState<float> O, float dt, PairOut out, PairRec RF, PairRec RW,
+            const WinRec *__restrict__ table, const int *__restrict__ nwin,
+            uint32_t *__restrict__ health) {
+    __shared__ __align__(16) RecSmem<SH> sm;
+    pdl_enter();
+    const int tid = threadIdx.x;
+    const int ncy = g.ncy;
+    const float khf = g.khf;
+    const int nw = __ldg(nwin + blockIdx.x);
+    if (nw == 0) return;
+    if (tid == 0) {
+        mbar_init(&sm.bar, 1);
+        fence_mbar_init();
+    }
+    if (tid < 4) sm.offx[tid] = tid < 3 ? (float)(1 - tid) * khf : 0.f;
+    uint32_t parity = 0u;
+    for (int wi = 0; wi < nw; wi++) {
+        __syncthreads();  // the previous window is finished with shared memory
+        if (tid == 0) {
+            // the window's record, then one bulk copy per record array and
+            // segment and per offset run, all completing on the mbarrier
+            const WinRec R = table[(size_t)blockIdx.x * kRecMaxWin + wi];
+            sm.win = R;
+            if (R.mode == kRecStaged) {
+                uint32_t bytes = (uint32_t)R.tot * 36u;
+                int at = 0;
+                for (int sgi = 0; sgi < 6; sgi++) {
+                    sm.base[sgi] = at - R.first[sgi];
+                    at += R.n[sgi];
+                }
+                for (int d = 0; d < 3; d++) {
+                    const int col = R.cx + d - 1;
+                    if (col >= 0 && col < g.ncx) bytes += 2u * 4u * (uint32_t)kRecOffRun;
+                }
+                fence_proxy_async_smem();  // the previous window's reads before the copies
+                mbar_expect_tx(&sm.bar, bytes);
+                at = 0;
+                for (int sgi = 0; sgi < 6; sgi++) {
+                    const int c = R.n[sgi];
+                    if (c > 0) {
+                        const bool fl = sgi & 1;
+                        const int j = R.first[sgi];
+                        bulk_g2s(&sm.t[at], (fl ? RF.t : RW.t) + j, (uint32_t)c * 8u, &sm.bar);
+                        bulk_g2s(&sm.y[at], (fl ? RF.y : RW.y) + j, (uint32_t)c * 8u, &sm.bar);
+                        bulk_g2s(&sm.v[at], (fl ? RF.v : RW.v) + j, (uint32_t)c * 16u, &sm.bar);
+                        bulk_g2s(&sm.inv[at], (fl ? RF.inv : RW.inv) + j, (uint32_t)c * 4u,
+                                 &sm.bar);
+                    }
+                    at += c;
+                }
+                for (int d = 0; d < 3; d++) {
+                    const int col = R.cx + d - 1;
+                    if (col >= 0 && col < g.ncx) {
+                        const int so = col * ncy + R.rlo, sa = so & ~3;
+                        sm.oshift[d] = so - sa;
+                        bulk_g2s(&sm.foff[d][0], fstart + sa, 4u * kRecOffRun, &sm.bar);
+                        bulk_g2s(&sm.woff[d][0], wstart + sa, 4u * kRecOffRun, &sm.bar);
+                    }
+                }
+            }
+        }
+        __syncthreads();  // the window's record is visible
+        const int cur = sm.win.cur, we = sm.win.we, cx = sm.win.cx, rlo = sm.win.rlo;
+        const int mode = sm.win.mode;
+        const int i = cur + tid;
+        const bool active = i < we;
+        // the corrector's old state, fetched while the window is staged
+        double2 ro_r = make_double2(0., 0.);
+        float2 ro_v = make_float2(0.f, 0.f);
+        float ro_s = 0.f;
+        if (MODE == MODE_CORRECT && active) {
+            ro_r = O.r[i];
+            ro_v = O.v[i];
+            ro_s = O.rho[i];
+        }
+        Acc4 acc = {0.f, 0.f, 0.f, 0.f};
+        float Ia = 0.f;
+        int cxa = cx, cy = 0;
+        const unsigned amask = __ballot_sync(0xffffffffu, active);  // the warp's targets
+        if (mode == kRecStaged) {
+            const bool ok = mbar_wait(&sm.bar, parity);
+            parity ^= 1u;
+            if (!ok) {
+                // the copies did not complete in time: record it, give them one
+                // more bounded wait, and leave without touching the window
+                if (tid == 0) atomicOr(health, kHealthStall);
+                mbar_wait(&sm.bar, parity ^ 1u);
+                return;
+            }
+            const bool walls = (sm.win.n[0] | sm.win.n[2] | sm.win.n[4]) != 0;
+            if (active) {
+                const int own = sm.base[3] + i;
+                const float2 at_ = sm.t[own], ay_ = sm.y[own];
+                const float4 av = sm.v[own];
+                Ia = sm.inv[own];
+                const float xa = at_.x, ya = at_.y, yca = ay_.x, rowa = ay_.y;
+                cy = (int)rowa;
+                const float2 va = make_float2(av.x, av.y);
+                const float sa = av.z, Pa = av.w, Ra2 = K.two_rho0 + sa;
+                const float ybot = ya - K.reach, ytop = ya + K.reach;
+                uint16_t *const lst = sm.list + tid;
+                uint16_t *const wend = lst + SH::list * kRecT;
+                uint16_t *w = lst;
+                const int q = cy - rlo;
+                const int qlo = cy >= 1 ? q - 1 : q, qhi = cy + 1 < ncy ? q + 2 : q + 1;
+#pragma unroll
+                for (int d = 0; d < 3; d++) {
+                    const int col = cx + d - 1;
+                    if (col < 0 || col >= g.ncx) continue;
+                    const float xd = xa + (float)(1 - d) * khf;  // the target's x in column d's frame
+                    const int osh = sm.oshift[d];
+                    if (walls) {  // walls of the three rows (few; scanned whole)
+                        const int s = sm.base[2 * d] + sm.woff[d][qlo + osh];
+                        const int e = sm.base[2 * d] + sm.woff[d][qhi + osh];
+                        // the list is summed and emptied, by the whole warp
+                        // together, when some lane's list might overflow
+                        if (__any_sync(amask, wend - w < (e - s) * kRecT)) {
+                            rec_eval(sm, lst, (int)((w - lst) / kRecT), xa, yca, rowa, va, sa, Pa,
+                                     Ia, Ra2, khf, K, acc);
+                            w = lst;
+                        }
+                        for (int j = s; j < e; j++) {
+                            const float2 l = sm.t[j];
+                            const float dx = xd - l.x, dy = ya - l.y;
+                            *w = (uint16_t)(((uint32_t)j << 2) | (uint32_t)d);
+                            w += fmaf(dx, dx, dy * dy) <= K.four_h2 ? kRecT : 0;
+                        }
+                    }
+                    // the column's y-window [ybot, ytop] of the fluid rows
+                    const int bf = sm.base[2 * d + 1];
+                    const int re = bf + sm.foff[d][qhi + osh];
+                    const int lo = rec_bound<false>(sm.t, bf + sm.foff[d][qlo + osh], re, ybot);
+                    const int e = rec_bound<true>(sm.t, lo, re, ytop);
+                    if (__any_sync(amask, wend - w < (e - lo) * kRecT)) {
+                        rec_eval(sm, lst, (int)((w - lst) / kRecT), xa, yca, rowa, va, sa, Pa, Ia,
+                                 Ra2, khf, K, acc);
+                        w = lst;
+                    }
+                    if (d == 1) w = rec_scan<true>(sm.t, lo, e, xd, ya, K.four_h2, 1u, w);
+                    else w = rec_scan<false>(sm.t, lo, e, xd, ya, K.four_h2, (uint32_t)d, w);
+                }
+                rec_eval(sm, lst, (int)((w - lst) / kRecT), xa, yca, rowa, va, sa, Pa, Ia, Ra2,
+                         khf, K, acc);
+            }
+        } else if (active) {
+            // neighbour block too large for shared memory (or a chunk with more
+            // windows than the table holds): every target from global memory
+            const uint32_t ki = __ldg(F.key + i);
+            cxa = (int)(ki / (uint32_t)ncy);
+            cy = (int)ki - cxa * ncy;
+            const float2 la = __ldg(F.loc + i);
+            const float2 va = __ldg(F.v + i);
+            const float sa = __ldg(F.rho + i);
+            Ia = rcp_approx(P.rho0 + sa);
+            const float pa = STORED_P ? __ldg(F.p + i) : eos(sa, P);
+            target_global<STORED_P>(F, fstart, wstart, Wl, g, P, K, i, cxa, cy, la, va, sa, pa * Ia,
+                                    Ia, K.two_rho0 + sa, acc);
+        }
+        if (active) {
+            const float mb = P.m * P.bwen_h;
+            const float ax = acc.ax * mb;
+            const float ay = fmaf(acc.ay, mb, -P.g);
+            const float drho = mb * fmaf(-P.k_psi, acc.diff, acc.cont);
+            if constexpr (MODE == MODE_FORCES) {
+                F.a[i] = make_float2(ax, ay);
+                F.drho[i] = drho;
+            } else {
+                // Integrate_SymplecticCorrector (src/SPH_integration.h:289-309),
+                // as in k_pairs_tiled
+                const float e = -drho * Ia * dt;
+                const float ie = rcp_approx(2.f + e);
+                const float s_new = ro_s * ((2.f - e) * ie) - P.rho0 * (2.f * e * ie);
+                const float2 nv = make_float2(fmaf(ax, dt, ro_v.x), fmaf(ay, dt, ro_v.y));
+                const float hdt = 0.5f * dt;
+                const double2 rn = make_double2(ro_r.x + (double)((nv.x + ro_v.x) * hdt),
+                                                ro_r.y + (double)((nv.y + ro_v.y) * hdt));
+                out.r[i] = rn;
+                reinterpret_cast<float2 *>(out.v)[i] = nv;
+                reinterpret_cast<float *>(out.rho)[i] = s_new;
+                uint32_t nk;
+                if (out_of_domain_bits(rn, out.boxb)) {
+                    nk = (uint32_t)g.ncells;
+                    atomicOr(health, kHealthRemoved);
+                } else {
+                    int ncx_, ncy_;
+                    nk = cell_key(g, rn, (uint32_t)(cxa * ncy + cy), &ncx_, &ncy_);
+                    if (nk == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
+                }
+                if (!(nv.x == nv.x) || !(nv.y == nv.y) || !(s_new == s_new))
+                    atomicOr(health, kHealthNan);
+                out.key[i] = nk;
+                out.slot[i] = atomicAdd(out.counts + nk, 1u);
+            }
+        }
+    }
+}
+
+}  // namespace tsph

@@ -18,6 +18,8 @@ import numpy as np
 from . import build as _build
 
 # status codes (tsph.h)
+N_TILE_SHAPES = 3  # pair-kernel variants (TSPH_N_TILE_SHAPES)
+TILE_SHAPES = {"wide": 0, "deep": 1, "rec": 2}
 OK, ERR_ARG, ERR_CUDA, ERR_STATE, ERR_NOMEM, ERR_NUMERIC, ERR_DENSITY, ERR_ESCAPED, \
     ERR_UNSUPPORTED = range(9)
 FLUID, WALL = 0, 1
@@ -523,10 +525,10 @@ class ParticleSystem:
         _check(self._L.tsph_state_restore(self._h))
 
     def autotune(self):
-        """Time both tile shapes of the pair kernel, keep the faster:
-        (shape, [us shape 0, us shape 1])."""
+        """Time every variant of the pair kernel, keep the fastest:
+        (variant, [median us of each variant])."""
         c = C.c_int32()
-        us = np.zeros(2)
+        us = np.zeros(N_TILE_SHAPES)
         _check(self._L.tsph_autotune(self._h, C.byref(c), _p(us)))
         return c.value, us
 
