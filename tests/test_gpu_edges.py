@@ -105,12 +105,14 @@ def test_boundary_integral_isolated_particle(gpu_tsph, oracle_mod):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp64", "fp32"])
-def test_particle_thrown_out_inside_the_fused_step(gpu_tsph, oracle_mod, precision):
+@pytest.mark.parametrize("precision,variant", [("fp64", None), ("fp32", 0), ("fp32", 2)])
+def test_particle_thrown_out_inside_the_fused_step(gpu_tsph, oracle_mod, precision, variant):
     ps = _set()
     geo.create_block_of_fluid(ps, 0.3, 0.3, 0.4, 0.4)
     case = _case(ps, 0)
     g = gpu_tsph.ParticleSystem.from_case(case, precision)
+    if variant is not None:
+        g.set_tile_shape(variant)
     o = oracle_mod.PortSystem.from_case(case)
     st = g.download()
     v = st["v"].copy()

@@ -12,11 +12,13 @@ import pytest
 from tinysph_old_gb300 import cases
 
 
-def _run(gpu_tsph, case, precision, steps, pdl):
+def _run(gpu_tsph, case, precision, steps, pdl, variant=None):
     old = os.environ.get("TSPH_PDL")
     os.environ["TSPH_PDL"] = "1" if pdl else "0"
     try:
         s = gpu_tsph.ParticleSystem.from_case(case, precision)
+        if variant is not None:
+            s.set_tile_shape(variant)
         s.step(case.wall_model, case.dt, steps)
         return s.download()
     finally:
@@ -27,14 +29,14 @@ def _run(gpu_tsph, case, precision, steps, pdl):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("precision,variant", [("fp32", 0), ("fp32", 2), ("fp64", None)])
 @pytest.mark.parametrize("builder,steps", [
     (lambda: cases.dam_break_mdbc(dp=0.005), 300),
     (lambda: cases.still_water_dbc(dp=0.01), 300),
     (lambda: cases.outlet_channel_mdbc(dp=0.005), 300),
 ])
-def test_pdl_on_and_off_agree_bit_for_bit(gpu_tsph, builder, steps, precision):
-    a = _run(gpu_tsph, builder(), precision, steps, True)
-    b = _run(gpu_tsph, builder(), precision, steps, False)
+def test_pdl_on_and_off_agree_bit_for_bit(gpu_tsph, builder, steps, precision, variant):
+    a = _run(gpu_tsph, builder(), precision, steps, True, variant)
+    b = _run(gpu_tsph, builder(), precision, steps, False, variant)
     for f in ("r", "v", "rho", "p", "type"):
         assert np.array_equal(a[f], b[f]), f

@@ -78,7 +78,7 @@ template <typename T> class Engine final : public EngineBase {
     FluidState<T> Fsv_{};          // the saved state (tsph_state_save)
     T *wsv_ = nullptr;             // saved wall rho, drho, p, rho_o (4 nw)
     uint32_t *fstart_sv_ = nullptr;
-    bool saved_ = false, saved_cells_ = false;
+    bool saved_ = false, saved_cells_ = false, saved_kept_ = false;
     bool kicked_ = false;          // a kick (apply_update phase 1) awaits its drift
     bool capturing_ = false;       // enqueue_step is being captured into a graph
     cudaStream_t st2_ = nullptr;   // side stream: captures the conditional re-binning body
@@ -94,13 +94,14 @@ template <typename T> class Engine final : public EngineBase {
     // ---- graphs keyed by (model, dt bits)
     std::map<std::pair<int, long long>, cudaGraphExec_t> graphs_;
     // kernel launches: eager ones counted as they are made; a graph's kernels
-    // counted at capture (outside / inside the conditional re-binning body),
-    // its launches then add the outside ones and the body's executions
-    // (counted on the device in rebins_) add the body's
+    // counted at capture (outside / inside each conditional body: 1 the
+    // re-binning after the predictor, 2 the sort after the corrector, 3 the
+    // in-order copy instead of it), its launches then add the outside ones and
+    // the bodies' executions (counted on the device in body_runs_) add theirs
     long long launched_ = 0;
-    int cap_main_ = 0, cap_body_ = 0, body_kernels_ = 0;
-    bool in_body_ = false;
-    uint32_t *rebins_ = nullptr;
+    int cap_main_ = 0, cap_body_[4] = {0, 0, 0, 0}, body_kernels_[4] = {0, 0, 0, 0};
+    int body_ = 0;  // the conditional body being captured (0: none)
+    uint32_t *body_runs_ = nullptr;  // [1..3]: executions of each body
     std::map<std::pair<int, long long>, int> graph_kernels_;
 
     // ---- profiling
@@ -152,7 +153,7 @@ template <typename T> class Engine final : public EngineBase {
             cudaEventRecord(a, st_);
         }
         if (!capturing_) launched_++;
-        else if (in_body_) cap_body_++;
+        else if (body_) cap_body_[body_]++;
         else cap_main_++;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3((unsigned)grid);
@@ -231,7 +232,7 @@ template <typename T> class Engine final : public EngineBase {
                     const T2 *sa, const T *sdrho, const T *sp, FluidState<T> D,
                     const double2 *or2, const T2 *ov2, const T *orho2, OldState<T> Od,
                     std::string &err, const uint32_t *gate = nullptr,
-                    const uint8_t *stype = nullptr) {
+                    const uint8_t *stype = nullptr, uint32_t *runs = nullptr) {
         int rc;
         if ((rc = scan(err, gate))) return rc;
         const int *ntot = reinterpret_cast<const int *>(fstart_ + ncells_ + 1);
@@ -247,7 +248,7 @@ template <typename T> class Engine final : public EngineBase {
                       (const uint32_t *)tmp_src_,
                       by_y ? (const long long *)tmp_y_ : (const long long *)nullptr, grid_, sr, sv,
                       srho, sid, sa, sdrho, sp, D, or2, ov2, orho2, Od, gate,
-                      D.type ? stype : (const uint8_t *)nullptr);
+                      D.type ? stype : (const uint8_t *)nullptr, lbin_, gen_, runs);
     }
 
     // the histogram is zero between sorts (the scan clears it)
@@ -273,8 +274,18 @@ template <typename T> class Engine final : public EngineBase {
     PairRec rec_f_{}, rec_s_{}, rec_w_{};
     WinRec *rec_table_ = nullptr;  // windows of each chunk of 128 targets
     int *rec_nwin_ = nullptr;
-    TileConst Krec_{}, Krec_skin_{};
+    TileConst Krec_{}, Krec_build_{};  // pair terms / list building (radius 2h + 2 sigma)
     bool rec_setup_ = false;
+    int tiled_best_ = 0;  // the faster of shapes 0 and 1 (per-function calls with shape 2)
+    // cells kept over several steps (fused step with shape 2)
+    float2 *lbin_ = nullptr;      // cell-relative positions at the last binning (F_ order)
+    float2 *bloc_ = nullptr;      // the corrector's new cell-relative positions
+    uint16_t *rec_list_ = nullptr;
+    uint8_t *rec_cnt_ = nullptr;
+    uint32_t *gen_ = nullptr;     // {sorts, sort the lists were built after, pass builds}
+    uint32_t *need_sort_ = nullptr;
+    float sig2_ = 0.f;
+    bool cells_kept_ = false;     // F_ moved since its binning (within sigma)
 
   public:
     // time every pair-kernel variant on the current particles (forces pass,
@@ -293,6 +304,8 @@ template <typename T> class Engine final : public EngineBase {
                 err = "cell lists are stale: call tsph_particle_to_cell first";
                 return 3;
             }
+            int rc0;
+            if ((rc0 = ensure_exact_cells(err))) return rc0;
             const bool prof = prof_;
             prof_ = false;
             TSPH_CK(cudaMemcpyAsync(Bv_, F_.a, sizeof(T2) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
@@ -304,10 +317,17 @@ template <typename T> class Engine final : public EngineBase {
             int rc = 0;
             for (int shape = 0; shape < kShapes && !rc; shape++) {
                 tile_shape_ = shape;
-                rc = fluid_pairs<MODE_FORCES>(F_, false, T(0), PairOut{}, err);  // warm
+                tiled_best_ = shape == 2 ? tiled_best_ : shape;
+                // shape 2 as the fused step runs it: the first pass builds the
+                // lists (its state is as binned), the timed ones sum them
+                auto pass = [&]() {
+                    return shape == 2 ? fluid_pairs_rec<MODE_FORCES>(F_, T(0), PairOut{}, err)
+                                      : fluid_pairs<MODE_FORCES>(F_, false, T(0), PairOut{}, err);
+                };
+                rc = pass();  // warm
                 cudaEventRecord(evs[0], st_);
                 for (int rep = 0; rep < kReps && !rc; rep++) {
-                    rc = fluid_pairs<MODE_FORCES>(F_, false, T(0), PairOut{}, err);
+                    rc = pass();
                     cudaEventRecord(evs[rep + 1], st_);
                 }
                 if (rc) break;
@@ -317,6 +337,7 @@ template <typename T> class Engine final : public EngineBase {
                     cudaEventElapsedTime(&t[rep], evs[rep], evs[rep + 1]);
                 std::sort(t.begin(), t.end());
                 med[shape] = 0.5 * (t[kReps / 2 - 1] + t[kReps / 2]);
+                if (shape == 1) tiled_best_ = med[1] < med[0] ? 1 : 0;
             }
             for (auto &e : evs) ev_pool_.push_back(e);
             prof_ = prof;
@@ -525,6 +546,7 @@ template <typename T> class Engine final : public EngineBase {
         TSPH_CK(cudaGetLastError());
         saved_ = true;
         saved_cells_ = cells_;
+        saved_kept_ = cells_kept_;
         return 0;
     }
 
@@ -538,9 +560,10 @@ template <typename T> class Engine final : public EngineBase {
                                 cudaMemcpyDeviceToDevice, st_));
         TSPH_CK(cudaGetLastError());
         cells_ = saved_cells_;
+        cells_kept_ = saved_kept_;
         exported_ = false;
         kicked_ = false;
-        return 0;
+        return mark_stale(err);
     }
 
     int set_tile_shape(int shape, std::string &err) override {
@@ -599,42 +622,10 @@ template <typename T> class Engine final : public EngineBase {
             const int nb = blocks_for(nf_, kTileT);
             const TileConst K = skinned ? Kskin_ : K_;
             const uint32_t *fs = fstart_, *ws = wstart_;
-            if (tile_shape_ == 2) {
-                int rc;
-                if (!rec_setup_) {
-                    const void *kr[4] = {(const void *)k_pairs_rec<MODE_FORCES, false, RecStd>,
-                                         (const void *)k_pairs_rec<MODE_FORCES, true, RecStd>,
-                                         (const void *)k_pairs_rec<MODE_CORRECT, false, RecStd>,
-                                         (const void *)k_pairs_rec<MODE_CORRECT, true, RecStd>};
-                    for (const void *k : kr)
-                        TSPH_CK(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
-                                                     (int)cudaSharedmemCarveoutMaxShared));
-                    rec_setup_ = true;
-                }
-                const PairRec RX = X.r == Fs_.r ? rec_s_ : rec_f_;
-                const int nchunks = blocks_for(nf_, kRecT);
-                const int rb = blocks_for((long long)nw_ + nf_);
-                const int tb = rb + blocks_for(nchunks);
-                const WinRec *tab = rec_table_;
-                const int *nwin = rec_nwin_;
-                if (stored_p)
-                    rc = launch(CAT_PAIR, k_pair_records<true>, tb, kBlock, err, X, fs, W_, nw_,
-                                grid_, P_, RX, rec_w_, rb, ws, nchunks, RecStd::cap, rec_table_,
-                                rec_nwin_);
-                else
-                    rc = launch(CAT_PAIR, k_pair_records<false>, tb, kBlock, err, X, fs, W_, nw_,
-                                grid_, P_, RX, rec_w_, rb, ws, nchunks, RecStd::cap, rec_table_,
-                                rec_nwin_);
-                if (rc) return rc;
-                const TileConst KR = skinned ? Krec_skin_ : Krec_;
-                if (stored_p)
-                    return launch(CAT_PAIR, k_pairs_rec<MODE, true, RecStd>, nchunks, kRecT, err, X,
-                                  fs, ws, W_, grid_, P_, KR, O_, dt, po, RX, rec_w_, tab, nwin,
-                                  health_);
-                return launch(CAT_PAIR, k_pairs_rec<MODE, false, RecStd>, nchunks, kRecT, err, X,
-                              fs, ws, W_, grid_, P_, KR, O_, dt, po, RX, rec_w_, tab, nwin, health_);
-            }
-            if (tile_shape_ == 1) {
+            // shape 2 keeps its lists only inside the fused step (fluid_pairs_rec);
+            // every other pair pass takes the faster tiled shape
+            const int shape = tile_shape_ == 2 ? tiled_best_ : tile_shape_;
+            if (shape == 1) {
                 if (stored_p)
                     return launch(CAT_PAIR, k_pairs_tiled<MODE, true, TileDeep>, nb, kTileT, err,
                                   X, fs, ws, W_, grid_, P_, K, O_, dt, po, health_);
@@ -655,13 +646,71 @@ template <typename T> class Engine final : public EngineBase {
         }
     }
 
+    // the pair pass over pair records with kept lists (shape 2, the fused
+    // step and the autotuner): the records kernel forms X's records and the
+    // window table and decides whether this pass builds the lists (a sort
+    // happened since they were built) or sums the stored ones
+    template <int MODE>
+    int fluid_pairs_rec(const FluidState<T> &X, T dt, PairOut po, std::string &err,
+                        cudaGraphConditionalHandle cond_sort = 0,
+                        cudaGraphConditionalHandle cond_copy = 0) {
+        if constexpr (std::is_same<T, float>::value) {
+            int rc;
+            if (!rec_setup_) {
+                const void *kr[2] = {(const void *)k_pairs_rec<MODE_FORCES, false, RecStd>,
+                                     (const void *)k_pairs_rec<MODE_CORRECT, false, RecStd>};
+                for (const void *k : kr)
+                    TSPH_CK(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                                 (int)cudaSharedmemCarveoutMaxShared));
+                rec_setup_ = true;
+            }
+            const uint32_t *fs = fstart_, *ws = wstart_;
+            const PairRec RX = X.r == Fs_.r ? rec_s_ : rec_f_;
+            const int nchunks = blocks_for(nf_, kRecT);
+            const int rb = blocks_for((long long)nw_ + nf_);
+            const int tb = rb + blocks_for(nchunks);
+            if ((rc = launch(CAT_PAIR, k_pair_records<false>, tb, kBlock, err, X, fs, W_, nw_, grid_,
+                             P_, RX, rec_w_, rb, ws, nchunks, RecStd::cap, rec_table_, rec_nwin_,
+                             gen_)))
+                return rc;
+            RecStep S{rec_list_, rec_cnt_, gen_, (const float2 *)lbin_, sig2_, bloc_, need_sort_,
+                      cond_sort, cond_copy, capturing_ ? 1 : 0};
+            return launch(CAT_PAIR, k_pairs_rec<MODE, false, RecStd>, nchunks, kRecT, err, X, fs, ws,
+                          W_, grid_, P_, Krec_, Krec_build_, O_, dt, po, RX, rec_w_,
+                          (const WinRec *)rec_table_, (const int *)rec_nwin_, S, health_);
+        } else {
+            (void)X;
+            (void)dt;
+            (void)po;
+            (void)cond_sort;
+            (void)cond_copy;
+            err = "pair records: FP32 build only";
+            return 8;
+        }
+    }
+
+    // cells kept over several steps are re-binned at the current positions
+    // before anything that needs the reference's cells (tiled pair passes,
+    // cell lists, pair digests)
+    int ensure_exact_cells(std::string &err) {
+        if (!cells_kept_) return 0;
+        return particle_to_cell(err);
+    }
+
+    // the state changed outside the fused step: neighbour lists and binning
+    // positions are stale (the next fused step re-bins first)
+    int mark_stale(std::string &err) {
+        TSPH_CK(cudaMemsetAsync(gen_ + 1, 0xff, 4, st_));
+        return 0;
+    }
+
     // re-binning of the predicted state Fs_ (+ old state O_): sort into F_
     // and B, copy back (FP32 fused step, when the skin was exceeded)
     int rebin_predicted(const uint32_t *gate, std::string &err) {
         int rc;
         if ((rc = launch(CAT_SORT, k_bin_gated<T>, blocks_for(nf_), kBlock, err,
                          (const FluidState<T>)Fs_, (const uint32_t *)fstart_, grid_, keyB_, slotB_,
-                         counts_, health_, gate, in_body_ ? rebins_ : (uint32_t *)nullptr)))
+                         counts_, health_, gate, body_ == 1 ? body_runs_ + 1 : (uint32_t *)nullptr)))
             return rc;
         if ((rc = sort_finish(Fs_.r, Fs_.v, Fs_.rho, Fs_.id, nullptr, nullptr, nullptr, F_, O_.r,
                               O_.v, O_.rho, OldState<T>{Br_, Bv_, Brho_}, err, gate)))
@@ -669,6 +718,44 @@ template <typename T> class Engine final : public EngineBase {
         return launch(CAT_SORT, k_copy_back<T>, blocks_for(nf_), kBlock, err,
                       (const FluidState<T>)F_, (const double2 *)Br_, (const T2 *)Bv_,
                       (const T *)Brho_, (const uint32_t *)fstart_, ncells_, Fs_, O_, gate);
+    }
+
+    // during capture: an IF node on `cond` after the current work, its body
+    // captured from `body` (kernels counted as conditional body `id`)
+    template <typename F>
+    int add_cond_body(cudaGraphConditionalHandle cond, int id, const char *what, F body,
+                      std::string &err) {
+        cudaGraph_t cg = nullptr;
+        cudaStreamCaptureStatus cs;
+        const cudaGraphNode_t *deps = nullptr;
+        size_t nd = 0;
+        TSPH_CK(cudaStreamGetCaptureInfo(st_, &cs, nullptr, &cg, &deps, nullptr, &nd));
+        cudaGraphNodeParams np = {};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = cond;
+        np.conditional.type = cudaGraphCondTypeIf;
+        np.conditional.size = 1;
+        cudaGraphNode_t cn;
+        TSPH_CK(cudaGraphAddNode(&cn, cg, deps, nullptr, nd, &np));
+        cudaGraph_t g = np.conditional.phGraph_out[0];
+        if (!st2_) TSPH_CK(cudaStreamCreateWithFlags(&st2_, cudaStreamNonBlocking));
+        TSPH_CK(cudaStreamBeginCaptureToGraph(st2_, g, nullptr, nullptr, 0,
+                                              cudaStreamCaptureModeThreadLocal));
+        std::swap(st_, st2_);
+        body_ = id;
+        int rc = body();
+        body_ = 0;
+        std::swap(st_, st2_);
+        cudaGraph_t bodyc = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(st2_, &bodyc);
+        if (rc) return rc;
+        if (e != cudaSuccess) {
+            err = std::string("cudaStreamEndCapture (") + what + "): " + cudaGetErrorString(e);
+            return 2;
+        }
+        TSPH_CK(cudaStreamUpdateCaptureDependencies(st_, &cn, nullptr, 1,
+                                                    cudaStreamSetCaptureDependencies));
+        return 0;
     }
 
     // one fused step (enqueue only)
@@ -680,6 +767,13 @@ template <typename T> class Engine final : public EngineBase {
         if constexpr (std::is_same<T, float>::value) skinned = skin_ > 0.f;
         // FP32 mDBC step with the skin: mDBC and the predictor share a launch
         const bool mdbc_fused = model == 0 && nw_ > 0 && skinned;
+        // pair records with kept lists (shape 2): the cells are kept over
+        // several steps, re-binned after the predictor when a particle moved
+        // sigma since its binning or the lists are stale, and after the
+        // corrector when a particle moved sigma or left the domain
+        const bool rec = skinned && tile_shape_ == 2 && model != 2 && !zones_on_;
+        const KeepCells kc = rec ? KeepCells{(const float2 *)lbin_, sig2_, gen_, need_sort_}
+                                 : KeepCells{nullptr, 0.f, nullptr, nullptr};
         if (model == 0 && !mdbc_fused && (rc = do_mdbc(err))) return rc;
         if (model == 2 && (rc = do_bt_density(err))) return rc;
         if (skinned) {
@@ -702,14 +796,14 @@ template <typename T> class Engine final : public EngineBase {
                     const int nbm = blocks_for((long long)nw_ * kMdbcLanes);
                     rc = launch(CAT_MDBC, k_mdbc_f32_predict, nbm + blocks_for(nf_), kBlock, err, W_,
                                 nw_, nbm, (const uint32_t *)fstart_, F_, grid_, P_, dt, Fs_, O_,
-                                skin_, rebuild_, health_, cond, capturing_ ? 1 : 0);
+                                skin_, rebuild_, health_, cond, capturing_ ? 1 : 0, kc);
                     if (rc) return rc;
                 }
             }
             if (!mdbc_fused &&
                 (rc = launch(CAT_OTHER, k_predict_keep<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
                              (const uint32_t *)fstart_, W_, nw_, grid_, dt, Fs_, O_, skin_,
-                             rebuild_, health_, cond, capturing_ ? 1 : 0)))
+                             rebuild_, health_, cond, capturing_ ? 1 : 0, kc)))
                 return rc;
             if (capturing_) {
                 TSPH_CK(cudaStreamGetCaptureInfo(st_, &cs, nullptr, &cg, &deps, nullptr, &nd));
@@ -725,9 +819,9 @@ template <typename T> class Engine final : public EngineBase {
                 TSPH_CK(cudaStreamBeginCaptureToGraph(st2_, body, nullptr, nullptr, 0,
                                                       cudaStreamCaptureModeThreadLocal));
                 std::swap(st_, st2_);
-                in_body_ = true;
+                body_ = 1;
                 rc = rebin_predicted(nullptr, err);
-                in_body_ = false;
+                body_ = 0;
                 std::swap(st_, st2_);
                 cudaGraph_t bodyc = nullptr;
                 const cudaError_t e = cudaStreamEndCapture(st2_, &bodyc);
@@ -756,16 +850,59 @@ template <typename T> class Engine final : public EngineBase {
         // forces at the predicted state + corrector + bin
         if ((rc = zero_counts(err))) return rc;
         PairOut po{Br_, (void *)Bv_, (void *)Brho_, keyB_, slotB_, counts_, box_, make_box_bits(box_)};
+        auto wall_rows = [&]() -> int {
+            if (nw_ == 0) return 0;
+            return launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
+                          (const uint32_t *)fstart_, nbr_fluid(Fs_, false), grid_, P_, dbc, true, dt,
+                          (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
+                          (const uint32_t *)nullptr, false);
+        };
+        auto sort_new = [&](const uint32_t *gate, uint32_t *runs) -> int {
+            return sort_finish(Br_, Bv_, Brho_, Fs_.id, nullptr, nullptr, nullptr, F_, nullptr,
+                               nullptr, nullptr, O_, err, gate, nullptr, runs);
+        };
+        if (rec) {
+            cudaGraphConditionalHandle cs_ = 0, cc_ = 0;
+            if (capturing_) {
+                cudaGraph_t cg = nullptr;
+                cudaStreamCaptureStatus cst;
+                TSPH_CK(cudaStreamGetCaptureInfo(st_, &cst, nullptr, &cg, nullptr, nullptr, nullptr));
+                TSPH_CK(cudaGraphConditionalHandleCreate(&cs_, cg, 0, cudaGraphCondAssignDefault));
+                TSPH_CK(cudaGraphConditionalHandleCreate(&cc_, cg, 1, cudaGraphCondAssignDefault));
+            }
+            if ((rc = fluid_pairs_rec<MODE_CORRECT>(Fs_, dt, po, err, cs_, cc_))) return rc;
+            if ((rc = wall_rows())) return rc;
+            auto copy_kept = [&](const uint32_t *skip, uint32_t *runs) -> int {
+                return launch(CAT_SORT, k_copy_kept<T>, blocks_for(nf_), kBlock, err, F_,
+                              (const double2 *)Br_, (const T2 *)Bv_, (const T *)Brho_,
+                              (const float2 *)bloc_, (const uint32_t *)keyB_, counts_,
+                              (const uint32_t *)fstart_, ncells_, skip, runs);
+            };
+            if (capturing_) {
+                if ((rc = add_cond_body(cs_, 2, "sort body",
+                                        [&]() { return sort_new(nullptr, body_runs_ + 2); }, err)))
+                    return rc;
+                if ((rc = add_cond_body(cc_, 3, "copy body",
+                                        [&]() { return copy_kept(need_sort_, body_runs_ + 3); },
+                                        err)))
+                    return rc;
+            } else {
+                if ((rc = sort_new(need_sort_, nullptr))) return rc;
+                if ((rc = copy_kept(need_sort_, nullptr))) return rc;
+            }
+            // forces at the new state (a, drho for the next predictor)
+            if ((rc = fluid_pairs_rec<MODE_FORCES>(F_, dt, PairOut{}, err))) return rc;
+            if (dbc && nw_ > 0 &&
+                (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
+                             (const uint32_t *)fstart_, nbr_fluid(F_, false), grid_, P_, true, false,
+                             dt, (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
+                             (const uint32_t *)nullptr, false)))
+                return rc;
+            return 0;
+        }
         if ((rc = fluid_pairs<MODE_CORRECT>(Fs_, false, dt, po, err, skinned))) return rc;
-        if (nw_ > 0 &&
-            (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
-                         (const uint32_t *)fstart_, nbr_fluid(Fs_, false), grid_, P_, dbc, true, dt,
-                         (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
-                         (const uint32_t *)nullptr, false)))
-            return rc;
-        if ((rc = sort_finish(Br_, Bv_, Brho_, Fs_.id, nullptr, nullptr, nullptr, F_, nullptr,
-                              nullptr, nullptr, O_, err)))
-            return rc;
+        if ((rc = wall_rows())) return rc;
+        if ((rc = sort_new(nullptr, nullptr))) return rc;
         // forces at the new state (a, drho for the next predictor)
         if ((rc = fluid_pairs<MODE_FORCES>(F_, false, dt, PairOut{}, err))) return rc;
         if (dbc && nw_ > 0 &&
@@ -861,8 +998,14 @@ template <typename T> class Engine final : public EngineBase {
             const float margin = 8.f * std::ldexp(1.f, std::ilogb((float)ytop) - 23);
             Krec_ = K_;
             Krec_.reach = K_.reach + margin;
-            Krec_skin_ = Kskin_;
-            Krec_skin_.reach = Kskin_.reach + margin;
+            // kept cells: a re-binning is due once a particle has moved sigma
+            // (Euclidean) from where it was binned; lists then hold the
+            // neighbours within 2h + 2 sigma (<= kh: inside the 3 x 3 block)
+            sig2_ = skin_ * skin_;
+            const double rl = 2.0 * hs.h + 2.0 * (double)skin_;
+            Krec_build_ = K_;
+            Krec_build_.four_h2 = (float)(rl * rl);
+            Krec_build_.reach = (float)(rl * 1.0001) + margin;
         }
         // grid tables
         int rc;
@@ -906,8 +1049,18 @@ template <typename T> class Engine final : public EngineBase {
             if ((rc = alloc_rec(rec_f_, nf_)) || (rc = alloc_rec(rec_s_, nf_)) ||
                 (rc = alloc_rec(rec_w_, nw_)) ||
                 (rc = alloc(&rec_table_, (size_t)nchunks * kRecMaxWin, err)) ||
-                (rc = alloc(&rec_nwin_, nchunks, err)))
+                (rc = alloc(&rec_nwin_, nchunks, err)) || (rc = alloc(&bloc_, nf_, err)) ||
+                (rc = alloc(&rec_list_, (size_t)nchunks * RecStd::list * kRecT, err)) ||
+                (rc = alloc(&rec_cnt_, (size_t)nchunks * kRecT, err)))
                 return rc;
+        }
+        if ((rc = alloc(&lbin_, nf_, err)) || (rc = alloc(&gen_, 4, err)) ||
+            (rc = alloc(&need_sort_, 1, err)))
+            return rc;
+        {
+            const uint32_t g0[4] = {1u, 0u, 0u, 0u};  // no lists yet: stale
+            TSPH_CK(cudaMemcpy(gen_, g0, 16, cudaMemcpyHostToDevice));
+            TSPH_CK(cudaMemset(need_sort_, 0, 4));
         }
         if (zones_on_) {
             zlist_cap_ = 1 << 16;
@@ -931,12 +1084,12 @@ template <typename T> class Engine final : public EngineBase {
         if ((rc = alloc(&counts_, ncells_ + 1, err)) || (rc = alloc(&fstart_, ncells_ + 32, err)) ||
             (rc = alloc(&wstart_, ncells_ + 32, err)) || (rc = alloc(&tile_sums_, ntiles, err)) ||
             (rc = alloc(&health_, 1, err)) || (rc = alloc(&removed_, 1, err)) ||
-            (rc = alloc(&rebuild_, 1, err)) || (rc = alloc(&rebins_, 1, err)) ||
+            (rc = alloc(&rebuild_, 1, err)) || (rc = alloc(&body_runs_, 4, err)) ||
             (rc = alloc(&dtot_, 4 * (size_t)blocks_for(nf_), err)))
             return rc;
         TSPH_CK(cudaMemset(health_, 0, 4));
         TSPH_CK(cudaMemset(removed_, 0, 4));
-        TSPH_CK(cudaMemset(rebins_, 0, 4));
+        TSPH_CK(cudaMemset(body_runs_, 0, 16));
         TSPH_CK(cudaMemset(counts_, 0, sizeof(uint32_t) * (ncells_ + 1)));
         // staging
         if ((rc = alloc(&S_.r, id_cap_, err)) || (rc = alloc(&S_.v, id_cap_, err)) ||
@@ -1095,6 +1248,7 @@ template <typename T> class Engine final : public EngineBase {
                          (const uint32_t *)fstart_, ncells_)))
             return rc;
         cells_ = true;
+        cells_kept_ = false;
         exported_ = false;
         return collect_profile(err);
     }
@@ -1132,6 +1286,7 @@ template <typename T> class Engine final : public EngineBase {
             return 3;
         }
         int rc;
+        if ((rc = ensure_exact_cells(err))) return rc;
         wall_model_ = model;
         if ((rc = fluid_pairs<MODE_FORCES>(F_, true, T(0), PairOut{}, err))) return rc;
         if (model == 1 && nw_ > 0 &&
@@ -1231,7 +1386,8 @@ template <typename T> class Engine final : public EngineBase {
                 cudaGraph_t g;
                 TSPH_CK(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
                 capturing_ = true;
-                cap_main_ = cap_body_ = 0;
+                cap_main_ = 0;
+                for (int b = 0; b < 4; b++) cap_body_[b] = 0;
                 rc = enqueue_step(model, (T)dt, err);
                 capturing_ = false;
                 cudaGraph_t g2 = nullptr;
@@ -1254,7 +1410,8 @@ template <typename T> class Engine final : public EngineBase {
                 }
                 it = graphs_.emplace(key, ex).first;
                 graph_kernels_[key] = cap_main_;
-                if (cap_body_) body_kernels_ = cap_body_;
+                for (int b = 1; b < 4; b++)
+                    if (cap_body_[b]) body_kernels_[b] = cap_body_[b];
             }
             for (int s = 0; s < nsteps; s++) TSPH_CK(cudaGraphLaunch(it->second, st_));
             launched_ += (long long)nsteps * graph_kernels_[key];
@@ -1264,19 +1421,24 @@ template <typename T> class Engine final : public EngineBase {
                          (const uint32_t *)fstart_, ncells_, W_, nw_, P_, health_)))
             return rc;
         cells_ = true;
+        // with kept lists the cells are those of the last binning, which may
+        // be some steps old (every particle within sigma of where it was binned)
+        if constexpr (std::is_same<T, float>::value)
+            if (skin_ > 0.f && tile_shape_ == 2 && model != 2) cells_kept_ = true;
         exported_ = false;
         return collect_profile(err);
     }
 
     int kernel_launches(long long *count, int reset, std::string &err) override {
         (void)err;
-        uint32_t runs = 0;
-        TSPH_CK(cudaMemcpyAsync(&runs, rebins_, 4, cudaMemcpyDeviceToHost, st_));
+        uint32_t runs[4] = {0, 0, 0, 0};
+        TSPH_CK(cudaMemcpyAsync(runs, body_runs_, 16, cudaMemcpyDeviceToHost, st_));
         TSPH_CK(cudaStreamSynchronize(st_));
-        *count = launched_ + (long long)runs * body_kernels_;
+        *count = launched_;
+        for (int b = 1; b < 4; b++) *count += (long long)runs[b] * body_kernels_[b];
         if (reset) {
             launched_ = 0;
-            TSPH_CK(cudaMemsetAsync(rebins_, 0, 4, st_));
+            TSPH_CK(cudaMemsetAsync(body_runs_, 0, 16, st_));
         }
         return 0;
     }
@@ -1444,6 +1606,8 @@ template <typename T> class Engine final : public EngineBase {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
         }
+        int rc0;
+        if ((rc0 = ensure_exact_cells(err))) return rc0;
         TSPH_CK(cudaStreamSynchronize(st_));
         std::vector<uint32_t> fs(ncells_ + 2), ws(ncells_ + 1), fid(nf_), wid(nw_);
         TSPH_CK(cudaMemcpy(fs.data(), fstart_, 4 * fs.size(), cudaMemcpyDeviceToHost));
@@ -1478,6 +1642,8 @@ template <typename T> class Engine final : public EngineBase {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
         }
+        int rc0;
+        if ((rc0 = ensure_exact_cells(err))) return rc0;
         int rc;
         if (!dig_count_) {
             if ((rc = alloc(&dig_count_, id_cap_, err)) || (rc = alloc(&dig_sum_, id_cap_, err)) ||

@@ -362,10 +362,15 @@ __global__ void k_rank_scatter(const uint32_t *__restrict__ key, const int *__re
                                const double2 *__restrict__ or2, const typename V2<T>::t *__restrict__ ov2,
                                const T *__restrict__ orho2, OldState<T> O,
                                const uint32_t *__restrict__ gate,
-                               const uint8_t *__restrict__ stype) {
+                               const uint8_t *__restrict__ stype, float2 *__restrict__ lbin,
+                               uint32_t *__restrict__ gen, uint32_t *__restrict__ runs) {
     pdl_enter();
     if (gated_off(gate)) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j == 0) {
+        if (gen) atomicAdd(gen, 1u);    // a new order: neighbour lists built before are stale
+        if (runs) atomicAdd(runs, 1u);  // executions of a conditional sort
+    }
     if (j >= *n_ptr) return;
     const uint32_t src = tmp_src[j];
     const uint32_t k = key[src];
@@ -391,13 +396,14 @@ __global__ void k_rank_scatter(const uint32_t *__restrict__ key, const int *__re
     D.rho[f] = srho[src];
     D.id[f] = sid[src];
     D.key[f] = k;
+    float2 l = make_float2(0.f, 0.f);
     if (k < (uint32_t)g.ncells) {
         const int cx = (int)(k / (uint32_t)g.ncy);
         const int cy = (int)k - cx * g.ncy;
-        D.loc[f] = cell_local(g, r, cx, cy);
-    } else {
-        D.loc[f] = make_float2(0.f, 0.f);
+        l = cell_local(g, r, cx, cy);
     }
+    D.loc[f] = l;
+    if (lbin) lbin[f] = l;
     if (sa) D.a[f] = sa[src];
     if (sdrho) D.drho[f] = sdrho[src];
     if (sp) D.p[f] = sp[src];
@@ -1254,6 +1260,19 @@ __global__ void k_predict_bin(FluidState<T> F, const uint32_t *__restrict__ fsta
 // graph, the conditional node `cond`), which runs the re-binning before the
 // pair pass.
 // the predictor of one fluid row f (shared with the mDBC-fused launch)
+// Cells kept over several steps (the pair-record step): a re-binning is due
+// once some particle has moved more than sqrt(sig2) from where it was binned
+// (lbin: its cell-relative position then), or when the neighbour lists are
+// stale (gen[0], the sorts so far, differs from gen[1], the sort they were
+// built after).  With lbin == nullptr the test is the half step's own move
+// against the skin.
+struct KeepCells {
+    const float2 *lbin;
+    float sig2;
+    const uint32_t *gen;
+    uint32_t *clear;  // zeroed by the predictor (the corrector's need-sort flag), or nullptr
+};
+
 template <typename T>
 __device__ __forceinline__ void predict_keep_fluid(int f, const FluidState<T> &F,
                                                    const uint32_t *__restrict__ fstart,
@@ -1261,7 +1280,9 @@ __device__ __forceinline__ void predict_keep_fluid(int f, const FluidState<T> &F
                                                    const OldState<T> &O, float skin,
                                                    uint32_t *__restrict__ rebuild,
                                                    uint32_t *__restrict__ health,
-                                                   cudaGraphConditionalHandle cond, int use_cond) {
+                                                   cudaGraphConditionalHandle cond, int use_cond,
+                                                   const KeepCells &kc) {
+    if (f == 0 && kc.clear) *kc.clear = 0u;
     if (f >= n_live(fstart, g.ncells)) return;
     const double2 r = F.r[f];
     const auto v = F.v[f];
@@ -1279,10 +1300,19 @@ __device__ __forceinline__ void predict_keep_fluid(int f, const FluidState<T> &F
     D.v[f] = nv;
     D.rho[f] = s + F.drho[f] * dt * T(0.5);
     const float2 l = F.loc[f];
-    D.loc[f] = make_float2(l.x + dx, l.y + dy);
+    const float2 ln = make_float2(l.x + dx, l.y + dy);
+    D.loc[f] = ln;
     D.key[f] = F.key[f];
     D.id[f] = F.id[f];
-    if (!(fabsf(dx) <= skin && fabsf(dy) <= skin)) {
+    bool rebin;
+    if (kc.lbin) {
+        const float2 lb = kc.lbin[f];
+        const float ex = ln.x - lb.x, ey = ln.y - lb.y;
+        rebin = !(fmaf(ex, ex, ey * ey) <= kc.sig2) || __ldg(kc.gen) != __ldg(kc.gen + 1);
+    } else {
+        rebin = !(fabsf(dx) <= skin && fabsf(dy) <= skin);
+    }
+    if (rebin) {
         atomicOr(rebuild, 1u);
         if (use_cond) cudaGraphSetConditional(cond, 1u);
     }
@@ -1320,7 +1350,7 @@ __global__ void k_predict_keep(FluidState<T> F, const uint32_t *__restrict__ fst
                                WallState<T> Wl, int nw, Grid g, T dt, FluidState<T> D,
                                OldState<T> O, float skin, uint32_t *__restrict__ rebuild,
                                uint32_t *__restrict__ health, cudaGraphConditionalHandle cond,
-                               int use_cond) {
+                               int use_cond, KeepCells kc) {
     pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nw) {
@@ -1329,7 +1359,8 @@ __global__ void k_predict_keep(FluidState<T> F, const uint32_t *__restrict__ fst
         Wl.rho[i] = r + Wl.drho[i] * dt * T(0.5);
         return;
     }
-    predict_keep_fluid<T>(i - nw, F, fstart, g, dt, D, O, skin, rebuild, health, cond, use_cond);
+    predict_keep_fluid<T>(i - nw, F, fstart, g, dt, D, O, skin, rebuild, health, cond, use_cond,
+                          kc);
 }
 
 // gated re-binning of the predicted state: keys + histogram slots

@@ -72,6 +72,23 @@ struct PairRec {  // one set of pair records (fluid rows or walls)
     float *inv;
 };
 
+// Neighbour lists kept between passes (the fused step).  A pass right after
+// a binning (positions exactly as binned) builds every target's list of the
+// neighbours within 2h + 2 sigma and stores it; later passes, while every
+// particle stays within sigma of where it was binned, sum the stored lists
+// (the kernel factor clamped at zero beyond 2h) with no candidate search.
+struct RecStep {
+    uint16_t *glist;            // [chunk][list][128]: entries (staged index << 2 | column)
+    uint8_t *gcnt;              // [chunk][128]: entries, or 255 (did not fit: global path)
+    uint32_t *gen;              // {sorts, sort the lists were built after, this pass builds}
+    const float2 *lbin;         // cell-relative positions at the binning
+    float sig2;                 // squared displacement allowed since the binning
+    float2 *bloc;               // MODE_CORRECT: new cell-relative position (kept cell)
+    uint32_t *need_sort;        // MODE_CORRECT: set when the cells must be rebuilt
+    cudaGraphConditionalHandle cond_sort, cond_copy;
+    int use_cond;
+};
+
 template <class SH> struct RecSmem {
     float4 v[SH::cap];
     float2 t[SH::cap];
@@ -87,6 +104,7 @@ template <class SH> struct RecSmem {
     int base[6];  // staged index of global row j of segment s = base[s] + j
     WinRec win;
     float offx[4];
+    __align__(16) uint8_t cnt[kRecT];  // stored list lengths of the chunk's targets
     unsigned long long bar;
 };
 
@@ -178,8 +196,15 @@ __global__ void __launch_bounds__(kBlock)
 k_pair_records(FluidState<float> F, const uint32_t *__restrict__ fstart, WallState<float> Wl,
                int nw, Grid g, Phys<float> P, PairRec RF, PairRec RW, int rec_blocks,
                const uint32_t *__restrict__ wstart, int nchunks, int cap,
-               WinRec *__restrict__ table, int *__restrict__ nwin) {
+               WinRec *__restrict__ table, int *__restrict__ nwin, uint32_t *__restrict__ gen) {
     pdl_enter();
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        // the coming pair pass builds the lists when a sort happened since
+        // they were built
+        const uint32_t now = gen[0];
+        gen[2] = now != gen[1] ? 1u : 0u;
+        gen[1] = now;
+    }
     if ((int)blockIdx.x >= rec_blocks) {
         const int c = ((int)blockIdx.x - rec_blocks) * blockDim.x + threadIdx.x;
         if (c < nchunks) rec_window_table(c, cap, F, fstart, wstart, g, table, nwin);
@@ -314,10 +339,10 @@ __device__ __forceinline__ void rec_eval(const RecSmem<SH> &sm, const uint16_t *
         const float2 c0 = sm.y[j0], c1 = sm.y[j1];
         const float4 v0 = sm.v[j0], v1 = sm.v[j1];
         const float i0 = sm.inv[j0], i1 = sm.inv[j1];
-        pair_terms((xa + ox0) - a0.x, fmaf(rowa - c0.y, khf, yca - c0.x), va.x - v0.x,
-                   va.y - v0.y, sa, Pa, Ia, Ra2, v0.z, v0.w, i0, K, acc);
-        pair_terms((xa + ox1) - a1.x, fmaf(rowa - c1.y, khf, yca - c1.x), va.x - v1.x,
-                   va.y - v1.y, sa, Pa, Ia, Ra2, v1.z, v1.w, i1, K, acc);
+        pair_terms<true>((xa + ox0) - a0.x, fmaf(rowa - c0.y, khf, yca - c0.x), va.x - v0.x,
+                         va.y - v0.y, sa, Pa, Ia, Ra2, v0.z, v0.w, i0, K, acc);
+        pair_terms<true>((xa + ox1) - a1.x, fmaf(rowa - c1.y, khf, yca - c1.x), va.x - v1.x,
+                         va.y - v1.y, sa, Pa, Ia, Ra2, v1.z, v1.w, i1, K, acc);
     }
     if (k < cnt) {
         const uint32_t e = lst[k * kRecT];
@@ -325,18 +350,31 @@ __device__ __forceinline__ void rec_eval(const RecSmem<SH> &sm, const uint16_t *
         const float ox = sm.offx[e & 3u];
         const float2 a = sm.t[j], c = sm.y[j];
         const float4 v = sm.v[j];
-        pair_terms((xa + ox) - a.x, fmaf(rowa - c.y, khf, yca - c.x), va.x - v.x, va.y - v.y, sa,
-                   Pa, Ia, Ra2, v.z, v.w, sm.inv[j], K, acc);
+        pair_terms<true>((xa + ox) - a.x, fmaf(rowa - c.y, khf, yca - c.x), va.x - v.x,
+                         va.y - v.y, sa, Pa, Ia, Ra2, v.z, v.w, sm.inv[j], K, acc);
     }
+}
+
+// store a target's current list segment [0, cnt) after the entries already
+// stored (gpos), or mark the list as too long
+__device__ __forceinline__ void rec_store(uint16_t *__restrict__ gl, const uint16_t *lst, int cnt,
+                                          int cap, int &gpos, bool &over) {
+    if (over) return;
+    if (gpos + cnt > cap) {
+        over = true;
+        return;
+    }
+    for (int k = 0; k < cnt; k++) gl[(size_t)(gpos + k) * kRecT] = lst[k * kRecT];
+    gpos += cnt;
 }
 
 template <int MODE, bool STORED_P, class SH>
 __global__ void __launch_bounds__(kRecT, 8)
 k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
             const uint32_t *__restrict__ wstart, WallState<float> Wl, Grid g, Phys<float> P,
-            TileConst K, OldState<float> O, float dt, PairOut out, PairRec RF, PairRec RW,
-            const WinRec *__restrict__ table, const int *__restrict__ nwin,
-            uint32_t *__restrict__ health) {
+            TileConst K, TileConst Kb, OldState<float> O, float dt, PairOut out, PairRec RF,
+            PairRec RW, const WinRec *__restrict__ table, const int *__restrict__ nwin,
+            RecStep S, uint32_t *__restrict__ health) {
     __shared__ __align__(16) RecSmem<SH> sm;
     pdl_enter();
     const int tid = threadIdx.x;
@@ -344,6 +382,10 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
     const float khf = g.khf;
     const int nw = __ldg(nwin + blockIdx.x);
     if (nw == 0) return;
+    const bool build = __ldg(S.gen + 2) != 0u;  // this pass builds and stores the lists
+    const int t0 = blockIdx.x * kRecT;
+    // the chunk's stored lists: column (i - t0) of a [list][128] block
+    uint16_t *const gblock = S.glist + (size_t)blockIdx.x * SH::list * kRecT;
     if (tid == 0) {
         mbar_init(&sm.bar, 1);
         fence_mbar_init();
@@ -354,7 +396,8 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
         __syncthreads();  // the previous window is finished with shared memory
         if (tid == 0) {
             // the window's record, then one bulk copy per record array and
-            // segment and per offset run, all completing on the mbarrier
+            // segment, per offset run (lists built here) or of the chunk's
+            // stored lists (lists kept), all completing on the mbarrier
             const WinRec R = table[(size_t)blockIdx.x * kRecMaxWin + wi];
             sm.win = R;
             if (R.mode == kRecStaged) {
@@ -364,10 +407,14 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                     sm.base[sgi] = at - R.first[sgi];
                     at += R.n[sgi];
                 }
-                for (int d = 0; d < 3; d++) {
-                    const int col = R.cx + d - 1;
-                    if (col >= 0 && col < g.ncx) bytes += 2u * 4u * (uint32_t)kRecOffRun;
+                const bool lists = !build;
+                if (build) {
+                    for (int d = 0; d < 3; d++) {
+                        const int col = R.cx + d - 1;
+                        if (col >= 0 && col < g.ncx) bytes += 2u * 4u * (uint32_t)kRecOffRun;
+                    }
                 }
+                if (lists) bytes += (uint32_t)(SH::list * kRecT * 2 + kRecT);
                 fence_proxy_async_smem();  // the previous window's reads before the copies
                 mbar_expect_tx(&sm.bar, bytes);
                 at = 0;
@@ -384,14 +431,20 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                     }
                     at += c;
                 }
-                for (int d = 0; d < 3; d++) {
-                    const int col = R.cx + d - 1;
-                    if (col >= 0 && col < g.ncx) {
-                        const int so = col * ncy + R.rlo, sa = so & ~3;
-                        sm.oshift[d] = so - sa;
-                        bulk_g2s(&sm.foff[d][0], fstart + sa, 4u * kRecOffRun, &sm.bar);
-                        bulk_g2s(&sm.woff[d][0], wstart + sa, 4u * kRecOffRun, &sm.bar);
+                if (build) {
+                    for (int d = 0; d < 3; d++) {
+                        const int col = R.cx + d - 1;
+                        if (col >= 0 && col < g.ncx) {
+                            const int so = col * ncy + R.rlo, sa = so & ~3;
+                            sm.oshift[d] = so - sa;
+                            bulk_g2s(&sm.foff[d][0], fstart + sa, 4u * kRecOffRun, &sm.bar);
+                            bulk_g2s(&sm.woff[d][0], wstart + sa, 4u * kRecOffRun, &sm.bar);
+                        }
                     }
+                }
+                if (lists) {
+                    bulk_g2s(sm.list, gblock, (uint32_t)(SH::list * kRecT * 2), &sm.bar);
+                    bulk_g2s(sm.cnt, S.gcnt + t0, (uint32_t)kRecT, &sm.bar);
                 }
             }
         }
@@ -400,18 +453,22 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
         const int mode = sm.win.mode;
         const int i = cur + tid;
         const bool active = i < we;
-        // the corrector's old state, fetched while the window is staged
+        const int col_i = i - t0;  // the target's column of the chunk's lists
+        // the corrector's old state and binning position, fetched while the
+        // window is staged
         double2 ro_r = make_double2(0., 0.);
-        float2 ro_v = make_float2(0.f, 0.f);
+        float2 ro_v = make_float2(0.f, 0.f), lb = make_float2(0.f, 0.f);
         float ro_s = 0.f;
         if (MODE == MODE_CORRECT && active) {
             ro_r = O.r[i];
             ro_v = O.v[i];
             ro_s = O.rho[i];
+            lb = S.lbin[i];
         }
         Acc4 acc = {0.f, 0.f, 0.f, 0.f};
         float Ia = 0.f;
         int cxa = cx, cy = 0;
+        bool global = mode != kRecStaged;
         const unsigned amask = __ballot_sync(0xffffffffu, active);  // the warp's targets
         if (mode == kRecStaged) {
             const bool ok = mbar_wait(&sm.bar, parity);
@@ -433,54 +490,75 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 cy = (int)rowa;
                 const float2 va = make_float2(av.x, av.y);
                 const float sa = av.z, Pa = av.w, Ra2 = K.two_rho0 + sa;
-                const float ybot = ya - K.reach, ytop = ya + K.reach;
-                uint16_t *const lst = sm.list + tid;
-                uint16_t *const wend = lst + SH::list * kRecT;
-                uint16_t *w = lst;
-                const int q = cy - rlo;
-                const int qlo = cy >= 1 ? q - 1 : q, qhi = cy + 1 < ncy ? q + 2 : q + 1;
+                uint16_t *const lst = sm.list + col_i;
+                if (!build) {
+                    // the stored list (built after the last binning)
+                    const int c = (int)sm.cnt[col_i];
+                    if (c == 255) global = true;
+                    else rec_eval(sm, lst, c, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K, acc);
+                } else {
+                    // phase 1 at radius Kb (2h + 2 sigma), the list stored
+                    // segment by segment as it is summed
+                    const float ybot = ya - Kb.reach, ytop = ya + Kb.reach;
+                    uint16_t *const wend = lst + SH::list * kRecT;
+                    uint16_t *w = lst;
+                    uint16_t *const gl = gblock + col_i;
+                    int gpos = 0;
+                    bool over = false;
+                    const int q = cy - rlo;
+                    const int qlo = cy >= 1 ? q - 1 : q, qhi = cy + 1 < ncy ? q + 2 : q + 1;
 #pragma unroll
-                for (int d = 0; d < 3; d++) {
-                    const int col = cx + d - 1;
-                    if (col < 0 || col >= g.ncx) continue;
-                    const float xd = xa + (float)(1 - d) * khf;  // the target's x in column d's frame
-                    const int osh = sm.oshift[d];
-                    if (walls) {  // walls of the three rows (few; scanned whole)
-                        const int s = sm.base[2 * d] + sm.woff[d][qlo + osh];
-                        const int e = sm.base[2 * d] + sm.woff[d][qhi + osh];
-                        // the list is summed and emptied, by the whole warp
-                        // together, when some lane's list might overflow
-                        if (__any_sync(amask, wend - w < (e - s) * kRecT)) {
-                            rec_eval(sm, lst, (int)((w - lst) / kRecT), xa, yca, rowa, va, sa, Pa,
-                                     Ia, Ra2, khf, K, acc);
+                    for (int d = 0; d < 3; d++) {
+                        const int col = cx + d - 1;
+                        if (col < 0 || col >= g.ncx) continue;
+                        const float xd = xa + (float)(1 - d) * khf;  // the target's x in column d's frame
+                        const int osh = sm.oshift[d];
+                        if (walls) {  // walls of the three rows (few; scanned whole)
+                            const int s0 = sm.base[2 * d] + sm.woff[d][qlo + osh];
+                            const int e = sm.base[2 * d] + sm.woff[d][qhi + osh];
+                            // the list is summed and emptied, by the whole warp
+                            // together, when some lane's list might overflow
+                            if (__any_sync(amask, wend - w < (e - s0) * kRecT)) {
+                                const int cnt = (int)((w - lst) / kRecT);
+                                rec_store(gl, lst, cnt, SH::list, gpos, over);
+                                rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K,
+                                         acc);
+                                w = lst;
+                            }
+                            for (int j = s0; j < e; j++) {
+                                const float2 l = sm.t[j];
+                                const float dx = xd - l.x, dy = ya - l.y;
+                                *w = (uint16_t)(((uint32_t)j << 2) | (uint32_t)d);
+                                w += fmaf(dx, dx, dy * dy) <= Kb.four_h2 ? kRecT : 0;
+                            }
+                        }
+                        // the column's y-window [ybot, ytop] of the fluid rows
+                        const int bf = sm.base[2 * d + 1];
+                        const int re = bf + sm.foff[d][qhi + osh];
+                        const int lo = rec_bound<false>(sm.t, bf + sm.foff[d][qlo + osh], re, ybot);
+                        const int e = rec_bound<true>(sm.t, lo, re, ytop);
+                        if (__any_sync(amask, wend - w < (e - lo) * kRecT)) {
+                            const int cnt = (int)((w - lst) / kRecT);
+                            rec_store(gl, lst, cnt, SH::list, gpos, over);
+                            rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K, acc);
                             w = lst;
                         }
-                        for (int j = s; j < e; j++) {
-                            const float2 l = sm.t[j];
-                            const float dx = xd - l.x, dy = ya - l.y;
-                            *w = (uint16_t)(((uint32_t)j << 2) | (uint32_t)d);
-                            w += fmaf(dx, dx, dy * dy) <= K.four_h2 ? kRecT : 0;
-                        }
+                        if (d == 1) w = rec_scan<true>(sm.t, lo, e, xd, ya, Kb.four_h2, 1u, w);
+                        else w = rec_scan<false>(sm.t, lo, e, xd, ya, Kb.four_h2, (uint32_t)d, w);
                     }
-                    // the column's y-window [ybot, ytop] of the fluid rows
-                    const int bf = sm.base[2 * d + 1];
-                    const int re = bf + sm.foff[d][qhi + osh];
-                    const int lo = rec_bound<false>(sm.t, bf + sm.foff[d][qlo + osh], re, ybot);
-                    const int e = rec_bound<true>(sm.t, lo, re, ytop);
-                    if (__any_sync(amask, wend - w < (e - lo) * kRecT)) {
-                        rec_eval(sm, lst, (int)((w - lst) / kRecT), xa, yca, rowa, va, sa, Pa, Ia,
-                                 Ra2, khf, K, acc);
-                        w = lst;
-                    }
-                    if (d == 1) w = rec_scan<true>(sm.t, lo, e, xd, ya, K.four_h2, 1u, w);
-                    else w = rec_scan<false>(sm.t, lo, e, xd, ya, K.four_h2, (uint32_t)d, w);
+                    const int cnt = (int)((w - lst) / kRecT);
+                    rec_store(gl, lst, cnt, SH::list, gpos, over);
+                    rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K, acc);
+                    S.gcnt[t0 + col_i] = over ? (uint8_t)255 : (uint8_t)gpos;
                 }
-                rec_eval(sm, lst, (int)((w - lst) / kRecT), xa, yca, rowa, va, sa, Pa, Ia, Ra2,
-                         khf, K, acc);
             }
-        } else if (active) {
-            // neighbour block too large for shared memory (or a chunk with more
-            // windows than the table holds): every target from global memory
+        } else if (active && build) {
+            S.gcnt[t0 + col_i] = (uint8_t)255;  // no list: this window takes the global path
+        }
+        if (active && global) {
+            // neighbour block too large for shared memory, a chunk with more
+            // windows than the table holds, or a list that did not fit: every
+            // in-support neighbour from global memory
             const uint32_t ki = __ldg(F.key + i);
             cxa = (int)(ki / (uint32_t)ncy);
             cy = (int)ki - cxa * ncy;
@@ -489,6 +567,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
             const float sa = __ldg(F.rho + i);
             Ia = rcp_approx(P.rho0 + sa);
             const float pa = STORED_P ? __ldg(F.p + i) : eos(sa, P);
+            acc = Acc4{0.f, 0.f, 0.f, 0.f};
             target_global<STORED_P>(F, fstart, wstart, Wl, g, P, K, i, cxa, cy, la, va, sa, pa * Ia,
                                     Ia, K.two_rho0 + sa, acc);
         }
@@ -514,21 +593,61 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 reinterpret_cast<float2 *>(out.v)[i] = nv;
                 reinterpret_cast<float *>(out.rho)[i] = s_new;
                 uint32_t nk;
+                bool resort = false;
                 if (out_of_domain_bits(rn, out.boxb)) {
                     nk = (uint32_t)g.ncells;
                     atomicOr(health, kHealthRemoved);
+                    resort = true;
                 } else {
                     int ncx_, ncy_;
                     nk = cell_key(g, rn, (uint32_t)(cxa * ncy + cy), &ncx_, &ncy_);
-                    if (nk == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
+                    if (nk == (uint32_t)g.ncells) {
+                        atomicOr(health, kHealthEscaped);
+                        resort = true;
+                    }
                 }
                 if (!(nv.x == nv.x) || !(nv.y == nv.y) || !(s_new == s_new))
                     atomicOr(health, kHealthNan);
                 out.key[i] = nk;
                 out.slot[i] = atomicAdd(out.counts + nk, 1u);
+                // the new position relative to the kept cell, and whether the
+                // cells must be rebuilt before the next pass
+                const float2 ln = make_float2((float)(rn.x - __ldg(g.ax.org + cxa)),
+                                              (float)(rn.y - __ldg(g.ay.org + cy)));
+                S.bloc[i] = ln;
+                const float ex = ln.x - lb.x, ey = ln.y - lb.y;
+                if (resort || !(fmaf(ex, ex, ey * ey) <= S.sig2)) {
+                    *S.need_sort = 1u;
+                    if (S.use_cond) {
+                        cudaGraphSetConditional(S.cond_sort, 1u);
+                        cudaGraphSetConditional(S.cond_copy, 0u);
+                    }
+                }
             }
         }
     }
+}
+
+// the corrector's output, in the kept order (no re-binning this step): new
+// r, v, rho and cell-relative positions into the current state; the
+// histogram slots the corrector counted are cleared
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+k_copy_kept(FluidState<T> D, const double2 *__restrict__ br, const typename V2<T>::t *__restrict__ bv,
+            const T *__restrict__ brho, const float2 *__restrict__ bloc,
+            const uint32_t *__restrict__ bkey, uint32_t *__restrict__ counts,
+            const uint32_t *__restrict__ fstart, int ncells, const uint32_t *__restrict__ skip,
+            uint32_t *__restrict__ runs) {
+    pdl_enter();
+    if (__ldg(skip) != 0u) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0 && runs) atomicAdd(runs, 1u);
+    if (i >= n_live(fstart, ncells)) return;
+    D.r[i] = br[i];
+    D.v[i] = bv[i];
+    D.rho[i] = brho[i];
+    D.loc[i] = bloc[i];
+    counts[bkey[i]] = 0u;
 }
 
 }  // namespace tsph

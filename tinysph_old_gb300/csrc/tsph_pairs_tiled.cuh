@@ -81,13 +81,17 @@ __device__ __forceinline__ float sqrt_approx(float x) {
     return r;
 }
 
-// Ra2 = 2 rho0 + (rho_a - rho0), so rho_a + rho_b = Ra2 + sb
+// Ra2 = 2 rho0 + (rho_a - rho0), so rho_a + rho_b = Ra2 + sb.  With CLAMP the
+// kernel factor (1 - q/2) is clamped at 0, so a pair beyond 2h adds exactly
+// zero to every sum (lists that hold neighbours up to a larger radius).
+template <bool CLAMP = false>
 __device__ __forceinline__ void pair_terms(float dx, float dy, float dvx, float dvy, float sa,
                                            float Pa, float Ia, float Ra2, float sb, float Pb,
                                            float Ib, const TileConst &K, Acc4 &acc) {
     const float dy2 = dy * dy;
     const float r2 = fmaf(dx, dx, dy2);
-    const float w1 = fmaf(sqrt_approx(r2), K.neg_half_inv_h, 1.f);
+    float w1 = fmaf(sqrt_approx(r2), K.neg_half_inv_h, 1.f);
+    if (CLAMP) w1 = fmaxf(w1, 0.f);
     const float w3 = w1 * w1 * w1;
     const float drdv = fmaf(dx, dvx, dy * dvy);
     const float inv_den = rcp_approx(r2 + K.eps_h2);
@@ -598,14 +602,15 @@ static __global__ void __launch_bounds__(kBlock)
 k_mdbc_f32_predict(WallState<float> Wl, int nw, int nbm, const uint32_t *__restrict__ fstart,
                 FluidState<float> F, Grid g, Phys<float> P, float dt, FluidState<float> D,
                 OldState<float> O, float skin, uint32_t *__restrict__ rebuild,
-                uint32_t *__restrict__ health, cudaGraphConditionalHandle cond, int use_cond) {
+                uint32_t *__restrict__ health, cudaGraphConditionalHandle cond, int use_cond,
+                KeepCells kc) {
     pdl_enter();
     if ((int)blockIdx.x < nbm) {
         mdbc_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, true, dt);
         return;
     }
     predict_keep_fluid<float>(((int)blockIdx.x - nbm) * blockDim.x + threadIdx.x, F, fstart, g, dt,
-                              D, O, skin, rebuild, health, cond, use_cond);
+                              D, O, skin, rebuild, health, cond, use_cond, kc);
 }
 
 }  // namespace tsph
