@@ -394,7 +394,9 @@ int tsph_write_vtk(tsph_system *s, const char *path);
  * buffer zones and their capacities, constants, domain, precision, tile
  * shape; no counterpart in the reference)
  * and a new system restarted from it: stepping it continues the saved run
- * bit for bit. */
+ * bit for bit.  Saving re-bins a system that steps with kept neighbour lists
+ * (tile shape 2), so the saved run and the restarted one go on from the same
+ * binning. */
 int tsph_save_checkpoint(tsph_system *s, const char *path);
 int tsph_load_checkpoint(const char *path, void *stream, tsph_system **out);
 int tsph_get_profile(tsph_system *s, tsph_profile_t *out, int reset);

@@ -286,6 +286,10 @@ template <typename T> class Engine final : public EngineBase {
     uint32_t *need_sort_ = nullptr;
     float sig2_ = 0.f;
     bool cells_kept_ = false;     // F_ moved since its binning (within sigma)
+    long long rec_passes_ = 0;    // kept-list pair passes run (host count)
+    long long rec_passes_sv_ = -1;
+    float2 *lbin_sv_ = nullptr;   // binning positions and list counters at state_save
+    uint32_t *gen_sv_ = nullptr;
 
   public:
     // time every pair-kernel variant on the current particles (forces pass,
@@ -293,7 +297,9 @@ template <typename T> class Engine final : public EngineBase {
     // the median kept; the fastest wins.  FP32 build only.
     static constexpr int kShapes = 3;
     int autotune(int *choice, double *us, std::string &err) override {
-        if constexpr (!std::is_same<T, float>::value) {
+        // the FP64 build, boundary-integral walls and buffer zones use the
+        // per-particle pair kernel: nothing to choose
+        if (!std::is_same<T, float>::value || wall_model_ == 2 || zones_on_) {
             tile_shape_ = 0;
             if (choice) *choice = 0;
             if (us)
@@ -537,9 +543,16 @@ template <typename T> class Engine final : public EngineBase {
                 (rc = alloc(&Fsv_.id, n, err)) || (rc = alloc(&Fsv_.key, n, err)) ||
                 (rc = alloc(&Fsv_.loc, n, err)) || (rc = alloc(&wsv_, 4 * nw, err)) ||
                 (F_.type && (rc = alloc(&Fsv_.type, n, err))) ||
-                (rc = alloc(&fstart_sv_, (size_t)ncells_ + 1, err)))
+                (rc = alloc(&fstart_sv_, (size_t)ncells_ + 1, err)) ||
+                (rc = alloc(&lbin_sv_, n, err)) || (rc = alloc(&gen_sv_, 4, err)))
                 return rc;
         }
+        // the kept-list state goes with it (restored when no kept-list pass
+        // ran in between, so stepping on from the restored state is the same
+        // as stepping on from the saved one)
+        TSPH_CK(cudaMemcpyAsync(lbin_sv_, lbin_, sizeof(float2) * n, cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(gen_sv_, gen_, 16, cudaMemcpyDeviceToDevice, st_));
+        rec_passes_sv_ = rec_passes_;
         copy_state(Fsv_, F_, wsv_, false);
         TSPH_CK(cudaMemcpyAsync(fstart_sv_, fstart_, 4 * ((size_t)ncells_ + 1),
                                 cudaMemcpyDeviceToDevice, st_));
@@ -563,7 +576,11 @@ template <typename T> class Engine final : public EngineBase {
         cells_kept_ = saved_kept_;
         exported_ = false;
         kicked_ = false;
-        return mark_stale(err);
+        if (rec_passes_ != rec_passes_sv_) return mark_stale(err);
+        TSPH_CK(cudaMemcpyAsync(lbin_, lbin_sv_, sizeof(float2) * (size_t)nf_,
+                                cudaMemcpyDeviceToDevice, st_));
+        TSPH_CK(cudaMemcpyAsync(gen_, gen_sv_, 16, cudaMemcpyDeviceToDevice, st_));
+        return 0;
     }
 
     int set_tile_shape(int shape, std::string &err) override {
@@ -664,6 +681,7 @@ template <typename T> class Engine final : public EngineBase {
                                                  (int)cudaSharedmemCarveoutMaxShared));
                 rec_setup_ = true;
             }
+            rec_passes_++;
             const uint32_t *fs = fstart_, *ws = wstart_;
             const PairRec RX = X.r == Fs_.r ? rec_s_ : rec_f_;
             const int nchunks = blocks_for(nf_, kRecT);
@@ -697,6 +715,10 @@ template <typename T> class Engine final : public EngineBase {
         return particle_to_cell(err);
     }
 
+  public:
+    int settle_cells(std::string &err) override { return ensure_exact_cells(err); }
+
+  private:
     // the state changed outside the fused step: neighbour lists and binning
     // positions are stale (the next fused step re-bins first)
     int mark_stale(std::string &err) {
@@ -1373,6 +1395,7 @@ template <typename T> class Engine final : public EngineBase {
             exported_ = false;
             return 0;
         }
+        wall_model_ = model;
         if (tile_shape_ < 0 && (rc = autotune(nullptr, nullptr, err))) return rc;
         if (prof_) {
             for (int s = 0; s < nsteps; s++)
@@ -1424,7 +1447,10 @@ template <typename T> class Engine final : public EngineBase {
         // with kept lists the cells are those of the last binning, which may
         // be some steps old (every particle within sigma of where it was binned)
         if constexpr (std::is_same<T, float>::value)
-            if (skin_ > 0.f && tile_shape_ == 2 && model != 2) cells_kept_ = true;
+            if (skin_ > 0.f && tile_shape_ == 2 && model != 2 && !zones_on_) {
+                cells_kept_ = true;
+                rec_passes_ += nsteps;  // graph replays run kept-list passes too
+            }
         exported_ = false;
         return collect_profile(err);
     }

@@ -88,6 +88,9 @@ class EngineBase {
     virtual void set_profiling(bool on) = 0;
     virtual Profile profile(bool reset) = 0;
     virtual bool cells_valid() const = 0;
+    // cells kept over several steps (kept neighbour lists) re-binned at the
+    // current positions; nothing when they are the current positions' cells
+    virtual int settle_cells(std::string &err) = 0;
     virtual void invalidate_cells() = 0;
 };
 

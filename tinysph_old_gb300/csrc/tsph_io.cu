@@ -84,6 +84,13 @@ int tsph_write_vtk(tsph_system *s, const char *path) {
 
 int tsph_save_checkpoint(tsph_system *s, const char *path) {
     if (!s || !path) return io_fail(TSPH_ERR_ARG, "null argument");
+    // a system stepping with kept neighbour lists is re-binned first, so the
+    // run that goes on and a run restarted from the file continue from the
+    // same binning (and so bit for bit alike)
+    if (s->eng) {
+        std::string err;
+        if (s->eng->settle_cells(err)) return io_fail(TSPH_ERR_CUDA, err);
+    }
     Snapshot z;
     int rc = snapshot(s, z);
     if (rc) return rc;

@@ -26,10 +26,10 @@
 // y-sorted column (both ends by binary search on the coarse y), so every lane
 // of a warp runs about the same number of candidates, and keeps the
 // in-support neighbours in a per-thread list of (staged index, column)
-// entries; when a column might not fit in some lane's list, the whole warp
-// sums its lists (phase 2) and empties them first (a warp-uniform step, so
-// no lane waits on another's), and the pairs are still summed in candidate
-// order.  Phase 2 sums the WCSPH pair terms (pair_terms
+// entries; a segment is scanned in pieces of at most a list's capacity, and
+// when a piece might not fit in some lane's list the whole warp sums its lists
+// (phase 2) and empties them first (a warp-uniform step, so no lane waits on
+// another's): the pairs are still summed in candidate order.  Phase 2 sums the WCSPH pair terms (pair_terms
 // of k_pairs_tiled) over the list.
 //
 // With the cells of the last binning kept through the predictor the columns
@@ -286,11 +286,13 @@ __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
-// phase 1 over one column's fluid candidates [s, e) (the column's y-window):
-// entry = staged index << 2 | column
-template <bool EXCL>
+// phase 1 over candidates [s, e) of one segment: entry = staged index << 2 |
+// column for every candidate within the test radius (h2 = its square);
+// `excl` (the target's own column) also drops r = 0, the target itself
 __device__ __forceinline__ uint16_t *rec_scan(const float2 *__restrict__ t, int s, int e, float xa,
-                                              float ya, float h2, uint32_t col, uint16_t *w) {
+                                              float ya, float h2, bool excl, uint32_t col,
+                                              uint16_t *w) {
+    const float lo2 = excl ? 0.f : -1.f;  // kept when lo2 < r2 <= h2
     int j = s;
     uint32_t ent = ((uint32_t)s << 2) | col;
     for (; j + 1 < e; j += 2, ent += 8u) {
@@ -299,15 +301,16 @@ __device__ __forceinline__ uint16_t *rec_scan(const float2 *__restrict__ t, int 
         const float dx1 = xa - l1.x, dy1 = ya - l1.y;
         const float r0 = fmaf(dx0, dx0, dy0 * dy0), r1 = fmaf(dx1, dx1, dy1 * dy1);
         *w = (uint16_t)ent;
-        w += support_test<EXCL>(r0, h2) ? kRecT : 0;
+        w += (r0 <= h2 && r0 > lo2) ? kRecT : 0;
         *w = (uint16_t)(ent + 4u);
-        w += support_test<EXCL>(r1, h2) ? kRecT : 0;
+        w += (r1 <= h2 && r1 > lo2) ? kRecT : 0;
     }
     if (j < e) {
         const float2 l = t[j];
         const float dx = xa - l.x, dy = ya - l.y;
+        const float r = fmaf(dx, dx, dy * dy);
         *w = (uint16_t)ent;
-        w += support_test<EXCL>(fmaf(dx, dx, dy * dy), h2) ? kRecT : 0;
+        w += (r <= h2 && r > lo2) ? kRecT : 0;
     }
     return w;
 }
@@ -507,44 +510,43 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                     bool over = false;
                     const int q = cy - rlo;
                     const int qlo = cy >= 1 ? q - 1 : q, qhi = cy + 1 < ncy ? q + 2 : q + 1;
-#pragma unroll
-                    for (int d = 0; d < 3; d++) {
+                    // the six segments in staged order: walls (scanned whole)
+                    // and fluid (over its y-window) of the three columns
+#pragma unroll 1
+                    for (int sgi = walls ? 0 : 1; sgi < 6; sgi += walls ? 1 : 2) {
+                        const int d = sgi >> 1;
                         const int col = cx + d - 1;
                         if (col < 0 || col >= g.ncx) continue;
                         const float xd = xa + (float)(1 - d) * khf;  // the target's x in column d's frame
                         const int osh = sm.oshift[d];
-                        if (walls) {  // walls of the three rows (few; scanned whole)
-                            const int s0 = sm.base[2 * d] + sm.woff[d][qlo + osh];
-                            const int e = sm.base[2 * d] + sm.woff[d][qhi + osh];
-                            // the list is summed and emptied, by the whole warp
-                            // together, when some lane's list might overflow
-                            if (__any_sync(amask, wend - w < (e - s0) * kRecT)) {
+                        const int bs = sm.base[sgi];
+                        int lo, e;
+                        if (sgi & 1) {
+                            const int re = bs + sm.foff[d][qhi + osh];
+                            lo = rec_bound<false>(sm.t, bs + sm.foff[d][qlo + osh], re, ybot);
+                            e = rec_bound<true>(sm.t, lo, re, ytop);
+                        } else {
+                            lo = bs + sm.woff[d][qlo + osh];
+                            e = bs + sm.woff[d][qhi + osh];
+                        }
+                        // pieces of at most a list's capacity; before a piece
+                        // that might not fit in some lane's list, the whole warp
+                        // sums and empties its lists (the warp runs as many
+                        // pieces as its longest segment needs)
+                        const int np =
+                            (int)__reduce_max_sync(amask, (unsigned)((e - lo + SH::list - 1) / SH::list));
+                        for (int pc = 0; pc < np; pc++) {
+                            const int pl = min(e, lo + pc * SH::list);
+                            const int pe = min(e, pl + SH::list);
+                            if (__any_sync(amask, wend - w < (pe - pl) * kRecT)) {
                                 const int cnt = (int)((w - lst) / kRecT);
                                 rec_store(gl, lst, cnt, SH::list, gpos, over);
                                 rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K,
                                          acc);
                                 w = lst;
                             }
-                            for (int j = s0; j < e; j++) {
-                                const float2 l = sm.t[j];
-                                const float dx = xd - l.x, dy = ya - l.y;
-                                *w = (uint16_t)(((uint32_t)j << 2) | (uint32_t)d);
-                                w += fmaf(dx, dx, dy * dy) <= Kb.four_h2 ? kRecT : 0;
-                            }
+                            w = rec_scan(sm.t, pl, pe, xd, ya, Kb.four_h2, sgi == 3, (uint32_t)d, w);
                         }
-                        // the column's y-window [ybot, ytop] of the fluid rows
-                        const int bf = sm.base[2 * d + 1];
-                        const int re = bf + sm.foff[d][qhi + osh];
-                        const int lo = rec_bound<false>(sm.t, bf + sm.foff[d][qlo + osh], re, ybot);
-                        const int e = rec_bound<true>(sm.t, lo, re, ytop);
-                        if (__any_sync(amask, wend - w < (e - lo) * kRecT)) {
-                            const int cnt = (int)((w - lst) / kRecT);
-                            rec_store(gl, lst, cnt, SH::list, gpos, over);
-                            rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K, acc);
-                            w = lst;
-                        }
-                        if (d == 1) w = rec_scan<true>(sm.t, lo, e, xd, ya, Kb.four_h2, 1u, w);
-                        else w = rec_scan<false>(sm.t, lo, e, xd, ya, Kb.four_h2, (uint32_t)d, w);
                     }
                     const int cnt = (int)((w - lst) / kRecT);
                     rec_store(gl, lst, cnt, SH::list, gpos, over);
