@@ -282,7 +282,7 @@ template <typename T> class Engine final : public EngineBase {
     float2 *bloc_ = nullptr;      // the corrector's new cell-relative positions
     uint16_t *rec_list_ = nullptr;
     uint8_t *rec_cnt_ = nullptr;
-    uint32_t *gen_ = nullptr;     // {sorts, sort the lists were built after, pass builds}
+    uint32_t *gen_ = nullptr;     // {sorts, sort the lists were built after, -, CTAs done}
     uint32_t *need_sort_ = nullptr;
     float sig2_ = 0.f;
     bool cells_kept_ = false;     // F_ moved since its binning (within sigma)

@@ -77,10 +77,13 @@ struct PairRec {  // one set of pair records (fluid rows or walls)
 // neighbours within 2h + 2 sigma and stores it; later passes, while every
 // particle stays within sigma of where it was binned, sum the stored lists
 // (the kernel factor clamped at zero beyond 2h) with no candidate search.
+// A pass builds when the count of sorts (gen[0], bumped by every sort)
+// differs from the sort the lists were built after (gen[1], set by the last
+// CTA of every pass).
 struct RecStep {
     uint16_t *glist;            // [chunk][list][128]: entries (staged index << 2 | column)
     uint8_t *gcnt;              // [chunk][128]: entries, or 255 (did not fit: global path)
-    uint32_t *gen;              // {sorts, sort the lists were built after, this pass builds}
+    uint32_t *gen;              // {sorts, sort the lists were built after, -, CTAs done}
     const float2 *lbin;         // cell-relative positions at the binning
     float sig2;                 // squared displacement allowed since the binning
     float2 *bloc;               // MODE_CORRECT: new cell-relative position (kept cell)
@@ -190,7 +193,8 @@ __device__ __forceinline__ void rec_window_table(int c, int cap, const FluidStat
 
 // pair records of the fluid rows [0, n_live) and the walls [0, nw) of a state
 // (p from the EOS of rho, or the stored p); the blocks from `rec_blocks` on
-// build the window table, one thread per chunk of 128 targets
+// build the window table, one thread per chunk of 128 targets, when the
+// coming pass builds the lists
 template <bool STORED_P>
 __global__ void __launch_bounds__(kBlock)
 k_pair_records(FluidState<float> F, const uint32_t *__restrict__ fstart, WallState<float> Wl,
@@ -198,16 +202,12 @@ k_pair_records(FluidState<float> F, const uint32_t *__restrict__ fstart, WallSta
                const uint32_t *__restrict__ wstart, int nchunks, int cap,
                WinRec *__restrict__ table, int *__restrict__ nwin, uint32_t *__restrict__ gen) {
     pdl_enter();
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        // the coming pair pass builds the lists when a sort happened since
-        // they were built
-        const uint32_t now = gen[0];
-        gen[2] = now != gen[1] ? 1u : 0u;
-        gen[1] = now;
-    }
     if ((int)blockIdx.x >= rec_blocks) {
+        // the table is rebuilt only for a pass that builds the lists (a sort
+        // happened since they were built); otherwise it still holds
         const int c = ((int)blockIdx.x - rec_blocks) * blockDim.x + threadIdx.x;
-        if (c < nchunks) rec_window_table(c, cap, F, fstart, wstart, g, table, nwin);
+        if (c < nchunks && __ldg(gen) != __ldg(gen + 1))
+            rec_window_table(c, cap, F, fstart, wstart, g, table, nwin);
         return;
     }
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -384,8 +384,19 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
     const int ncy = g.ncy;
     const float khf = g.khf;
     const int nw = __ldg(nwin + blockIdx.x);
-    if (nw == 0) return;
-    const bool build = __ldg(S.gen + 2) != 0u;  // this pass builds and stores the lists
+    // this pass builds and stores the lists when a sort happened since they
+    // were built (the last CTA to finish records the sort they are built after)
+    const bool build = __ldg(S.gen) != __ldg(S.gen + 1);
+    auto finish = [&]() {
+        if (tid == 0) {
+            __threadfence();
+            if (atomicAdd(S.gen + 3, 1u) == gridDim.x - 1) {
+                S.gen[1] = S.gen[0];
+                S.gen[3] = 0u;
+                __threadfence();
+            }
+        }
+    };
     const int t0 = blockIdx.x * kRecT;
     // the chunk's stored lists: column (i - t0) of a [list][128] block
     uint16_t *const gblock = S.glist + (size_t)blockIdx.x * SH::list * kRecT;
@@ -481,6 +492,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 // more bounded wait, and leave without touching the window
                 if (tid == 0) atomicOr(health, kHealthStall);
                 mbar_wait(&sm.bar, parity ^ 1u);
+                finish();
                 return;
             }
             const bool walls = (sm.win.n[0] | sm.win.n[2] | sm.win.n[4]) != 0;
@@ -628,6 +640,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
             }
         }
     }
+    finish();
 }
 
 // the corrector's output, in the kept order (no re-binning this step): new
