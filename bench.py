@@ -83,18 +83,65 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
-def profile_traffic():
-    """dram bytes per launch of the pair kernel from the committed ncu summary."""
-    p = os.path.join(ROOT, "profiles", "k_pairs_tiled_dam_break_720k.md")
+SM_COUNT = 152
+# the pair kernel of each variant (tsph_set_tile_shape) and its ncu summary
+PAIR_KERNELS = {0: "k_pairs_tiled (wide: 608 staged, 36 list entries)",
+                1: "k_pairs_tiled (deep: 512 staged, 44 list entries)",
+                2: "k_pairs_rec (pair records, window staging by cp.async.bulk)"}
+PAIR_PROFILES = {"k_pairs_tiled": "k_pairs_tiled_dam_break_720k.md",
+                 "k_pairs_rec": "k_pairs_rec_dam_break_720k.md"}
+
+
+def profile_figures(kernel):
+    """Figures of the kernel's committed ncu summary (lines "key: value"):
+    dram_bytes_per_launch_fullsize, warp_inst_per_particle, smem_frac."""
+    name = kernel.split()[0]
+    p = os.path.join(ROOT, "profiles", PAIR_PROFILES.get(name, name + ".md"))
+    out = {}
     if not os.path.exists(p):
-        return None
+        return out
+    out["file"] = os.path.relpath(p, ROOT)
+    keys = {"dram_bytes_per_launch_fullsize": "dram_bytes_per_launch",
+            "warp_inst_per_particle": "warp_inst_per_particle", "smem_frac": "smem_frac"}
     for line in open(p):
-        if line.startswith("dram_bytes_per_launch_fullsize:"):
+        k = line.split(":", 1)[0].strip()
+        if k in keys:
             try:
-                return float(line.split(":", 1)[1].split()[0])
-            except ValueError:
-                return None
-    return None
+                out[keys[k]] = float(line.split(":", 1)[1].split()[0])
+            except (ValueError, IndexError):
+                pass
+    return out
+
+
+def graph_kernel_split(s, model, dt, flush, stream, steps=20):
+    """Per-kernel time of `steps` replayed graph steps from CUPTI kernel
+    records (tinysph_old_gb300.timeline), or None without CUPTI."""
+    import torch
+
+    from tinysph_old_gb300 import timeline
+
+    try:
+        tl = timeline.Timeline()
+    except (FileNotFoundError, OSError):
+        return None
+    torch.cuda.synchronize()
+    try:
+        tl.start()
+    except RuntimeError:  # CUPTI taken (e.g. under a profiler)
+        return None
+    with torch.cuda.stream(stream):
+        for _ in range(steps):
+            flush.zero_()
+            s.step(model, dt, 1)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    tl.stop()
+    out = timeline.split(tl.records(), steps)
+    if not out["by_kernel"]:
+        return None
+    out["source"] = (f"CUPTI kernel records of {steps} graph steps (L2 flushed between "
+                     "steps); exclusive_us partitions the busy time of a step")
+    return out
 
 
 class ClockSampler:
@@ -735,8 +782,16 @@ def main():
     s.add_particles(a["type"], a["r"], a["v"], a["rho"], a["p"], gnr)
     s.divide_to_cells()
     s.particle_to_cell()
+    tune = None
     if args.tile_shape != "auto":
         s.set_tile_shape(sph.TILE_SHAPES[args.tile_shape])
+        shape = sph.TILE_SHAPES[args.tile_shape]
+    else:
+        # the autotuner's choice (median of 10 forces passes per variant)
+        shape, tune_us = s.autotune()
+        names = {v: k for k, v in sph.TILE_SHAPES.items()}
+        tune = {"chosen": names.get(shape, str(shape)),
+                "median_us": {names.get(k, str(k)): float(u) for k, u in enumerate(tune_us)}}
     n = s.np
     model = case.wall_model
     dt = case.dt
@@ -775,7 +830,12 @@ def main():
     value = whole_job_rate(world, n, args.steps, ms)
     health = s.health()
 
-    # ---- per-kernel timing for the roofline (eager launches with events)
+    # ---- the graph step split by kernel (CUPTI kernel records of replayed
+    # graph steps, L2 flushed in between as in the timed loop)
+    graph_split = graph_kernel_split(s, model, dt, flush, stream, steps=20)
+
+    # ---- per-kernel timing for the roofline: eager launches of the same
+    # kernels, each bracketed by CUDA events on the system's stream
     s.set_profiling(True)
     s.profile(reset=True)
     prof_steps = 5
@@ -786,29 +846,54 @@ def main():
     nfluid = int(np.sum(a["type"] == 0))
     peak, peak_kind = measured_peaks()
     achieved = PAIR_BYTES_PER_PARTICLE * nfluid / (pair_avg_us * 1e-6) / 1e9
-    traffic = profile_traffic()
+    pair_kernel = PAIR_KERNELS.get(shape, "k_pairs_tiled")
+    pk = profile_figures(pair_kernel)
+    sm_mhz = (clocks.summary() or {}).get("sm_mhz") or 2070.0
+    graph_pair_us = None
+    if graph_split and pair_kernel.split()[0] in graph_split["by_kernel"]:
+        graph_pair_us = graph_split["by_kernel"][pair_kernel.split()[0]]["us"] / max(
+            graph_split["by_kernel"][pair_kernel.split()[0]]["launches"], 1e-9)
+    issue = None
+    if pk.get("warp_inst_per_particle"):
+        # issue rate against the SMs' peak: 4 schedulers per SM, one warp
+        # instruction per scheduler per clock
+        inst = pk["warp_inst_per_particle"] * nfluid
+        issue = inst / (pair_avg_us * 1e-6) / (SM_COUNT * 4 * sm_mhz * 1e6)
 
-    # ---- e2e through the C ABI with pinned host buffers
+    # ---- e2e through the C ABI with pinned host buffers: each step uploads
+    # its input state (r, v, rho) from pinned host memory, re-bins, steps and
+    # reads its result back into pinned host memory; the result's copy runs
+    # on a copy stream beside the next step's upload and kernels
+    # (tsph_download_async / tsph_download_wait)
     hr = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
     hv = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
     hrho = torch.empty((n,), dtype=torch.float64, pin_memory=True)
+    outs = [tuple(torch.empty_like(t, pin_memory=True) for t in (hr, hv, hrho))
+            for _ in range(2)]
     mask = sph.F_R | sph.F_V | sph.F_RHO
     s.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
-    for _ in range(2):  # warm
+
+    def e2e_step(k):
+        o = outs[k % 2]
         s.upload_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
         s.particle_to_cell()
         s.step(model, dt, 1)
-        s.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+        s.download_async(mask, r=o[0].data_ptr(), v=o[1].data_ptr(), rho=o[2].data_ptr())
+
+    for k in range(2):  # warm
+        e2e_step(k)
+    s.download_wait()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    for _ in range(args.e2e_steps):
-        s.upload_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
-        s.particle_to_cell()
-        s.step(model, dt, 1)
-        s.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+    for k in range(args.e2e_steps):
+        e2e_step(k)
+    s.download_wait()
     e2e_s = time.perf_counter() - t0
     e2e_value = world * n * args.e2e_steps / e2e_s
     xfer = n * (16 + 16 + 8)
+    # the result read back equals the state the step leaves on the device
+    ref_after = s.download()
+    e2e_ok = bool(np.array_equal(outs[(args.e2e_steps - 1) % 2][0].numpy(), ref_after["r"]))
 
     # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
@@ -840,17 +925,34 @@ def main():
             "e2e": {"value": e2e_value, "unit": "particle-steps/s",
                     "h2d_bytes_per_step": xfer, "d2h_bytes_per_step": xfer,
                     "path": "tsph_upload(r,v,rho) + tsph_particle_to_cell + tsph_step(1) + "
-                            "tsph_download(r,v,rho), pinned host buffers"},
+                            "tsph_download_async(r,v,rho) (waited one step later), pinned "
+                            "host buffers",
+                    "result_matches_device_state": e2e_ok},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_pairs_tiled (forces + corrector / forces)",
+                         "frac": achieved / peak, "traffic": pk.get("dram_bytes_per_launch"),
+                         "kernel": pair_kernel,
                          "bytes_per_unit": PAIR_BYTES_PER_PARTICLE, "unit_count": nfluid,
-                         "avg_launch_us": pair_avg_us, "peak_kind": peak_kind},
+                         "avg_launch_us": pair_avg_us,
+                         "avg_launch_source": "eager launches bracketed by CUDA events",
+                         "graph_avg_launch_us": graph_pair_us, "peak_kind": peak_kind,
+                         # the kernel is issue-bound, not HBM-bound: its issue rate
+                         # and shared-memory throughput against their peaks
+                         "issue_frac": issue,
+                         "warp_inst_per_particle": pk.get("warp_inst_per_particle"),
+                         "smem_frac": pk.get("smem_frac"),
+                         "profile": pk.get("file")},
             "step_roofline": {"bytes_per_particle_step": STEP_BYTES_PER_PARTICLE,
                               "achieved_gbs": STEP_BYTES_PER_PARTICLE * value / world / 1e9,
                               "frac": STEP_BYTES_PER_PARTICLE * value / world / 1e9 / peak},
-            "kernel_us_per_step": {k: prof[k] / prof_steps for k in
-                                   ("pair_us", "sort_us", "mdbc_us", "other_us")},
+            "kernel_us_per_step": graph_split or {
+                "source": "unavailable (no CUPTI): see eager_kernel_us_per_step"},
+            "eager_kernel_us_per_step": {
+                "source": "5 steps launched eagerly, every kernel bracketed by CUDA events "
+                          "(no graph, no programmatic dependent launch overlap): an upper "
+                          "bound per category, not the graph step's split",
+                **{k: prof[k] / prof_steps for k in ("pair_us", "sort_us", "mdbc_us",
+                                                     "other_us")}},
+            "autotune": tune,
             "gpu_launches": int(timed_launches),
             "clocks": clocks.summary(),
             "health": health,

@@ -238,6 +238,18 @@ int tsph_step(tsph_system *s, int wall_model, double dt, int nsteps);
 /* state transfer in the reference's order; `fields` is a TSPH_F_* mask */
 int tsph_download(tsph_system *s, int fields, const tsph_host_state *out);
 int tsph_upload(tsph_system *s, int fields, const tsph_host_state *in);
+/* Pipelined download (no counterpart in the reference, whose state lives in
+ * host memory): tsph_download_async exports r, v, a, rho, drho and p (other
+ * fields: TSPH_ERR_ARG) into a staging set of its own on the system's stream
+ * and starts the device-to-host copies on a copy stream, then returns; the
+ * copies run beside the calls that follow (the next upload and step).
+ * tsph_download_wait blocks until they are done.  Until then the host
+ * buffers (pinned memory for a true overlap) must stay valid and unread.  At
+ * most one download is in flight: a second tsph_download_async first waits
+ * for the one before.  A state with erased particles is downloaded
+ * synchronously (its rows are compacted on the host). */
+int tsph_download_async(tsph_system *s, int fields, const tsph_host_state *out);
+int tsph_download_wait(tsph_system *s);
 /* wait for the system's stream */
 int tsph_sync(tsph_system *s);
 /* device health word (TSPH_HEALTH_*), optionally cleared */
@@ -276,7 +288,8 @@ int tsph_water_front(tsph_system *s, double y_max, double *x_front);
  * around every launch on the system's stream; tsph_profile returns the sums
  * since the last reset.  Off by default (graph replay, no events). */
 typedef struct {
-    double pair_us;      /* pair-loop + fused integrator kernels          */
+    double pair_us;      /* pair-loop + fused integrator kernels (the pair
+                            records of variant 2 count as other)          */
     int pair_launches;
     double sort_us;      /* cell keys, scan, stable scatter                */
     int sort_launches;

@@ -326,14 +326,24 @@ def main_inflow_tank_bottom():
     out = {f"geom_{k}": g[k] for k in ("r", "v", "rho", "p", "type")}
     out["dt"] = np.float64(case.dt)
     out["snaps"] = np.array([500, 1000, 1500])
-    R = O.RefSystem.from_case(case)
+    # the reference's own spread (the jet meets the ledge and the tank: the
+    # last bits are amplified), as for cases/flowDrop_mDBC
+    runs = [O.RefSystem.from_case(case)]
+    runs += [O.RefSystem.from_case(_perturbed_walls(cases.inflow_tank_bottom_mdbc(dp=dp), u))
+             for u in (2.0 ** -53, 2.0 ** -24)]
     done = 0
     for n in out["snaps"]:
-        R.step_zones(case.dt, int(n) - done)
+        for R in runs:
+            R.step_zones(case.dt, int(n) - done)
         done = int(n)
-        st = R.state()
+        st = runs[0].state()
         for k in ("r", "v", "rho", "p", "type"):
             out[f"step{n}_{k}"] = st[k]
+        for R, tag in zip(runs[1:], ("spread64", "spread32")):
+            pt = R.state()
+            assert np.array_equal(pt["type"], st["type"]), (n, tag)
+            for k in ("r", "v", "rho", "p"):
+                out[f"step{n}_{k}_{tag}"] = np.float64(np.max(np.abs(pt[k] - st[k])))
     np.savez_compressed(os.path.join(HERE, "inflow_tank_bottom_mdbc_dp0.02.npz"), **out)
 
 

@@ -248,3 +248,36 @@ def test_ale_larger_case_vs_oracle(gpu_tsph, oracle_mod):
     P2.ale_step(case.dt, 0, 3)
     s2.step(case.dt, 0, 3)
     _check_state(s2.download(), P2.ale_state(), case.dt, 3, rates, case.cs, tag="dp0.004")
+
+
+@pytest.mark.gpu
+def test_ale_still_water_vs_reference_golden(gpu_tsph):
+    """cases/ALESPH_stillWater (boundary-integral tank, hydrostatic start,
+    h = 2 dp): gradients and fluxes at the golden input, then the fused step
+    against the reference's RUN loop snapshot by snapshot."""
+    g = np.load(os.path.join(GOLD, "still_water_ale_dp0.02.npz"))
+    case = cases.still_water_ale(dp=0.02)
+    s = _gpu(gpu_tsph, case, g)
+    st = s.download()
+    fl = st["type"] == 0
+    s.gradient()
+    s.forces(float(g["dt"]))
+    st = s.download()
+    e = _err(st["grad"][fl], g["forces_grad"][fl])
+    assert e <= _rate_tol(g["forces_grad"][fl]), e
+    for k in RATES:
+        e = _err(st[k][fl], g[f"forces_{k}"][fl])
+        assert e <= _rate_tol(g[f"forces_{k}"][fl]), (k, e)
+    s = _gpu(gpu_tsph, case, g)
+    every = int(g["snap_every"])
+    dt = float(g["dt"])
+    rates = {f: g[f"forces_{f}"] for f in RATES}
+    for k in range(every, int(g["nsteps"]) + 1, every):
+        s.step(dt, k - every, every)
+        st = s.download()
+        ref = {f: g[f"step{k}_{f}"] for f in ("r", "v", "rho", "p", "omega", "omegarho",
+                                              "omegav", "domega", "domegarho", "domegav",
+                                              "index")}
+        ref["type"] = g["init_type"]
+        _check_state(st, ref, dt, k, rates, case.cs, tag=f"step{k}")
+    assert s.health() & ~gpu_tsph.HEALTH_REMOVED == 0

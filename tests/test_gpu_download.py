@@ -1,0 +1,72 @@
+"""tsph_download_async / tsph_download_wait: a pipelined loop (upload a
+state, re-bin, step, start the result's download, wait for it one step
+later) leaves in the host buffers exactly what tsph_download returns, in
+both precisions; a state with erased particles falls back to the
+synchronous download; other fields are refused."""
+
+import numpy as np
+import pytest
+
+from tinysph_old_gb300 import cases
+
+
+def _buffers(n, torch):
+    return tuple(torch.empty(shape, dtype=torch.float64, pin_memory=True)
+                 for shape in ((n, 2), (n, 2), (n,)))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_pipelined_download_matches_the_synchronous_one(gpu_tsph, precision):
+    torch = pytest.importorskip("torch")
+    case = cases.dam_break_mdbc(dp=0.01)
+    s = gpu_tsph.ParticleSystem.from_case(case, precision)
+    n = s.np
+    mask = gpu_tsph.F_R | gpu_tsph.F_V | gpu_tsph.F_RHO
+    inp = _buffers(n, torch)
+    s.download_ptrs(mask, r=inp[0].data_ptr(), v=inp[1].data_ptr(), rho=inp[2].data_ptr())
+    outs = [_buffers(n, torch) for _ in range(2)]
+    expect = []
+    for k in range(4):
+        s.upload_ptrs(mask, r=inp[0].data_ptr(), v=inp[1].data_ptr(), rho=inp[2].data_ptr())
+        s.particle_to_cell()
+        s.step(case.wall_model, case.dt, 3 + k)  # a different result every call
+        o = outs[k % 2]
+        s.download_async(mask, r=o[0].data_ptr(), v=o[1].data_ptr(), rho=o[2].data_ptr())
+        if k > 0:
+            # the previous result, complete once the next download has started
+            prev = outs[(k - 1) % 2]
+            want = expect[-1]
+            assert np.array_equal(prev[0].numpy(), want["r"])
+            assert np.array_equal(prev[1].numpy(), want["v"])
+            assert np.array_equal(prev[2].numpy(), want["rho"])
+        s.download_wait()
+        expect.append(s.download())
+        # a second wait is a no-op
+        s.download_wait()
+    last = outs[3 % 2]
+    assert np.array_equal(last[0].numpy(), expect[-1]["r"])
+    assert np.array_equal(last[2].numpy(), expect[-1]["rho"])
+
+
+@pytest.mark.gpu
+def test_download_async_with_erased_particles_and_bad_fields(gpu_tsph):
+    case = cases.dam_break_mdbc(dp=0.02)
+    s = gpu_tsph.ParticleSystem.from_case(case, "fp32")
+    st = s.download()
+    r = st["r"].copy()
+    fl = np.flatnonzero(st["type"] == 0)
+    r[fl[5]] = (0.5, case.domain[3] + 0.5)  # leaves the domain
+    s.upload(r=r)
+    assert s.remove_out_of_domain() == 1
+    s.particle_to_cell()
+    n = s.np
+    assert n == case.np - 1
+    out_r = np.zeros((n, 2))
+    out_p = np.zeros(n)
+    s.download_async(gpu_tsph.F_R | gpu_tsph.F_P, r=out_r.ctypes.data, p=out_p.ctypes.data)
+    s.download_wait()
+    want = s.download()
+    assert np.array_equal(out_r, want["r"]) and np.array_equal(out_p, want["p"])
+    with pytest.raises(gpu_tsph.TsphError):
+        s.download_async(gpu_tsph.F_INDEX, index=np.zeros(n, dtype=np.int32).ctypes.data)

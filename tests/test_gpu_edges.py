@@ -132,6 +132,58 @@ def test_particle_thrown_out_inside_the_fused_step(gpu_tsph, oracle_mod, precisi
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("precision,variant", [("fp64", None), ("fp32", 0), ("fp32", 2)])
+def test_fused_step_erase_skips_the_particle_after_an_erased_one(gpu_tsph, oracle_mod, precision,
+                                                                 variant):
+    """Three particles of consecutive indices leave the domain in the same
+    fused step.  RemoveParticlesOutOfDomain erases inside a forward loop
+    (src/SPH_btdebug.h:14-29), so the first is erased, the second is not
+    examined in that step (it goes on, outside the domain, and is erased in
+    the next one) and the third is erased: the fused step keeps the oracle's
+    survivor set step by step."""
+    ps = _set()
+    geo.create_block_of_fluid(ps, 0.3, 0.3, 0.4, 0.4)
+    case = _case(ps, 0)
+    g = gpu_tsph.ParticleSystem.from_case(case, precision)
+    if variant is not None:
+        g.set_tile_shape(variant)
+    o = oracle_mod.PortSystem.from_case(case)
+    st = g.download()
+    v = st["v"].copy()
+    r = st["r"].copy()
+    n = len(r)
+    # The right edge is the one side where a point can lie outside the box
+    # (x > xm - 0.01) and still inside the cell grid, which reaches
+    # x0 - 0.273 h + ncx kh: there the skipped particle stays binned until the
+    # next step erases it.  All three reach that band in the first step.
+    xm, eps = case.domain[1], 0.01
+    kh, of = case.kap * case.h, 0.273 * case.h
+    ncx = int((xm - case.domain[0] + of) / kh) + 1
+    grid_right = case.domain[0] - of + ncx * kh
+    x_start, vx = xm - eps - 0.005, 20.0
+    x_next = x_start + vx * case.dt
+    assert xm - eps + 1e-3 < x_next < grid_right - 1e-3
+    for k, y in zip((n - 3, n - 2, n - 1), (0.40, 0.44, 0.48)):
+        assert st["type"][k] == 0
+        r[k] = (x_start, y)
+        v[k] = (vx, 0.0)
+    g.upload(r=r, v=v)
+    g.particle_to_cell()
+    o.set_state(r=r, v=v)
+    o.clear_cells()
+    o.particle_to_cell()
+    counts = []
+    for _ in range(4):
+        g.step(0, case.dt, 1)
+        o.step(0, case.dt, 1)
+        assert g.np == o.np()
+        counts.append(g.np)
+        _compare(g, o, precision)
+    # the erase with the skip: n -> n - 2 in one step, n - 3 in the next
+    assert counts[:2] == [n - 2, n - 3] and counts[-1] == n - 3
+
+
+@pytest.mark.gpu
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_remove_skips_the_particle_after_an_erased_one(gpu_tsph, oracle_mod, precision):
     """RemoveParticlesOutOfDomain erases inside a forward loop

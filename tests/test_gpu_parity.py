@@ -23,6 +23,7 @@ CASES = [
     ("dam_break_mdbc_dp0.02.npz", lambda: cases.dam_break_mdbc(dp=0.02), 0),
     ("still_water_dbc_dp0.02.npz", lambda: cases.still_water_dbc(dp=0.02), 1),
     ("dam_break_dbc_dp0.02.npz", lambda: cases.dam_break_dbc(dp=0.02), 1),
+    ("still_water_mdbc_dp0.02.npz", lambda: cases.still_water_mdbc(dp=0.02), 0),
 ]
 
 

@@ -3,16 +3,22 @@ runs (tests/golden/inflow_slab_mdbc_dp0.005.npz: cases/inflowSlab_mDBC, the
 inlet creating particles; outlet_channel_mdbc_dp0.005.npz: the outlet's
 retyping and its erasures, including the reference's skip of the particle
 after an erased one; flow_drop_mdbc_dp0.02.npz: cases/flowDrop_mDBC, a
-y-oriented inlet and two outlets facing +x and -x).  The jet's impact on
-the floor amplifies differences in the last bits (the reference itself,
-run with its walls moved by a few units of roundoff, departs from its own
-run by 5e-7 of the pressure scale after 1000 steps); for it the bar is at
-least ten times that spread, recorded in the fixture at each precision's
-roundoff.  Particle count, order and types exact; fields within
+y-oriented inlet and two outlets facing +x and -x; flow_drop_bt_dp0.02.npz:
+cases/flowDrop_BT, the same jet over one boundary-integral floor, up to the
+reference's first erasure; inflow_tank_bottom_mdbc_dp0.02.npz:
+cases/inflowTankBottom_mDBC, an inlet feeding a ledge above a tank).  A
+jet's impact on a floor amplifies differences in the last bits (the
+reference itself, run with its walls moved by a few units of roundoff,
+departs from its own run by 5e-7 of the pressure scale after 1000 steps of
+flowDrop_mDBC); for the two mDBC jets the bar is at least ten times that
+spread, recorded in the fixture at each precision's roundoff.  The BT jet's
+snapshots end before it reaches the floor (the reference's own run is
+undefined after its first erasure), so its bars are the plain ones.  Particle count, order and types exact; fields within
 1e-9 of their scale (FP64 build: CUDA's pow against glibc's in the last
 bits, grown quadratically with the step count as the flow through the
 outlet amplifies them: 1.5e-7 relative after 600 steps) or the FP32 bars of
-the WCSPH parity tests grown with the step count."""
+the WCSPH parity tests grown with the step count (positions with its square:
+a falling jet integrates its velocity error)."""
 
 import os
 
@@ -30,7 +36,9 @@ def _tol(precision, field, ref, steps, g):
         bar = 1e-9 * max(1.0, mag) * (1 + (steps / 50) ** 2)
     else:
         base = {"r": 1e-9, "v": 2e-6 + 1e-5 * mag, "rho": 2e-4, "p": 5e-2 + 1e-6 * mag}[field]
-        bar = base * (1 + steps / 10)
+        # positions integrate the velocity error, which grows with the step
+        # count: their bar grows with its square
+        bar = base * (1 + steps / 10) ** (2 if field == "r" else 1)
     # a flow that amplifies differences in the last bits: 10x the reference's
     # own spread under a roundoff-sized perturbation at this precision
     key = f"step{steps}_{field}_spread{precision[2:]}"
@@ -45,12 +53,15 @@ def _tol(precision, field, ref, steps, g):
     ("inflow_slab_mdbc_dp0.005.npz", lambda: cases.inflow_slab_mdbc(dp=0.005)),
     ("outlet_channel_mdbc_dp0.005.npz", lambda: cases.outlet_channel_mdbc(dp=0.005)),
     ("flow_drop_mdbc_dp0.02.npz", lambda: cases.flow_drop_mdbc(dp=0.02)),
+    ("flow_drop_bt_dp0.02.npz", lambda: cases.flow_drop_bt(dp=0.02)),
+    ("inflow_tank_bottom_mdbc_dp0.02.npz", lambda: cases.inflow_tank_bottom_mdbc(dp=0.02)),
 ])
 def test_zones_match_the_reference(gpu_tsph, fname, builder, precision):
     g = np.load(os.path.join(GOLD, fname))
     case = builder()
     s = gpu_tsph.ParticleSystem.from_case(case, precision)
     done = 0
+    over = []
     for n in g["snaps"]:
         s.step(case.wall_model, float(g["dt"]), int(n) - done)
         done = int(n)
@@ -62,4 +73,7 @@ def test_zones_match_the_reference(gpu_tsph, fname, builder, precision):
             ref = g[f"step{n}_{f}"]
             e = float(np.max(np.abs(st[f] - ref)))
             lim = _tol(precision, f, ref, int(n), g)
-            assert e <= lim, (n, f, e, lim)
+            print(fname, precision, int(n), f, f"{e:.3g}/{lim:.3g}")
+            if not e <= lim:
+                over.append((int(n), f, e, lim))
+    assert not over, over

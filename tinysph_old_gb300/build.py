@@ -86,5 +86,50 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return LIB
 
 
+TRACE_LIB = os.path.join(PKG, "libtsph_trace.so")
+
+
+def _cupti_dirs():
+    """(include dir, library dir) of CUPTI in the CUDA toolkit, or None."""
+    cuda = os.path.dirname(os.path.dirname(os.path.realpath(nvcc())))
+    for inc, lib in ((os.path.join(cuda, "include"), os.path.join(cuda, "lib64")),
+                     *[(os.path.join(cuda, "targets", t, "include"),
+                        os.path.join(cuda, "targets", t, "lib"))
+                       for t in ("x86_64-linux", "sbsa-linux", "aarch64-linux")],
+                     (os.path.join(cuda, "extras", "CUPTI", "include"),
+                      os.path.join(cuda, "extras", "CUPTI", "lib64"))):
+        if os.path.exists(os.path.join(inc, "cupti.h")) and os.path.exists(
+                os.path.join(lib, "libcupti.so")):
+            return inc, lib
+    return None
+
+
+def build_trace(force: bool = False) -> str | None:
+    """The optional kernel-timeline library (csrc/tsph_trace.cpp, CUPTI
+    activity records), used by the benchmark's per-kernel split of a graph
+    step.  Returns None where CUPTI is not installed."""
+    src = os.path.join(CSRC, "tsph_trace.cpp")
+    if not force and os.path.exists(TRACE_LIB) and \
+            os.path.getmtime(TRACE_LIB) >= os.path.getmtime(src):
+        return TRACE_LIB
+    dirs = _cupti_dirs()
+    cxx = shutil.which("g++")
+    if dirs is None or cxx is None:
+        return None
+    inc, lib = dirs
+    tmp = TRACE_LIB + ".tmp"
+    cmd = [cxx, "-std=c++17", "-O2", "-shared", "-fPIC", src, "-o", tmp, f"-I{inc}",
+           f"-I{os.path.join(os.path.dirname(inc), 'include')}", f"-L{lib}", "-lcupti",
+           f"-Wl,-rpath,{lib}"]
+    r = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT)
+    if r.returncode != 0:
+        print("libtsph_trace.so not built:\n" + r.stdout.decode(errors="replace"),
+              file=sys.stderr)
+        return None
+    os.replace(tmp, TRACE_LIB)
+    return TRACE_LIB
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_trace(force="--force" in sys.argv))

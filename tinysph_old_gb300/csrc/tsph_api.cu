@@ -436,6 +436,22 @@ int tsph_download(tsph_system *s, int fields, const tsph_host_state *out) {
     return TSPH_OK;
 }
 
+int tsph_download_async(tsph_system *s, int fields, const tsph_host_state *out) {
+    NEED(s);
+    if (!out) return fail(TSPH_ERR_ARG, "null output");
+    ENGINE(s);
+    RUN(s->eng->download_async(fields, out->r, out->v, out->a, out->rho, out->drho, out->p,
+                               err_));
+    return TSPH_OK;
+}
+
+int tsph_download_wait(tsph_system *s) {
+    NEED(s);
+    ENGINE(s);
+    RUN(s->eng->download_wait(err_));
+    return TSPH_OK;
+}
+
 int tsph_upload(tsph_system *s, int fields, const tsph_host_state *in) {
     NEED(s);
     if (!in) return fail(TSPH_ERR_ARG, "null input");

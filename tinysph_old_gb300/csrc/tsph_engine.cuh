@@ -46,6 +46,10 @@ template <typename T> class Engine final : public EngineBase {
     uint32_t *zlist_ = nullptr, *zcount_ = nullptr;
     int zlist_cap_ = 0;
     uint8_t *zlive_ = nullptr, *zcand_ = nullptr;
+    // the fused step's RemoveParticlesOutOfDomain: erase candidates and the
+    // indices removed so far
+    uint8_t *rm_cand_ = nullptr, *dead_ = nullptr;
+    uint32_t *rm_list_ = nullptr, *rm_count_ = nullptr;
     int ncells_ = 0;
     Grid grid_{};
     Phys<T> P_{};
@@ -85,6 +89,11 @@ template <typename T> class Engine final : public EngineBase {
     float skin_ = 0.f;             // per-axis move allowed without re-binning (FP32 fused step)
     WallState<T> W_{};
     Staging S_{};
+    // asynchronous download: its own staging set, copy stream and events
+    Staging D_{};
+    cudaStream_t cs_ = nullptr;
+    cudaEvent_t ev_x_ = nullptr, ev_d_ = nullptr;
+    bool d_pending_ = false;
     double *dtot_ = nullptr;
     long long *bx_ = nullptr, *by_ = nullptr;
     double *ox_ = nullptr, *oy_ = nullptr;
@@ -687,7 +696,8 @@ template <typename T> class Engine final : public EngineBase {
             const int nchunks = blocks_for(nf_, kRecT);
             const int rb = blocks_for((long long)nw_ + nf_);
             const int tb = rb + blocks_for(nchunks);
-            if ((rc = launch(CAT_PAIR, k_pair_records<false>, tb, kBlock, err, X, fs, W_, nw_, grid_,
+            // the records kernel is timed apart from the pair kernel (CAT_OTHER)
+            if ((rc = launch(CAT_OTHER, k_pair_records<false>, tb, kBlock, err, X, fs, W_, nw_, grid_,
                              P_, RX, rec_w_, rb, ws, nchunks, RecStd::cap, rec_table_, rec_nwin_,
                              gen_)))
                 return rc;
@@ -872,6 +882,12 @@ template <typename T> class Engine final : public EngineBase {
         // forces at the predicted state + corrector + bin
         if ((rc = zero_counts(err))) return rc;
         PairOut po{Br_, (void *)Bv_, (void *)Brho_, keyB_, slotB_, counts_, box_, make_box_bits(box_)};
+        po.rm = Removal{rm_cand_, rm_list_, rm_count_, kRemovalCap, (const uint32_t *)Fs_.id};
+        // the erase of the corrector's candidates, before the sort
+        auto resolve = [&](const uint32_t *gate) -> int {
+            return launch(CAT_SORT, k_resolve_removal, 1, kResolveThreads, err, po.rm, dead_, keyB_,
+                          slotB_, counts_, ncells_, health_, gate);
+        };
         auto wall_rows = [&]() -> int {
             if (nw_ == 0) return 0;
             return launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
@@ -902,13 +918,18 @@ template <typename T> class Engine final : public EngineBase {
             };
             if (capturing_) {
                 if ((rc = add_cond_body(cs_, 2, "sort body",
-                                        [&]() { return sort_new(nullptr, body_runs_ + 2); }, err)))
+                                        [&]() {
+                                            int r = resolve(nullptr);
+                                            return r ? r : sort_new(nullptr, body_runs_ + 2);
+                                        },
+                                        err)))
                     return rc;
                 if ((rc = add_cond_body(cc_, 3, "copy body",
                                         [&]() { return copy_kept(need_sort_, body_runs_ + 3); },
                                         err)))
                     return rc;
             } else {
+                if ((rc = resolve(need_sort_))) return rc;
                 if ((rc = sort_new(need_sort_, nullptr))) return rc;
                 if ((rc = copy_kept(need_sort_, nullptr))) return rc;
             }
@@ -924,6 +945,7 @@ template <typename T> class Engine final : public EngineBase {
         }
         if ((rc = fluid_pairs<MODE_CORRECT>(Fs_, false, dt, po, err, skinned))) return rc;
         if ((rc = wall_rows())) return rc;
+        if ((rc = resolve(nullptr))) return rc;
         if ((rc = sort_new(nullptr, nullptr))) return rc;
         // forces at the new state (a, drho for the next predictor)
         if ((rc = fluid_pairs<MODE_FORCES>(F_, false, dt, PairOut{}, err))) return rc;
@@ -938,6 +960,10 @@ template <typename T> class Engine final : public EngineBase {
 
   public:
     ~Engine() override {
+        if (cs_) cudaStreamSynchronize(cs_);  // a download still in flight
+        if (cs_) cudaStreamDestroy(cs_);
+        if (ev_x_) cudaEventDestroy(ev_x_);
+        if (ev_d_) cudaEventDestroy(ev_d_);
         for (auto &g : graphs_) cudaGraphExecDestroy(g.second);
         for (auto &m : marks_) {
             cudaEventDestroy(m.a);
@@ -1109,6 +1135,12 @@ template <typename T> class Engine final : public EngineBase {
             (rc = alloc(&rebuild_, 1, err)) || (rc = alloc(&body_runs_, 4, err)) ||
             (rc = alloc(&dtot_, 4 * (size_t)blocks_for(nf_), err)))
             return rc;
+        if ((rc = alloc(&rm_cand_, id_cap_, err)) || (rc = alloc(&dead_, id_cap_, err)) ||
+            (rc = alloc(&rm_list_, kRemovalCap, err)) || (rc = alloc(&rm_count_, 1, err)))
+            return rc;
+        TSPH_CK(cudaMemset(rm_cand_, 0, (size_t)std::max(id_cap_, 1)));
+        TSPH_CK(cudaMemset(dead_, 0, (size_t)std::max(id_cap_, 1)));
+        TSPH_CK(cudaMemset(rm_count_, 0, 4));
         TSPH_CK(cudaMemset(health_, 0, 4));
         TSPH_CK(cudaMemset(removed_, 0, 4));
         TSPH_CK(cudaMemset(body_runs_, 0, 16));
@@ -1351,7 +1383,7 @@ template <typename T> class Engine final : public EngineBase {
                          zlive_, zcand_)) ||
             (rc = launch(CAT_OTHER, k_remove_apply<T>, blocks_for(nf_), kBlock, err, F_,
                          (const uint32_t *)fstart_, ncells_, (const uint8_t *)zlive_,
-                         (const uint8_t *)zcand_, removed_, health_)))
+                         (const uint8_t *)zcand_, removed_, health_, dead_)))
             return rc;
         uint32_t h = 0;
         TSPH_CK(cudaMemcpyAsync(&h, removed_, 4, cudaMemcpyDeviceToHost, st_));
@@ -1579,6 +1611,56 @@ template <typename T> class Engine final : public EngineBase {
                 if (dense || alive[i]) type[o++] = t[i];
         }
         return collect_profile(err);
+    }
+
+    // tsph_download_async: the export into a staging set of its own on the
+    // system's stream, then the device-to-host copies on a copy stream, so
+    // that the copies run beside whatever the caller enqueues next (the next
+    // step's upload and kernels); download_wait ends them.  One download in
+    // flight at a time.  States with erased particles take the synchronous
+    // path (their rows are compacted on the host).
+    int download_async(int mask, double *r, double *v, double *a, double *rho, double *drho,
+                       double *p, std::string &err) override {
+        int rc;
+        if (mask & ~63) {
+            err = "tsph_download_async: r, v, a, rho, drho and p only";
+            return 1;
+        }
+        if ((rc = download_wait(err))) return rc;
+        bool dense = false;
+        if ((rc = dense_by_count(dense, err))) return rc;
+        if (!dense) return download(mask, r, v, a, rho, drho, p, nullptr, nullptr, err);
+        if (!D_.r) {
+            if ((rc = alloc(&D_.r, id_cap_, err)) || (rc = alloc(&D_.v, id_cap_, err)) ||
+                (rc = alloc(&D_.a, id_cap_, err)) || (rc = alloc(&D_.rho, id_cap_, err)) ||
+                (rc = alloc(&D_.drho, id_cap_, err)) || (rc = alloc(&D_.p, id_cap_, err)) ||
+                (rc = alloc(&D_.alive, id_cap_, err)))
+                return rc;
+            TSPH_CK(cudaStreamCreateWithFlags(&cs_, cudaStreamNonBlocking));
+            TSPH_CK(cudaEventCreateWithFlags(&ev_x_, cudaEventDisableTiming));
+            TSPH_CK(cudaEventCreateWithFlags(&ev_d_, cudaEventDisableTiming));
+        }
+        if ((rc = launch(CAT_OTHER, k_export<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                         (const uint32_t *)fstart_, ncells_, W_, nw_, P_.rho0, D_, mask)))
+            return rc;
+        TSPH_CK(cudaEventRecord(ev_x_, st_));
+        TSPH_CK(cudaStreamWaitEvent(cs_, ev_x_, 0));
+        const void *src[6] = {D_.r, D_.v, D_.a, D_.rho, D_.drho, D_.p};
+        double *dst[6] = {r, v, a, rho, drho, p};
+        for (int k = 0; k < 6; k++)
+            if ((mask & (1 << k)) && dst[k])
+                TSPH_CK(cudaMemcpyAsync(dst[k], src[k], (k < 3 ? 16 : 8) * (size_t)ntot_,
+                                        cudaMemcpyDeviceToHost, cs_));
+        TSPH_CK(cudaEventRecord(ev_d_, cs_));
+        d_pending_ = true;
+        return 0;
+    }
+
+    int download_wait(std::string &err) override {
+        if (!d_pending_) return 0;
+        d_pending_ = false;
+        TSPH_CK(cudaEventSynchronize(ev_d_));
+        return 0;
     }
 
     int upload(int mask, const double *r, const double *v, const double *a, const double *rho,

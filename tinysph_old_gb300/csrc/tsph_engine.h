@@ -56,6 +56,9 @@ class EngineBase {
     // reports which indices are alive (removed particles are not)
     virtual int download(int mask, double *r, double *v, double *a, double *rho, double *drho,
                          double *p, int32_t *index, int32_t *type, std::string &err) = 0;
+    virtual int download_async(int mask, double *r, double *v, double *a, double *rho,
+                               double *drho, double *p, std::string &err) = 0;
+    virtual int download_wait(std::string &err) = 0;
     virtual int upload(int mask, const double *r, const double *v, const double *a,
                        const double *rho, const double *drho, const double *p,
                        std::string &err) = 0;

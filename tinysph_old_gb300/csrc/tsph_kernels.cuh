@@ -519,6 +519,22 @@ __device__ __forceinline__ bool out_of_domain(double2 r, Box box) {
 // ---------------------------------------------------------- pair loop
 enum { MODE_FORCES = 0, MODE_CORRECT = 1, MODE_DIGEST = 2 };
 
+// RemoveParticlesOutOfDomain inside the fused step (src/SPH_btdebug.h:4-31).
+// The reference erases inside a forward loop, so the particle right after an
+// erased one is not examined in that call.  The corrector lists the fluid it
+// moved outside the box as erase candidates (their cell kept aside, no
+// histogram slot yet); k_resolve_removal then erases a candidate unless the
+// run of candidates just before it (in index order, over present indices)
+// has odd length, and counts every listed row into the histogram.
+struct Removal {
+    uint8_t *cand = nullptr;  // [particle index]: erase candidate this step
+    uint32_t *list = nullptr; // rows of the candidates
+    uint32_t *count = nullptr;
+    int cap = 0;
+    const uint32_t *ids = nullptr;  // particle index of each row of the corrected state
+};
+constexpr int kRemovalCap = 8192;  // candidates resolved per step
+
 struct PairOut {  // where MODE_CORRECT writes the new (unsorted) state
     double2 *r;
     void *v;
@@ -526,7 +542,19 @@ struct PairOut {  // where MODE_CORRECT writes the new (unsorted) state
     uint32_t *key, *slot, *counts;
     Box box;
     BoxBits boxb;
+    Removal rm{};
 };
+
+// a listed erase candidate: its cell if it survives the erase, no slot yet;
+// false when the list is full (the candidate is then erased at once)
+__device__ __forceinline__ bool list_removal(const Removal &rm, int row) {
+    if (!rm.list) return false;
+    const uint32_t k = atomicAdd(rm.count, 1u);
+    if (k >= (uint32_t)rm.cap) return false;
+    rm.list[k] = (uint32_t)row;
+    rm.cand[rm.ids[row]] = 1;
+    return true;
+}
 
 // ordered bits with -0.0 folded onto +0.0 (they compare equal in FP64)
 __host__ __device__ inline long long ordered_bits_fold0(double x) {
@@ -669,7 +697,9 @@ template <typename T> struct BtAcc {
 
 // One pair of the boundary-integral flavour, src/SPH_interactionBT.h:99-172
 // (a = fluid target, b = neighbour): a fluid neighbour adds the WCSPH terms
-// and W m / rho_b to the Shepard sum gamma; a wall neighbour with normal n_b
+// and W m / rho_b to the Shepard sum gamma (a buffer-zone neighbour, `shep`
+// false, adds the terms but not to gamma: the sum takes fluid-typed
+// particles only); a wall neighbour with normal n_b
 // adds W (p_temp + visco) dp n_b rho_b to the momentum sum and
 // -(dv . n_b) W rho_b dp to the continuity sum (its diffusion term is not
 // used).  Arithmetic in the reference's order; out-of-support pairs add
@@ -678,7 +708,7 @@ template <typename T> struct BtAcc {
 template <typename T>
 __device__ __forceinline__ void bt_pair(T drx, T dry, T dvx, T dvy, T arho, T nrho, T ap, T np_,
                                         bool wall, T nbx, T nby, const Phys<T> &P,
-                                        BtAcc<T> &acc) {
+                                        BtAcc<T> &acc, bool shep = true) {
     T drs, W, F;
     if constexpr (std::is_same<T, double>::value) {
         drs = sqrt((drx * drx) + (dry * dry));
@@ -732,7 +762,7 @@ __device__ __forceinline__ void bt_pair(T drx, T dry, T dvx, T dvy, T arho, T nr
         const T DT = psi * drdW * P.m / nrho;
         acc.cont += dvdW * P.m;
         acc.diff -= DT;
-        acc.gamma += W * P.m / nrho;
+        if (shep) acc.gamma += W * P.m / nrho;
     }
 }
 
@@ -807,8 +837,9 @@ k_fluid_pairs(FluidState<T> F, const uint32_t *__restrict__ fstart,
                         nbx = (T)nb.x;
                         nby = (T)nb.y;
                     }
+                    const bool shep = part == 1 && !(N.type && __ldg(N.type + j) != 0);
                     bt_pair<T>(drx, dry, va.x - vb.x, va.y - vb.y, rho_a, nrho, pa, pb, part == 0,
-                               nbx, nby, P, bacc);
+                               nbx, nby, P, bacc, shep);
                 }
                 continue;
             }
@@ -897,17 +928,22 @@ k_fluid_pairs(FluidState<T> F, const uint32_t *__restrict__ fstart,
             reinterpret_cast<typename V2<T>::t *>(out.v)[i] = nv;
             reinterpret_cast<T *>(out.rho)[i] = s_new;
             uint32_t nk;
+            bool listed = false;
+            int ncx_, ncy_;
             if (out_of_domain(rn, out.box)) {
-                nk = (uint32_t)ncells;
-                atomicOr(health, kHealthRemoved);
+                nk = cell_key(g, rn, key, &ncx_, &ncy_);  // kept if the erase skips it
+                listed = list_removal(out.rm, i);
+                if (!listed) {
+                    nk = (uint32_t)ncells;
+                    atomicOr(health, kHealthRemoved);
+                }
             } else {
-                int ncx_, ncy_;
                 nk = cell_key(g, rn, key, &ncx_, &ncy_);
                 if (nk == (uint32_t)ncells) atomicOr(health, kHealthEscaped);
             }
             if (!(nv.x == nv.x) || !(nv.y == nv.y) || !(s_new == s_new)) atomicOr(health, kHealthNan);
             out.key[i] = nk;
-            out.slot[i] = atomicAdd(out.counts + nk, 1u);
+            if (!listed) out.slot[i] = atomicAdd(out.counts + nk, 1u);
         }
     }
 }
@@ -939,6 +975,7 @@ k_bt_density(WallState<T> Wl, int nw, const uint32_t *__restrict__ fstart, Nbr<T
         const float offy = (float)(-kDY[k]) * g.khf;
         const int j0 = (int)__ldg(fstart + c), j1 = (int)__ldg(fstart + c + 1);
         for (int j = j0; j < j1; j++) {
+            if (NF.type && __ldg(NF.type + j) != 0) continue;  // fluid only (buffer zones)
             T W;
             if constexpr (std::is_same<T, float>::value) {
                 const float2 lb = __ldg(NF.loc + j);
@@ -1551,6 +1588,49 @@ __global__ void k_totals(FluidState<T> F, const uint32_t *__restrict__ fstart, i
         for (int w = 0; w < kBlock / 32; w++) s += sh[threadIdx.x][w];
         out[(size_t)blockIdx.x * 4 + threadIdx.x] = s;
     }
+}
+
+// RemoveParticlesOutOfDomain's erase over the corrector's candidates (one
+// block; before the sort): all parities are read before any erase is
+// written.  A candidate that survives keeps the cell it was binned into; one
+// outside the cell grid cannot be binned and is dropped as escaped.
+constexpr int kResolveThreads = 1024;
+static __global__ void __launch_bounds__(kResolveThreads)
+k_resolve_removal(Removal rm, uint8_t *__restrict__ dead, uint32_t *__restrict__ key,
+                  uint32_t *__restrict__ slot, uint32_t *__restrict__ counts, int ncells,
+                  uint32_t *__restrict__ health, const uint32_t *__restrict__ gate) {
+    pdl_enter();
+    if (gated_off(gate)) return;
+    __shared__ uint8_t erase[kRemovalCap];
+    const int n = (int)min(*rm.count, (uint32_t)rm.cap);
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const int id = (int)rm.ids[rm.list[k]];
+        int c = 0;
+        for (int j = id - 1; j >= 0; j--) {
+            if (dead[j]) continue;
+            if (!rm.cand[j]) break;
+            c++;
+        }
+        erase[k] = (c & 1) == 0 ? 1 : 0;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        const uint32_t row = rm.list[k];
+        uint32_t kk = key[row];
+        if (erase[k]) {
+            kk = (uint32_t)ncells;
+            dead[rm.ids[row]] = 1;
+            atomicOr(health, kHealthRemoved);
+        } else if (kk == (uint32_t)ncells) {
+            dead[rm.ids[row]] = 1;
+            atomicOr(health, kHealthEscaped);
+        }
+        key[row] = kk;
+        slot[row] = atomicAdd(counts + kk, 1u);
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) rm.cand[rm.ids[rm.list[k]]] = 0;
+    if (threadIdx.x == 0) *rm.count = 0u;
 }
 
 }  // namespace tsph

@@ -607,13 +607,18 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 reinterpret_cast<float2 *>(out.v)[i] = nv;
                 reinterpret_cast<float *>(out.rho)[i] = s_new;
                 uint32_t nk;
-                bool resort = false;
+                bool resort = false, listed = false;
+                int ncx_, ncy_;
                 if (out_of_domain_bits(rn, out.boxb)) {
-                    nk = (uint32_t)g.ncells;
-                    atomicOr(health, kHealthRemoved);
+                    // an erase candidate: its cell kept in case the erase skips it
+                    nk = cell_key(g, rn, (uint32_t)(cxa * ncy + cy), &ncx_, &ncy_);
+                    listed = list_removal(out.rm, i);
+                    if (!listed) {
+                        nk = (uint32_t)g.ncells;
+                        atomicOr(health, kHealthRemoved);
+                    }
                     resort = true;
                 } else {
-                    int ncx_, ncy_;
                     nk = cell_key(g, rn, (uint32_t)(cxa * ncy + cy), &ncx_, &ncy_);
                     if (nk == (uint32_t)g.ncells) {
                         atomicOr(health, kHealthEscaped);
@@ -623,7 +628,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 if (!(nv.x == nv.x) || !(nv.y == nv.y) || !(s_new == s_new))
                     atomicOr(health, kHealthNan);
                 out.key[i] = nk;
-                out.slot[i] = atomicAdd(out.counts + nk, 1u);
+                if (!listed) out.slot[i] = atomicAdd(out.counts + nk, 1u);
                 // the new position relative to the kept cell, and whether the
                 // cells must be rebuilt before the next pass
                 const float2 ln = make_float2((float)(rn.x - __ldg(g.ax.org + cxa)),

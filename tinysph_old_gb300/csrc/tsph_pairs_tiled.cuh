@@ -394,18 +394,24 @@ k_pairs_tiled(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 reinterpret_cast<float2 *>(out.v)[i] = nv;
                 reinterpret_cast<float *>(out.rho)[i] = s_new;
                 uint32_t nk;
+                bool listed = false;
+                int ncx_, ncy_;
                 if (out_of_domain_bits(rn, out.boxb)) {
-                    nk = (uint32_t)g.ncells;
-                    atomicOr(health, kHealthRemoved);
+                    // an erase candidate: its cell kept in case the erase skips it
+                    nk = cell_key(g, rn, (uint32_t)(cx * ncy + cy), &ncx_, &ncy_);
+                    listed = list_removal(out.rm, i);
+                    if (!listed) {
+                        nk = (uint32_t)g.ncells;
+                        atomicOr(health, kHealthRemoved);
+                    }
                 } else {
-                    int ncx_, ncy_;
                     nk = cell_key(g, rn, (uint32_t)(cx * ncy + cy), &ncx_, &ncy_);
                     if (nk == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
                 }
                 if (!(nv.x == nv.x) || !(nv.y == nv.y) || !(s_new == s_new))
                     atomicOr(health, kHealthNan);
                 out.key[i] = nk;
-                out.slot[i] = atomicAdd(out.counts + nk, 1u);
+                if (!listed) out.slot[i] = atomicAdd(out.counts + nk, 1u);
             }
         }
         cur = we;

@@ -177,13 +177,15 @@ __global__ void k_remove_mark(FluidState<T> F, const uint32_t *__restrict__ fsta
 template <typename T>
 __global__ void k_remove_apply(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
                                const uint8_t *__restrict__ live, const uint8_t *__restrict__ cand,
-                               uint32_t *__restrict__ removed, uint32_t *__restrict__ health) {
+                               uint32_t *__restrict__ removed, uint32_t *__restrict__ health,
+                               uint8_t *__restrict__ dead) {
     pdl_enter();
     const int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= n_live(fstart, ncells) || F.key[f] == (uint32_t)ncells) return;
     const int id = (int)F.id[f];
     if (!cand[id] || skipped_after_erase(live, cand, id)) return;
     F.key[f] = (uint32_t)ncells;
+    if (dead) dead[id] = 1;
     atomicAdd(removed, 1u);
     atomicOr(health, kHealthRemoved);
 }

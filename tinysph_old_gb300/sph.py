@@ -39,6 +39,7 @@ ABI_SYMBOLS = (
     "tsph_add_buffer_zone", "tsph_set_zone_capacity", "tsph_bz_inlet", "tsph_bz_outlet",
     "tsph_compute_forces", "tsph_symplectic_predictor", "tsph_symplectic_corrector",
     "tsph_remove_out_of_domain", "tsph_step", "tsph_download", "tsph_upload", "tsph_sync",
+    "tsph_download_async", "tsph_download_wait",
     "tsph_health", "tsph_kernel_launches", "tsph_fluid_totals", "tsph_set_profiling",
     "tsph_get_profile",
     "tsph_water_level", "tsph_point_fields", "tsph_water_front", "tsph_autotune",
@@ -151,6 +152,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_step.argtypes = [P, I, D, I]
     L.tsph_download.argtypes = [P, I, C.POINTER(_HostState)]
     L.tsph_upload.argtypes = [P, I, C.POINTER(_HostState)]
+    L.tsph_download_async.argtypes = [P, I, C.POINTER(_HostState)]
+    L.tsph_download_wait.argtypes = [P]
     L.tsph_health.argtypes = [P, C.POINTER(C.c_uint32), I]
     L.tsph_kernel_launches.argtypes = [P, C.POINTER(C.c_longlong), I]
     L.tsph_fluid_totals.argtypes = [P, P]
@@ -422,6 +425,17 @@ class ParticleSystem:
         for k, v in ptrs.items():
             setattr(hs, k, v)
         _check(self._L.tsph_download(self._h, int(mask), C.byref(hs)))
+
+    def download_async(self, mask, **ptrs):
+        """Start a download into raw host pointers (pinned buffers, kept
+        valid until download_wait); r, v, a, rho, drho and p only."""
+        hs = _HostState()
+        for k, v in ptrs.items():
+            setattr(hs, k, v)
+        _check(self._L.tsph_download_async(self._h, int(mask), C.byref(hs)))
+
+    def download_wait(self):
+        _check(self._L.tsph_download_wait(self._h))
 
     def sync(self):
         _check(self._L.tsph_sync(self._h))
