@@ -1,7 +1,9 @@
 """tsph_kernel_launches: the kernels a system launched.  A graph step counts
 its kernels, so the count grows by the same amount per step (the conditional
-re-binning stays off at these speeds); the end-of-call equation of state adds
-one per call; reset clears it."""
+re-binning and sort stay off at these speeds: four kernels per FP32 mDBC step
+over pair records with kept lists, mDBC + predictor, two pair passes and the
+wall rows, more with the tiled kernels); the end-of-call equation of state
+adds one per call; reset clears it."""
 
 import pytest
 
@@ -19,6 +21,6 @@ def test_kernel_launch_count_per_graph_step(gpu_tsph):
     s.step(case.wall_model, case.dt, 15)
     c15 = s.kernel_launches(reset=True)
     per_step = (c15 - c5) / 10
-    assert per_step == int(per_step) and 6 <= per_step <= 12, (c5, c15)
+    assert per_step == int(per_step) and 4 <= per_step <= 12, (c5, c15)
     assert c5 == 5 * per_step + 1  # + the equation of state after the call
     assert s.kernel_launches() == 0

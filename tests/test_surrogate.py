@@ -190,15 +190,20 @@ def test_bf16_tensor_core_inference_matches_the_fp32_forward(gpu_tsph):
 
 
 @pytest.mark.gpu
-def test_fallback_windows_reproduce_plain_stepping(gpu_tsph):
+@pytest.mark.parametrize("variant", [0, 2])
+def test_fallback_windows_reproduce_plain_stepping(gpu_tsph, variant):
     """A rollout whose every window fails its check (tolerance below zero)
     restores the saved state and runs the plain steps: bit-identical to plain
-    stepping."""
+    stepping, with the tiled pair kernel and with the pair-records kernel
+    (whose kept neighbour lists the window's own binnings overwrite: the
+    restore rebuilds them at the saved binning positions)."""
     from tinysph_old_gb300 import surrogate as S
 
     case = cases.dam_break_mdbc(dp=0.02)
     a = gpu_tsph.ParticleSystem.from_case(case)
     b = gpu_tsph.ParticleSystem.from_case(case)
+    a.set_tile_shape(variant)
+    b.set_tile_shape(variant)
     a.step(0, case.dt, 8)
     b.step(0, case.dt, 8)
     ro = S.Rollout(a, S.Model.zero(), case.dt, 0, case.h, use_net=False, tol_density=-1.0)

@@ -288,7 +288,6 @@ template <typename T> class Engine final : public EngineBase {
     int tiled_best_ = 0;  // the faster of shapes 0 and 1 (per-function calls with shape 2)
     // cells kept over several steps (fused step with shape 2)
     float2 *lbin_ = nullptr;      // cell-relative positions at the last binning (F_ order)
-    float2 *bloc_ = nullptr;      // the corrector's new cell-relative positions
     uint16_t *rec_list_ = nullptr;
     uint8_t *rec_cnt_ = nullptr;
     uint32_t *gen_ = nullptr;     // {sorts, sort the lists were built after, -, CTAs done}
@@ -585,11 +584,30 @@ template <typename T> class Engine final : public EngineBase {
         cells_kept_ = saved_kept_;
         exported_ = false;
         kicked_ = false;
-        if (rec_passes_ != rec_passes_sv_) return mark_stale(err);
         TSPH_CK(cudaMemcpyAsync(lbin_, lbin_sv_, sizeof(float2) * (size_t)nf_,
                                 cudaMemcpyDeviceToDevice, st_));
         TSPH_CK(cudaMemcpyAsync(gen_, gen_sv_, 16, cudaMemcpyDeviceToDevice, st_));
-        return 0;
+        // the window table of the restored cells (a binning since the save
+        // may have rebuilt it for other cells)
+        int rc;
+        if ((rc = pair_records(F_, nullptr, true, err))) return rc;
+        if (rec_passes_ == rec_passes_sv_) return 0;  // the lists are the saved state's
+        // lists rebuilt since the save: when the saved state's were current,
+        // build them again at its binning positions (the same lists), else
+        // leave them stale as they were
+        if constexpr (std::is_same<T, float>::value) {
+            uint32_t g[4];
+            TSPH_CK(cudaMemcpyAsync(g, gen_sv_, 16, cudaMemcpyDeviceToHost, st_));
+            TSPH_CK(cudaStreamSynchronize(st_));
+            if (g[0] == g[1] && rec_f_.t && tile_shape_ == 2) {
+                if ((rc = launch(CAT_OTHER, k_lbin_records, blocks_for(nf_), kBlock, err, rec_f_,
+                                 (const float2 *)lbin_, (const uint32_t *)F_.key,
+                                 (const uint32_t *)fstart_, grid_)))
+                    return rc;
+                return fluid_pairs_rec<MODE_LISTS>(F_, T(0), PairOut{}, err, 0, false);
+            }
+        }
+        return mark_stale(err);
     }
 
     int set_tile_shape(int shape, std::string &err) override {
@@ -678,13 +696,13 @@ template <typename T> class Engine final : public EngineBase {
     // happened since they were built) or sums the stored ones
     template <int MODE>
     int fluid_pairs_rec(const FluidState<T> &X, T dt, PairOut po, std::string &err,
-                        cudaGraphConditionalHandle cond_sort = 0,
-                        cudaGraphConditionalHandle cond_copy = 0) {
+                        cudaGraphConditionalHandle cond_sort = 0, bool records = true) {
         if constexpr (std::is_same<T, float>::value) {
             int rc;
             if (!rec_setup_) {
-                const void *kr[2] = {(const void *)k_pairs_rec<MODE_FORCES, false, RecStd>,
-                                     (const void *)k_pairs_rec<MODE_CORRECT, false, RecStd>};
+                const void *kr[3] = {(const void *)k_pairs_rec<MODE_FORCES, false, RecStd>,
+                                     (const void *)k_pairs_rec<MODE_CORRECT, false, RecStd>,
+                                     (const void *)k_pairs_rec<MODE_LISTS, false, RecStd>};
                 for (const void *k : kr)
                     TSPH_CK(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
                                                  (int)cudaSharedmemCarveoutMaxShared));
@@ -694,15 +712,11 @@ template <typename T> class Engine final : public EngineBase {
             const uint32_t *fs = fstart_, *ws = wstart_;
             const PairRec RX = X.r == Fs_.r ? rec_s_ : rec_f_;
             const int nchunks = blocks_for(nf_, kRecT);
-            const int rb = blocks_for((long long)nw_ + nf_);
-            const int tb = rb + blocks_for(nchunks);
-            // the records kernel is timed apart from the pair kernel (CAT_OTHER)
-            if ((rc = launch(CAT_OTHER, k_pair_records<false>, tb, kBlock, err, X, fs, W_, nw_, grid_,
-                             P_, RX, rec_w_, rb, ws, nchunks, RecStd::cap, rec_table_, rec_nwin_,
-                             gen_)))
-                return rc;
-            RecStep S{rec_list_, rec_cnt_, gen_, (const float2 *)lbin_, sig2_, bloc_, need_sort_,
-                      cond_sort, cond_copy, capturing_ ? 1 : 0};
+            if (records && (rc = pair_records(X, nullptr, false, err))) return rc;
+            // MODE_CORRECT writes the new state into F_ in the kept order,
+            // with its cell-relative positions and the next pass's records
+            RecStep S{rec_list_, rec_cnt_, gen_, (const float2 *)lbin_, sig2_, F_.loc, rec_f_,
+                      need_sort_, cond_sort, capturing_ ? 1 : 0};
             return launch(CAT_PAIR, k_pairs_rec<MODE, false, RecStd>, nchunks, kRecT, err, X, fs, ws,
                           W_, grid_, P_, Krec_, Krec_build_, O_, dt, po, RX, rec_w_,
                           (const WinRec *)rec_table_, (const int *)rec_nwin_, S, health_);
@@ -711,9 +725,48 @@ template <typename T> class Engine final : public EngineBase {
             (void)dt;
             (void)po;
             (void)cond_sort;
-            (void)cond_copy;
+            (void)records;
             err = "pair records: FP32 build only";
             return 8;
+        }
+    }
+
+    // the neighbour lists of F_ at its binned positions (MODE_LISTS pass,
+    // records of F_ already formed), for systems whose fused step keeps them
+    int build_lists(std::string &err) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (!rec_f_.t || tile_shape_ != 2 || skin_ <= 0.f || wall_model_ == 2 || zones_on_)
+                return 0;
+            int rc;
+            return fluid_pairs_rec<MODE_LISTS>(F_, T(0), PairOut{}, err, 0, false);
+        } else {
+            (void)err;
+            return 0;
+        }
+    }
+
+    // the pair records of state X (fluid rows and walls) and, after a sort
+    // (or when forced), the window table: for passes whose records no
+    // producer wrote (after a binning, the autotuner)
+    int pair_records(const FluidState<T> &X, const uint32_t *gate, bool force_table,
+                     std::string &err) {
+        if constexpr (std::is_same<T, float>::value) {
+            if (!rec_f_.t) return 0;
+            const PairRec RX = X.r == Fs_.r ? rec_s_ : rec_f_;
+            const int nchunks = blocks_for(nf_, kRecT);
+            const int rb = blocks_for((long long)nw_ + nf_);
+            const int tb = rb + blocks_for(nchunks);
+            // the records kernel is timed apart from the pair kernel (CAT_OTHER)
+            return launch(CAT_OTHER, k_pair_records<false>, tb, kBlock, err, X,
+                          (const uint32_t *)fstart_, W_, nw_, grid_, P_, RX, rec_w_, rb,
+                          (const uint32_t *)wstart_, nchunks, RecStd::cap, rec_table_, rec_nwin_,
+                          gen_, gate, force_table ? 1 : 0);
+        } else {
+            (void)X;
+            (void)gate;
+            (void)force_table;
+            (void)err;
+            return 0;
         }
     }
 
@@ -828,14 +881,16 @@ template <typename T> class Engine final : public EngineBase {
                     const int nbm = blocks_for((long long)nw_ * kMdbcLanes);
                     rc = launch(CAT_MDBC, k_mdbc_f32_predict, nbm + blocks_for(nf_), kBlock, err, W_,
                                 nw_, nbm, (const uint32_t *)fstart_, F_, grid_, P_, dt, Fs_, O_,
-                                skin_, rebuild_, health_, cond, capturing_ ? 1 : 0, kc);
+                                skin_, rebuild_, health_, cond, capturing_ ? 1 : 0, kc,
+                                rec ? rec_s_ : PairRec{}, rec ? rec_w_ : PairRec{});
                     if (rc) return rc;
                 }
             }
             if (!mdbc_fused &&
                 (rc = launch(CAT_OTHER, k_predict_keep<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
                              (const uint32_t *)fstart_, W_, nw_, grid_, dt, Fs_, O_, skin_,
-                             rebuild_, health_, cond, capturing_ ? 1 : 0, kc)))
+                             rebuild_, health_, cond, capturing_ ? 1 : 0, kc,
+                             rec ? rec_s_ : PairRec{}, rec ? rec_w_ : PairRec{}, P_)))
                 return rc;
             if (capturing_) {
                 TSPH_CK(cudaStreamGetCaptureInfo(st_, &cs, nullptr, &cg, &deps, nullptr, &nd));
@@ -853,6 +908,7 @@ template <typename T> class Engine final : public EngineBase {
                 std::swap(st_, st2_);
                 body_ = 1;
                 rc = rebin_predicted(nullptr, err);
+                if (!rc && rec) rc = pair_records(Fs_, nullptr, false, err);
                 body_ = 0;
                 std::swap(st_, st2_);
                 cudaGraph_t bodyc = nullptr;
@@ -865,7 +921,8 @@ template <typename T> class Engine final : public EngineBase {
                 }
                 TSPH_CK(cudaStreamUpdateCaptureDependencies(st_, &cn, nullptr, 1,
                                                             cudaStreamSetCaptureDependencies));
-            } else if ((rc = rebin_predicted(rebuild_, err))) {
+            } else if ((rc = rebin_predicted(rebuild_, err)) ||
+                       (rec && (rc = pair_records(Fs_, rebuild_, false, err)))) {
                 return rc;
             }
         } else {
@@ -888,63 +945,74 @@ template <typename T> class Engine final : public EngineBase {
             return launch(CAT_SORT, k_resolve_removal, 1, kResolveThreads, err, po.rm, dead_, keyB_,
                           slotB_, counts_, ncells_, health_, gate);
         };
-        auto wall_rows = [&]() -> int {
+        auto wall_rows = [&](PairRec RW) -> int {
             if (nw_ == 0) return 0;
             return launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
                           (const uint32_t *)fstart_, nbr_fluid(Fs_, false), grid_, P_, dbc, true, dt,
                           (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
-                          (const uint32_t *)nullptr, false);
+                          (const uint32_t *)nullptr, false, RW);
         };
         auto sort_new = [&](const uint32_t *gate, uint32_t *runs) -> int {
             return sort_finish(Br_, Bv_, Brho_, Fs_.id, nullptr, nullptr, nullptr, F_, nullptr,
                                nullptr, nullptr, O_, err, gate, nullptr, runs);
         };
         if (rec) {
-            cudaGraphConditionalHandle cs_ = 0, cc_ = 0;
+            // The corrector writes the new state into F_ in the kept order,
+            // with the next pass's pair records (the walls' from k_wall_rows).
+            // Only when some particle left its kept cell's reach or the
+            // domain does the sort run: histogram, erase, sort of F_ into Fs_,
+            // rows copied back, records and window table of the new order
+            // (a conditional node in a graph, kernels gated on need_sort_
+            // otherwise).
+            cudaGraphConditionalHandle cs_ = 0;
             if (capturing_) {
                 cudaGraph_t cg = nullptr;
                 cudaStreamCaptureStatus cst;
                 TSPH_CK(cudaStreamGetCaptureInfo(st_, &cst, nullptr, &cg, nullptr, nullptr, nullptr));
                 TSPH_CK(cudaGraphConditionalHandleCreate(&cs_, cg, 0, cudaGraphCondAssignDefault));
-                TSPH_CK(cudaGraphConditionalHandleCreate(&cc_, cg, 1, cudaGraphCondAssignDefault));
             }
-            if ((rc = fluid_pairs_rec<MODE_CORRECT>(Fs_, dt, po, err, cs_, cc_))) return rc;
-            if ((rc = wall_rows())) return rc;
-            auto copy_kept = [&](const uint32_t *skip, uint32_t *runs) -> int {
-                return launch(CAT_SORT, k_copy_kept<T>, blocks_for(nf_), kBlock, err, F_,
-                              (const double2 *)Br_, (const T2 *)Bv_, (const T *)Brho_,
-                              (const float2 *)bloc_, (const uint32_t *)keyB_, counts_,
-                              (const uint32_t *)fstart_, ncells_, skip, runs);
+            PairOut pk{F_.r, (void *)F_.v, (void *)F_.rho, keyB_, slotB_, counts_, box_,
+                       make_box_bits(box_)};
+            pk.rm = Removal{rm_cand_, rm_list_, rm_count_, kRemovalCap, (const uint32_t *)F_.id};
+            if ((rc = fluid_pairs_rec<MODE_CORRECT>(Fs_, dt, pk, err, cs_, false))) return rc;
+            if ((rc = wall_rows(rec_w_))) return rc;
+            auto sort_kept = [&](const uint32_t *gate, uint32_t *runs) -> int {
+                int r;
+                if ((r = launch(CAT_SORT, k_hist_kept<T>, blocks_for(nf_), kBlock, err,
+                                (const FluidState<T>)F_, (const uint32_t *)keyB_, slotB_, counts_,
+                                (const uint8_t *)rm_cand_, (const uint32_t *)fstart_, ncells_, gate,
+                                runs)) ||
+                    (r = launch(CAT_SORT, k_resolve_removal, 1, kResolveThreads, err, pk.rm, dead_,
+                                keyB_, slotB_, counts_, ncells_, health_, gate)) ||
+                    (r = sort_finish(F_.r, F_.v, F_.rho, F_.id, nullptr, nullptr, nullptr, Fs_,
+                                     nullptr, nullptr, nullptr, O_, err, gate)) ||
+                    (r = launch(CAT_SORT, k_copy_rows<T>, blocks_for(nf_), kBlock, err, F_,
+                                (const FluidState<T>)Fs_, (const uint32_t *)fstart_, ncells_,
+                                gate)) ||
+                    (r = pair_records(F_, gate, false, err)))
+                    return r;
+                return 0;
             };
             if (capturing_) {
                 if ((rc = add_cond_body(cs_, 2, "sort body",
-                                        [&]() {
-                                            int r = resolve(nullptr);
-                                            return r ? r : sort_new(nullptr, body_runs_ + 2);
-                                        },
+                                        [&]() { return sort_kept(nullptr, body_runs_ + 2); },
                                         err)))
                     return rc;
-                if ((rc = add_cond_body(cc_, 3, "copy body",
-                                        [&]() { return copy_kept(need_sort_, body_runs_ + 3); },
-                                        err)))
-                    return rc;
-            } else {
-                if ((rc = resolve(need_sort_))) return rc;
-                if ((rc = sort_new(need_sort_, nullptr))) return rc;
-                if ((rc = copy_kept(need_sort_, nullptr))) return rc;
+            } else if ((rc = sort_kept(need_sort_, nullptr))) {
+                return rc;
             }
             // forces at the new state (a, drho for the next predictor)
-            if ((rc = fluid_pairs_rec<MODE_FORCES>(F_, dt, PairOut{}, err))) return rc;
+            if ((rc = fluid_pairs_rec<MODE_FORCES>(F_, dt, PairOut{}, err, 0, false))) return rc;
             if (dbc && nw_ > 0 &&
                 (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
                              (const uint32_t *)fstart_, nbr_fluid(F_, false), grid_, P_, true, false,
                              dt, (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
-                             (const uint32_t *)nullptr, false)))
+                             (const uint32_t *)nullptr, false, PairRec{})))
                 return rc;
             return 0;
         }
         if ((rc = fluid_pairs<MODE_CORRECT>(Fs_, false, dt, po, err, skinned))) return rc;
-        if ((rc = wall_rows())) return rc;
+        if ((rc = wall_rows(PairRec{}))) return rc;
         if ((rc = resolve(nullptr))) return rc;
         if ((rc = sort_new(nullptr, nullptr))) return rc;
         // forces at the new state (a, drho for the next predictor)
@@ -953,7 +1021,7 @@ template <typename T> class Engine final : public EngineBase {
             (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
                          (const uint32_t *)fstart_, nbr_fluid(F_, false), grid_, P_, true, false, dt,
                          (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
-                         (const uint32_t *)nullptr, false)))
+                         (const uint32_t *)nullptr, false, PairRec{})))
             return rc;
         return 0;
     }
@@ -1097,7 +1165,7 @@ template <typename T> class Engine final : public EngineBase {
             if ((rc = alloc_rec(rec_f_, nf_)) || (rc = alloc_rec(rec_s_, nf_)) ||
                 (rc = alloc_rec(rec_w_, nw_)) ||
                 (rc = alloc(&rec_table_, (size_t)nchunks * kRecMaxWin, err)) ||
-                (rc = alloc(&rec_nwin_, nchunks, err)) || (rc = alloc(&bloc_, nf_, err)) ||
+                (rc = alloc(&rec_nwin_, nchunks, err)) ||
                 (rc = alloc(&rec_list_, (size_t)nchunks * RecStd::list * kRecT, err)) ||
                 (rc = alloc(&rec_cnt_, (size_t)nchunks * kRecT, err)))
                 return rc;
@@ -1301,6 +1369,12 @@ template <typename T> class Engine final : public EngineBase {
                          (const FluidState<T>)Fs_, O_, OldState<T>{Br_, Bv_, Brho_},
                          (const uint32_t *)fstart_, ncells_)))
             return rc;
+        // pair records and window table of the new order (FP32 build); with
+        // kept lists (the fused step over pair records) also the lists of
+        // the new order, built at the binned positions, so that the next
+        // step keeps these cells
+        if ((rc = pair_records(F_, nullptr, false, err))) return rc;
+        if ((rc = build_lists(err))) return rc;
         cells_ = true;
         cells_kept_ = false;
         exported_ = false;
@@ -1347,7 +1421,7 @@ template <typename T> class Engine final : public EngineBase {
             (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
                          (const uint32_t *)fstart_, nbr_fluid(F_, true), grid_, P_, true, false, T(0),
                          (int32_t *)nullptr, (long long *)nullptr, (int32_t *)nullptr,
-                         (const uint32_t *)nullptr, false)))
+                         (const uint32_t *)nullptr, false, PairRec{})))
             return rc;
         return collect_profile(err);
     }
@@ -1768,7 +1842,7 @@ template <typename T> class Engine final : public EngineBase {
             (rc = launch(CAT_OTHER, k_wall_rows<T>, blocks_for(nw_), kBlock, err, W_, nw_,
                          (const uint32_t *)fstart_, nbr_fluid(F_, true), grid_, P_, true, false, T(0),
                          dig_count_ + nf_, dig_sum_ + nf_, dig_xor_ + nf_, (const uint32_t *)F_.id,
-                         true)))
+                         true, PairRec{})))
             return rc;
         TSPH_CK(cudaStreamSynchronize(st_));
         uint32_t nl = 0;

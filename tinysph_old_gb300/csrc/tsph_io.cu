@@ -183,16 +183,19 @@ int tsph_load_checkpoint(const char *path, void *stream, tsph_system **out) {
         tsph_destroy(s);
         return rc;
     }
+    // the saved variant of the pair kernel before the binning, which then
+    // prepares what that variant keeps (neighbour lists)
     if ((rc = tsph_add_particles(s, n, type.data(), r.data(), v.data(), rho.data(), p.data(),
                                  any_gnr ? gnr.data() : nullptr)) ||
-        (rc = tsph_divide_to_cells(s)) || (rc = tsph_particle_to_cell(s))) {
+        (rc = tsph_divide_to_cells(s)) ||
+        (head[2] >= 0 && (rc = tsph_set_tile_shape(s, head[2]))) ||
+        (rc = tsph_particle_to_cell(s))) {
         tsph_destroy(s);
         return rc;
     }
     tsph_host_state in = {nullptr, nullptr, a.data(), nullptr, drho.data(), nullptr, nullptr,
                           nullptr};
-    if ((rc = tsph_upload(s, TSPH_F_A | TSPH_F_DRHO, &in)) ||
-        (head[2] >= 0 && (rc = tsph_set_tile_shape(s, head[2])))) {
+    if ((rc = tsph_upload(s, TSPH_F_A | TSPH_F_DRHO, &in))) {
         tsph_destroy(s);
         return rc;
     }

@@ -517,7 +517,36 @@ __device__ __forceinline__ bool out_of_domain(double2 r, Box box) {
 }
 
 // ---------------------------------------------------------- pair loop
-enum { MODE_FORCES = 0, MODE_CORRECT = 1, MODE_DIGEST = 2 };
+// MODE_LISTS (pair kernel over pair records only): build and store the
+// neighbour lists, compute nothing else
+enum { MODE_FORCES = 0, MODE_CORRECT = 1, MODE_DIGEST = 2, MODE_LISTS = 3 };
+
+// 1/x by the hardware's approximate reciprocal (rcp.approx.ftz.f32)
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// One set of pair records (fluid rows or walls; FP32 pair kernel over pair
+// records): per row, t = (x, row kh + y) and y = (y, row) with (x, y) the
+// position relative to the row's cell, v = (vx, vy, rho - rho0, p / rho),
+// inv = 1 / rho.  Written by whichever kernel last changed the row (the
+// predictor, the corrector, the walls' density kernels) or by k_pair_records.
+struct PairRec {
+    float2 *t, *y;
+    float4 *v;
+    float *inv;
+};
+
+// a wall's density-dependent record fields (walls do not move: their t, y
+// stay as k_pair_records wrote them)
+__device__ __forceinline__ void wall_record(const PairRec &RW, int w, float s,
+                                            const Phys<float> &P) {
+    const float ib = rcp_approx(P.rho0 + s);
+    RW.v[w] = make_float4(0.f, 0.f, s, eos(s, P) * ib);
+    RW.inv[w] = ib;
+}
 
 // RemoveParticlesOutOfDomain inside the fused step (src/SPH_btdebug.h:4-31).
 // The reference erases inside a forward loop, so the particle right after an
@@ -1010,7 +1039,7 @@ __global__ void __launch_bounds__(kBlock)
 k_wall_rows(WallState<T> Wl, int nw, const uint32_t *__restrict__ fstart, Nbr<T> NF, Grid g,
             Phys<T> P, bool dbc, bool correct, T dt, int32_t *__restrict__ dig_count,
             long long *__restrict__ dig_sum, int32_t *__restrict__ dig_xor,
-            const uint32_t *__restrict__ fid, bool digest) {
+            const uint32_t *__restrict__ fid, bool digest, PairRec RW) {
     pdl_enter();
     const int w = blockIdx.x * blockDim.x + threadIdx.x;
     if (w >= nw) return;
@@ -1079,7 +1108,12 @@ k_wall_rows(WallState<T> Wl, int nw, const uint32_t *__restrict__ fstart, Nbr<T>
         else drho = acc.cont + acc.diff;
         Wl.drho[w] = drho;
     }
-    if (correct) Wl.rho[w] = corrector_rho(Wl.rho_o[w], sa, drho, dt, P.rho0);
+    if (correct) {
+        const T sn = corrector_rho(Wl.rho_o[w], sa, drho, dt, P.rho0);
+        Wl.rho[w] = sn;
+        if constexpr (std::is_same<T, float>::value)
+            if (RW.v) wall_record(RW, w, sn, P);
+    }
 }
 
 // ------------------------------------------------------------- mDBC
@@ -1318,7 +1352,9 @@ __device__ __forceinline__ void predict_keep_fluid(int f, const FluidState<T> &F
                                                    uint32_t *__restrict__ rebuild,
                                                    uint32_t *__restrict__ health,
                                                    cudaGraphConditionalHandle cond, int use_cond,
-                                                   const KeepCells &kc) {
+                                                   const KeepCells &kc,
+                                                   const PairRec &R = PairRec{},
+                                                   const Phys<T> *P = nullptr) {
     if (f == 0 && kc.clear) *kc.clear = 0u;
     if (f >= n_live(fstart, g.ncells)) return;
     const double2 r = F.r[f];
@@ -1335,12 +1371,24 @@ __device__ __forceinline__ void predict_keep_fluid(int f, const FluidState<T> &F
     nv.x = v.x + a.x * dt * T(0.5);
     nv.y = v.y + a.y * dt * T(0.5);
     D.v[f] = nv;
-    D.rho[f] = s + F.drho[f] * dt * T(0.5);
+    const T sp = s + F.drho[f] * dt * T(0.5);
+    D.rho[f] = sp;
     const float2 l = F.loc[f];
     const float2 ln = make_float2(l.x + dx, l.y + dy);
     D.loc[f] = ln;
-    D.key[f] = F.key[f];
+    const uint32_t key = F.key[f];
+    D.key[f] = key;
     D.id[f] = F.id[f];
+    if constexpr (std::is_same<T, float>::value) {
+        if (R.t) {  // the pair records of the predicted state (kept cells)
+            const float row = (float)(key % (uint32_t)g.ncy);
+            const float ib = rcp_approx(P->rho0 + sp);
+            R.t[f] = make_float2(ln.x, fmaf(row, g.khf, ln.y));
+            R.y[f] = make_float2(ln.y, row);
+            R.v[f] = make_float4(nv.x, nv.y, sp, eos(sp, *P) * ib);
+            R.inv[f] = ib;
+        }
+    }
     bool rebin;
     if (kc.lbin) {
         const float2 lb = kc.lbin[f];
@@ -1387,17 +1435,20 @@ __global__ void k_predict_keep(FluidState<T> F, const uint32_t *__restrict__ fst
                                WallState<T> Wl, int nw, Grid g, T dt, FluidState<T> D,
                                OldState<T> O, float skin, uint32_t *__restrict__ rebuild,
                                uint32_t *__restrict__ health, cudaGraphConditionalHandle cond,
-                               int use_cond, KeepCells kc) {
+                               int use_cond, KeepCells kc, PairRec RS, PairRec RW, Phys<T> P) {
     pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < nw) {
         const T r = Wl.rho[i];
         Wl.rho_o[i] = r;
-        Wl.rho[i] = r + Wl.drho[i] * dt * T(0.5);
+        const T rp = r + Wl.drho[i] * dt * T(0.5);
+        Wl.rho[i] = rp;
+        if constexpr (std::is_same<T, float>::value)
+            if (RW.v) wall_record(RW, i, rp, P);
         return;
     }
     predict_keep_fluid<T>(i - nw, F, fstart, g, dt, D, O, skin, rebuild, health, cond, use_cond,
-                          kc);
+                          kc, RS, &P);
 }
 
 // gated re-binning of the predicted state: keys + histogram slots

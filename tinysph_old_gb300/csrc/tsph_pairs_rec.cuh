@@ -66,11 +66,6 @@ template <int CAP, int LIST> struct RecShape {
 };
 typedef RecShape<472, 38> RecStd;
 
-struct PairRec {  // one set of pair records (fluid rows or walls)
-    float2 *t, *y;
-    float4 *v;
-    float *inv;
-};
 
 // Neighbour lists kept between passes (the fused step).  A pass right after
 // a binning (positions exactly as binned) builds every target's list of the
@@ -86,9 +81,13 @@ struct RecStep {
     uint32_t *gen;              // {sorts, sort the lists were built after, -, CTAs done}
     const float2 *lbin;         // cell-relative positions at the binning
     float sig2;                 // squared displacement allowed since the binning
-    float2 *bloc;               // MODE_CORRECT: new cell-relative position (kept cell)
+    // MODE_CORRECT: the new state is written in the kept order (out.r, out.v,
+    // out.rho are the current buffers); these take its cell-relative
+    // positions and the pair records of the next pass
+    float2 *nloc;
+    PairRec nrec;
     uint32_t *need_sort;        // MODE_CORRECT: set when the cells must be rebuilt
-    cudaGraphConditionalHandle cond_sort, cond_copy;
+    cudaGraphConditionalHandle cond_sort;
     int use_cond;
 };
 
@@ -200,13 +199,15 @@ __global__ void __launch_bounds__(kBlock)
 k_pair_records(FluidState<float> F, const uint32_t *__restrict__ fstart, WallState<float> Wl,
                int nw, Grid g, Phys<float> P, PairRec RF, PairRec RW, int rec_blocks,
                const uint32_t *__restrict__ wstart, int nchunks, int cap,
-               WinRec *__restrict__ table, int *__restrict__ nwin, uint32_t *__restrict__ gen) {
+               WinRec *__restrict__ table, int *__restrict__ nwin, uint32_t *__restrict__ gen,
+               const uint32_t *__restrict__ gate, int force_table) {
     pdl_enter();
+    if (gated_off(gate)) return;
     if ((int)blockIdx.x >= rec_blocks) {
-        // the table is rebuilt only for a pass that builds the lists (a sort
-        // happened since they were built); otherwise it still holds
+        // the table follows the cells: rebuilt after a sort (the lists are
+        // then stale until a pass builds them), or on request
         const int c = ((int)blockIdx.x - rec_blocks) * blockDim.x + threadIdx.x;
-        if (c < nchunks && __ldg(gen) != __ldg(gen + 1))
+        if (c < nchunks && (force_table || __ldg(gen) != __ldg(gen + 1)))
             rec_window_table(c, cap, F, fstart, wstart, g, table, nwin);
         return;
     }
@@ -386,7 +387,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
     const int nw = __ldg(nwin + blockIdx.x);
     // this pass builds and stores the lists when a sort happened since they
     // were built (the last CTA to finish records the sort they are built after)
-    const bool build = __ldg(S.gen) != __ldg(S.gen + 1);
+    const bool build = MODE == MODE_LISTS || __ldg(S.gen) != __ldg(S.gen + 1);
     auto finish = [&]() {
         if (tid == 0) {
             __threadfence();
@@ -510,7 +511,8 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                     // the stored list (built after the last binning)
                     const int c = (int)sm.cnt[col_i];
                     if (c == 255) global = true;
-                    else rec_eval(sm, lst, c, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K, acc);
+                    else if (MODE != MODE_LISTS)
+                        rec_eval(sm, lst, c, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K, acc);
                 } else {
                     // phase 1 at radius Kb (2h + 2 sigma), the list stored
                     // segment by segment as it is summed
@@ -553,8 +555,9 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                             if (__any_sync(amask, wend - w < (pe - pl) * kRecT)) {
                                 const int cnt = (int)((w - lst) / kRecT);
                                 rec_store(gl, lst, cnt, SH::list, gpos, over);
-                                rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K,
-                                         acc);
+                                if (MODE != MODE_LISTS)
+                                    rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf,
+                                             K, acc);
                                 w = lst;
                             }
                             w = rec_scan(sm.t, pl, pe, xd, ya, Kb.four_h2, sgi == 3, (uint32_t)d, w);
@@ -562,13 +565,15 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                     }
                     const int cnt = (int)((w - lst) / kRecT);
                     rec_store(gl, lst, cnt, SH::list, gpos, over);
-                    rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K, acc);
+                    if (MODE != MODE_LISTS)
+                        rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K, acc);
                     S.gcnt[t0 + col_i] = over ? (uint8_t)255 : (uint8_t)gpos;
                 }
             }
         } else if (active && build) {
             S.gcnt[t0 + col_i] = (uint8_t)255;  // no list: this window takes the global path
         }
+        if (MODE == MODE_LISTS) continue;  // lists stored: nothing to sum
         if (active && global) {
             // neighbour block too large for shared memory, a chunk with more
             // windows than the table holds, or a list that did not fit: every
@@ -627,20 +632,25 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 }
                 if (!(nv.x == nv.x) || !(nv.y == nv.y) || !(s_new == s_new))
                     atomicOr(health, kHealthNan);
+                // the new cell for a sort (its histogram slot is taken by the
+                // sort itself, which runs only when some particle needs it)
                 out.key[i] = nk;
-                if (!listed) out.slot[i] = atomicAdd(out.counts + nk, 1u);
-                // the new position relative to the kept cell, and whether the
-                // cells must be rebuilt before the next pass
+                (void)listed;
+                // the new position relative to the kept cell, the pair
+                // records of the next pass, and whether the cells must be
+                // rebuilt before it
                 const float2 ln = make_float2((float)(rn.x - __ldg(g.ax.org + cxa)),
                                               (float)(rn.y - __ldg(g.ay.org + cy)));
-                S.bloc[i] = ln;
+                S.nloc[i] = ln;
+                const float ib = rcp_approx(P.rho0 + s_new);
+                S.nrec.t[i] = make_float2(ln.x, fmaf((float)cy, khf, ln.y));
+                S.nrec.y[i] = make_float2(ln.y, (float)cy);
+                S.nrec.v[i] = make_float4(nv.x, nv.y, s_new, eos(s_new, P) * ib);
+                S.nrec.inv[i] = ib;
                 const float ex = ln.x - lb.x, ey = ln.y - lb.y;
                 if (resort || !(fmaf(ex, ex, ey * ey) <= S.sig2)) {
                     *S.need_sort = 1u;
-                    if (S.use_cond) {
-                        cudaGraphSetConditional(S.cond_sort, 1u);
-                        cudaGraphSetConditional(S.cond_copy, 0u);
-                    }
+                    if (S.use_cond) cudaGraphSetConditional(S.cond_sort, 1u);
                 }
             }
         }
@@ -648,26 +658,57 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
     finish();
 }
 
-// the corrector's output, in the kept order (no re-binning this step): new
-// r, v, rho and cell-relative positions into the current state; the
-// histogram slots the corrector counted are cleared
+// the search fields (t, y) of the fluid records at the binning positions
+// (lbin): lists rebuilt from them are the lists that were built right after
+// that binning (a restored state whose lists were overwritten since)
+static __global__ void __launch_bounds__(kBlock)
+k_lbin_records(PairRec R, const float2 *__restrict__ lbin, const uint32_t *__restrict__ key,
+               const uint32_t *__restrict__ fstart, Grid g) {
+    pdl_enter();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_live(fstart, g.ncells)) return;
+    const float2 l = lbin[i];
+    const uint32_t k = key[i];
+    const int cx = (int)(k / (uint32_t)g.ncy);
+    const float row = (float)((int)k - cx * g.ncy);
+    R.t[i] = make_float2(l.x, fmaf(row, g.khf, l.y));
+    R.y[i] = make_float2(l.y, row);
+}
+
+// the sort of a kept-order state (when some particle left its kept cell's
+// reach, or the domain): the histogram slots of the corrector's new cells,
+// except the erase candidates, whose slots the erase takes
 template <typename T>
 __global__ void __launch_bounds__(kBlock)
-k_copy_kept(FluidState<T> D, const double2 *__restrict__ br, const typename V2<T>::t *__restrict__ bv,
-            const T *__restrict__ brho, const float2 *__restrict__ bloc,
-            const uint32_t *__restrict__ bkey, uint32_t *__restrict__ counts,
-            const uint32_t *__restrict__ fstart, int ncells, const uint32_t *__restrict__ skip,
+k_hist_kept(FluidState<T> X, const uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
+            uint32_t *__restrict__ counts, const uint8_t *__restrict__ cand,
+            const uint32_t *__restrict__ fstart, int ncells, const uint32_t *__restrict__ gate,
             uint32_t *__restrict__ runs) {
     pdl_enter();
-    if (__ldg(skip) != 0u) return;
+    if (gated_off(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0 && runs) atomicAdd(runs, 1u);
     if (i >= n_live(fstart, ncells)) return;
-    D.r[i] = br[i];
-    D.v[i] = bv[i];
-    D.rho[i] = brho[i];
-    D.loc[i] = bloc[i];
-    counts[bkey[i]] = 0u;
+    if (cand[X.id[i]]) return;
+    slot[i] = atomicAdd(counts + key[i], 1u);
+}
+
+// the sorted rows (r, v, rho, id, key, loc of S) back into the buffers the
+// graph reads (D)
+template <typename T>
+__global__ void __launch_bounds__(kBlock)
+k_copy_rows(FluidState<T> D, const FluidState<T> S, const uint32_t *__restrict__ fstart,
+            int ncells, const uint32_t *__restrict__ gate) {
+    pdl_enter();
+    if (gated_off(gate)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= (int)__ldg(fstart + ncells + 1)) return;
+    D.r[i] = S.r[i];
+    D.v[i] = S.v[i];
+    D.rho[i] = S.rho[i];
+    D.id[i] = S.id[i];
+    D.key[i] = S.key[i];
+    D.loc[i] = S.loc[i];
 }
 
 }  // namespace tsph

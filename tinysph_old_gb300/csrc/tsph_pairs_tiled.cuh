@@ -53,12 +53,6 @@ template <class SH> struct TileSmem {
     uint16_t list[SH::list * kTileT];
 };
 
-__device__ __forceinline__ float rcp_approx(float x) {
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-}
-
 // Pair terms with the constant factors (m, bwen/h, k_psi) applied once per
 // target by the caller: a = -m bwen_h sum dr w^3 (P_a I_b + P_b I_a + Pi),
 // drho = m bwen_h (sum w^3 dr.dv - k_psi sum psi r^2 w^3 I_b).
@@ -450,7 +444,8 @@ constexpr int kMdbcLanes = 8;
 __device__ __forceinline__ void mdbc_wall(int gid, const WallState<float> &Wl, int nw,
                                            const uint32_t *__restrict__ fstart,
                                            const FluidState<float> &F, const Grid &g,
-                                           const Phys<float> &P, bool predict, float dt) {
+                                           const Phys<float> &P, bool predict, float dt,
+                                           const PairRec &RW) {
     const int w = gid / kMdbcLanes, sub = gid % kMdbcLanes;
     const bool valid = w < nw;
     float s[12];
@@ -585,7 +580,9 @@ __device__ __forceinline__ void mdbc_wall(int gid, const WallState<float> &Wl, i
     const float rw = (float)dens;
     if (predict) {
         Wl.rho_o[w] = rw;
-        Wl.rho[w] = rw + Wl.drho[w] * dt * 0.5f;
+        const float rp = rw + Wl.drho[w] * dt * 0.5f;
+        Wl.rho[w] = rp;
+        if (RW.v) wall_record(RW, w, rp, P);
     } else {
         Wl.rho[w] = rw;
     }
@@ -595,7 +592,8 @@ static __global__ void __launch_bounds__(kBlock)
 k_mdbc_f32(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidState<float> F,
             Grid g, Phys<float> P) {
     pdl_enter();
-    mdbc_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, false, 0.f);
+    mdbc_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, false, 0.f,
+              PairRec{});
 }
 
 // mDBC and the predictor of a step in one launch: the first nbm blocks
@@ -609,14 +607,14 @@ k_mdbc_f32_predict(WallState<float> Wl, int nw, int nbm, const uint32_t *__restr
                 FluidState<float> F, Grid g, Phys<float> P, float dt, FluidState<float> D,
                 OldState<float> O, float skin, uint32_t *__restrict__ rebuild,
                 uint32_t *__restrict__ health, cudaGraphConditionalHandle cond, int use_cond,
-                KeepCells kc) {
+                KeepCells kc, PairRec RS, PairRec RW) {
     pdl_enter();
     if ((int)blockIdx.x < nbm) {
-        mdbc_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, true, dt);
+        mdbc_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, true, dt, RW);
         return;
     }
     predict_keep_fluid<float>(((int)blockIdx.x - nbm) * blockDim.x + threadIdx.x, F, fstart, g, dt,
-                              D, O, skin, rebuild, health, cond, use_cond, kc);
+                              D, O, skin, rebuild, health, cond, use_cond, kc, RS, &P);
 }
 
 }  // namespace tsph

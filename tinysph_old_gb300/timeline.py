@@ -79,7 +79,9 @@ def split(records, steps: int, prefix: str = "k_"):
     busy = 0.0
     last_end = None
     for name, s, e, _ in records:
-        if not name.startswith(prefix):
+        # kernels of a conditional node whose body did not run come with no
+        # timestamps
+        if not name.startswith(prefix) or s == 0:
             continue
         d = by.setdefault(name, {"us": 0.0, "exclusive_us": 0.0, "launches": 0})
         d["us"] += (e - s) * 1e-3
