@@ -860,26 +860,39 @@ def main():
         inst = pk["warp_inst_per_particle"] * nfluid
         issue = inst / (pair_avg_us * 1e-6) / (SM_COUNT * 4 * sm_mhz * 1e6)
 
-    # ---- e2e through the C ABI with pinned host buffers: each step uploads
-    # its input state (r, v, rho) from pinned host memory, re-bins, steps and
-    # reads its result back into pinned host memory; the result's copy runs
-    # on a copy stream beside the next step's upload and kernels
+    # ---- e2e through the C ABI with pinned host buffers: each step takes its
+    # input state (r, v, rho) from pinned host memory, re-bins, steps and
+    # reads its result back into pinned host memory.  The copies run on copy
+    # streams beside the kernels: the next step's input is staged while this
+    # step computes (tsph_upload_async, applied by tsph_particle_to_cell) and
+    # this step's result is read back while the next one computes
     # (tsph_download_async / tsph_download_wait)
     hr = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
     hv = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
     hrho = torch.empty((n,), dtype=torch.float64, pin_memory=True)
+    ha = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+    hdrho = torch.empty((n,), dtype=torch.float64, pin_memory=True)
     outs = [tuple(torch.empty_like(t, pin_memory=True) for t in (hr, hv, hrho))
             for _ in range(2)]
+    # a step's whole input: r, v, rho and the last forces pass's a, drho (the
+    # predictor's rates); its result read back: r, v, rho
+    mask_in = sph.F_R | sph.F_V | sph.F_A | sph.F_RHO | sph.F_DRHO
     mask = sph.F_R | sph.F_V | sph.F_RHO
-    s.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+    inp = dict(r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr(), a=ha.data_ptr(),
+               drho=hdrho.data_ptr())
+    s.download_ptrs(mask_in, **inp)
+
+    def stage():
+        s.upload_async(mask_in, **inp)
 
     def e2e_step(k):
         o = outs[k % 2]
-        s.upload_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
-        s.particle_to_cell()
+        s.particle_to_cell()  # applies this step's staged input
         s.step(model, dt, 1)
+        stage()  # the next step's input, beside this step's kernels
         s.download_async(mask, r=o[0].data_ptr(), v=o[1].data_ptr(), rho=o[2].data_ptr())
 
+    stage()
     for k in range(2):  # warm
         e2e_step(k)
     s.download_wait()
@@ -889,9 +902,13 @@ def main():
         e2e_step(k)
     s.download_wait()
     e2e_s = time.perf_counter() - t0
+    # the input staged by the last step, stepped once more synchronously: the
+    # results read back equal it (every e2e step starts from the same input)
+    s.particle_to_cell()
+    s.step(model, dt, 1)
     e2e_value = world * n * args.e2e_steps / e2e_s
+    xfer_in = n * (16 + 16 + 16 + 8 + 8)
     xfer = n * (16 + 16 + 8)
-    # the result read back equals the state the step leaves on the device
     ref_after = s.download()
     e2e_ok = bool(np.array_equal(outs[(args.e2e_steps - 1) % 2][0].numpy(), ref_after["r"]))
 
@@ -923,10 +940,11 @@ def main():
                        "l2": "flushed (256 MB write) between timed steps",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s",
-                    "h2d_bytes_per_step": xfer, "d2h_bytes_per_step": xfer,
-                    "path": "tsph_upload(r,v,rho) + tsph_particle_to_cell + tsph_step(1) + "
-                            "tsph_download_async(r,v,rho) (waited one step later), pinned "
-                            "host buffers",
+                    "h2d_bytes_per_step": xfer_in, "d2h_bytes_per_step": xfer,
+                    "path": "tsph_upload_async(r,v,a,rho,drho) (staged during the previous "
+                            "step) + tsph_particle_to_cell + tsph_step(1) + "
+                            "tsph_download_async(r,v,rho) (waited one step later), pinned host "
+                            "buffers",
                     "result_matches_device_state": e2e_ok},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": pk.get("dram_bytes_per_launch"),

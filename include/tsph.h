@@ -53,6 +53,9 @@ enum {
 /* a pipelined kernel gave up waiting for its own staging pipeline (a bounded
  * wait ran out; the step's results are not valid) */
 #define TSPH_HEALTH_STALL 0x10u
+/* a staged upload (tsph_upload_async) was not applied: some particle index is
+ * no longer live (erased), so its rows do not map one to one onto the state */
+#define TSPH_HEALTH_UPLOAD 0x20u
 
 /* particle types, src/SPH_defs.h:44-48 (fluid = 0, wall = 1) */
 enum { TSPH_FLUID = 0, TSPH_WALL = 1 };
@@ -250,6 +253,18 @@ int tsph_upload(tsph_system *s, int fields, const tsph_host_state *in);
  * synchronously (its rows are compacted on the host). */
 int tsph_download_async(tsph_system *s, int fields, const tsph_host_state *out);
 int tsph_download_wait(tsph_system *s);
+/* Staged upload (no counterpart in the reference): the host-to-device copies
+ * of r, v, a, rho, drho and p (other fields: TSPH_ERR_ARG) start on a copy
+ * stream of their own, beside the work already enqueued (a step in flight),
+ * and the call returns; the next tsph_particle_to_cell applies them and bins
+ * the new state.  Between the two, only tsph_download_async / _wait and
+ * tsph_health may be called (tsph_download and tsph_upload return
+ * TSPH_ERR_STATE; calls that need cell lists find them stale).  Every
+ * particle index must still be live (no erased particles: the rows are taken
+ * as indices 0..n-1); otherwise the upload is dropped and TSPH_HEALTH_UPLOAD
+ * is raised.  The host buffers (pinned for a true overlap) must stay valid
+ * until tsph_particle_to_cell returns. */
+int tsph_upload_async(tsph_system *s, int fields, const tsph_host_state *in);
 /* wait for the system's stream */
 int tsph_sync(tsph_system *s);
 /* device health word (TSPH_HEALTH_*), optionally cleared */

@@ -70,3 +70,75 @@ def test_download_async_with_erased_particles_and_bad_fields(gpu_tsph):
     assert np.array_equal(out_r, want["r"]) and np.array_equal(out_p, want["p"])
     with pytest.raises(gpu_tsph.TsphError):
         s.download_async(gpu_tsph.F_INDEX, index=np.zeros(n, dtype=np.int32).ctypes.data)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_staged_upload_matches_the_synchronous_one(gpu_tsph, precision):
+    """tsph_upload_async + tsph_particle_to_cell leaves the state that
+    tsph_upload + tsph_particle_to_cell leaves, also when the upload is
+    staged while a step is in flight and the previous result is still being
+    read back; between staging and binning only downloads of the
+    asynchronous kind are accepted."""
+    torch = pytest.importorskip("torch")
+    case = cases.dam_break_mdbc(dp=0.01)
+    a = gpu_tsph.ParticleSystem.from_case(case, precision)
+    b = gpu_tsph.ParticleSystem.from_case(case, precision)
+    if precision == "fp32":
+        a.set_tile_shape(2)
+        b.set_tile_shape(2)
+    n = a.np
+    # a step's whole input: positions, velocities, densities and the rates of
+    # the last forces pass (the predictor's a, drho)
+    mask = gpu_tsph.F_R | gpu_tsph.F_V | gpu_tsph.F_A | gpu_tsph.F_RHO | gpu_tsph.F_DRHO
+    a.step(case.wall_model, case.dt, 5)
+    inp = _buffers(n, torch) + tuple(torch.empty(sh, dtype=torch.float64, pin_memory=True)
+                                     for sh in ((n, 2), (n,)))
+    ptrs = dict(r=inp[0].data_ptr(), v=inp[1].data_ptr(), rho=inp[2].data_ptr(),
+                a=inp[3].data_ptr(), drho=inp[4].data_ptr())
+    a.download_ptrs(mask, **ptrs)
+    # reference: synchronous upload of the same state, then the same steps
+    b.upload_ptrs(mask, **ptrs)
+    b.particle_to_cell()
+    b.step(case.wall_model, case.dt, 3)
+    want = b.download()
+    # pipelined: stage the upload while a's steps run, read a's result back
+    outs = [_buffers(n, torch) for _ in range(2)]
+    a.step(case.wall_model, case.dt, 2)
+    a.upload_async(mask, **ptrs)
+    o = outs[0]
+    m3 = gpu_tsph.F_R | gpu_tsph.F_V | gpu_tsph.F_RHO
+    a.download_async(m3, r=o[0].data_ptr(), v=o[1].data_ptr(), rho=o[2].data_ptr())
+    with pytest.raises(gpu_tsph.TsphError):
+        a.download()
+    with pytest.raises(gpu_tsph.TsphError):
+        a.upload_ptrs(mask, **ptrs)
+    with pytest.raises(gpu_tsph.TsphError):
+        a.step(case.wall_model, case.dt, 1)
+    a.download_wait()
+    a.particle_to_cell()
+    a.step(case.wall_model, case.dt, 3)
+    got = a.download()
+    assert a.health() == 0
+    for f in ("r", "v", "rho", "p", "a"):
+        assert np.array_equal(got[f], want[f]), f
+
+
+@pytest.mark.gpu
+def test_staged_upload_with_erased_particles_is_dropped(gpu_tsph):
+    case = cases.dam_break_mdbc(dp=0.02)
+    s = gpu_tsph.ParticleSystem.from_case(case, "fp32")
+    st = s.download()
+    r = st["r"].copy()
+    r[np.flatnonzero(st["type"] == 0)[3]] = (0.5, case.domain[3] + 0.5)
+    s.upload(r=r)
+    assert s.remove_out_of_domain() == 1
+    s.particle_to_cell()
+    before = s.download()
+    n = s.np
+    r2 = np.ascontiguousarray(before["r"] + 1e-4)
+    s.upload_async(gpu_tsph.F_R, r=r2.ctypes.data)
+    s.particle_to_cell()
+    assert s.health() & gpu_tsph.HEALTH_UPLOAD
+    after = s.download()
+    assert np.array_equal(after["r"], before["r"]) and n == s.np

@@ -445,6 +445,14 @@ int tsph_download_async(tsph_system *s, int fields, const tsph_host_state *out) 
     return TSPH_OK;
 }
 
+int tsph_upload_async(tsph_system *s, int fields, const tsph_host_state *in) {
+    NEED(s);
+    if (!in) return fail(TSPH_ERR_ARG, "null input");
+    ENGINE(s);
+    RUN(s->eng->upload_async(fields, in->r, in->v, in->a, in->rho, in->drho, in->p, err_));
+    return TSPH_OK;
+}
+
 int tsph_download_wait(tsph_system *s) {
     NEED(s);
     ENGINE(s);

@@ -94,6 +94,12 @@ template <typename T> class Engine final : public EngineBase {
     cudaStream_t cs_ = nullptr;
     cudaEvent_t ev_x_ = nullptr, ev_d_ = nullptr;
     bool d_pending_ = false;
+    // staged upload: host-to-device copies into S_ on their own stream,
+    // applied by the next particle_to_cell
+    cudaStream_t cu_ = nullptr;
+    cudaEvent_t ev_up_ = nullptr, ev_imp_ = nullptr;
+    bool up_pending_ = false;
+    int up_mask_ = 0;
     double *dtot_ = nullptr;
     long long *bx_ = nullptr, *by_ = nullptr;
     double *ox_ = nullptr, *oy_ = nullptr;
@@ -314,7 +320,7 @@ template <typename T> class Engine final : public EngineBase {
                 for (int k = 0; k < kShapes; k++) us[k] = 0;
             return 0;
         } else {
-            if (!cells_) {
+            if (!cells_ok()) {
                 err = "cell lists are stale: call tsph_particle_to_cell first";
                 return 3;
             }
@@ -380,7 +386,7 @@ template <typename T> class Engine final : public EngineBase {
     int export_graph(int K, int cap, double2 *pos, float2 *vel, float *srho, float *wall,
                      int32_t *id, int32_t *deg, int32_t *nbr, float2 *acc, float *rate,
                      int *n_nodes, int *n_wall, std::string &err) override {
-        if (!cells_) {
+        if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
         }
@@ -416,7 +422,7 @@ template <typename T> class Engine final : public EngineBase {
 
     int apply_update(const float *y, double su, double ss, double kdt, bool add_rates,
                      bool zero_momentum, int phase, std::string &err) override {
-        if (!exported_ || !cells_) {
+        if (!exported_ || !cells_ok()) {
             err = "apply_update needs the order of the last export_graph (no re-binning since)";
             return 3;
         }
@@ -457,7 +463,7 @@ template <typename T> class Engine final : public EngineBase {
             err = "no surrogate window was applied";
             return 3;
         }
-        if (!cells_) {
+        if (!cells_ok()) {
             err = "cell lists are stale: the check follows a forces pass at the window's end";
             return 3;
         }
@@ -1032,6 +1038,10 @@ template <typename T> class Engine final : public EngineBase {
         if (cs_) cudaStreamDestroy(cs_);
         if (ev_x_) cudaEventDestroy(ev_x_);
         if (ev_d_) cudaEventDestroy(ev_d_);
+        if (cu_) cudaStreamSynchronize(cu_);  // a staged upload's copies
+        if (cu_) cudaStreamDestroy(cu_);
+        if (ev_up_) cudaEventDestroy(ev_up_);
+        if (ev_imp_) cudaEventDestroy(ev_imp_);
         for (auto &g : graphs_) cudaGraphExecDestroy(g.second);
         for (auto &m : marks_) {
             cudaEventDestroy(m.a);
@@ -1355,6 +1365,7 @@ template <typename T> class Engine final : public EngineBase {
 
     int particle_to_cell(std::string &err) override {
         int rc;
+        if ((rc = apply_staged_upload(err))) return rc;
         if ((rc = zero_counts(err))) return rc;
         const int *nptr = reinterpret_cast<const int *>(fstart_ + ncells_);
         if ((rc = launch(CAT_SORT, k_bin_keep_dead, blocks_for(nf_), kBlock, err,
@@ -1389,7 +1400,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int bt_density(std::string &err) override {
-        if (!cells_) {
+        if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
         }
@@ -1399,7 +1410,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int mdbc_density(std::string &err) override {
-        if (!cells_) {
+        if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
         }
@@ -1409,7 +1420,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int compute_forces(int model, std::string &err) override {
-        if (!cells_) {
+        if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
         }
@@ -1490,7 +1501,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int step(int model, double dt, int nsteps, std::string &err) override {
-        if (!cells_) {
+        if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
         }
@@ -1580,7 +1591,7 @@ template <typename T> class Engine final : public EngineBase {
         TSPH_CK(cudaMemcpyAsync(&nl, fstart_ + ncells_, 4, cudaMemcpyDeviceToHost, st_));
         TSPH_CK(cudaStreamSynchronize(st_));
         // particles marked by tsph_remove_out_of_domain but not yet re-binned
-        if (!cells_) {
+        if (!cells_ok()) {
             std::vector<uint32_t> key(nl);
             if (nl) TSPH_CK(cudaMemcpy(key.data(), F_.key, 4 * (size_t)nl, cudaMemcpyDeviceToHost));
             for (uint32_t k : key) rm += (k == (uint32_t)ncells_);
@@ -1641,6 +1652,10 @@ template <typename T> class Engine final : public EngineBase {
 
     int download(int mask, double *r, double *v, double *a, double *rho, double *drho, double *p,
                  int32_t *index, int32_t *type, std::string &err) override {
+        if (up_pending_) {  // its staging set holds the staged upload
+            err = "an upload is staged: call tsph_particle_to_cell first";
+            return 3;
+        }
         TSPH_CK(cudaMemsetAsync(S_.alive, 0, ntot_, st_));
         int rc = launch(CAT_OTHER, k_export<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
                         (const uint32_t *)fstart_, ncells_, W_, nw_, P_.rho0, S_, mask & 63);
@@ -1737,8 +1752,66 @@ template <typename T> class Engine final : public EngineBase {
         return 0;
     }
 
+    int upload_async(int mask, const double *r, const double *v, const double *a,
+                     const double *rho, const double *drho, const double *p,
+                     std::string &err) override {
+        if (mask & ~63) {
+            err = "tsph_upload_async: r, v, a, rho, drho and p only";
+            return 1;
+        }
+        if (zones_on_) {
+            err = "tsph_upload_async: systems with buffer zones use tsph_upload";
+            return 8;
+        }
+        if (up_pending_) {
+            err = "an upload is staged: call tsph_particle_to_cell first";
+            return 3;
+        }
+        if (!cu_) {
+            TSPH_CK(cudaStreamCreateWithFlags(&cu_, cudaStreamNonBlocking));
+            TSPH_CK(cudaEventCreateWithFlags(&ev_up_, cudaEventDisableTiming));
+            TSPH_CK(cudaEventCreateWithFlags(&ev_imp_, cudaEventDisableTiming));
+            TSPH_CK(cudaEventRecord(ev_imp_, st_));
+        }
+        // the staging set is free once the last staged import has read it
+        TSPH_CK(cudaStreamWaitEvent(cu_, ev_imp_, 0));
+        void *dst[6] = {S_.r, S_.v, S_.a, S_.rho, S_.drho, S_.p};
+        const double *src[6] = {r, v, a, rho, drho, p};
+        int m = 0;
+        for (int k = 0; k < 6; k++)
+            if ((mask & (1 << k)) && src[k]) {
+                TSPH_CK(cudaMemcpyAsync(dst[k], src[k], (k < 3 ? 16 : 8) * (size_t)ntot_,
+                                        cudaMemcpyHostToDevice, cu_));
+                m |= 1 << k;
+            }
+        TSPH_CK(cudaEventRecord(ev_up_, cu_));
+        up_pending_ = true;
+        up_mask_ = m;
+        return 0;
+    }
+
+    // cell lists valid and no staged upload waiting for particle_to_cell
+    bool cells_ok() const { return cells_ && !up_pending_; }
+
+    // the staged upload into the state (start of particle_to_cell)
+    int apply_staged_upload(std::string &err) {
+        if (!up_pending_) return 0;
+        up_pending_ = false;
+        TSPH_CK(cudaStreamWaitEvent(st_, ev_up_, 0));
+        int rc = launch(CAT_OTHER, k_import<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                        (const uint32_t *)fstart_, ncells_, W_, nw_, P_.rho0, S_, up_mask_,
+                        ntot_, health_);
+        if (rc) return rc;
+        TSPH_CK(cudaEventRecord(ev_imp_, st_));
+        return 0;
+    }
+
     int upload(int mask, const double *r, const double *v, const double *a, const double *rho,
                const double *drho, const double *p, std::string &err) override {
+        if (up_pending_) {
+            err = "an upload is staged: call tsph_particle_to_cell first";
+            return 3;
+        }
         // every index live (the usual case) needs no alive map
         int rc;
         std::vector<uint8_t> alive;
@@ -1776,7 +1849,8 @@ template <typename T> class Engine final : public EngineBase {
             return rc;
         // walls keep r and v (static); only fluid rows take them
         if ((rc = launch(CAT_OTHER, k_import<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
-                         (const uint32_t *)fstart_, ncells_, W_, nw_, P_.rho0, S_, mask & 63)))
+                         (const uint32_t *)fstart_, ncells_, W_, nw_, P_.rho0, S_, mask & 63, -1,
+                         health_)))
             return rc;
         TSPH_CK(cudaStreamSynchronize(st_));
         if (mask & 1) cells_ = false;
@@ -1784,7 +1858,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int get_cells(int32_t *cell_start, int32_t *cell_list, std::string &err) override {
-        if (!cells_) {
+        if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
         }
@@ -1820,7 +1894,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int pair_digest(int32_t *count, int64_t *sum, int32_t *xr, std::string &err) override {
-        if (!cells_) {
+        if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
         }
@@ -1916,7 +1990,7 @@ template <typename T> class Engine final : public EngineBase {
 
     int water_level(int n, const double *x, const double *y0, const int32_t *inverse, double *out,
                     std::string &err) override {
-        if (!cells_) {
+        if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
         }
@@ -1976,7 +2050,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int point_fields(int n, const double *xy, double *out, std::string &err) override {
-        if (!cells_) {
+        if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
         }

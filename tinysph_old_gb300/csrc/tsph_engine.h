@@ -59,6 +59,9 @@ class EngineBase {
     virtual int download_async(int mask, double *r, double *v, double *a, double *rho,
                                double *drho, double *p, std::string &err) = 0;
     virtual int download_wait(std::string &err) = 0;
+    virtual int upload_async(int mask, const double *r, const double *v, const double *a,
+                             const double *rho, const double *drho, const double *p,
+                             std::string &err) = 0;
     virtual int upload(int mask, const double *r, const double *v, const double *a,
                        const double *rho, const double *drho, const double *p,
                        std::string &err) = 0;

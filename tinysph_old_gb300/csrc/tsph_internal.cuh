@@ -188,6 +188,7 @@ template <typename T> __device__ __forceinline__ T eos(T stored, const Phys<T> &
 
 // device health word bits (mirror TSPH_HEALTH_* in tsph.h)
 constexpr uint32_t kHealthNan = 0x1u, kHealthDensity = 0x2u, kHealthEscaped = 0x4u,
-                   kHealthRemoved = 0x8u, kHealthStall = 0x10u;
+                   kHealthRemoved = 0x8u, kHealthStall = 0x10u,
+                   kHealthUpload = 0x20u;
 
 }  // namespace tsph

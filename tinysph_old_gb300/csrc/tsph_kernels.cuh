@@ -1569,11 +1569,18 @@ static __global__ void __launch_bounds__(kBlock) k_count_alive(const uint8_t *__
     }
 }
 
+// `ntot` >= 0: a staged upload whose rows are the indices 0..ntot-1; applied
+// only when every index is live, else TSPH_HEALTH_UPLOAD
 template <typename T>
 __global__ void k_import(FluidState<T> F, const uint32_t *__restrict__ fstart, int ncells,
-                         WallState<T> Wl, int nw, T rho0, Staging S, int mask) {
+                         WallState<T> Wl, int nw, T rho0, Staging S, int mask, int ntot,
+                         uint32_t *__restrict__ health) {
     pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ntot >= 0 && n_live(fstart, ncells) + nw != ntot) {
+        if (i == 0) atomicOr(health, kHealthUpload);
+        return;
+    }
     if (i < nw) {
         const uint32_t id = Wl.id[i];
         if (mask & 8) Wl.rho[i] = rho_stored_from_full<T>(S.rho[id], (double)rho0);

@@ -28,6 +28,7 @@ PREC_FP32, PREC_FP64 = 0, 1
 F_R, F_V, F_A, F_RHO, F_DRHO, F_P, F_INDEX, F_TYPE = (1 << k for k in range(8))
 F_ALL = F_R | F_V | F_A | F_RHO | F_DRHO | F_P | F_INDEX | F_TYPE
 HEALTH_NAN, HEALTH_DENSITY, HEALTH_ESCAPED, HEALTH_REMOVED = 1, 2, 4, 8
+HEALTH_STALL, HEALTH_UPLOAD = 0x10, 0x20
 
 # the C entry points declared in include/tsph.h
 ABI_SYMBOLS = (
@@ -39,7 +40,7 @@ ABI_SYMBOLS = (
     "tsph_add_buffer_zone", "tsph_set_zone_capacity", "tsph_bz_inlet", "tsph_bz_outlet",
     "tsph_compute_forces", "tsph_symplectic_predictor", "tsph_symplectic_corrector",
     "tsph_remove_out_of_domain", "tsph_step", "tsph_download", "tsph_upload", "tsph_sync",
-    "tsph_download_async", "tsph_download_wait",
+    "tsph_download_async", "tsph_download_wait", "tsph_upload_async",
     "tsph_health", "tsph_kernel_launches", "tsph_fluid_totals", "tsph_set_profiling",
     "tsph_get_profile",
     "tsph_water_level", "tsph_point_fields", "tsph_water_front", "tsph_autotune",
@@ -154,6 +155,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_upload.argtypes = [P, I, C.POINTER(_HostState)]
     L.tsph_download_async.argtypes = [P, I, C.POINTER(_HostState)]
     L.tsph_download_wait.argtypes = [P]
+    L.tsph_upload_async.argtypes = [P, I, C.POINTER(_HostState)]
     L.tsph_health.argtypes = [P, C.POINTER(C.c_uint32), I]
     L.tsph_kernel_launches.argtypes = [P, C.POINTER(C.c_longlong), I]
     L.tsph_fluid_totals.argtypes = [P, P]
@@ -436,6 +438,14 @@ class ParticleSystem:
 
     def download_wait(self):
         _check(self._L.tsph_download_wait(self._h))
+
+    def upload_async(self, mask, **ptrs):
+        """Stage an upload from raw host pointers (pinned buffers, kept valid
+        until particle_to_cell, which applies it); r, v, a, rho, drho, p."""
+        hs = _HostState()
+        for k, v in ptrs.items():
+            setattr(hs, k, v)
+        _check(self._L.tsph_upload_async(self._h, int(mask), C.byref(hs)))
 
     def sync(self):
         _check(self._L.tsph_sync(self._h))
