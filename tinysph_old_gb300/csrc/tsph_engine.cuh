@@ -723,8 +723,11 @@ template <typename T> class Engine final : public EngineBase {
             // with its cell-relative positions and the next pass's records
             RecStep S{rec_list_, rec_cnt_, gen_, (const float2 *)lbin_, sig2_, F_.loc, rec_f_,
                       need_sort_, cond_sort, capturing_ ? 1 : 0};
+            // the corrector's old state: F_ itself (the predictor leaves it
+            // in place; the pass overwrites each row after reading it)
+            const OldState<T> OF{F_.r, F_.v, F_.rho};
             return launch(CAT_PAIR, k_pairs_rec<MODE, false, RecStd>, nchunks, kRecT, err, X, fs, ws,
-                          W_, grid_, P_, Krec_, Krec_build_, O_, dt, po, RX, rec_w_,
+                          W_, grid_, P_, Krec_, Krec_build_, OF, dt, po, RX, rec_w_,
                           (const WinRec *)rec_table_, (const int *)rec_nwin_, S, health_);
         } else {
             (void)X;
@@ -797,8 +800,16 @@ template <typename T> class Engine final : public EngineBase {
 
     // re-binning of the predicted state Fs_ (+ old state O_): sort into F_
     // and B, copy back (FP32 fused step, when the skin was exceeded)
-    int rebin_predicted(const uint32_t *gate, std::string &err) {
+    // With `rec` (the fused step over pair records) the old state lives in
+    // F_ itself (the predictor writes no O_): it is copied into O_ to be
+    // carried through the sort and lands back in F_.
+    int rebin_predicted(const uint32_t *gate, T dt, bool rec, std::string &err) {
         int rc;
+        const OldState<T> FO{F_.r, F_.v, F_.rho};
+        if ((rc = launch(CAT_SORT, k_predict_r<T>, blocks_for(nf_), kBlock, err, Fs_,
+                         rec ? FO : O_, O_, (const uint32_t *)fstart_, ncells_, dt, gate,
+                         rec ? 1 : 0)))
+            return rc;
         if ((rc = launch(CAT_SORT, k_bin_gated<T>, blocks_for(nf_), kBlock, err,
                          (const FluidState<T>)Fs_, (const uint32_t *)fstart_, grid_, keyB_, slotB_,
                          counts_, health_, gate, body_ == 1 ? body_runs_ + 1 : (uint32_t *)nullptr)))
@@ -808,7 +819,8 @@ template <typename T> class Engine final : public EngineBase {
             return rc;
         return launch(CAT_SORT, k_copy_back<T>, blocks_for(nf_), kBlock, err,
                       (const FluidState<T>)F_, (const double2 *)Br_, (const T2 *)Bv_,
-                      (const T *)Brho_, (const uint32_t *)fstart_, ncells_, Fs_, O_, gate);
+                      (const T *)Brho_, (const uint32_t *)fstart_, ncells_, Fs_, rec ? FO : O_,
+                      gate);
     }
 
     // during capture: an IF node on `cond` after the current work, its body
@@ -913,7 +925,7 @@ template <typename T> class Engine final : public EngineBase {
                                                       cudaStreamCaptureModeThreadLocal));
                 std::swap(st_, st2_);
                 body_ = 1;
-                rc = rebin_predicted(nullptr, err);
+                rc = rebin_predicted(nullptr, dt, rec, err);
                 if (!rc && rec) rc = pair_records(Fs_, nullptr, false, err);
                 body_ = 0;
                 std::swap(st_, st2_);
@@ -927,7 +939,7 @@ template <typename T> class Engine final : public EngineBase {
                 }
                 TSPH_CK(cudaStreamUpdateCaptureDependencies(st_, &cn, nullptr, 1,
                                                             cudaStreamSetCaptureDependencies));
-            } else if ((rc = rebin_predicted(rebuild_, err)) ||
+            } else if ((rc = rebin_predicted(rebuild_, dt, rec, err)) ||
                        (rec && (rc = pair_records(Fs_, rebuild_, false, err)))) {
                 return rc;
             }

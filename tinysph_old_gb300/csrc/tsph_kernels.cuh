@@ -1357,16 +1357,18 @@ __device__ __forceinline__ void predict_keep_fluid(int f, const FluidState<T> &F
                                                    const Phys<T> *P = nullptr) {
     if (f == 0 && kc.clear) *kc.clear = 0u;
     if (f >= n_live(fstart, g.ncells)) return;
-    const double2 r = F.r[f];
     const auto v = F.v[f];
     const auto a = F.a[f];
     const T s = F.rho[f];
-    O.r[f] = r;
-    O.v[f] = v;
-    O.rho[f] = s;
+    if (!R.t) {  // the corrector over pair records reads the old state from F itself
+        O.r[f] = F.r[f];
+        O.v[f] = v;
+        O.rho[f] = s;
+    }
     const float hdt = (float)dt * 0.5f;
     const float dx = (float)v.x * hdt, dy = (float)v.y * hdt;
-    D.r[f] = make_double2(r.x + (double)dx, r.y + (double)dy);
+    // the predicted FP64 position (r + dx) is formed only by a re-binning
+    // (k_predict_r): the pair passes use the cell-relative position
     typename V2<T>::t nv;
     nv.x = v.x + a.x * dt * T(0.5);
     nv.y = v.y + a.y * dt * T(0.5);
@@ -1449,6 +1451,29 @@ __global__ void k_predict_keep(FluidState<T> F, const uint32_t *__restrict__ fst
     }
     predict_keep_fluid<T>(i - nw, F, fstart, g, dt, D, O, skin, rebuild, health, cond, use_cond,
                           kc, RS, &P);
+}
+
+// the predicted FP64 positions of a re-binning: r_old + (v_old dt/2), with
+// the displacement formed in FP32 exactly as the predictor forms it, from
+// the old state O; with `copy` the old state is also copied into C
+template <typename T>
+__global__ void k_predict_r(FluidState<T> D, OldState<T> O, OldState<T> C,
+                            const uint32_t *__restrict__ fstart, int ncells, T dt,
+                            const uint32_t *__restrict__ gate, int copy) {
+    pdl_enter();
+    if (gated_off(gate)) return;
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= n_live(fstart, ncells)) return;
+    const double2 r = O.r[f];
+    const auto v = O.v[f];
+    const float hdt = (float)dt * 0.5f;
+    const float dx = (float)v.x * hdt, dy = (float)v.y * hdt;
+    D.r[f] = make_double2(r.x + (double)dx, r.y + (double)dy);
+    if (copy) {
+        C.r[f] = r;
+        C.v[f] = v;
+        C.rho[f] = O.rho[f];
+    }
 }
 
 // gated re-binning of the predicted state: keys + histogram slots
