@@ -2,8 +2,9 @@
 its kernels, so the count grows by the same amount per step (the conditional
 re-binning and sort stay off at these speeds: four kernels per FP32 mDBC step
 over pair records with kept lists, mDBC + predictor, two pair passes and the
-wall rows, more with the tiled kernels); the end-of-call equation of state
-adds one per call; reset clears it."""
+wall rows, more with the tiled kernels); the equation of state that brings
+the stored pressure up to date runs once, at the first call that reads the
+state after the steps; reset clears it."""
 
 import pytest
 
@@ -22,5 +23,12 @@ def test_kernel_launch_count_per_graph_step(gpu_tsph):
     c15 = s.kernel_launches(reset=True)
     per_step = (c15 - c5) / 10
     assert per_step == int(per_step) and 4 <= per_step <= 12, (c5, c15)
-    assert c5 == 5 * per_step + 1  # + the equation of state after the call
+    assert c5 == 5 * per_step  # no equation of state between the steps
     assert s.kernel_launches() == 0
+    # a download after steps runs the equation of state once before its own
+    # kernels; a second download finds the pressure up to date
+    s.download()
+    stale = s.kernel_launches(reset=True)
+    s.download()
+    fresh = s.kernel_launches(reset=True)
+    assert stale == fresh + 1, (stale, fresh)

@@ -155,6 +155,26 @@ template <typename T> class Engine final : public EngineBase {
         return e;
     }
 
+    // The state's pressure array after tsph_step.  The step's own passes form
+    // p = EOS(rho) inside their pair records and never read the array, so a
+    // step only marks it out of date; every other entry point first runs the
+    // EOS over the state (TSPH_FRESH_P), so what any call sees or replaces is
+    // the state the reference's step leaves (p = EOS(rho), its step body
+    // :110-111), without an EOS launch per step of a time loop.
+    bool p_stale_ = false;
+    int fresh_p(std::string &err) {
+        if (!p_stale_) return 0;
+        const int rc = launch(CAT_OTHER, k_eos<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
+                              (const uint32_t *)fstart_, ncells_, W_, nw_, P_, health_);
+        if (rc == 0) p_stale_ = false;
+        return rc;
+    }
+#define TSPH_FRESH_P(err)                     \
+    do {                                      \
+        const int rc_p_ = fresh_p(err);       \
+        if (rc_p_) return rc_p_;              \
+    } while (0)
+
     // launch with optional event bracketing for the profile.  Every kernel
     // launched here begins with pdl_enter(), so it may be launched with
     // programmatic stream serialisation: its launch overlaps the previous
@@ -311,6 +331,7 @@ template <typename T> class Engine final : public EngineBase {
     // the median kept; the fastest wins.  FP32 build only.
     static constexpr int kShapes = 3;
     int autotune(int *choice, double *us, std::string &err) override {
+        TSPH_FRESH_P(err);
         // the FP64 build, boundary-integral walls and buffer zones use the
         // per-particle pair kernel: nothing to choose
         if (!std::is_same<T, float>::value || wall_model_ == 2 || zones_on_) {
@@ -386,6 +407,7 @@ template <typename T> class Engine final : public EngineBase {
     int export_graph(int K, int cap, double2 *pos, float2 *vel, float *srho, float *wall,
                      int32_t *id, int32_t *deg, int32_t *nbr, float2 *acc, float *rate,
                      int *n_nodes, int *n_wall, std::string &err) override {
+        TSPH_FRESH_P(err);
         if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
@@ -422,6 +444,7 @@ template <typename T> class Engine final : public EngineBase {
 
     int apply_update(const float *y, double su, double ss, double kdt, bool add_rates,
                      bool zero_momentum, int phase, std::string &err) override {
+        TSPH_FRESH_P(err);
         if (!exported_ || !cells_ok()) {
             err = "apply_update needs the order of the last export_graph (no re-binning since)";
             return 3;
@@ -459,6 +482,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int window_check(double kdt, double out[5], std::string &err) override {
+        TSPH_FRESH_P(err);
         if (!wref_.rho) {
             err = "no surrogate window was applied";
             return 3;
@@ -490,6 +514,7 @@ template <typename T> class Engine final : public EngineBase {
 
     // BZ_Integrate_inlet, src/SPH_buffer_zones.h:10-108
     int bz_inlet(int zone, double dt, std::string &err) override {
+        TSPH_FRESH_P(err);
         if (!zones_on_ || zone < 0 || zone >= (int)zones_.size()) {
             err = "no such buffer zone";
             return 1;
@@ -525,6 +550,7 @@ template <typename T> class Engine final : public EngineBase {
     // BZ_Integrate_outlet, src/SPH_buffer_zones.h:111-206 (x zones; the
     // reference's y branches are empty)
     int bz_outlet(int zone, double dt, std::string &err) override {
+        TSPH_FRESH_P(err);
         (void)dt;
         if (!zones_on_ || zone < 0 || zone >= (int)zones_.size()) {
             err = "no such buffer zone";
@@ -548,6 +574,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int state_save(std::string &err) override {
+        TSPH_FRESH_P(err);
         int rc;
         const size_t n = (size_t)nf_, nw = (size_t)nw_;
         if (!saved_) {
@@ -582,6 +609,7 @@ template <typename T> class Engine final : public EngineBase {
             err = "no saved state";
             return 3;
         }
+        p_stale_ = false;  // the saved pressure was brought up to date by state_save
         copy_state(F_, Fsv_, wsv_, true);
         TSPH_CK(cudaMemcpyAsync(fstart_, fstart_sv_, 4 * ((size_t)ncells_ + 1),
                                 cudaMemcpyDeviceToDevice, st_));
@@ -605,7 +633,7 @@ template <typename T> class Engine final : public EngineBase {
             uint32_t g[4];
             TSPH_CK(cudaMemcpyAsync(g, gen_sv_, 16, cudaMemcpyDeviceToHost, st_));
             TSPH_CK(cudaStreamSynchronize(st_));
-            if (g[0] == g[1] && rec_f_.t && tile_shape_ == 2) {
+            if (g[0] == g[1] && rec_f_.e && tile_shape_ == 2) {
                 if ((rc = launch(CAT_OTHER, k_lbin_records, blocks_for(nf_), kBlock, err, rec_f_,
                                  (const float2 *)lbin_, (const uint32_t *)F_.key,
                                  (const uint32_t *)fstart_, grid_)))
@@ -617,6 +645,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int set_tile_shape(int shape, std::string &err) override {
+        TSPH_FRESH_P(err);
         if (shape < 0 || shape >= kShapes) {
             err = "tile shape must be 0, 1 or 2";
             return 1;
@@ -744,7 +773,7 @@ template <typename T> class Engine final : public EngineBase {
     // records of F_ already formed), for systems whose fused step keeps them
     int build_lists(std::string &err) {
         if constexpr (std::is_same<T, float>::value) {
-            if (!rec_f_.t || tile_shape_ != 2 || skin_ <= 0.f || wall_model_ == 2 || zones_on_)
+            if (!rec_f_.e || tile_shape_ != 2 || skin_ <= 0.f || wall_model_ == 2 || zones_on_)
                 return 0;
             int rc;
             return fluid_pairs_rec<MODE_LISTS>(F_, T(0), PairOut{}, err, 0, false);
@@ -760,7 +789,7 @@ template <typename T> class Engine final : public EngineBase {
     int pair_records(const FluidState<T> &X, const uint32_t *gate, bool force_table,
                      std::string &err) {
         if constexpr (std::is_same<T, float>::value) {
-            if (!rec_f_.t) return 0;
+            if (!rec_f_.e) return 0;
             const PairRec RX = X.r == Fs_.r ? rec_s_ : rec_f_;
             const int nchunks = blocks_for(nf_, kRecT);
             const int rb = blocks_for((long long)nw_ + nf_);
@@ -788,7 +817,10 @@ template <typename T> class Engine final : public EngineBase {
     }
 
   public:
-    int settle_cells(std::string &err) override { return ensure_exact_cells(err); }
+    int settle_cells(std::string &err) override {
+        TSPH_FRESH_P(err);
+        return ensure_exact_cells(err);
+    }
 
   private:
     // the state changed outside the fused step: neighbour lists and binning
@@ -883,8 +915,9 @@ template <typename T> class Engine final : public EngineBase {
             // predictor in the current order; the re-binning runs only when
             // some particle moved more than the skin: in a graph as the body
             // of a conditional node the predictor switches on, otherwise as
-            // kernels gated on rebuild_
-            TSPH_CK(cudaMemsetAsync(rebuild_, 0, 4, st_));
+            // kernels gated on rebuild_ (which only that gating reads: a
+            // graph step needs no memset node for it)
+            if (!capturing_) TSPH_CK(cudaMemsetAsync(rebuild_, 0, 4, st_));
             cudaGraphConditionalHandle cond = 0;
             cudaGraph_t cg = nullptr;
             cudaStreamCaptureStatus cs;
@@ -1173,13 +1206,12 @@ template <typename T> class Engine final : public EngineBase {
         };
         if ((rc = alloc_state(F_)) || (rc = alloc_state(Fs_))) return rc;
         if constexpr (std::is_same<T, float>::value) {
-            // pair records (tile shape 2); four spare records: a window's
-            // copies are widened to 4-record boundaries
+            // pair records (tile shape 2): two 16-byte arrays per state, so
+            // every window copy starts on a 16-byte boundary
             auto alloc_rec = [&](PairRec &R, int n) -> int {
                 int r;
                 const int cap = n + kRecPad;
-                if ((r = alloc(&R.t, cap, err)) || (r = alloc(&R.y, cap, err)) ||
-                    (r = alloc(&R.v, cap, err)) || (r = alloc(&R.inv, cap, err)))
+                if ((r = alloc(&R.e, cap, err)) || (r = alloc(&R.v, cap, err)))
                     return r;
                 return 0;
             };
@@ -1376,6 +1408,7 @@ template <typename T> class Engine final : public EngineBase {
     void invalidate_cells() override { cells_ = false; }
 
     int particle_to_cell(std::string &err) override {
+        TSPH_FRESH_P(err);
         int rc;
         if ((rc = apply_staged_upload(err))) return rc;
         if ((rc = zero_counts(err))) return rc;
@@ -1408,10 +1441,12 @@ template <typename T> class Engine final : public EngineBase {
         int rc = launch(CAT_OTHER, k_eos<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
                         (const uint32_t *)fstart_, ncells_, W_, nw_, P_, health_);
         if (rc) return rc;
+        p_stale_ = false;
         return collect_profile(err);
     }
 
     int bt_density(std::string &err) override {
+        TSPH_FRESH_P(err);
         if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
@@ -1422,6 +1457,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int mdbc_density(std::string &err) override {
+        TSPH_FRESH_P(err);
         if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
@@ -1432,6 +1468,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int compute_forces(int model, std::string &err) override {
+        TSPH_FRESH_P(err);
         if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
@@ -1450,6 +1487,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int predictor(double dt, std::string &err) override {
+        TSPH_FRESH_P(err);
         int rc = launch(CAT_OTHER, k_predict_inplace<T>, blocks_for(nw_ + nf_), kBlock, err, F_, O_,
                         (const uint32_t *)fstart_, ncells_, W_, nw_, (T)dt);
         if (rc) return rc;
@@ -1458,6 +1496,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int corrector(double dt, std::string &err) override {
+        TSPH_FRESH_P(err);
         int rc = launch(CAT_OTHER, k_correct_inplace<T>, blocks_for(nw_ + nf_), kBlock, err, F_, O_,
                         (const uint32_t *)fstart_, ncells_, W_, nw_, (T)dt, P_.rho0);
         if (rc) return rc;
@@ -1469,6 +1508,7 @@ template <typename T> class Engine final : public EngineBase {
     // after an erased one (the fused step's corrector removes every particle
     // outside the box instead)
     int remove_out_of_domain(int *removed, std::string &err) override {
+        TSPH_FRESH_P(err);
         int rc;
         if (!zlive_ && ((rc = alloc(&zlive_, id_cap_, err)) || (rc = alloc(&zcand_, id_cap_, err))))
             return rc;
@@ -1568,10 +1608,9 @@ template <typename T> class Engine final : public EngineBase {
             for (int s = 0; s < nsteps; s++) TSPH_CK(cudaGraphLaunch(it->second, st_));
             launched_ += (long long)nsteps * graph_kernels_[key];
         }
-        // the reference's state after a step holds p = EOS(rho) (step body :110-111)
-        if ((rc = launch(CAT_OTHER, k_eos<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
-                         (const uint32_t *)fstart_, ncells_, W_, nw_, P_, health_)))
-            return rc;
+        // the reference's state after a step holds p = EOS(rho) (step body
+        // :110-111): formed by the next entry point that reads the state
+        p_stale_ = true;
         cells_ = true;
         // with kept lists the cells are those of the last binning, which may
         // be some steps old (every particle within sigma of where it was binned)
@@ -1664,6 +1703,7 @@ template <typename T> class Engine final : public EngineBase {
 
     int download(int mask, double *r, double *v, double *a, double *rho, double *drho, double *p,
                  int32_t *index, int32_t *type, std::string &err) override {
+        TSPH_FRESH_P(err);
         if (up_pending_) {  // its staging set holds the staged upload
             err = "an upload is staged: call tsph_particle_to_cell first";
             return 3;
@@ -1722,6 +1762,7 @@ template <typename T> class Engine final : public EngineBase {
     // path (their rows are compacted on the host).
     int download_async(int mask, double *r, double *v, double *a, double *rho, double *drho,
                        double *p, std::string &err) override {
+        TSPH_FRESH_P(err);
         int rc;
         if (mask & ~63) {
             err = "tsph_download_async: r, v, a, rho, drho and p only";
@@ -1767,6 +1808,8 @@ template <typename T> class Engine final : public EngineBase {
     int upload_async(int mask, const double *r, const double *v, const double *a,
                      const double *rho, const double *drho, const double *p,
                      std::string &err) override {
+        // (only stages copies: the pressure is brought up to date by the
+        // tsph_particle_to_cell that applies them, before it does)
         if (mask & ~63) {
             err = "tsph_upload_async: r, v, a, rho, drho and p only";
             return 1;
@@ -1820,6 +1863,7 @@ template <typename T> class Engine final : public EngineBase {
 
     int upload(int mask, const double *r, const double *v, const double *a, const double *rho,
                const double *drho, const double *p, std::string &err) override {
+        TSPH_FRESH_P(err);
         if (up_pending_) {
             err = "an upload is staged: call tsph_particle_to_cell first";
             return 3;
@@ -1870,6 +1914,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int get_cells(int32_t *cell_start, int32_t *cell_list, std::string &err) override {
+        TSPH_FRESH_P(err);
         if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
@@ -1906,6 +1951,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int pair_digest(int32_t *count, int64_t *sum, int32_t *xr, std::string &err) override {
+        TSPH_FRESH_P(err);
         if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
@@ -1969,6 +2015,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int totals(double out[4], std::string &err) override {
+        TSPH_FRESH_P(err);
         const int nb = blocks_for(nf_);
         int rc = launch(CAT_OTHER, k_totals<T>, nb, kBlock, err, F_, (const uint32_t *)fstart_,
                         ncells_, m64_, dtot_);
@@ -2002,6 +2049,7 @@ template <typename T> class Engine final : public EngineBase {
 
     int water_level(int n, const double *x, const double *y0, const int32_t *inverse, double *out,
                     std::string &err) override {
+        TSPH_FRESH_P(err);
         if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
@@ -2062,6 +2110,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int point_fields(int n, const double *xy, double *out, std::string &err) override {
+        TSPH_FRESH_P(err);
         if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
@@ -2079,6 +2128,7 @@ template <typename T> class Engine final : public EngineBase {
     }
 
     int water_front(double y_max, double *x, std::string &err) override {
+        TSPH_FRESH_P(err);
         int rc;
         if ((rc = probe_scratch(64, err))) return rc;
         unsigned long long *d_best = reinterpret_cast<unsigned long long *>(pr_d_);

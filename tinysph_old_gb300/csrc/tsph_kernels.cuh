@@ -534,18 +534,17 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // inv = 1 / rho.  Written by whichever kernel last changed the row (the
 // predictor, the corrector, the walls' density kernels) or by k_pair_records.
 struct PairRec {
-    float2 *t, *y;
-    float4 *v;
-    float *inv;
+    float4 *e;  // {x - x of the particle's own cell, y - y of that cell, cell row, 1/rho}
+    float4 *v;  // {vx, vy, rho - rho0, p/rho}
 };
 
-// a wall's density-dependent record fields (walls do not move: their t, y
-// stay as k_pair_records wrote them)
+// a wall's density-dependent record fields (walls do not move: the position
+// part of e stays as k_pair_records wrote it)
 __device__ __forceinline__ void wall_record(const PairRec &RW, int w, float s,
                                             const Phys<float> &P) {
     const float ib = rcp_approx(P.rho0 + s);
     RW.v[w] = make_float4(0.f, 0.f, s, eos(s, P) * ib);
-    RW.inv[w] = ib;
+    reinterpret_cast<float *>(RW.e + w)[3] = ib;
 }
 
 // RemoveParticlesOutOfDomain inside the fused step (src/SPH_btdebug.h:4-31).
@@ -1360,7 +1359,7 @@ __device__ __forceinline__ void predict_keep_fluid(int f, const FluidState<T> &F
     const auto v = F.v[f];
     const auto a = F.a[f];
     const T s = F.rho[f];
-    if (!R.t) {  // the corrector over pair records reads the old state from F itself
+    if (!R.e) {  // the corrector over pair records reads the old state from F itself
         O.r[f] = F.r[f];
         O.v[f] = v;
         O.rho[f] = s;
@@ -1382,13 +1381,11 @@ __device__ __forceinline__ void predict_keep_fluid(int f, const FluidState<T> &F
     D.key[f] = key;
     D.id[f] = F.id[f];
     if constexpr (std::is_same<T, float>::value) {
-        if (R.t) {  // the pair records of the predicted state (kept cells)
+        if (R.e) {  // the pair records of the predicted state (kept cells)
             const float row = (float)(key % (uint32_t)g.ncy);
             const float ib = rcp_approx(P->rho0 + sp);
-            R.t[f] = make_float2(ln.x, fmaf(row, g.khf, ln.y));
-            R.y[f] = make_float2(ln.y, row);
+            R.e[f] = make_float4(ln.x, ln.y, row, ib);
             R.v[f] = make_float4(nv.x, nv.y, sp, eos(sp, *P) * ib);
-            R.inv[f] = ib;
         }
     }
     bool rebin;

@@ -3,18 +3,17 @@
 // src/SPH_integration.h:289-309) over pair records staged by bulk copies.
 //
 // Pair records.  Before a pair pass, every particle's neighbour-side values
-// are formed once, in the sorted order, by k_pair_records (four arrays, so a
-// window's record is a few contiguous ranges of each):
-//   rt[i] = {x relative to the particle's own cell, y relative to the grid's
-//            first row (~1e-7 m rounding)}                 support test
-//   ry[i] = {y relative to the particle's own cell, cell row as a float}
+// are formed once, in the sorted order, by k_pair_records (two arrays of
+// 16-byte records, so a window's records are a few contiguous ranges of each,
+// and a neighbour is two 128-bit shared-memory loads):
+//   re[i] = {x relative to the particle's own cell, y relative to that cell,
+//            cell row as a float, 1/rho}
 //   rv[i] = {vx, vy, rho - rho0, p/rho}
-//   ri[i] = 1/rho
-// The support test and the window search use the coarse y of rt (its rounding
-// can only move pairs within ~1e-4 h of r = 2h, where W and dW vanish to
-// ~1e-12 of their scale); the pair terms form dy from the cell-relative y and
-// the exact row difference, and dx from the cell-relative x and the column
-// offset, as precisely as k_pairs_tiled.
+// The support test and the window search use a coarse y in the grid's frame,
+// fmaf(row, kh, y) (~1e-7 m rounding: it can only move pairs within ~1e-4 h
+// of r = 2h, where W and dW vanish to ~1e-12 of their scale); the pair terms
+// form dy from the cell-relative y and the exact row difference, and dx from
+// the cell-relative x and the column offset, as precisely as k_pairs_tiled.
 //
 // Work decomposition: a CTA takes 128 consecutive fluid targets (one thread
 // each) and walks them in windows of at most kRecRows rows of one column.
@@ -44,7 +43,7 @@ namespace tsph {
 
 constexpr int kRecT = 128;    // targets per CTA (one thread each)
 constexpr int kRecRows = 16;  // max target rows per window
-constexpr int kRecPad = 4;    // records per 16 bytes of the narrowest array (ri)
+constexpr int kRecPad = 1;    // records per 16 bytes (every record array is 16 B wide)
 
 constexpr unsigned long long kWaitNs = 4000000000ull;  // bounded mbarrier waits (4 s)
 constexpr int kRecMaxWin = 4;  // windows per chunk in the window table
@@ -64,7 +63,7 @@ struct __align__(16) WinRec {
 template <int CAP, int LIST> struct RecShape {
     static constexpr int cap = CAP, list = LIST;
 };
-typedef RecShape<472, 38> RecStd;
+typedef RecShape<528, 38> RecStd;
 
 
 // Neighbour lists kept between passes (the fused step).  A pass right after
@@ -92,10 +91,8 @@ struct RecStep {
 };
 
 template <class SH> struct RecSmem {
+    float4 e[SH::cap];
     float4 v[SH::cap];
-    float2 t[SH::cap];
-    float2 y[SH::cap];
-    float inv[SH::cap];
     uint16_t list[SH::list * kRecT];
     // fstart / wstart of the staged rows of each column, copied from the
     // 4-aligned index below (col * ncy + rlo); row q of column d is at
@@ -105,7 +102,6 @@ template <class SH> struct RecSmem {
     int oshift[3];
     int base[6];  // staged index of global row j of segment s = base[s] + j
     WinRec win;
-    float offx[4];
     __align__(16) uint8_t cnt[kRecT];  // stored list lengths of the chunk's targets
     unsigned long long bar;
 };
@@ -224,10 +220,8 @@ k_pair_records(FluidState<float> F, const uint32_t *__restrict__ fstart, WallSta
     const int cx = (int)(key / (uint32_t)g.ncy);
     const float row = (float)((int)key - cx * g.ncy);
     const float ib = rcp_approx(P.rho0 + s);
-    (wall ? RW.t : RF.t)[j] = make_float2(l.x, fmaf(row, g.khf, l.y));
-    (wall ? RW.y : RF.y)[j] = make_float2(l.y, row);
+    (wall ? RW.e : RF.e)[j] = make_float4(l.x, l.y, row, ib);
     (wall ? RW.v : RF.v)[j] = make_float4(v.x, v.y, s, p * ib);
-    (wall ? RW.inv : RF.inv)[j] = ib;
 }
 
 // ---------------------------------------------------------------- plumbing
@@ -287,19 +281,24 @@ __device__ __forceinline__ void fence_mbar_init() {
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
 }
 
+// the coarse y of a record in the grid's frame (support test and search)
+__device__ __forceinline__ float rec_ycoarse(const float4 &r, float khf) {
+    return fmaf(r.z, khf, r.y);
+}
+
 // phase 1 over candidates [s, e) of one segment: entry = staged index << 2 |
 // column for every candidate within the test radius (h2 = its square);
 // `excl` (the target's own column) also drops r = 0, the target itself
-__device__ __forceinline__ uint16_t *rec_scan(const float2 *__restrict__ t, int s, int e, float xa,
-                                              float ya, float h2, bool excl, uint32_t col,
-                                              uint16_t *w) {
+__device__ __forceinline__ uint16_t *rec_scan(const float4 *__restrict__ t, int s, int e, float xa,
+                                              float ya, float khf, float h2, bool excl,
+                                              uint32_t col, uint16_t *w) {
     const float lo2 = excl ? 0.f : -1.f;  // kept when lo2 < r2 <= h2
     int j = s;
     uint32_t ent = ((uint32_t)s << 2) | col;
     for (; j + 1 < e; j += 2, ent += 8u) {
-        const float2 l0 = t[j], l1 = t[j + 1];
-        const float dx0 = xa - l0.x, dy0 = ya - l0.y;
-        const float dx1 = xa - l1.x, dy1 = ya - l1.y;
+        const float4 l0 = t[j], l1 = t[j + 1];
+        const float dx0 = xa - l0.x, dy0 = ya - rec_ycoarse(l0, khf);
+        const float dx1 = xa - l1.x, dy1 = ya - rec_ycoarse(l1, khf);
         const float r0 = fmaf(dx0, dx0, dy0 * dy0), r1 = fmaf(dx1, dx1, dy1 * dy1);
         *w = (uint16_t)ent;
         w += (r0 <= h2 && r0 > lo2) ? kRecT : 0;
@@ -307,8 +306,8 @@ __device__ __forceinline__ uint16_t *rec_scan(const float2 *__restrict__ t, int 
         w += (r1 <= h2 && r1 > lo2) ? kRecT : 0;
     }
     if (j < e) {
-        const float2 l = t[j];
-        const float dx = xa - l.x, dy = ya - l.y;
+        const float4 l = t[j];
+        const float dx = xa - l.x, dy = ya - rec_ycoarse(l, khf);
         const float r = fmaf(dx, dx, dy * dy);
         *w = (uint16_t)ent;
         w += (r <= h2 && r > lo2) ? kRecT : 0;
@@ -318,10 +317,11 @@ __device__ __forceinline__ uint16_t *rec_scan(const float2 *__restrict__ t, int 
 
 // first index of [lo, hi) whose coarse y is not below y (ABOVE: above y)
 template <bool ABOVE>
-__device__ __forceinline__ int rec_bound(const float2 *__restrict__ t, int lo, int hi, float y) {
+__device__ __forceinline__ int rec_bound(const float4 *__restrict__ t, int lo, int hi, float y,
+                                         float khf) {
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        const float ym = t[mid].y;
+        const float ym = rec_ycoarse(t[mid], khf);
         if (ABOVE ? !(ym > y) : (ym < y)) lo = mid + 1;
         else hi = mid;
     }
@@ -329,33 +329,37 @@ __device__ __forceinline__ int rec_bound(const float2 *__restrict__ t, int lo, i
 }
 
 // phase 2: the pair terms over list entries [0, cnt)
+// the target's x in the frame of neighbour column code c (0, 1, 2: the
+// column right of, at, left of the target's), by selects instead of a
+// shared-memory table
+__device__ __forceinline__ float rec_xcol(uint32_t c, float xp, float x0, float xm) {
+    return (c & 2u) ? xm : ((c & 1u) ? x0 : xp);
+}
+
 template <class SH>
 __device__ __forceinline__ void rec_eval(const RecSmem<SH> &sm, const uint16_t *lst, int cnt,
                                          float xa, float yca, float rowa, float2 va, float sa,
                                          float Pa, float Ia, float Ra2, float khf,
                                          const TileConst &K, Acc4 &acc) {
+    const float xp = xa + khf, xm = xa - khf;
     int k = 0;
     for (; k + 1 < cnt; k += 2) {
         const uint32_t e0 = lst[k * kRecT], e1 = lst[(k + 1) * kRecT];
         const int j0 = (int)(e0 >> 2), j1 = (int)(e1 >> 2);
-        const float ox0 = sm.offx[e0 & 3u], ox1 = sm.offx[e1 & 3u];
-        const float2 a0 = sm.t[j0], a1 = sm.t[j1];
-        const float2 c0 = sm.y[j0], c1 = sm.y[j1];
+        const float4 a0 = sm.e[j0], a1 = sm.e[j1];
         const float4 v0 = sm.v[j0], v1 = sm.v[j1];
-        const float i0 = sm.inv[j0], i1 = sm.inv[j1];
-        pair_terms<true>((xa + ox0) - a0.x, fmaf(rowa - c0.y, khf, yca - c0.x), va.x - v0.x,
-                         va.y - v0.y, sa, Pa, Ia, Ra2, v0.z, v0.w, i0, K, acc);
-        pair_terms<true>((xa + ox1) - a1.x, fmaf(rowa - c1.y, khf, yca - c1.x), va.x - v1.x,
-                         va.y - v1.y, sa, Pa, Ia, Ra2, v1.z, v1.w, i1, K, acc);
+        pair_terms<true>(rec_xcol(e0, xp, xa, xm) - a0.x, fmaf(rowa - a0.z, khf, yca - a0.y),
+                         va.x - v0.x, va.y - v0.y, sa, Pa, Ia, Ra2, v0.z, v0.w, a0.w, K, acc);
+        pair_terms<true>(rec_xcol(e1, xp, xa, xm) - a1.x, fmaf(rowa - a1.z, khf, yca - a1.y),
+                         va.x - v1.x, va.y - v1.y, sa, Pa, Ia, Ra2, v1.z, v1.w, a1.w, K, acc);
     }
     if (k < cnt) {
         const uint32_t e = lst[k * kRecT];
         const int j = (int)(e >> 2);
-        const float ox = sm.offx[e & 3u];
-        const float2 a = sm.t[j], c = sm.y[j];
+        const float4 a = sm.e[j];
         const float4 v = sm.v[j];
-        pair_terms<true>((xa + ox) - a.x, fmaf(rowa - c.y, khf, yca - c.x), va.x - v.x,
-                         va.y - v.y, sa, Pa, Ia, Ra2, v.z, v.w, sm.inv[j], K, acc);
+        pair_terms<true>(rec_xcol(e, xp, xa, xm) - a.x, fmaf(rowa - a.z, khf, yca - a.y),
+                         va.x - v.x, va.y - v.y, sa, Pa, Ia, Ra2, v.z, v.w, a.w, K, acc);
     }
 }
 
@@ -405,7 +409,6 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
         mbar_init(&sm.bar, 1);
         fence_mbar_init();
     }
-    if (tid < 4) sm.offx[tid] = tid < 3 ? (float)(1 - tid) * khf : 0.f;
     uint32_t parity = 0u;
     for (int wi = 0; wi < nw; wi++) {
         __syncthreads();  // the previous window is finished with shared memory
@@ -416,7 +419,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
             const WinRec R = table[(size_t)blockIdx.x * kRecMaxWin + wi];
             sm.win = R;
             if (R.mode == kRecStaged) {
-                uint32_t bytes = (uint32_t)R.tot * 36u;
+                uint32_t bytes = (uint32_t)R.tot * 32u;
                 int at = 0;
                 for (int sgi = 0; sgi < 6; sgi++) {
                     sm.base[sgi] = at - R.first[sgi];
@@ -438,11 +441,8 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                     if (c > 0) {
                         const bool fl = sgi & 1;
                         const int j = R.first[sgi];
-                        bulk_g2s(&sm.t[at], (fl ? RF.t : RW.t) + j, (uint32_t)c * 8u, &sm.bar);
-                        bulk_g2s(&sm.y[at], (fl ? RF.y : RW.y) + j, (uint32_t)c * 8u, &sm.bar);
+                        bulk_g2s(&sm.e[at], (fl ? RF.e : RW.e) + j, (uint32_t)c * 16u, &sm.bar);
                         bulk_g2s(&sm.v[at], (fl ? RF.v : RW.v) + j, (uint32_t)c * 16u, &sm.bar);
-                        bulk_g2s(&sm.inv[at], (fl ? RF.inv : RW.inv) + j, (uint32_t)c * 4u,
-                                 &sm.bar);
                     }
                     at += c;
                 }
@@ -499,10 +499,10 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
             const bool walls = (sm.win.n[0] | sm.win.n[2] | sm.win.n[4]) != 0;
             if (active) {
                 const int own = sm.base[3] + i;
-                const float2 at_ = sm.t[own], ay_ = sm.y[own];
+                const float4 ae = sm.e[own];
                 const float4 av = sm.v[own];
-                Ia = sm.inv[own];
-                const float xa = at_.x, ya = at_.y, yca = ay_.x, rowa = ay_.y;
+                Ia = ae.w;
+                const float xa = ae.x, ya = rec_ycoarse(ae, khf), yca = ae.y, rowa = ae.z;
                 cy = (int)rowa;
                 const float2 va = make_float2(av.x, av.y);
                 const float sa = av.z, Pa = av.w, Ra2 = K.two_rho0 + sa;
@@ -537,8 +537,8 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                         int lo, e;
                         if (sgi & 1) {
                             const int re = bs + sm.foff[d][qhi + osh];
-                            lo = rec_bound<false>(sm.t, bs + sm.foff[d][qlo + osh], re, ybot);
-                            e = rec_bound<true>(sm.t, lo, re, ytop);
+                            lo = rec_bound<false>(sm.e, bs + sm.foff[d][qlo + osh], re, ybot, khf);
+                            e = rec_bound<true>(sm.e, lo, re, ytop, khf);
                         } else {
                             lo = bs + sm.woff[d][qlo + osh];
                             e = bs + sm.woff[d][qhi + osh];
@@ -560,7 +560,8 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                                              K, acc);
                                 w = lst;
                             }
-                            w = rec_scan(sm.t, pl, pe, xd, ya, Kb.four_h2, sgi == 3, (uint32_t)d, w);
+                            w = rec_scan(sm.e, pl, pe, xd, ya, khf, Kb.four_h2, sgi == 3,
+                                         (uint32_t)d, w);
                         }
                     }
                     const int cnt = (int)((w - lst) / kRecT);
@@ -643,10 +644,8 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                                               (float)(rn.y - __ldg(g.ay.org + cy)));
                 S.nloc[i] = ln;
                 const float ib = rcp_approx(P.rho0 + s_new);
-                S.nrec.t[i] = make_float2(ln.x, fmaf((float)cy, khf, ln.y));
-                S.nrec.y[i] = make_float2(ln.y, (float)cy);
+                S.nrec.e[i] = make_float4(ln.x, ln.y, (float)cy, ib);
                 S.nrec.v[i] = make_float4(nv.x, nv.y, s_new, eos(s_new, P) * ib);
-                S.nrec.inv[i] = ib;
                 const float ex = ln.x - lb.x, ey = ln.y - lb.y;
                 if (resort || !(fmaf(ex, ex, ey * ey) <= S.sig2)) {
                     *S.need_sort = 1u;
@@ -658,9 +657,10 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
     finish();
 }
 
-// the search fields (t, y) of the fluid records at the binning positions
-// (lbin): lists rebuilt from them are the lists that were built right after
-// that binning (a restored state whose lists were overwritten since)
+// the position fields of the fluid records (x, y, row of e) at the binning
+// positions (lbin): lists rebuilt from them are the lists that were built
+// right after that binning (a restored state whose lists were overwritten
+// since)
 static __global__ void __launch_bounds__(kBlock)
 k_lbin_records(PairRec R, const float2 *__restrict__ lbin, const uint32_t *__restrict__ key,
                const uint32_t *__restrict__ fstart, Grid g) {
@@ -671,8 +671,10 @@ k_lbin_records(PairRec R, const float2 *__restrict__ lbin, const uint32_t *__res
     const uint32_t k = key[i];
     const int cx = (int)(k / (uint32_t)g.ncy);
     const float row = (float)((int)k - cx * g.ncy);
-    R.t[i] = make_float2(l.x, fmaf(row, g.khf, l.y));
-    R.y[i] = make_float2(l.y, row);
+    float *const e = reinterpret_cast<float *>(R.e + i);
+    e[0] = l.x;
+    e[1] = l.y;
+    e[2] = row;
 }
 
 // the sort of a kept-order state (when some particle left its kept cell's

@@ -441,6 +441,56 @@ namespace tsph {
 // (rho_o = rho, rho += drho dt/2, as k_predict_keep does for walls).
 constexpr int kMdbcLanes = 8;
 
+// the ghost node's 3x3 moment system of one wall (its 12 FP32 sums) solved
+// in FP64, the density extrapolated to the wall particle and clamped, then
+// the wall's predictor step when `predict`
+__device__ __forceinline__ void solve_mdbc(int w, const float *s, const WallState<float> &Wl,
+                                           const Phys<float> &P, bool predict, float dt,
+                                           const PairRec &RW) {
+    // The reference solves A x = (sum m W, sum m dr_x F, sum m dr_y F) for
+    // x = (rho, grad rho).  With m = V_b rho_b and A's first column
+    // (sum V W, sum V dr_x F, sum V dr_y F), the same system with the
+    // right-hand side sum V (rho_b - rho0) (W, dr_x F, dr_y F) has the
+    // solution (rho - rho0, grad rho): identical in exact arithmetic, ~1000x
+    // smaller numbers (and rounding errors) in FP32.
+    const double rhoWsum = s[0], drhodx = s[1], drhody = s[2];
+    const double a11 = s[3], a12 = s[4], a13 = s[5], a21 = s[6], a22 = s[7], a23 = s[8],
+                 a31 = s[9], a32 = s[10], a33 = s[11];
+    const double det = det3(a11, a12, a13, a21, a22, a23, a31, a32, a33);
+    double dens;
+    if (det > 0.001) {
+        const double id = 1.0 / det;
+        const double i11 = (a22 * a33 - a23 * a32) * id;
+        const double i12 = -(a12 * a33 - a13 * a32) * id;
+        const double i13 = (a12 * a23 - a13 * a22) * id;
+        const double i21 = -(a21 * a33 - a23 * a31) * id;
+        const double i22 = (a11 * a33 - a13 * a31) * id;
+        const double i23 = -(a11 * a23 - a13 * a21) * id;
+        const double i31 = (a21 * a32 - a22 * a31) * id;
+        const double i32 = -(a11 * a32 - a12 * a31) * id;
+        const double i33 = (a11 * a22 - a12 * a21) * id;
+        const double dens_temp = rhoWsum * i11 + drhodx * i12 + drhody * i13;
+        const double grx = -(rhoWsum * i21 + drhodx * i22 + drhody * i23);
+        const double gry = -(rhoWsum * i31 + drhodx * i32 + drhody * i33);
+        const float2 gnd = Wl.gnd[w];
+        dens = dens_temp + grx * (double)gnd.x + gry * (double)gnd.y;  // rho - rho0
+    } else if (a11 > 0) {
+        dens = rhoWsum / a11;  // Shepard, shifted
+    } else {
+        dens = 1000. - (double)P.rho0;
+    }
+    if (dens + (double)P.rho0 < 1000.) dens = 1000. - (double)P.rho0;  // clamp of src/SPH_mDBC.h:44
+    const float rw = (float)dens;
+    if (predict) {
+        Wl.rho_o[w] = rw;
+        const float rp = rw + Wl.drho[w] * dt * 0.5f;
+        Wl.rho[w] = rp;
+        if (RW.v) wall_record(RW, w, rp, P);
+    } else {
+        Wl.rho[w] = rw;
+    }
+}
+
 __device__ __forceinline__ void mdbc_wall(int gid, const WallState<float> &Wl, int nw,
                                            const uint32_t *__restrict__ fstart,
                                            const FluidState<float> &F, const Grid &g,
@@ -543,49 +593,24 @@ __device__ __forceinline__ void mdbc_wall(int gid, const WallState<float> &Wl, i
 #pragma unroll
         for (int o = kMdbcLanes / 2; o > 0; o >>= 1) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
     }
-    if (!valid || sub != 0) return;
-    // The reference solves A x = (sum m W, sum m dr_x F, sum m dr_y F) for
-    // x = (rho, grad rho).  With m = V_b rho_b and A's first column
-    // (sum V W, sum V dr_x F, sum V dr_y F), the same system with the
-    // right-hand side sum V (rho_b - rho0) (W, dr_x F, dr_y F) has the
-    // solution (rho - rho0, grad rho): identical in exact arithmetic, ~1000x
-    // smaller numbers (and rounding errors) in FP32.
-    const double rhoWsum = s[0], drhodx = s[1], drhody = s[2];
-    const double a11 = s[3], a12 = s[4], a13 = s[5], a21 = s[6], a22 = s[7], a23 = s[8],
-                 a31 = s[9], a32 = s[10], a33 = s[11];
-    const double det = det3(a11, a12, a13, a21, a22, a23, a31, a32, a33);
-    double dens;
-    if (det > 0.001) {
-        const double id = 1.0 / det;
-        const double i11 = (a22 * a33 - a23 * a32) * id;
-        const double i12 = -(a12 * a33 - a13 * a32) * id;
-        const double i13 = (a12 * a23 - a13 * a22) * id;
-        const double i21 = -(a21 * a33 - a23 * a31) * id;
-        const double i22 = (a11 * a33 - a13 * a31) * id;
-        const double i23 = -(a11 * a23 - a13 * a21) * id;
-        const double i31 = (a21 * a32 - a22 * a31) * id;
-        const double i32 = -(a11 * a32 - a12 * a31) * id;
-        const double i33 = (a11 * a22 - a12 * a21) * id;
-        const double dens_temp = rhoWsum * i11 + drhodx * i12 + drhody * i13;
-        const double grx = -(rhoWsum * i21 + drhodx * i22 + drhody * i23);
-        const double gry = -(rhoWsum * i31 + drhodx * i32 + drhody * i33);
-        const float2 gnd = Wl.gnd[w];
-        dens = dens_temp + grx * (double)gnd.x + gry * (double)gnd.y;  // rho - rho0
-    } else if (a11 > 0) {
-        dens = rhoWsum / a11;  // Shepard, shifted
-    } else {
-        dens = 1000. - (double)P.rho0;
-    }
-    if (dens + (double)P.rho0 < 1000.) dens = 1000. - (double)P.rho0;  // clamp of src/SPH_mDBC.h:44
-    const float rw = (float)dens;
-    if (predict) {
-        Wl.rho_o[w] = rw;
-        const float rp = rw + Wl.drho[w] * dt * 0.5f;
-        Wl.rho[w] = rp;
-        if (RW.v) wall_record(RW, w, rp, P);
-    } else {
-        Wl.rho[w] = rw;
-    }
+    // The FP64 solve runs one wall per lane: GB300 issues FP64 at a small
+    // fraction of the FP32 rate and a warp instruction costs the same with 4
+    // lanes active as with 32, so the block's 32 walls hand their sums to its
+    // first warp (lane l solves wall l of the block) instead of solving in
+    // lane 0 of each group of 8.
+    constexpr int kWallsPerBlock = kBlock / kMdbcLanes;
+    __shared__ float sums[12][kWallsPerBlock + 1];
+    const int wl = (int)threadIdx.x / kMdbcLanes;
+#pragma unroll
+    for (int q = 0; q < 12; q++)
+        if (q % kMdbcLanes == sub) sums[q][wl] = s[q];
+    __syncthreads();
+    if (threadIdx.x >= kWallsPerBlock) return;
+    const int ws = gid / kBlock * kWallsPerBlock + (int)threadIdx.x;
+    if (ws >= nw) return;
+#pragma unroll
+    for (int q = 0; q < 12; q++) s[q] = sums[q][threadIdx.x];
+    solve_mdbc(ws, s, Wl, P, predict, dt, RW);
 }
 
 static __global__ void __launch_bounds__(kBlock)
