@@ -235,7 +235,12 @@ int tsph_remove_out_of_domain(tsph_system *s, int *removed);
  * SPH_simulationSymplectic.h:58-118 for DBC, cases/damBreakLong_BT/
  * SPH_simulationSymplectic.h for BT walls) as fused kernels replayed from a
  * CUDA graph.  Requires tsph_particle_to_cell to have been called once (INIT,
- * :41-45).  Leaves the state the reference has after the same steps. */
+ * :41-45).  Leaves the state the reference has after the same steps; its
+ * pressure (p = EOS(rho), which the steps form inside their pair records) is
+ * written to the state by the next call that reads or replaces the state
+ * (download, probes, per-function calls, save), not after every call, so a
+ * time loop of tsph_step calls runs no equation-of-state launch between
+ * steps. */
 int tsph_step(tsph_system *s, int wall_model, double dt, int nsteps);
 
 /* state transfer in the reference's order; `fields` is a TSPH_F_* mask */

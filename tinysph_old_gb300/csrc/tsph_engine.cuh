@@ -930,7 +930,8 @@ template <typename T> class Engine final : public EngineBase {
             if constexpr (std::is_same<T, float>::value) {
                 if (mdbc_fused) {
                     const int nbm = blocks_for((long long)nw_ * kMdbcLanes);
-                    rc = launch(CAT_MDBC, k_mdbc_f32_predict, nbm + blocks_for(nf_), kBlock, err, W_,
+                    rc = launch(CAT_MDBC, k_mdbc_f32_predict,
+                                nbm + blocks_for((nf_ + kPredU - 1) / kPredU), kBlock, err, W_,
                                 nw_, nbm, (const uint32_t *)fstart_, F_, grid_, P_, dt, Fs_, O_,
                                 skin_, rebuild_, health_, cond, capturing_ ? 1 : 0, kc,
                                 rec ? rec_s_ : PairRec{}, rec ? rec_w_ : PairRec{});
@@ -1030,9 +1031,9 @@ template <typename T> class Engine final : public EngineBase {
             auto sort_kept = [&](const uint32_t *gate, uint32_t *runs) -> int {
                 int r;
                 if ((r = launch(CAT_SORT, k_hist_kept<T>, blocks_for(nf_), kBlock, err,
-                                (const FluidState<T>)F_, (const uint32_t *)keyB_, slotB_, counts_,
-                                (const uint8_t *)rm_cand_, (const uint32_t *)fstart_, ncells_, gate,
-                                runs)) ||
+                                (const FluidState<T>)F_, keyB_, slotB_, counts_,
+                                (const uint8_t *)rm_cand_, (const uint32_t *)fstart_, grid_,
+                                make_box_bits(box_), health_, gate, runs)) ||
                     (r = launch(CAT_SORT, k_resolve_removal, 1, kResolveThreads, err, pk.rm, dead_,
                                 keyB_, slotB_, counts_, ncells_, health_, gate)) ||
                     (r = sort_finish(F_.r, F_.v, F_.rho, F_.id, nullptr, nullptr, nullptr, Fs_,

@@ -1404,6 +1404,79 @@ __device__ __forceinline__ void predict_keep_fluid(int f, const FluidState<T> &F
         atomicOr(health, kHealthNan);
 }
 
+// The fluid predictor of the fused FP32 step over U particles per thread
+// (f0, f0 + stride, ...): every particle's loads are issued before the first
+// store, so a thread keeps U particles' reads in flight (with one particle
+// per thread the launch waits on memory latency with few bytes in flight).
+// The arithmetic is predict_keep_fluid<float>'s, particle by particle.
+template <int U>
+__device__ __forceinline__ void predict_keep_fluid_f32(
+    int f0, int stride, const FluidState<float> &F, const uint32_t *__restrict__ fstart,
+    const Grid &g, float dt, const FluidState<float> &D, const OldState<float> &O, float skin,
+    uint32_t *__restrict__ rebuild, uint32_t *__restrict__ health,
+    cudaGraphConditionalHandle cond, int use_cond, const KeepCells &kc, const PairRec &R,
+    const Phys<float> &P) {
+    if (f0 == 0 && kc.clear) *kc.clear = 0u;
+    const int nl = n_live(fstart, g.ncells);
+    float2 v[U], a[U], l[U], lb[U];
+    float s[U], ds[U];
+    uint32_t key[U], id[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        const int f = f0 + u * stride;
+        if (f < nl) {
+            v[u] = F.v[f];
+            a[u] = F.a[f];
+            s[u] = F.rho[f];
+            ds[u] = F.drho[f];
+            l[u] = F.loc[f];
+            key[u] = F.key[f];
+            id[u] = F.id[f];
+            lb[u] = kc.lbin ? kc.lbin[f] : make_float2(0.f, 0.f);
+        }
+    }
+    const bool stale = kc.lbin && __ldg(kc.gen) != __ldg(kc.gen + 1);
+    bool rebin = false, nan = false;
+    const float hdt = dt * 0.5f;
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+        const int f = f0 + u * stride;
+        if (f >= nl) continue;
+        if (!R.e) {  // the corrector over pair records reads the old state from F itself
+            O.r[f] = F.r[f];
+            O.v[f] = v[u];
+            O.rho[f] = s[u];
+        }
+        const float dx = v[u].x * hdt, dy = v[u].y * hdt;
+        const float2 nv = make_float2(v[u].x + a[u].x * dt * 0.5f, v[u].y + a[u].y * dt * 0.5f);
+        D.v[f] = nv;
+        const float sp = s[u] + ds[u] * dt * 0.5f;
+        D.rho[f] = sp;
+        const float2 ln = make_float2(l[u].x + dx, l[u].y + dy);
+        D.loc[f] = ln;
+        D.key[f] = key[u];
+        D.id[f] = id[u];
+        if (R.e) {  // the pair records of the predicted state (kept cells)
+            const float row = (float)(key[u] % (uint32_t)g.ncy);
+            const float ib = rcp_approx(P.rho0 + sp);
+            R.e[f] = make_float4(ln.x, ln.y, row, ib);
+            R.v[f] = make_float4(nv.x, nv.y, sp, eos(sp, P) * ib);
+        }
+        if (kc.lbin) {
+            const float ex = ln.x - lb[u].x, ey = ln.y - lb[u].y;
+            rebin |= !(fmaf(ex, ex, ey * ey) <= kc.sig2) || stale;
+        } else {
+            rebin |= !(fabsf(dx) <= skin && fabsf(dy) <= skin);
+        }
+        nan |= !(nv.x == nv.x) || !(nv.y == nv.y) || !(dx == dx) || !(dy == dy);
+    }
+    if (rebin) {
+        atomicOr(rebuild, 1u);
+        if (use_cond) cudaGraphSetConditional(cond, 1u);
+    }
+    if (nan) atomicOr(health, kHealthNan);
+}
+
 // the copy-back of a re-binning: every field of the sorted state S (and the
 // old state carried in B) into the current buffers D and O, one launch over
 // the rows in use (live and removed, fstart[ncells + 1]) instead of one copy

@@ -612,31 +612,23 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 out.r[i] = rn;
                 reinterpret_cast<float2 *>(out.v)[i] = nv;
                 reinterpret_cast<float *>(out.rho)[i] = s_new;
-                uint32_t nk;
-                bool resort = false, listed = false;
-                int ncx_, ncy_;
+                bool resort = false;
                 if (out_of_domain_bits(rn, out.boxb)) {
-                    // an erase candidate: its cell kept in case the erase skips it
-                    nk = cell_key(g, rn, (uint32_t)(cxa * ncy + cy), &ncx_, &ncy_);
-                    listed = list_removal(out.rm, i);
-                    if (!listed) {
+                    // an erase candidate: its cell kept in case the erase
+                    // skips it (the cell of every other particle is found by
+                    // the sort, k_hist_kept, which runs only when some
+                    // particle needs it; so is its histogram slot)
+                    int ncx_, ncy_;
+                    uint32_t nk = cell_key(g, rn, (uint32_t)(cxa * ncy + cy), &ncx_, &ncy_);
+                    if (!list_removal(out.rm, i)) {
                         nk = (uint32_t)g.ncells;
                         atomicOr(health, kHealthRemoved);
                     }
+                    out.key[i] = nk;
                     resort = true;
-                } else {
-                    nk = cell_key(g, rn, (uint32_t)(cxa * ncy + cy), &ncx_, &ncy_);
-                    if (nk == (uint32_t)g.ncells) {
-                        atomicOr(health, kHealthEscaped);
-                        resort = true;
-                    }
                 }
                 if (!(nv.x == nv.x) || !(nv.y == nv.y) || !(s_new == s_new))
                     atomicOr(health, kHealthNan);
-                // the new cell for a sort (its histogram slot is taken by the
-                // sort itself, which runs only when some particle needs it)
-                out.key[i] = nk;
-                (void)listed;
                 // the new position relative to the kept cell, the pair
                 // records of the next pass, and whether the cells must be
                 // rebuilt before it
@@ -678,21 +670,34 @@ k_lbin_records(PairRec R, const float2 *__restrict__ lbin, const uint32_t *__res
 }
 
 // the sort of a kept-order state (when some particle left its kept cell's
-// reach, or the domain): the histogram slots of the corrector's new cells,
-// except the erase candidates, whose slots the erase takes
+// reach, or the domain): the cell of every particle at its new position (the
+// kept cell as the starting guess) and its histogram slot, except the erase
+// candidates, whose slots the erase takes; a particle outside the removal box
+// that could not be listed keeps the removed key the corrector gave it
 template <typename T>
 __global__ void __launch_bounds__(kBlock)
-k_hist_kept(FluidState<T> X, const uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
+k_hist_kept(FluidState<T> X, uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
             uint32_t *__restrict__ counts, const uint8_t *__restrict__ cand,
-            const uint32_t *__restrict__ fstart, int ncells, const uint32_t *__restrict__ gate,
+            const uint32_t *__restrict__ fstart, Grid g, BoxBits box,
+            uint32_t *__restrict__ health, const uint32_t *__restrict__ gate,
             uint32_t *__restrict__ runs) {
     pdl_enter();
     if (gated_off(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0 && runs) atomicAdd(runs, 1u);
-    if (i >= n_live(fstart, ncells)) return;
+    if (i >= n_live(fstart, g.ncells)) return;
     if (cand[X.id[i]]) return;
-    slot[i] = atomicAdd(counts + key[i], 1u);
+    const double2 r = X.r[i];
+    uint32_t k;
+    if (out_of_domain_bits(r, box)) {
+        k = key[i];
+    } else {
+        int cx, cy;
+        k = cell_key(g, r, X.key[i], &cx, &cy);
+        if (k == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
+        key[i] = k;
+    }
+    slot[i] = atomicAdd(counts + k, 1u);
 }
 
 // the sorted rows (r, v, rho, id, key, loc of S) back into the buffers the

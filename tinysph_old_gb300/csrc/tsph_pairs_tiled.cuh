@@ -621,13 +621,16 @@ k_mdbc_f32(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, Flu
               PairRec{});
 }
 
+// fluid particles per thread of the fused predictor
+constexpr int kPredU = 4;
+
 // mDBC and the predictor of a step in one launch: the first nbm blocks
 // compute the walls' densities (each wall then takes its predictor step),
 // the rest run the fluid predictor in the current cell order.  The two halves
 // touch disjoint data (mDBC reads F's type, key, loc and rho and writes the
 // walls; the fluid predictor reads F and writes D and O), so the
 // latency-bound ghost-node sums overlap the bandwidth-bound predictor.
-static __global__ void __launch_bounds__(kBlock)
+static __global__ void __launch_bounds__(kBlock, 4)
 k_mdbc_f32_predict(WallState<float> Wl, int nw, int nbm, const uint32_t *__restrict__ fstart,
                 FluidState<float> F, Grid g, Phys<float> P, float dt, FluidState<float> D,
                 OldState<float> O, float skin, uint32_t *__restrict__ rebuild,
@@ -638,8 +641,9 @@ k_mdbc_f32_predict(WallState<float> Wl, int nw, int nbm, const uint32_t *__restr
         mdbc_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, true, dt, RW);
         return;
     }
-    predict_keep_fluid<float>(((int)blockIdx.x - nbm) * blockDim.x + threadIdx.x, F, fstart, g, dt,
-                              D, O, skin, rebuild, health, cond, use_cond, kc, RS, &P);
+    predict_keep_fluid_f32<kPredU>(((int)blockIdx.x - nbm) * blockDim.x + threadIdx.x,
+                                   ((int)gridDim.x - nbm) * blockDim.x, F, fstart, g, dt, D, O,
+                                   skin, rebuild, health, cond, use_cond, kc, RS, P);
 }
 
 }  // namespace tsph
