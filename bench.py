@@ -542,7 +542,8 @@ def run_batch(args, rank, world, local):
                         "tsph_download(r,v,rho), pinned host buffers"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
-                     "kernel": f"k_pairs_tiled, largest group {big.key}",
+                     "kernel": f"{PAIR_KERNELS.get(big.system.tile_shape, 'k_pairs_tiled')}, "
+                               f"largest group {big.key}",
                      "bytes_per_unit": PAIR_BYTES_PER_PARTICLE, "unit_count": nfl_big,
                      "avg_launch_us": pair_us, "peak_kind": peak_kind},
         "gpu_launches": int(timed_launches),

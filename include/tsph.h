@@ -323,7 +323,7 @@ typedef struct {
  *     target, 1 = the same with 512 and 44 (for h ~ 1.5 dp),
  * 2 = pair records: a pass forms every particle's neighbour-side values and
  *     the table of each chunk's windows once, then one CTA per 128 targets
- *     stages each window's record ranges with bulk copies (472 staged
+ *     stages each window's record ranges with bulk copies (528 staged
  *     neighbours, 38 list entries per target).
  * tsph_autotune times every variant on the current particles (a warm-up and
  * 10 timed forces passes each, the median kept; the state is left as it was)
@@ -333,6 +333,8 @@ typedef struct {
 #define TSPH_N_TILE_SHAPES 3
 int tsph_autotune(tsph_system *s, int32_t *shape, double us[TSPH_N_TILE_SHAPES]);
 int tsph_set_tile_shape(tsph_system *s, int shape);
+/* the variant in use (-1 before the first tsph_step or tsph_autotune) */
+int tsph_get_tile_shape(tsph_system *s, int32_t *shape);
 int tsph_set_profiling(tsph_system *s, int on);
 
 /* ---- the particle graph of the learned surrogate (no counterpart in the

@@ -608,6 +608,14 @@ int tsph_set_tile_shape(tsph_system *s, int shape) {
     return TSPH_OK;
 }
 
+int tsph_get_tile_shape(tsph_system *s, int32_t *shape) {
+    NEED(s);
+    ENGINE(s);
+    if (!shape) return fail(TSPH_ERR_ARG, "tsph_get_tile_shape: shape is NULL");
+    *shape = s->eng->tile_shape();
+    return TSPH_OK;
+}
+
 int tsph_set_profiling(tsph_system *s, int on) {
     NEED(s);
     s->profiling = on != 0;

@@ -44,7 +44,7 @@ ABI_SYMBOLS = (
     "tsph_health", "tsph_kernel_launches", "tsph_fluid_totals", "tsph_set_profiling",
     "tsph_get_profile",
     "tsph_water_level", "tsph_point_fields", "tsph_water_front", "tsph_autotune",
-    "tsph_set_tile_shape", "tsph_write_vtk", "tsph_save_checkpoint", "tsph_load_checkpoint",
+    "tsph_set_tile_shape", "tsph_get_tile_shape", "tsph_write_vtk", "tsph_save_checkpoint", "tsph_load_checkpoint",
     "tsph_export_graph", "tsph_apply_update", "tsph_window_check", "tsph_get_stream",
     "tsph_state_save", "tsph_state_restore", "tsph_gnn_n_params", "tsph_gnn_create",
     "tsph_gnn_destroy", "tsph_gnn_set_params", "tsph_gnn_get_params", "tsph_gnn_get_grads",
@@ -166,6 +166,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_water_front.argtypes = [P, D, C.POINTER(D)]
     L.tsph_autotune.argtypes = [P, P, P]
     L.tsph_set_tile_shape.argtypes = [P, I]
+    L.tsph_get_tile_shape.argtypes = [P, P]
     L.tsph_write_vtk.argtypes = [P, C.c_char_p]
     L.tsph_export_graph.argtypes = [P, I, I] + [P] * 9 + [C.POINTER(C.c_int32)] * 2
     L.tsph_apply_update.argtypes = [P, P, D, D, D, I, I]
@@ -558,6 +559,13 @@ class ParticleSystem:
 
     def set_tile_shape(self, shape: int):
         _check(self._L.tsph_set_tile_shape(self._h, int(shape)))
+
+    @property
+    def tile_shape(self) -> int:
+        """The pair-kernel variant in use (-1 before the first step)."""
+        c = C.c_int32()
+        _check(self._L.tsph_get_tile_shape(self._h, C.byref(c)))
+        return c.value
 
     def set_profiling(self, on: bool):
         _check(self._L.tsph_set_profiling(self._h, 1 if on else 0))
