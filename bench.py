@@ -398,9 +398,11 @@ BATCH_METRIC = "particle-steps/s, 512 seeded dam-break/still-water cases (2k-100
 
 
 def run_batch(args, rank, world, local):
-    """Batched workload: 512 seeded cases packed into one system per group of
-    equal constants, one step = one time step of every case; next to it the
-    same cases stepped one system at a time (the plain path looped per case)."""
+    """Batched workload: 512 seeded cases packed into ONE particle system
+    (each case scaled to the system's spacing, gravity and removal box per
+    case from the system's case table), one step = one time step of every
+    case with one launch per kernel for the whole batch; next to it the same
+    cases stepped one system at a time (the plain path looped per case)."""
     import numpy as np
     import torch
 
@@ -409,90 +411,107 @@ def run_batch(args, rank, world, local):
 
     torch.cuda.set_device(local)
     specs = B.sample_specs(args.cases, seed=args.seed)
-    bt = B.Batch(specs)
+    stream = torch.cuda.Stream()
+    bt = B.Batch(specs, stream=stream.cuda_stream)
+    s = bt.system
     n = bt.np
     for _ in range(args.warmup):
         bt.step(1)
     bt.sync()
     torch.cuda.synchronize()
-    streams = bt._streams
-    main = torch.cuda.current_stream()
-    t_start = torch.cuda.Event(enable_timing=True)
-    ends = [torch.cuda.Event(enable_timing=True) for _ in streams]
-    for g in bt.groups:
-        g.system.kernel_launches(reset=True)
+    t0e, t1e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.kernel_launches(reset=True)
     with ClockSampler(local) as clocks:
-        t_start.record(main)
-        for st in streams:
-            st.wait_event(t_start)
-        bt.step(args.steps)
-        for st, e in zip(streams, ends):
-            e.record(st)
-        torch.cuda.synchronize()
-    ms = max(t_start.elapsed_time(e) for e in ends)
-    timed_launches = sum(g.system.kernel_launches() for g in bt.groups)
+        with torch.cuda.stream(stream):
+            t0e.record(stream)
+            bt.step(args.steps)
+            t1e.record(stream)
+        stream.synchronize()
+    torch.cuda.synchronize()
+    ms = t0e.elapsed_time(t1e)
+    timed_launches = s.kernel_launches()
     value = n * args.steps / (ms / 1000.0)
-    # per group: step time alone (for the projection to 0.5 s of every case)
-    group_ms = []
-    for g, st in zip(bt.groups, streams):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(st)
-        g.system.step(g.wall_model, g.dt, 5)
-        e1.record(st)
-        torch.cuda.synchronize()
-        group_ms.append(e0.elapsed_time(e1) / 5)
-    t_half = sum(round(0.5 / g.dt) * m for g, m in zip(bt.groups, group_ms)) / 1000.0
-    # pair-kernel roofline on the largest group (eager launches with events)
-    big = max(bt.groups, key=lambda g: g.np)
-    big.system.set_profiling(True)
-    big.system.profile(reset=True)
-    big.system.step(big.wall_model, big.dt, 3)
-    prof = big.system.profile(reset=True)
-    big.system.set_profiling(False)
+    # every case to 0.5 s of its own time: the system steps until the case
+    # with the smallest dt gets there (the coarser cases run further)
+    t_half = round(0.5 / bt.dt) * ms / args.steps / 1000.0
+    # the graph step split by kernel (CUPTI), as for the single case
+    flush = torch.empty(1, dtype=torch.float32, device="cuda")
+    split = graph_kernel_split(s, bt.wall_model, bt.dt, flush, stream, steps=10)
+    # pair-kernel roofline (eager launches with events)
+    s.set_profiling(True)
+    s.profile(reset=True)
+    s.step(bt.wall_model, bt.dt, 3)
+    prof = s.profile(reset=True)
+    s.set_profiling(False)
     pair_us = prof["pair_us"] / max(prof["pair_launches"], 1)
-    nfl_big = sum(int(np.sum(c.type == 0)) for c in big.cases)
+    nfl = sum(int(np.sum(c.type == 0)) for c in bt.cases)
     peak, peak_kind = measured_peaks()
-    achieved = PAIR_BYTES_PER_PARTICLE * nfl_big / (pair_us * 1e-6) / 1e9
-    # e2e: every group's state in from pinned host memory and out again per step
-    hostbufs = []
-    for g in bt.groups:
-        m = g.np
-        hostbufs.append([torch.empty((m, 2), dtype=torch.float64, pin_memory=True),
-                         torch.empty((m, 2), dtype=torch.float64, pin_memory=True),
-                         torch.empty((m,), dtype=torch.float64, pin_memory=True)])
+    achieved = PAIR_BYTES_PER_PARTICLE * nfl / (pair_us * 1e-6) / 1e9
+    # e2e: the whole batch's state in from pinned host memory and out again
+    # per step through the C ABI
+    hr = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+    hv = torch.empty((n, 2), dtype=torch.float64, pin_memory=True)
+    hrho = torch.empty((n,), dtype=torch.float64, pin_memory=True)
     mask = sph.F_R | sph.F_V | sph.F_RHO
-    for g, (hr, hv, hrho) in zip(bt.groups, hostbufs):
-        g.system.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+    s.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
     t0 = time.perf_counter()
     for _ in range(args.e2e_steps):
-        for g, (hr, hv, hrho) in zip(bt.groups, hostbufs):
-            g.system.upload_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
-            g.system.particle_to_cell()
-            g.system.step(g.wall_model, g.dt, 1)
-        for g, (hr, hv, hrho) in zip(bt.groups, hostbufs):
-            g.system.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+        s.upload_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
+        s.particle_to_cell()
+        s.step(bt.wall_model, bt.dt, 1)
+        s.download_ptrs(mask, r=hr.data_ptr(), v=hv.data_ptr(), rho=hrho.data_ptr())
     e2e_value = n * args.e2e_steps / (time.perf_counter() - t0)
+    health = s.health()
+    shape_used = s.tile_shape
+    s.close()
+    del bt
+    torch.cuda.empty_cache()
+    # the earlier packing, for comparison: one system per group of equal
+    # constants, groups on their own streams (one launch per kernel per group)
+    gb = B.GroupedBatch(specs)
+    for _ in range(args.warmup):
+        gb.step(1)
+    gb.sync()
+    torch.cuda.synchronize()
+    main = torch.cuda.current_stream()
+    g0 = torch.cuda.Event(enable_timing=True)
+    gends = [torch.cuda.Event(enable_timing=True) for _ in gb._streams]
+    g0.record(main)
+    for stq in gb._streams:
+        stq.wait_event(g0)
+    gb.step(args.steps)
+    for stq, e in zip(gb._streams, gends):
+        e.record(stq)
+    torch.cuda.synchronize()
+    gms = max(g0.elapsed_time(e) for e in gends)
+    grouped = {"value": gb.np * args.steps / (gms / 1000.0), "unit": "particle-steps/s",
+               "ms_per_step": gms / args.steps, "groups": len(gb.groups),
+               "how": "one system per (kind, dp) group, each on its own stream"}
+    for g in gb.groups:
+        g.system.close()
+    del gb
+    torch.cuda.empty_cache()
     # the plain path looped over the cases: each case alone, one system at a time
     loop_ms = 0.0
     loop_half = 0.0
     st0 = torch.cuda.Stream()
     for spec in specs:
         a = B.case_arrays(spec)
-        s = sph.ParticleSystem(a.h, a.kap, a.cs, 1000.0, 0.02, 0.1, spec.dp, a.domain, "fp32",
+        c = sph.ParticleSystem(a.h, a.kap, a.cs, 1000.0, 0.02, 0.1, spec.dp, a.domain, "fp32",
                                stream=st0.cuda_stream)
-        s.add_particles(a.type, a.r, None, a.rho, a.p, a.gnr if a.wall_model == 0 else None)
-        s.divide_to_cells()
-        s.particle_to_cell()
-        s.step(a.wall_model, a.dt, 3)
+        c.add_particles(a.type, a.r, None, a.rho, a.p, a.gnr)
+        c.divide_to_cells()
+        c.particle_to_cell()
+        c.step(a.wall_model, a.dt, 3)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(st0)
-        s.step(a.wall_model, a.dt, args.loop_steps)
+        c.step(a.wall_model, a.dt, args.loop_steps)
         e1.record(st0)
         st0.synchronize()
         case_ms = e0.elapsed_time(e1) / args.loop_steps
         loop_ms += case_ms
         loop_half += round(0.5 / a.dt) * case_ms / 1000.0
-        s.close()
+        c.close()
     looped_value = n / (loop_ms / 1000.0)
     cpu = None
     if not args.no_cpu:
@@ -507,9 +526,8 @@ def run_batch(args, rank, world, local):
             for i in range(a.np):
                 P.L.orc_add_particle(P.s, int(a.type[i]), float(a.p[i]), float(a.rho[i]),
                                      float(a.r[i, 0]), float(a.r[i, 1]), 0.0, 0.0, 0.0, 0.0)
-            if a.wall_model == 0:  # ghost nodes of the walls (walls come first)
-                for i in np.nonzero(a.type == 1)[0]:
-                    P.L.orc_add_gnr(P.s, float(a.gnr[i, 0]), float(a.gnr[i, 1]))
+            for i in np.nonzero(a.type == 1)[0]:  # ghost nodes of the walls (walls come first)
+                P.L.orc_add_gnr(P.s, float(a.gnr[i, 0]), float(a.gnr[i, 1]))
             P.set_threads(threads)
             P.divide_to_cells()
             P.particle_to_cell()
@@ -520,35 +538,44 @@ def run_batch(args, rank, world, local):
         cpu = {"value": tot / tt, "unit": "particle-steps/s", "cores": threads, "kind": "port",
                "sample": f"3 time steps of each of the first 4 cases ({tot // 3} particles, "
                          f"{tt:.1f} s, FP64 C restatement, OpenMP)"}
+    by_dp = {}
+    for c in bt.cases:
+        k = f"{c.spec.kind} dp={c.spec.dp:g}"
+        by_dp.setdefault(k, [0, 0])
+        by_dp[k][0] += 1
+        by_dp[k][1] += c.np
     line = {
         "metric": BATCH_METRIC, "value": value, "unit": "particle-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 pair math, f64 positions",
         "data": "synthetic (seeded tanks built like the reference's generators)",
-        "config": {"workload": f"{len(specs)} cases (seed {args.seed}) in {len(bt.groups)} packed "
-                               f"groups, {n} particles; one step = one time step of every case",
-                   "particles": n, "groups": [[g.key[0], g.key[1], len(g.cases), g.np]
-                                              for g in bt.groups],
+        "config": {"workload": f"{len(specs)} cases (seed {args.seed}) in one particle system "
+                               f"(case table: per-case scale, gravity and removal box), {n} "
+                               "particles; one step = one time step of every case",
+                   "particles": n, "cases": by_dp, "system_dp": bt.dp,
                    "l2": "inputs larger than L2 (no flush)", "parallelism": "single GPU"},
+        "launches_per_step": timed_launches / args.steps,
+        "grouped": grouped,
         "looped": {"value": looped_value, "unit": "particle-steps/s",
                    "ms_per_step": loop_ms, "speedup_batched": value / looped_value,
                    "how": "each case alone in its own system, CUDA-graph steps, one after another"},
-        "projected_s_to_0.5s_physical": {"batched": t_half, "looped": loop_half},
-        "group_ms_per_step": group_ms,
+        "projected_s_to_0.5s_physical": {"batched": t_half, "looped": loop_half,
+                                         "note": "batched: until the finest cases reach 0.5 s "
+                                                 "(coarser cases run further)"},
         "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": n * 40,
                 "d2h_bytes_per_step": n * 40,
-                "path": "per group tsph_upload(r,v,rho) + tsph_particle_to_cell + tsph_step(1) + "
-                        "tsph_download(r,v,rho), pinned host buffers"},
+                "path": "tsph_upload(r,v,rho) + tsph_particle_to_cell + tsph_step(1) + "
+                        "tsph_download(r,v,rho) of the whole batch, pinned host buffers"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None,
-                     "kernel": f"{PAIR_KERNELS.get(big.system.tile_shape, 'k_pairs_tiled')}, "
-                               f"largest group {big.key}",
-                     "bytes_per_unit": PAIR_BYTES_PER_PARTICLE, "unit_count": nfl_big,
+                     "kernel": PAIR_KERNELS.get(shape_used, "k_pairs_rec"),
+                     "bytes_per_unit": PAIR_BYTES_PER_PARTICLE, "unit_count": nfl,
                      "avg_launch_us": pair_us, "peak_kind": peak_kind},
+        "kernel_us_per_step": split,
         "gpu_launches": int(timed_launches),
         "clocks": clocks.summary(),
-        "health": [g.system.health() for g in bt.groups],
+        "health": health,
     }
     if cpu:
         line["cpu_baseline"] = cpu

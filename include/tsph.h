@@ -213,6 +213,27 @@ int tsph_add_buffer_zone(tsph_system *s, double x0, double xm, double y0, double
  * indices (defaults 65536 and 2^20); an inlet that would exceed them fails
  * with TSPH_ERR_NOMEM.  No counterpart in the reference. */
 int tsph_set_zone_capacity(tsph_system *s, int extra_rows, int extra_ids);
+
+/* Cases packed into one system (the batched workload; no counterpart in the
+ * reference, which runs one case per process).  Every case is placed in the
+ * system's frame scaled to the system's particle spacing (positions x
+ * lambda_k, plus an offset), so that h, the mass, c0, dt and the other SPH
+ * constants are the system's for every case; gravity scales with
+ * 1/lambda_k and stays per case, as does RemoveParticlesOutOfDomain's box
+ * (src/SPH_btdebug.h:4-31).  Per case k: x_range[2k..2k+1] = [lo, hi), the x
+ * range of its grid columns (cases do not share a column; a column between
+ * ranges goes to the nearest case), gravity[k], and removal[4k..4k+3] =
+ * (x_lo, x_hi, y_lo, y_hi): a fluid particle is erased when x < x_lo,
+ * x > x_hi, y < y_lo or y > y_hi (the reference's thresholds, eps included,
+ * in the system's frame).  Call after tsph_add_particles, before
+ * tsph_particle_to_cell; ncases = 0 removes the table.  FP32 build, mDBC
+ * walls, tsph_step only (the per-function force, corrector and removal calls
+ * and tsph_save_checkpoint return TSPH_ERR_UNSUPPORTED on a system with a case
+ * table); the fused step then uses the pair-record kernel, which reads each
+ * window's case from its grid column, so the whole batch takes one launch per
+ * kernel per step. */
+int tsph_set_cases(tsph_system *s, int ncases, const double *x_range, const double *gravity,
+                   const double *removal);
 /* BZ_Integrate_inlet / BZ_Integrate_outlet, src/SPH_buffer_zones.h:10-206 */
 int tsph_bz_inlet(tsph_system *s, int zone, double dt);
 int tsph_bz_outlet(tsph_system *s, int zone, double dt);

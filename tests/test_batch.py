@@ -1,6 +1,8 @@
 """Batched cases: the vectorised generators, the seeded batch, the packing of
-equal-constant cases into one domain, and (GPU) per-case results of a packed
-group against separate runs of the same cases."""
+every case into one particle system (scaled to the system's particle spacing,
+with a column range, a gravity and a removal box per case), and (GPU)
+per-case results of the packed batch against the oracle run on each case in
+its own units, including erasures at a case's own removal box."""
 
 import numpy as np
 import pytest
@@ -21,15 +23,16 @@ def test_vectorised_generators_match_the_reference_order(spec):
         c = cases.dam_break_mdbc(dp=spec.dp, cs=35.0, wall_height=0.8, tank_length=spec.tank,
                                  column=(spec.col_w, spec.col_h))
     else:
-        c = cases.still_water_dbc(dp=spec.dp, width=spec.col_w, depth=spec.col_h,
-                                  tank_height=spec.col_h + 0.1)
+        c = cases.still_water_tank_mdbc(dp=spec.dp, width=spec.col_w, depth=spec.col_h,
+                                        wall_height=spec.col_h + 0.1)
     ca = c.particles.arrays()
     assert a.np == c.np
     for k in ("r", "type", "rho", "p"):
         assert np.array_equal(getattr(a, k), ca[k]), k
-    if len(ca["gnr"]):
-        assert np.array_equal(a.gnr[:len(ca["gnr"])], ca["gnr"])
+    assert np.array_equal(a.gnr[:len(ca["gnr"])], ca["gnr"])
     assert (a.h, a.kap, a.cs, a.dt, a.wall_model) == (c.h, c.kap, c.cs, c.dt, c.wall_model)
+    if spec.kind == B.STILL_WATER:  # (a dam break's domain grows with its tank: x_1 = max(2, L + 0.1))
+        assert a.domain == c.domain
 
 
 def test_seeded_batch_spans_the_stated_sizes():
@@ -42,45 +45,92 @@ def test_seeded_batch_spans_the_stated_sizes():
     assert specs == B.sample_specs(512, seed=0)  # deterministic
 
 
-def test_packing_keeps_cases_apart():
+def test_scaled_packing_keeps_cases_apart():
     specs = B.sample_specs(64, seed=3)
-    for key, members in B.group_specs(specs).items():
-        g = B.pack([B.case_arrays(s) for _, s in members])
-        c0 = g.cases[0]
-        kh = c0.h * c0.kap
-        gap = B.SPLASH_GAP if key[0] == B.DAM_BREAK else 4 * kh
-        for k in range(len(g.cases) - 1):
-            right = g.offset[k] + g.cases[k].extent[1]
-            left = g.offset[k + 1] + g.cases[k + 1].extent[0]
-            assert left - right >= gap * (1 - 1e-12)
-            # no particle of one case within 2h of the next one
-            xr = (g.cases[k].r[:, 0] + g.offset[k]).max()
-            xl = (g.cases[k + 1].r[:, 0] + g.offset[k + 1]).min()
-            assert xl - xr > 2 * c0.h
-        assert all(len({(c.h, c.kap, c.cs, c.dt, c.wall_model) for c in g.cases}) == 1 for _ in [0])
+    cs = [B.case_arrays(s) for s in specs]
+    pk = B.pack_scaled(cs)
+    kh = pk.h * 2.1
+    # column ranges in order, CASE_GAP_CELLS cells apart
+    assert np.all(pk.ranges[1:, 0] - pk.ranges[:-1, 1] >= B.CASE_GAP_CELLS * kh * (1 - 1e-12))
+    for k, c in enumerate(cs):
+        lam = pk.scale[k]
+        # the system's spacing, h and step for every scaled case; gravity g / lambda
+        assert np.isclose(c.spec.dp * lam, pk.dp) and np.isclose(c.h * lam, pk.h)
+        assert np.isclose(c.dt * lam, pk.dt) and np.isclose(pk.gravity[k], 9.81 / lam)
+        r = c.r * lam + np.array([pk.offset[k], 0.0])
+        assert pk.ranges[k, 0] <= r[:, 0].min() and r[:, 0].max() < pk.ranges[k, 1]
+        # the removal box lies inside the case's columns: a fluid particle
+        # leaves them only by being erased, so no pair spans two cases
+        x_lo, x_hi, y_lo, y_hi = pk.boxes[k]
+        assert pk.ranges[k, 0] < x_lo and x_hi < pk.ranges[k, 1]
+        fl = c.type == B.FLUID
+        assert np.all((r[fl, 0] >= x_lo) & (r[fl, 0] <= x_hi))
+        assert np.all((r[fl, 1] >= y_lo) & (r[fl, 1] <= y_hi))
+        assert y_lo >= pk.domain[2] and y_hi <= pk.domain[3]
+
+
+def _oracle_case(oracle_mod, a):
+    P = oracle_mod.PortSystem(a.h, a.kap, a.cs, 1000.0, 0.02, 0.1, a.spec.dp, a.domain)
+    for i in range(a.np):
+        P.L.orc_add_particle(P.s, int(a.type[i]), float(a.p[i]), float(a.rho[i]),
+                             float(a.r[i, 0]), float(a.r[i, 1]), 0.0, 0.0, 0.0, 0.0)
+    for i in np.nonzero(a.type == B.WALL)[0]:  # walls come first
+        P.L.orc_add_gnr(P.s, float(a.gnr[i, 0]), float(a.gnr[i, 1]))
+    P.divide_to_cells()
+    P.particle_to_cell()
+    return P
 
 
 @pytest.mark.gpu
-def test_packed_group_matches_separate_runs(gpu_tsph):
-    specs = [B.CaseSpec(B.DAM_BREAK, 0.004, 1.0, 0.4, 0.3), B.CaseSpec(B.DAM_BREAK, 0.004, 1.6, 0.6, 0.25),
-             B.CaseSpec(B.STILL_WATER, 0.004, 1.0, 0.5, 0.3), B.CaseSpec(B.STILL_WATER, 0.004, 1.0, 0.3, 0.2),
-             B.CaseSpec(B.DAM_BREAK, 0.004, 0.9, 0.3, 0.45)]
-    bt = B.Batch(specs, streams=False)
-    assert len(bt.groups) == 2
-    nsteps = 200
-    bt.step(nsteps)
-    for k, spec in enumerate(specs):
-        a = B.case_arrays(spec)
-        s = gpu_tsph.ParticleSystem(a.h, a.kap, a.cs, 1000.0, 0.02, 0.1, spec.dp, a.domain, "fp32")
-        s.add_particles(a.type, a.r, None, a.rho, a.p, a.gnr if a.wall_model == 0 else None)
-        s.divide_to_cells()
-        s.particle_to_cell()
-        s.step(a.wall_model, a.dt, nsteps)
-        ref = s.download()
-        got = bt.case_state(k)
-        assert np.array_equal(got["index"], ref["index"]), k
-        er = float(np.max(np.abs(got["r"] - ref["r"])))
-        ev = float(np.max(np.abs(got["v"] - ref["v"])))
-        erho = float(np.max(np.abs(got["rho"] - ref["rho"])))
-        print(k, spec.kind, er, ev, erho)
-        assert er <= 1e-5 and ev <= 2e-3 and erho <= 2e-2, (k, er, ev, erho)
+def test_batch_in_one_system_matches_the_oracle_per_case(gpu_tsph, oracle_mod):
+    """Five cases of three spacings in one system (one launch per kernel per
+    step) against the oracle run on each case alone in its own units.  Two
+    consecutive fluid particles of the still-water case start beyond its
+    removal threshold x > x_m - 0.01 (inside its columns and the system's
+    grid): the first step erases the first and, as the reference's erase loop
+    does, skips the second, which goes one step later."""
+    import os
+
+    oracle_mod.PortSystem.set_threads(os.cpu_count() or 1)
+    # a shallow tank (15 particles per column) before a second case: chunks of
+    # 128 targets there span more columns than the window table holds, and
+    # the last window (global path) crosses into the next case
+    specs = [B.CaseSpec(B.DAM_BREAK, 0.004, 1.0, 0.4, 0.3),
+             B.CaseSpec(B.STILL_WATER, 0.003, 1.0, 0.5, 0.25),
+             B.CaseSpec(B.STILL_WATER, 0.004, 1.0, 0.5, 0.06),
+             B.CaseSpec(B.DAM_BREAK, 0.002, 0.9, 0.25, 0.2),
+             B.CaseSpec(B.STILL_WATER, 0.004, 1.0, 0.4, 0.2)]
+    arrays = [B.case_arrays(s) for s in specs]
+    sw = arrays[1]
+    fl = np.nonzero(sw.type == B.FLUID)[0]
+    out = fl[40:42]
+    xm = sw.domain[1]
+    sw.r[out[0]] = (xm - 0.005, 0.05)
+    sw.r[out[1]] = (xm - 0.004, 0.06)
+    bt = B.Batch(specs, arrays=arrays)
+    assert bt.system.tile_shape == 2
+    refs = [_oracle_case(oracle_mod, a) for a in arrays]
+    done = 0
+    for nsteps in (1, 1, 98):
+        bt.step(nsteps)
+        for P, a in zip(refs, arrays):
+            P.step(a.wall_model, a.dt, nsteps)
+        done += nsteps
+        st = bt.system.download()
+        for k, (P, a) in enumerate(zip(refs, arrays)):
+            got, ref = bt.case_state(k, st), P.state()
+            assert np.array_equal(got["index"], ref["index"]), (done, k)
+            f = ref["type"] == B.FLUID
+            er = float(np.max(np.abs(got["r"][f] - ref["r"][f])))
+            ev = float(np.max(np.abs(got["v"][f] - ref["v"][f])))
+            erho = float(np.max(np.abs(got["rho"] - ref["rho"])))
+            print(done, k, specs[k].kind, specs[k].dp, er, ev, erho)
+            assert er <= 1e-7 and ev <= 1e-4 and erho <= 1e-3, (done, k, er, ev, erho)
+            # walls do not move (equal up to the rounding of the scaling)
+            assert np.max(np.abs(got["r"][~f] - ref["r"][~f])) <= 1e-12
+        if done == 1:  # the first erased, the second skipped
+            ids = bt.case_state(1, st)["index"]
+            assert out[0] not in ids and out[1] in ids
+    ids = bt.case_state(1, st)["index"]
+    assert out[0] not in ids and out[1] not in ids
+    assert bt.system.np == sum(a.np for a in arrays) - 2

@@ -1,19 +1,28 @@
 """Many independent WCSPH cases stepped together on one GPU.
 
 The batched workload is a set of seeded dam-break and still-water tanks of
-different sizes and resolutions.  Cases that share every SPH constant (the
-same kind and particle spacing, hence the same h, dt, mass, sound speed and
-wall model) form a group.  A group is packed into one domain: the tanks sit
-side by side along x, each shifted by an entry of the group's case table and
-separated by an empty gap, and the group runs as one particle system, so
-every kernel launch of a step covers all of its cases at once (one counting
-sort, one pair pass over all cells of all tanks).  A particle interacts only
-with particles within 2h of it, so tanks more than 2h apart never see each
-other; the gap is wide enough that a particle thrown over a tank wall falls
-below the floor level (and leaves the domain) before it can reach the next
-tank.  Per-case results therefore agree with separate runs of each case up to
-FP32 rounding (the cell grid is aligned differently and the positions are
-shifted by the case offset).
+different sizes and resolutions (particle spacing dp in {0.004, 0.003,
+0.002} m), all with mDBC walls and the dam-break constants (h = sqrt(2) dp,
+c0 = 35 m/s, dt = 0.01 dp s).
+
+:class:`Batch` packs every case into ONE particle system, so each kernel
+launch of a step covers the whole batch.  Case k is scaled by
+lambda_k = dp_sys / dp_k (dp_sys the smallest spacing) and shifted along x:
+in that frame every case has the system's spacing, h, particle mass, sound
+speed and time step, and the SPH equations are those of the unscaled case
+with velocity and density unchanged, time scaled by lambda_k (one system step
+dt_sys advances case k by its own dt_k = dt_sys / lambda_k) and gravity
+g / lambda_k.  Gravity and RemoveParticlesOutOfDomain's box
+(src/SPH_btdebug.h:4-31) are therefore per case: the system's case table
+(``tsph_set_cases``) gives each grid column its case.  Cases sit side by side
+with gaps of several cells; a particle leaves its case only through that
+case's removal box, so no pair ever spans two cases.  Per-case results agree
+with separate runs of each case up to FP32 rounding (the scaled positions
+round differently).
+
+:class:`GroupedBatch` is the packing used before the case table: cases with
+identical constants side by side in one system per group, groups on their
+own streams (one launch per kernel per group).
 
 The case generators here are vectorised restatements of the ones in
 ``cases`` (bit-identical particles, tested), because a batch holds millions
@@ -37,10 +46,10 @@ FLUID, WALL = 0, 1
 @dataclass
 class CaseSpec:
     """One case of the batch.  Dam break: tank of length ``tank`` and walls
-    0.8 m high, water column ``col_w`` x ``col_h`` at the left wall, mDBC,
-    c0 = 35 m/s, h = sqrt(2) dp.  Still water: water ``tank`` wide and
-    ``col_h`` deep filling a tank of the same width, 3 DBC wall layers,
-    c0 = 20 m/s, h = 1.5 dp."""
+    0.8 m high, water column ``col_w`` x ``col_h`` at the left wall.  Still
+    water: a tank ``col_w`` wide with walls ``col_h`` + 0.1 m high, filled
+    ``col_h`` deep at rest (hydrostatic start).  Both with mDBC walls,
+    c0 = 35 m/s, h = sqrt(2) dp, dt = 0.01 dp."""
 
     kind: str
     dp: float
@@ -174,47 +183,37 @@ def case_arrays(spec: CaseSpec) -> CaseArrays:
         dom = _cases._pad(0.0, max(2.0, L + 0.1), 0.0, 1.0, nvl, dp)
         return CaseArrays(spec, typ, r, rho, p, gnr, h, kap, cs, 0.00005 * (dp / 0.005),
                           _cases.WALL_MDBC, dom, (dom[0], L + nvl * dp))
-    # still water (cases.still_water_dbc: water col_w wide filling the tank,
-    # col_h deep, tank col_h + 0.1 high, 3 wall layers, hydrostatic start)
-    return _still_water(spec, dp, spec.col_w, spec.col_h, spec.col_h + 0.1, 20.0, 3)
-
-
-def _still_water(spec, dp, width, depth, tank_height, cs, layers):
-    kap = 2.1
-    h = 1.5 * dp
-    nx, ny, nyw = int(round(width / dp)), int(round(depth / dp)), int(round(tank_height / dp))
+    # still water (cases.still_water_tank_mdbc: a tank col_w wide, walls
+    # col_h + 0.1 high, filled col_h deep at rest, hydrostatic start)
+    kap, cs, L, wall_h, depth = 2.1, 35.0, spec.col_w, spec.col_h + 0.1, spec.col_h
+    h = 1.0 * math.sqrt(2 * dp * dp)
+    kh = h * kap
+    parts = [
+        _wall_x_mdbc(dp, kh, 0.0 + dp, L - dp, 0.0, -1, dp / 2),
+        _wall_y_mdbc(dp, kh, 0.0, 0 + dp, wall_h, -1, dp / 2),
+        _wall_y_mdbc(dp, kh, L, 0 + dp, wall_h, +1, L - dp / 2),
+        _corner_mdbc(dp, kh, -1, -1, 0.0 + dp / 2, 0.0 + dp / 2),
+        _corner_mdbc(dp, kh, +1, -1, L - dp / 2, 0.0 + dp / 2),
+    ]
+    wx, wy, gx, gy = (np.concatenate(list(c)) for c in zip(*[tuple(p) for p in parts]))
+    fx, fy = _block(dp, 0 + dp, 0 + dp, L - dp, depth)
+    # Create_Block_of_FluidWP (src/SPH_create.h:689-727): p = 9.81 (H - y) 1000,
+    # rho from Pressure_to_density with libm pow, per distinct height
     b = cs * cs * 1000.0 / 7.0
-
-    def hydro(y):
-        # per distinct height, with math.pow (libm pow, as geometry.pressure_to_density)
-        uy, inv = np.unique(y, return_inverse=True)
-        up = np.array([0.0 if v >= depth else 9.81 * (depth - v) * 1000 for v in uy])
-        ur = np.array([1000.0 if v >= depth else math.pow(q / b + 1, 1.0 / 7) * 1000.0
-                       for v, q in zip(uy, up)])
-        return up[inv], ur[inv]
-
-    xs, ys = [], []
-    for l in range(layers):
-        i = np.arange(-layers, nx + layers, dtype=np.float64)
-        xs.append((i + 0.5) * dp)
-        ys.append(np.full(len(i), -(l + 0.5) * dp))
-    jw = np.arange(nyw, dtype=np.float64)
-    for side in (0, 1):
-        for l in range(layers):
-            x = -(l + 0.5) * dp if side == 0 else width + (l + 0.5) * dp
-            xs.append(np.full(nyw, x))
-            ys.append((jw + 0.5) * dp)
-    wx, wy = np.concatenate(xs), np.concatenate(ys)
-    i = np.arange(nx, dtype=np.float64)
-    j = np.arange(ny, dtype=np.float64)
-    fx, fy = np.repeat((i + 0.5) * dp, ny), np.tile((j + 0.5) * dp, nx)
-    x, y = np.concatenate([wx, fx]), np.concatenate([wy, fy])
-    p, rho = hydro(y)
-    typ = np.concatenate([np.full(len(wx), WALL, np.int32), np.full(len(fx), FLUID, np.int32)])
-    pad = (layers + 2) * dp
-    dom = (0.0 - pad, width + pad, 0.0 - pad, tank_height + pad)
-    return CaseArrays(spec, typ, np.stack([x, y], 1), rho, p, np.zeros((len(x), 2)), h, kap, cs,
-                      0.2 * h / cs, _cases.WALL_DBC, dom, (dom[0], dom[1]))
+    uy, inv = np.unique(fy, return_inverse=True)
+    up = 9.81 * (depth - uy) * 1000
+    ur = np.array([math.pow(q / b + 1, 1.0 / 7) * 1000.0 for q in up])
+    nw, nf = len(wx), len(fx)
+    r = np.stack([np.concatenate([wx, fx]), np.concatenate([wy, fy])], 1)
+    typ = np.concatenate([np.full(nw, WALL, np.int32), np.full(nf, FLUID, np.int32)])
+    gnr = np.zeros((nw + nf, 2))
+    gnr[:nw, 0], gnr[:nw, 1] = gx, gy
+    rho = np.concatenate([np.full(nw, 1000.0), ur[inv]])
+    p = np.concatenate([np.zeros(nw), up[inv]])
+    nvl = int(math.ceil(kap * h / dp))
+    dom = _cases._pad(0.0, L + 0.1, 0.0, wall_h + 0.1, nvl, dp)
+    return CaseArrays(spec, typ, r, rho, p, gnr, h, kap, cs, 0.00005 * (dp / 0.005),
+                      _cases.WALL_MDBC, dom, (dom[0], L + nvl * dp))
 
 
 # ---------------------------------------------------------------- packing
@@ -277,11 +276,11 @@ def group_specs(specs):
     return groups
 
 
-class Batch:
-    """The batched workload: one packed particle system per group of equal
-    constants.  ``step(n)`` advances every group by n of its own time steps
-    (all graph launches enqueued before any synchronisation, one stream per
-    group)."""
+class GroupedBatch:
+    """Cases packed one particle system per group of equal constants, each
+    group on its own stream (``step(n)``: every group advances by n of its
+    own time steps).  Used to generate the surrogate's training windows,
+    whose cases share one spacing."""
 
     def __init__(self, specs, precision="fp32", streams=True):
         from . import sph
@@ -341,4 +340,128 @@ class Batch:
         out = {f: st[f][sel] for f in st}
         out["index"] = out["index"] - lo
         out["r"] = out["r"] - np.array([g.offset[pos], 0.0])
+        return out
+
+
+# ------------------------------------------------------- one system, scaled
+# Gap between the column ranges of two packed cases, in cells: more than the
+# 2h support plus the distance a particle can travel past its case's removal
+# box in the step before the corrector erases it.
+CASE_GAP_CELLS = 4
+# margin of a case's column range beyond its removal thresholds (m, unscaled)
+CASE_MARGIN = 0.02
+
+
+@dataclass
+class ScaledPacking:
+    """Where the cases of a batch go in one system (see :class:`Batch`)."""
+
+    cases: list
+    dp: float           # the system's spacing (the finest case's)
+    h: float
+    dt: float
+    scale: np.ndarray   # lambda_k = dp / dp_k
+    offset: np.ndarray  # x shift of case k in the system's frame
+    base: np.ndarray    # first particle index of case k
+    ranges: np.ndarray  # [lo, hi) of case k's grid columns
+    boxes: np.ndarray   # removal thresholds (x_lo, x_hi, y_lo, y_hi) of case k
+    gravity: np.ndarray
+    domain: tuple
+
+
+def pack_scaled(case_list, kap=2.1) -> ScaledPacking:
+    """Case k scaled by dp / dp_k and placed along x with CASE_GAP_CELLS
+    cells between the column ranges of neighbouring cases; its removal box is
+    RemoveParticlesOutOfDomain's (src/SPH_btdebug.h:16-19, eps = 0.01 m) in
+    the system's frame."""
+    dp = min(c.spec.dp for c in case_list)
+    h = 1.0 * math.sqrt(2 * dp * dp)
+    kh = h * kap
+    gap = CASE_GAP_CELLS * kh
+    scale = np.array([dp / c.spec.dp for c in case_list])
+    offs, bases, ranges, boxes = [], [], [], []
+    x, base = 0.0, 0
+    for k, (c, lam) in enumerate(zip(case_list, scale)):
+        x0, x1, y0, y1 = c.domain
+        lo, hi = lam * (x0 - CASE_MARGIN), lam * (x1 + CASE_MARGIN)
+        off = (x + gap if k else 0.0) - lo
+        offs.append(off)
+        bases.append(base)
+        base += c.np
+        ranges.append((lo + off, hi + off))
+        boxes.append((lam * (x0 - 0.01) + off, lam * (x1 - 0.01) + off, lam * (y0 - 0.01),
+                      lam * (y1 + 0.01)))
+        x = hi + off
+    ranges = np.array(ranges)
+    ylo = min(lam * (c.domain[2] - CASE_MARGIN) for c, lam in zip(case_list, scale))
+    yhi = max(lam * (c.domain[3] + CASE_MARGIN) for c, lam in zip(case_list, scale))
+    return ScaledPacking(list(case_list), dp, h, 0.00005 * (dp / 0.005), scale, np.array(offs),
+                         np.array(bases, dtype=np.int64), ranges, np.array(boxes),
+                         9.81 / scale, (ranges[0, 0], ranges[-1, 1], ylo, yhi))
+
+
+class Batch:
+    """The batched workload in ONE particle system (module docstring): case k
+    scaled by ``scale[k]`` = dp_sys / dp_k and shifted by ``offset[k]`` along
+    x, its particles at ``base[k]`` .. ``base[k] + np_k`` of the system's
+    numbering, its gravity 9.81 / scale[k] and its removal box in the
+    system's case table.  One ``step`` advances every case by its own dt_k
+    (= dt / scale[k]) with one launch per kernel for the whole batch."""
+
+    def __init__(self, specs, precision="fp32", stream=None, arrays=None, kap=2.1):
+        from . import sph
+
+        self.specs = list(specs)
+        # `arrays`: the cases' particles when not those of case_arrays(spec)
+        self.cases = list(arrays) if arrays is not None else [case_arrays(sp) for sp in self.specs]
+        pk = pack_scaled(self.cases, kap)
+        self.packing = pk
+        self.dp, self.h, self.dt = pk.dp, pk.h, pk.dt
+        self.kap, self.cs = kap, 35.0
+        self.wall_model = _cases.WALL_MDBC
+        self.scale, self.offset, self.base = pk.scale, pk.offset, pk.base
+        self.ranges, self.boxes, self.gravity, self.domain = pk.ranges, pk.boxes, pk.gravity, pk.domain
+        typ = np.concatenate([c.type for c in self.cases])
+        r = np.concatenate([c.r * lam + np.array([off, 0.0])
+                            for c, lam, off in zip(self.cases, self.scale, self.offset)])
+        rho = np.concatenate([c.rho for c in self.cases])
+        p = np.concatenate([c.p for c in self.cases])
+        gnr = np.concatenate([(c.gnr * lam + np.array([off, 0.0])) * (c.type[:, None] == WALL)
+                              for c, lam, off in zip(self.cases, self.scale, self.offset)])
+        s = sph.ParticleSystem(self.h, self.kap, self.cs, 1000.0, 0.02, 0.1, self.dp,
+                               self.domain, precision, stream=stream)
+        s.add_particles(typ, r, None, rho, p, gnr)
+        s.divide_to_cells()
+        s.set_cases(self.ranges, self.gravity, self.boxes)
+        s.particle_to_cell()
+        self.system = s
+
+    @property
+    def np(self):
+        return int(sum(c.np for c in self.cases))
+
+    def step(self, n=1):
+        self.system.step(self.wall_model, self.dt, n)
+
+    def sync(self):
+        self.system.sync()
+
+    def case_dt(self, k):
+        """The physical time step of case k (one system step)."""
+        return self.dt / self.scale[k]
+
+    def case_state(self, k, st=None):
+        """State of batch case k in its own units, coordinates and particle
+        order (``st``: a download of the system to reuse)."""
+        st = self.system.download() if st is None else st
+        lo, hi = self.base[k], self.base[k] + self.cases[k].np
+        sel = (st["index"] >= lo) & (st["index"] < hi)
+        out = {f: st[f][sel] for f in st}
+        lam = self.scale[k]
+        out["index"] = out["index"] - lo
+        out["r"] = (out["r"] - np.array([self.offset[k], 0.0])) / lam
+        if "a" in out:
+            out["a"] = out["a"] * lam
+        if "drho" in out:
+            out["drho"] = out["drho"] * lam
         return out

@@ -136,6 +136,34 @@ def still_water_mdbc(dp: float = 0.02, dt: float | None = None) -> Case:
                 meta=dict(nvl=nvl, depth=0.5))
 
 
+def still_water_tank_mdbc(dp: float = 0.004, width: float = 0.8, depth: float = 0.3,
+                          wall_height: float = 0.4, cs: float = 35.0) -> Case:
+    """Still water with mDBC walls in a tank of a given size, with the dam
+    break's numerics (the batched workload's still-water cases): the walls
+    and corners of ``cases/stillWater_mDBC/geometry.h`` for a tank ``width``
+    wide with walls ``wall_height`` high, a hydrostatic block
+    (Create_Block_of_FluidWP) from (dp, dp) to (width - dp, depth);
+    h = sqrt(2 dp^2), kap = 2.1, visco = 0.02, delta = 0.1,
+    dt = 5e-5 * dp / 0.005; domain [0, width + 0.1] x [0, wall_height + 0.1]
+    padded."""
+    kap = 2.1
+    hh = 1.0 * math.sqrt(2 * dp * dp)
+    dt = 0.00005 * (dp / 0.005)
+    nvl = int(math.ceil(kap * hh / dp))
+    ps = geo.ParticleSet(dp, hh, kap, cs)
+    W = width
+    geo.create_wall_x_mdbc(ps, 0.0 + dp, W - dp, 0.0, -1, dp / 2)
+    geo.create_wall_y_mdbc(ps, 0.0, 0 + dp, wall_height, -1, dp / 2)
+    geo.create_wall_y_mdbc(ps, W, 0 + dp, wall_height, +1, W - dp / 2)
+    geo.create_corner_mdbc(ps, -1, -1, (0.0 + dp / 2, 0.0 + dp / 2))
+    geo.create_corner_mdbc(ps, +1, -1, (W - dp / 2, 0.0 + dp / 2))
+    geo.create_block_of_fluid_wp(ps, 0 + dp, 0 + dp, W - dp, depth)
+    return Case(name=f"still_water_tank_mdbc_dp{dp:g}", particles=ps, h=hh, kap=kap, cs=cs,
+                rho0=1000.0, visco=0.02, delta=0.1, dp=dp,
+                domain=_pad(0.0, W + 0.1, 0.0, wall_height + 0.1, nvl, dp),
+                wall_model=WALL_MDBC, dt=dt, meta=dict(nvl=nvl, depth=depth))
+
+
 def still_water_dbc(dp: float = 0.005, width: float = 0.5, depth: float = 0.3,
                     tank_height: float = 0.4, cs: float = 20.0, visco: float = 0.02,
                     delta: float = 0.1, layers: int = 3,

@@ -343,6 +343,24 @@ int tsph_add_buffer_zone(tsph_system *s, double x0, double xm, double y0, double
     return TSPH_OK;
 }
 
+int tsph_set_cases(tsph_system *s, int ncases, const double *x_range, const double *gravity,
+                   const double *removal) {
+    NEED(s);
+    if (ncases < 0 || (ncases > 0 && (!x_range || !gravity || !removal)))
+        return fail(TSPH_ERR_ARG, "tsph_set_cases: ncases >= 0 and the three arrays");
+    if (s->precision == TSPH_PREC_FP64)
+        return fail(TSPH_ERR_UNSUPPORTED, "tsph_set_cases: FP32 build only");
+    for (int k = 0; k < ncases; k++)
+        if (!(x_range[2 * k] < x_range[2 * k + 1]) || !(removal[4 * k] < removal[4 * k + 1]) ||
+            !(removal[4 * k + 2] < removal[4 * k + 3]))
+            return fail(TSPH_ERR_ARG, "tsph_set_cases: empty range of case " + std::to_string(k));
+    s->hs.case_x.assign(x_range, x_range + 2 * (size_t)ncases);
+    s->hs.case_g.assign(gravity, gravity + (size_t)ncases);
+    s->hs.case_box.assign(removal, removal + 4 * (size_t)ncases);
+    s->stale_engine = true;
+    return TSPH_OK;
+}
+
 int tsph_set_zone_capacity(tsph_system *s, int extra_rows, int extra_ids) {
     NEED(s);
     if (extra_rows < 0 || extra_ids < 0) return fail(TSPH_ERR_ARG, "capacities must be >= 0");

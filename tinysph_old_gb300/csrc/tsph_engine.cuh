@@ -324,6 +324,75 @@ template <typename T> class Engine final : public EngineBase {
     long long rec_passes_sv_ = -1;
     float2 *lbin_sv_ = nullptr;   // binning positions and list counters at state_save
     uint32_t *gen_sv_ = nullptr;
+    // cases packed into one system (tsph_set_cases): the case of each grid
+    // column and each case's gravity-dependent constants and removal box
+    int32_t *col_case_ = nullptr;
+    CaseConst *cases_ = nullptr;
+    bool cases_on_ = false;
+
+    // The case table of HostSetup on the device.  A column belongs to the case
+    // whose x range holds its centre (a column between ranges, to the nearest
+    // case); per case, gravity, the Fourtakas coefficients that follow from it
+    // (as make_tile_const forms them) and the removal thresholds as ordered
+    // bits.
+    int setup_cases(const HostSetup &hs, std::string &err) {
+        const int nc = (int)hs.case_g.size();
+        if ((int)hs.case_x.size() != 2 * nc || (int)hs.case_box.size() != 4 * nc) {
+            err = "case table: 2 x-range values, 1 gravity and 4 thresholds per case";
+            return 1;
+        }
+        std::vector<int32_t> cc(hs.ncx, -1);
+        for (int k = 0; k < nc; k++) {
+            const double lo = hs.case_x[2 * k], hi = hs.case_x[2 * k + 1];
+            // first column whose centre is at or above lo
+            int cx = (int)(std::lower_bound(hs.ox.begin(), hs.ox.end(), lo - 0.5 * hs.kh) -
+                           hs.ox.begin());
+            for (; cx < hs.ncx && hs.ox[cx] + 0.5 * hs.kh < hi; cx++)
+                if (hs.ox[cx] + 0.5 * hs.kh >= lo) cc[cx] = k;
+        }
+        int last = -1;
+        std::vector<int> dist(hs.ncx, 1 << 30);
+        for (int cx = 0; cx < hs.ncx; cx++) {  // nearest assigned column on the left
+            if (cc[cx] >= 0) last = cx;
+            else if (last >= 0) dist[cx] = cx - last;
+        }
+        std::vector<int32_t> out = cc;
+        for (int cx = 0; cx < hs.ncx; cx++)
+            if (cc[cx] < 0 && dist[cx] < (1 << 30)) out[cx] = cc[cx - dist[cx]];
+        last = -1;
+        for (int cx = hs.ncx - 1; cx >= 0; cx--) {  // or on the right, when nearer
+            if (cc[cx] >= 0) {
+                last = cx;
+            } else if (last >= 0 && last - cx < dist[cx]) {
+                out[cx] = cc[last];
+            }
+        }
+        for (int cx = 0; cx < hs.ncx; cx++)
+            if (out[cx] < 0) {
+                err = "case table: no case covers the grid";
+                return 1;
+            }
+        std::vector<CaseConst> C(nc);
+        for (int k = 0; k < nc; k++) {
+            const double g = hs.case_g[k];
+            const double xg = 7.0 * g / (hs.cs * hs.cs);
+            C[k].g = (float)g;
+            C[k].c1 = (float)(hs.rho0 * xg / 7.0);
+            C[k].c2 = (float)(-hs.rho0 * 3.0 / 49.0 * xg * xg);
+            C[k].pad = 0.f;
+            const double *b = &hs.case_box[4 * k];
+            C[k].box = BoxBits{ordered_bits_fold0(b[0]), ordered_bits_fold0(b[1]),
+                               ordered_bits_fold0(b[2]), ordered_bits_fold0(b[3])};
+        }
+        int rc;
+        if ((rc = alloc(&col_case_, hs.ncx, err)) || (rc = alloc(&cases_, nc, err))) return rc;
+        TSPH_CK(cudaMemcpy(col_case_, out.data(), 4 * (size_t)hs.ncx, cudaMemcpyHostToDevice));
+        TSPH_CK(cudaMemcpy(cases_, C.data(), sizeof(CaseConst) * (size_t)nc,
+                           cudaMemcpyHostToDevice));
+        cases_on_ = true;
+        tile_shape_ = 2;  // the pair-record kernel is the one that reads the table
+        return 0;
+    }
 
   public:
     // time every pair-kernel variant on the current particles (forces pass,
@@ -332,6 +401,12 @@ template <typename T> class Engine final : public EngineBase {
     static constexpr int kShapes = 3;
     int autotune(int *choice, double *us, std::string &err) override {
         TSPH_FRESH_P(err);
+        if (cases_on_) {  // packed cases: the pair-record kernel only
+            if (choice) *choice = 2;
+            if (us)
+                for (int k = 0; k < kShapes; k++) us[k] = 0;
+            return 0;
+        }
         // the FP64 build, boundary-integral walls and buffer zones use the
         // per-particle pair kernel: nothing to choose
         if (!std::is_same<T, float>::value || wall_model_ == 2 || zones_on_) {
@@ -650,6 +725,10 @@ template <typename T> class Engine final : public EngineBase {
             err = "tile shape must be 0, 1 or 2";
             return 1;
         }
+        if (cases_on_ && shape != 2) {
+            err = "packed cases: the pair-record kernel (shape 2) only";
+            return 1;
+        }
         tile_shape_ = shape;
         for (auto &g : graphs_) cudaGraphExecDestroy(g.second);
         graphs_.clear();
@@ -735,9 +814,11 @@ template <typename T> class Engine final : public EngineBase {
         if constexpr (std::is_same<T, float>::value) {
             int rc;
             if (!rec_setup_) {
-                const void *kr[3] = {(const void *)k_pairs_rec<MODE_FORCES, false, RecStd>,
+                const void *kr[5] = {(const void *)k_pairs_rec<MODE_FORCES, false, RecStd>,
                                      (const void *)k_pairs_rec<MODE_CORRECT, false, RecStd>,
-                                     (const void *)k_pairs_rec<MODE_LISTS, false, RecStd>};
+                                     (const void *)k_pairs_rec<MODE_LISTS, false, RecStd>,
+                                     (const void *)k_pairs_rec<MODE_FORCES, false, RecStd, true>,
+                                     (const void *)k_pairs_rec<MODE_CORRECT, false, RecStd, true>};
                 for (const void *k : kr)
                     TSPH_CK(cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
                                                  (int)cudaSharedmemCarveoutMaxShared));
@@ -751,10 +832,16 @@ template <typename T> class Engine final : public EngineBase {
             // MODE_CORRECT writes the new state into F_ in the kept order,
             // with its cell-relative positions and the next pass's records
             RecStep S{rec_list_, rec_cnt_, gen_, (const float2 *)lbin_, sig2_, F_.loc, rec_f_,
-                      need_sort_, cond_sort, capturing_ ? 1 : 0};
+                      need_sort_, cond_sort, capturing_ ? 1 : 0, col_case_, cases_};
             // the corrector's old state: F_ itself (the predictor leaves it
             // in place; the pass overwrites each row after reading it)
             const OldState<T> OF{F_.r, F_.v, F_.rho};
+            if constexpr (MODE != MODE_LISTS)  // (list building reads no case constant)
+                if (cases_on_)
+                    return launch(CAT_PAIR, k_pairs_rec<MODE, false, RecStd, true>, nchunks,
+                                  kRecT, err, X, fs, ws, W_, grid_, P_, Krec_, Krec_build_, OF, dt,
+                                  po, RX, rec_w_, (const WinRec *)rec_table_,
+                                  (const int *)rec_nwin_, S, health_);
             return launch(CAT_PAIR, k_pairs_rec<MODE, false, RecStd>, nchunks, kRecT, err, X, fs, ws,
                           W_, grid_, P_, Krec_, Krec_build_, OF, dt, po, RX, rec_w_,
                           (const WinRec *)rec_table_, (const int *)rec_nwin_, S, health_);
@@ -1033,7 +1120,8 @@ template <typename T> class Engine final : public EngineBase {
                 if ((r = launch(CAT_SORT, k_hist_kept<T>, blocks_for(nf_), kBlock, err,
                                 (const FluidState<T>)F_, keyB_, slotB_, counts_,
                                 (const uint8_t *)rm_cand_, (const uint32_t *)fstart_, grid_,
-                                make_box_bits(box_), health_, gate, runs)) ||
+                                make_box_bits(box_), health_, gate, runs,
+                                (const int32_t *)col_case_, (const CaseConst *)cases_)) ||
                     (r = launch(CAT_SORT, k_resolve_removal, 1, kResolveThreads, err, pk.rm, dead_,
                                 keyB_, slotB_, counts_, ncells_, health_, gate)) ||
                     (r = sort_finish(F_.r, F_.v, F_.rho, F_.id, nullptr, nullptr, nullptr, Fs_,
@@ -1228,6 +1316,18 @@ template <typename T> class Engine final : public EngineBase {
         if ((rc = alloc(&lbin_, nf_, err)) || (rc = alloc(&gen_, 4, err)) ||
             (rc = alloc(&need_sort_, 1, err)))
             return rc;
+        if (!hs.case_g.empty()) {
+            if constexpr (std::is_same<T, float>::value) {
+                if (!hs.zones.empty()) {
+                    err = "packed cases: no buffer zones";
+                    return 1;
+                }
+                if ((rc = setup_cases(hs, err))) return rc;
+            } else {
+                err = "packed cases: FP32 build only";
+                return 8;
+            }
+        }
         {
             const uint32_t g0[4] = {1u, 0u, 0u, 0u};  // no lists yet: stale
             TSPH_CK(cudaMemcpy(gen_, g0, 16, cudaMemcpyHostToDevice));
@@ -1470,6 +1570,10 @@ template <typename T> class Engine final : public EngineBase {
 
     int compute_forces(int model, std::string &err) override {
         TSPH_FRESH_P(err);
+        if (cases_on_) {
+            err = "packed cases: per-case gravity and removal boxes are applied by tsph_step only";
+            return 8;
+        }
         if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
@@ -1498,6 +1602,10 @@ template <typename T> class Engine final : public EngineBase {
 
     int corrector(double dt, std::string &err) override {
         TSPH_FRESH_P(err);
+        if (cases_on_) {
+            err = "packed cases: per-case gravity and removal boxes are applied by tsph_step only";
+            return 8;
+        }
         int rc = launch(CAT_OTHER, k_correct_inplace<T>, blocks_for(nw_ + nf_), kBlock, err, F_, O_,
                         (const uint32_t *)fstart_, ncells_, W_, nw_, (T)dt, P_.rho0);
         if (rc) return rc;
@@ -1510,6 +1618,10 @@ template <typename T> class Engine final : public EngineBase {
     // outside the box instead)
     int remove_out_of_domain(int *removed, std::string &err) override {
         TSPH_FRESH_P(err);
+        if (cases_on_) {
+            err = "packed cases: per-case gravity and removal boxes are applied by tsph_step only";
+            return 8;
+        }
         int rc;
         if (!zlive_ && ((rc = alloc(&zlive_, id_cap_, err)) || (rc = alloc(&zcand_, id_cap_, err))))
             return rc;
@@ -1557,6 +1669,10 @@ template <typename T> class Engine final : public EngineBase {
         if (!cells_ok()) {
             err = "cell lists are stale: call tsph_particle_to_cell first";
             return 3;
+        }
+        if (cases_on_ && model != 0) {
+            err = "packed cases: mDBC walls only";
+            return 8;
         }
         int rc;
         if (zones_on_) {

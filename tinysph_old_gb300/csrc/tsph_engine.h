@@ -29,6 +29,11 @@ struct HostSetup {
     // room for particles the inlets create
     std::vector<double> zones;
     int extra_rows = 65536, extra_ids = 1 << 20;
+    // cases packed into one system (tsph_set_cases): per case the x range
+    // [lo, hi) of its grid columns, its gravity, and its removal thresholds
+    // (x_lo, x_hi, y_lo, y_hi: removed when x < x_lo, x > x_hi, y < y_lo or
+    // y > y_hi); empty for a single case
+    std::vector<double> case_x, case_g, case_box;
 };
 
 struct Profile {

@@ -84,6 +84,8 @@ int tsph_write_vtk(tsph_system *s, const char *path) {
 
 int tsph_save_checkpoint(tsph_system *s, const char *path) {
     if (!s || !path) return io_fail(TSPH_ERR_ARG, "null argument");
+    if (!s->hs.case_g.empty())
+        return io_fail(TSPH_ERR_UNSUPPORTED, "checkpoints of packed cases are not written");
     // a system stepping with kept neighbour lists is re-binned first, so the
     // run that goes on and a run restarted from the file continue from the
     // same binning (and so bit for bit alike)

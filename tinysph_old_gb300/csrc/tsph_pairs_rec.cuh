@@ -74,6 +74,15 @@ typedef RecShape<528, 38> RecStd;
 // A pass builds when the count of sorts (gen[0], bumped by every sort)
 // differs from the sort the lists were built after (gen[1], set by the last
 // CTA of every pass).
+// Cases packed into one system (the batched workload): every case scaled to
+// the system's particle spacing, so that all SPH constants but gravity (and
+// the two Fourtakas coefficients that follow from it) are shared; each case
+// keeps its own removal box.  A grid column belongs to one case.
+struct CaseConst {
+    float g, c1, c2, pad;
+    BoxBits box;
+};
+
 struct RecStep {
     uint16_t *glist;            // [chunk][list][128]: entries (staged index << 2 | column)
     uint8_t *gcnt;              // [chunk][128]: entries, or 255 (did not fit: global path)
@@ -88,6 +97,10 @@ struct RecStep {
     uint32_t *need_sort;        // MODE_CORRECT: set when the cells must be rebuilt
     cudaGraphConditionalHandle cond_sort;
     int use_cond;
+    // packed cases (kernels instantiated with CASES): the case of each grid
+    // column and each case's constants
+    const int32_t *col_case = nullptr;
+    const CaseConst *cases = nullptr;
 };
 
 template <class SH> struct RecSmem {
@@ -104,7 +117,17 @@ template <class SH> struct RecSmem {
     WinRec win;
     __align__(16) uint8_t cnt[kRecT];  // stored list lengths of the chunk's targets
     unsigned long long bar;
+    // the window's case (kernels with CASES) and its pair constants
+    TileConst kc;
+    int kcase;
 };
+
+// the window's constants: the case's copy in shared memory, or the system's
+template <bool CASES, class A>
+__device__ __forceinline__ const A &rec_pick(const A &case_copy, const A &system) {
+    if constexpr (CASES) return case_copy;
+    else return system;
+}
 
 // ---------------------------------------------------------------- records
 // The windows of chunk c (targets [128 c, 128 c + 128) of the live rows): at
@@ -376,7 +399,7 @@ __device__ __forceinline__ void rec_store(uint16_t *__restrict__ gl, const uint1
     gpos += cnt;
 }
 
-template <int MODE, bool STORED_P, class SH>
+template <int MODE, bool STORED_P, class SH, bool CASES = false>
 __global__ void __launch_bounds__(kRecT, 8)
 k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
             const uint32_t *__restrict__ wstart, WallState<float> Wl, Grid g, Phys<float> P,
@@ -418,6 +441,13 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
             // stored lists (lists kept), all completing on the mbarrier
             const WinRec R = table[(size_t)blockIdx.x * kRecMaxWin + wi];
             sm.win = R;
+            if constexpr (CASES) {
+                const CaseConst C = S.cases[__ldg(S.col_case + R.cx)];
+                sm.kc = K;
+                sm.kc.c1 = C.c1;
+                sm.kc.c2 = C.c2;
+                sm.kcase = __ldg(S.col_case + R.cx);
+            }
             if (R.mode == kRecStaged) {
                 uint32_t bytes = (uint32_t)R.tot * 32u;
                 int at = 0;
@@ -484,6 +514,8 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
         float Ia = 0.f;
         int cxa = cx, cy = 0;
         bool global = mode != kRecStaged;
+        int tcase = 0;  // the target's case (kernels with CASES)
+        if constexpr (CASES) tcase = sm.kcase;
         const unsigned amask = __ballot_sync(0xffffffffu, active);  // the warp's targets
         if (mode == kRecStaged) {
             const bool ok = mbar_wait(&sm.bar, parity);
@@ -512,7 +544,8 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                     const int c = (int)sm.cnt[col_i];
                     if (c == 255) global = true;
                     else if (MODE != MODE_LISTS)
-                        rec_eval(sm, lst, c, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K, acc);
+                        rec_eval(sm, lst, c, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf,
+                                 rec_pick<CASES>(sm.kc, K), acc);
                 } else {
                     // phase 1 at radius Kb (2h + 2 sigma), the list stored
                     // segment by segment as it is summed
@@ -557,7 +590,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                                 rec_store(gl, lst, cnt, SH::list, gpos, over);
                                 if (MODE != MODE_LISTS)
                                     rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf,
-                                             K, acc);
+                                             rec_pick<CASES>(sm.kc, K), acc);
                                 w = lst;
                             }
                             w = rec_scan(sm.e, pl, pe, xd, ya, khf, Kb.four_h2, sgi == 3,
@@ -567,7 +600,8 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                     const int cnt = (int)((w - lst) / kRecT);
                     rec_store(gl, lst, cnt, SH::list, gpos, over);
                     if (MODE != MODE_LISTS)
-                        rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf, K, acc);
+                        rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf,
+                                 rec_pick<CASES>(sm.kc, K), acc);
                     S.gcnt[t0 + col_i] = over ? (uint8_t)255 : (uint8_t)gpos;
                 }
             }
@@ -588,13 +622,24 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
             Ia = rcp_approx(P.rho0 + sa);
             const float pa = STORED_P ? __ldg(F.p + i) : eos(sa, P);
             acc = Acc4{0.f, 0.f, 0.f, 0.f};
-            target_global<STORED_P>(F, fstart, wstart, Wl, g, P, K, i, cxa, cy, la, va, sa, pa * Ia,
-                                    Ia, K.two_rho0 + sa, acc);
+            if constexpr (CASES) {
+                // a global-path window may span several columns, and so
+                // several cases: the target's own column gives its case
+                tcase = __ldg(S.col_case + cxa);
+                TileConst Kt = K;
+                Kt.c1 = S.cases[tcase].c1;
+                Kt.c2 = S.cases[tcase].c2;
+                target_global<STORED_P>(F, fstart, wstart, Wl, g, P, Kt, i, cxa, cy, la, va, sa,
+                                        pa * Ia, Ia, K.two_rho0 + sa, acc);
+            } else {
+                target_global<STORED_P>(F, fstart, wstart, Wl, g, P, K, i, cxa, cy, la, va, sa,
+                                        pa * Ia, Ia, K.two_rho0 + sa, acc);
+            }
         }
         if (active) {
             const float mb = P.m * P.bwen_h;
             const float ax = acc.ax * mb;
-            const float ay = fmaf(acc.ay, mb, -P.g);
+            const float ay = fmaf(acc.ay, mb, -(CASES ? S.cases[tcase].g : P.g));
             const float drho = mb * fmaf(-P.k_psi, acc.diff, acc.cont);
             if constexpr (MODE == MODE_FORCES) {
                 F.a[i] = make_float2(ax, ay);
@@ -613,7 +658,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 reinterpret_cast<float2 *>(out.v)[i] = nv;
                 reinterpret_cast<float *>(out.rho)[i] = s_new;
                 bool resort = false;
-                if (out_of_domain_bits(rn, out.boxb)) {
+                if (out_of_domain_bits(rn, CASES ? S.cases[tcase].box : out.boxb)) {
                     // an erase candidate: its cell kept in case the erase
                     // skips it (the cell of every other particle is found by
                     // the sort, k_hist_kept, which runs only when some
@@ -680,7 +725,8 @@ k_hist_kept(FluidState<T> X, uint32_t *__restrict__ key, uint32_t *__restrict__ 
             uint32_t *__restrict__ counts, const uint8_t *__restrict__ cand,
             const uint32_t *__restrict__ fstart, Grid g, BoxBits box,
             uint32_t *__restrict__ health, const uint32_t *__restrict__ gate,
-            uint32_t *__restrict__ runs) {
+            uint32_t *__restrict__ runs, const int32_t *__restrict__ col_case,
+            const CaseConst *__restrict__ cases) {
     pdl_enter();
     if (gated_off(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -688,6 +734,8 @@ k_hist_kept(FluidState<T> X, uint32_t *__restrict__ key, uint32_t *__restrict__ 
     if (i >= n_live(fstart, g.ncells)) return;
     if (cand[X.id[i]]) return;
     const double2 r = X.r[i];
+    if (col_case)  // packed cases: the removal box of the particle's case
+        box = cases[__ldg(col_case + X.key[i] / (uint32_t)g.ncy)].box;
     uint32_t k;
     if (out_of_domain_bits(r, box)) {
         k = key[i];

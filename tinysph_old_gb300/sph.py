@@ -44,7 +44,7 @@ ABI_SYMBOLS = (
     "tsph_health", "tsph_kernel_launches", "tsph_fluid_totals", "tsph_set_profiling",
     "tsph_get_profile",
     "tsph_water_level", "tsph_point_fields", "tsph_water_front", "tsph_autotune",
-    "tsph_set_tile_shape", "tsph_get_tile_shape", "tsph_write_vtk", "tsph_save_checkpoint", "tsph_load_checkpoint",
+    "tsph_set_tile_shape", "tsph_get_tile_shape", "tsph_set_cases", "tsph_write_vtk", "tsph_save_checkpoint", "tsph_load_checkpoint",
     "tsph_export_graph", "tsph_apply_update", "tsph_window_check", "tsph_get_stream",
     "tsph_state_save", "tsph_state_restore", "tsph_gnn_n_params", "tsph_gnn_create",
     "tsph_gnn_destroy", "tsph_gnn_set_params", "tsph_gnn_get_params", "tsph_gnn_get_grads",
@@ -167,6 +167,7 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_autotune.argtypes = [P, P, P]
     L.tsph_set_tile_shape.argtypes = [P, I]
     L.tsph_get_tile_shape.argtypes = [P, P]
+    L.tsph_set_cases.argtypes = [P, I, P, P, P]
     L.tsph_write_vtk.argtypes = [P, C.c_char_p]
     L.tsph_export_graph.argtypes = [P, I, I] + [P] * 9 + [C.POINTER(C.c_int32)] * 2
     L.tsph_apply_update.argtypes = [P, P, D, D, D, I, I]
@@ -559,6 +560,17 @@ class ParticleSystem:
 
     def set_tile_shape(self, shape: int):
         _check(self._L.tsph_set_tile_shape(self._h, int(shape)))
+
+    def set_cases(self, x_range, gravity, removal):
+        """Cases packed into this system (tsph_set_cases): per case the x
+        range [lo, hi) of its columns, its gravity and its removal thresholds
+        (x_lo, x_hi, y_lo, y_hi); before particle_to_cell."""
+        xr = np.ascontiguousarray(x_range, dtype=np.float64).reshape(-1, 2)
+        g = np.ascontiguousarray(gravity, dtype=np.float64).reshape(-1)
+        bx = np.ascontiguousarray(removal, dtype=np.float64).reshape(-1, 4)
+        if not (len(xr) == len(g) == len(bx)):
+            raise ValueError("one x range, gravity and removal box per case")
+        _check(self._L.tsph_set_cases(self._h, len(g), _p(xr), _p(g), _p(bx)))
 
     @property
     def tile_shape(self) -> int:

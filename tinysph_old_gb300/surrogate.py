@@ -250,7 +250,7 @@ def generate(specs, t_end, samples_per_case, cases_per_system=25, k=K_STRIDE, lo
 
     out = []
     for c0 in range(0, len(specs), cases_per_system):
-        bt = B.Batch(specs[c0:c0 + cases_per_system], streams=False)
+        bt = B.GroupedBatch(specs[c0:c0 + cases_per_system], streams=False)
         for g in bt.groups:
             s, dt = g.system, g.dt
             nsteps = int(round(t_end / dt))
