@@ -144,6 +144,40 @@ def graph_kernel_split(s, model, dt, flush, stream, steps=20):
     return out
 
 
+def graph_timeline(s, model, dt, stream, steps):
+    """Start, duration and idle time before each kernel of `steps`
+    back-to-back replayed graph steps (CUPTI kernel records, microseconds
+    from the first kernel), or None without CUPTI."""
+    import torch
+
+    from tinysph_old_gb300 import timeline
+
+    try:
+        tl = timeline.Timeline()
+    except (FileNotFoundError, OSError):
+        return None
+    torch.cuda.synchronize()
+    try:
+        tl.start()
+    except RuntimeError:
+        return None
+    with torch.cuda.stream(stream):
+        s.step(model, dt, steps)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    tl.stop()
+    recs = [r for r in tl.records() if r[1] != 0]
+    if not recs:
+        return None
+    t0, last = recs[0][1], None
+    out = []
+    for name, st, en, _ in recs:
+        idle = 0.0 if last is None else max(0.0, (st - last) * 1e-3)
+        out.append([name, round((st - t0) * 1e-3, 2), round((en - st) * 1e-3, 2), round(idle, 2)])
+        last = en if last is None else max(last, en)
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -463,6 +497,7 @@ def run_batch(args, rank, world, local):
     e2e_value = n * args.e2e_steps / (time.perf_counter() - t0)
     health = s.health()
     shape_used = s.tile_shape
+    bt_cases, bt_dp = bt.cases, bt.dp
     s.close()
     del bt
     torch.cuda.empty_cache()
@@ -539,7 +574,7 @@ def run_batch(args, rank, world, local):
                "sample": f"3 time steps of each of the first 4 cases ({tot // 3} particles, "
                          f"{tt:.1f} s, FP64 C restatement, OpenMP)"}
     by_dp = {}
-    for c in bt.cases:
+    for c in bt_cases:
         k = f"{c.spec.kind} dp={c.spec.dp:g}"
         by_dp.setdefault(k, [0, 0])
         by_dp[k][0] += 1
@@ -553,7 +588,7 @@ def run_batch(args, rank, world, local):
         "config": {"workload": f"{len(specs)} cases (seed {args.seed}) in one particle system "
                                f"(case table: per-case scale, gravity and removal box), {n} "
                                "particles; one step = one time step of every case",
-                   "particles": n, "cases": by_dp, "system_dp": bt.dp,
+                   "particles": n, "cases": by_dp, "system_dp": bt_dp,
                    "l2": "inputs larger than L2 (no flush)", "parallelism": "single GPU"},
         "launches_per_step": timed_launches / args.steps,
         "grouped": grouped,
@@ -762,6 +797,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=0,
                     help="CPU baseline sample (0 = auto, ~10-30 s)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--timeline", type=int, default=0,
+                    help="add the kernel timeline of this many back-to-back graph steps")
     ap.add_argument("--tile-shape", default="auto", choices=["auto", "wide", "deep", "rec"],
                     help="pair-kernel variant: timed on the particles (auto) or fixed, "
                          "e.g. to profile one variant")
@@ -861,6 +898,7 @@ def main():
     # ---- the graph step split by kernel (CUPTI kernel records of replayed
     # graph steps, L2 flushed in between as in the timed loop)
     graph_split = graph_kernel_split(s, model, dt, flush, stream, steps=20)
+    timeline_recs = graph_timeline(s, model, dt, stream, args.timeline) if args.timeline else None
 
     # ---- per-kernel timing for the roofline: eager launches of the same
     # kernels, each bracketed by CUDA events on the system's stream
@@ -999,6 +1037,9 @@ def main():
                 **{k: prof[k] / prof_steps for k in ("pair_us", "sort_us", "mdbc_us",
                                                      "other_us")}},
             "autotune": tune,
+            **({"timeline": {"steps": args.timeline, "columns": ["kernel", "start_us",
+                                                                 "duration_us", "idle_before_us"],
+                             "records": timeline_recs}} if args.timeline else {}),
             "gpu_launches": int(timed_launches),
             "clocks": clocks.summary(),
             "health": health,
