@@ -134,3 +134,38 @@ def test_batch_in_one_system_matches_the_oracle_per_case(gpu_tsph, oracle_mod):
     ids = bt.case_state(1, st)["index"]
     assert out[0] not in ids and out[1] not in ids
     assert bt.system.np == sum(a.np for a in arrays) - 2
+
+
+@pytest.mark.gpu
+def test_case_table_rules(gpu_tsph, tmp_path):
+    """tsph_set_cases: FP32 only, non-empty ranges; on a system with a case
+    table the per-function force, corrector and removal calls and checkpoints
+    are refused (they would apply the system's gravity and box)."""
+    specs = [B.CaseSpec(B.DAM_BREAK, 0.004, 1.0, 0.4, 0.3),
+             B.CaseSpec(B.STILL_WATER, 0.002, 1.0, 0.4, 0.2)]
+    bt = B.Batch(specs)
+    s = bt.system
+    E = gpu_tsph.TsphError
+    for call in (lambda: s.compute_forces(gpu_tsph.WALL_MDBC), lambda: s.corrector(bt.dt),
+                 lambda: s.remove_out_of_domain(),
+                 lambda: s.save_checkpoint(str(tmp_path / "c.bin"))):
+        with pytest.raises(E) as e:
+            call()
+        assert e.value.status == gpu_tsph.ERR_UNSUPPORTED
+    with pytest.raises(E) as e:  # only the mDBC fused step reads the table
+        s.step(gpu_tsph.WALL_DBC, bt.dt, 1)
+    assert e.value.status == gpu_tsph.ERR_UNSUPPORTED
+    with pytest.raises(E) as e:
+        s.set_tile_shape(0)
+    assert e.value.status == gpu_tsph.ERR_ARG
+    a = B.case_arrays(specs[0])
+    f = gpu_tsph.ParticleSystem(a.h, a.kap, a.cs, 1000.0, 0.02, 0.1, a.spec.dp, a.domain, "fp32")
+    with pytest.raises(E) as e:  # an empty range
+        f.set_cases([[1.0, 1.0]], [9.81], [[0.0, 1.0, 0.0, 1.0]])
+    assert e.value.status == gpu_tsph.ERR_ARG
+    d = gpu_tsph.ParticleSystem(a.h, a.kap, a.cs, 1000.0, 0.02, 0.1, a.spec.dp, a.domain, "fp64")
+    with pytest.raises(E) as e:
+        d.set_cases([[0.0, 1.0]], [9.81], [[0.0, 1.0, 0.0, 1.0]])
+    assert e.value.status == gpu_tsph.ERR_UNSUPPORTED
+    s.step(bt.wall_model, bt.dt, 2)
+    assert s.health() == 0
