@@ -852,7 +852,7 @@ def main():
         s.set_tile_shape(sph.TILE_SHAPES[args.tile_shape])
         shape = sph.TILE_SHAPES[args.tile_shape]
     else:
-        # the autotuner's choice (median of 10 forces passes per variant)
+        # the autotuner's choice (median of 20 forces passes per variant)
         shape, tune_us = s.autotune()
         names = {v: k for k, v in sph.TILE_SHAPES.items()}
         tune = {"chosen": names.get(shape, str(shape)),

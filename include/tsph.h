@@ -347,7 +347,7 @@ typedef struct {
  *     stages each window's record ranges with bulk copies (528 staged
  *     neighbours, 38 list entries per target).
  * tsph_autotune times every variant on the current particles (a warm-up and
- * 10 timed forces passes each, the median kept; the state is left as it was)
+ * 20 timed forces passes each, the median kept; the state is left as it was)
  * and keeps the fastest; the first tsph_step does this by itself.
  * us (may be NULL) receives TSPH_N_TILE_SHAPES median times in microseconds.
  * No counterpart in the reference. */

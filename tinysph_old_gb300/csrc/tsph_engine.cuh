@@ -396,7 +396,7 @@ template <typename T> class Engine final : public EngineBase {
 
   public:
     // time every pair-kernel variant on the current particles (forces pass,
-    // a and drho saved and restored): a warm-up and 10 timed launches each,
+    // a and drho saved and restored): a warm-up and 20 timed launches each,
     // the median kept; the fastest wins.  FP32 build only.
     static constexpr int kShapes = 3;
     int autotune(int *choice, double *us, std::string &err) override {
@@ -426,7 +426,7 @@ template <typename T> class Engine final : public EngineBase {
             prof_ = false;
             TSPH_CK(cudaMemcpyAsync(Bv_, F_.a, sizeof(T2) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
             TSPH_CK(cudaMemcpyAsync(Brho_, F_.drho, sizeof(T) * (size_t)nf_, cudaMemcpyDeviceToDevice, st_));
-            constexpr int kReps = 10;
+            constexpr int kReps = 20;
             std::vector<cudaEvent_t> evs(kReps + 1);
             for (auto &e : evs) e = ev();
             double med[kShapes] = {0, 0, 0};

@@ -52,10 +52,12 @@ enum { kRecStaged = 0, kRecGlobal = 1 };
 
 // One window of a chunk (written by k_pair_records, read by k_pairs_rec):
 // targets [cur, we) in rows rlo+1.. of column cx, staged rows [rlo, rlo+nr);
-// segment s (walls, fluid of columns cx-1, cx, cx+1) is staged from the
-// 4-aligned global row first[s], n[s] rows (a multiple of 4).
+// segment s (walls, fluid of columns cx-1, cx, cx+1) is staged from global
+// row first[s], n[s] rows.  lrows: the entries of the longest stored list of
+// the window's targets (set by the pass that builds the lists; -1: not known,
+// the whole list block), the rows of the list block a later pass copies.
 struct __align__(16) WinRec {
-    int cur, we, cx, rlo, nr, mode, tot, pad;
+    int cur, we, cx, rlo, nr, mode, tot, lrows;
     int first[6];
     int n[6];
 };
@@ -120,6 +122,7 @@ template <class SH> struct RecSmem {
     // the window's case (kernels with CASES) and its pair constants
     TileConst kc;
     int kcase;
+    int lmax;  // the longest list stored in this window (a pass that builds them)
 };
 
 // the window's constants: the case's copy in shared memory, or the system's
@@ -201,7 +204,7 @@ __device__ __forceinline__ void rec_window_table(int c, int cap, const FluidStat
         R.we = we;
         R.cx = cx;
         R.tot = tot;
-        R.pad = 0;
+        R.lrows = -1;
         table[(size_t)c * kRecMaxWin + nwc] = R;
         nwc++;
         cur = we;
@@ -433,9 +436,13 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
         fence_mbar_init();
     }
     uint32_t parity = 0u;
+    // a pass that builds the lists records, per window, its longest list
+    WinRec *const table_w = const_cast<WinRec *>(table) + (size_t)blockIdx.x * kRecMaxWin;
     for (int wi = 0; wi < nw; wi++) {
         __syncthreads();  // the previous window is finished with shared memory
         if (tid == 0) {
+            if (build && wi > 0) table_w[wi - 1].lrows = sm.lmax;
+            sm.lmax = 0;
             // the window's record, then one bulk copy per record array and
             // segment, per offset run (lists built here) or of the chunk's
             // stored lists (lists kept), all completing on the mbarrier
@@ -462,7 +469,8 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                         if (col >= 0 && col < g.ncx) bytes += 2u * 4u * (uint32_t)kRecOffRun;
                     }
                 }
-                if (lists) bytes += (uint32_t)(SH::list * kRecT * 2 + kRecT);
+                const int lr = R.lrows < 0 ? SH::list : R.lrows;  // list rows to copy
+                if (lists) bytes += (uint32_t)(lr * kRecT * 2 + kRecT);
                 fence_proxy_async_smem();  // the previous window's reads before the copies
                 mbar_expect_tx(&sm.bar, bytes);
                 at = 0;
@@ -488,7 +496,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                     }
                 }
                 if (lists) {
-                    bulk_g2s(sm.list, gblock, (uint32_t)(SH::list * kRecT * 2), &sm.bar);
+                    if (lr > 0) bulk_g2s(sm.list, gblock, (uint32_t)(lr * kRecT * 2), &sm.bar);
                     bulk_g2s(sm.cnt, S.gcnt + t0, (uint32_t)kRecT, &sm.bar);
                 }
             }
@@ -603,6 +611,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                         rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf,
                                  rec_pick<CASES>(sm.kc, K), acc);
                     S.gcnt[t0 + col_i] = over ? (uint8_t)255 : (uint8_t)gpos;
+                    if (!over) atomicMax(&sm.lmax, gpos);
                 }
             }
         } else if (active && build) {
@@ -690,6 +699,10 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                 }
             }
         }
+    }
+    if (build) {  // the last window's longest list
+        __syncthreads();
+        if (tid == 0 && nw > 0) table_w[nw - 1].lrows = sm.lmax;
     }
     finish();
 }
