@@ -221,8 +221,9 @@ int tsph_set_zone_capacity(tsph_system *s, int extra_rows, int extra_ids);
  * constants are the system's for every case; gravity scales with
  * 1/lambda_k and stays per case, as does RemoveParticlesOutOfDomain's box
  * (src/SPH_btdebug.h:4-31).  Per case k: x_range[2k..2k+1] = [lo, hi), the x
- * range of its grid columns (cases do not share a column; a column between
- * ranges goes to the nearest case), gravity[k], and removal[4k..4k+3] =
+ * range of its grid columns (disjoint ranges: cases do not share a column;
+ * a column between ranges goes to the nearest case), gravity[k], and
+ * removal[4k..4k+3] =
  * (x_lo, x_hi, y_lo, y_hi): a fluid particle is erased when x < x_lo,
  * x > x_hi, y < y_lo or y > y_hi (the reference's thresholds, eps included,
  * in the system's frame).  Call after tsph_add_particles, before

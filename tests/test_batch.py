@@ -163,6 +163,10 @@ def test_case_table_rules(gpu_tsph, tmp_path):
     with pytest.raises(E) as e:  # an empty range
         f.set_cases([[1.0, 1.0]], [9.81], [[0.0, 1.0, 0.0, 1.0]])
     assert e.value.status == gpu_tsph.ERR_ARG
+    with pytest.raises(E) as e:  # two cases sharing columns
+        f.set_cases([[0.0, 1.0], [0.5, 2.0]], [9.81, 9.81],
+                    [[0.1, 0.9, 0.0, 1.0], [0.6, 1.9, 0.0, 1.0]])
+    assert e.value.status == gpu_tsph.ERR_ARG
     d = gpu_tsph.ParticleSystem(a.h, a.kap, a.cs, 1000.0, 0.02, 0.1, a.spec.dp, a.domain, "fp64")
     with pytest.raises(E) as e:
         d.set_cases([[0.0, 1.0]], [9.81], [[0.0, 1.0, 0.0, 1.0]])

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstring>
 #include <memory>
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -354,6 +355,14 @@ int tsph_set_cases(tsph_system *s, int ncases, const double *x_range, const doub
         if (!(x_range[2 * k] < x_range[2 * k + 1]) || !(removal[4 * k] < removal[4 * k + 1]) ||
             !(removal[4 * k + 2] < removal[4 * k + 3]))
             return fail(TSPH_ERR_ARG, "tsph_set_cases: empty range of case " + std::to_string(k));
+    {  // cases do not share columns: their x ranges are disjoint
+        std::vector<std::pair<double, double>> xr((size_t)ncases);
+        for (int k = 0; k < ncases; k++) xr[k] = {x_range[2 * k], x_range[2 * k + 1]};
+        std::sort(xr.begin(), xr.end());
+        for (int k = 1; k < ncases; k++)
+            if (xr[k].first < xr[k - 1].second)
+                return fail(TSPH_ERR_ARG, "tsph_set_cases: the x ranges of two cases overlap");
+    }
     s->hs.case_x.assign(x_range, x_range + 2 * (size_t)ncases);
     s->hs.case_g.assign(gravity, gravity + (size_t)ncases);
     s->hs.case_box.assign(removal, removal + 4 * (size_t)ncases);
