@@ -145,7 +145,12 @@ int tsph_divide_to_cells(tsph_system *s);
 /* Clear_cells, src/SPH_find_pairs.h:74-92 (marks the cell lists stale) */
 int tsph_clear_cells(tsph_system *s);
 /* Particle_To_Cell, src/SPH_find_pairs.h:45-72: GPU counting sort by cell
- * (exact FP64 cell index, histogram, scan, stable scatter, SoA reorder). */
+ * (exact FP64 cell index, histogram, scan, stable scatter, SoA reorder).
+ * On an FP32 system stepping with kept cells (the pair-record step) and
+ * binned before, the cells and neighbour lists are kept when every particle
+ * is within the skin of where it was binned (the decision is taken on the
+ * device; the sort runs only when needed); the cell lists are then exact
+ * again for every call that reads them (tsph_get_cells re-bins first). */
 int tsph_particle_to_cell(tsph_system *s);
 /* cells[c].cp as CSR in the reference's numbering: cell c holds
  * cell_list[cell_start[c] .. cell_start[c+1]), ascending particle index.

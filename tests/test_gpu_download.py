@@ -76,10 +76,10 @@ def test_download_async_with_erased_particles_and_bad_fields(gpu_tsph):
 @pytest.mark.parametrize("precision", ["fp32", "fp64"])
 def test_staged_upload_matches_the_synchronous_one(gpu_tsph, precision):
     """tsph_upload_async + tsph_particle_to_cell leaves the state that
-    tsph_upload + tsph_particle_to_cell leaves, also when the upload is
-    staged while a step is in flight and the previous result is still being
-    read back; between staging and binning only downloads of the
-    asynchronous kind are accepted."""
+    tsph_upload + tsph_particle_to_cell leaves (FP64 bit for bit, FP32 to
+    rounding), also when the upload is staged while a step is in flight and
+    the previous result is still being read back; between staging and
+    binning only downloads of the asynchronous kind are accepted."""
     torch = pytest.importorskip("torch")
     case = cases.dam_break_mdbc(dp=0.01)
     a = gpu_tsph.ParticleSystem.from_case(case, precision)
@@ -121,7 +121,14 @@ def test_staged_upload_matches_the_synchronous_one(gpu_tsph, precision):
     got = a.download()
     assert a.health() == 0
     for f in ("r", "v", "rho", "p", "a"):
-        assert np.array_equal(got[f], want[f]), f
+        if precision == "fp64":
+            assert np.array_equal(got[f], want[f]), f
+        else:
+            # the FP32 pair-record step keeps a's cells (every particle within
+            # sigma of where a binned it) while b bins afresh: the pair sums
+            # run in another order, equal to FP32 rounding
+            d = float(np.max(np.abs(got[f] - want[f])))
+            assert d <= 1e-5 * max(1.0, float(np.max(np.abs(want[f])))), (f, d)
 
 
 @pytest.mark.gpu
@@ -142,3 +149,44 @@ def test_staged_upload_with_erased_particles_is_dropped(gpu_tsph):
     assert s.health() & gpu_tsph.HEALTH_UPLOAD
     after = s.download()
     assert np.array_equal(after["r"], before["r"]) and n == s.np
+
+
+@pytest.mark.gpu
+def test_binning_after_an_upload_keeps_cells_within_sigma(gpu_tsph):
+    """On the FP32 pair-record step, Particle_To_Cell after an upload keeps
+    the cells and lists when every particle is within sigma of where it was
+    binned: uploading a system's own state changes nothing (the next steps
+    are bit for bit those of the system left alone).  A particle moved
+    further re-bins the state (gated on the device's check): the exact cell
+    lists then equal a fresh system's, and stepping goes on healthily."""
+    case = cases.dam_break_mdbc(dp=0.01)
+    a = gpu_tsph.ParticleSystem.from_case(case, "fp32")
+    b = gpu_tsph.ParticleSystem.from_case(case, "fp32")
+    for s in (a, b):
+        s.set_tile_shape(2)
+        s.step(case.wall_model, case.dt, 6)
+    mask = gpu_tsph.F_R | gpu_tsph.F_V | gpu_tsph.F_A | gpu_tsph.F_RHO | gpu_tsph.F_DRHO
+    st = a.download()
+    bufs = {k: np.ascontiguousarray(st[k]) for k in ("r", "v", "a", "rho", "drho")}
+    a.upload_async(mask, **{k: v.ctypes.data for k, v in bufs.items()})
+    a.particle_to_cell()
+    a.step(case.wall_model, case.dt, 4)
+    b.step(case.wall_model, case.dt, 4)
+    ga, gb = a.download(), b.download()
+    for f in ("r", "v", "a", "rho", "drho", "p"):
+        assert np.array_equal(ga[f], gb[f]), f
+    # one fluid particle moved half a spacing: re-binned
+    r = ga["r"].copy()
+    k = int(np.flatnonzero(ga["type"] == 0)[17])
+    r[k, 0] += 0.5 * case.dp
+    r = np.ascontiguousarray(r)
+    a.upload_async(gpu_tsph.F_R, r=r.ctypes.data)
+    a.particle_to_cell()
+    c = gpu_tsph.ParticleSystem.from_case(case, "fp32")
+    c.upload(r=r)
+    c.particle_to_cell()
+    sa, la = a.get_cells()
+    sc, lc = c.get_cells()
+    assert np.array_equal(sa, sc) and np.array_equal(la, lc)
+    a.step(case.wall_model, case.dt, 3)
+    assert a.health() == 0

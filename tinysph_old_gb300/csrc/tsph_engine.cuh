@@ -318,6 +318,8 @@ template <typename T> class Engine final : public EngineBase {
     uint8_t *rec_cnt_ = nullptr;
     uint32_t *gen_ = nullptr;     // {sorts, sort the lists were built after, -, CTAs done}
     uint32_t *need_sort_ = nullptr;
+    uint32_t *pc_gate_ = nullptr;  // set when an applied upload cannot keep the cells
+    bool binned_ = false;          // a binning has formed lbin_ and the lists
     float sig2_ = 0.f;
     bool cells_kept_ = false;     // F_ moved since its binning (within sigma)
     long long rec_passes_ = 0;    // kept-list pair passes run (host count)
@@ -900,7 +902,7 @@ template <typename T> class Engine final : public EngineBase {
     // cell lists, pair digests)
     int ensure_exact_cells(std::string &err) {
         if (!cells_kept_) return 0;
-        return particle_to_cell(err);
+        return bin_particles(err, false);
     }
 
   public:
@@ -1314,7 +1316,7 @@ template <typename T> class Engine final : public EngineBase {
                 return rc;
         }
         if ((rc = alloc(&lbin_, nf_, err)) || (rc = alloc(&gen_, 4, err)) ||
-            (rc = alloc(&need_sort_, 1, err)))
+            (rc = alloc(&need_sort_, 1, err)) || (rc = alloc(&pc_gate_, 1, err)))
             return rc;
         if (!hs.case_g.empty()) {
             if constexpr (std::is_same<T, float>::value) {
@@ -1508,24 +1510,59 @@ template <typename T> class Engine final : public EngineBase {
     bool cells_valid() const override { return cells_; }
     void invalidate_cells() override { cells_ = false; }
 
-    int particle_to_cell(std::string &err) override {
+    int particle_to_cell(std::string &err) override { return bin_particles(err, true); }
+
+    // Particle_To_Cell.  With `allow_keep`, on a system whose fused step keeps
+    // its cells (the pair-record step) and was binned before, the state (an
+    // upload applied in the kept order) keeps its cells and lists when every
+    // particle is still within sigma of where it was binned, as a step would:
+    // the re-binning below then runs gated on the device flag that the check
+    // sets (no host round trip), and the cells count as kept (calls that need
+    // exact cells re-bin first).  Without it (exact cells asked for), the
+    // state is re-binned.
+    int bin_particles(std::string &err, bool allow_keep) {
         TSPH_FRESH_P(err);
         int rc;
+        const uint32_t *gate = nullptr;
+        bool kept = false;
+        if constexpr (std::is_same<T, float>::value)
+            if (allow_keep && binned_ && rec_f_.e && tile_shape_ == 2 && skin_ > 0.f &&
+                wall_model_ != 2 && !zones_on_) {
+                if ((rc = apply_staged_upload(err))) return rc;
+                TSPH_CK(cudaMemsetAsync(pc_gate_, 0, 4, st_));
+                if ((rc = launch(CAT_OTHER, k_upload_keep, blocks_for(nw_ + nf_), kBlock, err, F_,
+                                 (const uint32_t *)fstart_, W_, nw_, grid_, P_,
+                                 (const float2 *)lbin_, sig2_, (const uint32_t *)gen_, rec_f_,
+                                 rec_w_, pc_gate_)))
+                    return rc;
+                gate = pc_gate_;
+                kept = true;
+            }
         if ((rc = apply_staged_upload(err))) return rc;
         if ((rc = zero_counts(err))) return rc;
         const int *nptr = reinterpret_cast<const int *>(fstart_ + ncells_);
         if ((rc = launch(CAT_SORT, k_bin_keep_dead, blocks_for(nf_), kBlock, err,
                          (const double2 *)F_.r, (const uint32_t *)F_.key, nptr, grid_, keyB_, slotB_,
-                         counts_, health_)))
+                         counts_, health_, gate)))
             return rc;
         // gather everything into Fs_ (+ old state into B), then copy back
         if ((rc = sort_finish(F_.r, F_.v, F_.rho, F_.id, F_.a, F_.drho, F_.p, Fs_, O_.r, O_.v,
-                              O_.rho, OldState<T>{Br_, Bv_, Brho_}, err, nullptr, F_.type)))
+                              O_.rho, OldState<T>{Br_, Bv_, Brho_}, err, gate, F_.type)))
             return rc;
         if ((rc = launch(CAT_SORT, k_copy_state<T>, blocks_for(nf_), kBlock, err, F_,
                          (const FluidState<T>)Fs_, O_, OldState<T>{Br_, Bv_, Brho_},
-                         (const uint32_t *)fstart_, ncells_)))
+                         (const uint32_t *)fstart_, ncells_, gate)))
             return rc;
+        if (kept) {
+            // the records and window table of the new order when it was
+            // re-binned; its lists are then stale (a sort bumped the count),
+            // and the first pass of the next step builds them
+            if ((rc = pair_records(F_, gate, false, err))) return rc;
+            cells_ = true;
+            cells_kept_ = true;  // kept, or re-binned: settled when exact cells are asked for
+            exported_ = false;
+            return collect_profile(err);
+        }
         // pair records and window table of the new order (FP32 build); with
         // kept lists (the fused step over pair records) also the lists of
         // the new order, built at the binned positions, so that the next
@@ -1534,6 +1571,7 @@ template <typename T> class Engine final : public EngineBase {
         if ((rc = build_lists(err))) return rc;
         cells_ = true;
         cells_kept_ = false;
+        binned_ = true;
         exported_ = false;
         return collect_profile(err);
     }

@@ -167,8 +167,10 @@ __device__ __forceinline__ bool gated_off(const uint32_t *gate) {
 static __global__ void k_bin_keep_dead(const double2 *__restrict__ r, const uint32_t *__restrict__ old_key,
                                 const int *__restrict__ n_ptr, Grid g,
                                 uint32_t *__restrict__ key, uint32_t *__restrict__ slot,
-                                uint32_t *__restrict__ counts, uint32_t *__restrict__ health) {
+                                uint32_t *__restrict__ counts, uint32_t *__restrict__ health,
+                                const uint32_t *__restrict__ gate) {
     pdl_enter();
+    if (gated_off(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= *n_ptr) return;
     uint32_t k;
@@ -1483,8 +1485,10 @@ __device__ __forceinline__ void predict_keep_fluid_f32(
 // per array over the whole capacity
 template <typename T>
 __global__ void k_copy_state(FluidState<T> D, FluidState<T> S, OldState<T> O, OldState<T> B,
-                             const uint32_t *__restrict__ fstart, int ncells) {
+                             const uint32_t *__restrict__ fstart, int ncells,
+                             const uint32_t *__restrict__ gate) {
     pdl_enter();
+    if (gated_off(gate)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= (int)__ldg(fstart + ncells + 1)) return;
     D.r[i] = S.r[i];

@@ -727,6 +727,42 @@ k_lbin_records(PairRec R, const float2 *__restrict__ lbin, const uint32_t *__res
     e[2] = row;
 }
 
+// An uploaded state applied in the current (kept) order: every fluid row's
+// position relative to its kept cell and its pair records are formed from
+// the uploaded fields, the walls' records from their uploaded densities, and
+// `flag` is set when the kept cells cannot stay: a particle more than sigma
+// from where it was binned (or not finite), or lists not built after the
+// last binning.  The re-binning kernels that follow are gated on `flag`.
+static __global__ void __launch_bounds__(kBlock)
+k_upload_keep(FluidState<float> F, const uint32_t *__restrict__ fstart, WallState<float> Wl,
+              int nw, Grid g, Phys<float> P, const float2 *__restrict__ lbin, float sig2,
+              const uint32_t *__restrict__ gen, PairRec RF, PairRec RW,
+              uint32_t *__restrict__ flag) {
+    pdl_enter();
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < nw) {
+        wall_record(RW, i, Wl.rho[i], P);
+        return;
+    }
+    const int f = i - nw;
+    if (f == 0 && __ldg(gen) != __ldg(gen + 1)) *flag = 1u;
+    if (f >= n_live(fstart, g.ncells)) return;
+    const uint32_t key = F.key[f];
+    if (key >= (uint32_t)g.ncells) return;  // a removed row
+    const int cx = (int)(key / (uint32_t)g.ncy);
+    const int cy = (int)key - cx * g.ncy;
+    const float2 ln = cell_local(g, F.r[f], cx, cy);
+    F.loc[f] = ln;
+    const float2 lb = lbin[f];
+    const float ex = ln.x - lb.x, ey = ln.y - lb.y;
+    if (!(fmaf(ex, ex, ey * ey) <= sig2)) *flag = 1u;
+    const float s = F.rho[f];
+    const float2 v = F.v[f];
+    const float ib = rcp_approx(P.rho0 + s);
+    RF.e[f] = make_float4(ln.x, ln.y, (float)cy, ib);
+    RF.v[f] = make_float4(v.x, v.y, s, eos(s, P) * ib);
+}
+
 // the sort of a kept-order state (when some particle left its kept cell's
 // reach, or the domain): the cell of every particle at its new position (the
 // kept cell as the starting guess) and its histogram slot, except the erase
