@@ -178,6 +178,45 @@ def graph_timeline(s, model, dt, stream, steps):
     return out
 
 
+def measure_forms(plain_value):
+    """The batched and surrogate forms of the metric, each run as its own
+    bench process (shorter runs than their own workloads' defaults), against
+    this run's plain step: {"batched": {...}, "surrogate": {...}}."""
+    runs = {
+        "batched": ["--workload", "batch", "--steps", "30", "--warmup", "3", "--no-cpu",
+                    "--loop-steps", "0", "--e2e-steps", "2"],
+        "surrogate": ["--workload", "surrogate", "--steps", "50", "--warmup", "2", "--no-cpu",
+                      "--e2e-steps", "2"],
+    }
+    out = {}
+    for name, extra in runs.items():
+        try:
+            res = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *extra],
+                                 capture_output=True, text=True, timeout=600, cwd=ROOT)
+            lines = [ln for ln in res.stdout.splitlines() if ln.startswith("{")]
+            if res.returncode != 0 or not lines:
+                out[name] = {"error": (res.stderr or "no result line").strip()[-300:]}
+                continue
+            d = json.loads(lines[-1])
+        except (subprocess.TimeoutExpired, OSError, ValueError) as e:
+            out[name] = {"error": str(e)[:300]}
+            continue
+        f = {"value": d.get("value"), "unit": d.get("unit"), "ms_per_step": d.get("ms_per_step"),
+             "over_plain": d["value"] / plain_value if d.get("value") else None,
+             "workload": d.get("config", {}).get("workload")}
+        if name == "batched":
+            f["launches_per_step"] = d.get("launches_per_step")
+            f["grouped"] = (d.get("grouped") or {}).get("value")
+            f["front_error"] = ("per case against the oracle and against separate plain runs to "
+                                "FP32 rounding (tests/test_batch.py)")
+        else:
+            f["fallback_rate"] = d.get("fallback_rate")
+            f["plain_same_loop"] = (d.get("plain") or {}).get("value")
+            f["front_error_end"] = d.get("front_error_end")
+        out[name] = f
+    return out
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -526,11 +565,12 @@ def run_batch(args, rank, world, local):
         g.system.close()
     del gb
     torch.cuda.empty_cache()
-    # the plain path looped over the cases: each case alone, one system at a time
+    # the plain path looped over the cases: each case alone, one system at a
+    # time (--loop-steps 0 leaves it out)
     loop_ms = 0.0
     loop_half = 0.0
     st0 = torch.cuda.Stream()
-    for spec in specs:
+    for spec in (specs if args.loop_steps > 0 else []):
         a = B.case_arrays(spec)
         c = sph.ParticleSystem(a.h, a.kap, a.cs, 1000.0, 0.02, 0.1, spec.dp, a.domain, "fp32",
                                stream=st0.cuda_stream)
@@ -547,7 +587,7 @@ def run_batch(args, rank, world, local):
         loop_ms += case_ms
         loop_half += round(0.5 / a.dt) * case_ms / 1000.0
         c.close()
-    looped_value = n / (loop_ms / 1000.0)
+    looped_value = n / (loop_ms / 1000.0) if loop_ms > 0 else None
     cpu = None
     if not args.no_cpu:
         sys.path.insert(0, os.path.join(ROOT, "oracle"))
@@ -593,7 +633,8 @@ def run_batch(args, rank, world, local):
         "launches_per_step": timed_launches / args.steps,
         "grouped": grouped,
         "looped": {"value": looped_value, "unit": "particle-steps/s",
-                   "ms_per_step": loop_ms, "speedup_batched": value / looped_value,
+                   "ms_per_step": loop_ms,
+                   "speedup_batched": value / looped_value if looped_value else None,
                    "how": "each case alone in its own system, CUDA-graph steps, one after another"},
         "projected_s_to_0.5s_physical": {"batched": t_half, "looped": loop_half,
                                          "note": "batched: until the finest cases reach 0.5 s "
@@ -797,6 +838,8 @@ def main():
     ap.add_argument("--cpu-steps", type=int, default=0,
                     help="CPU baseline sample (0 = auto, ~10-30 s)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="leave out the batched and surrogate forms measured beside the plain step")
     ap.add_argument("--timeline", type=int, default=0,
                     help="add the kernel timeline of this many back-to-back graph steps")
     ap.add_argument("--tile-shape", default="auto", choices=["auto", "wide", "deep", "rec"],
@@ -1047,6 +1090,8 @@ def main():
         }
         if cpu:
             line["cpu_baseline"] = cpu
+        if not args.no_forms and world == 1:
+            line["forms"] = measure_forms(value)
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
