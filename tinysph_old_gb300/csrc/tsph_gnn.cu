@@ -815,21 +815,35 @@ __global__ void __launch_bounds__(kGB) k_inf_edge(GraphDev G, const bf16 *__rest
     const int d = G.deg[i];
     const double2 ri = G.pos[i];
     const float2 vi = G.vel[i];
+    // kEdgeU neighbours' Q rows are gathered before any is used, so a warp
+    // keeps that many L2 round trips in flight; the sums still run in
+    // neighbour order
+    constexpr int kEdgeU = 4;
     for (int k0 = 0; k0 < d; k0 += 32) {
         const EdgeLane mine = edge_lane(G, i, ri, vi, k0 + lane);
         const int cnt = min(32, d - k0);
-        for (int tt = 0; tt < cnt; tt++) {
-            const int j = __shfl_sync(0xffffffffu, mine.j, tt);
-            const float2 qj = unpack_bf16(*reinterpret_cast<const uint32_t *>(Q + (size_t)j * H + c0));
-            float z0 = pi.x + qj.x, z1 = pi.y + qj.y;
+        for (int tt = 0; tt < cnt; tt += kEdgeU) {
+            uint32_t qv[kEdgeU];
 #pragma unroll
-            for (int q = 0; q < EIN; q++) {
-                const float eq = __shfl_sync(0xffffffffu, mine.e[q], tt);
-                z0 = fmaf(w0[q], eq, z0);
-                z1 = fmaf(w1[q], eq, z1);
+            for (int u = 0; u < kEdgeU; u++) {
+                const int j = __shfl_sync(0xffffffffu, mine.j, (tt + u) & 31);
+                qv[u] = tt + u < cnt ? *reinterpret_cast<const uint32_t *>(Q + (size_t)j * H + c0)
+                                     : 0u;
             }
-            s0 += silu_hw(z0);
-            s1 += silu_hw(z1);
+#pragma unroll
+            for (int u = 0; u < kEdgeU; u++) {
+                if (tt + u >= cnt) break;  // (warp-uniform)
+                const float2 qj = unpack_bf16(qv[u]);
+                float z0 = pi.x + qj.x, z1 = pi.y + qj.y;
+#pragma unroll
+                for (int q = 0; q < EIN; q++) {
+                    const float eq = __shfl_sync(0xffffffffu, mine.e[q], tt + u);
+                    z0 = fmaf(w0[q], eq, z0);
+                    z1 = fmaf(w1[q], eq, z1);
+                }
+                s0 += silu_hw(z0);
+                s1 += silu_hw(z1);
+            }
         }
     }
     *reinterpret_cast<uint32_t *>(S + (size_t)i * H + c0) = pack_bf16(s0, s1);
