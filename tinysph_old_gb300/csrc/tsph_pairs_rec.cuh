@@ -125,12 +125,6 @@ template <class SH> struct RecSmem {
     int lmax;  // the longest list stored in this window (a pass that builds them)
 };
 
-// the window's constants: the case's copy in shared memory, or the system's
-template <bool CASES, class A>
-__device__ __forceinline__ const A &rec_pick(const A &case_copy, const A &system) {
-    if constexpr (CASES) return case_copy;
-    else return system;
-}
 
 // ---------------------------------------------------------------- records
 // The windows of chunk c (targets [128 c, 128 c + 128) of the live rows): at
@@ -503,6 +497,13 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
         }
         __syncthreads();  // the window's record is visible
         const int cur = sm.win.cur, we = sm.win.we, cx = sm.win.cx, rlo = sm.win.rlo;
+        // the window's pair constants: the system's, with the case's two
+        // gravity-dependent coefficients in registers (kernels with CASES)
+        TileConst Kw = K;
+        if constexpr (CASES) {
+            Kw.c1 = sm.kc.c1;
+            Kw.c2 = sm.kc.c2;
+        }
         const int mode = sm.win.mode;
         const int i = cur + tid;
         const bool active = i < we;
@@ -553,7 +554,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                     if (c == 255) global = true;
                     else if (MODE != MODE_LISTS)
                         rec_eval(sm, lst, c, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf,
-                                 rec_pick<CASES>(sm.kc, K), acc);
+                                 Kw, acc);
                 } else {
                     // phase 1 at radius Kb (2h + 2 sigma), the list stored
                     // segment by segment as it is summed
@@ -598,7 +599,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                                 rec_store(gl, lst, cnt, SH::list, gpos, over);
                                 if (MODE != MODE_LISTS)
                                     rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf,
-                                             rec_pick<CASES>(sm.kc, K), acc);
+                                             Kw, acc);
                                 w = lst;
                             }
                             w = rec_scan(sm.e, pl, pe, xd, ya, khf, Kb.four_h2, sgi == 3,
@@ -609,7 +610,7 @@ k_pairs_rec(FluidState<float> F, const uint32_t *__restrict__ fstart,
                     rec_store(gl, lst, cnt, SH::list, gpos, over);
                     if (MODE != MODE_LISTS)
                         rec_eval(sm, lst, cnt, xa, yca, rowa, va, sa, Pa, Ia, Ra2, khf,
-                                 rec_pick<CASES>(sm.kc, K), acc);
+                                 Kw, acc);
                     S.gcnt[t0 + col_i] = over ? (uint8_t)255 : (uint8_t)gpos;
                     if (!over) atomicMax(&sm.lmax, gpos);
                 }
