@@ -319,6 +319,7 @@ template <typename T> class Engine final : public EngineBase {
     uint32_t *gen_ = nullptr;     // {sorts, sort the lists were built after, -, CTAs done}
     uint32_t *need_sort_ = nullptr;
     uint32_t *pc_gate_ = nullptr;  // set when an applied upload cannot keep the cells
+    int sm_count_ = 152;           // the device's SMs (grid shapes)
     bool binned_ = false;          // a binning has formed lbin_ and the lists
     float sig2_ = 0.f;
     bool cells_kept_ = false;     // F_ moved since its binning (within sigma)
@@ -1019,11 +1020,14 @@ template <typename T> class Engine final : public EngineBase {
             if constexpr (std::is_same<T, float>::value) {
                 if (mdbc_fused) {
                     const int nbm = blocks_for((long long)nw_ * kMdbcLanes);
+                    // walls needing more than one wave (4 blocks per SM)
+                    // share their waves with the predictor's blocks
+                    const int inter = nbm > 4 * sm_count_ ? 1 : 0;
                     rc = launch(CAT_MDBC, k_mdbc_f32_predict,
                                 nbm + blocks_for((nf_ + kPredU - 1) / kPredU), kBlock, err, W_,
                                 nw_, nbm, (const uint32_t *)fstart_, F_, grid_, P_, dt, Fs_, O_,
                                 skin_, rebuild_, health_, cond, capturing_ ? 1 : 0, kc,
-                                rec ? rec_s_ : PairRec{}, rec ? rec_w_ : PairRec{});
+                                rec ? rec_s_ : PairRec{}, rec ? rec_w_ : PairRec{}, inter);
                     if (rc) return rc;
                 }
             }
@@ -1192,6 +1196,12 @@ template <typename T> class Engine final : public EngineBase {
 
     int init(const HostSetup &hs, void *stream, std::string &err) override {
         if (const char *v = std::getenv("TSPH_PDL")) pdl_ = std::atoi(v) != 0;
+        {
+            int dev = 0, sms = 0;
+            TSPH_CK(cudaGetDevice(&dev));
+            TSPH_CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            if (sms > 0) sm_count_ = sms;
+        }
         if (stream) {
             st_ = static_cast<cudaStream_t>(stream);
         } else {

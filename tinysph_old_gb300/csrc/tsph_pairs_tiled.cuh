@@ -635,15 +635,36 @@ k_mdbc_f32_predict(WallState<float> Wl, int nw, int nbm, const uint32_t *__restr
                 FluidState<float> F, Grid g, Phys<float> P, float dt, FluidState<float> D,
                 OldState<float> O, float skin, uint32_t *__restrict__ rebuild,
                 uint32_t *__restrict__ health, cudaGraphConditionalHandle cond, int use_cond,
-                KeepCells kc, PairRec RS, PairRec RW) {
+                KeepCells kc, PairRec RS, PairRec RW, int interleave) {
     pdl_enter();
-    if ((int)blockIdx.x < nbm) {
-        mdbc_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, true, dt, RW);
+    // The block's half: mDBC blocks first (their one wave runs ahead of the
+    // predictor's blocks), or, when the walls need several waves
+    // (`interleave`), mDBC and predictor blocks alternating, so that the
+    // latency-bound ghost-node sums share every wave with the bandwidth-bound
+    // predictor
+    const int b = (int)blockIdx.x, nbp = (int)gridDim.x - nbm;
+    int bm = -1, bp = -1;
+    if (interleave) {
+        const int pairs = min(nbm, nbp);
+        if (b < 2 * pairs) {
+            if (b & 1) bp = b >> 1;
+            else bm = b >> 1;
+        } else if (nbm > pairs) {
+            bm = b - pairs;
+        } else {
+            bp = b - pairs;
+        }
+    } else if (b < nbm) {
+        bm = b;
+    } else {
+        bp = b - nbm;
+    }
+    if (bm >= 0) {
+        mdbc_wall(bm * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, true, dt, RW);
         return;
     }
-    predict_keep_fluid_f32<kPredU>(((int)blockIdx.x - nbm) * blockDim.x + threadIdx.x,
-                                   ((int)gridDim.x - nbm) * blockDim.x, F, fstart, g, dt, D, O,
-                                   skin, rebuild, health, cond, use_cond, kc, RS, P);
+    predict_keep_fluid_f32<kPredU>(bp * blockDim.x + threadIdx.x, nbp * blockDim.x, F, fstart, g,
+                                   dt, D, O, skin, rebuild, health, cond, use_cond, kc, RS, P);
 }
 
 }  // namespace tsph
