@@ -40,10 +40,15 @@ PAIR_BYTES_PER_PARTICLE = 80.0   # mean algorithmic bytes of the two pair launch
 STEP_BYTES_PER_PARTICLE = 344.0  # algorithmic bytes per particle-step (byte model)
 METRIC = "particle-steps/s, 720k dam break, 1 GB300: surrogate/batched vs plain, <=1% front err"
 # ALE-SPH byte model per fluid particle: flux pass reads loc, key, v, rho - rho0,
-# omega (32 B) and writes the three rates (16 B); whole step (leap-frog one
-# 124 B, fluxes 48 B, leap-frog two + binning 164 B, placement 36 B,
-# rank + scatter 188 B, scan 15 B)
+# omega (32 B) and writes the three rates (16 B); whole step with a sort every
+# step (leap-frog one 124 B, fluxes 48 B, leap-frog two + binning 164 B,
+# placement 36 B, rank + scatter 188 B, scan 15 B); on kept cells (leap-frog
+# one 124 B, fluxes 48 B, leap-frog two in place with the skin check 160 B)
+# plus, per sort, histogram 28 B, scan 15 B, placement 36 B, rank + scatter
+# of every field 270 B, copy back 192 B
 ALE_FLUX_BYTES_PER_PARTICLE = 48.0
+ALE_KEPT_STEP_BYTES = 332.0
+ALE_SORT_BYTES = 541.0
 INFER_KERNELS = 5  # one network forward: node kernel, then edge + node kernel for each of 2 layers
 ALE_STEP_BYTES_PER_PARTICLE = 575.0
 ALE_METRIC = "particle-steps/s, ALE-SPH dam break dp=0.0004 (1.1M fluid), 1 GB300"
@@ -357,6 +362,8 @@ def run_ale(args, rank, world, local):
     nrm[:len(nn)] = nn
     s.add_particles(a["type"], a["r"], a["v"], a["rho"], a["p"], nrm)
     s.set_scheme(sph.ALE_MUSCL if args.scheme == "muscl" else sph.ALE_AS_WRITTEN)
+    kept = not args.ale_sort_every_step
+    s.set_keep_cells(kept)
     s.divide_to_cells()
     s.particle_to_cell()
     n = s.np
@@ -373,6 +380,7 @@ def run_ale(args, rank, world, local):
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
+    sorts0 = s.sort_count()
     with ClockSampler(local) as clocks:
         with torch.cuda.stream(stream):
             for k in range(args.steps):
@@ -383,6 +391,9 @@ def run_ale(args, rank, world, local):
                 ends[k].record(stream)
         stream.synchronize()
     torch.cuda.synchronize()
+    sorts_per_step = (s.sort_count() - sorts0) / args.steps if kept else 1.0
+    step_bytes = (ALE_KEPT_STEP_BYTES + ALE_SORT_BYTES * sorts_per_step if kept
+                  else ALE_STEP_BYTES_PER_PARTICLE)
     ms = sum(starts[k].elapsed_time(ends[k]) for k in range(args.steps))
     ms = max_over_ranks(ms, dist, "cuda")
     value = whole_job_rate(world, n, args.steps, ms)
@@ -443,6 +454,9 @@ def run_ale(args, rank, world, local):
             "config": {"workload": f"ALE-SPH dam break dp={args.dp}, {n} particles "
                                    f"({nfluid} fluid), scheme {args.scheme}",
                        "particles": n, "fluid": nfluid, "dp": args.dp,
+                       "cells": ("kept: sorted when a particle moved 0.95 (kh - 2h) / 2 since "
+                                 "its binning or left the domain" if kept
+                                 else "sorted every step (the reference's cell order)"),
                        "l2": "flushed (256 MB write) between timed steps",
                        "parallelism": f"replicas x{world}" if world > 1 else "single GPU"},
             "e2e": {"value": e2e_value, "unit": "particle-steps/s", "h2d_bytes_per_step": xfer,
@@ -453,10 +467,13 @@ def run_ale(args, rank, world, local):
                          "frac": achieved / peak, "traffic": None, "kernel": "k_ale_flux",
                          "bytes_per_unit": ALE_FLUX_BYTES_PER_PARTICLE, "unit_count": nfluid,
                          "avg_launch_us": flux_us, "peak_kind": peak_kind},
-            "step_roofline": {"bytes_per_particle_step": ALE_STEP_BYTES_PER_PARTICLE,
-                              "achieved_gbs": ALE_STEP_BYTES_PER_PARTICLE * value / world / 1e9,
-                              "frac": ALE_STEP_BYTES_PER_PARTICLE * value / world / 1e9 / peak},
-            "gpu_launches": args.steps * (8 if args.scheme == "muscl" else 7),
+            "step_roofline": {"bytes_per_particle_step": step_bytes,
+                              "achieved_gbs": step_bytes * value / world / 1e9,
+                              "frac": step_bytes * value / world / 1e9 / peak},
+            "sorts_per_step": sorts_per_step,
+            # kept cells: part one, fluxes, part two, and the six sort kernels
+            # (launched every step, gated on the device); otherwise seven
+            "gpu_launches": args.steps * ((9 if kept else 7) + (1 if args.scheme == "muscl" else 0)),
             "clocks": clocks.summary(),
             "health": s.health(),
         }
@@ -831,6 +848,9 @@ def main():
                     help="batch workload: timed steps per case of the looped comparison")
     ap.add_argument("--scheme", default="as_written", choices=["as_written", "muscl"],
                     help="ALE interface states (ALE workload only)")
+    ap.add_argument("--ale-sort-every-step", action="store_true",
+                    help="ALE workload: sort every step (the reference's cell order) instead of "
+                         "keeping the cells while every particle is within the skin")
     ap.add_argument("--dp", type=float, default=None,
                     help="particle spacing (default 0.0005 dam break, 0.0004 ALE)")
     ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64"])

@@ -513,6 +513,17 @@ int tsph_ale_add_particles(tsph_ale_system *s, int n, const int32_t *type, const
                            const double *v, const double *rho, const double *p,
                            const double *normal);
 int tsph_ale_set_scheme(tsph_ale_system *s, int scheme);
+/* Kept cells for tsph_ale_step (on by default; no counterpart in the
+ * reference, whose RUN loop re-bins and sorts every step,
+ * cases/ALESPH_dambreakLong/MUSCL.h:80-140): the cells of the last binning
+ * stay while every fluid particle is within 0.95 (kh - 2h) / 2 of where it
+ * was binned and none left the domain; part two then runs in place and the
+ * sort only when one did.  The pair sums are the same up to FP32 summation
+ * order; off, every step sorts into the reference's cell order (needs kh >
+ * 2h to be on). */
+int tsph_ale_set_keep_cells(tsph_ale_system *s, int on);
+/* sorts run by tsph_ale_step on kept cells since the system was built */
+int tsph_ale_sort_count(tsph_ale_system *s, long long *n);
 int tsph_ale_np(tsph_ale_system *s, int *np);
 /* Divide_To_Cells + Particle_To_Cell, src/SPH_find_pairs.h:5-72 */
 int tsph_ale_divide_to_cells(tsph_ale_system *s);

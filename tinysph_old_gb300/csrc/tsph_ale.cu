@@ -54,6 +54,10 @@ struct AleWalls {
 struct AleConst {
     float h, inv_h, m, c0, rho0, g, dp, four_h2, awen, bwen_h, b_eos;
     float dx_exact;  // below this |dx| the FP32 cell-local difference may carry the wrong sign
+    // |dy| beyond which the rows above / below of a target stop: 2h, plus
+    // twice the skin, since on kept cells a cell's y order may be off by two
+    // moves of at most the skin each
+    float reach;
 };
 
 __device__ __forceinline__ float ale_eos(float s, const AleConst &K) {
@@ -127,14 +131,20 @@ __global__ void k_ale_lf1(AleFluid F, const uint32_t *__restrict__ fstart, int n
 }
 
 // Integrate_LeapFrog_partTwo, src/RALESPH_integration.h:38-107, for target i:
-// returns the new position, the new conserved state goes to D[o].  STEP
-// (the fused step, out of place): the leap-frog copies and the derived rho, v
-// are not written (the sort derives rho, v from the conserved state; the
-// copies are dead until the next part one).
-template <bool STEP>
+// returns the new position, the new conserved state goes to D[o].  FORM:
+// kLf2Single (the per-function entry point, in place: everything, the
+// leap-frog copies and the derived rho, v included); kLf2Moved (the fused
+// step before its sort, out of place: no copies, no derived rho, v -- the
+// sort derives them from the conserved state; the copies are dead until the
+// next part one); kLf2Kept (the fused step on kept cells, in place: derived
+// rho, v, no copies, and the rates and the index, which stay, not rewritten).
+enum { kLf2Single = 0, kLf2Moved = 1, kLf2Kept = 2 };
+template <int FORM>
 __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int o, float dtf,
                                        float hf, int step, float rho0, float &s_out,
                                        float2 &v_out) {
+    constexpr bool COPIES = FORM == kLf2Single, DERIVED = FORM != kLf2Moved,
+                   MOVE = FORM != kLf2Kept;
     double2 r = F.r[i];
     // the reference's p was computed from the density the fluxes used
     const float s_flux = F.s[i];
@@ -144,7 +154,7 @@ __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int
     if (step == 1) {
         const double om0 = F.om[i], omr0 = F.omr[i];
         const double2 omv0 = F.omv[i];
-        if (!STEP) {
+        if (COPIES) {
             D.om_o[o] = om0;
             D.omr_o[o] = omr0;
             D.omv_o[o] = omv0;
@@ -162,23 +172,25 @@ __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int
         const double2 o2 = F.omv_o[i];
         omv = make_double2(add_f(o2.x, dv.x, dtf), add_f(o2.y, dv.y, dtf));
         derive(om, omr, omv, rho0, s_out, v_out);
-        if (!STEP) {
+        if (COPIES) {
             D.om_o[o] = F.om_o[i];
             D.omr_o[o] = F.omr_o[i];
             D.omv_o[o] = o2;
         }
     }
-    if (!STEP) {
+    if (DERIVED) {
         D.s[o] = s_out;
         D.v[o] = v_out;
     }
     D.om[o] = om;
     D.omr[o] = omr;
     D.omv[o] = omv;
-    D.dom[o] = F.dom[i];
-    D.domr[o] = F.domr[i];
-    D.domv[o] = dv;
-    D.id[o] = F.id[i];
+    if (MOVE) {
+        D.dom[o] = F.dom[i];
+        D.domr[o] = F.domr[i];
+        D.domv[o] = dv;
+        D.id[o] = F.id[i];
+    }
     D.r[o] = r;
     D.ps[o] = s_flux;
     return r;
@@ -191,7 +203,7 @@ __global__ void k_ale_lf2(AleFluid F, const uint32_t *__restrict__ fstart, int n
     if (i >= n_live_ale(fstart, ncells)) return;
     float sn;
     float2 vn;
-    lf2<false>(F, i, F, i, dtf, hf, step, rho0, sn, vn);
+    lf2<kLf2Single>(F, i, F, i, dtf, hf, step, rho0, sn, vn);
 }
 
 // part two out of place + RemoveParticlesOutOfDomain (src/SPH_btdebug.h:4-31)
@@ -204,7 +216,7 @@ __global__ void k_ale_lf2_bin(AleFluid F, const uint32_t *__restrict__ fstart, G
     if (i >= n_live_ale(fstart, g.ncells)) return;
     float sn;
     float2 v;
-    const double2 rn = lf2<true>(F, i, D, i, dtf, hf, step, rho0, sn, v);
+    const double2 rn = lf2<kLf2Moved>(F, i, D, i, dtf, hf, step, rho0, sn, v);
     if (!(v.x == v.x) || !(v.y == v.y) || !(sn == sn)) atomicOr(health, kHealthNan);
     uint32_t k;
     if (out_of_domain_bits(rn, boxb)) {
@@ -217,6 +229,80 @@ __global__ void k_ale_lf2_bin(AleFluid F, const uint32_t *__restrict__ fstart, G
     }
     key[i] = k;
     slot[i] = atomicAdd(counts + k, 1u);
+}
+
+// part two in place on kept cells (the fused step between sorts): the new
+// position's cell-local coordinates against the particle's kept cell.  `gate`
+// is raised when a particle has moved more than the skin since its binning
+// (sig2 = skin^2) or left the domain (RemoveParticlesOutOfDomain,
+// src/SPH_btdebug.h:4-31), and the sort that follows runs.
+__global__ void k_ale_lf2_keep(AleFluid F, const uint32_t *__restrict__ fstart, Grid g, float dtf,
+                               float hf, int step, float rho0, BoxBits boxb,
+                               const float2 *__restrict__ lbin, float sig2,
+                               uint32_t *__restrict__ gate, uint32_t *__restrict__ health) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_live_ale(fstart, g.ncells)) return;
+    float sn;
+    float2 v;
+    const double2 rn = lf2<kLf2Kept>(F, i, F, i, dtf, hf, step, rho0, sn, v);
+    if (!(v.x == v.x) || !(v.y == v.y) || !(sn == sn)) atomicOr(health, kHealthNan);
+    if (out_of_domain_bits(rn, boxb)) {
+        atomicOr(health, kHealthRemoved);
+        *gate = 1u;
+        return;
+    }
+    const uint32_t k = F.key[i];
+    const int cx = (int)(k / (uint32_t)g.ncy), cy = (int)k - cx * g.ncy;
+    const float2 l = cell_local(g, rn, cx, cy);
+    F.loc[i] = l;
+    const float2 b = lbin[i];
+    const float dx = l.x - b.x, dy = l.y - b.y;
+    if (!(fmaf(dx, dx, dy * dy) <= sig2)) *gate = 1u;
+}
+
+// cell and histogram slot of every live particle for the sort on kept cells
+// (runs when k_ale_lf2_keep raised `gate`; `runs` counts the sorts); out of
+// the domain -> the last bucket
+__global__ void k_ale_hist_gated(AleFluid F, const uint32_t *__restrict__ fstart, Grid g,
+                                 BoxBits boxb, uint32_t *__restrict__ key,
+                                 uint32_t *__restrict__ slot, uint32_t *__restrict__ counts,
+                                 uint32_t *__restrict__ health, const uint32_t *__restrict__ gate,
+                                 unsigned long long *__restrict__ runs) {
+    if (gated_off(gate)) return;
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(runs, 1ull);
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_live_ale(fstart, g.ncells)) return;
+    const double2 r = F.r[i];
+    uint32_t k = (uint32_t)g.ncells;
+    if (!out_of_domain_bits(r, boxb)) {
+        int cx, cy;
+        k = cell_key(g, r, F.key[i], &cx, &cy);
+        if (k == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
+    }
+    key[i] = k;
+    slot[i] = atomicAdd(counts + k, 1u);
+}
+
+// the sorted state back into the step's arrays after a sort on kept cells
+// (the leap-frog copies are dead after a fused step and stay behind)
+__global__ void k_ale_copy_gated(AleFluid S, AleFluid D, const uint32_t *__restrict__ fstart,
+                                 int ncells, const uint32_t *__restrict__ gate) {
+    if (gated_off(gate)) return;
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= (int)fstart[ncells + 1]) return;
+    D.r[j] = S.r[j];
+    D.loc[j] = S.loc[j];
+    D.key[j] = S.key[j];
+    D.id[j] = S.id[j];
+    D.om[j] = S.om[j];
+    D.omr[j] = S.omr[j];
+    D.omv[j] = S.omv[j];
+    D.dom[j] = S.dom[j];
+    D.domr[j] = S.domr[j];
+    D.domv[j] = S.domv[j];
+    D.s[j] = S.s[j];
+    D.v[j] = S.v[j];
+    D.ps[j] = S.ps[j];
 }
 
 // cell key of the current positions (per-function Particle_To_Cell)
@@ -235,17 +321,21 @@ __global__ void k_ale_bin(AleFluid F, const uint32_t *__restrict__ fstart, Grid 
     slot[i] = atomicAdd(counts + k, 1u);
 }
 
-// rank inside the cell by (y, particle index) and move the record (+ loc).
-// STEP: after the fused step's part two — the leap-frog copies stay behind
-// and rho - rho0, v are derived from the conserved state; otherwise (a plain
-// re-binning) every field moves as it is.
+// rank inside the cell by (y, particle index) and move the record (+ loc,
+// and loc as the binning position into lbin).  STEP: after the fused step's
+// part two — the leap-frog copies stay behind and rho - rho0, v are derived
+// from the conserved state; otherwise (a plain re-binning, or the sort on
+// kept cells) every field moves as it is.  `gate` (may be null): runs only
+// when it is set.
 template <bool STEP>
 __global__ void k_ale_rank_scatter(const uint32_t *__restrict__ key, const int *__restrict__ n_ptr,
                                    const uint32_t *__restrict__ start,
                                    const uint32_t *__restrict__ tmp_id,
                                    const uint32_t *__restrict__ tmp_src,
                                    const long long *__restrict__ tmp_y, Grid g, AleFluid S,
-                                   AleFluid D, float rho0) {
+                                   AleFluid D, float rho0, float2 *__restrict__ lbin,
+                                   const uint32_t *__restrict__ gate) {
+    if (gated_off(gate)) return;
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= *n_ptr) return;
     const uint32_t src = tmp_src[j];
@@ -268,7 +358,9 @@ __global__ void k_ale_rank_scatter(const uint32_t *__restrict__ key, const int *
     D.id[f] = S.id[src];
     if (k < (uint32_t)g.ncells) {
         const int cx = (int)(k / (uint32_t)g.ncy), cy = (int)k - cx * g.ncy;
-        D.loc[f] = cell_local(g, r, cx, cy);
+        const float2 l = cell_local(g, r, cx, cy);
+        D.loc[f] = l;
+        lbin[f] = l;
     }
     const double om = S.om[src], omr = S.omr[src];
     const double2 omv = S.omv[src];
@@ -663,7 +755,7 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
     const int t1 = min(t0 + kAleT, nl);
     if (tid < 4) sm.offy[tid] = tid < 3 ? (float)(1 - tid) * g.khf : 0.f;
     const float khf = g.khf;
-    const float reach = 2.f * K.h * 1.0001f;
+    const float reach = K.reach;
     // the CTA's last target: when it lies in the first window's column and
     // rows, that window is the whole CTA (no further lookups for its end)
     const uint32_t klast = __ldg(F.key + t1 - 1);
@@ -1034,6 +1126,15 @@ class AleEngine {
     uint32_t *keyB = nullptr, *slotB = nullptr, *tmp_id = nullptr, *tmp_src = nullptr;
     long long *tmp_y = nullptr;
     uint32_t *health = nullptr;
+    // kept cells (the fused step): the cells of the last binning stay while
+    // every particle is within `skin` of where it was binned (lbin: its
+    // cell-local position then) and none left the domain; `gate` raised by
+    // part two runs the sort, `sort_runs` counts those sorts
+    bool keep = true;
+    float skin = 0.f;
+    float2 *lbin = nullptr;
+    uint32_t *gate = nullptr;
+    unsigned long long *sort_runs = nullptr;
     // the leap-frog copies (omega_o, ...) hold part one's values: false after
     // a fused step (its re-binning leaves them behind)
     bool copies_valid = true;
@@ -1103,6 +1204,10 @@ class AleEngine {
         K.b_eos = (float)(cs * cs * rho0 / 7.0);
         // FP32 x_a - x_b from cell-local positions: a few ulps of kh
         K.dx_exact = (float)(4e-6 * kh);
+        // the move allowed between two binnings: every pair within 2h stays
+        // inside the 3 x 3 cell block (kh >= 2h + 2 skin) with a margin
+        skin = (float)std::max(0.0, 0.95 * 0.5 * (kh - 2.0 * h));
+        K.reach = 2.f * K.h * 1.0001f + 2.f * skin;
         int rc;
         if ((rc = alloc(&grad, (size_t)12 * nf, err))) return rc;
         ACK(cudaMemset(grad, 0, sizeof(float) * 12 * std::max(nf, 1)));
@@ -1113,7 +1218,9 @@ class AleEngine {
             (rc = alloc(&keyB, nf, err)) || (rc = alloc(&slotB, nf, err)) ||
             (rc = alloc(&tmp_id, nf, err)) || (rc = alloc(&tmp_src, nf, err)) ||
             (rc = alloc(&tmp_y, nf, err)) ||
-            (rc = alloc(&health, 1, err)) || (rc = alloc(&dbx, bx.size(), err)) ||
+            (rc = alloc(&health, 1, err)) || (rc = alloc(&lbin, nf, err)) ||
+            (rc = alloc(&gate, 1, err)) || (rc = alloc(&sort_runs, 1, err)) ||
+            (rc = alloc(&dbx, bx.size(), err)) ||
             (rc = alloc(&dby, by.size(), err)) || (rc = alloc(&dox, ox.size(), err)) ||
             (rc = alloc(&doy, oy.size(), err)))
             return rc;
@@ -1123,6 +1230,8 @@ class AleEngine {
         ACK(cudaMemcpy(doy, oy.data(), 8 * oy.size(), cudaMemcpyHostToDevice));
         ACK(cudaMemset(counts, 0, 4 * (size_t)(ncells + 1)));
         ACK(cudaMemset(health, 0, 4));
+        ACK(cudaMemset(gate, 0, 4));
+        ACK(cudaMemset(sort_runs, 0, 8));
         grid.ax = Axis{dbx, dox, ncx};
         grid.ay = Axis{dby, doy, ncy};
         grid.ncx = ncx;
@@ -1224,21 +1333,23 @@ class AleEngine {
         return 0;
     }
 
-    // counting sort of X (keys in keyB/slotB, histogram in counts) into Y
-    int sort(AleFluid X, AleFluid Y, bool step_sort, std::string &err) {
+    // counting sort of X (keys in keyB/slotB, histogram in counts) into Y;
+    // with `g` every kernel runs only when the word it points to is set
+    int sort(AleFluid X, AleFluid Y, bool step_sort, std::string &err,
+             const uint32_t *g = nullptr) {
         const int n = ncells + 1;
         const int nt = (n + kScanTile - 1) / kScanTile;
-        k_scan_tiles_clear<<<nt, kScanThreads, 0, st>>>(counts, fstart, tiles, n, nullptr);
-        k_scan_add_tiles<<<nblk(n), kBlock, 0, st>>>(fstart, tiles, nt, n, nullptr);
+        k_scan_tiles_clear<<<nt, kScanThreads, 0, st>>>(counts, fstart, tiles, n, g);
+        k_scan_add_tiles<<<nblk(n), kBlock, 0, st>>>(fstart, tiles, nt, n, g);
         const int *ntot_ = reinterpret_cast<const int *>(fstart + ncells + 1);
         k_place<<<nblk(nf), kBlock, 0, st>>>(keyB, slotB, X.id, ntot_, fstart, tmp_id, tmp_src,
-                                             X.r, tmp_y, nullptr);
+                                             X.r, tmp_y, g);
         if (step_sort)
-            k_ale_rank_scatter<true><<<nblk(nf), kBlock, 0, st>>>(keyB, ntot_, fstart, tmp_id, tmp_src,
-                                                                  tmp_y, grid, X, Y, (float)rho0);
+            k_ale_rank_scatter<true><<<nblk(nf), kBlock, 0, st>>>(
+                keyB, ntot_, fstart, tmp_id, tmp_src, tmp_y, grid, X, Y, (float)rho0, lbin, g);
         else
             k_ale_rank_scatter<false><<<nblk(nf), kBlock, 0, st>>>(
-                keyB, ntot_, fstart, tmp_id, tmp_src, tmp_y, grid, X, Y, (float)rho0);
+                keyB, ntot_, fstart, tmp_id, tmp_src, tmp_y, grid, X, Y, (float)rho0, lbin, g);
         ACK(cudaGetLastError());
         return 0;
     }
@@ -1288,18 +1399,35 @@ class AleEngine {
         return 0;
     }
 
+    // the RUN body nsteps times.  On kept cells (`keep`, the default) part two
+    // runs in place and the sort only when a particle moved more than the
+    // skin or left the domain; otherwise every step re-bins and sorts (the
+    // reference's cell order every step)
     int step(double dt, int step0, int nsteps, std::string &err) {
         const Box box{x0, xm, y0, ym};
+        const BoxBits boxb = make_box_bits(box);
+        const bool kept = keep && skin > 0.f;
         for (int k = 1; k <= nsteps; k++) {
             const int stp = step0 + k;
             int rc;
             if (stp > 1 && (rc = lf1(dt, err))) return rc;
             if (scheme == TSPH_ALE_MUSCL && (rc = gradient(err))) return rc;
             if ((rc = forces(err))) return rc;
-            k_ale_lf2_bin<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, (float)dt, (float)(dt * 0.5),
-                                                       stp, (float)rho0, make_box_bits(box),
-                                                       B, keyB, slotB, counts, health);
-            if ((rc = sort(B, A, true, err))) return rc;
+            if (kept) {
+                ACK(cudaMemsetAsync(gate, 0, 4, st));
+                k_ale_lf2_keep<<<nblk(nf), kBlock, 0, st>>>(
+                    A, fstart, grid, (float)dt, (float)(dt * 0.5), stp, (float)rho0, boxb, lbin,
+                    skin * skin, gate, health);
+                k_ale_hist_gated<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, boxb, keyB, slotB,
+                                                              counts, health, gate, sort_runs);
+                if ((rc = sort(A, B, false, err, gate))) return rc;
+                k_ale_copy_gated<<<nblk(nf), kBlock, 0, st>>>(B, A, fstart, ncells, gate);
+            } else {
+                k_ale_lf2_bin<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, (float)dt,
+                                                           (float)(dt * 0.5), stp, (float)rho0,
+                                                           boxb, B, keyB, slotB, counts, health);
+                if ((rc = sort(B, A, true, err))) return rc;
+            }
         }
         ACK(cudaGetLastError());
         cells = true;
@@ -1548,6 +1676,24 @@ int tsph_ale_add_particles(tsph_ale_system *s, int n, const int32_t *type, const
         s->e.nrm.push_back(normal ? normal[2 * i] : 0.);
         s->e.nrm.push_back(normal ? normal[2 * i + 1] : 0.);
     }
+    return TSPH_OK;
+}
+
+int tsph_ale_set_keep_cells(tsph_ale_system *s, int on) {
+    if (!s) return afail(TSPH_ERR_ARG, "null system handle");
+    s->e.keep = on != 0;
+    return TSPH_OK;
+}
+
+int tsph_ale_sort_count(tsph_ale_system *s, long long *n) {
+    if (!s || !n) return afail(TSPH_ERR_ARG, "null argument");
+    *n = 0;
+    if (!s->e.built) return TSPH_OK;
+    unsigned long long v = 0;
+    cudaError_t e = cudaMemcpyAsync(&v, s->e.sort_runs, 8, cudaMemcpyDeviceToHost, s->e.st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s->e.st);
+    if (e != cudaSuccess) return afail(TSPH_ERR_CUDA, cudaGetErrorString(e));
+    *n = (long long)v;
     return TSPH_OK;
 }
 

@@ -50,6 +50,7 @@ ABI_SYMBOLS = (
     "tsph_gnn_destroy", "tsph_gnn_set_params", "tsph_gnn_get_params", "tsph_gnn_get_grads",
     "tsph_gnn_forward", "tsph_gnn_infer", "tsph_gnn_loss_grad", "tsph_gnn_adam",
     "tsph_ale_create", "tsph_ale_destroy", "tsph_ale_add_particles", "tsph_ale_set_scheme",
+    "tsph_ale_set_keep_cells", "tsph_ale_sort_count",
     "tsph_ale_np", "tsph_ale_divide_to_cells", "tsph_ale_particle_to_cell", "tsph_ale_gradient",
     "tsph_ale_forces", "tsph_ale_leapfrog_one", "tsph_ale_leapfrog_two", "tsph_ale_step",
     "tsph_ale_download", "tsph_ale_upload", "tsph_ale_sync", "tsph_ale_health",
@@ -193,6 +194,8 @@ def load(build_if_missing: bool = True) -> C.CDLL:
         getattr(L, f).argtypes = [P]
     L.tsph_ale_add_particles.argtypes = [P, I, P, P, P, P, P, P]
     L.tsph_ale_set_scheme.argtypes = [P, I]
+    L.tsph_ale_set_keep_cells.argtypes = [P, I]
+    L.tsph_ale_sort_count.argtypes = [P, C.POINTER(C.c_longlong)]
     L.tsph_ale_np.argtypes = [P, C.POINTER(I)]
     L.tsph_ale_forces.argtypes = [P, D]
     L.tsph_ale_leapfrog_one.argtypes = [P, D]
@@ -706,6 +709,18 @@ class AleSystem:
 
     def set_scheme(self, scheme):
         _check(self._L.tsph_ale_set_scheme(self._h, int(scheme)))
+
+    def set_keep_cells(self, on: bool):
+        """Kept cells for :meth:`step` (default on): the sort runs only when a
+        particle moved more than the skin since its binning or left the
+        domain; off, every step sorts (the reference's cell order)."""
+        _check(self._L.tsph_ale_set_keep_cells(self._h, 1 if on else 0))
+
+    def sort_count(self) -> int:
+        """Sorts that :meth:`step` ran on kept cells since the system was built."""
+        n = C.c_longlong()
+        _check(self._L.tsph_ale_sort_count(self._h, C.byref(n)))
+        return int(n.value)
 
     @property
     def np(self) -> int:
