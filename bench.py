@@ -183,6 +183,37 @@ def graph_timeline(s, model, dt, stream, steps):
     return out
 
 
+def eager_split(run_step, stream, steps, flush):
+    """Per-kernel time per step of `steps` eager steps (`run_step(k)` launches
+    step k on `stream`, the L2 flushed before each, as in the timed region):
+    CUPTI kernel records, or None without CUPTI.  Each kernel's launches per
+    step and its time, gated kernels that exit at once included."""
+    import torch
+
+    from tinysph_old_gb300 import timeline
+
+    try:
+        tl = timeline.Timeline()
+    except (FileNotFoundError, OSError):
+        return None
+    torch.cuda.synchronize()
+    try:
+        tl.start()
+    except RuntimeError:
+        return None
+    with torch.cuda.stream(stream):
+        for k in range(steps):
+            flush.zero_()
+            run_step(k)
+    stream.synchronize()
+    torch.cuda.synchronize()
+    tl.stop()
+    out = timeline.split(tl.records(), steps)
+    out["source"] = (f"CUPTI kernel records of {steps} eager steps (L2 flushed between steps); "
+                     "exclusive_us partitions the busy time of a step")
+    return out
+
+
 def measure_forms(plain_value):
     """The batched and surrogate forms of the metric, each run as its own
     bench process (shorter runs than their own workloads' defaults), against
@@ -392,6 +423,14 @@ def run_ale(args, rank, world, local):
         stream.synchronize()
     torch.cuda.synchronize()
     sorts_per_step = (s.sort_count() - sorts0) / args.steps if kept else 1.0
+    split_state = {"step": step}
+
+    def one_step(_k):
+        s.step(dt, split_state["step"], 1)
+        split_state["step"] += 1
+
+    kernel_split = eager_split(one_step, stream, 20, flush)
+    step = split_state["step"]
     step_bytes = (ALE_KEPT_STEP_BYTES + ALE_SORT_BYTES * sorts_per_step if kept
                   else ALE_STEP_BYTES_PER_PARTICLE)
     ms = sum(starts[k].elapsed_time(ends[k]) for k in range(args.steps))
@@ -471,6 +510,7 @@ def run_ale(args, rank, world, local):
                               "achieved_gbs": step_bytes * value / world / 1e9,
                               "frac": step_bytes * value / world / 1e9 / peak},
             "sorts_per_step": sorts_per_step,
+            "kernel_us_per_step": kernel_split,
             # kept cells: part one, fluxes, part two, and the six sort kernels
             # (launched every step, gated on the device); otherwise seven
             "gpu_launches": args.steps * ((9 if kept else 7) + (1 if args.scheme == "muscl" else 0)),

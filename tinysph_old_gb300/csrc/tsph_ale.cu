@@ -53,6 +53,7 @@ struct AleWalls {
 
 struct AleConst {
     float h, inv_h, m, c0, rho0, g, dp, four_h2, awen, bwen_h, b_eos;
+    float inv_rho0, inv_c0, inv_c02;  // products instead of divisions in the pair terms
     float dx_exact;  // below this |dx| the FP32 cell-local difference may carry the wrong sign
     // |dy| beyond which the rows above / below of a target stop: 2h, plus
     // twice the skin, since on kept cells a cell's y order may be off by two
@@ -61,7 +62,7 @@ struct AleConst {
 };
 
 __device__ __forceinline__ float ale_eos(float s, const AleConst &K) {
-    const float x = s / K.rho0;
+    const float x = s * K.inv_rho0;
     return K.b_eos * x * (7.f + x * (21.f + x * (35.f + x * (35.f + x * (21.f + x * (7.f + x))))));
 }
 
@@ -137,14 +138,19 @@ __global__ void k_ale_lf1(AleFluid F, const uint32_t *__restrict__ fstart, int n
 // step before its sort, out of place: no copies, no derived rho, v -- the
 // sort derives them from the conserved state; the copies are dead until the
 // next part one); kLf2Kept (the fused step on kept cells, in place: derived
-// rho, v, no copies, and the rates and the index, which stay, not rewritten).
-enum { kLf2Single = 0, kLf2Moved = 1, kLf2Kept = 2 };
+// rho, v, no copies, and the rates and the index, which stay, not rewritten);
+// kLf2KeptNext (as kLf2Kept, then the next step's part one with the same
+// rates and step, src/RALESPH_integration.h:10-36: the new state goes to the
+// leap-frog copies, the half-step state and its rho, v to omega, omega*rho,
+// omega*v, s, v -- bit for bit what k_ale_lf1 would write next).
+enum { kLf2Single = 0, kLf2Moved = 1, kLf2Kept = 2, kLf2KeptNext = 3 };
 template <int FORM>
 __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int o, float dtf,
                                        float hf, int step, float rho0, float &s_out,
                                        float2 &v_out) {
-    constexpr bool COPIES = FORM == kLf2Single, DERIVED = FORM != kLf2Moved,
-                   MOVE = FORM != kLf2Kept;
+    constexpr bool NEXT = FORM == kLf2KeptNext;
+    constexpr bool COPIES = FORM == kLf2Single, DERIVED = FORM != kLf2Moved && !NEXT,
+                   MOVE = FORM != kLf2Kept && !NEXT;
     double2 r = F.r[i];
     // the reference's p was computed from the density the fluxes used
     const float s_flux = F.s[i];
@@ -182,9 +188,25 @@ __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int
         D.s[o] = s_out;
         D.v[o] = v_out;
     }
-    D.om[o] = om;
-    D.omr[o] = omr;
-    D.omv[o] = omv;
+    if (NEXT) {
+        D.om_o[o] = om;
+        D.omr_o[o] = omr;
+        D.omv_o[o] = omv;
+        const double omh = add_f(om, F.dom[i], hf), omrh = add_f(omr, F.domr[i], hf);
+        const double2 omvh = make_double2(add_f(omv.x, dv.x, hf), add_f(omv.y, dv.y, hf));
+        D.om[o] = omh;
+        D.omr[o] = omrh;
+        D.omv[o] = omvh;
+        float sh;
+        float2 vh;
+        derive(omh, omrh, omvh, rho0, sh, vh);
+        D.s[o] = sh;
+        D.v[o] = vh;
+    } else {
+        D.om[o] = om;
+        D.omr[o] = omr;
+        D.omv[o] = omv;
+    }
     if (MOVE) {
         D.dom[o] = F.dom[i];
         D.domr[o] = F.domr[i];
@@ -231,8 +253,9 @@ __global__ void k_ale_lf2_bin(AleFluid F, const uint32_t *__restrict__ fstart, G
     slot[i] = atomicAdd(counts + k, 1u);
 }
 
-// part two in place on kept cells (the fused step between sorts): the new
-// position's cell-local coordinates against the particle's kept cell.  `gate`
+// part two in place on kept cells (the fused step between sorts), followed
+// by the next step's part one (kLf2KeptNext): the new position's cell-local
+// coordinates against the particle's kept cell.  `gate`
 // is raised when a particle has moved more than the skin since its binning
 // (sig2 = skin^2) or left the domain (RemoveParticlesOutOfDomain,
 // src/SPH_btdebug.h:4-31), and the sort that follows runs.
@@ -244,7 +267,7 @@ __global__ void k_ale_lf2_keep(AleFluid F, const uint32_t *__restrict__ fstart, 
     if (i >= n_live_ale(fstart, g.ncells)) return;
     float sn;
     float2 v;
-    const double2 rn = lf2<kLf2Kept>(F, i, F, i, dtf, hf, step, rho0, sn, v);
+    const double2 rn = lf2<kLf2KeptNext>(F, i, F, i, dtf, hf, step, rho0, sn, v);
     if (!(v.x == v.x) || !(v.y == v.y) || !(sn == sn)) atomicOr(health, kHealthNan);
     if (out_of_domain_bits(rn, boxb)) {
         atomicOr(health, kHealthRemoved);
@@ -262,7 +285,8 @@ __global__ void k_ale_lf2_keep(AleFluid F, const uint32_t *__restrict__ fstart, 
 
 // cell and histogram slot of every live particle for the sort on kept cells
 // (runs when k_ale_lf2_keep raised `gate`; `runs` counts the sorts); out of
-// the domain -> the last bucket
+// the domain -> the last bucket.  This and the other gated kernels loop over
+// their items grid-stride, so that a small grid skips at little cost.
 __global__ void k_ale_hist_gated(AleFluid F, const uint32_t *__restrict__ fstart, Grid g,
                                  BoxBits boxb, uint32_t *__restrict__ key,
                                  uint32_t *__restrict__ slot, uint32_t *__restrict__ counts,
@@ -270,39 +294,62 @@ __global__ void k_ale_hist_gated(AleFluid F, const uint32_t *__restrict__ fstart
                                  unsigned long long *__restrict__ runs) {
     if (gated_off(gate)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(runs, 1ull);
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n_live_ale(fstart, g.ncells)) return;
-    const double2 r = F.r[i];
-    uint32_t k = (uint32_t)g.ncells;
-    if (!out_of_domain_bits(r, boxb)) {
-        int cx, cy;
-        k = cell_key(g, r, F.key[i], &cx, &cy);
-        if (k == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
+    const int nl = n_live_ale(fstart, g.ncells);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nl; i += gridDim.x * blockDim.x) {
+        const double2 r = F.r[i];
+        uint32_t k = (uint32_t)g.ncells;
+        if (!out_of_domain_bits(r, boxb)) {
+            int cx, cy;
+            k = cell_key(g, r, F.key[i], &cx, &cy);
+            if (k == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
+        }
+        key[i] = k;
+        slot[i] = atomicAdd(counts + k, 1u);
     }
-    key[i] = k;
-    slot[i] = atomicAdd(counts + k, 1u);
 }
 
 // the sorted state back into the step's arrays after a sort on kept cells
-// (the leap-frog copies are dead after a fused step and stay behind)
+// (the leap-frog copies included: they hold the state at the end of the step)
 __global__ void k_ale_copy_gated(AleFluid S, AleFluid D, const uint32_t *__restrict__ fstart,
                                  int ncells, const uint32_t *__restrict__ gate) {
     if (gated_off(gate)) return;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= (int)fstart[ncells + 1]) return;
-    D.r[j] = S.r[j];
-    D.loc[j] = S.loc[j];
-    D.key[j] = S.key[j];
-    D.id[j] = S.id[j];
-    D.om[j] = S.om[j];
-    D.omr[j] = S.omr[j];
-    D.omv[j] = S.omv[j];
-    D.dom[j] = S.dom[j];
-    D.domr[j] = S.domr[j];
-    D.domv[j] = S.domv[j];
-    D.s[j] = S.s[j];
-    D.v[j] = S.v[j];
-    D.ps[j] = S.ps[j];
+    const int n = (int)fstart[ncells + 1];
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        D.r[j] = S.r[j];
+        D.loc[j] = S.loc[j];
+        D.key[j] = S.key[j];
+        D.id[j] = S.id[j];
+        D.om[j] = S.om[j];
+        D.omr[j] = S.omr[j];
+        D.omv[j] = S.omv[j];
+        D.om_o[j] = S.om_o[j];
+        D.omr_o[j] = S.omr_o[j];
+        D.omv_o[j] = S.omv_o[j];
+        D.dom[j] = S.dom[j];
+        D.domr[j] = S.domr[j];
+        D.domv[j] = S.domv[j];
+        D.s[j] = S.s[j];
+        D.v[j] = S.v[j];
+        D.ps[j] = S.ps[j];
+    }
+}
+
+// undo a part one applied ahead (k_ale_lf2_keep): the state at the end of
+// the step back from the leap-frog copies, rho - rho0 and v derived from it
+__global__ void k_ale_unhalf(AleFluid F, const uint32_t *__restrict__ fstart, int ncells,
+                             float rho0) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_live_ale(fstart, ncells)) return;
+    const double om = F.om_o[i], omr = F.omr_o[i];
+    const double2 omv = F.omv_o[i];
+    F.om[i] = om;
+    F.omr[i] = omr;
+    F.omv[i] = omv;
+    float s;
+    float2 v;
+    derive(om, omr, omv, rho0, s, v);
+    F.s[i] = s;
+    F.v[i] = v;
 }
 
 // cell key of the current positions (per-function Particle_To_Cell)
@@ -336,53 +383,54 @@ __global__ void k_ale_rank_scatter(const uint32_t *__restrict__ key, const int *
                                    AleFluid D, float rho0, float2 *__restrict__ lbin,
                                    const uint32_t *__restrict__ gate) {
     if (gated_off(gate)) return;
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= *n_ptr) return;
-    const uint32_t src = tmp_src[j];
-    const uint32_t k = key[src];
-    uint32_t f = (uint32_t)j;
-    if (k != (uint32_t)g.ncells) {
-        const uint32_t lo = start[k], hi = start[k + 1];
-        const uint32_t me = tmp_id[j];
-        const long long my = tmp_y[j];
-        uint32_t rank = 0;
-        for (uint32_t m = lo; m < hi; m++) {
-            const long long ym = tmp_y[m];
-            rank += (ym < my || (ym == my && tmp_id[m] < me)) ? 1u : 0u;
+    const int n = *n_ptr;
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const uint32_t src = tmp_src[j];
+        const uint32_t k = key[src];
+        uint32_t f = (uint32_t)j;
+        if (k != (uint32_t)g.ncells) {
+            const uint32_t lo = start[k], hi = start[k + 1];
+            const uint32_t me = tmp_id[j];
+            const long long my = tmp_y[j];
+            uint32_t rank = 0;
+            for (uint32_t m = lo; m < hi; m++) {
+                const long long ym = tmp_y[m];
+                rank += (ym < my || (ym == my && tmp_id[m] < me)) ? 1u : 0u;
+            }
+            f = lo + rank;
         }
-        f = lo + rank;
-    }
-    const double2 r = S.r[src];
-    D.r[f] = r;
-    D.key[f] = k;
-    D.id[f] = S.id[src];
-    if (k < (uint32_t)g.ncells) {
-        const int cx = (int)(k / (uint32_t)g.ncy), cy = (int)k - cx * g.ncy;
-        const float2 l = cell_local(g, r, cx, cy);
-        D.loc[f] = l;
-        lbin[f] = l;
-    }
-    const double om = S.om[src], omr = S.omr[src];
-    const double2 omv = S.omv[src];
-    D.om[f] = om;
-    D.omr[f] = omr;
-    D.omv[f] = omv;
-    D.dom[f] = S.dom[src];
-    D.domr[f] = S.domr[src];
-    D.domv[f] = S.domv[src];
-    D.ps[f] = S.ps[src];
-    if (STEP) {
-        float sn;
-        float2 vn;
-        derive(om, omr, omv, rho0, sn, vn);
-        D.s[f] = sn;
-        D.v[f] = vn;
-    } else {
-        D.om_o[f] = S.om_o[src];
-        D.omr_o[f] = S.omr_o[src];
-        D.omv_o[f] = S.omv_o[src];
-        D.s[f] = S.s[src];
-        D.v[f] = S.v[src];
+        const double2 r = S.r[src];
+        D.r[f] = r;
+        D.key[f] = k;
+        D.id[f] = S.id[src];
+        if (k < (uint32_t)g.ncells) {
+            const int cx = (int)(k / (uint32_t)g.ncy), cy = (int)k - cx * g.ncy;
+            const float2 l = cell_local(g, r, cx, cy);
+            D.loc[f] = l;
+            lbin[f] = l;
+        }
+        const double om = S.om[src], omr = S.omr[src];
+        const double2 omv = S.omv[src];
+        D.om[f] = om;
+        D.omr[f] = omr;
+        D.omv[f] = omv;
+        D.dom[f] = S.dom[src];
+        D.domr[f] = S.domr[src];
+        D.domv[f] = S.domv[src];
+        D.ps[f] = S.ps[src];
+        if (STEP) {
+            float sn;
+            float2 vn;
+            derive(om, omr, omv, rho0, sn, vn);
+            D.s[f] = sn;
+            D.v[f] = vn;
+        } else {
+            D.om_o[f] = S.om_o[src];
+            D.omr_o[f] = S.omr_o[src];
+            D.omv_o[f] = S.omv_o[src];
+            D.s[f] = S.s[src];
+            D.v[f] = S.v[src];
+        }
     }
 }
 
@@ -675,7 +723,7 @@ __device__ __forceinline__ void ale_pair(float dx, float dy, float2 va, float sa
     if (qb.w < 0.f) {
         // BT wall: rho* = rho_a (1 + v_a . n_b / c0), pressure along n_b
         const float vn = va.x * qb.x + va.y * qb.y;
-        const float sw = sa + rhoa * vn / K.c0;
+        const float sw = fmaf(rhoa * vn, K.inv_c0, sa);
         const float ps = SCHEME == 2 ? K.c0 * K.c0 * sw : ale_eos(sw, K);
         const float wdp = W * K.dp;
         acc.dvx = fmaf(-2.f * wdp * ps, qb.x, acc.dvx);
@@ -695,7 +743,7 @@ __device__ __forceinline__ void ale_pair(float dx, float dy, float2 va, float sa
         const float vss = 0.5f * (vR + vL) - 0.5f * (sb - sa) * K.c0 * ale_rcp(rbar);
         const float d = vL - vR;
         const float beta = fminf(3.f * fmaxf(d, 0.f), K.c0);
-        ss = 0.5f * (sa + sb) + 0.5f * beta * d * rbar / (K.c0 * K.c0);
+        ss = 0.5f * (sa + sb) + 0.5f * beta * d * rbar * K.inv_c02;
         const float t = vss - 0.5f * (vL + vR);
         vsx = fmaf(nx, t, 0.5f * (va.x + qb.x));
         vsy = fmaf(ny, t, 0.5f * (va.y + qb.y));
@@ -1135,9 +1183,16 @@ class AleEngine {
     float2 *lbin = nullptr;
     uint32_t *gate = nullptr;
     unsigned long long *sort_runs = nullptr;
+    int gated_blocks = 4 * 152;  // grid of a gated launch: 4 blocks per SM
     // the leap-frog copies (omega_o, ...) hold part one's values: false after
     // a fused step (its re-binning leaves them behind)
     bool copies_valid = true;
+    // a fused step on kept cells ends with the next step's part one applied
+    // (for a step of half_dt): omega, omega*rho, omega*v, s, v hold the
+    // half-step state and the leap-frog copies the state at the end of the
+    // step; normalize() puts the end-of-step state back
+    bool half = false;
+    double half_dt = 0.0;
     float *grad = nullptr;
     AleStage stg{};  // download / upload staging (allocated on first use)
     long long *dbx = nullptr, *dby = nullptr;
@@ -1150,6 +1205,16 @@ class AleEngine {
         allocs.clear();
         stg = AleStage{};
         built = false;
+        half = false;
+    }
+
+    // the state at the end of the last step (undo a part one applied ahead)
+    int normalize(std::string &err) {
+        if (!half) return 0;
+        k_ale_unhalf<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, (float)rho0);
+        ACK(cudaGetLastError());
+        half = false;
+        return 0;
     }
 
     template <typename P> int alloc(P **q, size_t n, std::string &err) {
@@ -1202,6 +1267,15 @@ class AleEngine {
         K.awen = (float)(0.557 / (h * h));
         K.bwen_h = (float)((double)(float)(-2.7852 / (h * h * h)) / h);
         K.b_eos = (float)(cs * cs * rho0 / 7.0);
+        {
+            int dev = 0, sms = 0;
+            ACK(cudaGetDevice(&dev));
+            ACK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+            if (sms > 0) gated_blocks = 4 * sms;
+        }
+        K.inv_rho0 = (float)(1.0 / rho0);
+        K.inv_c0 = (float)(1.0 / cs);
+        K.inv_c02 = (float)(1.0 / (cs * cs));
         // FP32 x_a - x_b from cell-local positions: a few ulps of kh
         K.dx_exact = (float)(4e-6 * kh);
         // the move allowed between two binnings: every pair within 2h stays
@@ -1339,22 +1413,26 @@ class AleEngine {
              const uint32_t *g = nullptr) {
         const int n = ncells + 1;
         const int nt = (n + kScanTile - 1) / kScanTile;
+        // gated: grid-stride kernels on a small grid (cheap to skip)
+        const int bn = g ? std::min(nblk(n), gated_blocks) : nblk(n);
+        const int bf = g ? std::min(nblk(nf), gated_blocks) : nblk(nf);
         k_scan_tiles_clear<<<nt, kScanThreads, 0, st>>>(counts, fstart, tiles, n, g);
-        k_scan_add_tiles<<<nblk(n), kBlock, 0, st>>>(fstart, tiles, nt, n, g);
+        k_scan_add_tiles<<<bn, kBlock, 0, st>>>(fstart, tiles, nt, n, g);
         const int *ntot_ = reinterpret_cast<const int *>(fstart + ncells + 1);
-        k_place<<<nblk(nf), kBlock, 0, st>>>(keyB, slotB, X.id, ntot_, fstart, tmp_id, tmp_src,
-                                             X.r, tmp_y, g);
+        k_place<<<bf, kBlock, 0, st>>>(keyB, slotB, X.id, ntot_, fstart, tmp_id, tmp_src, X.r,
+                                       tmp_y, g);
         if (step_sort)
-            k_ale_rank_scatter<true><<<nblk(nf), kBlock, 0, st>>>(
+            k_ale_rank_scatter<true><<<bf, kBlock, 0, st>>>(
                 keyB, ntot_, fstart, tmp_id, tmp_src, tmp_y, grid, X, Y, (float)rho0, lbin, g);
         else
-            k_ale_rank_scatter<false><<<nblk(nf), kBlock, 0, st>>>(
+            k_ale_rank_scatter<false><<<bf, kBlock, 0, st>>>(
                 keyB, ntot_, fstart, tmp_id, tmp_src, tmp_y, grid, X, Y, (float)rho0, lbin, g);
         ACK(cudaGetLastError());
         return 0;
     }
 
     int particle_to_cell(std::string &err) {
+        if (int rc = normalize(err)) return rc;
         k_ale_bin<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, keyB, slotB, counts, health);
         int rc = sort(A, B, false, err);
         if (rc) return rc;
@@ -1364,12 +1442,14 @@ class AleEngine {
     }
 
     int gradient(std::string &err) {
+        if (int rc = normalize(err)) return rc;
         k_ale_grad<<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
         ACK(cudaGetLastError());
         return 0;
     }
 
     int forces(std::string &err) {
+        if (int rc = normalize(err)) return rc;
         if (scheme == TSPH_ALE_MUSCL)
             k_ale_flux<1><<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
         else if (scheme == TSPH_ALE_FIRST_ORDER)
@@ -1381,6 +1461,13 @@ class AleEngine {
     }
 
     int lf1(double dt, std::string &err) {
+        if (half && half_dt == dt) {
+            // applied ahead by the last fused step, bit for bit
+            half = false;
+            copies_valid = true;
+            return 0;
+        }
+        if (int rc = normalize(err)) return rc;
         k_ale_lf1<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, (float)(dt * 0.5), (float)rho0);
         ACK(cudaGetLastError());
         copies_valid = true;
@@ -1388,6 +1475,7 @@ class AleEngine {
     }
 
     int lf2(double dt, int step, std::string &err) {
+        if (int rc = normalize(err)) return rc;
         if (step != 1 && !copies_valid) {
             err = "Integrate_LeapFrog_partTwo (step > 1) needs part one of the same step first";
             return TSPH_ERR_STATE;
@@ -1410,7 +1498,10 @@ class AleEngine {
         for (int k = 1; k <= nsteps; k++) {
             const int stp = step0 + k;
             int rc;
-            if (stp > 1 && (rc = lf1(dt, err))) return rc;
+            // part one: applied ahead by the last step, or now
+            if (half && (stp == 1 || half_dt != dt) && (rc = normalize(err))) return rc;
+            if (stp > 1 && !half && (rc = lf1(dt, err))) return rc;
+            half = false;
             if (scheme == TSPH_ALE_MUSCL && (rc = gradient(err))) return rc;
             if ((rc = forces(err))) return rc;
             if (kept) {
@@ -1418,10 +1509,13 @@ class AleEngine {
                 k_ale_lf2_keep<<<nblk(nf), kBlock, 0, st>>>(
                     A, fstart, grid, (float)dt, (float)(dt * 0.5), stp, (float)rho0, boxb, lbin,
                     skin * skin, gate, health);
-                k_ale_hist_gated<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, boxb, keyB, slotB,
-                                                              counts, health, gate, sort_runs);
+                const int bg = std::min(nblk(nf), gated_blocks);
+                k_ale_hist_gated<<<bg, kBlock, 0, st>>>(A, fstart, grid, boxb, keyB, slotB, counts,
+                                                        health, gate, sort_runs);
                 if ((rc = sort(A, B, false, err, gate))) return rc;
-                k_ale_copy_gated<<<nblk(nf), kBlock, 0, st>>>(B, A, fstart, ncells, gate);
+                k_ale_copy_gated<<<bg, kBlock, 0, st>>>(B, A, fstart, ncells, gate);
+                half = true;
+                half_dt = dt;
             } else {
                 k_ale_lf2_bin<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, (float)dt,
                                                            (float)(dt * 0.5), stp, (float)rho0,
@@ -1452,6 +1546,7 @@ class AleEngine {
     // host copies whole arrays, otherwise it keeps the live ones
     int download(int mask, const tsph_ale_host_state *o, std::string &err) {
         int rc;
+        if ((rc = normalize(err))) return rc;
         AleStage S{};
         struct Want {
             int bit;
@@ -1537,6 +1632,7 @@ class AleEngine {
     // follow), host arrays in the reference's order: staged by index, applied
     // per fluid row on the device (k_ale_import)
     int upload(int mask, const tsph_ale_host_state *in, std::string &err) {
+        if (int rc = normalize(err)) return rc;
         ACK(cudaStreamSynchronize(st));
         uint32_t nl = 0;
         ACK(cudaMemcpy(&nl, fstart + ncells, 4, cudaMemcpyDeviceToHost));

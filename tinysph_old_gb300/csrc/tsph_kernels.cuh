@@ -268,37 +268,43 @@ static __global__ void __launch_bounds__(kScanThreads) k_scan_tiles_clear(uint32
     if (threadIdx.x == 0) tile_sums[blockIdx.x] = total;
 }
 
-// add the tile offsets; each block sums the tile totals before its own tile
-// (at most a few hundred), the last block writes the grand total to out[n]
+// add the tile offsets over chunks of blockDim.x items (grid-stride over
+// the chunks, so any grid size gives the same result: a gated launch can
+// use a small grid); each chunk sums the tile totals before its own tile
+// (at most a few hundred), the last chunk writes the grand total to out[n]
 static __global__ void k_scan_add_tiles(uint32_t *__restrict__ out,
                                         const uint32_t *__restrict__ tile_sums, int ntiles, int n,
                                         const uint32_t *__restrict__ gate) {
     pdl_enter();
     if (gated_off(gate)) return;
     __shared__ uint32_t red[kBlock / 32];
-    const int i0 = blockIdx.x * blockDim.x;
-    const int t = i0 / kScanTile;
-    const bool last = blockIdx.x == gridDim.x - 1;
-    const int upto = last ? ntiles : t;
-    uint32_t acc = 0;
-    for (int u = threadIdx.x; u < upto; u += blockDim.x) acc += tile_sums[u];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
-    __syncthreads();
-    uint32_t tot = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += red[w];
-    uint32_t off = tot;
-    if (last) {
-        // total of all tiles; the offset of this block's own tile excludes it
-        if (threadIdx.x == 0) out[n] = tot;
-        uint32_t mine = 0;
-        if (t < ntiles) mine = tile_sums[t];
-        uint32_t after = 0;
-        for (int u = t + 1; u < ntiles; u++) after += tile_sums[u];
-        off = tot - mine - after;
+    const int nch = max(1, (n + (int)blockDim.x - 1) / (int)blockDim.x);
+    for (int c = blockIdx.x; c < nch; c += gridDim.x) {
+        const int i0 = c * blockDim.x;
+        const int t = i0 / kScanTile;
+        const bool last = c == nch - 1;
+        const int upto = last ? ntiles : t;
+        uint32_t acc = 0;
+        for (int u = threadIdx.x; u < upto; u += blockDim.x) acc += tile_sums[u];
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+        __syncthreads();
+        uint32_t tot = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) tot += red[w];
+        uint32_t off = tot;
+        if (last) {
+            // total of all tiles; the offset of this chunk's own tile excludes it
+            if (threadIdx.x == 0) out[n] = tot;
+            uint32_t mine = 0;
+            if (t < ntiles) mine = tile_sums[t];
+            uint32_t after = 0;
+            for (int u = t + 1; u < ntiles; u++) after += tile_sums[u];
+            off = tot - mine - after;
+        }
+        const int i = i0 + threadIdx.x;
+        if (i < n) out[i] += off;
+        __syncthreads();  // red is reused by the next chunk
     }
-    const int i = i0 + threadIdx.x;
-    if (i < n) out[i] += off;
 }
 
 static __global__ void __launch_bounds__(kScanThreads) k_scan_sums(uint32_t *__restrict__ tile_sums, int ntiles,
@@ -339,12 +345,14 @@ static __global__ void k_place(const uint32_t *__restrict__ key, const uint32_t 
                         long long *__restrict__ tmp_y, const uint32_t *__restrict__ gate) {
     pdl_enter();
     if (gated_off(gate)) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= *n_ptr) return;
-    const uint32_t d = start[key[i]] + slot[i];
-    tmp_id[d] = id[i];
-    tmp_src[d] = (uint32_t)i;
-    if (r) tmp_y[d] = ordered_bits(r[i].y);
+    // grid-stride: any grid size (a gated launch can use a small grid)
+    const int n = *n_ptr;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t d = start[key[i]] + slot[i];
+        tmp_id[d] = id[i];
+        tmp_src[d] = (uint32_t)i;
+        if (r) tmp_y[d] = ordered_bits(r[i].y);
+    }
 }
 
 // rank: final position = cell start + number of cell members that order
