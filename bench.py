@@ -42,13 +42,13 @@ METRIC = "particle-steps/s, 720k dam break, 1 GB300: surrogate/batched vs plain,
 # ALE-SPH byte model per fluid particle: flux pass reads loc, key, v, rho - rho0,
 # omega (32 B) and writes the three rates (16 B); whole step with a sort every
 # step (leap-frog one 124 B, fluxes 48 B, leap-frog two + binning 164 B,
-# placement 36 B, rank + scatter 188 B, scan 15 B); on kept cells (leap-frog
-# one 124 B, fluxes 48 B, leap-frog two in place with the skin check 160 B)
-# plus, per sort, histogram 28 B, scan 15 B, placement 36 B, rank + scatter
-# of every field 270 B, copy back 192 B
+# placement 36 B, rank + scatter 188 B, scan 15 B); on kept cells (fluxes
+# 48 B, leap-frog two in place with the skin check and the next step's
+# leap-frog one 192 B) plus, per sort, histogram 28 B, scan 15 B, placement
+# 36 B, rank + scatter of every field 270 B, copy back 256 B
 ALE_FLUX_BYTES_PER_PARTICLE = 48.0
-ALE_KEPT_STEP_BYTES = 332.0
-ALE_SORT_BYTES = 541.0
+ALE_KEPT_STEP_BYTES = 240.0
+ALE_SORT_BYTES = 605.0
 INFER_KERNELS = 5  # one network forward: node kernel, then edge + node kernel for each of 2 layers
 ALE_STEP_BYTES_PER_PARTICLE = 575.0
 ALE_METRIC = "particle-steps/s, ALE-SPH dam break dp=0.0004 (1.1M fluid), 1 GB300"
@@ -511,9 +511,10 @@ def run_ale(args, rank, world, local):
                               "frac": step_bytes * value / world / 1e9 / peak},
             "sorts_per_step": sorts_per_step,
             "kernel_us_per_step": kernel_split,
-            # kept cells: part one, fluxes, part two, and the six sort kernels
-            # (launched every step, gated on the device); otherwise seven
-            "gpu_launches": args.steps * ((9 if kept else 7) + (1 if args.scheme == "muscl" else 0)),
+            # kept cells: fluxes, part two with the next part one, and the six
+            # sort kernels (launched every step, gated on the device);
+            # otherwise part one, fluxes, part two and four sort kernels
+            "gpu_launches": args.steps * ((8 if kept else 7) + (1 if args.scheme == "muscl" else 0)),
             "clocks": clocks.summary(),
             "health": s.health(),
         }
