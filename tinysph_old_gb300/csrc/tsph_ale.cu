@@ -157,6 +157,11 @@ __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int
     const float2 dv = F.domv[i];
     double om, omr;
     double2 omv;
+    // the increments rate x step of part two (as add_f forms them), and the
+    // factor that makes them the next part one's rate x dt/2: 1 at step 1
+    // (part two's step is dt/2 there), else 1/2 -- dt/2 is dt halved in FP32
+    // as in FP64, so (rate x dt) / 2 is rate x dt/2 exactly
+    double i0, i1, i2, i3, half_of;
     if (step == 1) {
         const double om0 = F.om[i], omr0 = F.omr[i];
         const double2 omv0 = F.omv[i];
@@ -165,19 +170,31 @@ __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int
             D.omr_o[o] = omr0;
             D.omv_o[o] = omv0;
         }
-        om = add_f(om0, F.dom[i], hf);
-        omr = add_f(omr0, F.domr[i], hf);
-        omv = make_double2(add_f(omv0.x, dv.x, hf), add_f(omv0.y, dv.y, hf));
+        i0 = (double)(F.dom[i] * hf);
+        i1 = (double)(F.domr[i] * hf);
+        i2 = (double)(dv.x * hf);
+        i3 = (double)(dv.y * hf);
+        half_of = 1.0;
+        om = om0 + i0;
+        omr = omr0 + i1;
+        omv = make_double2(omv0.x + i2, omv0.y + i3);
         derive(om, omr, omv, rho0, s_out, v_out);
         r = make_double2(add_f(r.x, v_out.x, hf), add_f(r.y, v_out.y, hf));
     } else {
         const float2 v0 = F.v[i];
         r = make_double2(add_f(r.x, v0.x, dtf), add_f(r.y, v0.y, dtf));
-        om = add_f(F.om_o[i], F.dom[i], dtf);
-        omr = add_f(F.omr_o[i], F.domr[i], dtf);
+        i0 = (double)(F.dom[i] * dtf);
+        i1 = (double)(F.domr[i] * dtf);
+        i2 = (double)(dv.x * dtf);
+        i3 = (double)(dv.y * dtf);
+        half_of = 0.5;
+        om = F.om_o[i] + i0;
+        omr = F.omr_o[i] + i1;
         const double2 o2 = F.omv_o[i];
-        omv = make_double2(add_f(o2.x, dv.x, dtf), add_f(o2.y, dv.y, dtf));
-        derive(om, omr, omv, rho0, s_out, v_out);
+        omv = make_double2(o2.x + i2, o2.y + i3);
+        // NEXT stores the half-step rho, v only (derived below; they carry a
+        // NaN of the new state to the caller's check as well)
+        if (!NEXT) derive(om, omr, omv, rho0, s_out, v_out);
         if (COPIES) {
             D.om_o[o] = F.om_o[i];
             D.omr_o[o] = F.omr_o[i];
@@ -192,8 +209,10 @@ __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int
         D.om_o[o] = om;
         D.omr_o[o] = omr;
         D.omv_o[o] = omv;
-        const double omh = add_f(om, F.dom[i], hf), omrh = add_f(omr, F.domr[i], hf);
-        const double2 omvh = make_double2(add_f(omv.x, dv.x, hf), add_f(omv.y, dv.y, hf));
+        // the next part one: one rounding of x + increment x factor, as
+        // add_f(x, rate, dt/2) rounds x + rate x dt/2
+        const double omh = fma(i0, half_of, om), omrh = fma(i1, half_of, omr);
+        const double2 omvh = make_double2(fma(i2, half_of, omv.x), fma(i3, half_of, omv.y));
         D.om[o] = omh;
         D.omr[o] = omrh;
         D.omv[o] = omvh;
@@ -202,6 +221,10 @@ __device__ __forceinline__ double2 lf2(const AleFluid &F, int i, AleFluid D, int
         derive(omh, omrh, omvh, rho0, sh, vh);
         D.s[o] = sh;
         D.v[o] = vh;
+        if (step != 1) {
+            s_out = sh;
+            v_out = vh;
+        }
     } else {
         D.om[o] = om;
         D.omr[o] = omr;
