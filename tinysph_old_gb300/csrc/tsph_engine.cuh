@@ -294,11 +294,13 @@ template <typename T> class Engine final : public EngineBase {
 
     int do_mdbc(std::string &err) {
         if (nw_ == 0) return 0;
-        if constexpr (std::is_same<T, float>::value)
-            return launch(CAT_MDBC, k_mdbc_f32, blocks_for((long long)nw_ * kMdbcLanes), kBlock, err,
-                          W_, nw_,
+        if constexpr (std::is_same<T, float>::value) {
+            const int lanes = mdbc_lanes(nw_, sm_count_);
+            return launch(CAT_MDBC, lanes == kMdbcLanes ? k_mdbc_f32<kMdbcLanes>
+                                                        : k_mdbc_f32<kMdbcLanesMany>,
+                          blocks_for((long long)nw_ * lanes), kBlock, err, W_, nw_,
                           (const uint32_t *)fstart_, F_, grid_, P_);
-        else
+        } else
             return launch(CAT_MDBC, k_mdbc<T>, blocks_for((long long)nw_ * 32), kBlock, err, W_,
                           nw_, (const uint32_t *)fstart_, nbr_fluid(F_, false), grid_, P_);
     }
@@ -1019,11 +1021,13 @@ template <typename T> class Engine final : public EngineBase {
             }
             if constexpr (std::is_same<T, float>::value) {
                 if (mdbc_fused) {
-                    const int nbm = blocks_for((long long)nw_ * kMdbcLanes);
+                    const int lanes = mdbc_lanes(nw_, sm_count_);
+                    const int nbm = blocks_for((long long)nw_ * lanes);
                     // walls needing more than one wave (4 blocks per SM)
                     // share their waves with the predictor's blocks
                     const int inter = nbm > 4 * sm_count_ ? 1 : 0;
-                    rc = launch(CAT_MDBC, k_mdbc_f32_predict,
+                    rc = launch(CAT_MDBC, lanes == kMdbcLanes ? k_mdbc_f32_predict<kMdbcLanes>
+                                                              : k_mdbc_f32_predict<kMdbcLanesMany>,
                                 nbm + blocks_for((nf_ + kPredU - 1) / kPredU), kBlock, err, W_,
                                 nw_, nbm, (const uint32_t *)fstart_, F_, grid_, P_, dt, Fs_, O_,
                                 skin_, rebuild_, health_, cond, capturing_ ? 1 : 0, kc,

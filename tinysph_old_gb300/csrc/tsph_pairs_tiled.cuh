@@ -439,7 +439,15 @@ namespace tsph {
 // clamp at 1000 of src/SPH_mDBC.h:43-44.
 // With `predict` the wall's predictor step follows in the same thread
 // (rho_o = rho, rho += drho dt/2, as k_predict_keep does for walls).
-constexpr int kMdbcLanes = 8;
+// Lanes per wall particle: 4 while the walls fit in about two waves of
+// resident threads, 2 beyond (a thread then walks more candidates, but more
+// walls are in flight: the sums wait on their candidates' loads).  Measured on
+// GB300: 19k walls 17.7 us with 4 lanes (19.7 with 8, 21.2 with 2); 1.2 M
+// walls 243 us with 2 (299 with 4, 428 with 8, 270 with 1).
+constexpr int kMdbcLanes = 4, kMdbcLanesMany = 2;
+inline int mdbc_lanes(long long nw, int sms) {
+    return nw * kMdbcLanes > 2LL * sms * 4 * kBlock ? kMdbcLanesMany : kMdbcLanes;
+}
 
 // the ghost node's 3x3 moment system of one wall (its 12 FP32 sums) solved
 // in FP64, the density extrapolated to the wall particle and clamped, then
@@ -491,12 +499,13 @@ __device__ __forceinline__ void solve_mdbc(int w, const float *s, const WallStat
     }
 }
 
+template <int LANES>
 __device__ __forceinline__ void mdbc_wall(int gid, const WallState<float> &Wl, int nw,
                                            const uint32_t *__restrict__ fstart,
                                            const FluidState<float> &F, const Grid &g,
                                            const Phys<float> &P, bool predict, float dt,
                                            const PairRec &RW) {
-    const int w = gid / kMdbcLanes, sub = gid % kMdbcLanes;
+    const int w = gid / LANES, sub = gid % LANES;
     const bool valid = w < nw;
     float s[12];
 #pragma unroll
@@ -524,7 +533,7 @@ __device__ __forceinline__ void mdbc_wall(int gid, const WallState<float> &Wl, i
         }
         const int n01 = n[0] + n[1], ntot = n01 + n[2];
         constexpr int kUnroll = 4;
-        for (int e0 = sub; e0 < ntot; e0 += kUnroll * kMdbcLanes) {
+        for (int e0 = sub; e0 < ntot; e0 += kUnroll * LANES) {
             uint32_t kb[kUnroll];
             float2 lb[kUnroll];
             float sbv[kUnroll];
@@ -532,7 +541,7 @@ __device__ __forceinline__ void mdbc_wall(int gid, const WallState<float> &Wl, i
             bool use[kUnroll];
 #pragma unroll
             for (int u = 0; u < kUnroll; u++) {
-                const int e = e0 + u * kMdbcLanes;
+                const int e = e0 + u * LANES;
                 int d = 2, j = jlo[2] + e - n01;
                 if (e < n[0]) {
                     d = 0;
@@ -591,19 +600,19 @@ __device__ __forceinline__ void mdbc_wall(int gid, const WallState<float> &Wl, i
 #pragma unroll
     for (int q = 0; q < 12; q++) {
 #pragma unroll
-        for (int o = kMdbcLanes / 2; o > 0; o >>= 1) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
+        for (int o = LANES / 2; o > 0; o >>= 1) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
     }
     // The FP64 solve runs one wall per lane: GB300 issues FP64 at a small
     // fraction of the FP32 rate and a warp instruction costs the same with 4
     // lanes active as with 32, so the block's 32 walls hand their sums to its
     // first warp (lane l solves wall l of the block) instead of solving in
     // lane 0 of each group of 8.
-    constexpr int kWallsPerBlock = kBlock / kMdbcLanes;
+    constexpr int kWallsPerBlock = kBlock / LANES;
     __shared__ float sums[12][kWallsPerBlock + 1];
-    const int wl = (int)threadIdx.x / kMdbcLanes;
+    const int wl = (int)threadIdx.x / LANES;
 #pragma unroll
     for (int q = 0; q < 12; q++)
-        if (q % kMdbcLanes == sub) sums[q][wl] = s[q];
+        if (q % LANES == sub) sums[q][wl] = s[q];
     __syncthreads();
     if (threadIdx.x >= kWallsPerBlock) return;
     const int ws = gid / kBlock * kWallsPerBlock + (int)threadIdx.x;
@@ -613,11 +622,12 @@ __device__ __forceinline__ void mdbc_wall(int gid, const WallState<float> &Wl, i
     solve_mdbc(ws, s, Wl, P, predict, dt, RW);
 }
 
+template <int LANES>
 static __global__ void __launch_bounds__(kBlock)
 k_mdbc_f32(WallState<float> Wl, int nw, const uint32_t *__restrict__ fstart, FluidState<float> F,
             Grid g, Phys<float> P) {
     pdl_enter();
-    mdbc_wall(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, false, 0.f,
+    mdbc_wall<LANES>(blockIdx.x * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, false, 0.f,
               PairRec{});
 }
 
@@ -630,6 +640,7 @@ constexpr int kPredU = 4;
 // touch disjoint data (mDBC reads F's type, key, loc and rho and writes the
 // walls; the fluid predictor reads F and writes D and O), so the
 // latency-bound ghost-node sums overlap the bandwidth-bound predictor.
+template <int LANES>
 static __global__ void __launch_bounds__(kBlock, 4)
 k_mdbc_f32_predict(WallState<float> Wl, int nw, int nbm, const uint32_t *__restrict__ fstart,
                 FluidState<float> F, Grid g, Phys<float> P, float dt, FluidState<float> D,
@@ -660,7 +671,7 @@ k_mdbc_f32_predict(WallState<float> Wl, int nw, int nbm, const uint32_t *__restr
         bp = b - nbm;
     }
     if (bm >= 0) {
-        mdbc_wall(bm * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, true, dt, RW);
+        mdbc_wall<LANES>(bm * blockDim.x + threadIdx.x, Wl, nw, fstart, F, g, P, true, dt, RW);
         return;
     }
     predict_keep_fluid_f32<kPredU>(bp * blockDim.x + threadIdx.x, nbp * blockDim.x, F, fstart, g,
