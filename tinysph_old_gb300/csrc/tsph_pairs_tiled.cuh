@@ -431,8 +431,9 @@ inline TileConst make_tile_const(const Phys<float> &P, double h, double rho0, do
 
 namespace tsph {
 
-// mDBC ghost-node density, FP32 build: 8 lanes per wall particle (a launch
-// of one wave, which leaves room beside it for the fused predictor's blocks),
+// mDBC ghost-node density, FP32 build: 4 or 2 lanes per wall particle
+// (kMdbcLanes, kMdbcLanesMany below; the fused launch leaves room beside
+// its wall blocks for the predictor's),
 // the 12 moment sums (src/SPH_kernel_approx.h:1237-1287) in FP32, reduced
 // with shuffles; the 3x3 solve in FP64 with one reciprocal of the determinant
 // (threshold 0.001 and the Shepard / 1000 fall-backs of :1290-1333), the
