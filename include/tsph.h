@@ -513,12 +513,12 @@ int tsph_ale_add_particles(tsph_ale_system *s, int n, const int32_t *type, const
                            const double *v, const double *rho, const double *p,
                            const double *normal);
 int tsph_ale_set_scheme(tsph_ale_system *s, int scheme);
-/* Kept cells for tsph_ale_step (on by default; no counterpart in the
- * reference, whose RUN loop re-bins and sorts every step,
- * cases/ALESPH_dambreakLong/MUSCL.h:80-140): the cells of the last binning
- * stay while every fluid particle is within 0.95 (kh - 2h) / 2 of where it
- * was binned and none left the domain; part two then runs in place and the
- * sort only when one did.  The pair sums are the same up to FP32 summation
+/* Kept cells for tsph_ale_step and tsph_ale_particle_to_cell (on by
+ * default; no counterpart in the reference, whose RUN loop re-bins and sorts
+ * every step, cases/ALESPH_dambreakLong/MUSCL.h:80-140): the cells of the
+ * last binning stay while every fluid particle is within 0.95 (kh - 2h) / 2
+ * of where it was binned and none left the domain; part two then runs in
+ * place and the sort only when one did.  The pair sums are the same up to FP32 summation
  * order; off, every step sorts into the reference's cell order (needs kh >
  * 2h to be on). */
 int tsph_ale_set_keep_cells(tsph_ale_system *s, int on);
@@ -541,6 +541,21 @@ int tsph_ale_leapfrog_two(tsph_ale_system *s, double dt, int step);
 int tsph_ale_step(tsph_ale_system *s, double dt, int step0, int nsteps);
 int tsph_ale_download(tsph_ale_system *s, int fields, const tsph_ale_host_state *out);
 int tsph_ale_upload(tsph_ale_system *s, int fields, const tsph_ale_host_state *in);
+/* Pipelined transfers of r, v and rho (TSPH_ALE_F_R | _V | _RHO; other
+ * fields TSPH_ERR_ARG), as tsph_download_async / tsph_download_wait /
+ * tsph_upload_async for the WCSPH system (no counterpart in the reference,
+ * whose state lives in host memory).  tsph_ale_download_async exports into a
+ * staging set of its own and starts the device-to-host copies on a copy
+ * stream; tsph_ale_download_wait blocks until they are done (host buffers,
+ * pinned for a true overlap, valid and unread until then; with removed
+ * particles the download is synchronous).  tsph_ale_upload_async starts the
+ * host-to-device copies on a copy stream beside the work in flight; the next
+ * tsph_ale_particle_to_cell applies them (only if every particle is still
+ * live, else TSPH_HEALTH_UPLOAD and nothing changes) and bins the state;
+ * until then the calls that read or write the state return TSPH_ERR_STATE. */
+int tsph_ale_download_async(tsph_ale_system *s, int fields, const tsph_ale_host_state *out);
+int tsph_ale_download_wait(tsph_ale_system *s);
+int tsph_ale_upload_async(tsph_ale_system *s, int fields, const tsph_ale_host_state *in);
 int tsph_ale_sync(tsph_ale_system *s);
 int tsph_ale_health(tsph_ale_system *s, uint32_t *flags, int clear);
 

@@ -182,6 +182,7 @@ def test_ale_fused_equals_per_function_sequence(gpu_tsph, scheme):
     a = _gpu(gpu_tsph, case, g, scheme)
     b = _gpu(gpu_tsph, case, g, scheme)
     a.set_keep_cells(False)
+    b.set_keep_cells(False)
     a.step(dt, 0, 4)
     for stp in range(1, 5):
         if stp > 1:
@@ -264,6 +265,78 @@ def test_ale_part_one_ahead_is_exact(gpu_tsph):
     x, y = d.download(), e.download()
     for f in fields:
         assert np.array_equal(x[f], y[f]), f
+
+
+@pytest.mark.gpu
+def test_ale_pipelined_transfers_equal_synchronous(gpu_tsph):
+    """The pipelined loop (staged upload applied by particle_to_cell, step,
+    download read back a step later) gives bit for bit the synchronous
+    loop's results; a staged upload blocks the calls that use the state."""
+    torch = pytest.importorskip("torch")
+    case = cases.dam_break_ale(dp=0.004)
+    dt = case.dt
+    a, b = gpu_tsph.AleSystem.from_case(case), gpu_tsph.AleSystem.from_case(case)
+    a.step(dt, 0, 3)
+    b.step(dt, 0, 3)
+    n = a.np
+    mask = gpu_tsph.ALE_F_R | gpu_tsph.ALE_F_V | gpu_tsph.ALE_F_RHO
+    hin = [torch.empty(shape, dtype=torch.float64, pin_memory=True)
+           for shape in ((n, 2), (n, 2), (n,))]
+    a.download_ptrs(mask, r=hin[0].data_ptr(), v=hin[1].data_ptr(), rho=hin[2].data_ptr())
+    ptr = dict(r=hin[0].data_ptr(), v=hin[1].data_ptr(), rho=hin[2].data_ptr())
+    outs = [[torch.empty_like(t, pin_memory=True) for t in hin] for _ in range(4)]
+    sync = []
+    for k in range(4):
+        a.upload_ptrs(mask, **ptr)
+        a.particle_to_cell()
+        a.step(dt, 3 + k, 1)
+        sync.append(a.download(gpu_tsph.ALE_F_R | gpu_tsph.ALE_F_V | gpu_tsph.ALE_F_RHO))
+    b.upload_async(mask, **ptr)
+    with pytest.raises(gpu_tsph.TsphError):
+        b.step(dt, 3, 1)
+    for k in range(4):
+        if k:
+            b.upload_async(mask, **ptr)
+        b.particle_to_cell()
+        b.step(dt, 3 + k, 1)
+        o = outs[k]
+        b.download_async(mask, r=o[0].data_ptr(), v=o[1].data_ptr(), rho=o[2].data_ptr())
+    b.download_wait()
+    for k in range(4):
+        o = [t.numpy() for t in outs[k]]
+        assert np.array_equal(o[0], sync[k]["r"]), k
+        assert np.array_equal(o[1], sync[k]["v"]), k
+        assert np.array_equal(o[2], sync[k]["rho"]), k
+    assert b.health() & ~gpu_tsph.HEALTH_REMOVED == 0
+
+
+@pytest.mark.gpu
+def test_ale_particle_to_cell_on_kept_cells(gpu_tsph):
+    """particle_to_cell on kept cells: positions moved within the skin keep
+    the cells (no sort), a move past it sorts; the fluxes then equal those
+    of a full re-binning within the FP32 bars."""
+    case = cases.dam_break_ale(dp=0.004)
+    s = gpu_tsph.AleSystem.from_case(case)
+    ref = gpu_tsph.AleSystem.from_case(case)
+    ref.set_keep_cells(False)
+    st = s.download()
+    fl = st["type"] == 0
+    skin = 0.95 * 0.5 * (case.kap * case.h - 2.0 * case.h)
+    rng = np.random.default_rng(3)
+    for move, sorts in ((0.3 * skin, 0), (3.0 * skin, 1)):
+        r = st["r"].copy()
+        d = rng.normal(size=(int(fl.sum()), 2))
+        d *= move / np.linalg.norm(d, axis=1, keepdims=True)
+        r[fl] += d
+        n0 = s.sort_count()
+        for sys_ in (s, ref):
+            sys_.upload(r=r)
+            sys_.particle_to_cell()
+            sys_.forces(case.dt)
+        assert s.sort_count() - n0 == sorts, move
+        x, y = s.download(), ref.download()
+        for f in RATES:
+            assert _err(x[f][fl], y[f][fl]) <= _rate_tol(y[f][fl]), (move, f)
 
 
 @pytest.mark.gpu

@@ -307,11 +307,11 @@ __global__ void k_ale_lf2_keep(AleFluid F, const uint32_t *__restrict__ fstart, 
 }
 
 // cell and histogram slot of every live particle for the sort on kept cells
-// (runs when k_ale_lf2_keep raised `gate`; `runs` counts the sorts); out of
-// the domain -> the last bucket.  This and the other gated kernels loop over
+// (runs when `gate` was raised; `runs` counts the sorts); with `remove` (a
+// step's sort) out of the domain -> the last bucket.  This and the other gated kernels loop over
 // their items grid-stride, so that a small grid skips at little cost.
 __global__ void k_ale_hist_gated(AleFluid F, const uint32_t *__restrict__ fstart, Grid g,
-                                 BoxBits boxb, uint32_t *__restrict__ key,
+                                 BoxBits boxb, int remove, uint32_t *__restrict__ key,
                                  uint32_t *__restrict__ slot, uint32_t *__restrict__ counts,
                                  uint32_t *__restrict__ health, const uint32_t *__restrict__ gate,
                                  unsigned long long *__restrict__ runs) {
@@ -321,7 +321,7 @@ __global__ void k_ale_hist_gated(AleFluid F, const uint32_t *__restrict__ fstart
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nl; i += gridDim.x * blockDim.x) {
         const double2 r = F.r[i];
         uint32_t k = (uint32_t)g.ncells;
-        if (!out_of_domain_bits(r, boxb)) {
+        if (!(remove && out_of_domain_bits(r, boxb))) {
             int cx, cy;
             k = cell_key(g, r, F.key[i], &cx, &cy);
             if (k == (uint32_t)g.ncells) atomicOr(health, kHealthEscaped);
@@ -373,6 +373,23 @@ __global__ void k_ale_unhalf(AleFluid F, const uint32_t *__restrict__ fstart, in
     derive(om, omr, omv, rho0, s, v);
     F.s[i] = s;
     F.v[i] = v;
+}
+
+// Particle_To_Cell on kept cells: each live particle's cell-local position
+// against its kept cell; `gate` raised when one moved more than the skin
+// since its binning (sig2 = skin^2) or left its cell's block for good
+__global__ void k_ale_relocate(AleFluid F, const uint32_t *__restrict__ fstart, Grid g,
+                               const float2 *__restrict__ lbin, float sig2,
+                               uint32_t *__restrict__ gate) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_live_ale(fstart, g.ncells)) return;
+    const uint32_t k = F.key[i];
+    const int cx = (int)(k / (uint32_t)g.ncy), cy = (int)k - cx * g.ncy;
+    const float2 l = cell_local(g, F.r[i], cx, cy);
+    F.loc[i] = l;
+    const float2 b = lbin[i];
+    const float dx = l.x - b.x, dy = l.y - b.y;
+    if (!(fmaf(dx, dx, dy * dy) <= sig2)) *gate = 1u;
 }
 
 // cell key of the current positions (per-function Particle_To_Cell)
@@ -1143,7 +1160,14 @@ __global__ void k_ale_export(AleFluid F, const uint32_t *__restrict__ fstart, in
 // following: omega first (same rho = omega rho / omega, same v = omega v /
 // (rho omega)), then rho, v, r
 __global__ void k_ale_import(AleFluid F, const uint32_t *__restrict__ fstart, int ncells,
-                             AleStage S, double rho0) {
+                             AleStage S, double rho0, int nw, int ntot,
+                             uint32_t *__restrict__ health) {
+    // a staged upload (health given) applies only while every index is live,
+    // else TSPH_HEALTH_UPLOAD and nothing changes
+    if (health && (int)fstart[ncells] + nw != ntot) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(health, kHealthUpload);
+        return;
+    }
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n_live_ale(fstart, ncells)) return;
     const uint32_t i = F.id[j];
@@ -1216,19 +1240,42 @@ class AleEngine {
     // step; normalize() puts the end-of-step state back
     bool half = false;
     double half_dt = 0.0;
+    // pipelined transfers (r, v, rho): the download's and the upload's own
+    // staging sets, copy streams and events; `binned`: a sort has given every
+    // live particle its cell (kept-cell re-binning needs one)
+    AleStage dstg{}, ustg{};
+    cudaStream_t cs_d = nullptr, cs_u = nullptr;
+    cudaEvent_t ev_x = nullptr, ev_d = nullptr, ev_up = nullptr, ev_imp = nullptr;
+    bool d_pending = false, up_pending = false, binned = false;
+    int up_mask = 0;
     float *grad = nullptr;
     AleStage stg{};  // download / upload staging (allocated on first use)
     long long *dbx = nullptr, *dby = nullptr;
     double *dox = nullptr, *doy = nullptr;
 
-    ~AleEngine() { release(); if (own && st) cudaStreamDestroy(st); }
+    ~AleEngine() {
+        if (d_pending) cudaEventSynchronize(ev_d);
+        if (st) cudaStreamSynchronize(st);
+        if (cs_u) cudaStreamSynchronize(cs_u);
+        release();
+        for (cudaStream_t q : {cs_d, cs_u})
+            if (q) cudaStreamDestroy(q);
+        for (cudaEvent_t q : {ev_x, ev_d, ev_up, ev_imp})
+            if (q) cudaEventDestroy(q);
+        if (own && st) cudaStreamDestroy(st);
+    }
 
     void release() {
         for (void *q : allocs) cudaFree(q);
         allocs.clear();
         stg = AleStage{};
+        dstg = AleStage{};
+        ustg = AleStage{};
         built = false;
         half = false;
+        d_pending = false;
+        up_pending = false;
+        binned = false;
     }
 
     // the state at the end of the last step (undo a part one applied ahead)
@@ -1456,15 +1503,43 @@ class AleEngine {
 
     int particle_to_cell(std::string &err) {
         if (int rc = normalize(err)) return rc;
+        if (up_pending) {
+            // the staged upload first (every index live, checked on the device)
+            AleStage S{};
+            if (up_mask & TSPH_ALE_F_R) S.r = ustg.r;
+            if (up_mask & TSPH_ALE_F_V) S.v = ustg.v;
+            if (up_mask & TSPH_ALE_F_RHO) S.rho = ustg.rho;
+            ACK(cudaStreamWaitEvent(st, ev_up, 0));
+            k_ale_import<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, S, rho0, nw, ntot, health);
+            ACK(cudaGetLastError());
+            ACK(cudaEventRecord(ev_imp, st));
+            up_pending = false;
+        }
+        if (keep && skin > 0.f && binned) {
+            // kept cells: the sort only when a particle moved past the skin
+            const Box box{x0, xm, y0, ym};
+            const int bg = std::min(nblk(nf), gated_blocks);
+            ACK(cudaMemsetAsync(gate, 0, 4, st));
+            k_ale_relocate<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, lbin, skin * skin, gate);
+            k_ale_hist_gated<<<bg, kBlock, 0, st>>>(A, fstart, grid, make_box_bits(box), 0, keyB,
+                                                    slotB, counts, health, gate, sort_runs);
+            if (int rc = sort(A, B, false, err, gate)) return rc;
+            k_ale_copy_gated<<<bg, kBlock, 0, st>>>(B, A, fstart, ncells, gate);
+            ACK(cudaGetLastError());
+            cells = true;
+            return 0;
+        }
         k_ale_bin<<<nblk(nf), kBlock, 0, st>>>(A, fstart, grid, keyB, slotB, counts, health);
         int rc = sort(A, B, false, err);
         if (rc) return rc;
         std::swap(A, B);
         cells = true;
+        binned = true;
         return 0;
     }
 
     int gradient(std::string &err) {
+        if (int rc = no_staged_upload(err)) return rc;
         if (int rc = normalize(err)) return rc;
         k_ale_grad<<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
         ACK(cudaGetLastError());
@@ -1472,6 +1547,7 @@ class AleEngine {
     }
 
     int forces(std::string &err) {
+        if (int rc = no_staged_upload(err)) return rc;
         if (int rc = normalize(err)) return rc;
         if (scheme == TSPH_ALE_MUSCL)
             k_ale_flux<1><<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
@@ -1484,6 +1560,7 @@ class AleEngine {
     }
 
     int lf1(double dt, std::string &err) {
+        if (int rc = no_staged_upload(err)) return rc;
         if (half && half_dt == dt) {
             // applied ahead by the last fused step, bit for bit
             half = false;
@@ -1498,6 +1575,7 @@ class AleEngine {
     }
 
     int lf2(double dt, int step, std::string &err) {
+        if (int rc = no_staged_upload(err)) return rc;
         if (int rc = normalize(err)) return rc;
         if (step != 1 && !copies_valid) {
             err = "Integrate_LeapFrog_partTwo (step > 1) needs part one of the same step first";
@@ -1515,6 +1593,7 @@ class AleEngine {
     // skin or left the domain; otherwise every step re-bins and sorts (the
     // reference's cell order every step)
     int step(double dt, int step0, int nsteps, std::string &err) {
+        if (int rc = no_staged_upload(err)) return rc;
         const Box box{x0, xm, y0, ym};
         const BoxBits boxb = make_box_bits(box);
         const bool kept = keep && skin > 0.f;
@@ -1533,8 +1612,8 @@ class AleEngine {
                     A, fstart, grid, (float)dt, (float)(dt * 0.5), stp, (float)rho0, boxb, lbin,
                     skin * skin, gate, health);
                 const int bg = std::min(nblk(nf), gated_blocks);
-                k_ale_hist_gated<<<bg, kBlock, 0, st>>>(A, fstart, grid, boxb, keyB, slotB, counts,
-                                                        health, gate, sort_runs);
+                k_ale_hist_gated<<<bg, kBlock, 0, st>>>(A, fstart, grid, boxb, 1, keyB, slotB,
+                                                        counts, health, gate, sort_runs);
                 if ((rc = sort(A, B, false, err, gate))) return rc;
                 k_ale_copy_gated<<<bg, kBlock, 0, st>>>(B, A, fstart, ncells, gate);
                 half = true;
@@ -1569,7 +1648,7 @@ class AleEngine {
     // host copies whole arrays, otherwise it keeps the live ones
     int download(int mask, const tsph_ale_host_state *o, std::string &err) {
         int rc;
-        if ((rc = normalize(err))) return rc;
+        if ((rc = no_staged_upload(err)) || (rc = normalize(err))) return rc;
         AleStage S{};
         struct Want {
             int bit;
@@ -1651,10 +1730,124 @@ class AleEngine {
         return 0;
     }
 
+    // refuse calls that read or write the state while an upload is staged
+    int no_staged_upload(std::string &err) const {
+        if (!up_pending) return 0;
+        err = "an upload is staged: call tsph_ale_particle_to_cell first";
+        return TSPH_ERR_STATE;
+    }
+
+    int transfer_streams(std::string &err) {
+        if (cs_d) return 0;
+        ACK(cudaStreamCreateWithFlags(&cs_d, cudaStreamNonBlocking));
+        ACK(cudaStreamCreateWithFlags(&cs_u, cudaStreamNonBlocking));
+        for (cudaEvent_t *q : {&ev_x, &ev_d, &ev_up, &ev_imp})
+            ACK(cudaEventCreateWithFlags(q, cudaEventDisableTiming));
+        ACK(cudaEventRecord(ev_imp, st));
+        return 0;
+    }
+
+    // pipelined download of r, v, rho: exported on the system's stream into
+    // a staging set of its own, copied to the host on a copy stream; with
+    // removed particles a synchronous download (rows compacted on the host)
+    int download_async(int mask, const tsph_ale_host_state *o, std::string &err) {
+        int rc;
+        if (mask & ~(TSPH_ALE_F_R | TSPH_ALE_F_V | TSPH_ALE_F_RHO)) {
+            err = "tsph_ale_download_async: r, v and rho only";
+            return TSPH_ERR_ARG;
+        }
+        // (allowed while an upload is staged: the export reads the state the
+        // staged upload changes only when particle_to_cell applies it)
+        if ((rc = download_wait(err)) || (rc = normalize(err))) return rc;
+        uint32_t nl = 0;
+        ACK(cudaMemcpyAsync(&nl, fstart + ncells, 4, cudaMemcpyDeviceToHost, st));
+        ACK(cudaStreamSynchronize(st));
+        if ((long long)nl + nw != (long long)ntot) {
+            if (up_pending) {
+                err = "tsph_ale_download_async after removals with an upload staged";
+                return TSPH_ERR_STATE;
+            }
+            return download(mask, o, err);
+        }
+        if ((rc = transfer_streams(err))) return rc;
+        AleStage S{};
+        struct Want {
+            int bit;
+            double *host;
+            double **dev;
+            double **use;
+            int width;
+        };
+        const Want want[] = {{TSPH_ALE_F_R, o->r, &dstg.r, &S.r, 2},
+                             {TSPH_ALE_F_V, o->v, &dstg.v, &S.v, 2},
+                             {TSPH_ALE_F_RHO, o->rho, &dstg.rho, &S.rho, 1}};
+        for (const Want &q : want) {
+            if (!(mask & q.bit) || !q.host) continue;
+            if ((rc = stage(q.dev, (size_t)q.width, err))) return rc;
+            *q.use = *q.dev;
+        }
+        if ((rc = stage(&dstg.alive, 1, err))) return rc;
+        S.alive = dstg.alive;
+        k_ale_export<<<nblk(nw + nf), kBlock, 0, st>>>(A, fstart, ncells, W, nw, S, rho0, dp * dp,
+                                                       cs * cs * rho0 / 7.);
+        ACK(cudaGetLastError());
+        ACK(cudaEventRecord(ev_x, st));
+        ACK(cudaStreamWaitEvent(cs_d, ev_x, 0));
+        for (const Want &q : want)
+            if (*q.use)
+                ACK(cudaMemcpyAsync(q.host, *q.use, 8 * (size_t)q.width * ntot,
+                                    cudaMemcpyDeviceToHost, cs_d));
+        ACK(cudaEventRecord(ev_d, cs_d));
+        d_pending = true;
+        return 0;
+    }
+
+    int download_wait(std::string &err) {
+        if (!d_pending) return 0;
+        d_pending = false;
+        ACK(cudaEventSynchronize(ev_d));
+        return 0;
+    }
+
+    // staged upload of r, v, rho: host-to-device copies on a copy stream
+    // beside the work in flight, applied by the next particle_to_cell
+    int upload_async(int mask, const tsph_ale_host_state *in, std::string &err) {
+        int rc;
+        if (mask & ~(TSPH_ALE_F_R | TSPH_ALE_F_V | TSPH_ALE_F_RHO)) {
+            err = "tsph_ale_upload_async: r, v and rho only";
+            return TSPH_ERR_ARG;
+        }
+        if ((rc = no_staged_upload(err)) || (rc = transfer_streams(err))) return rc;
+        struct Put {
+            int bit;
+            const double *host;
+            double **dev;
+            int width;
+        };
+        const Put put[] = {{TSPH_ALE_F_R, in->r, &ustg.r, 2},
+                           {TSPH_ALE_F_V, in->v, &ustg.v, 2},
+                           {TSPH_ALE_F_RHO, in->rho, &ustg.rho, 1}};
+        // the staging set is free once the last staged import has read it
+        ACK(cudaStreamWaitEvent(cs_u, ev_imp, 0));
+        int m = 0;
+        for (const Put &q : put) {
+            if (!(mask & q.bit) || !q.host) continue;
+            if ((rc = stage(q.dev, (size_t)q.width, err))) return rc;
+            ACK(cudaMemcpyAsync(*q.dev, q.host, 8 * (size_t)q.width * ntot,
+                                cudaMemcpyHostToDevice, cs_u));
+            m |= q.bit;
+        }
+        ACK(cudaEventRecord(ev_up, cs_u));
+        up_pending = true;
+        up_mask = m;
+        return 0;
+    }
+
     // upload omega, v, rho and r of fluid particles (omega*v and omega*rho
     // follow), host arrays in the reference's order: staged by index, applied
     // per fluid row on the device (k_ale_import)
     int upload(int mask, const tsph_ale_host_state *in, std::string &err) {
+        if (int rc = no_staged_upload(err)) return rc;
         if (int rc = normalize(err)) return rc;
         ACK(cudaStreamSynchronize(st));
         uint32_t nl = 0;
@@ -1682,7 +1875,7 @@ class AleEngine {
             ACK(cudaMemcpyAsync(*q.dev, q.host, 8 * (size_t)q.width * ntot, cudaMemcpyHostToDevice, st));
             *q.use = *q.dev;
         }
-        k_ale_import<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, S, rho0);
+        k_ale_import<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, S, rho0, nw, ntot, nullptr);
         ACK(cudaGetLastError());
         ACK(cudaStreamSynchronize(st));
         if (mask & TSPH_ALE_F_R) cells = false;
@@ -1914,6 +2107,26 @@ int tsph_ale_upload(tsph_ale_system *s, int fields, const tsph_ale_host_state *i
     AREADY(s);
     if (!in) return afail(TSPH_ERR_ARG, "null input");
     ARUN(s->e.upload(fields, in, err_));
+    return TSPH_OK;
+}
+
+int tsph_ale_download_async(tsph_ale_system *s, int fields, const tsph_ale_host_state *out) {
+    AREADY(s);
+    if (!out) return afail(TSPH_ERR_ARG, "null output");
+    ARUN(s->e.download_async(fields, out, err_));
+    return TSPH_OK;
+}
+
+int tsph_ale_download_wait(tsph_ale_system *s) {
+    AREADY(s);
+    ARUN(s->e.download_wait(err_));
+    return TSPH_OK;
+}
+
+int tsph_ale_upload_async(tsph_ale_system *s, int fields, const tsph_ale_host_state *in) {
+    AREADY(s);
+    if (!in) return afail(TSPH_ERR_ARG, "null input");
+    ARUN(s->e.upload_async(fields, in, err_));
     return TSPH_OK;
 }
 

@@ -54,6 +54,7 @@ ABI_SYMBOLS = (
     "tsph_ale_np", "tsph_ale_divide_to_cells", "tsph_ale_particle_to_cell", "tsph_ale_gradient",
     "tsph_ale_forces", "tsph_ale_leapfrog_one", "tsph_ale_leapfrog_two", "tsph_ale_step",
     "tsph_ale_download", "tsph_ale_upload", "tsph_ale_sync", "tsph_ale_health",
+    "tsph_ale_download_async", "tsph_ale_download_wait", "tsph_ale_upload_async",
 )
 
 ALE_AS_WRITTEN = 0
@@ -203,6 +204,9 @@ def load(build_if_missing: bool = True) -> C.CDLL:
     L.tsph_ale_step.argtypes = [P, D, I, I]
     L.tsph_ale_download.argtypes = [P, I, C.POINTER(_AleHostState)]
     L.tsph_ale_upload.argtypes = [P, I, C.POINTER(_AleHostState)]
+    L.tsph_ale_download_async.argtypes = [P, I, C.POINTER(_AleHostState)]
+    L.tsph_ale_download_wait.argtypes = [P]
+    L.tsph_ale_upload_async.argtypes = [P, I, C.POINTER(_AleHostState)]
     L.tsph_ale_health.argtypes = [P, C.POINTER(C.c_uint32), I]
     _lib = L
     return L
@@ -801,6 +805,25 @@ class AleSystem:
         for k, v in ptrs.items():
             setattr(hs, k, v)
         _check(self._L.tsph_ale_download(self._h, int(mask), C.byref(hs)))
+
+    def download_async(self, mask, **ptrs):
+        """Pipelined download of r, v, rho into raw host pointers (pinned for
+        an overlap); valid after :meth:`download_wait`."""
+        hs = _AleHostState()
+        for k, v in ptrs.items():
+            setattr(hs, k, v)
+        _check(self._L.tsph_ale_download_async(self._h, int(mask), C.byref(hs)))
+
+    def download_wait(self):
+        _check(self._L.tsph_ale_download_wait(self._h))
+
+    def upload_async(self, mask, **ptrs):
+        """Staged upload of r, v, rho from raw host pointers (pinned for an
+        overlap), applied by the next :meth:`particle_to_cell`."""
+        hs = _AleHostState()
+        for k, v in ptrs.items():
+            setattr(hs, k, v)
+        _check(self._L.tsph_ale_upload_async(self._h, int(mask), C.byref(hs)))
 
     def sync(self):
         _check(self._L.tsph_ale_sync(self._h))
