@@ -59,6 +59,25 @@ struct AleConst {
     // twice the skin, since on kept cells a cell's y order may be off by two
     // moves of at most the skin each
     float reach;
+    float list_r2;  // (2h + 2 skin)^2: the radius of the lists kept between sorts
+};
+
+// neighbour lists of the flux kernel kept between sorts (kept cells): per
+// target (sorted row i) up to kAleList entries ent[k * nfa + i] (the staged
+// index << 2 | row code of its window, which repeats while the cells stay)
+// and their count cnt[i] (0xFF: the target takes the global-memory path);
+// cta_gen[b] the sort generation CTA b built them for, *gen the current one
+// (every sort increments it); lbin the fluid's binning positions, from which
+// they are built (2h + 2 skin: complete while every particle is within the
+// skin of its binning)
+struct AleLists {
+    uint16_t *ent;
+    uint8_t *cnt;
+    uint32_t *cta_gen;
+    const uint32_t *gen;
+    const float2 *lbin;
+    long long nfa;
+    int keep;
 };
 
 __device__ __forceinline__ float ale_eos(float s, const AleConst &K) {
@@ -421,8 +440,10 @@ __global__ void k_ale_rank_scatter(const uint32_t *__restrict__ key, const int *
                                    const uint32_t *__restrict__ tmp_src,
                                    const long long *__restrict__ tmp_y, Grid g, AleFluid S,
                                    AleFluid D, float rho0, float2 *__restrict__ lbin,
-                                   const uint32_t *__restrict__ gate) {
+                                   const uint32_t *__restrict__ gate, uint32_t *__restrict__ gen) {
     if (gated_off(gate)) return;
+    // a new cell order: the flux kernel's kept lists are stale
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(gen, 1u);
     const int n = *n_ptr;
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         const uint32_t src = tmp_src[j];
@@ -754,6 +775,8 @@ template <int SCHEME>
 __device__ __forceinline__ void ale_pair(float dx, float dy, float2 va, float sa, float rhoa,
                                          float4 qb, const AleConst &K, AleAcc &acc) {
     const float r2 = fmaf(dx, dx, dy * dy);
+    // a kept list holds neighbours up to 2h + 2 skin and the target itself
+    if (!(r2 > 0.f && r2 <= K.four_h2)) return;
     const float inv_r = rsqrtf(r2);
     const float r = r2 * inv_r;
     const float w1 = fmaf(-0.5f * K.inv_h, r, 1.f);
@@ -806,19 +829,22 @@ __device__ __forceinline__ void ale_pair(float dx, float dy, float2 va, float sa
 }
 
 // the bounded append of a row range that could overflow the list: one
-// candidate at a time, at most up to the list's end (the support test with
-// the particle itself and coincident particles excluded, 0 < r^2 <= 4h^2); a
-// candidate past the end sets `overflow`.  Inlined: out of line, its calls
-// from the unrolled loops made the kernel spill registers.
+// candidate at a time, at most up to the list's end (0 < r^2 <= h2: the
+// particle itself and coincident particles excluded; with `with_zero`
+// r^2 <= h2, for the lists kept between sorts); a candidate past the end
+// sets `overflow`.  Inlined: out of line, its calls from the unrolled loops
+// made the kernel spill registers.
 static __device__ __forceinline__ uint16_t *append_bounded_ale(const float2 *loc, uint16_t *lst,
                                                             uint16_t *w, int j0, int j1,
                                                             uint32_t code, float bx, float by,
-                                                            float h2, bool &overflow) {
+                                                            float h2, bool with_zero,
+                                                            bool &overflow) {
     uint16_t *const wend = lst + kAleList * kAleT;
     for (int j = j0; j < j1; j++) {
         const float2 lb = loc[j];
         const float dx = bx - lb.x, dy = by - lb.y;
-        if (in_support(fmaf(dx, dx, dy * dy), __float_as_uint(h2))) {
+        const float r2 = fmaf(dx, dx, dy * dy);
+        if (with_zero ? r2 <= h2 : in_support(r2, __float_as_uint(h2))) {
             if (w < wend) {
                 *w = (uint16_t)(((uint32_t)j << 2) | code);
                 w += kAleT;
@@ -830,10 +856,27 @@ static __device__ __forceinline__ uint16_t *append_bounded_ale(const float2 *loc
     return w;
 }
 
+// slot e of a window's staged block (segments walls 0, fluid 0, walls 1,
+// ...): the row j it stages, whether a wall, and x of its cell's origin
+// relative to the centre column's
+__device__ __forceinline__ void ale_slot(int e, const int *w0, const int *f0, const int *wb,
+                                         const int *fb, float khf, int &j, bool &wall,
+                                         float &xs) {
+    j = e + w0[0];
+    wall = true;
+    xs = -khf;
+    if (e >= fb[0]) { j = e - fb[0] + f0[0]; wall = false; }
+    if (e >= wb[1]) { j = e - wb[1] + w0[1]; wall = true; xs = 0.f; }
+    if (e >= fb[1]) { j = e - fb[1] + f0[1]; wall = false; }
+    if (e >= wb[2]) { j = e - wb[2] + w0[2]; wall = true; xs = khf; }
+    if (e >= fb[2]) { j = e - fb[2] + f0[2]; wall = false; }
+}
+
 template <int SCHEME>
 __global__ void __launch_bounds__(kAleT, 8)
 k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
-                 const uint32_t *__restrict__ wstart, AleWalls Wl, Grid g, AleConst K) {
+                 const uint32_t *__restrict__ wstart, AleWalls Wl, Grid g, AleConst K,
+                 AleLists L) {
     __shared__ AleTile sm;
     const int tid = threadIdx.x;
     const int ncy = g.ncy;
@@ -841,6 +884,11 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
     const int t0 = blockIdx.x * kAleT;
     if (t0 >= nl) return;
     const int t1 = min(t0 + kAleT, nl);
+    // lists: mode 0 built per window (kept cells off), 1 built from the
+    // binning positions and stored (first call after a sort), 2 the stored
+    // ones (the cells, hence the windows, unchanged since)
+    int mode = 0;
+    if (L.keep) mode = L.cta_gen[blockIdx.x] == *L.gen ? 2 : 1;
     if (tid < 4) sm.offy[tid] = tid < 3 ? (float)(1 - tid) * g.khf : 0.f;
     const float khf = g.khf;
     const float reach = K.reach;
@@ -912,24 +960,21 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
             float st_s[kStage];
             double st_o[kStage];
             bool st_w[kStage];
+            const float2 *const floc = mode == 1 ? L.lbin : F.loc;
 #pragma unroll
             for (int u = 0; u < kStage; u++) {
                 const int e = tid + u * kAleT;
-                int j = e + w0[0];
-                bool wall = true;
-                float xs = -khf;  // x of the cell's origin relative to the centre column's
-                if (e >= fb[0]) { j = e - fb[0] + f0[0]; wall = false; }
-                if (e >= wb[1]) { j = e - wb[1] + w0[1]; wall = true; xs = 0.f; }
-                if (e >= fb[1]) { j = e - fb[1] + f0[1]; wall = false; }
-                if (e >= wb[2]) { j = e - wb[2] + w0[2]; wall = true; xs = khf; }
-                if (e >= fb[2]) { j = e - fb[2] + f0[2]; wall = false; }
+                int j;
+                bool wall;
+                float xs;
+                ale_slot(e, w0, f0, wb, fb, khf, j, wall, xs);
                 st_w[u] = wall;
                 st_l[u] = make_float2(0.f, 0.f);
                 st_v[u] = make_float2(0.f, 0.f);
                 st_s[u] = 0.f;
                 st_o[u] = 0.0;
                 if (e < tot) {
-                    st_l[u] = __ldg((wall ? Wl.loc : F.loc) + j);
+                    st_l[u] = __ldg((wall ? Wl.loc : floc) + j);
                     st_l[u].x += xs;
                     st_v[u] = __ldg((wall ? Wl.n : F.v) + j);
                     st_s[u] = __ldg((wall ? Wl.s : F.s) + j);
@@ -947,22 +992,31 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                 }
             }
             __syncthreads();
-            if (active) {
+            bool overflow = false;
+            int cnt = 0;
+            uint16_t *const lst = sm.list + tid;
+            if (active && mode == 2) {
+                // the list stored after the last sort
+                const int c = (int)L.cnt[i];
+                if (c > kAleList) {
+                    overflow = true;
+                } else {
+                    for (int k = 0; k < c; k++) lst[k * kAleT] = L.ent[(size_t)k * L.nfa + i];
+                    cnt = c;
+                }
+            } else if (active) {
                 const int cy = (int)ki - cx * ncy;
                 const int own = fb[1] + (i - f0[1]);
                 const float2 la = sm.loc[own];
-                const float4 qa = sm.q[own];
-                va = make_float2(qa.x, qa.y);
-                sa = qa.z;
-                const float rhoa = K.rho0 + sa;
-                // in-support neighbours into the list (entry: staged index << 2
-                // | row code); per column the rows below, own and above are
-                // staged ranges [R0, R1), [R1, R2), [R2, R3).  A range that
-                // could overflow the list is appended one at a time, bounded
-                // (a target with more than kAleList neighbours takes the
-                // global-memory path)
-                bool overflow = false;
-                uint16_t *const lst = sm.list + tid;
+                // neighbours into the list (entry: staged index << 2 | row
+                // code): mode 0 the in-support ones (0 < r^2 <= 4h^2), mode 1
+                // those within 2h + 2 skin of the binning positions (the
+                // target itself included: the pair terms skip r = 0); per
+                // column the rows below, own and above are staged ranges
+                // [R0, R1), [R1, R2), [R2, R3).  A range that could overflow
+                // the list is appended one at a time, bounded (a target with
+                // more than kAleList neighbours takes the global-memory path)
+                const float h2 = mode == 1 ? K.list_r2 : K.four_h2;
                 uint16_t *const wend = lst + kAleList * kAleT;
                 uint16_t *w = lst;
                 const float by_b = la.y + khf, by_a = la.y - khf;
@@ -981,36 +1035,64 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                         const int R0 = hb ? base + offs[q - 1] : R1;
                         const int R3 = ha ? base + offs[q + 2] : R2;
                         if (wend - w < (R2 - R1) * kAleT)
-                            w = append_bounded_ale(sm.loc, lst, w, R1, R2, 1u, la.x, la.y,
-                                                   K.four_h2, overflow);
-                        else if (d == 1 && kind == 1)
-                            w = scan_own<kAleT, true>(sm.loc, R1, R2, la.x, la.y, K.four_h2, w);
+                            w = append_bounded_ale(sm.loc, lst, w, R1, R2, 1u, la.x, la.y, h2,
+                                                   mode == 1, overflow);
+                        else if (d == 1 && kind == 1 && mode == 0)
+                            w = scan_own<kAleT, true>(sm.loc, R1, R2, la.x, la.y, h2, w);
                         else
-                            w = scan_own<kAleT, false>(sm.loc, R1, R2, la.x, la.y, K.four_h2, w);
+                            w = scan_own<kAleT, false>(sm.loc, R1, R2, la.x, la.y, h2, w);
                         if (wend - w < (R3 - R2) * kAleT)
-                            w = append_bounded_ale(sm.loc, lst, w, R2, R3, 2u, la.x, by_a,
-                                                   K.four_h2, overflow);
+                            w = append_bounded_ale(sm.loc, lst, w, R2, R3, 2u, la.x, by_a, h2,
+                                                   mode == 1, overflow);
                         else
-                            w = scan_above<kAleT>(sm.loc, R2, R3, la.x, by_a, K.four_h2, reach, w);
+                            w = scan_above<kAleT>(sm.loc, R2, R3, la.x, by_a, h2, reach, w);
                         if (wend - w < (R1 - R0) * kAleT)
-                            w = append_bounded_ale(sm.loc, lst, w, R0, R1, 0u, la.x, by_b,
-                                                   K.four_h2, overflow);
+                            w = append_bounded_ale(sm.loc, lst, w, R0, R1, 0u, la.x, by_b, h2,
+                                                   mode == 1, overflow);
                         else
-                            w = scan_below<kAleT>(sm.loc, R0, R1, la.x, by_b, K.four_h2, reach, w);
+                            w = scan_below<kAleT>(sm.loc, R0, R1, la.x, by_b, h2, reach, w);
                     }
                 }
-                const int cnt = (int)((w - lst) / kAleT);
-                if (!overflow) {
-                    for (int k = 0; k < cnt; k++) {
-                        const uint32_t e = lst[k * kAleT];
-                        const int j = (int)(e >> 2);
-                        const float oy = sm.offy[e & 3u];
-                        const float2 lb = sm.loc[j];
-                        ale_pair<SCHEME>(la.x - lb.x, (la.y + oy) - lb.y, va, sa, rhoa, sm.q[j], K,
-                                 acc);
-                    }
-                    done = true;
+                cnt = (int)((w - lst) / kAleT);
+                if (mode == 1) {
+                    L.cnt[i] = overflow ? (uint8_t)0xFF : (uint8_t)cnt;
+                    if (!overflow)
+                        for (int k = 0; k < cnt; k++) L.ent[(size_t)k * L.nfa + i] = lst[k * kAleT];
                 }
+            }
+            if (mode == 1) {
+                // the pair terms at the current positions: the fluid's staged
+                // positions again (the walls' do not move)
+                __syncthreads();
+                for (int e = tid; e < tot; e += kAleT) {
+                    int j;
+                    bool wall;
+                    float xs;
+                    ale_slot(e, w0, f0, wb, fb, khf, j, wall, xs);
+                    if (!wall) {
+                        float2 l = __ldg(F.loc + j);
+                        l.x += xs;
+                        sm.loc[e] = l;
+                    }
+                }
+                __syncthreads();
+            }
+            if (active && !overflow) {
+                const int own = fb[1] + (i - f0[1]);
+                const float2 la = sm.loc[own];
+                const float4 qa = sm.q[own];
+                va = make_float2(qa.x, qa.y);
+                sa = qa.z;
+                const float rhoa = K.rho0 + sa;
+                for (int k = 0; k < cnt; k++) {
+                    const uint32_t e = lst[k * kAleT];
+                    const int j = (int)(e >> 2);
+                    const float oy = sm.offy[e & 3u];
+                    const float2 lb = sm.loc[j];
+                    ale_pair<SCHEME>(la.x - lb.x, (la.y + oy) - lb.y, va, sa, rhoa, sm.q[j], K,
+                                     acc);
+                }
+                done = true;
             }
         }
         if (active && !done) {
@@ -1079,6 +1161,8 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
         cur = we;
         rows = kAleRows;
     }
+    // (the generation changes only with a sort, never during this launch)
+    if (mode == 1 && tid == 0) L.cta_gen[blockIdx.x] = *L.gen;
 }
 
 #define ACK(call)                                                                 \
@@ -1231,6 +1315,11 @@ class AleEngine {
     uint32_t *gate = nullptr;
     unsigned long long *sort_runs = nullptr;
     int gated_blocks = 4 * 152;  // grid of a gated launch: 4 blocks per SM
+    // the flux kernel's lists kept between sorts (AleLists)
+    uint16_t *list_ent = nullptr;
+    uint8_t *list_cnt = nullptr;
+    uint32_t *list_cta_gen = nullptr, *list_gen = nullptr;
+    long long list_nfa = 0;
     // the leap-frog copies (omega_o, ...) hold part one's values: false after
     // a fused step (its re-binning leaves them behind)
     bool copies_valid = true;
@@ -1352,6 +1441,10 @@ class AleEngine {
         // inside the 3 x 3 cell block (kh >= 2h + 2 skin) with a margin
         skin = (float)std::max(0.0, 0.95 * 0.5 * (kh - 2.0 * h));
         K.reach = 2.f * K.h * 1.0001f + 2.f * skin;
+        {
+            const double rl = 2.0 * h + 2.0 * (double)skin;
+            K.list_r2 = (float)(rl * rl);
+        }
         int rc;
         if ((rc = alloc(&grad, (size_t)12 * nf, err))) return rc;
         ACK(cudaMemset(grad, 0, sizeof(float) * 12 * std::max(nf, 1)));
@@ -1364,6 +1457,9 @@ class AleEngine {
             (rc = alloc(&tmp_y, nf, err)) ||
             (rc = alloc(&health, 1, err)) || (rc = alloc(&lbin, nf, err)) ||
             (rc = alloc(&gate, 1, err)) || (rc = alloc(&sort_runs, 1, err)) ||
+            (rc = alloc(&list_ent, (size_t)kAleList * (size_t)(nblk(nf, kAleT) * kAleT), err)) ||
+            (rc = alloc(&list_cnt, nf, err)) ||
+            (rc = alloc(&list_cta_gen, nblk(nf, kAleT), err)) || (rc = alloc(&list_gen, 1, err)) ||
             (rc = alloc(&dbx, bx.size(), err)) ||
             (rc = alloc(&dby, by.size(), err)) || (rc = alloc(&dox, ox.size(), err)) ||
             (rc = alloc(&doy, oy.size(), err)))
@@ -1376,6 +1472,9 @@ class AleEngine {
         ACK(cudaMemset(health, 0, 4));
         ACK(cudaMemset(gate, 0, 4));
         ACK(cudaMemset(sort_runs, 0, 8));
+        list_nfa = (long long)nblk(nf, kAleT) * kAleT;
+        ACK(cudaMemset(list_cta_gen, 0xFF, 4 * (size_t)nblk(nf, kAleT)));
+        ACK(cudaMemset(list_gen, 0, 4));
         grid.ax = Axis{dbx, dox, ncx};
         grid.ay = Axis{dby, doy, ncy};
         grid.ncx = ncx;
@@ -1492,11 +1591,13 @@ class AleEngine {
         k_place<<<bf, kBlock, 0, st>>>(keyB, slotB, X.id, ntot_, fstart, tmp_id, tmp_src, X.r,
                                        tmp_y, g);
         if (step_sort)
-            k_ale_rank_scatter<true><<<bf, kBlock, 0, st>>>(
-                keyB, ntot_, fstart, tmp_id, tmp_src, tmp_y, grid, X, Y, (float)rho0, lbin, g);
+            k_ale_rank_scatter<true><<<bf, kBlock, 0, st>>>(keyB, ntot_, fstart, tmp_id, tmp_src,
+                                                             tmp_y, grid, X, Y, (float)rho0, lbin,
+                                                             g, list_gen);
         else
-            k_ale_rank_scatter<false><<<bf, kBlock, 0, st>>>(
-                keyB, ntot_, fstart, tmp_id, tmp_src, tmp_y, grid, X, Y, (float)rho0, lbin, g);
+            k_ale_rank_scatter<false><<<bf, kBlock, 0, st>>>(keyB, ntot_, fstart, tmp_id, tmp_src,
+                                                              tmp_y, grid, X, Y, (float)rho0, lbin,
+                                                              g, list_gen);
         ACK(cudaGetLastError());
         return 0;
     }
@@ -1546,15 +1647,24 @@ class AleEngine {
         return 0;
     }
 
+    // the flux kernel's kept lists: on with kept cells (the cells, hence
+    // its windows, change only with a sort, which makes them stale)
+    AleLists lists() const {
+        return AleLists{list_ent, list_cnt, list_cta_gen, list_gen, lbin, list_nfa,
+                        keep && skin > 0.f ? 1 : 0};
+    }
+
     int forces(std::string &err) {
         if (int rc = no_staged_upload(err)) return rc;
         if (int rc = normalize(err)) return rc;
         if (scheme == TSPH_ALE_MUSCL)
             k_ale_flux<1><<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
         else if (scheme == TSPH_ALE_FIRST_ORDER)
-            k_ale_flux_tiled<2><<<nblk(nf, kAleT), kAleT, 0, st>>>(A, fstart, wstart, W, grid, K);
+            k_ale_flux_tiled<2><<<nblk(nf, kAleT), kAleT, 0, st>>>(A, fstart, wstart, W, grid, K,
+                                                                   lists());
         else
-            k_ale_flux_tiled<0><<<nblk(nf, kAleT), kAleT, 0, st>>>(A, fstart, wstart, W, grid, K);
+            k_ale_flux_tiled<0><<<nblk(nf, kAleT), kAleT, 0, st>>>(A, fstart, wstart, W, grid, K,
+                                                                   lists());
         ACK(cudaGetLastError());
         return 0;
     }
