@@ -78,6 +78,7 @@ struct AleLists {
     const float2 *lbin;
     long long nfa;
     int keep;
+    uint32_t *gate_clear;  // the fused step's sort word, cleared at the start (or null)
 };
 
 __device__ __forceinline__ float ale_eos(float s, const AleConst &K) {
@@ -130,6 +131,7 @@ __device__ __forceinline__ double add_f(double x, float rate, float step) {
 // Integrate_LeapFrog_partOne, src/RALESPH_integration.h:10-36 (in place)
 __global__ void k_ale_lf1(AleFluid F, const uint32_t *__restrict__ fstart, int ncells, float hf,
                           float rho0) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_live_ale(fstart, ncells)) return;
     const double om = F.om[i], omr = F.omr[i];
@@ -305,6 +307,7 @@ __global__ void k_ale_lf2_keep(AleFluid F, const uint32_t *__restrict__ fstart, 
                                float hf, int step, float rho0, BoxBits boxb,
                                const float2 *__restrict__ lbin, float sig2,
                                uint32_t *__restrict__ gate, uint32_t *__restrict__ health) {
+    pdl_enter();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_live_ale(fstart, g.ncells)) return;
     float sn;
@@ -334,6 +337,7 @@ __global__ void k_ale_hist_gated(AleFluid F, const uint32_t *__restrict__ fstart
                                  uint32_t *__restrict__ slot, uint32_t *__restrict__ counts,
                                  uint32_t *__restrict__ health, const uint32_t *__restrict__ gate,
                                  unsigned long long *__restrict__ runs) {
+    pdl_enter();
     if (gated_off(gate)) return;
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(runs, 1ull);
     const int nl = n_live_ale(fstart, g.ncells);
@@ -354,6 +358,7 @@ __global__ void k_ale_hist_gated(AleFluid F, const uint32_t *__restrict__ fstart
 // (the leap-frog copies included: they hold the state at the end of the step)
 __global__ void k_ale_copy_gated(AleFluid S, AleFluid D, const uint32_t *__restrict__ fstart,
                                  int ncells, const uint32_t *__restrict__ gate) {
+    pdl_enter();
     if (gated_off(gate)) return;
     const int n = (int)fstart[ncells + 1];
     for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
@@ -441,6 +446,7 @@ __global__ void k_ale_rank_scatter(const uint32_t *__restrict__ key, const int *
                                    const long long *__restrict__ tmp_y, Grid g, AleFluid S,
                                    AleFluid D, float rho0, float2 *__restrict__ lbin,
                                    const uint32_t *__restrict__ gate, uint32_t *__restrict__ gen) {
+    pdl_enter();
     if (gated_off(gate)) return;
     // a new cell order: the flux kernel's kept lists are stale
     if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(gen, 1u);
@@ -878,7 +884,11 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                  const uint32_t *__restrict__ wstart, AleWalls Wl, Grid g, AleConst K,
                  AleLists L) {
     __shared__ AleTile sm;
+    pdl_enter();
     const int tid = threadIdx.x;
+    // the step's sort word, raised again by its part two (this launch runs
+    // after the last sort's kernels have read it)
+    if (L.gate_clear && blockIdx.x == 0 && tid == 0) *L.gate_clear = 0u;
     const int ncy = g.ncy;
     const int nl = n_live_ale(fstart, g.ncells);
     const int t0 = blockIdx.x * kAleT;
@@ -1367,6 +1377,23 @@ class AleEngine {
         binned = false;
     }
 
+    // a launch with programmatic dependent launch: the kernel (which starts
+    // with pdl_enter) is scheduled while the previous one finishes
+    template <typename... KA, typename... Args>
+    int alaunch(void (*kern)(KA...), int grid, int block, std::string &err, Args... args) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3((unsigned)grid);
+        cfg.blockDim = dim3((unsigned)block);
+        cfg.stream = st;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        ACK(cudaLaunchKernelEx(&cfg, kern, args...));
+        return 0;
+    }
+
     // the state at the end of the last step (undo a part one applied ahead)
     int normalize(std::string &err) {
         if (!half) return 0;
@@ -1585,21 +1612,28 @@ class AleEngine {
         // gated: grid-stride kernels on a small grid (cheap to skip)
         const int bn = g ? std::min(nblk(n), gated_blocks) : nblk(n);
         const int bf = g ? std::min(nblk(nf), gated_blocks) : nblk(nf);
-        k_scan_tiles_clear<<<nt, kScanThreads, 0, st>>>(counts, fstart, tiles, n, g);
-        k_scan_add_tiles<<<bn, kBlock, 0, st>>>(fstart, tiles, nt, n, g);
+        int rc;
         const int *ntot_ = reinterpret_cast<const int *>(fstart + ncells + 1);
-        k_place<<<bf, kBlock, 0, st>>>(keyB, slotB, X.id, ntot_, fstart, tmp_id, tmp_src, X.r,
-                                       tmp_y, g);
+        const long long *ty = tmp_y;
+        if ((rc = alaunch(k_scan_tiles_clear, nt, kScanThreads, err, counts, fstart, tiles, n, g)) ||
+            (rc = alaunch(k_scan_add_tiles, bn, kBlock, err, fstart, (const uint32_t *)tiles, nt,
+                          n, g)) ||
+            (rc = alaunch(k_place, bf, kBlock, err, (const uint32_t *)keyB,
+                          (const uint32_t *)slotB, (const uint32_t *)X.id, ntot_,
+                          (const uint32_t *)fstart, tmp_id, tmp_src, (const double2 *)X.r, tmp_y,
+                          g)))
+            return rc;
         if (step_sort)
-            k_ale_rank_scatter<true><<<bf, kBlock, 0, st>>>(keyB, ntot_, fstart, tmp_id, tmp_src,
-                                                             tmp_y, grid, X, Y, (float)rho0, lbin,
-                                                             g, list_gen);
+            rc = alaunch(k_ale_rank_scatter<true>, bf, kBlock, err, (const uint32_t *)keyB, ntot_,
+                         (const uint32_t *)fstart, (const uint32_t *)tmp_id,
+                         (const uint32_t *)tmp_src, ty, grid, X, Y, (float)rho0, lbin, g,
+                         list_gen);
         else
-            k_ale_rank_scatter<false><<<bf, kBlock, 0, st>>>(keyB, ntot_, fstart, tmp_id, tmp_src,
-                                                              tmp_y, grid, X, Y, (float)rho0, lbin,
-                                                              g, list_gen);
-        ACK(cudaGetLastError());
-        return 0;
+            rc = alaunch(k_ale_rank_scatter<false>, bf, kBlock, err, (const uint32_t *)keyB, ntot_,
+                         (const uint32_t *)fstart, (const uint32_t *)tmp_id,
+                         (const uint32_t *)tmp_src, ty, grid, X, Y, (float)rho0, lbin, g,
+                         list_gen);
+        return rc;
     }
 
     int particle_to_cell(std::string &err) {
@@ -1649,22 +1683,21 @@ class AleEngine {
 
     // the flux kernel's kept lists: on with kept cells (the cells, hence
     // its windows, change only with a sort, which makes them stale)
-    AleLists lists() const {
+    AleLists lists(uint32_t *clear = nullptr) const {
         return AleLists{list_ent, list_cnt, list_cta_gen, list_gen, lbin, list_nfa,
-                        keep && skin > 0.f ? 1 : 0};
+                        keep && skin > 0.f ? 1 : 0, clear};
     }
+    uint32_t *gate_clear = nullptr;  // set by the fused step around its forces()
 
     int forces(std::string &err) {
         if (int rc = no_staged_upload(err)) return rc;
         if (int rc = normalize(err)) return rc;
         if (scheme == TSPH_ALE_MUSCL)
             k_ale_flux<1><<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
-        else if (scheme == TSPH_ALE_FIRST_ORDER)
-            k_ale_flux_tiled<2><<<nblk(nf, kAleT), kAleT, 0, st>>>(A, fstart, wstart, W, grid, K,
-                                                                   lists());
         else
-            k_ale_flux_tiled<0><<<nblk(nf, kAleT), kAleT, 0, st>>>(A, fstart, wstart, W, grid, K,
-                                                                   lists());
+            return alaunch(scheme == TSPH_ALE_FIRST_ORDER ? k_ale_flux_tiled<2> : k_ale_flux_tiled<0>,
+                           nblk(nf, kAleT), kAleT, err, A, (const uint32_t *)fstart,
+                           (const uint32_t *)wstart, W, grid, K, lists(gate_clear));
         ACK(cudaGetLastError());
         return 0;
     }
@@ -1678,8 +1711,9 @@ class AleEngine {
             return 0;
         }
         if (int rc = normalize(err)) return rc;
-        k_ale_lf1<<<nblk(nf), kBlock, 0, st>>>(A, fstart, ncells, (float)(dt * 0.5), (float)rho0);
-        ACK(cudaGetLastError());
+        if (int rc = alaunch(k_ale_lf1, nblk(nf), kBlock, err, A, (const uint32_t *)fstart, ncells,
+                             (float)(dt * 0.5), (float)rho0))
+            return rc;
         copies_valid = true;
         return 0;
     }
@@ -1715,17 +1749,25 @@ class AleEngine {
             if (stp > 1 && !half && (rc = lf1(dt, err))) return rc;
             half = false;
             if (scheme == TSPH_ALE_MUSCL && (rc = gradient(err))) return rc;
-            if ((rc = forces(err))) return rc;
+            // on kept cells the tiled flux kernel clears the sort word
+            const bool tiled = scheme != TSPH_ALE_MUSCL;
+            gate_clear = kept && tiled ? gate : nullptr;
+            rc = forces(err);
+            gate_clear = nullptr;
+            if (rc) return rc;
             if (kept) {
-                ACK(cudaMemsetAsync(gate, 0, 4, st));
-                k_ale_lf2_keep<<<nblk(nf), kBlock, 0, st>>>(
-                    A, fstart, grid, (float)dt, (float)(dt * 0.5), stp, (float)rho0, boxb, lbin,
-                    skin * skin, gate, health);
+                if (!tiled) ACK(cudaMemsetAsync(gate, 0, 4, st));
                 const int bg = std::min(nblk(nf), gated_blocks);
-                k_ale_hist_gated<<<bg, kBlock, 0, st>>>(A, fstart, grid, boxb, 1, keyB, slotB,
-                                                        counts, health, gate, sort_runs);
-                if ((rc = sort(A, B, false, err, gate))) return rc;
-                k_ale_copy_gated<<<bg, kBlock, 0, st>>>(B, A, fstart, ncells, gate);
+                if ((rc = alaunch(k_ale_lf2_keep, nblk(nf), kBlock, err, A, (const uint32_t *)fstart,
+                                  grid, (float)dt, (float)(dt * 0.5), stp, (float)rho0, boxb,
+                                  (const float2 *)lbin, skin * skin, gate, health)) ||
+                    (rc = alaunch(k_ale_hist_gated, bg, kBlock, err, A, (const uint32_t *)fstart,
+                                  grid, boxb, 1, keyB, slotB, counts, health,
+                                  (const uint32_t *)gate, sort_runs)) ||
+                    (rc = sort(A, B, false, err, gate)) ||
+                    (rc = alaunch(k_ale_copy_gated, bg, kBlock, err, B, A, (const uint32_t *)fstart,
+                                  ncells, (const uint32_t *)gate)))
+                    return rc;
                 half = true;
                 half_dt = dt;
             } else {
