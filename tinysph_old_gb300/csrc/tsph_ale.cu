@@ -1353,9 +1353,6 @@ class AleEngine {
     double *dox = nullptr, *doy = nullptr;
 
     ~AleEngine() {
-        if (d_pending) cudaEventSynchronize(ev_d);
-        if (st) cudaStreamSynchronize(st);
-        if (cs_u) cudaStreamSynchronize(cs_u);
         release();
         for (cudaStream_t q : {cs_d, cs_u})
             if (q) cudaStreamDestroy(q);
@@ -1365,6 +1362,10 @@ class AleEngine {
     }
 
     void release() {
+        // copies still in flight read or write the staging sets: done first
+        if (d_pending) cudaEventSynchronize(ev_d);
+        if (cs_u) cudaStreamSynchronize(cs_u);
+        if (st) cudaStreamSynchronize(st);
         for (void *q : allocs) cudaFree(q);
         allocs.clear();
         stg = AleStage{};
