@@ -32,3 +32,12 @@ def test_kernel_launch_count_per_graph_step(gpu_tsph):
     s.download()
     fresh = s.kernel_launches(reset=True)
     assert stale == fresh + 1, (stale, fresh)
+    # a download that does not ask for the pressure leaves it stale: the
+    # full download after it still runs the equation of state
+    s.step(case.wall_model, case.dt, 1)
+    s.kernel_launches(reset=True)
+    s.download(gpu_tsph.F_R | gpu_tsph.F_V | gpu_tsph.F_RHO)
+    no_p = s.kernel_launches(reset=True)
+    s.download()
+    with_p = s.kernel_launches(reset=True)
+    assert with_p == fresh + 1 and no_p < with_p, (no_p, with_p, fresh)

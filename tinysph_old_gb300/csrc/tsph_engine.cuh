@@ -162,6 +162,7 @@ template <typename T> class Engine final : public EngineBase {
     // the state the reference's step leaves (p = EOS(rho), its step body
     // :110-111), without an EOS launch per step of a time loop.
     bool p_stale_ = false;
+    static constexpr int kFieldP = 1 << 5;  // the pressure's bit in a field mask (TSPH_F_P)
     int fresh_p(std::string &err) {
         if (!p_stale_) return 0;
         const int rc = launch(CAT_OTHER, k_eos<T>, blocks_for(nw_ + nf_), kBlock, err, F_,
@@ -1872,7 +1873,8 @@ template <typename T> class Engine final : public EngineBase {
 
     int download(int mask, double *r, double *v, double *a, double *rho, double *drho, double *p,
                  int32_t *index, int32_t *type, std::string &err) override {
-        TSPH_FRESH_P(err);
+        // the stored pressure is brought up to date only when it is asked for
+        if (mask & kFieldP) TSPH_FRESH_P(err);
         if (up_pending_) {  // its staging set holds the staged upload
             err = "an upload is staged: call tsph_particle_to_cell first";
             return 3;
@@ -1931,7 +1933,7 @@ template <typename T> class Engine final : public EngineBase {
     // path (their rows are compacted on the host).
     int download_async(int mask, double *r, double *v, double *a, double *rho, double *drho,
                        double *p, std::string &err) override {
-        TSPH_FRESH_P(err);
+        if (mask & kFieldP) TSPH_FRESH_P(err);
         int rc;
         if (mask & ~63) {
             err = "tsph_download_async: r, v, a, rho, drho and p only";
