@@ -533,10 +533,13 @@ def run_ale(args, rank, world, local):
                               "frac": step_bytes * value / world / 1e9 / peak},
             "sorts_per_step": sorts_per_step,
             "kernel_us_per_step": kernel_split,
-            # kept cells: fluxes, part two with the next part one, and the six
-            # sort kernels (launched every step, gated on the device);
-            # otherwise part one, fluxes, part two and four sort kernels
-            "gpu_launches": args.steps * ((8 if kept else 7) + (1 if args.scheme == "muscl" else 0)),
+            # kept cells: the fluxes with part two and the next part one in
+            # one launch (MUSCL: the gradient, the fluxes, part two), and
+            # the six sort kernels (launched every step, gated on the
+            # device); otherwise part one, fluxes, part two and four sort
+            # kernels
+            "gpu_launches": args.steps * ((7 if args.scheme != "muscl" else 9) if kept
+                                          else (8 if args.scheme == "muscl" else 7)),
             "clocks": clocks.summary(),
             "health": s.health(),
         }

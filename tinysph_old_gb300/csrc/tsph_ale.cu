@@ -81,6 +81,20 @@ struct AleLists {
     uint32_t *gate_clear;  // the fused step's sort word, cleared at the start (or null)
 };
 
+// the fused step's part two (and next part one) in the flux kernel's
+// epilogue (NEXT): each target's new state goes to D, the spare set (other
+// CTAs still read the target's half-step state as a neighbour); the sort
+// word of this step is `gate_set` (raised by a move past the skin or a
+// removal), `gate_clear_next` the next step's, cleared here (the two
+// alternate: a launch cannot clear the word its own blocks raise)
+struct AleNext {
+    AleFluid D;
+    float dtf, hf, rho0, sig2;
+    int step;
+    BoxBits boxb;
+    uint32_t *gate_set, *gate_clear_next, *health;
+};
+
 __device__ __forceinline__ float ale_eos(float s, const AleConst &K) {
     const float x = s * K.inv_rho0;
     return K.b_eos * x * (7.f + x * (21.f + x * (35.f + x * (35.f + x * (21.f + x * (7.f + x))))));
@@ -878,17 +892,20 @@ __device__ __forceinline__ void ale_slot(int e, const int *w0, const int *f0, co
     if (e >= fb[2]) { j = e - fb[2] + f0[2]; wall = false; }
 }
 
-template <int SCHEME>
+template <int SCHEME, bool NEXT>
 __global__ void __launch_bounds__(kAleT, 8)
 k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                  const uint32_t *__restrict__ wstart, AleWalls Wl, Grid g, AleConst K,
-                 AleLists L) {
+                 AleLists L, AleNext N) {
     __shared__ AleTile sm;
     pdl_enter();
     const int tid = threadIdx.x;
     // the step's sort word, raised again by its part two (this launch runs
-    // after the last sort's kernels have read it)
-    if (L.gate_clear && blockIdx.x == 0 && tid == 0) *L.gate_clear = 0u;
+    // after the last sort's kernels have read it); fused: the next step's
+    if (blockIdx.x == 0 && tid == 0) {
+        if (NEXT) *N.gate_clear_next = 0u;
+        else if (L.gate_clear) *L.gate_clear = 0u;
+    }
     const int ncy = g.ncy;
     const int nl = n_live_ale(fstart, g.ncells);
     const int t0 = blockIdx.x * kAleT;
@@ -1157,15 +1174,38 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
                     if (j != i && F.id[j] < me && ale_has_support(F, fstart, wstart, Wl, g, K, j))
                         zero = false;
             }
-            if (zero) {
-                F.dom[i] = 0.f;
-                F.domr[i] = 0.f;
-                F.domv[i] = make_float2(0.f, 0.f);
-            } else {
+            float rd = 0.f, rr = 0.f;
+            float2 rv = make_float2(0.f, 0.f);
+            if (!zero) {
                 const float ao = (float)F.om[i];
-                F.dom[i] = acc.dom * ao;
-                F.domr[i] = acc.domr * ao;
-                F.domv[i] = make_float2(acc.dvx * ao, acc.dvy * ao - K.g * ao * (K.rho0 + sa));
+                rd = acc.dom * ao;
+                rr = acc.domr * ao;
+                rv = make_float2(acc.dvx * ao, acc.dvy * ao - K.g * ao * (K.rho0 + sa));
+            }
+            F.dom[i] = rd;
+            F.domr[i] = rr;
+            F.domv[i] = rv;
+            if (NEXT) {
+                // k_ale_lf2_keep for this target, into the spare set
+                float sn;
+                float2 vn;
+                const double2 rn = lf2<kLf2KeptNext>(F, i, N.D, i, N.dtf, N.hf, N.step, N.rho0, sn, vn);
+                N.D.dom[i] = rd;
+                N.D.domr[i] = rr;
+                N.D.domv[i] = rv;
+                N.D.key[i] = ki;
+                N.D.id[i] = F.id[i];
+                if (!(vn.x == vn.x) || !(vn.y == vn.y) || !(sn == sn)) atomicOr(N.health, kHealthNan);
+                if (out_of_domain_bits(rn, N.boxb)) {
+                    atomicOr(N.health, kHealthRemoved);
+                    *N.gate_set = 1u;
+                } else {
+                    const float2 l = cell_local(g, rn, cx, cy);
+                    N.D.loc[i] = l;
+                    const float2 b = L.lbin[i];
+                    const float ex = l.x - b.x, ey = l.y - b.y;
+                    if (!(fmaf(ex, ex, ey * ey) <= N.sig2)) *N.gate_set = 1u;
+                }
             }
         }
         cur = we;
@@ -1323,6 +1363,8 @@ class AleEngine {
     float skin = 0.f;
     float2 *lbin = nullptr;
     uint32_t *gate = nullptr;
+    uint32_t *gate2 = nullptr;  // the fused steps' two alternating sort words
+    int gate_parity = 0;
     unsigned long long *sort_runs = nullptr;
     int gated_blocks = 4 * 152;  // grid of a gated launch: 4 blocks per SM
     // the flux kernel's lists kept between sorts (AleLists)
@@ -1484,7 +1526,8 @@ class AleEngine {
             (rc = alloc(&tmp_id, nf, err)) || (rc = alloc(&tmp_src, nf, err)) ||
             (rc = alloc(&tmp_y, nf, err)) ||
             (rc = alloc(&health, 1, err)) || (rc = alloc(&lbin, nf, err)) ||
-            (rc = alloc(&gate, 1, err)) || (rc = alloc(&sort_runs, 1, err)) ||
+            (rc = alloc(&gate, 1, err)) || (rc = alloc(&gate2, 2, err)) ||
+            (rc = alloc(&sort_runs, 1, err)) ||
             (rc = alloc(&list_ent, (size_t)kAleList * (size_t)(nblk(nf, kAleT) * kAleT), err)) ||
             (rc = alloc(&list_cnt, nf, err)) ||
             (rc = alloc(&list_cta_gen, nblk(nf, kAleT), err)) || (rc = alloc(&list_gen, 1, err)) ||
@@ -1499,6 +1542,8 @@ class AleEngine {
         ACK(cudaMemset(counts, 0, 4 * (size_t)(ncells + 1)));
         ACK(cudaMemset(health, 0, 4));
         ACK(cudaMemset(gate, 0, 4));
+        ACK(cudaMemset(gate2, 0, 8));
+        gate_parity = 0;
         ACK(cudaMemset(sort_runs, 0, 8));
         list_nfa = (long long)nblk(nf, kAleT) * kAleT;
         ACK(cudaMemset(list_cta_gen, 0xFF, 4 * (size_t)nblk(nf, kAleT)));
@@ -1696,9 +1741,10 @@ class AleEngine {
         if (scheme == TSPH_ALE_MUSCL)
             k_ale_flux<1><<<nblk(nf), kBlock, 0, st>>>(A, fstart, wstart, W, grid, K);
         else
-            return alaunch(scheme == TSPH_ALE_FIRST_ORDER ? k_ale_flux_tiled<2> : k_ale_flux_tiled<0>,
+            return alaunch(scheme == TSPH_ALE_FIRST_ORDER ? k_ale_flux_tiled<2, false>
+                                                          : k_ale_flux_tiled<0, false>,
                            nblk(nf, kAleT), kAleT, err, A, (const uint32_t *)fstart,
-                           (const uint32_t *)wstart, W, grid, K, lists(gate_clear));
+                           (const uint32_t *)wstart, W, grid, K, lists(gate_clear), AleNext{});
         ACK(cudaGetLastError());
         return 0;
     }
@@ -1750,6 +1796,40 @@ class AleEngine {
             if (stp > 1 && !half && (rc = lf1(dt, err))) return rc;
             half = false;
             if (scheme == TSPH_ALE_MUSCL && (rc = gradient(err))) return rc;
+            if (kept && scheme != TSPH_ALE_MUSCL) {
+                // fluxes and part two (+ the next part one) in one launch,
+                // the new state into the spare set, which becomes the state
+                uint32_t *gs = gate2 + gate_parity, *gn = gate2 + (gate_parity ^ 1);
+                AleNext nx{};
+                nx.D = B;
+                nx.dtf = (float)dt;
+                nx.hf = (float)(dt * 0.5);
+                nx.rho0 = (float)rho0;
+                nx.sig2 = skin * skin;
+                nx.step = stp;
+                nx.boxb = boxb;
+                nx.gate_set = gs;
+                nx.gate_clear_next = gn;
+                nx.health = health;
+                const int bg = std::min(nblk(nf), gated_blocks);
+                if ((rc = alaunch(scheme == TSPH_ALE_FIRST_ORDER ? k_ale_flux_tiled<2, true>
+                                                                 : k_ale_flux_tiled<0, true>,
+                                  nblk(nf, kAleT), kAleT, err, A, (const uint32_t *)fstart,
+                                  (const uint32_t *)wstart, W, grid, K, lists(), nx)))
+                    return rc;
+                std::swap(A, B);
+                if ((rc = alaunch(k_ale_hist_gated, bg, kBlock, err, A, (const uint32_t *)fstart,
+                                  grid, boxb, 1, keyB, slotB, counts, health,
+                                  (const uint32_t *)gs, sort_runs)) ||
+                    (rc = sort(A, B, false, err, gs)) ||
+                    (rc = alaunch(k_ale_copy_gated, bg, kBlock, err, B, A, (const uint32_t *)fstart,
+                                  ncells, (const uint32_t *)gs)))
+                    return rc;
+                gate_parity ^= 1;
+                half = true;
+                half_dt = dt;
+                continue;
+            }
             // on kept cells the tiled flux kernel clears the sort word
             const bool tiled = scheme != TSPH_ALE_MUSCL;
             gate_clear = kept && tiled ? gate : nullptr;
