@@ -876,6 +876,10 @@ static __device__ __forceinline__ uint16_t *append_bounded_ale(const float2 *loc
     return w;
 }
 
+__device__ __forceinline__ void l2_prefetch(const void *p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
 // slot e of a window's staged block (segments walls 0, fluid 0, walls 1,
 // ...): the row j it stages, whether a wall, and x of its cell's origin
 // relative to the centre column's
@@ -944,6 +948,17 @@ k_ale_flux_tiled(AleFluid F, const uint32_t *__restrict__ fstart,
         const int i = cur + tid;
         const bool active = i < we;
         const uint32_t ki = active ? __ldg(F.key + i) : 0u;  // fetched with the offsets
+        if (NEXT && active) {
+            // the target's state for the part two in the epilogue, on its way
+            // to L2 while the pair sums run (no registers held)
+            l2_prefetch(F.r + i);
+            l2_prefetch(F.om_o + i);
+            l2_prefetch(F.omr_o + i);
+            l2_prefetch(F.omv_o + i);
+            l2_prefetch(F.v + i);
+            l2_prefetch(F.s + i);
+            l2_prefetch(L.lbin + i);
+        }
         __syncthreads();
         for (int e = tid; e < 3 * (nr + 1); e += kAleT) {
             const int dxi = e / (nr + 1), q = e - dxi * (nr + 1);
