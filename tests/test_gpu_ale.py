@@ -233,6 +233,35 @@ def test_ale_kept_cells_vs_sort_every_step(gpu_tsph, scheme):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("scheme", [0, 2])
+def test_ale_removal_on_kept_cells(gpu_tsph, scheme):
+    """Removal inside the fused step on kept cells: six fluid particles put
+    just outside the domain box (inside the cell grid) leave the system at
+    the next step, as with a sort every step (src/SPH_btdebug.h:4-31); the
+    rest agrees within the FP32 bars."""
+    case = cases.dam_break_ale(dp=0.004)
+    a = case.particles.arrays()
+    fl = np.flatnonzero(a["type"] == 0)
+    r = a["r"].copy()
+    moved = fl[:: len(fl) // 6][:6]
+    r[moved, 0] = case.domain[1] + 0.1 * case.h
+    runs = []
+    for keep in (True, False):
+        s = gpu_tsph.AleSystem.from_case(case, scheme=scheme)
+        s.set_keep_cells(keep)
+        s.upload(r=r)
+        s.particle_to_cell()
+        s.step(case.dt, 0, 3)
+        runs.append((s.download(), s.health()))
+    (kept, hk), (ref, he) = runs
+    assert hk & gpu_tsph.HEALTH_REMOVED and he & gpu_tsph.HEALTH_REMOVED
+    assert len(kept["index"]) == case.np - 6
+    assert not np.isin(moved, kept["index"]).any()
+    rates = {f: ref[f] for f in RATES}
+    _check_state(kept, ref, case.dt, 3, rates, case.cs, tag=f"removal, scheme {scheme}")
+
+
+@pytest.mark.gpu
 def test_ale_part_one_ahead_is_exact(gpu_tsph):
     """On kept cells a step ends with the next step's part one applied; the
     state seen by a download, a second call of the step, or a per-function
