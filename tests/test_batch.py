@@ -137,6 +137,47 @@ def test_batch_in_one_system_matches_the_oracle_per_case(gpu_tsph, oracle_mod):
 
 
 @pytest.mark.gpu
+def test_batch_pipelined_transfers_equal_synchronous(gpu_tsph):
+    """The case-table system through the pipelined transfers (the staged
+    upload applied by particle_to_cell, the step, the download read back a
+    step later) gives bit for bit the synchronous loop's results."""
+    torch = pytest.importorskip("torch")
+    specs = [B.CaseSpec(B.DAM_BREAK, 0.004, 1.0, 0.4, 0.3),
+             B.CaseSpec(B.STILL_WATER, 0.002, 1.0, 0.4, 0.2)]
+    a, b = B.Batch(specs), B.Batch(specs)
+    a.step(3)
+    b.step(3)
+    sa, sb = a.system, b.system
+    n = sa.np
+    mask = gpu_tsph.F_R | gpu_tsph.F_V | gpu_tsph.F_RHO
+    hin = [torch.empty(shape, dtype=torch.float64, pin_memory=True)
+           for shape in ((n, 2), (n, 2), (n,))]
+    ptr = dict(r=hin[0].data_ptr(), v=hin[1].data_ptr(), rho=hin[2].data_ptr())
+    sa.download_ptrs(mask, **ptr)
+    sync = []
+    for _ in range(3):
+        sa.upload_ptrs(mask, **ptr)
+        sa.particle_to_cell()
+        a.step(1)
+        sync.append(sa.download(mask))
+    outs = [[torch.empty_like(t, pin_memory=True) for t in hin] for _ in range(3)]
+    sb.upload_async(mask, **ptr)
+    for k in range(3):
+        if k:
+            sb.upload_async(mask, **ptr)
+        sb.particle_to_cell()
+        b.step(1)
+        o = outs[k]
+        sb.download_async(mask, r=o[0].data_ptr(), v=o[1].data_ptr(), rho=o[2].data_ptr())
+    sb.download_wait()
+    for k in range(3):
+        o = [t.numpy() for t in outs[k]]
+        assert np.array_equal(o[0], sync[k]["r"]), k
+        assert np.array_equal(o[1], sync[k]["v"]), k
+        assert np.array_equal(o[2], sync[k]["rho"]), k
+
+
+@pytest.mark.gpu
 def test_case_table_rules(gpu_tsph, tmp_path):
     """tsph_set_cases: FP32 only, non-empty ranges; on a system with a case
     table the per-function force, corrector and removal calls and checkpoints
